@@ -1,0 +1,427 @@
+#!/usr/bin/env python
+"""COSX G-kernel benchmark (the workload of the reference's G microbench):
+
+  27 seeded waters (O-H 0.9572 A, HOH 104.52 deg, oxygens uniform in a 10 A
+  cube with O-O >= 2.7 A, random orientations), def2-SVP-structured basis
+  (648 AOs), atom-centred grid (~3.8e5 points), D = 2 C C^T with C (648, 135)
+  seeded N(0, 1) and orthonormalised, proj = identity, F = fl32(X D),
+  screening k_tile_tol = 1e-11.
+
+One step = the two K builds of one SCF cycle (full 1/r and erf(w r)/r,
+w = 0.3), each: FP64 AO values -> F GEMM -> sub-block stats -> fused screen
++ G kernels -> K GEMM, all on the device.  The metric is COSX G TFLOP/s:
+the algorithmic flop model of the kept (sub-block, shell pair) tasks
+(pyscf_wb97mv_fast_gb300/flops_model.py) divided by the step time.
+
+  value  : device-resident inputs, wb_cosx_get_k through the engine
+  e2e    : host (pinned) coordinates, weights and density matrix copied in
+           and both K matrices copied out every step, through
+           GpuKBuilder/get_k_only_gpu-equivalent calls
+  roofline: the fused G kernels alone (wb_cosx_g), CUDA events on the
+           launching stream, against the FP32 FMA peak measured in the same
+           run (wb_fp32_fma_probe)
+  cpu_baseline: the FP64 OpenMP oracle on a bounded sample of the points
+
+--impl reference times the reference's CPU path for this workload on the
+host cores.  PySCF (the reference's CPU implementation) is not installed,
+so it is the C/OpenMP restatement of it (the oracle port), on a bounded
+sample per step, same metric and unit.
+
+Multi-GPU (torchrun, N > 1): replicas -- every rank runs the same workload
+on its own GPU; value = sum of the per-rank work / max time over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NWATER, BOX, SEED = 27, 10.0, 27
+GRID_LEVEL = 2
+NOCC = 135
+OMEGAS = (0.0, 0.3)
+TILE_TOL = 1e-11
+METRIC = 'COSX G TFLOP/s (algorithmic flop model of kept tasks)'
+UNIT = 'TFLOP/s'
+
+
+def workload(small=False):
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    from pyscf_wb97mv_fast_gb300.systems import water_cluster
+    if small:
+        mol = Molecule.build(water_cluster(8, box=7.0, seed=8), 'synthetic-svp')
+        g = build_grids(mol, level=1)
+        nocc = 40
+    else:
+        mol = Molecule.build(water_cluster(NWATER, box=BOX, seed=SEED),
+                             'synthetic-svp')
+        g = build_grids(mol, level=GRID_LEVEL)
+        nocc = NOCC
+    rng = np.random.default_rng(SEED)
+    c, _ = np.linalg.qr(rng.normal(size=(mol.nao, nocc)))
+    dm = 2.0 * c @ c.T
+    return mol, g, dm
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,'
+              'clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.FIELDS,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown',
+                 'sw_power_cap']
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(',')]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith('active'):
+                    reasons.add(nm)
+        return {'sm_mhz': statistics.median(sm) if sm else None,
+                'sm_max_mhz': smax, 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(path):
+        with open(path) as fh:
+            return json.load(fh)
+    return None
+
+
+def fp32_peak(torch):
+    """FP32 FMA throughput of this GPU (TFLOP/s), best of 5 probe launches."""
+    from pyscf_wb97mv_fast_gb300 import _native
+    lib = _native.lib()
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    out = torch.empty(nsm * 2048, dtype=torch.float32, device='cuda')
+    flops = _native.ctypes.c_double()
+    stream = _native.ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    best = 0.0
+    for it in range(7):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _native.check(lib.wb_fp32_fma_probe(20000, _native.ptr(out), out.numel(),
+                                            stream, _native.ctypes.byref(flops)))
+        e1.record()
+        e1.synchronize()
+        if it >= 2:
+            best = max(best, flops.value / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def traffic_from_profile():
+    path = os.path.join(ROOT, 'profiles', 'cosx_g_water27_traffic.json')
+    if os.path.exists(path):
+        with open(path) as fh:
+            return json.load(fh)
+    return None
+
+
+def cpu_baseline(mol, g, dm, engine, budget_s=15.0):
+    """FP64 oracle G on a bounded sample of the grid, both omegas."""
+    import oracle
+    rows = engine.pair_table()
+    flops_per_pt = float(rows[:, 7].sum())
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(1)
+    X_idx = rng.choice(g.size, 64, replace=False)
+    t0 = time.perf_counter()
+    run_sample(oracle, mol, g, dm, X_idx)
+    t_probe = time.perf_counter() - t0
+    n = int(max(64, min(g.size, 64 * budget_s / max(t_probe, 1e-3))))
+    idx = np.sort(rng.choice(g.size, n, replace=False))
+    t0 = time.perf_counter()
+    run_sample(oracle, mol, g, dm, idx)
+    dt = time.perf_counter() - t0
+    work = flops_per_pt * n * len(OMEGAS)
+    return {'value': work / dt / 1e12, 'unit': UNIT, 'cores': cores,
+            'kind': 'port',
+            'sample': '%d of %d grid points, omega in %s, FP64 oracle, all '
+                      'shell pairs (no screening), OpenMP %d threads'
+                      % (n, g.size, list(OMEGAS), cores),
+            'seconds': dt}
+
+
+def run_sample(oracle, mol, g, dm, idx):
+    coords = g.coords[idx]
+    X = oracle.ao_eval(mol, coords)
+    F = X @ dm
+    for w in OMEGAS:
+        oracle.cosx_g(mol, coords, F, w)
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference's path."""
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    import oracle
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine  # noqa: F401
+    mol, g, dm = workload(args.small)
+    # model flops per point of all pairs (the CPU path does no screening)
+    from pyscf_wb97mv_fast_gb300.flops_model import pair_flops_table
+    flops_per_pt = float(pair_flops_table(mol).sum())
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(2)
+    npts = args.ref_points
+    times = []
+    for step in range(args.warmup + args.steps):
+        idx = np.sort(rng.choice(g.size, npts, replace=False))
+        t0 = time.perf_counter()
+        run_sample(oracle, mol, g, dm, idx)
+        if step >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    tstep = sum(times) / len(times)
+    value = flops_per_pt * npts * len(OMEGAS) / tstep / 1e12
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT,
+        'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': tstep * 1e3, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+        'data': 'synthetic',
+        'config': config_dict(mol, g, args),
+        'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': cores,
+                         'kind': 'port',
+                         'sample': '%d of %d grid points per step, both omegas, '
+                                   'FP64 C/OpenMP restatement of the reference '
+                                   'path (PySCF absent)' % (npts, g.size)},
+        'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line))
+
+
+def config_dict(mol, g, args):
+    return {'workload': 'cosx_g_water%d_svp' % (8 if args.small else NWATER),
+            'molecule': '%d seeded waters in a %.0f A cube (seed %d)'
+                        % (8 if args.small else NWATER, 7.0 if args.small else BOX,
+                           8 if args.small else SEED),
+            'basis': 'synthetic def2-SVP structure', 'nao': mol.nao,
+            'grid_points': int(g.size), 'omegas': list(OMEGAS),
+            'k_tile_tol': TILE_TOL, 'proj': 'identity',
+            'l2': 'inputs larger than L2 (X alone is %.1f GB)'
+                  % (8.0 * mol.nao * g.size / 1e9),
+            'gemm': args.gemm, 'parallelism': 'replicas'}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--gemm', default='native', choices=['native', 'emulated'])
+    ap.add_argument('--small', action='store_true',
+                    help='8 waters / grid level 1 (profiling captures)')
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--ref-points', type=int, default=400)
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group('nccl')
+
+    from pyscf_wb97mv_fast_gb300 import build as _build
+    _build.build()
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine, round32
+
+    mol, g, dm = workload(args.small)
+    eng = CosxEngine(mol, device=local)
+    dev = eng.device
+    coords_d = eng.relative(g.coords)
+    w_d = torch.as_tensor(g.weights, device=dev)
+    qd_d = torch.as_tensor(dm, device=dev)
+    emulated = args.gemm == 'emulated'
+    K = [torch.empty((mol.nao, mol.nao), dtype=torch.float64, device=dev)
+         for _ in OMEGAS]
+
+    def step():
+        for i, w in enumerate(OMEGAS):
+            eng.get_k(coords_d, w_d, qd_d, w, tile_tol=TILE_TOL,
+                      emulated_gemm=emulated, out=K[i], stats=False)
+
+    # one counted call per omega: kept tasks, model flops, launches
+    flops_step, launches_step, kept, total = 0.0, 0, 0, 0
+    for i, w in enumerate(OMEGAS):
+        eng.get_k(coords_d, w_d, qd_d, w, tile_tol=TILE_TOL,
+                  emulated_gemm=emulated, out=K[i], stats=True)
+        st = eng.last_stats
+        flops_step += st['model_flops']
+        launches_step += st['kernel_launches']
+        kept += st['pairs_kept']
+        total += st['pairs_total']
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        return e0.elapsed_time(e1) / 1e3 / steps
+
+    with ClockSampler(local) as clocks:
+        t_step = timed(step, args.steps, args.warmup)
+    if world > 1:
+        tt = torch.tensor([t_step], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = world * flops_step / t_step / 1e12
+
+    # -- e2e: pinned host inputs in, K out, every step ----------------------------
+    coords_rel_h = (g.coords - eng.origin).astype(np.float64)
+    c_h = torch.from_numpy(np.ascontiguousarray(coords_rel_h)).pin_memory()
+    w_h = torch.from_numpy(np.ascontiguousarray(g.weights)).pin_memory()
+    d_h = torch.from_numpy(np.ascontiguousarray(dm)).pin_memory()
+    k_h = [torch.empty((mol.nao, mol.nao), dtype=torch.float64).pin_memory()
+           for _ in OMEGAS]
+    c_d2 = torch.empty_like(coords_d)
+    w_d2 = torch.empty_like(w_d)
+    q_d2 = torch.empty_like(qd_d)
+
+    def e2e_step():
+        c_d2.copy_(c_h, non_blocking=True)
+        w_d2.copy_(w_h, non_blocking=True)
+        q_d2.copy_(d_h, non_blocking=True)
+        for i, w in enumerate(OMEGAS):
+            eng.get_k(c_d2, w_d2, q_d2, w, tile_tol=TILE_TOL,
+                      emulated_gemm=emulated, out=K[i], stats=False)
+            Ks = (K[i] + K[i].T) * 0.5
+            k_h[i].copy_(Ks, non_blocking=True)
+
+    t_e2e = timed(e2e_step, args.steps, 1)
+    if world > 1:
+        tt = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    h2d = c_h.numel() * 8 + w_h.numel() * 8 + d_h.numel() * 8
+    d2h = sum(k.numel() * 8 for k in k_h)
+
+    # -- roofline of the fused G kernels (wb_cosx_g on the same F) -----------------
+    n = g.size
+    ld = round32(n)
+    X = eng.ao_eval(coords_d)
+    F = (qd_d.T @ X).to(torch.float32)          # F^T = (X QD)^T, AO-major
+    F = F.contiguous()
+    Gt = torch.empty((mol.nao, ld), dtype=torch.float32, device=dev)
+    g_flops = 0.0
+    for w in OMEGAS:
+        eng.g(coords_d, w_d, F, w, TILE_TOL, out=Gt, stats=True)
+        g_flops += eng.last_stats['model_flops']
+
+    def g_step():
+        for w in OMEGAS:
+            eng.g(coords_d, w_d, F, w, TILE_TOL, out=Gt, stats=False)
+    t_g = timed(g_step, max(2, args.steps), 1)
+    del X
+    peak = fp32_peak(torch)
+    achieved = g_flops / t_g / 1e12
+    prof = traffic_from_profile()
+    roofline = {'bound': 'fp32', 'achieved': achieved, 'peak': peak,
+                'unit': 'TFLOP/s', 'frac': achieved / peak if peak else None,
+                'traffic': prof.get('bytes_per_launch') if prof else None,
+                'peak_source': 'measured in this run: wb_fp32_fma_probe '
+                               '(FFMA-only kernel, all SMs)',
+                'kernel': 'fused screen + G kernels (10 class launches) of '
+                          'both omegas',
+                'ms': t_g * 1e3}
+    mp = measured_peaks()
+    if mp:
+        roofline['measured_peaks_file'] = {'hbm_gbs': mp.get('hbm_gbs'),
+                                           'bf16_tflops': mp.get('bf16_tflops')}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(mol, g, dm, eng)
+
+    if rank == 0:
+        line = {
+            'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': t_step * 1e3, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic (seeded generators; no PySCF grids or basis)',
+            'config': config_dict(mol, g, args),
+            'e2e': {'value': world * flops_step / t_e2e / 1e12, 'unit': UNIT,
+                    'ms_per_step': t_e2e * 1e3, 'h2d_bytes_per_step': h2d,
+                    'd2h_bytes_per_step': d2h},
+            'roofline': roofline,
+            'cpu_baseline': cpu,
+            'clocks': clocks.summary(),
+            'gpu_launches': launches_step * args.steps,
+            'tasks_kept': kept, 'tasks_total': total,
+            'model_flops_per_step': flops_step,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

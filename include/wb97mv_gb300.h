@@ -1,0 +1,190 @@
+/*
+ * wb97mv_gb300.h -- C ABI of the GB300 (sm_103a) COSX exchange hot path.
+ *
+ * Plain C: no CUDA, PyTorch or C++ types cross this boundary.  Device
+ * buffers are raw pointers owned by the caller; `stream` is a cudaStream_t
+ * passed as void*.  Every entry point returns an int status (0 = WB_OK,
+ * > 0 = one of the WB_ERR_* codes below); wb_last_error() holds a one-line
+ * description of the last failure on the calling thread.  No C++
+ * exception crosses the boundary and nothing falls back to the CPU.
+ *
+ * Layouts.  Per-grid-point matrices are AO-major: element (mu, g) of X, F
+ * and G sits at mu * ldp + g, ldp = npts rounded up to a multiple of 32 (one
+ * warp-sized sub-block).  Coordinates are FP64 (npts, 3) row-major, in the
+ * frame of the handle's `origin`.  Square AO matrices (QD, K) are
+ * (nao, nao) row-major.
+ *
+ * The reference computes the same quantities in Python/CuPy; each function
+ * names the reference interface it replaces (paths inside the reference
+ * project Cedrus810/pyscf-wb97mv-fast).
+ */
+#ifndef WB97MV_GB300_H
+#define WB97MV_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* -- status codes --------------------------------------------------------- */
+#define WB_OK 0
+#define WB_ERR_INVALID_ARGUMENT 1
+#define WB_ERR_UNSUPPORTED 2      /* reference: gpu/xc.py:30 Unsupported */
+#define WB_ERR_CUDA 3
+#define WB_ERR_CUBLAS 4
+#define WB_ERR_OUT_OF_MEMORY 5
+#define WB_ERR_WORKSPACE 6        /* workspace pointer/size too small */
+#define WB_ERR_NO_DEVICE 7
+
+/* Basis description (libcint conventions: per-primitive radial norm folded
+ * into the coefficients, contracted functions normalised).  Shell s has
+ * nprim exponents at exps[shell_exp_off[s]] and an (nprim, nctr) row-major
+ * coefficient block at coeffs[shell_coef_off[s]].  Replaces the Mole
+ * accessors read by gpu/shellpairs.py:187-221 and gpu/ao_eval.py:66-111. */
+typedef struct wb_basis {
+    int natm;
+    int nbas;
+    const double* atom_coords;   /* (natm, 3) bohr */
+    const int* shell_atom;       /* (nbas,) */
+    const int* shell_l;          /* (nbas,) 0..3 */
+    const int* shell_nprim;      /* (nbas,) */
+    const int* shell_nctr;       /* (nbas,) */
+    const int* shell_exp_off;    /* (nbas,) */
+    const int* shell_coef_off;   /* (nbas,) */
+    const double* exps;
+    const double* coeffs;
+} wb_basis;
+
+/* Counters of one G / K build.  tasks = (32-point sub-block, shell pair);
+ * integrals = sum over kept tasks of points * nfi * nfj (the definition of
+ * benchmarks/experimental/cosx/cint_shim.c:75-77); model_flops = the
+ * algorithmic flop model of kept tasks (pyscf_wb97mv_fast_gb300/
+ * flops_model.py).  Mirrors GpuKBuilder.last_stats (gpu/sgx_k.py:743-748). */
+typedef struct wb_cosx_stats {
+    int64_t tasks_total;
+    int64_t tasks_kept;
+    double integrals;
+    double model_flops;
+    int64_t tasks_kept_class[10];
+    double model_flops_class[10];
+    int32_t kernel_launches;      /* device kernels launched by the call */
+    int32_t reserved;
+} wb_cosx_stats;
+
+typedef struct wb_cosx_info {
+    int nao;
+    int nbas;                     /* after splitting general contractions */
+    int npairs;                   /* kept shell pairs */
+    int nprim_pairs;
+    int class_pairs[10];          /* pairs per (la >= lb) class */
+    int class_prim_pairs[10];
+} wb_cosx_info;
+
+typedef struct wb_cosx wb_cosx;   /* opaque per-(molecule, device) handle */
+
+/* Flags of wb_cosx_get_k */
+#define WB_K_GEMM_NATIVE_FP64 0   /* cuBLAS DGEMM */
+#define WB_K_GEMM_EMULATED_FP64 1 /* cuBLAS FP64 fixed-point emulation */
+
+/* Build the packed shell-pair tables of a molecule on the host (FP64) and
+ * upload them to the current device.  origin (3,) is subtracted from every
+ * centre (the kernels work in a molecule-centred frame).  pair_cutoff is the
+ * primitive magnitude cut (1e-14 in the reference).  Replaces
+ * ShellPairs.__init__ + to_device (gpu/shellpairs.py:184-437) and
+ * GpuKBuilder._build (gpu/sgx_k.py:593-612).  Out-of-scope bases (l > 3,
+ * nprim > 16, nctr * (2l+1) > 16, spinor/cartesian) return
+ * WB_ERR_UNSUPPORTED. */
+int wb_cosx_create(const wb_basis* basis, const double origin[3],
+                   double pair_cutoff, wb_cosx** out);
+int wb_cosx_destroy(wb_cosx* h);
+int wb_cosx_get_info(const wb_cosx* h, wb_cosx_info* info);
+
+/* Host copies of the pair tables, for tests: per pair (ia0, ib0, pp0,
+ * npp | diag << 16, class, ish, jsh, model flops per point) as int64 rows of
+ * 8; returns the number of rows written (<= cap). */
+int64_t wb_cosx_export_pairs(const wb_cosx* h, int64_t* rows, int64_t cap);
+
+/* Bytes of device workspace wb_cosx_get_k / wb_cosx_g need for a grid of
+ * npts points processed in tiles of tile_pts points (0 = one tile). */
+size_t wb_cosx_workspace_bytes(const wb_cosx* h, int64_t npts,
+                               int64_t tile_pts);
+
+/* One full COSX K build on the device:
+ *   per tile: X = AO values (FP64)                  gpu/ao_eval.py:186-329
+ *             F = fl32(X QD)  (FP64 GEMM)           gpu/sgx_k.py:719-722
+ *             sub-block stats + fused screen + G    gpu/sgx_k.py:754-781,
+ *               G_gv = sum_mu A^g_mu,v F_g,mu       :866-924, :165-400
+ *             K += X^T (w o G)  (FP64 GEMM)         gpu/sgx_k.py:734
+ * qd = proj @ dm (nao, nao) row-major, FP64.  k_out (nao, nao) row-major is
+ * overwritten with the unsymmetrised K (the caller applies proj^T and
+ * (K + K^T)/2, gpu/sgx_k.py:736-742).  tile_tol = 0 keeps every task.
+ * Replaces GpuKBuilder.get_k (gpu/sgx_k.py:663-751). */
+int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
+                  int64_t npts, const double* qd, double omega,
+                  double tile_tol, int64_t tile_pts, int flags,
+                  double* k_out, void* workspace, size_t workspace_bytes,
+                  void* stream, wb_cosx_stats* stats);
+
+/* The fused G kernels alone on one tile: f (nao, ldp) FP32 AO-major in,
+ * g_out (nao, ldp) FP32 out (overwritten).  weights (npts,) FP64 feed the
+ * screening estimate.  Replaces GpuKBuilder._tasks + _launch
+ * (gpu/sgx_k.py:813-843, :754-781). */
+int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
+              int64_t npts, const float* f, double omega, double tile_tol,
+              float* g_out, void* workspace, size_t workspace_bytes,
+              void* stream, wb_cosx_stats* stats);
+
+/* AO values X (nao, ldp) FP64 AO-major at npts points (FP64 arithmetic).
+ * Replaces AoEvaluator.eval(deriv=0) with dtype FP64 (gpu/ao_eval.py:186-329). */
+int wb_ao_eval(const wb_cosx* h, const double* coords, int64_t npts,
+               double* x_out, void* stream);
+
+/* Dense contracted spherical A[g, mu, nu] (npts, nao, nao) FP32 for small
+ * validation systems.  Replaces int3c1e_fp32 (gpu/int3c1e.py:284-314). */
+int wb_int3c1e_dense(const wb_cosx* h, const double* coords, int64_t npts,
+                     double omega, float* out, void* stream);
+
+/* FP32 Boys F_0..F_nmax (nmax <= 6) of n arguments: out (nmax+1, n).
+ * Replaces boys_eval (gpu/boys.py:194-204). */
+int wb_boys_fp32(const float* t, int64_t n, int nmax, float* out,
+                 void* stream);
+
+/* Host FP64 Boys F_0..F_nmax at one argument (used to build the table). */
+int wb_boys_f64_host(int nmax, double t, double* out);
+
+/* VV10 double sum over n points (FP32 pair terms, FP64 per-point sums):
+ *   F_i = -1.5 sum_j q_j / (g gp (g + gp)),  U_i = sum_j T (1/g + 1/(g+gp)),
+ *   W_i = sum_j T (1/g + 1/(g+gp)) R^2,  g = R^2 w0_i + kappa_i, gp likewise.
+ * xyz (n, 3), q, w0, kappa (n,) FP32; F, U, W (n,) FP64.  Tile pairs whose
+ * bound is below tile_tol are skipped (0 keeps every pair).
+ * Replaces Vv10Kernel.kernel_sum (gpu/vv10.py:167-240). */
+int wb_vv10_kernel_sum(const float* xyz, const float* q, const float* w0,
+                       const float* kappa, int64_t n, double tile_tol,
+                       double* f_out, double* u_out, double* w_out,
+                       void* stream, int64_t* pairs_kept);
+
+/* Becke fuzzy-cell weights (host, FP64, OpenMP): for each point its
+ * owner atom's cell weight.  Grid construction helper for the synthetic
+ * workloads (PySCF builds the grids in the reference). */
+int wb_becke_partition(const double* points, int64_t n, const int* owner,
+                       const double* atom_coords, int natm, double* out);
+
+/* FP32 FMA throughput probe: launches 8 CTAs per SM x 256 threads, each
+ * thread 8 independent FMA chains for iters x 16 steps; *flops receives the
+ * flop count of the launch (FMA = 2).  out needs nsm * 2048 floats.  The
+ * caller times it (events on `stream`): the measured FP32 peak used as the
+ * roofline denominator of the FP32-pipe kernels.  No reference counterpart
+ * (the reference reports no roofline). */
+int wb_fp32_fma_probe(int64_t iters, float* out, int64_t out_len,
+                      void* stream, double* flops);
+
+const char* wb_status_string(int status);
+const char* wb_last_error(void);
+int wb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WB97MV_GB300_H */

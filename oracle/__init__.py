@@ -1,0 +1,144 @@
+"""FP64 CPU oracle of the COSX path -- TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
+arm use this package, and only as the checker or the timed CPU baseline.
+The product library never imports, links or calls it.
+
+``build()`` compiles cosx_oracle.c with gcc (-O2 -fopenmp) into
+oracle/liboracle.so.  The Python functions below wrap it and add the NumPy
+pieces of the reference's K assembly (gpu/sgx_k.py:717-742):
+
+    F = X (proj @ dm),  G = sum_mu A F  (oracle_cosx_g),
+    K = X^T (w o G),  K <- proj^T K if sym,  K <- (K + K^T) / 2.
+
+Parity is pinned by tests/test_oracle_golden.py against vectors produced by
+the reference's own Python (tests/golden/make_golden.py) and against
+closed-form values.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, 'cosx_oracle.c')
+LIB = os.path.join(HERE, 'liboracle.so')
+
+_lib = None
+
+
+def build(force=False):
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= os.path.getmtime(SRC)):
+        return LIB
+    cmd = ['gcc', '-O2', '-fopenmp', '-shared', '-fPIC', '-std=c11',
+           '-D_DEFAULT_SOURCE', SRC, '-o', LIB + '.tmp', '-lm']
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError('oracle build failed:\n' + res.stderr)
+    os.replace(LIB + '.tmp', LIB)
+    return LIB
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(LIB)
+        P, I, D, I64 = (ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                        ctypes.c_int64)
+        basis = [I, I] + [P] * 9 + [P] * 4
+        _lib.oracle_boys.argtypes = [I, D, P]
+        _lib.oracle_int3c1e.argtypes = basis + [P, I64, D, P]
+        _lib.oracle_cosx_g.argtypes = basis + [P, I64, D, P, P]
+        _lib.oracle_ao_eval.argtypes = basis + [P, I64, P]
+        _lib.oracle_vv10_sum.argtypes = [P, P, P, P, I64, P, P, P]
+        for f in ('oracle_boys', 'oracle_int3c1e', 'oracle_cosx_g',
+                  'oracle_ao_eval', 'oracle_vv10_sum'):
+            getattr(_lib, f).restype = I
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class _Basis:
+    """Keeps the packed arrays alive for one call."""
+
+    def __init__(self, mol):
+        from pyscf_wb97mv_fast_gb300.basis import cart2sph
+        pk = mol.packed()
+        self.arrays = [pk['atom_coords'], pk['shell_atom'], pk['shell_l'],
+                       pk['shell_nprim'], pk['shell_nctr'], pk['shell_exp_off'],
+                       pk['shell_coef_off'], pk['exps'], pk['coeffs']]
+        self.c2s = [np.ascontiguousarray(cart2sph(l)) for l in range(4)]
+        self.args = ([pk['natm'], pk['nbas']] + [_p(a) for a in self.arrays]
+                     + [_p(c) for c in self.c2s])
+        self.nao = pk['nao']
+
+
+def boys(nmax, t):
+    out = np.zeros(nmax + 1)
+    _load().oracle_boys(int(nmax), float(t), _p(out))
+    return out
+
+
+def int3c1e(mol, coords, omega=0.0):
+    """(ng, nao, nao) FP64 dense integrals at absolute coordinates."""
+    b = _Basis(mol)
+    c = np.ascontiguousarray(coords, dtype=np.float64)
+    out = np.zeros((len(c), b.nao, b.nao))
+    _load().oracle_int3c1e(*b.args, _p(c), len(c), float(omega), _p(out))
+    return out
+
+
+def cosx_g(mol, coords, F, omega=0.0):
+    """G (ng, nao) FP64 for F (ng, nao)."""
+    b = _Basis(mol)
+    c = np.ascontiguousarray(coords, dtype=np.float64)
+    F = np.ascontiguousarray(F, dtype=np.float64)
+    G = np.zeros_like(F)
+    _load().oracle_cosx_g(*b.args, _p(c), len(c), float(omega), _p(F), _p(G))
+    return G
+
+
+def ao_eval(mol, coords):
+    """X (ng, nao) FP64."""
+    b = _Basis(mol)
+    c = np.ascontiguousarray(coords, dtype=np.float64)
+    X = np.zeros((len(c), b.nao))
+    _load().oracle_ao_eval(*b.args, _p(c), len(c), _p(X))
+    return X
+
+
+def vv10_sum(coords, q, w0, kappa):
+    """FP64 brute-force F (x -1.5), U, W."""
+    c = np.ascontiguousarray(coords, dtype=np.float64)
+    q, w0, kappa = (np.ascontiguousarray(a, dtype=np.float64)
+                    for a in (q, w0, kappa))
+    n = len(q)
+    F, U, W = np.zeros(n), np.zeros(n), np.zeros(n)
+    _load().oracle_vv10_sum(_p(c), _p(q), _p(w0), _p(kappa), n, _p(F), _p(U),
+                            _p(W))
+    return F, U, W
+
+
+def cosx_k(mol, coords, weights, dm, omega=0.0, proj=None, sym=False,
+           hermi=1, return_parts=False):
+    """FP64 COSX K of the reference's get_k (gpu/sgx_k.py:709-742) on a grid
+    (absolute coordinates): no screening, no FP32 rounding anywhere."""
+    X = ao_eval(mol, coords)
+    nao = X.shape[1]
+    proj = np.eye(nao) if proj is None else np.asarray(proj)
+    F = X @ (proj @ dm)
+    G = cosx_g(mol, coords, F, omega)
+    K = X.T @ (np.asarray(weights)[:, None] * G)
+    if sym:
+        K = proj.T @ K
+    if hermi == 1:
+        K = (K + K.T) * 0.5
+    if return_parts:
+        return K, X, F, G
+    return K

@@ -1,0 +1,235 @@
+"""CosxEngine: one native COSX handle (molecule x device) driven from PyTorch.
+
+Device buffers are torch tensors; every call passes raw pointers and the
+current torch stream through the C ABI (``_native``).  The engine owns the
+packed shell-pair tables (uploaded once per molecule) and a cached device
+workspace; it never copies data to the host except the final K and, when
+asked for, the counters of the last call.
+"""
+import numpy as np
+
+from pyscf_wb97mv_fast_gb300 import _native
+from pyscf_wb97mv_fast_gb300.basis import Molecule
+
+KSUB = 32          # grid points per sub-block = one warp
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def round32(n):
+    return (int(n) + KSUB - 1) // KSUB * KSUB
+
+
+def as_molecule(mol):
+    """A Molecule from a Molecule or a PySCF Mole."""
+    if isinstance(mol, Molecule):
+        return mol
+    if hasattr(mol, '_bas') and hasattr(mol, '_libcint_ctr_coeff'):
+        return Molecule.from_pyscf(mol)
+    raise TypeError('expected a Molecule or a PySCF Mole, got %r' % type(mol))
+
+
+class CosxEngine:
+    """Native COSX kernels for one molecule on one CUDA device.
+
+    origin: the molecule-centred frame of the kernels (default: mean of the
+    atom coordinates, as the reference's GpuKBuilder, gpu/sgx_k.py:564).
+    """
+
+    def __init__(self, mol, origin=None, pair_cutoff=1e-14, device=None):
+        torch = _torch()
+        self.mol = as_molecule(mol)
+        coords = self.mol.atom_coords()
+        self.origin = (coords.mean(axis=0) if origin is None
+                       else np.asarray(origin, dtype=np.float64))
+        if device is None:
+            device = torch.cuda.current_device()
+        if not isinstance(device, int):
+            device = torch.device(device).index or 0
+        self.device = torch.device('cuda', device)
+        self._packed = self.mol.packed()
+        p = self._packed
+        self._basis = _native.WbBasis(
+            p['natm'], p['nbas'], _native.ptr(p['atom_coords']),
+            _native.ptr(p['shell_atom']), _native.ptr(p['shell_l']),
+            _native.ptr(p['shell_nprim']), _native.ptr(p['shell_nctr']),
+            _native.ptr(p['shell_exp_off']), _native.ptr(p['shell_coef_off']),
+            _native.ptr(p['exps']), _native.ptr(p['coeffs']))
+        self._origin_c = np.ascontiguousarray(self.origin, dtype=np.float64)
+        lib = _native.lib()
+        handle = _native.ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _native.check(lib.wb_cosx_create(_native.ctypes.byref(self._basis),
+                                             _native.ptr(self._origin_c),
+                                             float(pair_cutoff),
+                                             _native.ctypes.byref(handle)),
+                          'wb_cosx_create')
+        self._h = handle
+        info = _native.WbCosxInfo()
+        _native.check(lib.wb_cosx_get_info(self._h, _native.ctypes.byref(info)))
+        self.nao = int(info.nao)
+        self.npairs = int(info.npairs)
+        self.nprim_pairs = int(info.nprim_pairs)
+        self.class_pairs = [int(x) for x in info.class_pairs]
+        self.class_prim_pairs = [int(x) for x in info.class_prim_pairs]
+        self.nvshell = int(info.nbas)
+        self._ws = None
+        self.last_stats = {}
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self):
+        if getattr(self, '_h', None):
+            _native.lib().wb_cosx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:                       # noqa: BLE001
+            pass
+
+    # -- helpers ------------------------------------------------------------
+    def pair_table(self):
+        """(npairs, 8) int64: ia0, ib0, pp0, npp|diag<<16, class, ish, jsh,
+        model flops per point."""
+        lib = _native.lib()
+        rows = np.zeros((max(self.npairs, 1), 8), dtype=np.int64)
+        n = lib.wb_cosx_export_pairs(self._h, _native.ptr(rows), self.npairs)
+        return rows[:n]
+
+    def workspace_bytes(self, npts, tile_pts=0):
+        return int(_native.lib().wb_cosx_workspace_bytes(self._h, int(npts),
+                                                         int(tile_pts)))
+
+    def workspace(self, nbytes):
+        torch = _torch()
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = None
+            self._ws = torch.empty(int(nbytes), dtype=torch.uint8,
+                                   device=self.device)
+        return self._ws
+
+    def relative(self, coords):
+        """Absolute FP64 coordinates (host or device) -> kernel frame, on
+        this engine's device."""
+        torch = _torch()
+        c = torch.as_tensor(coords, dtype=torch.float64, device=self.device)
+        o = torch.as_tensor(self.origin, dtype=torch.float64, device=self.device)
+        return (c - o).contiguous()
+
+    @staticmethod
+    def _stream():
+        return _native.ctypes.c_void_p(_torch().cuda.current_stream().cuda_stream)
+
+    # -- entry points ---------------------------------------------------------
+    def get_k(self, coords_rel, weights, qd, omega, tile_tol=1e-11,
+              tile_pts=0, emulated_gemm=False, out=None, stats=True):
+        """Unsymmetrised K = X^T (w o G) (nao, nao) FP64 on the device.
+        coords_rel (npts, 3) FP64 device (kernel frame), weights (npts,) FP64
+        device, qd (nao, nao) FP64 device = proj @ dm."""
+        torch = _torch()
+        npts = int(coords_rel.shape[0])
+        nbytes = self.workspace_bytes(npts, tile_pts)
+        ws = self.workspace(nbytes)
+        if out is None:
+            out = torch.empty((self.nao, self.nao), dtype=torch.float64,
+                              device=self.device)
+        st = _native.WbCosxStats() if stats else None
+        flags = (_native.WB_K_GEMM_EMULATED_FP64 if emulated_gemm
+                 else _native.WB_K_GEMM_NATIVE_FP64)
+        _native.check(_native.lib().wb_cosx_get_k(
+            self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
+            _native.ptr(qd.contiguous()), float(omega), float(tile_tol),
+            int(tile_pts), flags, _native.ptr(out), _native.ptr(ws), nbytes,
+            self._stream(), _native.ctypes.byref(st) if st is not None else None),
+            'wb_cosx_get_k')
+        if st is not None:
+            self.last_stats = st.as_dict()
+        return out
+
+    def g(self, coords_rel, weights, f, omega, tile_tol=0.0, out=None,
+          stats=True):
+        """G (nao, ld) FP32 from F (nao, ld) FP32 AO-major, one tile."""
+        torch = _torch()
+        npts = int(coords_rel.shape[0])
+        ld = round32(npts)
+        if f.shape != (self.nao, ld) or f.dtype != torch.float32:
+            raise ValueError('f must be (nao, %d) float32' % ld)
+        # the G-only call needs no X / F / G buffers in the workspace
+        nbytes = self.workspace_bytes(npts)
+        ws = self.workspace(nbytes)
+        if out is None:
+            out = torch.empty((self.nao, ld), dtype=torch.float32,
+                              device=self.device)
+        st = _native.WbCosxStats() if stats else None
+        _native.check(_native.lib().wb_cosx_g(
+            self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
+            _native.ptr(f.contiguous()), float(omega), float(tile_tol),
+            _native.ptr(out), _native.ptr(ws), nbytes, self._stream(),
+            _native.ctypes.byref(st) if st is not None else None), 'wb_cosx_g')
+        if st is not None:
+            self.last_stats = st.as_dict()
+        return out
+
+    def ao_eval(self, coords_rel, out=None):
+        """X (nao, ld) FP64 AO-major."""
+        torch = _torch()
+        npts = int(coords_rel.shape[0])
+        if out is None:
+            out = torch.empty((self.nao, round32(npts)), dtype=torch.float64,
+                              device=self.device)
+        _native.check(_native.lib().wb_ao_eval(
+            self._h, _native.ptr(coords_rel), npts, _native.ptr(out),
+            self._stream()), 'wb_ao_eval')
+        return out
+
+    def int3c1e_dense(self, coords_rel, omega=0.0):
+        """Dense (npts, nao, nao) FP32 contracted spherical integrals
+        (validation only; refuses more than 2 GiB)."""
+        torch = _torch()
+        npts = int(coords_rel.shape[0])
+        need = npts * self.nao * self.nao * 4
+        if need > (2 << 30):
+            raise MemoryError('dense int3c1e needs %d bytes' % need)
+        out = torch.empty((npts, self.nao, self.nao), dtype=torch.float32,
+                          device=self.device)
+        _native.check(_native.lib().wb_int3c1e_dense(
+            self._h, _native.ptr(coords_rel), npts, float(omega),
+            _native.ptr(out), self._stream()), 'wb_int3c1e_dense')
+        return out
+
+
+def boys_eval(T, nmax):
+    """FP32 Boys F_0..F_nmax of a CUDA float32 tensor: (nmax+1, n)."""
+    torch = _torch()
+    if not 0 <= nmax <= 6:
+        raise ValueError('nmax must be 0..6')
+    T = T.to(torch.float32).contiguous()
+    out = torch.empty((nmax + 1, T.numel()), dtype=torch.float32, device=T.device)
+    _native.check(_native.lib().wb_boys_fp32(
+        _native.ptr(T), T.numel(), int(nmax), _native.ptr(out),
+        CosxEngine._stream()), 'wb_boys_fp32')
+    return out
+
+
+def boys_f64_host(nmax, t):
+    """FP64 Boys F_0..F_nmax at one argument (the library's host routine)."""
+    out = np.zeros(nmax + 1)
+    _native.check(_native.lib().wb_boys_f64_host(int(nmax), float(t),
+                                                 _native.ptr(out)))
+    return out
+
+
+def becke_partition(points, owner, atom_coords):
+    """Becke fuzzy-cell weight of each point's owner atom (host, native)."""
+    points = np.ascontiguousarray(points, dtype=np.float64)
+    owner = np.ascontiguousarray(owner, dtype=np.int32)
+    atoms = np.ascontiguousarray(atom_coords, dtype=np.float64)
+    out = np.zeros(len(points))
+    _native.check(_native.lib().wb_becke_partition(
+        _native.ptr(points), len(points), _native.ptr(owner), _native.ptr(atoms),
+        len(atoms), _native.ptr(out)), 'wb_becke_partition')
+    return out

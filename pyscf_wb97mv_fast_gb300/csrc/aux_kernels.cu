@@ -1,0 +1,506 @@
+// Supporting kernels of the COSX K build: per-omega primitive constants,
+// grid coordinate split, sub-block statistics for the screen, FP64 AO
+// evaluation, precision casts, the dense validation kernel and the Boys
+// batch kernel.
+#include <cmath>
+
+#include "boys.cuh"
+#include "launch.hpp"
+
+namespace wb {
+
+// -- per-omega primitive-pair constants (gpu/sgx_k.py:783-811) --------------
+// theta = w^2 / (w^2 + p) (1 for w = 0), tp = theta p and the R000
+// coefficients c_n = pref sqrt(theta) (-2 p theta)^n, n = 0..6, formed in
+// FP64 (IEEE-rounded, so identical to a host evaluation) and stored as FP32
+// hi + lo.  pref already carries C_a C_b K_AB 2 pi / p and the s/p
+// spherical normalisation.
+__global__ void omega_kernel(int npp, const double* __restrict__ p,
+                             const double* __restrict__ pref, double omega,
+                             float4* __restrict__ om) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= npp) return;
+    const double pm = p[m];
+    double th = 1.0, sth = 1.0;
+    if (omega > 0.0) {
+        const double w2 = omega * omega;
+        th = w2 / (w2 + pm);
+        sth = sqrt(th);
+    }
+    const double tp = th * pm;
+    const double q = -2.0 * pm * th;
+    float rec[16];
+    rec[0] = (float)tp;
+    rec[1] = (float)(tp - (double)rec[0]);
+    double c = pref[m] * sth;
+    for (int n = 0; n < 7; ++n) {
+        const float hi = (float)c;
+        rec[2 + 2 * n] = hi;
+        rec[3 + 2 * n] = (float)(c - (double)hi);
+        c *= q;
+    }
+    float4* o = om + 4 * (long long)m;
+    o[0] = make_float4(rec[0], rec[1], rec[2], rec[3]);
+    o[1] = make_float4(rec[4], rec[5], rec[6], rec[7]);
+    o[2] = make_float4(rec[8], rec[9], rec[10], rec[11]);
+    o[3] = make_float4(rec[12], rec[13], rec[14], rec[15]);
+}
+
+cudaError_t launch_omega(int npp, const double* p, const double* pref,
+                         double omega, float4* om, cudaStream_t s) {
+    if (npp <= 0) return cudaSuccess;
+    omega_kernel<<<(npp + 255) / 256, 256, 0, s>>>(npp, p, pref, omega, om);
+    return cudaGetLastError();
+}
+
+// -- FP64 (npts, 3) -> FP32 SoA hi / lo, padded with zeros to ld ----------
+__global__ void grid_prep_kernel(const double* __restrict__ c, int64_t npts,
+                                 int64_t ld, float* __restrict__ hi,
+                                 float* __restrict__ lo) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ld) return;
+    for (int x = 0; x < 3; ++x) {
+        float h = 0.0f, l = 0.0f;
+        if (g < npts) {
+            const double v = c[g * 3 + x];
+            h = (float)v;
+            l = (float)(v - (double)h);
+        }
+        hi[x * ld + g] = h;
+        lo[x * ld + g] = l;
+    }
+}
+
+cudaError_t launch_grid_prep(const double* coords, int64_t npts, int64_t ld,
+                             float* hi, float* lo, cudaStream_t s) {
+    if (ld <= 0) return cudaSuccess;
+    grid_prep_kernel<<<(unsigned)((ld + 255) / 256), 256, 0, s>>>(coords, npts,
+                                                                  ld, hi, lo);
+    return cudaGetLastError();
+}
+
+// -- sub-block statistics (gpu/sgx_k.py:866-903) ---------------------------
+// One warp per 32-point sub-block: FP64 centroid and radius of the valid
+// points (centroid rounded to nearest FP32, radius rounded up), and for
+// every (virtual) shell msh = max_g fl32(w_g) sum_{t in shell} |F_tg|.
+__global__ void sub_stats_kernel(const double* __restrict__ coords,
+                                 const double* __restrict__ w,
+                                 const float* __restrict__ F, int64_t npts,
+                                 int64_t ld, int nvshell,
+                                 const int* __restrict__ vs_ao0,
+                                 const int* __restrict__ vs_nf,
+                                 float4* __restrict__ sub_cr,
+                                 float* __restrict__ msh) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int nsub = (int)(ld / 32);
+    if (warp >= nsub) return;
+    const int64_t g = (int64_t)warp * 32 + lane;
+    const bool valid = g < npts;
+    double cx = 0.0, cy = 0.0, cz = 0.0;
+    if (valid) { cx = coords[g * 3]; cy = coords[g * 3 + 1]; cz = coords[g * 3 + 2]; }
+    double sx = cx, sy = cy, sz = cz;
+    for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        sz += __shfl_xor_sync(0xffffffffu, sz, o);
+    }
+    const int64_t rem = npts - (int64_t)warp * 32;
+    const int nvalid = rem >= 32 ? 32 : (rem > 0 ? (int)rem : 0);
+    double mx = 0.0, my = 0.0, mz = 0.0;
+    if (nvalid > 0) { mx = sx / nvalid; my = sy / nvalid; mz = sz / nvalid; }
+    double d = 0.0;
+    if (valid) {
+        const double ex = cx - mx, ey = cy - my, ez = cz - mz;
+        d = sqrt(ex * ex + ey * ey + ez * ez);
+    }
+    for (int o = 16; o > 0; o >>= 1) d = fmax(d, __shfl_xor_sync(0xffffffffu, d, o));
+    if (lane == 0) {
+        float r = (float)d;
+        if ((double)r < d) r = nextafterf(r, INFINITY);
+        sub_cr[warp] = make_float4((float)mx, (float)my, (float)mz, r);
+    }
+    const float w32 = valid ? (float)w[g] : 0.0f;
+    for (int s = 0; s < nvshell; ++s) {
+        const int a0 = vs_ao0[s], nf = vs_nf[s];
+        float acc = 0.0f;
+        for (int t = 0; t < nf; ++t)
+            acc += fabsf(F[(int64_t)(a0 + t) * ld + g]) * w32;
+        for (int o = 16; o > 0; o >>= 1)
+            acc = fmaxf(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+        if (lane == 0) msh[(int64_t)warp * nvshell + s] = acc;
+    }
+}
+
+cudaError_t launch_sub_stats(const double* coords, const double* weights,
+                             const float* F, int64_t npts, int64_t ld,
+                             int nvshell, const int* vs_ao0, const int* vs_nf,
+                             float4* sub_cr, float* msh, cudaStream_t s) {
+    const int64_t nsub = ld / 32;
+    if (nsub <= 0) return cudaSuccess;
+    const int warps = 4;
+    sub_stats_kernel<<<(unsigned)((nsub + warps - 1) / warps), 32 * warps, 0, s>>>(
+        coords, weights, F, npts, ld, nvshell, vs_ao0, vs_nf, sub_cr, msh);
+    return cudaGetLastError();
+}
+
+// -- casts ---------------------------------------------------------------
+__global__ void f64_to_f32_kernel(const double* __restrict__ in,
+                                  float* __restrict__ out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = __double2float_rn(in[i]);
+}
+
+cudaError_t launch_f64_to_f32(const double* in, float* out, int64_t n,
+                              cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    f64_to_f32_kernel<<<(unsigned)blocks, 256, 0, s>>>(in, out, n);
+    return cudaGetLastError();
+}
+
+// out[mu, g] = w_g * (double) G[mu, g]  (gpu/sgx_k.py:734: FP64 weights)
+__global__ void weight_g_kernel(const float* __restrict__ G,
+                                const double* __restrict__ w, int64_t npts,
+                                int64_t ld, int64_t total,
+                                double* __restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t g = i % ld;
+        out[i] = g < npts ? w[g] * (double)G[i] : 0.0;
+    }
+}
+
+cudaError_t launch_weight_g(const float* G, const double* w, int64_t npts,
+                            int64_t ld, int nao, double* out, cudaStream_t s) {
+    const int64_t total = ld * nao;
+    if (total <= 0) return cudaSuccess;
+    int64_t blocks = (total + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    weight_g_kernel<<<(unsigned)blocks, 256, 0, s>>>(G, w, npts, ld, total, out);
+    return cudaGetLastError();
+}
+
+// -- FP64 AO evaluation (gpu/ao_eval.py:255-329, deriv 0) -------------------
+// One thread per (point, shell), threads of a block on consecutive points:
+// every AO column is written coalesced.  d = r - A in FP64, exp in FP64,
+// contraction, Cartesian monomials, cart -> sph with FP64 constants.
+__constant__ double c_c2s0[1];
+__constant__ double c_c2s1[9];
+__constant__ double c_c2s2[30];
+__constant__ double c_c2s3[70];
+
+template<int L>
+__device__ __forceinline__ const double* c2s_ptr() {
+    if constexpr (L == 0) return c_c2s0;
+    else if constexpr (L == 1) return c_c2s1;
+    else if constexpr (L == 2) return c_c2s2;
+    else return c_c2s3;
+}
+
+__device__ __forceinline__ double ipow(double x, int n) {
+    double r = 1.0;
+    for (int i = 0; i < n; ++i) r *= x;
+    return r;
+}
+
+template<int L>
+__device__ __forceinline__ void ao_shell(const AoArgs& A, int sh, int64_t g,
+                                         double dx, double dy, double dz,
+                                         double r2) {
+    constexpr int NC = (L + 1) * (L + 2) / 2, NS = 2 * L + 1;
+    double mono[NC];
+    {
+        int c = 0;
+#pragma unroll
+        for (int lx = L; lx >= 0; --lx)
+#pragma unroll
+            for (int ly = L - lx; ly >= 0; --ly) {
+                mono[c++] = ipow(dx, lx) * ipow(dy, ly) * ipow(dz, L - lx - ly);
+            }
+    }
+    const double* c2s = c2s_ptr<L>();
+    const int np = A.sh_np[sh], nc = A.sh_nc[sh];
+    const double* ex = A.exps + A.sh_eoff[sh];
+    const double* co = A.coeffs + A.sh_coff[sh];
+    const int ao0 = A.sh_ao0[sh];
+    for (int ci = 0; ci < nc; ++ci) {
+        double rad = 0.0;
+        for (int k = 0; k < np; ++k) rad += co[k * nc + ci] * exp(-ex[k] * r2);
+#pragma unroll
+        for (int m = 0; m < NS; ++m) {
+            double v = 0.0;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) v += c2s[c * NS + m] * mono[c];
+            A.X[(int64_t)(ao0 + ci * NS + m) * A.ld + g] = rad * v;
+        }
+    }
+}
+
+__global__ void ao_eval_kernel(const AoArgs A) {
+    const int sh = blockIdx.y;
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= A.ld) return;
+    const int l = A.sh_l[sh];
+    if (g >= A.npts) {
+        const int n = A.sh_nc[sh] * (2 * l + 1);
+        for (int i = 0; i < n; ++i) A.X[(int64_t)(A.sh_ao0[sh] + i) * A.ld + g] = 0.0;
+        return;
+    }
+    const double dx = A.coords[g * 3] - A.sh_ctr[sh * 3];
+    const double dy = A.coords[g * 3 + 1] - A.sh_ctr[sh * 3 + 1];
+    const double dz = A.coords[g * 3 + 2] - A.sh_ctr[sh * 3 + 2];
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    switch (l) {
+    case 0: ao_shell<0>(A, sh, g, dx, dy, dz, r2); break;
+    case 1: ao_shell<1>(A, sh, g, dx, dy, dz, r2); break;
+    case 2: ao_shell<2>(A, sh, g, dx, dy, dz, r2); break;
+    default: ao_shell<3>(A, sh, g, dx, dy, dz, r2); break;
+    }
+}
+
+cudaError_t launch_ao_eval(const AoArgs& a, cudaStream_t s) {
+    if (a.ld <= 0 || a.nbas <= 0) return cudaSuccess;
+    dim3 grid((unsigned)((a.ld + 127) / 128), (unsigned)a.nbas);
+    ao_eval_kernel<<<grid, 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// c2s tables filled by the host (same formula as the host pair builder)
+cudaError_t upload_c2s_tables(const double* t0, const double* t1,
+                              const double* t2, const double* t3) {
+    cudaError_t e;
+    if ((e = cudaMemcpyToSymbol(c_c2s0, t0, sizeof(double) * 1)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(c_c2s1, t1, sizeof(double) * 9)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(c_c2s2, t2, sizeof(double) * 30)) != cudaSuccess) return e;
+    return cudaMemcpyToSymbol(c_c2s3, t3, sizeof(double) * 70);
+}
+
+// -- dense contracted spherical A (validation, gpu/int3c1e.py:230-271) -------
+// One thread per (point, pair), run-time L, arrays in local memory.  Uses
+// the same pair tables and the same Boys / R / E math as the fused kernels
+// but forms the Cartesian block explicitly.
+__constant__ float c_c2s_f[4][70];
+
+__device__ void cart_comp(int l, int c, int* i, int* j, int* k) {
+    int r = 0;
+    while ((r + 1) * (r + 2) / 2 <= c) ++r;
+    *i = l - r;
+    *j = r - (c - r * (r + 1) / 2);
+    *k = l - *i - *j;
+}
+
+__device__ int e_index(int la, int lb, int i, int j, int t) {
+    // position of (i, j, t) in the packed per-axis list (E^{00}_0 excluded)
+    int n = 0;
+    for (int ii = 0; ii <= la; ++ii)
+        for (int jj = 0; jj <= lb; ++jj)
+            for (int tt = 0; tt <= ii + jj; ++tt) {
+                if (ii == 0 && jj == 0) continue;
+                if (ii == i && jj == j && tt == t) return n;
+                ++n;
+            }
+    return -1;
+}
+
+__device__ float e_val(const float* Em, int cnt, int ax, int la, int lb,
+                       int i, int j, int t) {
+    if (i == 0 && j == 0) return t == 0 ? 1.0f : 0.0f;
+    return Em[ax * cnt + e_index(la, lb, i, j, t)];
+}
+
+template<int LMAXC>
+__device__ void boys_dyn(int L, float T, float* F, const float4* tab) {
+    switch (L) {
+    case 0: boys_fp32<0>(T, F, tab); break;
+    case 1: boys_fp32<1>(T, F, tab); break;
+    case 2: boys_fp32<2>(T, F, tab); break;
+    case 3: boys_fp32<3>(T, F, tab); break;
+    case 4: boys_fp32<4>(T, F, tab); break;
+    case 5: boys_fp32<5>(T, F, tab); break;
+    default: boys_fp32<6>(T, F, tab); break;
+    }
+}
+
+struct DenseArgs {
+    CosxArgs a;
+    int npairs, nao;
+    const int* pclass;
+    const int* pl;          // (npairs, 2): la, lb
+    const int* estride;     // per class, floats
+    float* out;             // (npts, nao, nao)
+};
+
+__global__ void dense_kernel(const DenseArgs D) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)D.a.npts * D.npairs;
+    if (idx >= total) return;
+    const int64_t g = idx / D.npairs;
+    const int k = (int)(idx - g * D.npairs);
+    const CosxArgs& A = D.a;
+    const int4 hdr = A.hdr[k];
+    const int ia0 = hdr.x, ib0 = hdr.y, pp0 = hdr.z, npp = hdr.w & 0xffff;
+    const int cls = D.pclass[k];
+    const int la = D.pl[2 * k], lb = D.pl[2 * k + 1], L = la + lb;
+    const int nca = (la + 1) * (la + 2) / 2, ncb = (lb + 1) * (lb + 2) / 2;
+    int cnt = 0;
+    for (int i = 0; i <= la; ++i)
+        for (int j = 0; j <= lb; ++j) cnt += i + j + 1;
+    cnt -= 1;
+    const float gxh = A.gxyz_hi[g], gyh = A.gxyz_hi[A.ld + g], gzh = A.gxyz_hi[2 * A.ld + g];
+    const float gxl = A.gxyz_lo[g], gyl = A.gxyz_lo[A.ld + g], gzl = A.gxyz_lo[2 * A.ld + g];
+    float Ac[100];
+    for (int i = 0; i < 100; ++i) Ac[i] = 0.0f;
+    float R[7][7][7];
+    for (int m = pp0; m < pp0 + npp; ++m) {
+        const float4 ph = A.geo[2 * m], pl = A.geo[2 * m + 1];
+        const float dx = (ph.x - gxh) + (pl.x - gxl);
+        const float dy = (ph.y - gyh) + (pl.y - gyl);
+        const float dz = (ph.z - gzh) + (pl.z - gzl);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float* o = (const float*)(A.om + 4 * (int64_t)m);
+        const float T = fmaf(o[0], r2, o[1] * r2);
+        float Fb[7];
+        boys_dyn<6>(L, T, Fb, A.boys);
+        for (int t = 0; t < 7; ++t)
+            for (int u = 0; u < 7; ++u)
+                for (int v = 0; v < 7; ++v) R[t][u][v] = 0.0f;
+        for (int n = L; n >= 0; --n) {
+            const int mm = L - n;
+            for (int u = 0; u < mm; ++u)
+                for (int v = 0; v < mm - u; ++v)
+                    for (int t = mm - u - v; t >= 1; --t)
+                        R[t][u][v] = (t == 1) ? dx * R[0][u][v]
+                            : fmaf(dx, R[t - 1][u][v], (float)(t - 1) * R[t - 2][u][v]);
+            for (int v = 0; v < mm; ++v)
+                for (int u = mm - v; u >= 1; --u)
+                    R[0][u][v] = (u == 1) ? dy * R[0][0][v]
+                        : fmaf(dy, R[0][u - 1][v], (float)(u - 1) * R[0][u - 2][v]);
+            for (int v = mm; v >= 1; --v)
+                R[0][0][v] = (v == 1) ? dz * R[0][0][0]
+                    : fmaf(dz, R[0][0][v - 1], (float)(v - 1) * R[0][0][v - 2]);
+            R[0][0][0] = fmaf(o[2 + 2 * n], Fb[n], o[3 + 2 * n] * Fb[n]);
+        }
+        const float* Em = (const float*)A.Ecls[cls] +
+                          (int64_t)(m - A.pp_begin[cls]) * D.estride[cls];
+        for (int ca = 0; ca < nca; ++ca) {
+            int i, j, kk;
+            cart_comp(la, ca, &i, &j, &kk);
+            for (int cb = 0; cb < ncb; ++cb) {
+                int ip, jp, kp;
+                cart_comp(lb, cb, &ip, &jp, &kp);
+                float s = 0.0f;
+                for (int t = 0; t <= i + ip; ++t) {
+                    const float ex = e_val(Em, cnt, 0, la, lb, i, ip, t);
+                    for (int u = 0; u <= j + jp; ++u) {
+                        const float ey = e_val(Em, cnt, 1, la, lb, j, jp, u);
+                        for (int v = 0; v <= kk + kp; ++v)
+                            s += ex * ey * e_val(Em, cnt, 2, la, lb, kk, kp, v) * R[t][u][v];
+                    }
+                }
+                Ac[ca * ncb + cb] += s;
+            }
+        }
+    }
+    const int na = 2 * la + 1, nb = 2 * lb + 1;
+    float* row = D.out + g * (int64_t)D.nao * D.nao;
+    for (int mu = 0; mu < na; ++mu)
+        for (int nu = 0; nu < nb; ++nu) {
+            float v = 0.0f;
+            for (int ca = 0; ca < nca; ++ca) {
+                const float cam = la <= 1 ? (ca == mu ? 1.0f : 0.0f)
+                                          : c_c2s_f[la][ca * na + mu];
+                if (cam == 0.0f) continue;
+                for (int cb = 0; cb < ncb; ++cb) {
+                    const float cbn = lb <= 1 ? (cb == nu ? 1.0f : 0.0f)
+                                              : c_c2s_f[lb][cb * nb + nu];
+                    v += cam * cbn * Ac[ca * ncb + cb];
+                }
+            }
+            row[(int64_t)(ia0 + mu) * D.nao + ib0 + nu] = v;
+            row[(int64_t)(ib0 + nu) * D.nao + ia0 + mu] = v;
+        }
+}
+
+cudaError_t upload_c2s_f(const float* all /* 4 x 70 */) {
+    return cudaMemcpyToSymbol(c_c2s_f, all, sizeof(float) * 4 * 70);
+}
+
+cudaError_t launch_dense_impl(const CosxArgs& a, int npairs, const int* pclass,
+                              const int* pl, const int* estride, int nao,
+                              float* out, cudaStream_t s) {
+    DenseArgs D;
+    D.a = a; D.npairs = npairs; D.nao = nao; D.pclass = pclass; D.pl = pl;
+    D.estride = estride; D.out = out;
+    const int64_t total = (int64_t)a.npts * npairs;
+    if (total <= 0) return cudaSuccess;
+    dense_kernel<<<(unsigned)((total + 63) / 64), 64, 0, s>>>(D);
+    return cudaGetLastError();
+}
+
+// -- Boys batch (tests, gpu/boys.py:181-189) ---------------------------------
+template<int L>
+__global__ void boys_batch_kernel(const float* __restrict__ t, int64_t n,
+                                  const float4* __restrict__ tab,
+                                  float* __restrict__ out) {
+    __shared__ float4 stab[145 * 5];
+    for (int i = threadIdx.x; i < 145 * 5; i += blockDim.x) stab[i] = tab[i];
+    __syncthreads();
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float F[L + 1];
+    boys_fp32<L>(t[i], F, stab);
+#pragma unroll
+    for (int m = 0; m <= L; ++m) out[m * n + i] = F[m];
+}
+
+cudaError_t launch_boys(const float* t, int64_t n, int nmax,
+                        const float4* tab, float* out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    switch (nmax) {
+    case 0: boys_batch_kernel<0><<<blocks, 256, 0, s>>>(t, n, tab, out); break;
+    case 1: boys_batch_kernel<1><<<blocks, 256, 0, s>>>(t, n, tab, out); break;
+    case 2: boys_batch_kernel<2><<<blocks, 256, 0, s>>>(t, n, tab, out); break;
+    case 3: boys_batch_kernel<3><<<blocks, 256, 0, s>>>(t, n, tab, out); break;
+    case 4: boys_batch_kernel<4><<<blocks, 256, 0, s>>>(t, n, tab, out); break;
+    case 5: boys_batch_kernel<5><<<blocks, 256, 0, s>>>(t, n, tab, out); break;
+    case 6: boys_batch_kernel<6><<<blocks, 256, 0, s>>>(t, n, tab, out); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace wb
+
+namespace wb {
+
+// -- FP32 FMA throughput probe (the roofline denominator of the FP32-pipe
+// kernels): 8 independent FMA chains per thread, nothing but FFMA in the
+// loop; each thread writes one value so nothing is optimised away.
+__global__ void fma_probe_kernel(int64_t iters, float* __restrict__ out) {
+    float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f,
+          a3 = a0 + 3e-7f, a4 = a0 + 4e-7f, a5 = a0 + 5e-7f, a6 = a0 + 6e-7f,
+          a7 = a0 + 7e-7f;
+    const float m = 0.999999f, c = 1e-7f;
+    for (int64_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            a0 = fmaf(a0, m, c); a1 = fmaf(a1, m, c); a2 = fmaf(a2, m, c);
+            a3 = fmaf(a3, m, c); a4 = fmaf(a4, m, c); a5 = fmaf(a5, m, c);
+            a6 = fmaf(a6, m, c); a7 = fmaf(a7, m, c);
+        }
+    }
+    out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] =
+        a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+cudaError_t launch_fma_probe(int64_t iters, int blocks, int threads,
+                             float* out, cudaStream_t s) {
+    fma_probe_kernel<<<blocks, threads, 0, s>>>(iters, out);
+    return cudaGetLastError();
+}
+
+}  // namespace wb

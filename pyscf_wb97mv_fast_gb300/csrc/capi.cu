@@ -1,0 +1,647 @@
+// C ABI of libwb97mv_gb300 (declarations and contracts in
+// include/wb97mv_gb300.h).  Host orchestration of the COSX K build: table
+// upload, workspace carving, the per-tile pipeline and cuBLAS GEMMs.
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "host.hpp"
+#include "launch.hpp"
+#include "wb97mv_gb300.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(WB_ERR_OUT_OF_MEMORY, std::string(where) + ": " +
+                                              cudaGetErrorString(e));
+    return fail(WB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define WB_CUDA(call)                                              \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);        \
+    } while (0)
+
+#define WB_CUBLAS(call)                                            \
+    do {                                                           \
+        cublasStatus_t s_ = (call);                                \
+        if (s_ != CUBLAS_STATUS_SUCCESS)                           \
+            return fail(s_ == CUBLAS_STATUS_ALLOC_FAILED           \
+                            ? WB_ERR_OUT_OF_MEMORY : WB_ERR_CUBLAS,\
+                        std::string(#call) + " failed, status " +  \
+                            std::to_string((int)s_));              \
+    } while (0)
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+inline int64_t round32(int64_t x) { return (x + 31) / 32 * 32; }
+
+// Boys table per device, built once per process
+std::mutex g_boys_mu;
+std::map<int, float4*> g_boys;
+
+int device_boys(int dev, float4** out) {
+    std::lock_guard<std::mutex> lk(g_boys_mu);
+    auto it = g_boys.find(dev);
+    if (it != g_boys.end()) { *out = it->second; return WB_OK; }
+    const std::vector<float> tab = wb::boys_table();
+    float4* d = nullptr;
+    WB_CUDA(cudaMalloc(&d, tab.size() * sizeof(float)));
+    WB_CUDA(cudaMemcpy(d, tab.data(), tab.size() * sizeof(float),
+                       cudaMemcpyHostToDevice));
+    g_boys[dev] = d;
+    *out = d;
+    return WB_OK;
+}
+
+int upload_constants() {
+    std::vector<double> c[4];
+    for (int l = 0; l < 4; ++l) c[l] = wb::cart2sph(l);
+    WB_CUDA(wb::upload_c2s_tables(c[0].data(), c[1].data(), c[2].data(),
+                                  c[3].data()));
+    float f[4][70];
+    std::memset(f, 0, sizeof(f));
+    for (int l = 0; l < 4; ++l)
+        for (size_t i = 0; i < c[l].size(); ++i) f[l][i] = (float)c[l][i];
+    WB_CUDA(wb::upload_c2s_f(&f[0][0]));
+    return WB_OK;
+}
+
+}  // namespace
+
+struct wb_cosx {
+    int device = 0;
+    int nsm = 1;
+    wb::HostPairs hp;
+    cublasHandle_t cublas = nullptr;
+    void* block = nullptr;
+    // pair tables
+    float4* geo = nullptr;
+    double* p = nullptr;
+    double* pref = nullptr;
+    float4* E = nullptr;
+    int4* hdr = nullptr;
+    int2* pshell = nullptr;
+    float2* ptau = nullptr;
+    float4* bnd = nullptr;
+    float* bpref = nullptr;
+    long long* pflops = nullptr;
+    int* pnint = nullptr;
+    int* vs_ao0 = nullptr;
+    int* vs_nf = nullptr;
+    int* pclass = nullptr;
+    int* pl = nullptr;
+    int* estride = nullptr;
+    float4* boys = nullptr;
+    // AO evaluation (physical shells)
+    int nbas = 0;
+    int* sh_l = nullptr;
+    int* sh_np = nullptr;
+    int* sh_nc = nullptr;
+    int* sh_eoff = nullptr;
+    int* sh_coff = nullptr;
+    int* sh_ao0 = nullptr;
+    double* sh_ctr = nullptr;
+    double* exps = nullptr;
+    double* coeffs = nullptr;
+    int blocks_per_sm[wb::NCLASS] = {0};
+};
+
+namespace {
+
+struct WsLayout {
+    size_t om = 0, gh = 0, gl = 0, subcr = 0, msh = 0, counters = 0, work = 0;
+    size_t X = 0, F64 = 0, F32 = 0, G32 = 0, total = 0;
+};
+
+WsLayout ws_layout(const wb_cosx* h, int64_t ldt, bool full) {
+    WsLayout L;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align256(off + bytes);
+        return o;
+    };
+    const int64_t nsub = ldt / 32;
+    const int nao = h->hp.nao;
+    L.counters = take(sizeof(unsigned long long) * 3 * wb::NCLASS);
+    L.work = take(sizeof(int) * wb::NCLASS);
+    L.om = take(sizeof(float) * 16 * (size_t)std::max(h->hp.npp, 1));
+    L.gh = take(sizeof(float) * 3 * (size_t)ldt);
+    L.gl = take(sizeof(float) * 3 * (size_t)ldt);
+    L.subcr = take(sizeof(float4) * (size_t)nsub);
+    L.msh = take(sizeof(float) * (size_t)nsub * std::max(h->hp.nvshell, 1));
+    if (full) {
+        L.X = take(sizeof(double) * (size_t)nao * ldt);
+        L.F64 = take(sizeof(double) * (size_t)nao * ldt);
+        L.F32 = take(sizeof(float) * (size_t)nao * ldt);
+        L.G32 = take(sizeof(float) * (size_t)nao * ldt);
+    }
+    L.total = off;
+    return L;
+}
+
+template<typename T>
+T* at(void* base, size_t off) {
+    return reinterpret_cast<T*>(static_cast<char*>(base) + off);
+}
+
+wb::CosxArgs make_args(const wb_cosx* h, void* ws, const WsLayout& L,
+                       int64_t ldt, int64_t npts_t, const float* F, float* G,
+                       double tile_tol) {
+    wb::CosxArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.F = F;
+    a.G = G;
+    a.ld = ldt;
+    a.npts = (int)npts_t;
+    a.nsub = (int)(ldt / 32);
+    a.geo = h->geo;
+    a.om = at<float4>(ws, L.om);
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        a.Ecls[c] = h->E + h->hp.cls[c].e_base / 4;
+        a.pp_begin[c] = h->hp.cls[c].pp_begin;
+    }
+    a.hdr = h->hdr;
+    a.pshell = h->pshell;
+    a.ptau = h->ptau;
+    a.bnd = h->bnd;
+    a.bpref = h->bpref;
+    a.sub_cr = at<float4>(ws, L.subcr);
+    a.msh = at<float>(ws, L.msh);
+    a.nvshell = h->hp.nvshell;
+    a.tol = tile_tol > 0.0 ? (float)(tile_tol / 1.001) : 0.0f;
+    if (tile_tol > 0.0 && a.tol <= 0.0f) a.tol = 1e-38f;
+    a.gxyz_hi = at<float>(ws, L.gh);
+    a.gxyz_lo = at<float>(ws, L.gl);
+    a.boys = h->boys;
+    a.pflops = h->pflops;
+    a.pnint = h->pnint;
+    a.counters = at<unsigned long long>(ws, L.counters);
+    a.work = at<int>(ws, L.work);
+    return a;
+}
+
+// stats, sub-block prep and the class launches of one tile; F and G are
+// (nao, ldt) AO-major, G is zeroed here
+int run_g_tile(wb_cosx* h, const double* coords, const double* weights,
+               int64_t npts_t, int64_t ldt, const float* F, float* G,
+               double tile_tol, void* ws, const WsLayout& L, cudaStream_t s,
+               int* launches) {
+    const wb::CosxArgs a = make_args(h, ws, L, ldt, npts_t, F, G, tile_tol);
+    WB_CUDA(wb::launch_grid_prep(coords, npts_t, ldt, at<float>(ws, L.gh),
+                                 at<float>(ws, L.gl), s));
+    WB_CUDA(wb::launch_sub_stats(coords, weights, F, npts_t, ldt,
+                                 h->hp.nvshell, h->vs_ao0, h->vs_nf,
+                                 at<float4>(ws, L.subcr), at<float>(ws, L.msh),
+                                 s));
+    WB_CUDA(cudaMemsetAsync(G, 0, sizeof(float) * (size_t)h->hp.nao * ldt, s));
+    WB_CUDA(cudaMemsetAsync(at<int>(ws, L.work), 0, sizeof(int) * wb::NCLASS, s));
+    *launches += 2;
+    const int nsub = (int)(ldt / 32);
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        const wb::ClassRange& r = h->hp.cls[c];
+        if (r.pair_end <= r.pair_begin) continue;
+        const int want = (nsub + 3) / 4;
+        const int cap = std::max(1, h->blocks_per_sm[c]) * h->nsm;
+        const int grid = std::max(1, std::min(want, cap));
+        WB_CUDA(wb::launch_cosx_class_range(c, a, r.pair_begin, r.pair_end,
+                                            grid, s));
+        *launches += 1;
+    }
+    return WB_OK;
+}
+
+int read_stats(wb_cosx* h, void* ws, const WsLayout& L, int64_t ntasks_total,
+               cudaStream_t s, wb_cosx_stats* stats, int launches) {
+    if (!stats) return WB_OK;
+    unsigned long long c[3 * wb::NCLASS];
+    WB_CUDA(cudaMemcpyAsync(c, at<unsigned long long>(ws, L.counters),
+                            sizeof(c), cudaMemcpyDeviceToHost, s));
+    WB_CUDA(cudaStreamSynchronize(s));
+    std::memset(stats, 0, sizeof(*stats));
+    stats->tasks_total = ntasks_total;
+    for (int k = 0; k < wb::NCLASS; ++k) {
+        stats->tasks_kept += (int64_t)c[3 * k];
+        stats->tasks_kept_class[k] = (int64_t)c[3 * k];
+        stats->model_flops += (double)c[3 * k + 1];
+        stats->model_flops_class[k] = (double)c[3 * k + 1];
+        stats->integrals += (double)c[3 * k + 2];
+    }
+    stats->kernel_launches = launches;
+    (void)h;
+    return WB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wb_version(void) { return 1; }
+
+const char* wb_last_error(void) { return g_err.c_str(); }
+
+const char* wb_status_string(int status) {
+    switch (status) {
+    case WB_OK: return "ok";
+    case WB_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case WB_ERR_UNSUPPORTED: return "unsupported input";
+    case WB_ERR_CUDA: return "CUDA error";
+    case WB_ERR_CUBLAS: return "cuBLAS error";
+    case WB_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case WB_ERR_WORKSPACE: return "workspace too small";
+    case WB_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+int wb_boys_f64_host(int nmax, double t, double* out) {
+    if (nmax < 0 || nmax > 40 || !out || !(t >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_boys_f64_host: bad arguments");
+    wb::boys_f64(nmax, t, out);
+    return WB_OK;
+}
+
+int wb_becke_partition(const double* points, int64_t n, const int* owner,
+                       const double* atom_coords, int natm, double* out) {
+    if (n < 0 || natm <= 0 || (!points && n) || (!owner && n) || !atom_coords ||
+        (!out && n))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_becke_partition: bad arguments");
+    for (int64_t i = 0; i < n; ++i)
+        if (owner[i] < 0 || owner[i] >= natm)
+            return fail(WB_ERR_INVALID_ARGUMENT, "wb_becke_partition: bad owner");
+    wb::becke_partition(points, n, owner, atom_coords, natm, out);
+    return WB_OK;
+}
+
+int wb_cosx_create(const wb_basis* basis, const double origin[3],
+                   double pair_cutoff, wb_cosx** out) {
+    if (!basis || !origin || !out)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_create: null argument");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return fail(WB_ERR_NO_DEVICE, "wb_cosx_create: no CUDA device");
+    }
+    wb_cosx* h = new wb_cosx();
+    std::string err;
+    int st = wb::build_pairs(*basis, origin, pair_cutoff, h->hp, err);
+    if (st != WB_OK) {
+        delete h;
+        return fail(st, err);
+    }
+    auto cleanup = [&](int code) {
+        wb_cosx_destroy(h);
+        return code;
+    };
+    if (cudaGetDevice(&h->device) != cudaSuccess) return cleanup(cuda_fail(cudaGetLastError(), "cudaGetDevice"));
+    cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device);
+    if ((st = upload_constants()) != WB_OK) return cleanup(st);
+    if ((st = device_boys(h->device, &h->boys)) != WB_OK) return cleanup(st);
+
+    const wb::HostPairs& hp = h->hp;
+    // physical shell tables for the AO evaluation
+    h->nbas = basis->nbas;
+    std::vector<int> sh_ao0(basis->nbas);
+    {
+        int ao = 0;
+        for (int s = 0; s < basis->nbas; ++s) {
+            sh_ao0[s] = ao;
+            ao += basis->shell_nctr[s] * (2 * basis->shell_l[s] + 1);
+        }
+    }
+    int nexp = 0, ncoef = 0;
+    for (int s = 0; s < basis->nbas; ++s) {
+        nexp = std::max(nexp, basis->shell_exp_off[s] + basis->shell_nprim[s]);
+        ncoef = std::max(ncoef, basis->shell_coef_off[s] +
+                                    basis->shell_nprim[s] * basis->shell_nctr[s]);
+    }
+    std::vector<double> ctr(3 * (size_t)std::max(basis->nbas, 1));
+    for (int s = 0; s < basis->nbas; ++s)
+        for (int x = 0; x < 3; ++x)
+            ctr[3 * s + x] = basis->atom_coords[basis->shell_atom[s] * 3 + x] - origin[x];
+    std::vector<int> pl, estr(wb::NCLASS);
+    for (int k = 0; k < hp.npairs; ++k) {
+        pl.push_back(hp.vsh[hp.pshell[2 * k]].l);
+        pl.push_back(hp.vsh[hp.pshell[2 * k + 1]].l);
+    }
+    for (int la = 0; la <= 3; ++la)
+        for (int lb = 0; lb <= la; ++lb) estr[wb::class_of(la, lb)] = wb::e_stride(la, lb);
+
+    struct Piece { void** dst; const void* src; size_t bytes; };
+    std::vector<Piece> pieces;
+    auto add = [&](void** dst, const void* src, size_t bytes) {
+        pieces.push_back({dst, src, bytes});
+    };
+    add((void**)&h->geo, hp.geo.data(), hp.geo.size() * sizeof(float));
+    add((void**)&h->p, hp.p.data(), hp.p.size() * sizeof(double));
+    add((void**)&h->pref, hp.pref.data(), hp.pref.size() * sizeof(double));
+    add((void**)&h->E, hp.E.data(), hp.E.size() * sizeof(float));
+    add((void**)&h->hdr, hp.hdr.data(), hp.hdr.size() * sizeof(int32_t));
+    add((void**)&h->pshell, hp.pshell.data(), hp.pshell.size() * sizeof(int32_t));
+    add((void**)&h->ptau, hp.ptau.data(), hp.ptau.size() * sizeof(float));
+    add((void**)&h->bnd, hp.bnd.data(), hp.bnd.size() * sizeof(float));
+    add((void**)&h->bpref, hp.bpref.data(), hp.bpref.size() * sizeof(float));
+    add((void**)&h->pflops, hp.pflops.data(), hp.pflops.size() * sizeof(int64_t));
+    add((void**)&h->pnint, hp.pnint.data(), hp.pnint.size() * sizeof(int32_t));
+    add((void**)&h->vs_ao0, hp.vs_ao0.data(), hp.vs_ao0.size() * sizeof(int32_t));
+    add((void**)&h->vs_nf, hp.vs_nf.data(), hp.vs_nf.size() * sizeof(int32_t));
+    add((void**)&h->pclass, hp.pclass.data(), hp.pclass.size() * sizeof(int32_t));
+    add((void**)&h->pl, pl.data(), pl.size() * sizeof(int));
+    add((void**)&h->estride, estr.data(), estr.size() * sizeof(int));
+    add((void**)&h->sh_l, basis->shell_l, sizeof(int) * basis->nbas);
+    add((void**)&h->sh_np, basis->shell_nprim, sizeof(int) * basis->nbas);
+    add((void**)&h->sh_nc, basis->shell_nctr, sizeof(int) * basis->nbas);
+    add((void**)&h->sh_eoff, basis->shell_exp_off, sizeof(int) * basis->nbas);
+    add((void**)&h->sh_coff, basis->shell_coef_off, sizeof(int) * basis->nbas);
+    add((void**)&h->sh_ao0, sh_ao0.data(), sizeof(int) * basis->nbas);
+    add((void**)&h->sh_ctr, ctr.data(), sizeof(double) * 3 * basis->nbas);
+    add((void**)&h->exps, basis->exps, sizeof(double) * nexp);
+    add((void**)&h->coeffs, basis->coeffs, sizeof(double) * ncoef);
+    size_t total = 0;
+    for (const Piece& pc : pieces) total = align256(total + pc.bytes);
+    total = std::max<size_t>(total, 256);
+    cudaError_t e = cudaMalloc(&h->block, total);
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc(pair tables)"));
+    size_t off = 0;
+    for (const Piece& pc : pieces) {
+        char* dst = static_cast<char*>(h->block) + off;
+        *pc.dst = dst;
+        if (pc.bytes) {
+            e = cudaMemcpy(dst, pc.src, pc.bytes, cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMemcpy(pair tables)"));
+        }
+        off = align256(off + pc.bytes);
+    }
+    if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS)
+        return cleanup(fail(WB_ERR_CUBLAS, "cublasCreate failed"));
+    for (int c = 0; c < wb::NCLASS; ++c)
+        h->blocks_per_sm[c] = wb::cosx_class_blocks_per_sm(c);
+    *out = h;
+    return WB_OK;
+}
+
+int wb_cosx_destroy(wb_cosx* h) {
+    if (!h) return WB_OK;
+    if (h->cublas) cublasDestroy(h->cublas);
+    if (h->block) cudaFree(h->block);
+    delete h;
+    return WB_OK;
+}
+
+int wb_cosx_get_info(const wb_cosx* h, wb_cosx_info* info) {
+    if (!h || !info) return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_get_info: null");
+    std::memset(info, 0, sizeof(*info));
+    info->nao = h->hp.nao;
+    info->nbas = h->hp.nvshell;
+    info->npairs = h->hp.npairs;
+    info->nprim_pairs = h->hp.npp;
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        info->class_pairs[c] = h->hp.cls[c].pair_end - h->hp.cls[c].pair_begin;
+        info->class_prim_pairs[c] = h->hp.cls[c].pp_end - h->hp.cls[c].pp_begin;
+    }
+    return WB_OK;
+}
+
+int64_t wb_cosx_export_pairs(const wb_cosx* h, int64_t* rows, int64_t cap) {
+    if (!h) return 0;
+    const wb::HostPairs& hp = h->hp;
+    int64_t n = std::min<int64_t>(cap, hp.npairs);
+    for (int64_t k = 0; k < n && rows; ++k) {
+        int64_t* r = rows + 8 * k;
+        r[0] = hp.hdr[4 * k]; r[1] = hp.hdr[4 * k + 1]; r[2] = hp.hdr[4 * k + 2];
+        r[3] = hp.hdr[4 * k + 3]; r[4] = hp.pclass[k]; r[5] = hp.pish[k];
+        r[6] = hp.pjsh[k]; r[7] = hp.pflops[k];
+    }
+    return rows ? n : hp.npairs;
+}
+
+size_t wb_cosx_workspace_bytes(const wb_cosx* h, int64_t npts,
+                               int64_t tile_pts) {
+    if (!h || npts < 0) return 0;
+    int64_t t = tile_pts > 0 ? std::min(round32(tile_pts), round32(npts)) : round32(npts);
+    t = std::max<int64_t>(t, 32);
+    return ws_layout(h, t, true).total;
+}
+
+int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
+                  int64_t npts, const double* qd, double omega,
+                  double tile_tol, int64_t tile_pts, int flags, double* k_out,
+                  void* workspace, size_t workspace_bytes, void* stream,
+                  wb_cosx_stats* stats) {
+    if (!h || !k_out || !qd || npts < 0 || (npts && (!coords || !weights)))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_get_k: bad arguments");
+    if (!(omega >= 0.0) || !(tile_tol >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_get_k: omega and tile_tol must be >= 0");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int nao = h->hp.nao;
+    int64_t tile = tile_pts > 0 ? round32(tile_pts) : round32(std::max<int64_t>(npts, 1));
+    tile = std::max<int64_t>(std::min(tile, round32(std::max<int64_t>(npts, 1))), 32);
+    const WsLayout L = ws_layout(h, tile, true);
+    if (!workspace || workspace_bytes < L.total)
+        return fail(WB_ERR_WORKSPACE, "wb_cosx_get_k: workspace needs " +
+                                          std::to_string(L.total) + " bytes");
+    WB_CUBLAS(cublasSetStream(h->cublas, s));
+    if (flags & WB_K_GEMM_EMULATED_FP64) {
+        WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_FP64_EMULATED_FIXEDPOINT_MATH));
+        WB_CUBLAS(cublasSetEmulationStrategy(h->cublas, CUBLAS_EMULATION_STRATEGY_EAGER));
+    } else {
+        WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+    }
+    WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.counters), 0,
+                            sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+    WB_CUDA(wb::launch_omega(h->hp.npp, h->p, h->pref, omega,
+                             at<float4>(workspace, L.om), s));
+    int launches = 1;
+    if (npts == 0) {
+        WB_CUDA(cudaMemsetAsync(k_out, 0, sizeof(double) * nao * nao, s));
+        return read_stats(h, workspace, L, 0, s, stats, launches);
+    }
+    double* X = at<double>(workspace, L.X);
+    double* F64 = at<double>(workspace, L.F64);
+    float* F32 = at<float>(workspace, L.F32);
+    float* G32 = at<float>(workspace, L.G32);
+    int64_t ntasks = 0;
+    const double one = 1.0, zero = 0.0;
+    for (int64_t i0 = 0; i0 < npts; i0 += tile) {
+        const int64_t nt = std::min(tile, npts - i0);
+        const int64_t ldt = round32(nt);
+        const double* c = coords + 3 * i0;
+        const double* w = weights + i0;
+        wb::AoArgs ao;
+        ao.coords = c; ao.npts = nt; ao.ld = ldt; ao.nbas = h->nbas;
+        ao.sh_l = h->sh_l; ao.sh_np = h->sh_np; ao.sh_nc = h->sh_nc;
+        ao.sh_eoff = h->sh_eoff; ao.sh_coff = h->sh_coff; ao.sh_ao0 = h->sh_ao0;
+        ao.sh_ctr = h->sh_ctr; ao.exps = h->exps; ao.coeffs = h->coeffs; ao.X = X;
+        WB_CUDA(wb::launch_ao_eval(ao, s));
+        // F(g, mu) = sum_l X(g, l) QD(l, mu); QD row-major = col-major QD^T
+        WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)ldt, nao,
+                              nao, &one, X, (int)ldt, qd, nao, &zero, F64,
+                              (int)ldt));
+        WB_CUDA(wb::launch_f64_to_f32(F64, F32, (int64_t)nao * ldt, s));
+        launches += 3;
+        int st = run_g_tile(h, c, w, nt, ldt, F32, G32, tile_tol, workspace, L,
+                            s, &launches);
+        if (st != WB_OK) return st;
+        ntasks += (ldt / 32) * (int64_t)h->hp.npairs;
+        WB_CUDA(wb::launch_weight_g(G32, w, nt, ldt, nao, F64, s));
+        // K(mu, nu) += sum_g X(g, mu) WG(g, nu); written row-major
+        const double* beta = i0 == 0 ? &zero : &one;
+        WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nao, nao,
+                              (int)ldt, &one, F64, (int)ldt, X, (int)ldt, beta,
+                              k_out, nao));
+        launches += 2;
+    }
+    return read_stats(h, workspace, L, ntasks, s, stats, launches);
+}
+
+int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
+              int64_t npts, const float* f, double omega, double tile_tol,
+              float* g_out, void* workspace, size_t workspace_bytes,
+              void* stream, wb_cosx_stats* stats) {
+    if (!h || !f || !g_out || npts <= 0 || !coords || !weights)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_g: bad arguments");
+    if (!(omega >= 0.0) || !(tile_tol >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_g: omega and tile_tol must be >= 0");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t ldt = round32(npts);
+    const WsLayout L = ws_layout(h, ldt, false);
+    if (!workspace || workspace_bytes < L.total)
+        return fail(WB_ERR_WORKSPACE, "wb_cosx_g: workspace needs " +
+                                          std::to_string(L.total) + " bytes");
+    WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.counters), 0,
+                            sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+    WB_CUDA(wb::launch_omega(h->hp.npp, h->p, h->pref, omega,
+                             at<float4>(workspace, L.om), s));
+    int launches = 1;
+    int st = run_g_tile(h, coords, weights, npts, ldt, f, g_out, tile_tol,
+                        workspace, L, s, &launches);
+    if (st != WB_OK) return st;
+    return read_stats(h, workspace, L, (ldt / 32) * (int64_t)h->hp.npairs, s,
+                      stats, launches);
+}
+
+int wb_ao_eval(const wb_cosx* h, const double* coords, int64_t npts,
+               double* x_out, void* stream) {
+    if (!h || !x_out || npts < 0 || (npts && !coords))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_ao_eval: bad arguments");
+    wb::AoArgs ao;
+    ao.coords = coords; ao.npts = npts; ao.ld = round32(npts); ao.nbas = h->nbas;
+    ao.sh_l = h->sh_l; ao.sh_np = h->sh_np; ao.sh_nc = h->sh_nc;
+    ao.sh_eoff = h->sh_eoff; ao.sh_coff = h->sh_coff; ao.sh_ao0 = h->sh_ao0;
+    ao.sh_ctr = h->sh_ctr; ao.exps = h->exps; ao.coeffs = h->coeffs; ao.X = x_out;
+    WB_CUDA(wb::launch_ao_eval(ao, static_cast<cudaStream_t>(stream)));
+    return WB_OK;
+}
+
+int wb_int3c1e_dense(const wb_cosx* h, const double* coords, int64_t npts,
+                     double omega, float* out, void* stream) {
+    if (!h || !out || npts <= 0 || !coords || !(omega >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_int3c1e_dense: bad arguments");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t ldt = round32(npts);
+    const size_t om_bytes = align256(sizeof(float) * 16 * (size_t)std::max(h->hp.npp, 1));
+    const size_t g_bytes = align256(sizeof(float) * 3 * (size_t)ldt);
+    void* tmp = nullptr;
+    WB_CUDA(cudaMallocAsync(&tmp, om_bytes + 2 * g_bytes, s));
+    float4* om = static_cast<float4*>(tmp);
+    float* gh = at<float>(tmp, om_bytes);
+    float* gl = at<float>(tmp, om_bytes + g_bytes);
+    cudaError_t e = wb::launch_omega(h->hp.npp, h->p, h->pref, omega, om, s);
+    if (e == cudaSuccess) e = wb::launch_grid_prep(coords, npts, ldt, gh, gl, s);
+    if (e == cudaSuccess) {
+        e = cudaMemsetAsync(out, 0, sizeof(float) * (size_t)npts * h->hp.nao * h->hp.nao, s);
+    }
+    if (e == cudaSuccess) {
+        wb::CosxArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.ld = ldt; a.npts = (int)npts; a.geo = h->geo; a.om = om;
+        for (int c = 0; c < wb::NCLASS; ++c) {
+            a.Ecls[c] = h->E + h->hp.cls[c].e_base / 4;
+            a.pp_begin[c] = h->hp.cls[c].pp_begin;
+        }
+        a.hdr = h->hdr; a.gxyz_hi = gh; a.gxyz_lo = gl; a.boys = h->boys;
+        e = wb::launch_dense_impl(a, h->hp.npairs, h->pclass, h->pl, h->estride,
+                                  h->hp.nao, out, s);
+    }
+    cudaError_t e2 = cudaFreeAsync(tmp, s);
+    if (e != cudaSuccess) return cuda_fail(e, "wb_int3c1e_dense");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync");
+    return WB_OK;
+}
+
+int wb_boys_fp32(const float* t, int64_t n, int nmax, float* out,
+                 void* stream) {
+    if (nmax < 0 || nmax > 6)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_boys_fp32: nmax must be 0..6");
+    if (n < 0 || (n && (!t || !out)))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_boys_fp32: bad arguments");
+    int dev = 0;
+    WB_CUDA(cudaGetDevice(&dev));
+    float4* tab = nullptr;
+    int st = device_boys(dev, &tab);
+    if (st != WB_OK) return st;
+    WB_CUDA(wb::launch_boys(t, n, nmax, tab, out, static_cast<cudaStream_t>(stream)));
+    return WB_OK;
+}
+
+int wb_vv10_kernel_sum(const float* xyz, const float* q, const float* w0,
+                       const float* kappa, int64_t n, double tile_tol,
+                       double* f_out, double* u_out, double* w_out,
+                       void* stream, int64_t* pairs_kept) {
+    if (n < 0 || !(tile_tol >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_vv10_kernel_sum: bad arguments");
+    if (n && (!xyz || !q || !w0 || !kappa || !f_out || !u_out || !w_out))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_vv10_kernel_sum: null pointer");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (n == 0) {
+        if (pairs_kept) *pairs_kept = 0;
+        return WB_OK;
+    }
+    void* ws = nullptr;
+    WB_CUDA(cudaMallocAsync(&ws, wb::vv10_workspace_bytes(n), s));
+    cudaError_t e = wb::launch_vv10(xyz, q, w0, kappa, n, tile_tol, f_out,
+                                    u_out, w_out, ws, s);
+    unsigned long long kept = 0;
+    if (e == cudaSuccess && pairs_kept)
+        e = cudaMemcpyAsync(&kept, ws, sizeof(kept), cudaMemcpyDeviceToHost, s);
+    cudaError_t e2 = cudaFreeAsync(ws, s);
+    if (e == cudaSuccess && pairs_kept) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "wb_vv10_kernel_sum");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync");
+    if (pairs_kept) *pairs_kept = (int64_t)kept;
+    return WB_OK;
+}
+
+int wb_fp32_fma_probe(int64_t iters, float* out, int64_t out_len,
+                      void* stream, double* flops) {
+    int dev = 0, nsm = 1;
+    WB_CUDA(cudaGetDevice(&dev));
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = 256, blocks = nsm * 8;
+    if (!out || out_len < (int64_t)threads * blocks || iters <= 0)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_fp32_fma_probe: out needs "
+                    + std::to_string((int64_t)threads * blocks) + " floats");
+    WB_CUDA(wb::launch_fma_probe(iters, blocks, threads, out,
+                                 static_cast<cudaStream_t>(stream)));
+    if (flops) *flops = 2.0 * 8.0 * 16.0 * (double)iters * threads * blocks;
+    return WB_OK;
+}
+
+}  // extern "C"

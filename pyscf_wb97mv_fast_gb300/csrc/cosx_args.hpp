@@ -1,0 +1,44 @@
+// Argument block of the fused COSX class kernels (host + device visible).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wb {
+
+constexpr int kClasses = 10;
+
+// Everything one class launch reads.  Per primitive pair m (global index):
+//   geo[2m], geo[2m+1]   P hi (xyz, 0), P lo (xyz, 0)      molecule frame
+//   om[4m .. 4m+3]       tp_hi, tp_lo, c0_hi, c0_lo, ..., c6_hi, c6_lo
+//   Ecls[c] + (m - pp_begin[c]) * stride_c/4   packed Hermite E
+// Per pair k: hdr[k] = (ia0, ib0, pp0, npp | diag << 16), pshell[k] =
+// (virtual shell A, B), ptau[k] = (tau, tau * sum pref).
+struct CosxArgs {
+    const float* F;            // (nao, ld) AO-major, FP32
+    float* G;                  // (nao, ld) AO-major, FP32, accumulated
+    long long ld;              // padded point count (multiple of 32)
+    int npts;                  // valid points
+    int nsub;                  // ld / 32
+    const float4* geo;
+    const float4* om;
+    const float4* Ecls[kClasses];
+    int pp_begin[kClasses];
+    const int4* hdr;
+    const int2* pshell;
+    const float2* ptau;
+    const float4* bnd;         // per pp: P (FP32), p' = 0.75 p
+    const float* bpref;        // per pp: bound prefactor (rounded up)
+    const float4* sub_cr;      // per sub-block: centroid (xyz), radius
+    const float* msh;          // (nsub, nvshell): max_g w_g sum_shell |F|
+    int nvshell;
+    float tol;                 // tile_tol / 1.001, <= 0 keeps every task
+    const float* gxyz_hi;      // (3, ld) SoA grid coordinates, hi
+    const float* gxyz_lo;      // (3, ld) lo
+    const float4* boys;        // Boys table, BOYS_NODES rows of 5 float4
+    const long long* pflops;   // per pair model flops per point
+    const int* pnint;          // per pair nfi * nfj
+    unsigned long long* counters;  // per class: kept, flops, ints (3 each)
+    int* work;                 // per class dynamic sub-block counter
+};
+
+}  // namespace wb

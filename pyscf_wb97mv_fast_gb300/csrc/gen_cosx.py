@@ -1,0 +1,362 @@
+"""Generates csrc/generated/cosx_classes.cuh: one straight-line device
+function per shell-pair class (la >= lb, la <= 3) of the fused COSX kernel.
+
+For one task (shell pair A, B; one grid point g per thread) it computes
+
+    G_B[nu] += sum_mu A^g_{mu nu} F_A[mu]        (always)
+    G_A[mu] += sum_nu A^g_{mu nu} F_B[nu]        (A != B)
+
+without forming A: F is first taken to the Cartesian components of each
+shell (f0 = c2s F_A, h0 = c2s F_B; s/p normalisations are folded into the
+primitive prefactor), then for every primitive pair
+
+    R^{(n)}_000 = c_n F_n(T),  c_n = C_a C_b K_AB 2 pi / p sqrt(theta)
+                                     (-2 p theta)^n          (folded, hi+lo)
+    R_tuv       McMurchie-Davidson recurrence, in place, levels L .. 0
+    Ac[ca, cb]  = sum_t Ex sum_u Ey sum_v Ez R_tuv
+    Y[cb]      += f0[ca] Ac[ca, cb],   X[ca] += Ac[ca, cb] h0[cb]
+
+and finally G_B += c2s^T Y, G_A += c2s^T X.  The recurrence and the
+Hermite sum are the reference's math (pyscf_wb97mv_fast/gpu/sgx_k.py:
+200-307, gpu/shellpairs.py:447-485); the order of contraction (F first,
+no A block, no per-primitive contraction matrices) is this generator's.
+Constants of the d/f spherical transforms are applied as
+fmaf(c_hi, x, c_lo * x) (one rounding of the compensated product,
+gpu/int3c1e.py:17-31).
+
+Run as a script (or import and call ``write()``); ``build()`` of the
+package runs it before compiling.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from pyscf_wb97mv_fast_gb300.basis import cart2sph, cart_components  # noqa
+
+LMAX = 3
+
+
+def class_id(la, lb):
+    return la * (la + 1) // 2 + lb
+
+
+def classes():
+    return [(la, lb) for la in range(LMAX + 1) for lb in range(la + 1)]
+
+
+def e_entries(la, lb):
+    """Packed (i, i', t) per axis, E^{00}_0 excluded (it is 1)."""
+    out = []
+    for i in range(la + 1):
+        for j in range(lb + 1):
+            for t in range(i + j + 1):
+                if i == 0 and j == 0:
+                    continue
+                out.append((i, j, t))
+    return out
+
+
+def e_stride(la, lb):
+    n = 3 * len(e_entries(la, lb))
+    return (n + 3) // 4 * 4
+
+
+def hilo(c):
+    hi = np.float32(c)
+    lo = np.float32(np.float64(c) - np.float64(hi))
+    return hi, lo
+
+
+def flit(x):
+    """C float literal that round-trips exactly."""
+    x = np.float32(x)
+    if x == 0:
+        return '0.0f'
+    return '%.9ef' % float(x)
+
+
+def rname(t, u, v):
+    return 'r_%d_%d_%d' % (t, u, v)
+
+
+def gen_recurrence(L, lines, ind):
+    """In-place R recurrence over levels n = L .. 0 (only t+u+v <= L-n)."""
+    for n in range(L, -1, -1):
+        m = L - n
+        if m >= 1:
+            # t >= 1 entries: for each (u, v), t descending
+            for u in range(m):
+                for v in range(m - u):
+                    for t in range(m - u - v, 0, -1):
+                        if t == 1:
+                            expr = 'dx * %s' % rname(0, u, v)
+                        else:
+                            expr = 'fmaf(dx, %s, %s * %s)' % (
+                                rname(t - 1, u, v), flit(t - 1),
+                                rname(t - 2, u, v))
+                        lines.append('%s%s = %s;' % (ind, rname(t, u, v), expr))
+            # t = 0, u >= 1
+            for v in range(m):
+                for u in range(m - v, 0, -1):
+                    if u == 1:
+                        expr = 'dy * %s' % rname(0, 0, v)
+                    else:
+                        expr = 'fmaf(dy, %s, %s * %s)' % (
+                            rname(0, u - 1, v), flit(u - 1), rname(0, u - 2, v))
+                    lines.append('%s%s = %s;' % (ind, rname(0, u, v), expr))
+            # t = u = 0, v >= 1
+            for v in range(m, 0, -1):
+                if v == 1:
+                    expr = 'dz * %s' % rname(0, 0, 0)
+                else:
+                    expr = 'fmaf(dz, %s, %s * %s)' % (
+                        rname(0, 0, v - 1), flit(v - 1), rname(0, 0, v - 2))
+                lines.append('%s%s = %s;' % (ind, rname(0, 0, v), expr))
+        lines.append('%s%s = R000_%d;' % (ind, rname(0, 0, 0), n))
+
+
+def ename(ax, i, j, t):
+    return 'e%s_%d_%d_%d' % ('xyz'[ax], i, j, t)
+
+
+def gen_hermite(la, lb, ca_c, cb_c, ind, lines, tag):
+    """s = sum_t Ex sum_u Ey sum_v Ez R_tuv for one (ca, cb); returns the
+    variable holding it."""
+    (i, j, k) = ca_c
+    (ip, jp, kp) = cb_c
+    s_terms = []
+    for t in range(i + ip + 1):
+        u_terms = []
+        for u in range(j + jp + 1):
+            # z sum
+            if k == 0 and kp == 0:
+                zexpr = rname(t, u, 0)
+            else:
+                acc = None
+                for v in range(k + kp + 1):
+                    e = ename(2, k, kp, v)
+                    acc = ('%s * %s' % (e, rname(t, u, v)) if acc is None
+                           else 'fmaf(%s, %s, %s)' % (e, rname(t, u, v), acc))
+                zexpr = acc
+            if j == 0 and jp == 0:
+                u_terms.append(zexpr)
+            else:
+                u_terms.append((ename(1, j, jp, u), zexpr))
+        # combine u terms
+        if j == 0 and jp == 0:
+            yexpr = u_terms[0]
+        else:
+            acc = None
+            for (e, z) in u_terms:
+                zv = 'z%s_%d_%d' % (tag, t, len(lines))
+                lines.append('%sconst float %s = %s;' % (ind, zv, z))
+                acc = ('%s * %s' % (e, zv) if acc is None
+                       else 'fmaf(%s, %s, %s)' % (e, zv, acc))
+            yexpr = acc
+        if i == 0 and ip == 0:
+            s_terms.append(yexpr)
+        else:
+            s_terms.append((ename(0, i, ip, t), yexpr))
+    if i == 0 and ip == 0:
+        sexpr = s_terms[0]
+    else:
+        acc = None
+        for (e, y) in s_terms:
+            yv = 'y%s_%d' % (tag, len(lines))
+            lines.append('%sconst float %s = %s;' % (ind, yv, y))
+            acc = ('%s * %s' % (e, yv) if acc is None
+                   else 'fmaf(%s, %s, %s)' % (e, yv, acc))
+        sexpr = acc
+    sv = 's%s' % tag
+    lines.append('%sconst float %s = %s;' % (ind, sv, sexpr))
+    return sv
+
+
+def gen_transform_in(l, src, dst, ind, lines):
+    """dst[c] = sum_mu c2s[c, mu] src[mu] (compensated), l >= 2; identity
+    for l <= 1 (normalisation folded into the prefactor)."""
+    nc = (l + 1) * (l + 2) // 2
+    if l <= 1:
+        for c in range(nc):
+            lines.append('%sconst float %s%d = %s%d;' % (ind, dst, c, src, c))
+        return
+    c2s = cart2sph(l)
+    for c in range(nc):
+        terms = []
+        for mu in range(2 * l + 1):
+            v = c2s[c, mu]
+            if abs(v) < 1e-15:
+                continue
+            hi, lo = hilo(v)
+            terms.append('fmaf(%s, %s%d, %s * %s%d)' % (
+                flit(hi), src, mu, flit(lo), src, mu))
+        expr = ' + '.join(terms) if terms else '0.0f'
+        lines.append('%sconst float %s%d = %s;' % (ind, dst, c, expr))
+
+
+def gen_transform_out(l, src, dst, ind, lines):
+    """dst[mu] = sum_c c2s[c, mu] src[c] (compensated), l >= 2."""
+    if l <= 1:
+        for c in range(2 * l + 1):
+            lines.append('%sconst float %s%d = %s%d;' % (ind, dst, c, src, c))
+        return
+    c2s = cart2sph(l)
+    nc = (l + 1) * (l + 2) // 2
+    for mu in range(2 * l + 1):
+        terms = []
+        for c in range(nc):
+            v = c2s[c, mu]
+            if abs(v) < 1e-15:
+                continue
+            hi, lo = hilo(v)
+            terms.append('fmaf(%s, %s%d, %s * %s%d)' % (
+                flit(hi), src, c, flit(lo), src, c))
+        expr = ' + '.join(terms) if terms else '0.0f'
+        lines.append('%sconst float %s%d = %s;' % (ind, dst, mu, expr))
+
+
+def gen_class(la, lb, diag):
+    L = la + lb
+    na, nb = 2 * la + 1, 2 * lb + 1
+    ca = cart_components(la)
+    cb = cart_components(lb)
+    ents = e_entries(la, lb)
+    est = e_stride(la, lb)
+    lines = []
+    I = '    '
+    lines.append('template<> __device__ __forceinline__ void cosx_task<%d, %d, %s>('
+                 % (la, lb, 'true' if diag else 'false'))
+    lines.append('    const CosxArgs& A, const int4 hdr, const long long g,')
+    lines.append('    const float gxh, const float gyh, const float gzh,')
+    lines.append('    const float gxl, const float gyl, const float gzl,')
+    lines.append('    const float4* __restrict__ stab)')
+    lines.append('{')
+    lines.append(I + 'const long long ld = A.ld;')
+    lines.append(I + 'const float* __restrict__ Fp = A.F;')
+    lines.append(I + 'const int ia0 = hdr.x, ib0 = hdr.y, pp0 = hdr.z;')
+    lines.append(I + 'const int npp = hdr.w & 0xffff;')
+    # F loads
+    for mu in range(na):
+        lines.append(I + 'const float fa%d = Fp[(long long)(ia0 + %d) * ld + g];'
+                     % (mu, mu))
+    gen_transform_in(la, 'fa', 'f0_', I, lines)
+    if not diag:
+        for nu in range(nb):
+            lines.append(I + 'const float fb%d = Fp[(long long)(ib0 + %d) * ld + g];'
+                         % (nu, nu))
+        gen_transform_in(lb, 'fb', 'h0_', I, lines)
+    for c in range(len(cb)):
+        lines.append(I + 'float Y%d = 0.0f;' % c)
+    if not diag:
+        for c in range(len(ca)):
+            lines.append(I + 'float X%d = 0.0f;' % c)
+    # R variables
+    tuv = [(t, u, v) for t in range(L + 1) for u in range(L + 1 - t)
+           for v in range(L + 1 - t - u)]
+    lines.append(I + 'const float4* __restrict__ geo = A.geo;')
+    lines.append(I + 'const float4* __restrict__ om = A.om;')
+    if ents:
+        lines.append(I + 'const float4* __restrict__ Eb = A.Ecls[%d];' % class_id(la, lb))
+        lines.append(I + 'const int ppb = A.pp_begin[%d];' % class_id(la, lb))
+    lines.append(I + '#pragma unroll 1')
+    lines.append(I + 'for (int m = pp0; m < pp0 + npp; ++m) {')
+    J = I * 2
+    lines.append(J + 'const float4 ph = __ldg(geo + 2 * m);')
+    lines.append(J + 'const float4 pl = __ldg(geo + 2 * m + 1);')
+    lines.append(J + 'const float dx = (ph.x - gxh) + (pl.x - gxl);')
+    lines.append(J + 'const float dy = (ph.y - gyh) + (pl.y - gyl);')
+    lines.append(J + 'const float dz = (ph.z - gzh) + (pl.z - gzl);')
+    lines.append(J + 'const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));')
+    nom = 1 + (L + 1) // 2
+    for q in range(nom):
+        lines.append(J + 'const float4 o%d = __ldg(om + 4 * (long long)m + %d);' % (q, q))
+    lines.append(J + 'const float T = fmaf(o0.x, r2, o0.y * r2);')
+    lines.append(J + 'float Fb[%d];' % (L + 1))
+    lines.append(J + 'boys_fp32<%d>(T, Fb, stab);' % L)
+    # c_n hi/lo: record floats [tp_hi, tp_lo, c0h, c0l, c1h, c1l, ...]
+    comp = 'xyzw'
+    for n in range(L + 1):
+        fh = 2 + 2 * n
+        fl = fh + 1
+        ch = 'o%d.%s' % (fh // 4, comp[fh % 4])
+        cl = 'o%d.%s' % (fl // 4, comp[fl % 4])
+        lines.append(J + 'const float R000_%d = fmaf(%s, Fb[%d], %s * Fb[%d]);'
+                     % (n, ch, n, cl, n))
+    lines.append(J + 'float ' + ', '.join(rname(*x) for x in tuv) + ';')
+    gen_recurrence(L, lines, J)
+    # E loads
+    if ents:
+        nvec = est // 4
+        lines.append(J + 'const float4* __restrict__ Em = Eb + (long long)(m - ppb) * %d;' % nvec)
+        flat = []
+        for ax in range(3):
+            for (i, j, t) in ents:
+                flat.append(ename(ax, i, j, t))
+        while len(flat) % 4:
+            flat.append(None)
+        for q in range(nvec):
+            lines.append(J + 'const float4 ev%d = __ldg(Em + %d);' % (q, q))
+            for c in range(4):
+                nm = flat[4 * q + c]
+                if nm is not None:
+                    lines.append(J + 'const float %s = ev%d.%s;' % (nm, q, comp[c]))
+    # Hermite sums and accumulation
+    for ia, cac in enumerate(ca):
+        for ib, cbc in enumerate(cb):
+            tag = '%d_%d' % (ia, ib)
+            sv = gen_hermite(la, lb, cac, cbc, J, lines, tag)
+            lines.append(J + 'Y%d = fmaf(f0_%d, %s, Y%d);' % (ib, ia, sv, ib))
+            if not diag:
+                lines.append(J + 'X%d = fmaf(%s, h0_%d, X%d);' % (ia, sv, ib, ia))
+    lines.append(I + '}')
+    # outputs
+    gen_transform_out(lb, 'Y', 'gb', I, lines)
+    lines.append(I + 'float* __restrict__ Gp = A.G;')
+    for nu in range(nb):
+        lines.append(I + 'Gp[(long long)(ib0 + %d) * ld + g] += gb%d;' % (nu, nu))
+    if not diag:
+        gen_transform_out(la, 'X', 'ga', I, lines)
+        for mu in range(na):
+            lines.append(I + 'Gp[(long long)(ia0 + %d) * ld + g] += ga%d;' % (mu, mu))
+    lines.append('}')
+    return '\n'.join(lines)
+
+
+def source():
+    out = ['// Generated by csrc/gen_cosx.py -- do not edit by hand.',
+           '// One straight-line task body per shell-pair class (la >= lb).',
+           '#pragma once', '']
+    for (la, lb) in classes():
+        out.append(gen_class(la, lb, False))
+        out.append('')
+        if la == lb:
+            out.append(gen_class(la, lb, True))
+            out.append('')
+    # E strides table for the host
+    out.append('#define WB_E_STRIDES {%s}' % ', '.join(
+        str(e_stride(la, lb)) for (la, lb) in classes()))
+    out.append('')
+    return '\n'.join(out)
+
+
+def write(path=None):
+    if path is None:
+        path = os.path.join(HERE, 'generated', 'cosx_classes.cuh')
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    src = source()
+    old = None
+    if os.path.exists(path):
+        with open(path) as fh:
+            old = fh.read()
+    if old != src:
+        with open(path, 'w') as fh:
+            fh.write(src)
+    return path
+
+
+if __name__ == '__main__':
+    print(write())

@@ -1,0 +1,86 @@
+// Host-side (FP64) preprocessing of the COSX path: basis, shell pairs,
+// Boys table, Becke weights.  Internal header of libwb97mv_gb300.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "wb97mv_gb300.h"
+
+namespace wb {
+
+constexpr int LMAX = 3;
+constexpr int NCLASS = 10;          // (la >= lb) classes, la, lb <= 3
+constexpr int BOYS_NODES = 145;     // T_k = k / 4, k = 0..144 (T < 36)
+constexpr int BOYS_ROW = 20;        // floats per table row (kernel layout)
+constexpr int OMEGA_REC = 16;       // floats per primitive pair per omega
+constexpr int NIA_MAX = 16;         // functions per shell (reference cap)
+constexpr int PPR_MAX = 16;         // primitives per shell (reference cap)
+
+inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+inline int nsph(int l) { return 2 * l + 1; }
+inline int class_of(int la, int lb) { return la * (la + 1) / 2 + lb; }
+// packed Hermite coefficients per axis for a (la >= lb) class, E^{00}_0 = 1
+// excluded: sum_{i<=la, i'<=lb} (i + i' + 1) - 1
+int e_count_axis(int la, int lb);
+// floats of E per primitive pair (3 axes, padded to a multiple of 4)
+int e_stride(int la, int lb);
+
+void cart_components(int l, std::vector<int>& ix, std::vector<int>& iy,
+                     std::vector<int>& iz);
+// (ncart, nsph) row-major real-solid-harmonic transform, unit-sphere norm
+std::vector<double> cart2sph(int l);
+// max over spherical columns of sum_cart |c2s| (screening tau per shell)
+double c2s_tau(int l);
+
+// FP64 Boys F_0..F_nmax at T (series + downward recursion below T = 40,
+// F_0 from erf plus upward recursion above)
+void boys_f64(int nmax, double t, double* out);
+// kernel table: BOYS_NODES rows of BOYS_ROW floats
+std::vector<float> boys_table();
+
+struct VShell {                     // one contraction column of one shell
+    int phys, ci, atom, l, nprim, ao0;
+    double A[3];                    // centre relative to the origin
+    std::vector<double> exps, coef;
+    double cmax;                    // max |coef|
+};
+
+struct ClassRange {
+    int pair_begin = 0, pair_end = 0;
+    int pp_begin = 0, pp_end = 0;
+    int64_t e_base = 0;             // float offset of the class's E block
+};
+
+struct HostPairs {
+    int nao = 0, nbas_phys = 0, nvshell = 0, npairs = 0, npp = 0;
+    std::vector<VShell> vsh;
+    // per pair (device order: sorted by class)
+    std::vector<int32_t> hdr;       // 4 per pair: ia0, ib0, pp0, npp|diag<<16
+    std::vector<int32_t> pshell;    // 2 per pair: vshell A, vshell B
+    std::vector<float> ptau;        // 2 per pair: tau, tau * sum(pref)
+    std::vector<int32_t> pclass, pish, pjsh;
+    std::vector<int64_t> pflops;    // model flops per grid point
+    std::vector<int32_t> pnint;     // nfi * nfj
+    // per primitive pair
+    std::vector<float> geo;         // 8 per pp: P hi (3), 0, P lo (3), 0
+    std::vector<double> p, pref;    // exponent sum, folded prefactor
+    std::vector<float> bnd;         // 4 per pp: P (3), p' = 0.75 p
+    std::vector<float> bpref;       // bound prefactor, rounded up
+    std::vector<float> E;           // per class blocks, e_stride per pp
+    ClassRange cls[NCLASS];
+    // per virtual shell (for the sub-block statistics)
+    std::vector<int32_t> vs_ao0, vs_nf;
+};
+
+// Builds the pair tables; returns WB_OK or an error code with `err` set.
+int build_pairs(const wb_basis& b, const double origin[3], double cutoff,
+                HostPairs& out, std::string& err);
+
+// FLOP model of one (bra ish, ket jsh) task per grid point.
+int64_t model_flops(int la, int lb, int npi, int npj, bool diag);
+
+void becke_partition(const double* pts, int64_t n, const int* owner,
+                     const double* atoms, int natm, double* out);
+
+}  // namespace wb

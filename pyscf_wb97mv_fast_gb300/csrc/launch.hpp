@@ -1,0 +1,63 @@
+// Kernel launchers shared between the CUDA translation units and the C ABI.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "cosx_args.hpp"
+
+namespace wb {
+
+// per-class fused screen + G kernels (cosx_kernels_*.cu)
+cudaError_t launch_cosx_class_range(int cls, const CosxArgs& a, int pb,
+                                    int pe, int grid, cudaStream_t s);
+// max resident CTAs per SM of a class kernel (128 threads each)
+int cosx_class_blocks_per_sm(int cls);
+
+struct AoArgs {
+    const double* coords;       // (npts, 3) molecule frame
+    int64_t npts, ld;
+    int nbas;
+    const int* sh_l;
+    const int* sh_np;
+    const int* sh_nc;
+    const int* sh_eoff;
+    const int* sh_coff;
+    const int* sh_ao0;
+    const double* sh_ctr;       // (nbas, 3)
+    const double* exps;
+    const double* coeffs;
+    double* X;                  // (nao, ld)
+};
+
+cudaError_t launch_ao_eval(const AoArgs& a, cudaStream_t s);
+cudaError_t upload_c2s_tables(const double* t0, const double* t1,
+                              const double* t2, const double* t3);
+cudaError_t upload_c2s_f(const float* all /* 4 x 70 */);
+
+cudaError_t launch_omega(int npp, const double* p, const double* pref,
+                         double omega, float4* om, cudaStream_t s);
+cudaError_t launch_grid_prep(const double* coords, int64_t npts, int64_t ld,
+                             float* hi, float* lo, cudaStream_t s);
+cudaError_t launch_sub_stats(const double* coords, const double* weights,
+                             const float* F, int64_t npts, int64_t ld,
+                             int nvshell, const int* vs_ao0, const int* vs_nf,
+                             float4* sub_cr, float* msh, cudaStream_t s);
+cudaError_t launch_f64_to_f32(const double* in, float* out, int64_t n,
+                              cudaStream_t s);
+cudaError_t launch_weight_g(const float* G, const double* w, int64_t npts,
+                            int64_t ld, int nao, double* out, cudaStream_t s);
+cudaError_t launch_dense_impl(const CosxArgs& a, int npairs, const int* pclass,
+                              const int* pl, const int* estride, int nao,
+                              float* out, cudaStream_t s);
+cudaError_t launch_boys(const float* t, int64_t n, int nmax,
+                        const float4* tab, float* out, cudaStream_t s);
+// VV10 double sum; ws must hold vv10_workspace_bytes(n) bytes
+size_t vv10_workspace_bytes(int64_t n);
+cudaError_t launch_fma_probe(int64_t iters, int blocks, int threads,
+                             float* out, cudaStream_t s);
+cudaError_t launch_vv10(const float* xyz, const float* q, const float* w0,
+                        const float* kap, int64_t n, double tile_tol,
+                        double* F, double* U, double* W, void* ws,
+                        cudaStream_t s);
+
+}  // namespace wb

@@ -1,0 +1,188 @@
+// VV10 non-local correlation double sum (reference: gpu/vv10.py:47-98,
+// :128-164, :167-240; formula of libdft VXC_vv10nlc).
+//
+//   g_ij = R^2 w0_i + k_i,  gp_ij = R^2 w0_j + k_j,  gt = g + gp
+//   T  = q_j / (g gp gt),   Tu = T (1/g + 1/gt),   Tw = Tu R^2
+//   F_i = -1.5 sum_j T,  U_i = sum_j Tu,  W_i = sum_j Tw
+//
+// One thread per outer point, inner points staged through shared memory in
+// 256-point tiles.  Inside a tile the three sums are FP32 with Kahan
+// compensation, across tiles they accumulate in FP64 in a fixed order: no
+// atomics, bitwise reproducible.  One reciprocal per pair:
+// inv = 1 / (g gp gt), T = q inv, Tu = T gp (g + gt) inv.
+//
+// Distance pruning on the device: per 256-point tile the centroid, radius,
+// sum q, min w0 and min kappa (FP64); a (block, tile) pair is skipped when
+// the reference's bounds (gpu/vv10.py:21-31)
+//   F <= sum_J q / (g gp (g + gp)),  U <= 2 F / g_min,  W <= U Rmax^2
+// with g, gp at the minimum distance are all below tile_tol; tile_tol = 0
+// keeps every pair.
+#include <cmath>
+
+#include "launch.hpp"
+
+namespace wb {
+
+constexpr int kVvTile = 256;
+
+struct VvTileStats {
+    double cx, cy, cz, rad, qsum, w0min, kmin, pad;
+};
+
+size_t vv10_workspace_bytes(int64_t n) {
+    const int64_t nt = (n + kVvTile - 1) / kVvTile;
+    return (size_t)nt * sizeof(VvTileStats) + 256;
+}
+
+__global__ void vv10_tile_stats_kernel(const float* __restrict__ xyz,
+                                       const float* __restrict__ q,
+                                       const float* __restrict__ w0,
+                                       const float* __restrict__ kap,
+                                       int64_t n, VvTileStats* __restrict__ st) {
+    // one warp per tile
+    const int64_t tile = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int64_t nt = (n + kVvTile - 1) / kVvTile;
+    if (tile >= nt) return;
+    const int64_t i0 = tile * kVvTile;
+    const int64_t i1 = min(n, i0 + kVvTile);
+    double sx = 0, sy = 0, sz = 0, sq = 0, mw = INFINITY, mk = INFINITY;
+    for (int64_t i = i0 + lane; i < i1; i += 32) {
+        sx += xyz[3 * i]; sy += xyz[3 * i + 1]; sz += xyz[3 * i + 2];
+        sq += q[i];
+        mw = fmin(mw, (double)w0[i]);
+        mk = fmin(mk, (double)kap[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        sz += __shfl_xor_sync(0xffffffffu, sz, o);
+        sq += __shfl_xor_sync(0xffffffffu, sq, o);
+        mw = fmin(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+        mk = fmin(mk, __shfl_xor_sync(0xffffffffu, mk, o));
+    }
+    const double cnt = (double)(i1 - i0);
+    const double cx = sx / cnt, cy = sy / cnt, cz = sz / cnt;
+    double r = 0.0;
+    for (int64_t i = i0 + lane; i < i1; i += 32) {
+        const double dx = xyz[3 * i] - cx, dy = xyz[3 * i + 1] - cy,
+                     dz = xyz[3 * i + 2] - cz;
+        r = fmax(r, sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    for (int o = 16; o > 0; o >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, o));
+    if (lane == 0) {
+        VvTileStats s;
+        s.cx = cx; s.cy = cy; s.cz = cz; s.rad = r * (1.0 + 1e-12) + 1e-12;
+        s.qsum = sq; s.w0min = mw; s.kmin = mk; s.pad = 0.0;
+        st[tile] = s;
+    }
+}
+
+__device__ __forceinline__ bool vv10_keep(const VvTileStats& a,
+                                          const VvTileStats& b, double tol) {
+    if (tol <= 0.0) return true;
+    const double dx = a.cx - b.cx, dy = a.cy - b.cy, dz = a.cz - b.cz;
+    const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+    const double rmin = fmax(dist - a.rad - b.rad, 0.0);
+    const double rmax = dist + a.rad + b.rad;
+    const double gmin = rmin * rmin * a.w0min + a.kmin;
+    const double gpmin = rmin * rmin * b.w0min + b.kmin;
+    const double bf = b.qsum / (gmin * gpmin * (gmin + gpmin));
+    const double bu = bf * 2.0 / gmin;
+    const double bw = bu * rmax * rmax;
+    return fmax(fmax(bf, bu), bw) >= tol;
+}
+
+__global__ void __launch_bounds__(kVvTile)
+vv10_sum_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
+                const float* __restrict__ w0, const float* __restrict__ kap,
+                int64_t n, double tol, const VvTileStats* __restrict__ st,
+                double* __restrict__ F, double* __restrict__ U,
+                double* __restrict__ W, unsigned long long* __restrict__ kept) {
+    __shared__ float4 sp[kVvTile];      // x, y, z, q
+    __shared__ float2 sk[kVvTile];      // w0, kappa
+    __shared__ int s_keep[2];           // parity double buffer
+    const int64_t i = (int64_t)blockIdx.x * kVvTile + threadIdx.x;
+    const bool active = i < n;
+    float xi = 0.f, yi = 0.f, zi = 0.f, w0i = 0.f, ki = 1.f;
+    if (active) {
+        xi = xyz[3 * i]; yi = xyz[3 * i + 1]; zi = xyz[3 * i + 2];
+        w0i = w0[i]; ki = kap[i];
+    }
+    const int64_t nt = (n + kVvTile - 1) / kVvTile;
+    double f64 = 0.0, u64 = 0.0, w64 = 0.0;
+    unsigned long long nkept = 0;
+    for (int64_t jt = 0; jt < nt; ++jt) {
+        if (threadIdx.x == 0)
+            s_keep[jt & 1] = vv10_keep(st[blockIdx.x], st[jt], tol);
+        const int64_t j = jt * kVvTile + threadIdx.x;
+        __syncthreads();
+        if (!s_keep[jt & 1]) continue;  // uniform across the block
+        if (j < n) {
+            sp[threadIdx.x] = make_float4(xyz[3 * j], xyz[3 * j + 1],
+                                          xyz[3 * j + 2], q[j]);
+            sk[threadIdx.x] = make_float2(w0[j], kap[j]);
+        }
+        __syncthreads();
+        const int m = (int)min((int64_t)kVvTile, n - jt * kVvTile);
+        if (active) {
+            float fs = 0.f, fc = 0.f, us = 0.f, uc = 0.f, ws = 0.f, wc = 0.f;
+            for (int t = 0; t < m; ++t) {
+                const float4 pj = sp[t];
+                const float2 kj = sk[t];
+                const float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                const float g = fmaf(r2, w0i, ki);
+                const float gp = fmaf(r2, kj.x, kj.y);
+                const float gt = g + gp;
+                const float inv = __frcp_rn(g * gp * gt);
+                const float T = pj.w * inv;
+                const float Tu = T * (gp * (g + gt)) * inv;
+                const float Tw = Tu * r2;
+                float y, s;
+                y = T - fc;  s = fs + y; fc = (s - fs) - y; fs = s;
+                y = Tu - uc; s = us + y; uc = (s - us) - y; us = s;
+                y = Tw - wc; s = ws + y; wc = (s - ws) - y; ws = s;
+            }
+            f64 += (double)fs; u64 += (double)us; w64 += (double)ws;
+            nkept += (unsigned long long)m;
+        }
+        __syncthreads();
+    }
+    if (active) { F[i] = -1.5 * f64; U[i] = u64; W[i] = w64; }
+    if (kept) {
+        // block total of kept pairs (deterministic integer sum)
+        __shared__ unsigned long long red[kVvTile / 32];
+        unsigned long long v = nkept;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long t = 0;
+            for (int w = 0; w < kVvTile / 32; ++w) t += red[w];
+            atomicAdd(kept, t);
+        }
+    }
+}
+
+cudaError_t launch_vv10(const float* xyz, const float* q, const float* w0,
+                        const float* kap, int64_t n, double tile_tol,
+                        double* F, double* U, double* W, void* ws,
+                        cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t nt = (n + kVvTile - 1) / kVvTile;
+    char* base = (char*)ws;
+    unsigned long long* kept = (unsigned long long*)base;
+    VvTileStats* st = (VvTileStats*)(base + 256);
+    cudaError_t e = cudaMemsetAsync(kept, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    vv10_tile_stats_kernel<<<(unsigned)((nt * 32 + 127) / 128), 128, 0, s>>>(
+        xyz, q, w0, kap, n, st);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    vv10_sum_kernel<<<(unsigned)nt, kVvTile, 0, s>>>(xyz, q, w0, kap, n,
+                                                     tile_tol, st, F, U, W,
+                                                     kept);
+    return cudaGetLastError();
+}
+
+}  // namespace wb

@@ -1,0 +1,138 @@
+"""Install the GPU COSX path into a PySCF SCF object (reference:
+pyscf_wb97mv_fast/gpu/install.py:209-336).
+
+    hooks = install_gpu(mf, k=True)       # mf = dft.RKS(mol, xc='wb97m-v').COSX(pjs=True)
+    try:
+        e = mf.kernel()
+    finally:
+        hooks.restore_all()
+
+k=True replaces the module function ``pyscf.sgx.sgx_jk.get_k_only`` with a
+dispatcher: the SGX objects of this mf (``mf.with_df`` and the long-range
+copies in ``mf.with_df._rsh_df``) go to ``GpuKBuilder`` (FP32 fused
+kernels, screened with k_tile_tol, FP64 GEMMs); every other SGX object keeps
+the original.  ``vv10=True`` (default) replaces ``mf._numint.nr_nlc_vxc`` by
+the GPU VV10 flow.
+
+Deliberate contract change: no CPU fallback.  An error in a GPU flow of
+this mf propagates (Unsupported, NativeError, DeviceOutOfMemory) -- after
+the out-of-memory retry, which halves the grid tile twice like the
+reference's _run_with_oom_retry (:99-109).  Importing this module does not
+import PySCF; ``install_gpu`` does.
+"""
+import warnings
+
+from pyscf_wb97mv_fast_gb300.core.hooks import HookSet
+from pyscf_wb97mv_fast_gb300.gpu import sgx_k as sgx_k_mod
+
+DEFAULT_MEM_FRACTION = sgx_k_mod.DEFAULT_MEM_FRACTION
+
+
+def is_oom(exc):
+    """True when an exception is an out-of-memory condition."""
+    if isinstance(exc, MemoryError):
+        return True
+    text = str(exc).lower()
+    return 'out of memory' in text or 'cublas_status_alloc_failed' in text
+
+
+def _run_with_oom_retry(flow, builder):
+    """Run flow(builder); on out-of-memory halve the grid tile and retry,
+    twice, then re-raise."""
+    last = None
+    b = builder
+    for _ in range(3):
+        try:
+            return flow(b)
+        except Exception as exc:                       # noqa: BLE001
+            if not is_oom(exc):
+                raise
+            last = exc
+            cur = b.blksize or getattr(b, 'last_tile', None) or (1 << 20)
+            b = builder.with_blksize(max(32, int(cur) // 2))
+    raise last
+
+
+def _sgx_jk_module():
+    import pyscf.sgx.sgx_jk as mod
+    return mod
+
+
+def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
+                functional_factory=None, verify_ao=True,
+                gemm_dtype='float64', dtype='float32',
+                mem_fraction=DEFAULT_MEM_FRACTION, overlap=False,
+                semilocal=False, k=True, k_tile_tol=1e-11,
+                openblas_threads=None, vv10=True, k_gemm='native',
+                sgx_jk_module=None):
+    """Hook the GPU COSX K (and VV10) into mf; returns a HookSet.
+
+    The keyword names follow the reference; backend must be None or
+    'cuda' (there is one backend).  semilocal=True is not part of this
+    build and raises.  sgx_jk_module lets tests pass a stand-in for
+    pyscf.sgx.sgx_jk.
+    """
+    if backend not in (None, 'cuda', 'cupy'):
+        raise ValueError("backend must be None or 'cuda'")
+    if semilocal:
+        raise NotImplementedError(
+            'the semilocal XC hook (nr_rks) is not part of this build; '
+            'install with semilocal=False (stock PySCF keeps nr_rks)')
+    hooks = HookSet()
+    hooks.k_stats = []
+    hooks.timings = []
+    if k:
+        mod = sgx_jk_module if sgx_jk_module is not None else _sgx_jk_module()
+        holder = {}
+
+        def k_factory(orig):
+            def get_k_only(sgx, dm, hermi=1, direct_scf_tol=1e-13):
+                df = mf.with_df
+                rsh = getattr(df, '_rsh_df', None) or {}
+                if not (sgx is df or any(sgx is v for v in rsh.values()
+                                         if v is not None)):
+                    return orig(sgx, dm, hermi, direct_scf_tol)
+                b = holder.get('builder')
+                if b is None:
+                    b = sgx_k_mod.GpuKBuilder(mf.mol, tile_tol=k_tile_tol,
+                                              blksize=blksize, gemm=k_gemm)
+                    b._build()
+                    torch = sgx_k_mod._torch()
+                    free, _ = torch.cuda.mem_get_info(b.engine.device)
+                    b.mem_budget = int(free * mem_fraction)
+                    holder['builder'] = b
+                stats = {}
+
+                def flow(bb):
+                    kk = sgx_k_mod.get_k_only_gpu(bb, sgx, dm, hermi=hermi,
+                                                  direct_scf_tol=direct_scf_tol)
+                    stats.update(bb.last_stats)
+                    return kk
+                kk = _run_with_oom_retry(flow, b)
+                hooks.k_stats.append(dict(stats))
+                return kk
+            return get_k_only
+
+        hooks.wrap(mod, 'get_k_only', k_factory)
+    if vv10:
+        ni = getattr(mf, '_numint', None)
+        if ni is None:
+            raise TypeError('mf has no _numint; not a DFT object?')
+        from pyscf_wb97mv_fast_gb300.gpu import vv10 as vv10_mod
+        ctx = vv10_mod.Vv10Context(mf.mol, tile_tol=vv10_tile_tol)
+
+        def nlc_factory(orig):
+            def nr_nlc_vxc(mol, grids, xc_code, dm, relativity=0, hermi=1,
+                           max_memory=2000, verbose=None):
+                return vv10_mod.gpu_nr_nlc_vxc(ctx, ni, mol, grids, xc_code, dm,
+                                               relativity, hermi, max_memory,
+                                               verbose)
+            return nr_nlc_vxc
+        hooks.wrap(ni, 'nr_nlc_vxc', nlc_factory)
+    if overlap:
+        warnings.warn('overlap=True has no effect: the XC flows are not '
+                      'hooked in this build', RuntimeWarning)
+    return hooks
+
+
+install = install_gpu

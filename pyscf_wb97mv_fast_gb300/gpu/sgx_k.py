@@ -1,0 +1,223 @@
+"""GPU COSX exchange K behind the reference's builder interface.
+
+``GpuKBuilder`` and ``get_k_only_gpu`` keep the names, arguments and
+results of the reference (pyscf_wb97mv_fast/gpu/sgx_k.py:545-991): one
+builder per molecule, ``get_k(sgx, dm, omega, hermi, direct_scf_tol)``
+returns K (nao, nao) FP64 on the host for one RKS density matrix, with
+``proj`` / ``sym`` read from the SGX object exactly as
+``sgx_jk.get_k_only`` sets them up, and ``last_stats`` describing the call.
+
+What runs underneath is the native library: one ``wb_cosx_get_k`` call per
+K build does AO evaluation, F = fl32(X proj dm), the fused screen + G
+kernels and K = X^T (w o G) on the device; the proj^T K and (K + K^T)/2
+post-processing run on the device too, in FP64.
+
+Contract changes (deliberate): there is no CPU fallback.  Inputs outside
+the supported scope raise ``Unsupported`` (hermi != 1, several or
+asymmetric density matrices, l > 3, ...); device failures raise
+``NativeError`` / ``DeviceOutOfMemory``.  The install hook never calls the
+CPU original for an mf it owns.
+"""
+import os
+import time
+
+import numpy as np
+
+from pyscf_wb97mv_fast_gb300 import _native
+from pyscf_wb97mv_fast_gb300.cosx import KSUB, CosxEngine, as_molecule
+
+Unsupported = _native.Unsupported
+
+LMAX = 3
+_STATE_CACHE = 4           # grid states kept (full + LR copies alternate)
+_BYTES_PER_POINT_NAO = 24  # workspace per point and AO: X64, F64/WG64, F, G
+DEFAULT_MEM_FRACTION = 0.6
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class _GridState:
+    """Device copies of one grids object's coordinates (kernel frame) and
+    weights, plus the tile size (points per native call)."""
+
+    def __init__(self, builder, grids):
+        torch = _torch()
+        coords = np.asarray(grids.coords, dtype=np.float64)
+        weights = np.asarray(grids.weights, dtype=np.float64)
+        self.ngrids = coords.shape[0]
+        eng = builder.engine
+        self.coords = eng.relative(coords)
+        self.weights = torch.as_tensor(weights, dtype=torch.float64,
+                                       device=eng.device).contiguous()
+        self.grids_id = id(grids)
+
+
+class GpuKBuilder:
+    """Per-molecule COSX K builder on one CUDA device (reference:
+    GpuKBuilder, gpu/sgx_k.py:545-851).
+
+    tile_tol: screening threshold (1e-11 default, 0 keeps every task).
+    blksize: grid points per native call (None: as many as the memory
+    budget allows; the reference tiles by SMs x 32 warps x 32 points
+    because its target cards have 8-24 GB).
+    gemm: 'native' (cuBLAS DGEMM) or 'emulated' (cuBLAS FP64 emulation).
+    """
+
+    def __init__(self, mol, device=None, tile_tol=1e-11, mem_budget=None,
+                 origin=None, blksize=None, gemm='native'):
+        self.mol = mol
+        self.tile_tol = float(tile_tol)
+        self.origin = origin
+        self.device = device
+        self.mem_budget = mem_budget
+        self.blksize = None if blksize is None else int(blksize)
+        if gemm not in ('native', 'emulated'):
+            raise ValueError("gemm must be 'native' or 'emulated'")
+        self.gemm = gemm
+        self.engine = None
+        self._grids_states = {}
+        self.last_stats = {}
+        self._built = False
+
+    def _build(self):
+        if self._built:
+            return
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise _native.NativeError(_native.WB_ERR_NO_DEVICE,
+                                      'GpuKBuilder needs a CUDA device')
+        self.engine = CosxEngine(as_molecule(self.mol), origin=self.origin,
+                                 device=self.device)
+        self.nao = self.engine.nao
+        if self.mem_budget is None:
+            free, _ = torch.cuda.mem_get_info(self.engine.device)
+            self.mem_budget = int(free * DEFAULT_MEM_FRACTION)
+        self._built = True
+
+    def with_blksize(self, blksize):
+        """Clone sharing every cache; only the tile size changes (the OOM
+        lever, halved by install._run_with_oom_retry)."""
+        self._build()
+        clone = GpuKBuilder.__new__(GpuKBuilder)
+        clone.__dict__.update(self.__dict__)
+        clone.blksize = int(blksize)
+        return clone
+
+    def _tile(self, npts):
+        """Points per native call (0 = all of them in one tile)."""
+        if self.blksize is not None:
+            t = max(KSUB, self.blksize // KSUB * KSUB)
+        else:
+            per_pt = _BYTES_PER_POINT_NAO * max(self.nao, 1) + 64
+            t = max(KSUB, int(self.mem_budget // per_pt) // KSUB * KSUB)
+        self.last_tile = min(t, max(KSUB, npts))
+        return 0 if t >= npts else t
+
+    def _grid_state(self, grids):
+        key = (id(grids), int(np.asarray(grids.weights).size))
+        st = self._grids_states.get(key)
+        if st is None:
+            st = _GridState(self, grids)
+            self._grids_states[key] = st
+            while len(self._grids_states) > _STATE_CACHE:
+                self._grids_states.pop(next(iter(self._grids_states)))
+        return st
+
+    def get_k(self, sgx, dm, omega, hermi=1, direct_scf_tol=1e-13):
+        """K (nao, nao) FP64 host for one RKS density matrix on sgx's grid."""
+        t0 = time.perf_counter()
+        torch = _torch()
+        if hermi != 1:
+            raise Unsupported(_native.WB_ERR_UNSUPPORTED,
+                              'GPU COSX K supports hermi=1 only')
+        dm = np.asarray(dm)
+        if dm.ndim != 2 or dm.shape[0] != dm.shape[1]:
+            raise Unsupported(_native.WB_ERR_UNSUPPORTED,
+                              'GPU COSX K supports a single square density matrix')
+        if not np.allclose(dm, dm.T, rtol=0, atol=1e-12):
+            raise Unsupported(_native.WB_ERR_UNSUPPORTED,
+                              'GPU COSX K needs a symmetric density matrix')
+        self._build()
+        if dm.shape[0] != self.nao:
+            raise Unsupported(_native.WB_ERR_UNSUPPORTED,
+                              'dm does not match the molecule')
+        mol = sgx.mol
+        grids = sgx.grids
+        pjs = getattr(sgx, '_pjs_data', None)
+        if (pjs is None or getattr(pjs, 'mol', mol) is not mol
+                or getattr(pjs, 'grids', grids) is not grids
+                or getattr(pjs, '_itol', direct_scf_tol) != direct_scf_tol):
+            sgx._build_pjs(direct_scf_tol)
+            pjs = sgx._pjs_data
+        proj = np.asarray(pjs._overlap_correction_matrix, dtype=np.float64)
+        sym = bool(pjs.sym_ovlp)
+        state = self._grid_state(grids)
+        dev = self.engine.device
+        proj_d = torch.as_tensor(proj, device=dev)
+        qd = proj_d @ torch.as_tensor(dm, dtype=torch.float64, device=dev)
+        tk0 = time.perf_counter()
+        K = self.engine.get_k(state.coords, state.weights, qd, omega,
+                              tile_tol=self.tile_tol,
+                              tile_pts=self._tile(state.ngrids),
+                              emulated_gemm=(self.gemm == 'emulated'))
+        if sym:
+            K = proj_d.T @ K
+        K = (K + K.T) * 0.5
+        Kh = K.cpu().numpy()
+        st = dict(self.engine.last_stats)
+        st['wall'] = time.perf_counter() - t0
+        st['kernel'] = time.perf_counter() - tk0
+        self.last_stats = st
+        return Kh
+
+    def kernel_info(self):
+        """Per task class: pairs and primitive pairs of this molecule."""
+        self._build()
+        names = ['l%d%d' % (la, lb) for la in range(LMAX + 1)
+                 for lb in range(la + 1)]
+        return {n: (self.engine.class_pairs[i], self.engine.class_prim_pairs[i])
+                for i, n in enumerate(names)}
+
+
+def get_k_only_gpu(builder, sgx, dm, hermi=1, direct_scf_tol=1e-13):
+    """Same signature/contract as pyscf.sgx.sgx_jk.get_k_only for one RKS
+    dm; omega is read from sgx.mol.omega (reference gpu/sgx_k.py:983-991)."""
+    omega = float(getattr(sgx.mol, 'omega', 0.0) or 0.0)
+    return builder.get_k(sgx, dm, omega, hermi=hermi,
+                         direct_scf_tol=direct_scf_tol)
+
+
+class PjsData:
+    """The two attributes of PySCF's SGX PJS data the K build reads."""
+
+    def __init__(self, mol, grids, proj, sym=False, itol=1e-13):
+        self.mol = mol
+        self.grids = grids
+        self._overlap_correction_matrix = proj
+        self.sym_ovlp = sym
+        self._itol = itol
+
+
+class SyntheticSGX:
+    """Stand-in for PySCF's SGX object when PySCF is absent: ``mol``,
+    ``grids`` and the PJS data (proj = identity unless given)."""
+
+    def __init__(self, mol, grids, proj=None, sym=False):
+        self.mol = mol
+        self.grids = grids
+        self._proj = proj
+        self._sym = sym
+        self._pjs_data = None
+
+    def _build_pjs(self, direct_scf_tol=1e-13):
+        nao = self.mol.nao
+        proj = np.eye(nao) if self._proj is None else np.asarray(self._proj)
+        self._pjs_data = PjsData(self.mol, self.grids, proj, self._sym,
+                                 direct_scf_tol)
+
+
+def profiling_enabled():
+    return os.environ.get('PYSCF_WB97MV_KPROFILE') == '1'

@@ -1,0 +1,87 @@
+"""Synthetic molecules, basis conventions and grids (CPU)."""
+import math
+
+import numpy as np
+import pytest
+
+from pyscf_wb97mv_fast_gb300.basis import (Molecule, cart2sph, cart_components,
+                                           gto_norm)
+from pyscf_wb97mv_fast_gb300.grids import angular_grid, build_grids, radial_grid
+from pyscf_wb97mv_fast_gb300.systems import alkane, water_cluster
+
+
+def test_cart2sph_orthonormal_on_the_sphere():
+    xyz, w = angular_grid(20)
+    for l in range(4):
+        P = np.stack([xyz[:, 0] ** i * xyz[:, 1] ** j * xyz[:, 2] ** k
+                      for (i, j, k) in cart_components(l)], axis=1)
+        S = P @ cart2sph(l)
+        G = (S * w[:, None]).T @ S
+        assert np.allclose(G, np.eye(2 * l + 1), atol=1e-12)
+
+
+def test_contracted_functions_are_normalised():
+    mol = Molecule.build(water_cluster(1, 1.0, seed=0), 'synthetic-tzvp')
+    r, w = radial_grid(400, 1.0)
+    for sh in mol.shells:
+        for c in range(sh.nctr):
+            rad = (sh.coeffs[:, c][None, :] * r[:, None] ** sh.l
+                   * np.exp(-np.outer(r ** 2, sh.exps))).sum(axis=1)
+            assert (rad ** 2 * w).sum() == pytest.approx(1.0, rel=1e-6)
+
+
+def test_water_cluster_geometry():
+    atoms = water_cluster(27, box=10.0, seed=27)
+    xyz = np.array([a[1] for a in atoms]).reshape(27, 3, 3)
+    o = xyz[:, 0]
+    d = np.linalg.norm(o[:, None] - o[None], axis=2) + np.eye(27) * 99
+    assert d.min() >= 2.7
+    assert np.all((o >= 0) & (o <= 10.0))
+    for w in xyz:
+        oh1, oh2 = w[1] - w[0], w[2] - w[0]
+        assert np.linalg.norm(oh1) == pytest.approx(0.9572)
+        ang = math.degrees(math.acos(oh1 @ oh2 / (np.linalg.norm(oh1) * np.linalg.norm(oh2))))
+        assert ang == pytest.approx(104.52)
+    assert water_cluster(27, 10.0, 27) == atoms          # seeded
+
+
+def test_alkane_geometry_and_basis_size():
+    atoms = alkane(20)
+    assert len(atoms) == 62
+    xyz = np.array([a[1] for a in atoms])
+    sym = [a[0] for a in atoms]
+    d = np.linalg.norm(xyz[:, None] - xyz[None], axis=2) + np.eye(62) * 99
+    for i, s in enumerate(sym):
+        nb = np.sort(d[i][d[i] < 1.6])
+        if s == 'C':
+            assert len(nb) == 4
+            assert np.allclose(nb[nb > 1.3], 1.53) and np.allclose(nb[nb < 1.3], 1.09)
+    assert Molecule.build(atoms, 'synthetic-tzvp').nao == 872
+    assert Molecule.build(water_cluster(27, 10.0, 27)).nao == 648
+
+
+def test_grid_integrates_gaussians():
+    mol = Molecule.build(water_cluster(2, 3.2, seed=1))
+    g = build_grids(mol, level=1)
+    for a in (0.5, 3.0):
+        c = mol.atom_coords()[1]
+        f = np.exp(-a * ((g.coords - c) ** 2).sum(axis=1))
+        assert (f * g.weights).sum() == pytest.approx((math.pi / a) ** 1.5, rel=1e-3)
+
+
+def test_grid_subblocks_are_compact():
+    mol = Molecule.build(water_cluster(8, 7.0, seed=8))
+    g = build_grids(mol, level=1)
+    n = g.size // 32 * 32
+    blocks = g.coords[:n].reshape(-1, 32, 3)
+    cen = blocks.mean(axis=1)
+    rad = np.linalg.norm(blocks - cen[:, None], axis=2).max(axis=1)
+    assert np.median(rad) < 1.0          # bohr
+
+
+def test_gto_norm():
+    for l in range(4):
+        a = 1.7
+        r, w = radial_grid(300, 1.0)
+        v = (gto_norm(l, a) * r ** l * np.exp(-a * r * r)) ** 2
+        assert (v * w).sum() == pytest.approx(1.0, rel=1e-8)

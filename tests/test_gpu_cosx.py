@@ -1,0 +1,255 @@
+"""COSX kernels on the GPU vs the FP64 oracle and the reference's golden
+vectors (reference tests: tests/gpu/test_boys.py, test_int3c1e.py,
+test_sgx_k.py, test_ao_eval.py).  All calls go through the C ABI."""
+import os
+
+import numpy as np
+import pytest
+from scipy.special import gamma, gammainc
+
+import oracle
+from helpers import density, dimer, grid_subset, waters
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def ref_boys(n, T):
+    T = np.asarray(T, dtype=np.float64)
+    out = np.empty_like(T)
+    small = T < 1e-12
+    out[small] = 1.0 / (2 * n + 1)
+    Ts = T[~small]
+    out[~small] = gamma(n + 0.5) * gammainc(n + 0.5, Ts) / (2.0 * Ts ** (n + 0.5))
+    return out
+
+
+# -- Boys -----------------------------------------------------------------------
+
+def test_boys_fp32_relative_error():
+    torch = _torch()
+    from pyscf_wb97mv_fast_gb300.cosx import boys_eval
+    T = np.concatenate([[0.0, 1e-30, 1e-8], np.linspace(0, 50, 20001),
+                        np.geomspace(50, 1e6, 2000)]).astype(np.float32)
+    F = boys_eval(torch.as_tensor(T, device='cuda'), 6).cpu().numpy()
+    for n in range(7):
+        ref = ref_boys(n, T.astype(np.float64))
+        rel = np.abs(F[n] - ref) / ref
+        assert np.all(np.isfinite(F[n]))
+        assert rel.max() < 2e-7, (n, rel.max(), T[rel.argmax()])
+
+
+def test_boys_fp32_unbiased():
+    """Mean signed relative error over T in [0, 50] << FP32 eps (a biased
+    F_n biases every integral the same way)."""
+    torch = _torch()
+    from pyscf_wb97mv_fast_gb300.cosx import boys_eval
+    T = np.random.default_rng(0).uniform(0, 50, 1_000_000).astype(np.float32)
+    F = boys_eval(torch.as_tensor(T, device='cuda'), 6).cpu().numpy()
+    for n in range(7):
+        ref = ref_boys(n, T.astype(np.float64))
+        assert abs(np.mean((F[n] - ref) / ref)) < 1e-8, n
+
+
+def test_boys_nmax_slices_and_range():
+    torch = _torch()
+    from pyscf_wb97mv_fast_gb300.cosx import boys_eval
+    T = torch.as_tensor(np.linspace(0, 40, 101).astype(np.float32), device='cuda')
+    full = boys_eval(T, 6).cpu().numpy()
+    for nmax in (0, 2, 4, 6):
+        part = boys_eval(T, nmax).cpu().numpy()
+        assert part.shape == (nmax + 1, 101)
+        assert np.array_equal(part, full[:nmax + 1])
+    with pytest.raises(ValueError):
+        boys_eval(T, 7)
+
+
+# -- dense integrals and AO values vs the reference's own FP64 code -----------
+
+@pytest.mark.parametrize('tag,basis,gen', [('svp', 'synthetic-svp', False),
+                                           ('tzvp', 'synthetic-tzvp', False),
+                                           ('gen', 'synthetic-svp', True)])
+@pytest.mark.parametrize('omega', [0.0, 0.3])
+def test_dense_int3c1e_matches_reference(tag, basis, gen, omega):
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine
+    d = np.load(os.path.join(GOLDEN, 'int3c1e_%s.npz' % tag))
+    mol = dimer(basis, gen)
+    eng = CosxEngine(mol)
+    got = eng.int3c1e_dense(eng.relative(d['coords']), omega).cpu().numpy()
+    ref = d['A_w%g' % omega]
+    assert np.all(np.isfinite(got))
+    assert np.max(np.abs(got - ref)) < 1e-6 * np.abs(ref).max()
+    big = np.abs(ref) > 1e-3 * np.abs(ref).max()
+    assert abs(np.mean((got[big] - ref[big]) / ref[big])) < 1e-7
+    assert np.array_equal(got, got.transpose(0, 2, 1))
+    again = eng.int3c1e_dense(eng.relative(d['coords']), omega).cpu().numpy()
+    assert np.array_equal(got, again)
+
+
+@pytest.mark.parametrize('tag,basis,gen', [('svp', 'synthetic-svp', False),
+                                           ('tzvp', 'synthetic-tzvp', False),
+                                           ('gen', 'synthetic-svp', True)])
+def test_ao_eval_matches_reference(tag, basis, gen):
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine
+    d = np.load(os.path.join(GOLDEN, 'int3c1e_%s.npz' % tag))
+    eng = CosxEngine(dimer(basis, gen))
+    n = len(d['ao_coords'])
+    X = eng.ao_eval(eng.relative(d['ao_coords'])).cpu().numpy()[:, :n].T
+    ref = d['ao']
+    assert np.max(np.abs(X - ref)) < 1e-13 * np.abs(ref).max()
+
+
+# -- fused G kernels vs the FP64 oracle ----------------------------------------
+
+def _g_case(mol, npts, seed, omega, tile_tol=0.0):
+    torch = _torch()
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine, round32
+    eng = CosxEngine(mol)
+    coords, weights = grid_subset(mol, 1, npts, seed)
+    n = len(coords)
+    X = oracle.ao_eval(mol, coords)
+    dm = density(mol.nao, 10, seed)
+    F32 = (X @ dm).astype(np.float32)
+    ld = round32(n)
+    Fd = torch.zeros((mol.nao, ld), dtype=torch.float32, device=eng.device)
+    Fd[:, :n] = torch.as_tensor(F32.T, device=eng.device)
+    w = torch.as_tensor(weights, device=eng.device)
+    G = eng.g(eng.relative(coords), w, Fd, omega, tile_tol).cpu().numpy()[:, :n].T
+    Gref = oracle.cosx_g(mol, coords, F32.astype(np.float64), omega)
+    return eng, G, Gref, n
+
+
+@pytest.mark.parametrize('basis,gen', [('synthetic-svp', False),
+                                       ('synthetic-tzvp', False),
+                                       ('synthetic-svp', True)])
+@pytest.mark.parametrize('omega', [0.0, 0.3])
+def test_g_kernels_match_oracle(basis, gen, omega):
+    mol = dimer(basis, gen)
+    eng, G, Gref, n = _g_case(mol, 700, 3, omega)
+    scale = np.abs(Gref).max()
+    assert np.all(np.isfinite(G))
+    assert np.max(np.abs(G - Gref)) < 2e-6 * scale, np.max(np.abs(G - Gref)) / scale
+    st = eng.last_stats
+    assert st['pairs_kept'] == st['pairs_total']          # tile_tol = 0
+    # counters: model flops / integrals are exact sums over the pair table
+    rows = eng.pair_table()
+    nsub_full, rem = divmod(n, 32)
+    pts = 32 * nsub_full + rem
+    assert st['model_flops'] == float(rows[:, 7].sum() * pts)
+
+
+def test_g_kernels_bitwise_reproducible():
+    mol = dimer('synthetic-tzvp')
+    _, G1, _, _ = _g_case(mol, 900, 4, 0.3)
+    _, G2, _, _ = _g_case(mol, 900, 4, 0.3)
+    assert np.array_equal(G1, G2)
+
+
+# -- full K build vs the oracle and the reference --------------------------------
+
+def _k_gpu(mol, coords, weights, dm, omega, tile_tol=0.0, tile_pts=0):
+    torch = _torch()
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine
+    eng = CosxEngine(mol)
+    c = eng.relative(coords)
+    w = torch.as_tensor(weights, device=eng.device)
+    qd = torch.as_tensor(dm, device=eng.device)
+    K = eng.get_k(c, w, qd, omega, tile_tol=tile_tol, tile_pts=tile_pts)
+    K = ((K + K.T) * 0.5).cpu().numpy()
+    return K, eng.last_stats
+
+
+@pytest.mark.parametrize('basis,gen', [('synthetic-svp', False),
+                                       ('synthetic-tzvp', False),
+                                       ('synthetic-svp', True)])
+@pytest.mark.parametrize('omega', [0.0, 0.3])
+def test_k_matches_oracle(basis, gen, omega):
+    """Reference gate (tests/gpu/test_sgx_k.py:24-46): max|dK| < 1e-6
+    max|K|, |1/4 tr(D dK)| < 3e-7 (full) / 1e-7 (long range), K exactly
+    symmetric and bitwise reproducible."""
+    mol = dimer(basis, gen)
+    coords, weights = grid_subset(mol, 1, 4000, 1)
+    dm = density(mol.nao, 10, 2)
+    K1, st = _k_gpu(mol, coords, weights, dm, omega)
+    K2, _ = _k_gpu(mol, coords, weights, dm, omega)
+    Kref = oracle.cosx_k(mol, coords, weights, dm, omega)
+    assert np.array_equal(K1, K2)
+    assert np.array_equal(K1, K1.T)
+    assert np.max(np.abs(K1 - Kref)) < 1e-6 * np.abs(Kref).max()
+    gate = 3e-7 if omega == 0.0 else 1e-7
+    assert abs(0.25 * np.einsum('ij,ji->', dm, K1 - Kref)) < gate
+    assert st['pairs_kept'] == st['pairs_total']
+
+
+@pytest.mark.parametrize('omega', [0.0, 0.3])
+def test_k_matches_reference_golden(omega):
+    """The reference's own FP64 K on the same 160 points (dense A from
+    int3c1e_reference contracted as gpu/sgx_k.py:719-742)."""
+    d = np.load(os.path.join(GOLDEN, 'k_svp.npz'))
+    mol = dimer('synthetic-svp')
+    K, _ = _k_gpu(mol, d['coords'], d['weights'], d['dm'], omega)
+    ref = d['K_w%g' % omega]
+    assert np.max(np.abs(K - ref)) < 1e-6 * np.abs(ref).max()
+
+
+def test_k_tiles_do_not_change_result_beyond_rounding():
+    mol = dimer('synthetic-svp')
+    coords, weights = grid_subset(mol, 1, 5000, 3)
+    dm = density(mol.nao, 10, 3)
+    K1, _ = _k_gpu(mol, coords, weights, dm, 0.0)
+    K2, st = _k_gpu(mol, coords, weights, dm, 0.0, tile_pts=1024)
+    assert np.max(np.abs(K1 - K2)) < 1e-12 * np.abs(K1).max()
+    assert st['kernel_launches'] > 5
+
+
+@pytest.mark.parametrize('omega', [0.0, 0.3])
+def test_screening_error_and_savings(omega):
+    """Screened (1e-11) vs unscreened on 8 waters: |dK| and |1/4 tr(D dK)|
+    <= 1e-8 and tasks skipped (reference tests/gpu/test_sgx_k.py:226-244)."""
+    mol = waters(8, 7.0, 8)
+    coords, weights = grid_subset(mol, 1, 20000, 5)
+    dm = density(mol.nao, 40, 5)
+    K0, s0 = _k_gpu(mol, coords, weights, dm, omega, tile_tol=0.0)
+    K1, s1 = _k_gpu(mol, coords, weights, dm, omega, tile_tol=1e-11)
+    assert s0['pairs_kept'] == s0['pairs_total']
+    assert s1['pairs_kept'] < s1['pairs_total']
+    assert np.max(np.abs(K1 - K0)) < 1e-8
+    assert abs(0.25 * np.einsum('ij,ji->', dm, K1 - K0)) < 1e-8
+
+
+def test_builder_api_and_out_of_scope():
+    from pyscf_wb97mv_fast_gb300.gpu.sgx_k import (GpuKBuilder, SyntheticSGX,
+                                                   Unsupported, get_k_only_gpu)
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    mol = dimer('synthetic-svp')
+    g = build_grids(mol, level=0)
+    sgx = SyntheticSGX(mol, g)
+    dm = density(mol.nao, 10, 7)
+    b = GpuKBuilder(mol, tile_tol=0.0)
+    K = get_k_only_gpu(b, sgx, dm)
+    assert K.dtype == np.float64 and K.shape == (mol.nao, mol.nao)
+    assert np.array_equal(K, K.T)
+    Kref = oracle.cosx_k(mol, g.coords, g.weights, dm, 0.0)
+    assert np.max(np.abs(K - Kref)) < 1e-6 * np.abs(Kref).max()
+    assert b.last_stats['pairs_kept'] == b.last_stats['pairs_total']
+    mol.omega = 0.3
+    try:
+        K3 = get_k_only_gpu(b, sgx, dm)
+    finally:
+        mol.omega = 0.0
+    Kref3 = oracle.cosx_k(mol, g.coords, g.weights, dm, 0.3)
+    assert np.max(np.abs(K3 - Kref3)) < 1e-6 * np.abs(Kref3).max()
+    with pytest.raises(Unsupported):
+        get_k_only_gpu(b, sgx, dm, hermi=0)
+    with pytest.raises(Unsupported):
+        get_k_only_gpu(b, sgx, np.stack([dm, 0.5 * dm]))
+    asym = dm.copy()
+    asym[0, 1] += 1e-3
+    with pytest.raises(Unsupported):
+        get_k_only_gpu(b, sgx, asym)

@@ -1,0 +1,146 @@
+"""Hook mechanics, the install boundary with stand-in PySCF modules, and
+package layering (CPU)."""
+import subprocess
+import sys
+import types
+
+import pytest
+
+from pyscf_wb97mv_fast_gb300.core.hooks import HookSet, reset_diis, track_residual
+
+
+class Base:
+    def method(self):
+        return 'base'
+
+
+def test_wrap_restores_module_function_and_instance_shadow():
+    mod = types.ModuleType('m')
+    mod.f = lambda x: x + 1
+    orig = mod.f
+    obj = Base()
+    with HookSet() as hooks:
+        hooks.wrap(mod, 'f', lambda o: (lambda x: o(x) * 10))
+        hooks.wrap(obj, 'method', lambda o: (lambda: 'hooked:' + o()))
+        assert mod.f(1) == 20
+        assert obj.method() == 'hooked:base'
+        assert 'method' in obj.__dict__
+    assert mod.f is orig
+    assert 'method' not in obj.__dict__ and obj.method() == 'base'
+
+
+def test_restore_order_and_closed_state():
+    calls = []
+    hooks = HookSet()
+    mod = types.ModuleType('m')
+    mod.v = 1
+    hooks.on_restore(lambda: calls.append('first'))
+    hooks.wrap(mod, 'v', lambda o: o + 1)
+    hooks.on_restore(lambda: calls.append(('last', mod.v)))
+    hooks.restore_all()
+    assert calls == [('last', 2), 'first'] and mod.v == 1
+    with pytest.raises(RuntimeError):
+        hooks.wrap(mod, 'v', lambda o: o)
+    with pytest.raises(RuntimeError):
+        hooks.on_restore(lambda: None)
+
+
+def test_reset_diis_and_track_residual():
+    class FakeDiis:
+        space = 8
+        _buffer = {'x': 1}
+        _bookkeep = [1, 2]
+        _head = 2
+        _H = object()
+        _xprev = object()
+    d = FakeDiis()
+    d._buffer = {'x': 1}
+    reset_diis(d)
+    assert d._buffer == {} and d._bookkeep == [] and d._head == 0
+    assert d._H is None and d.space == 8
+    reset_diis(None)
+
+    class Mf:
+        callback = None
+    mf = Mf()
+    seen = []
+    with HookSet() as hooks:
+        track_residual(hooks, mf, seen.append)
+        mf.callback({'norm_gorb': 3.5})
+    assert seen == [3.5] and mf.callback is None
+
+
+def _fake_mf():
+    class Sgx:
+        pass
+    df = Sgx()
+    df._rsh_df = {'0.300000': Sgx()}
+    mf = types.SimpleNamespace(with_df=df, mol=None, _numint=types.SimpleNamespace())
+    return mf, Sgx
+
+
+def test_install_routes_only_this_mf_and_restores():
+    from pyscf_wb97mv_fast_gb300.gpu.install import install_gpu
+    mf, Sgx = _fake_mf()
+    mod = types.ModuleType('fake_sgx_jk')
+    calls = []
+    mod.get_k_only = lambda sgx, dm, hermi=1, tol=1e-13: calls.append(sgx) or 'cpu'
+    orig = mod.get_k_only
+    hooks = install_gpu(mf, k=True, vv10=False, sgx_jk_module=mod)
+    assert mod.get_k_only is not orig
+    other = Sgx()
+    assert mod.get_k_only(other, None) == 'cpu'   # foreign SGX object: original
+    assert calls == [other]
+    hooks.restore_all()
+    assert mod.get_k_only is orig
+
+
+def test_install_rejects_what_this_build_does_not_hook():
+    from pyscf_wb97mv_fast_gb300.gpu.install import install_gpu
+    mf, _ = _fake_mf()
+    with pytest.raises(NotImplementedError):
+        install_gpu(mf, semilocal=True, k=False, vv10=False)
+    with pytest.raises(ValueError):
+        install_gpu(mf, backend='numpy', k=False, vv10=False)
+
+
+def test_oom_retry_halves_tile_then_reraises():
+    from pyscf_wb97mv_fast_gb300.gpu.install import _run_with_oom_retry
+
+    class B:
+        def __init__(self, blksize):
+            self.blksize = blksize
+
+        def with_blksize(self, n):
+            return B(n)
+    seen = []
+
+    def flow(b):
+        seen.append(b.blksize)
+        raise MemoryError('out of memory')
+    with pytest.raises(MemoryError):
+        _run_with_oom_retry(flow, B(1024))
+    assert seen == [1024, 512, 256]
+
+    def ok_second(b):
+        seen.append(b.blksize)
+        if b.blksize > 600:
+            raise MemoryError('out of memory')
+        return b.blksize
+    seen.clear()
+    assert _run_with_oom_retry(ok_second, B(1024)) == 512
+
+    def other(b):
+        raise ValueError('not an OOM')
+    with pytest.raises(ValueError):
+        _run_with_oom_retry(other, B(1024))
+
+
+def test_import_has_no_side_effects():
+    code = ('import sys, pyscf_wb97mv_fast_gb300, pyscf_wb97mv_fast_gb300.gpu.install, '
+            'pyscf_wb97mv_fast_gb300.gpu.sgx_k;'
+            'print(any(m == "pyscf" or m.startswith("pyscf.") for m in sys.modules),'
+            ' "torch" in sys.modules)')
+    out = subprocess.run([sys.executable, '-c', code], capture_output=True,
+                         text=True, check=True).stdout.split()
+    assert out == ['False', 'False']
