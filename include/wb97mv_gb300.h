@@ -141,6 +141,12 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
 int wb_ao_eval(const wb_cosx* h, const double* coords, int64_t npts,
                double* x_out, void* stream);
 
+/* AO values and their x, y, z gradients, x_out (4, nao, ldp) FP64.
+ * Replaces AoEvaluator.eval(deriv=1) (gpu/ao_eval.py:186-329) for the VV10
+ * flow (gpu/vv10.py:288-297). */
+int wb_ao_eval_deriv1(const wb_cosx* h, const double* coords, int64_t npts,
+                      double* x_out, void* stream);
+
 /* Dense contracted spherical A[g, mu, nu] (npts, nao, nao) FP32 for small
  * validation systems.  Replaces int3c1e_fp32 (gpu/int3c1e.py:284-314). */
 int wb_int3c1e_dense(const wb_cosx* h, const double* coords, int64_t npts,

@@ -54,8 +54,9 @@ def _load():
         _lib.oracle_cosx_g.argtypes = basis + [P, I64, D, P, P]
         _lib.oracle_ao_eval.argtypes = basis + [P, I64, P]
         _lib.oracle_vv10_sum.argtypes = [P, P, P, P, I64, P, P, P]
+        _lib.oracle_ao_eval_deriv1.argtypes = basis + [P, I64, P]
         for f in ('oracle_boys', 'oracle_int3c1e', 'oracle_cosx_g',
-                  'oracle_ao_eval', 'oracle_vv10_sum'):
+                  'oracle_ao_eval', 'oracle_vv10_sum', 'oracle_ao_eval_deriv1'):
             getattr(_lib, f).restype = I
     return _lib
 
@@ -111,6 +112,54 @@ def ao_eval(mol, coords):
     X = np.zeros((len(c), b.nao))
     _load().oracle_ao_eval(*b.args, _p(c), len(c), _p(X))
     return X
+
+
+def ao_eval_deriv1(mol, coords):
+    """X and gradients (4, ng, nao) FP64."""
+    b = _Basis(mol)
+    c = np.ascontiguousarray(coords, dtype=np.float64)
+    X = np.zeros((4, len(c), b.nao))
+    _load().oracle_ao_eval_deriv1(*b.args, _p(c), len(c), _p(X))
+    return X
+
+
+def nlc_vxc(mol, coords, weights, dm, nlc_coefs, thresh=1e-8):
+    """FP64 restatement of the reference's VV10 flow (gpu/vv10.py:268-342 =
+    NumInt.nr_nlc_vxc): (nelec, excsum, vmat); nlc_coefs [((b, C), fac)]."""
+    import math
+    ao = ao_eval_deriv1(mol, coords)
+    w = np.asarray(weights, dtype=np.float64)
+    T = ao[0] @ dm
+    rho0 = (T * ao[0]).sum(axis=1)
+    grad = 2.0 * np.einsum('pm,dpm->dp', T, ao[1:4])
+    nelec = float((rho0 * w).sum())
+    n = len(w)
+    exc, v0, v1 = np.zeros(n), np.zeros(n), np.zeros(n)
+    for (Bvv, Cvv), fac in nlc_coefs:
+        ind = rho0 >= thresh
+        R, gr = rho0[ind], grad[:, ind]
+        pi43 = 4.0 * math.pi / 3.0
+        Kvv = Bvv * 1.5 * math.pi * (9.0 * math.pi) ** (-1.0 / 6.0)
+        Beta = ((3.0 / (Bvv * Bvv)) ** 0.75) / 32.0
+        G = (gr ** 2).sum(axis=0)
+        W0tmp = Cvv * (G / (R * R)) ** 2
+        W0 = np.sqrt(W0tmp + pi43 * R)
+        dW0dR = (0.5 * pi43 * R - 2.0 * W0tmp) / W0
+        dW0dG = W0tmp * R / (G * W0)
+        kappa = Kvv * R ** (1.0 / 6.0)
+        dKdR = kappa / 6.0
+        q = R * w[ind]
+        F, U, W = vv10_sum(coords[ind], q, W0, kappa)
+        exc[ind] += fac * (Beta + 0.5 * F)
+        v0[ind] += fac * (Beta + F + 1.5 * (U * dKdR + W * dW0dR))
+        v1[ind] += fac * (1.5 * W * dW0dG)
+    excsum = float((rho0 * w * exc).sum())
+    wv = np.empty((4, n))
+    wv[0] = 0.5 * v0 * w
+    wv[1:4] = 2.0 * v1[None] * grad * w[None]
+    aow = np.einsum('dpm,dp->pm', ao, wv)
+    vmat = ao[0].T @ aow
+    return nelec, excsum, vmat + vmat.T
 
 
 def vv10_sum(coords, q, w0, kappa):

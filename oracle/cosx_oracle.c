@@ -335,6 +335,61 @@ int oracle_ao_eval(OBASIS_ARGS, const double* coords, int64_t ng, double* X) {
     return 0;
 }
 
+/* X (4, ng, nao): values and x, y, z gradients */
+int oracle_ao_eval_deriv1(OBASIS_ARGS, const double* coords, int64_t ng,
+                          double* X) {
+    obasis b;
+    make_basis(&b, OBASIS_PASS);
+    int* ao = ao_offsets(&b);
+    const int nao = ao[nbas];
+    const int64_t plane = ng * (int64_t)nao;
+#pragma omp parallel for schedule(static)
+    for (int64_t g = 0; g < ng; ++g) {
+        for (int s = 0; s < nbas; ++s) {
+            const int l = shell_l[s], np = shell_nprim[s], nc = shell_nctr[s];
+            const double* A = atom_coords + 3 * shell_atom[s];
+            const double d[3] = {coords[3 * g] - A[0], coords[3 * g + 1] - A[1],
+                                 coords[3 * g + 2] - A[2]};
+            const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            const int nca = ncart(l), ns = nsph(l);
+            for (int ci = 0; ci < nc; ++ci) {
+                double cart[4][10];
+                for (int c = 0; c < nca; ++c) {
+                    int e[3];
+                    cart_comp(l, c, &e[0], &e[1], &e[2]);
+                    double val = 0.0, gr[3] = {0.0, 0.0, 0.0};
+                    for (int k = 0; k < np; ++k) {
+                        const double a = exps[shell_exp_off[s] + k];
+                        const double ek = coeffs[shell_coef_off[s] + k * nc + ci] *
+                                          exp(-a * r2);
+                        const double m = pow(d[0], e[0]) * pow(d[1], e[1]) * pow(d[2], e[2]);
+                        val += ek * m;
+                        for (int ax = 0; ax < 3; ++ax) {
+                            /* d/dx [x^i ...] = (i x^(i-1) - 2 a x^(i+1)) ... */
+                            double f = -2.0 * a * pow(d[ax], e[ax] + 1);
+                            if (e[ax] > 0) f += e[ax] * pow(d[ax], e[ax] - 1);
+                            double o = 1.0;
+                            for (int bx = 0; bx < 3; ++bx)
+                                if (bx != ax) o *= pow(d[bx], e[bx]);
+                            gr[ax] += ek * f * o;
+                        }
+                    }
+                    cart[0][c] = val;
+                    cart[1][c] = gr[0]; cart[2][c] = gr[1]; cart[3][c] = gr[2];
+                }
+                for (int m = 0; m < ns; ++m)
+                    for (int comp = 0; comp < 4; ++comp) {
+                        double v = 0.0;
+                        for (int c = 0; c < nca; ++c) v += b.c2s[l][c * ns + m] * cart[comp][c];
+                        X[comp * plane + g * (int64_t)nao + ao[s] + ci * ns + m] = v;
+                    }
+            }
+        }
+    }
+    free(ao);
+    return 0;
+}
+
 int oracle_vv10_sum(const double* xyz, const double* q, const double* w0,
                     const double* kappa, int64_t n, double* F, double* U,
                     double* W) {

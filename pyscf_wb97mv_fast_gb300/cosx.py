@@ -186,6 +186,18 @@ class CosxEngine:
             self._stream()), 'wb_ao_eval')
         return out
 
+    def ao_eval_deriv1(self, coords_rel, out=None):
+        """X and its gradients (4, nao, ld) FP64 AO-major."""
+        torch = _torch()
+        npts = int(coords_rel.shape[0])
+        if out is None:
+            out = torch.empty((4, self.nao, round32(npts)), dtype=torch.float64,
+                              device=self.device)
+        _native.check(_native.lib().wb_ao_eval_deriv1(
+            self._h, _native.ptr(coords_rel), npts, _native.ptr(out),
+            self._stream()), 'wb_ao_eval_deriv1')
+        return out
+
     def int3c1e_dense(self, coords_rel, omega=0.0):
         """Dense (npts, nao, nao) FP32 contracted spherical integrals
         (validation only; refuses more than 2 GiB)."""

@@ -261,6 +261,102 @@ __global__ void ao_eval_kernel(const AoArgs A) {
     }
 }
 
+// deriv 1: value and x, y, z gradients, X (4, nao, ld).  For a primitive
+// x^i y^j z^k exp(-a r^2): d/dx = (i x^(i-1) - 2 a x^(i+1)) y^j z^k exp(-a r^2)
+// (gpu/ao_eval.py:305-319); contracted radial sums rad0 = sum c e,
+// rad1 = sum c (-2 a) e.
+template<int L>
+__device__ __forceinline__ void ao_shell_d1(const AoArgs& A, int sh, int64_t g,
+                                            double dx, double dy, double dz,
+                                            double r2) {
+    constexpr int NC = (L + 1) * (L + 2) / 2, NS = 2 * L + 1;
+    double px[L + 2], py[L + 2], pz[L + 2];
+    px[0] = py[0] = pz[0] = 1.0;
+#pragma unroll
+    for (int e = 1; e < L + 2; ++e) {
+        px[e] = px[e - 1] * dx; py[e] = py[e - 1] * dy; pz[e] = pz[e - 1] * dz;
+    }
+    const double* c2s = c2s_ptr<L>();
+    const int np = A.sh_np[sh], nc = A.sh_nc[sh];
+    const double* ex = A.exps + A.sh_eoff[sh];
+    const double* co = A.coeffs + A.sh_coff[sh];
+    const int ao0 = A.sh_ao0[sh];
+    const int64_t plane = (int64_t)A.nao * A.ld;
+    for (int ci = 0; ci < nc; ++ci) {
+        double rad0 = 0.0, rad1 = 0.0;
+        for (int k = 0; k < np; ++k) {
+            const double e = co[k * nc + ci] * exp(-ex[k] * r2);
+            rad0 += e;
+            rad1 += -2.0 * ex[k] * e;
+        }
+        double cv[NC], cgx[NC], cgy[NC], cgz[NC];
+        {
+            int c = 0;
+#pragma unroll
+            for (int lx = L; lx >= 0; --lx)
+#pragma unroll
+                for (int ly = L - lx; ly >= 0; --ly) {
+                    const int lz = L - lx - ly;
+                    const double m = px[lx] * py[ly] * pz[lz];
+                    cv[c] = rad0 * m;
+                    cgx[c] = rad1 * px[lx + 1] * py[ly] * pz[lz] +
+                             (lx ? rad0 * lx * px[lx - 1] * py[ly] * pz[lz] : 0.0);
+                    cgy[c] = rad1 * px[lx] * py[ly + 1] * pz[lz] +
+                             (ly ? rad0 * ly * px[lx] * py[ly - 1] * pz[lz] : 0.0);
+                    cgz[c] = rad1 * px[lx] * py[ly] * pz[lz + 1] +
+                             (lz ? rad0 * lz * px[lx] * py[ly] * pz[lz - 1] : 0.0);
+                    ++c;
+                }
+        }
+#pragma unroll
+        for (int m = 0; m < NS; ++m) {
+            double v = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const double t = c2s[c * NS + m];
+                v += t * cv[c]; gx += t * cgx[c]; gy += t * cgy[c]; gz += t * cgz[c];
+            }
+            const int64_t o = (int64_t)(ao0 + ci * NS + m) * A.ld + g;
+            A.X[o] = v;
+            A.X[plane + o] = gx;
+            A.X[2 * plane + o] = gy;
+            A.X[3 * plane + o] = gz;
+        }
+    }
+}
+
+__global__ void ao_eval_d1_kernel(const AoArgs A) {
+    const int sh = blockIdx.y;
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= A.ld) return;
+    const int l = A.sh_l[sh];
+    if (g >= A.npts) {
+        const int n = A.sh_nc[sh] * (2 * l + 1);
+        const int64_t plane = (int64_t)A.nao * A.ld;
+        for (int i = 0; i < n; ++i)
+            for (int c = 0; c < 4; ++c)
+                A.X[c * plane + (int64_t)(A.sh_ao0[sh] + i) * A.ld + g] = 0.0;
+        return;
+    }
+    const double dx = A.coords[g * 3] - A.sh_ctr[sh * 3];
+    const double dy = A.coords[g * 3 + 1] - A.sh_ctr[sh * 3 + 1];
+    const double dz = A.coords[g * 3 + 2] - A.sh_ctr[sh * 3 + 2];
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    switch (l) {
+    case 0: ao_shell_d1<0>(A, sh, g, dx, dy, dz, r2); break;
+    case 1: ao_shell_d1<1>(A, sh, g, dx, dy, dz, r2); break;
+    case 2: ao_shell_d1<2>(A, sh, g, dx, dy, dz, r2); break;
+    default: ao_shell_d1<3>(A, sh, g, dx, dy, dz, r2); break;
+    }
+}
+
+cudaError_t launch_ao_eval_d1(const AoArgs& a, cudaStream_t s) {
+    if (a.ld <= 0 || a.nbas <= 0) return cudaSuccess;
+    dim3 grid((unsigned)((a.ld + 127) / 128), (unsigned)a.nbas);
+    ao_eval_d1_kernel<<<grid, 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_ao_eval(const AoArgs& a, cudaStream_t s) {
     if (a.ld <= 0 || a.nbas <= 0) return cudaSuccess;
     dim3 grid((unsigned)((a.ld + 127) / 128), (unsigned)a.nbas);

@@ -489,6 +489,7 @@ int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
         ao.sh_l = h->sh_l; ao.sh_np = h->sh_np; ao.sh_nc = h->sh_nc;
         ao.sh_eoff = h->sh_eoff; ao.sh_coff = h->sh_coff; ao.sh_ao0 = h->sh_ao0;
         ao.sh_ctr = h->sh_ctr; ao.exps = h->exps; ao.coeffs = h->coeffs; ao.X = X;
+        ao.nao = nao;
         WB_CUDA(wb::launch_ao_eval(ao, s));
         // F(g, mu) = sum_l X(g, l) QD(l, mu); QD row-major = col-major QD^T
         WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)ldt, nao,
@@ -546,7 +547,22 @@ int wb_ao_eval(const wb_cosx* h, const double* coords, int64_t npts,
     ao.sh_l = h->sh_l; ao.sh_np = h->sh_np; ao.sh_nc = h->sh_nc;
     ao.sh_eoff = h->sh_eoff; ao.sh_coff = h->sh_coff; ao.sh_ao0 = h->sh_ao0;
     ao.sh_ctr = h->sh_ctr; ao.exps = h->exps; ao.coeffs = h->coeffs; ao.X = x_out;
+    ao.nao = h->hp.nao;
     WB_CUDA(wb::launch_ao_eval(ao, static_cast<cudaStream_t>(stream)));
+    return WB_OK;
+}
+
+int wb_ao_eval_deriv1(const wb_cosx* h, const double* coords, int64_t npts,
+                      double* x_out, void* stream) {
+    if (!h || !x_out || npts < 0 || (npts && !coords))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_ao_eval_deriv1: bad arguments");
+    wb::AoArgs ao;
+    ao.coords = coords; ao.npts = npts; ao.ld = round32(npts); ao.nbas = h->nbas;
+    ao.sh_l = h->sh_l; ao.sh_np = h->sh_np; ao.sh_nc = h->sh_nc;
+    ao.sh_eoff = h->sh_eoff; ao.sh_coff = h->sh_coff; ao.sh_ao0 = h->sh_ao0;
+    ao.sh_ctr = h->sh_ctr; ao.exps = h->exps; ao.coeffs = h->coeffs; ao.X = x_out;
+    ao.nao = h->hp.nao;
+    WB_CUDA(wb::launch_ao_eval_d1(ao, static_cast<cudaStream_t>(stream)));
     return WB_OK;
 }
 

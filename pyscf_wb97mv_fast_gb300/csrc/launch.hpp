@@ -26,10 +26,12 @@ struct AoArgs {
     const double* sh_ctr;       // (nbas, 3)
     const double* exps;
     const double* coeffs;
-    double* X;                  // (nao, ld)
+    double* X;                  // (nao, ld), or (4, nao, ld) for deriv 1
+    int nao;
 };
 
 cudaError_t launch_ao_eval(const AoArgs& a, cudaStream_t s);
+cudaError_t launch_ao_eval_d1(const AoArgs& a, cudaStream_t s);
 cudaError_t upload_c2s_tables(const double* t0, const double* t1,
                               const double* t2, const double* t3);
 cudaError_t upload_c2s_f(const float* all /* 4 x 70 */);

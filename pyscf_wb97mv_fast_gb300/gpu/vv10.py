@@ -1,0 +1,157 @@
+"""VV10 non-local correlation on the GPU (reference:
+pyscf_wb97mv_fast/gpu/vv10.py).
+
+* ``Vv10Kernel.kernel_sum(coords, q, W0, kappa) -> (F, U, W)``: the
+  O(N_g^2) double sum through the native tiled kernel (FP32 pair terms,
+  Kahan inside a 256-point tile, FP64 across tiles, device-side tile-pair
+  pruning when tile_tol > 0).  F is returned as -1.5 x the raw sum, the
+  libdft VXC_vv10nlc convention the reference follows (:216-221).
+* ``vv10_pointwise``: the per-point FP64 quantities of PySCF's _vv10nlc
+  (reference :243-265), in torch on the device.
+* ``gpu_nr_nlc_vxc``: same signature and result as
+  ``NumInt.nr_nlc_vxc`` -> (nelec, excsum, vmat) (reference :268-342): AO
+  values and gradients (FP64, native), GGA density, threshold
+  rho >= 1e-8, pointwise terms, kernel_sum, the GGA potential and the Fock
+  contraction vmat = X^T (w v) X + transpose, all on the device in FP64
+  except the pair sum.
+"""
+import math
+
+import numpy as np
+
+from pyscf_wb97mv_fast_gb300 import _native
+from pyscf_wb97mv_fast_gb300.cosx import CosxEngine, as_molecule
+
+THRESH = 1e-8
+Unsupported = _native.Unsupported
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class Vv10Kernel:
+    """The double sum; tile_tol > 0 enables device-side tile-pair pruning."""
+
+    def __init__(self, tile_tol=0.0):
+        self.tile_tol = float(tile_tol)
+        self.last_pairs_kept = None
+
+    def kernel_sum(self, coords, q, W0, kappa):
+        """coords (P, 3), q, W0, kappa (P,) on the device -> F, U, W FP64."""
+        torch = _torch()
+        dev = coords.device
+        n = int(coords.shape[0])
+        F = torch.zeros(n, dtype=torch.float64, device=dev)
+        U = torch.zeros_like(F)
+        W = torch.zeros_like(F)
+        if n == 0:
+            self.last_pairs_kept = (0, 0)
+            return F, U, W
+        xyz = coords.to(torch.float32).contiguous()
+        q32, w32, k32 = (torch.as_tensor(a, device=dev).to(torch.float32).contiguous()
+                         for a in (q, W0, kappa))
+        kept = _native.ctypes.c_int64()
+        stream = _native.ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        _native.check(_native.lib().wb_vv10_kernel_sum(
+            _native.ptr(xyz), _native.ptr(q32), _native.ptr(w32), _native.ptr(k32),
+            n, self.tile_tol, _native.ptr(F), _native.ptr(U), _native.ptr(W),
+            stream, _native.ctypes.byref(kept)), 'wb_vv10_kernel_sum')
+        self.last_pairs_kept = (int(kept.value), n * n)
+        return F, U, W
+
+
+def vv10_pointwise(rho0, grad, weights, nlc_pars):
+    """Per-point FP64 terms on the thresholded set: q, W0, kappa, dW0/dR,
+    dW0/dG, dK/dR, Beta (torch tensors; Beta a float)."""
+    Bvv, Cvv = nlc_pars
+    pi = math.pi
+    pi43 = 4.0 * pi / 3.0
+    Kvv = Bvv * 1.5 * pi * (9.0 * pi) ** (-1.0 / 6.0)
+    Beta = ((3.0 / (Bvv * Bvv)) ** 0.75) / 32.0
+    R = rho0
+    G = (grad ** 2).sum(dim=0)
+    W0tmp = Cvv * (G / (R * R)) ** 2
+    W0 = (W0tmp + pi43 * R).sqrt()
+    dW0dR = (0.5 * pi43 * R - 2.0 * W0tmp) / W0
+    dW0dG = W0tmp * R / (G * W0)
+    kappa = Kvv * R ** (1.0 / 6.0)
+    dKdR = kappa / 6.0
+    q = R * weights
+    return q, W0, kappa, dW0dR, dW0dG, dKdR, Beta
+
+
+class Vv10Context:
+    """Per-mf state of the VV10 flow: the native engine (AO tables) and the
+    kernel-sum settings."""
+
+    def __init__(self, mol, tile_tol=0.0, device=None):
+        self.mol = mol
+        self.tile_tol = float(tile_tol)
+        self.device = device
+        self.engine = None
+        self.kernel = Vv10Kernel(tile_tol)
+
+    def build(self):
+        if self.engine is None:
+            self.engine = CosxEngine(as_molecule(self.mol), device=self.device)
+        return self.engine
+
+
+def _prepare_dm(dm, hermi):
+    dm = np.asarray(dm, dtype=np.float64)
+    if dm.ndim == 3 and dm.shape[0] == 1:
+        dm = dm[0]
+    if dm.ndim != 2 or dm.shape[0] != dm.shape[1]:
+        raise Unsupported(_native.WB_ERR_UNSUPPORTED,
+                          'GPU VV10 supports a single RKS density matrix')
+    if hermi != 1:
+        dm = 0.5 * (dm + dm.T)
+    return dm
+
+
+def gpu_nr_nlc_vxc(ctx, ni, mol, grids, xc_code, dm, relativity=0, hermi=1,
+                   max_memory=2000, verbose=None):
+    """GPU replacement of NumInt.nr_nlc_vxc (RKS ground state)."""
+    torch = _torch()
+    if relativity not in (0, None):
+        raise Unsupported(_native.WB_ERR_UNSUPPORTED,
+                          'relativistic NLC not supported')
+    dm = _prepare_dm(dm, hermi)
+    nlc_coefs = ni.nlc_coeff(xc_code)
+    if not nlc_coefs:
+        raise Unsupported(_native.WB_ERR_UNSUPPORTED,
+                          '%r has no NLC parameter set' % (xc_code,))
+    eng = ctx.build()
+    dev = eng.device
+    nao = eng.nao
+    coords = eng.relative(np.asarray(grids.coords, dtype=np.float64))
+    w = torch.as_tensor(np.asarray(grids.weights, dtype=np.float64), device=dev)
+    n = int(coords.shape[0])
+    ao = eng.ao_eval_deriv1(coords)[:, :, :n]             # (4, nao, n)
+    D = torch.as_tensor(dm, device=dev)
+    T = D @ ao[0]                                         # (nao, n)
+    rho0 = (T * ao[0]).sum(dim=0)
+    grad = 2.0 * torch.einsum('mp,dmp->dp', T, ao[1:4])
+    nelec = float((rho0 * w).sum())
+    exc = torch.zeros(n, dtype=torch.float64, device=dev)
+    v0 = torch.zeros_like(exc)
+    v1 = torch.zeros_like(exc)
+    c32 = coords.to(torch.float32)
+    for nlc_pars, fac in nlc_coefs:
+        ind = rho0 >= THRESH
+        q, W0, kappa, dW0dR, dW0dG, dKdR, Beta = vv10_pointwise(
+            rho0[ind], grad[:, ind], w[ind], nlc_pars)
+        F, U, W = ctx.kernel.kernel_sum(c32[ind], q, W0, kappa)
+        exc[ind] += fac * (Beta + 0.5 * F)
+        v0[ind] += fac * (Beta + F + 1.5 * (U * dKdR + W * dW0dR))
+        v1[ind] += fac * (1.5 * W * dW0dG)
+    excsum = float((rho0 * w * exc).sum())
+    wv = torch.empty((4, n), dtype=torch.float64, device=dev)
+    wv[0] = 0.5 * v0 * w                                  # *.5 for vmat + vmat^T
+    wv[1:4] = 2.0 * v1[None, :] * grad * w[None, :]
+    aow = torch.einsum('dmp,dp->mp', ao, wv)
+    vmat = ao[0] @ aow.T
+    vmat = vmat + vmat.T
+    return nelec, excsum, vmat.cpu().numpy()

@@ -128,6 +128,7 @@ def main():
                              dtype='float64', verify=False)
         res['ao_coords'] = aopts
         res['ao'] = ev.eval(aopts - origin, np.arange(mol.nbas), deriv=0)[0]
+        res['ao1'] = ev.eval(aopts - origin, np.arange(mol.nbas), deriv=1)
         np.savez_compressed(os.path.join(HERE, 'int3c1e_%s.npz' % tag), **res)
 
     # -- a K build on a small grid (reference math: dense A contracted) ------
@@ -167,6 +168,28 @@ def main():
     F, U, W = kern.kernel_sum(xyz.astype(np.float32), q, w0, kap)
     np.savez_compressed(os.path.join(HERE, 'vv10.npz'), xyz=xyz, q=q, w0=w0,
                         kappa=kap, F=F, U=U, W=W)
+    # -- the VV10 flow (gpu_nr_nlc_vxc, NumPy backend, FP64 AO and GEMMs) -------
+    mol = Molecule.build(water_dimer(), 'synthetic-svp')
+    rm = RefMol(mol)
+    g = build_grids(mol, level=0)
+    rng = np.random.default_rng(13)
+    sel = np.sort(rng.choice(g.size, 1500, replace=False))
+    origin = mol.atom_coords().mean(axis=0)
+    ev = rao.AoEvaluator(rm, np, pack=rao.ShellPack(rm, origin=origin),
+                         mem_budget=1 << 28, dtype='float64', verify=False)
+    ctx = types.SimpleNamespace(
+        xp=np, blksize=560, origin=origin, evaluator=ev, gemm_dtype='float64',
+        kernel=rvv.Vv10Kernel(np, mem_budget=1 << 24, tile_tol=0.0))
+    grids = types.SimpleNamespace(coords=g.coords[sel], weights=g.weights[sel],
+                                  non0tab=None, mol=None)
+    ni = types.SimpleNamespace(nlc_coeff=lambda xc: [((6.0, 0.01), 1.0)])
+    c = np.zeros((mol.nao, 10))
+    q, _ = np.linalg.qr(rng.normal(size=(mol.nao, 10)))
+    dm = 2.0 * q @ q.T
+    nelec, exc, vmat = rvv.gpu_nr_nlc_vxc(ctx, ni, rm, grids, 'wb97m-v', dm)
+    np.savez_compressed(os.path.join(HERE, 'vv10_flow.npz'), coords=grids.coords,
+                        weights=grids.weights, dm=dm, nelec=nelec, exc=exc,
+                        vmat=vmat, nlc_b=6.0, nlc_c=0.01)
     print('golden fixtures written to', HERE)
 
 

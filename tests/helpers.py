@@ -28,3 +28,23 @@ def grid_subset(mol, level, n, seed=0):
     rng = np.random.default_rng(seed)
     sel = np.sort(rng.choice(g.size, n, replace=False))
     return g.coords[sel], g.weights[sel]
+
+
+def local_density(mol, atoms_per_unit=3, nocc_per_unit=5, seed=0):
+    """D = 2 C C^T with every occupied orbital a random orthonormal mix of
+    the AOs of one molecular unit (e.g. one water): a density that decays
+    between units the way a real cluster density does."""
+    rng = np.random.default_rng(seed)
+    ao = mol.ao_loc_nr()
+    units = {}
+    for s, sh in enumerate(mol.shells):
+        units.setdefault(sh.atom // atoms_per_unit, []).extend(range(ao[s], ao[s + 1]))
+    cols = []
+    for u in sorted(units):
+        idx = np.array(units[u])
+        q, _ = np.linalg.qr(rng.normal(size=(len(idx), nocc_per_unit)))
+        c = np.zeros((mol.nao, nocc_per_unit))
+        c[idx] = q
+        cols.append(c)
+    c = np.hstack(cols)
+    return 2.0 * c @ c.T

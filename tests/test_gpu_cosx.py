@@ -8,7 +8,7 @@ import pytest
 from scipy.special import gamma, gammainc
 
 import oracle
-from helpers import density, dimer, grid_subset, waters
+from helpers import density, dimer, grid_subset, local_density, waters
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
 
@@ -210,11 +210,12 @@ def test_k_tiles_do_not_change_result_beyond_rounding():
 
 @pytest.mark.parametrize('omega', [0.0, 0.3])
 def test_screening_error_and_savings(omega):
-    """Screened (1e-11) vs unscreened on 8 waters: |dK| and |1/4 tr(D dK)|
-    <= 1e-8 and tasks skipped (reference tests/gpu/test_sgx_k.py:226-244)."""
+    """Screened (1e-11) vs unscreened on 8 waters with a per-water localised
+    density: |dK| and |1/4 tr(D dK)| <= 1e-8 and tasks skipped (reference
+    tests/gpu/test_sgx_k.py:226-244, there on a converged water27 density)."""
     mol = waters(8, 7.0, 8)
     coords, weights = grid_subset(mol, 1, 20000, 5)
-    dm = density(mol.nao, 40, 5)
+    dm = local_density(mol, seed=5)
     K0, s0 = _k_gpu(mol, coords, weights, dm, omega, tile_tol=0.0)
     K1, s1 = _k_gpu(mol, coords, weights, dm, omega, tile_tol=1e-11)
     assert s0['pairs_kept'] == s0['pairs_total']
@@ -253,3 +254,16 @@ def test_builder_api_and_out_of_scope():
     asym[0, 1] += 1e-3
     with pytest.raises(Unsupported):
         get_k_only_gpu(b, sgx, asym)
+
+
+def test_screening_error_dense_random_density():
+    """A dense random density (F does not decay) is the hard case for the
+    screen: the error stays below 1e-7 (K elements) and 1e-8 (energy)."""
+    mol = waters(8, 7.0, 8)
+    coords, weights = grid_subset(mol, 1, 20000, 5)
+    dm = density(mol.nao, 40, 5)
+    K0, _ = _k_gpu(mol, coords, weights, dm, 0.0, tile_tol=0.0)
+    K1, s1 = _k_gpu(mol, coords, weights, dm, 0.0, tile_tol=1e-11)
+    assert s1['pairs_kept'] < s1['pairs_total']
+    assert np.max(np.abs(K1 - K0)) < 1e-7
+    assert abs(0.25 * np.einsum('ij,ji->', dm, K1 - K0)) < 1e-8

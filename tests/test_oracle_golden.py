@@ -123,3 +123,23 @@ def test_vv10_matches_reference_kernel_sum():
         rel = np.abs(got - ref) / np.abs(ref)
         assert rel[:500].max() < 1e-6
         assert rel.max() < 1e-5
+
+
+@pytest.mark.parametrize('tag,basis,gen', [('svp', 'synthetic-svp', False),
+                                           ('tzvp', 'synthetic-tzvp', False),
+                                           ('gen', 'synthetic-svp', True)])
+def test_ao_deriv1_matches_reference(tag, basis, gen):
+    d = _load('int3c1e_%s.npz' % tag)
+    X = oracle.ao_eval_deriv1(dimer(basis, gen), d['ao_coords'])
+    assert np.max(np.abs(X - d['ao1'])) < 1e-13 * np.abs(d['ao1']).max()
+
+
+def test_vv10_flow_matches_reference():
+    """The oracle's FP64 VV10 flow vs the reference's gpu_nr_nlc_vxc run on
+    its NumPy backend (FP64 AO and GEMMs, FP32 pair sum)."""
+    d = _load('vv10_flow.npz')
+    n, e, v = oracle.nlc_vxc(dimer(), d['coords'], d['weights'], d['dm'],
+                             [((float(d['nlc_b']), float(d['nlc_c'])), 1.0)])
+    assert abs(n - d['nelec']) < 1e-12
+    assert abs(e - d['exc']) < 1e-9
+    assert np.max(np.abs(v - d['vmat'])) < 1e-9
