@@ -8,8 +8,8 @@
 // One thread per outer point, inner points staged through shared memory in
 // 256-point tiles.  Inside a tile the three sums are FP32 with Kahan
 // compensation, across tiles they accumulate in FP64 in a fixed order: no
-// atomics, bitwise reproducible.  One reciprocal per pair:
-// inv = 1 / (g gp gt), T = q inv, Tu = T gp (g + gt) inv.
+// atomics, bitwise reproducible.  Reciprocals are IEEE round-to-nearest
+// (__frcp_rn): T = q rcp(g gp gt), Tu = T (rcp(g) + rcp(gt)).
 //
 // Distance pruning on the device: per 256-point tile the centroid, radius,
 // sum q, min w0 and min kappa (FP64); a (block, tile) pair is skipped when
@@ -135,9 +135,8 @@ vv10_sum_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
                 const float g = fmaf(r2, w0i, ki);
                 const float gp = fmaf(r2, kj.x, kj.y);
                 const float gt = g + gp;
-                const float inv = __frcp_rn(g * gp * gt);
-                const float T = pj.w * inv;
-                const float Tu = T * (gp * (g + gt)) * inv;
+                const float T = pj.w * __frcp_rn(g * gp * gt);
+                const float Tu = T * (__frcp_rn(g) + __frcp_rn(gt));
                 const float Tw = Tu * r2;
                 float y, s;
                 y = T - fc;  s = fs + y; fc = (s - fs) - y; fs = s;
