@@ -261,7 +261,7 @@ def main():
     ap.add_argument('--steps', type=int, default=5)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    ap.add_argument('--gemm', default='native', choices=['native', 'emulated'])
+    ap.add_argument('--gemm', default='ozaki', choices=['ozaki', 'native', 'emulated'])
     ap.add_argument('--small', action='store_true',
                     help='8 waters / grid level 1 (profiling captures)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
@@ -289,25 +289,27 @@ def main():
     coords_d = eng.relative(g.coords)
     w_d = torch.as_tensor(g.weights, device=dev)
     qd_d = torch.as_tensor(dm, device=dev)
-    emulated = args.gemm == 'emulated'
     K = [torch.empty((mol.nao, mol.nao), dtype=torch.float64, device=dev)
          for _ in OMEGAS]
 
     def step():
         for i, w in enumerate(OMEGAS):
             eng.get_k(coords_d, w_d, qd_d, w, tile_tol=TILE_TOL,
-                      emulated_gemm=emulated, out=K[i], stats=False)
+                      gemm=args.gemm, out=K[i], stats=False)
 
     # one counted call per omega: kept tasks, model flops, launches
     flops_step, launches_step, kept, total = 0.0, 0, 0, 0
+    phases = {}
     for i, w in enumerate(OMEGAS):
         eng.get_k(coords_d, w_d, qd_d, w, tile_tol=TILE_TOL,
-                  emulated_gemm=emulated, out=K[i], stats=True)
+                  gemm=args.gemm, out=K[i], stats=True, profile=True)
         st = eng.last_stats
         flops_step += st['model_flops']
         launches_step += st['kernel_launches']
         kept += st['pairs_kept']
         total += st['pairs_total']
+        for k, v in st['phase_ms'].items():
+            phases[k] = phases.get(k, 0.0) + v
 
     def timed(fn, steps, warmup):
         for _ in range(warmup):
@@ -351,7 +353,7 @@ def main():
         q_d2.copy_(d_h, non_blocking=True)
         for i, w in enumerate(OMEGAS):
             eng.get_k(c_d2, w_d2, q_d2, w, tile_tol=TILE_TOL,
-                      emulated_gemm=emulated, out=K[i], stats=False)
+                      gemm=args.gemm, out=K[i], stats=False)
             Ks = (K[i] + K[i].T) * 0.5
             k_h[i].copy_(Ks, non_blocking=True)
 
@@ -417,6 +419,7 @@ def main():
             'gpu_launches': launches_step * args.steps,
             'tasks_kept': kept, 'tasks_total': total,
             'model_flops_per_step': flops_step,
+            'phases_ms_per_step': phases,
         }
         print(json.dumps(line))
     if world > 1:

@@ -71,6 +71,9 @@ typedef struct wb_cosx_stats {
     double model_flops_class[10];
     int32_t kernel_launches;      /* device kernels launched by the call */
     int32_t reserved;
+    /* with WB_K_PROFILE: device ms per phase, summed over tiles: AO
+     * values, F GEMM, F cast, sub-block stats + G kernels, w o G, K GEMM */
+    double phase_ms[6];
 } wb_cosx_stats;
 
 typedef struct wb_cosx_info {
@@ -87,6 +90,10 @@ typedef struct wb_cosx wb_cosx;   /* opaque per-(molecule, device) handle */
 /* Flags of wb_cosx_get_k */
 #define WB_K_GEMM_NATIVE_FP64 0   /* cuBLAS DGEMM */
 #define WB_K_GEMM_EMULATED_FP64 1 /* cuBLAS FP64 fixed-point emulation */
+#define WB_K_GEMM_OZAKI_BF16 2    /* FP64-accurate Ozaki split on bf16
+                                     tensor cores (7-bit slices, exact
+                                     FP32 level sums, FP64 combination) */
+#define WB_K_PROFILE 4            /* record per-phase CUDA events (stats) */
 
 /* Build the packed shell-pair tables of a molecule on the host (FP64) and
  * upload them to the current device.  origin (3,) is subtracted from every
@@ -135,6 +142,24 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
               int64_t npts, const float* f, double omega, double tile_tol,
               float* g_out, void* workspace, size_t workspace_bytes,
               void* stream, wb_cosx_stats* stats);
+
+/* The two FP64-accurate GEMMs of the K build on the bf16 tensor cores
+ * (Ozaki split, WB_K_GEMM_OZAKI_BF16), callable alone:
+ *   wb_cosx_ozaki_f: f_out (nao, ld) FP32 = fl32(X QD), x (nao, ld) FP64
+ *     AO-major, qd (nao, nao) row-major; needs 5 nao < 4096.
+ *     Replaces F = (X @ proj_dm).astype(float32) (gpu/sgx_k.py:722).
+ *   wb_cosx_ozaki_k: k_out (nao, nao) row-major (+)= X^T (w o G) over npts
+ *     points, g (nao, ld) FP32.  Replaces K += X.T @ (w64 * G)
+ *     (gpu/sgx_k.py:734).
+ * Workspace: wb_ozaki_workspace_bytes(nao, ld) bytes. */
+size_t wb_ozaki_workspace_bytes(int nao, int64_t ld);
+int wb_cosx_ozaki_f(wb_cosx* h, const double* x, const double* qd,
+                    int64_t ld, float* f_out, void* workspace,
+                    size_t workspace_bytes, void* stream);
+int wb_cosx_ozaki_k(wb_cosx* h, const double* x, const float* g,
+                    const double* weights, int64_t npts, int accumulate,
+                    double* k_out, void* workspace, size_t workspace_bytes,
+                    void* stream);
 
 /* AO values X (nao, ldp) FP64 AO-major at npts points (FP64 arithmetic).
  * Replaces AoEvaluator.eval(deriv=0) with dtype FP64 (gpu/ao_eval.py:186-329). */

@@ -24,6 +24,12 @@ WB_ERR_NO_DEVICE = 7
 
 WB_K_GEMM_NATIVE_FP64 = 0
 WB_K_GEMM_EMULATED_FP64 = 1
+WB_K_GEMM_OZAKI_BF16 = 2
+WB_K_PROFILE = 4
+GEMM_MODES = {'native': WB_K_GEMM_NATIVE_FP64,
+              'emulated': WB_K_GEMM_EMULATED_FP64,
+              'ozaki': WB_K_GEMM_OZAKI_BF16}
+PHASES = ('ao', 'f_gemm', 'f_cast', 'g', 'weight_g', 'k_gemm')
 
 NCLASS = 10
 
@@ -32,7 +38,9 @@ EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_cosx_get_k', 'wb_cosx_g', 'wb_ao_eval', 'wb_ao_eval_deriv1',
             'wb_int3c1e_dense',
             'wb_boys_fp32', 'wb_boys_f64_host', 'wb_vv10_kernel_sum',
-            'wb_becke_partition', 'wb_fp32_fma_probe', 'wb_status_string',
+            'wb_becke_partition', 'wb_fp32_fma_probe',
+            'wb_ozaki_workspace_bytes', 'wb_cosx_ozaki_f', 'wb_cosx_ozaki_k',
+            'wb_status_string',
             'wb_last_error', 'wb_version')
 
 
@@ -72,7 +80,8 @@ class WbCosxStats(ctypes.Structure):
                 ('integrals', ctypes.c_double), ('model_flops', ctypes.c_double),
                 ('tasks_kept_class', ctypes.c_int64 * NCLASS),
                 ('model_flops_class', ctypes.c_double * NCLASS),
-                ('kernel_launches', ctypes.c_int32), ('reserved', ctypes.c_int32)]
+                ('kernel_launches', ctypes.c_int32), ('reserved', ctypes.c_int32),
+                ('phase_ms', ctypes.c_double * 6)]
 
     def as_dict(self):
         return {'pairs_total': int(self.tasks_total),
@@ -81,7 +90,8 @@ class WbCosxStats(ctypes.Structure):
                 'model_flops': float(self.model_flops),
                 'kept_class': [int(x) for x in self.tasks_kept_class],
                 'flops_class': [float(x) for x in self.model_flops_class],
-                'kernel_launches': int(self.kernel_launches)}
+                'kernel_launches': int(self.kernel_launches),
+                'phase_ms': dict(zip(PHASES, [float(x) for x in self.phase_ms]))}
 
 
 class WbCosxInfo(ctypes.Structure):
@@ -121,6 +131,10 @@ def _declare(lib):
                                       ctypes.POINTER(_I64)]),
         'wb_becke_partition': (_INT, [_P, _I64, _P, _P, _INT, _P]),
         'wb_fp32_fma_probe': (_INT, [_I64, _P, _I64, _P, ctypes.POINTER(_D)]),
+        'wb_ozaki_workspace_bytes': (ctypes.c_size_t, [_INT, _I64]),
+        'wb_cosx_ozaki_f': (_INT, [_P, _P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
+        'wb_cosx_ozaki_k': (_INT, [_P, _P, _P, _P, _I64, _INT, _P, _P,
+                                   ctypes.c_size_t, _P]),
         'wb_status_string': (ctypes.c_char_p, [_INT]),
         'wb_last_error': (ctypes.c_char_p, []),
         'wb_version': (_INT, []),

@@ -23,7 +23,7 @@ LIBNAME = 'libwb97mv_gb300.so'
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 SOURCES = ['cosx_kernels_spd.cu', 'cosx_kernels_f.cu', 'aux_kernels.cu',
-           'vv10.cu', 'capi.cu', 'host_pairs.cpp']
+           'vv10.cu', 'ozaki.cu', 'capi.cu', 'host_pairs.cpp']
 
 
 def cuda_home():

@@ -126,10 +126,13 @@ class CosxEngine:
 
     # -- entry points ---------------------------------------------------------
     def get_k(self, coords_rel, weights, qd, omega, tile_tol=1e-11,
-              tile_pts=0, emulated_gemm=False, out=None, stats=True):
+              tile_pts=0, gemm='ozaki', out=None, stats=True,
+              profile=False):
         """Unsymmetrised K = X^T (w o G) (nao, nao) FP64 on the device.
         coords_rel (npts, 3) FP64 device (kernel frame), weights (npts,) FP64
-        device, qd (nao, nao) FP64 device = proj @ dm."""
+        device, qd (nao, nao) FP64 device = proj @ dm.  gemm: 'ozaki'
+        (FP64-accurate split on the bf16 tensor cores, default), 'native'
+        (cuBLAS DGEMM) or 'emulated' (cuBLAS FP64 emulation)."""
         torch = _torch()
         npts = int(coords_rel.shape[0])
         nbytes = self.workspace_bytes(npts, tile_pts)
@@ -138,8 +141,9 @@ class CosxEngine:
             out = torch.empty((self.nao, self.nao), dtype=torch.float64,
                               device=self.device)
         st = _native.WbCosxStats() if stats else None
-        flags = (_native.WB_K_GEMM_EMULATED_FP64 if emulated_gemm
-                 else _native.WB_K_GEMM_NATIVE_FP64)
+        flags = _native.GEMM_MODES[gemm]
+        if profile and stats:
+            flags |= _native.WB_K_PROFILE
         _native.check(_native.lib().wb_cosx_get_k(
             self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
             _native.ptr(qd.contiguous()), float(omega), float(tile_tol),
@@ -172,6 +176,35 @@ class CosxEngine:
             _native.ctypes.byref(st) if st is not None else None), 'wb_cosx_g')
         if st is not None:
             self.last_stats = st.as_dict()
+        return out
+
+    def ozaki_f(self, X, qd):
+        """F (nao, ld) FP32 = fl32(X QD) through the bf16 Ozaki split."""
+        torch = _torch()
+        ld = int(X.shape[1])
+        nbytes = int(_native.lib().wb_ozaki_workspace_bytes(self.nao, ld))
+        ws = self.workspace(nbytes)
+        out = torch.empty((self.nao, ld), dtype=torch.float32, device=self.device)
+        _native.check(_native.lib().wb_cosx_ozaki_f(
+            self._h, _native.ptr(X), _native.ptr(qd.contiguous()), ld,
+            _native.ptr(out), _native.ptr(ws), nbytes, self._stream()),
+            'wb_cosx_ozaki_f')
+        return out
+
+    def ozaki_k(self, X, G, weights, out=None, accumulate=False):
+        """K (nao, nao) FP64 = X^T (w o G) through the bf16 Ozaki split."""
+        torch = _torch()
+        npts = int(weights.shape[0])
+        ld = int(X.shape[1])
+        nbytes = int(_native.lib().wb_ozaki_workspace_bytes(self.nao, ld))
+        ws = self.workspace(nbytes)
+        if out is None:
+            out = torch.zeros((self.nao, self.nao), dtype=torch.float64,
+                              device=self.device)
+        _native.check(_native.lib().wb_cosx_ozaki_k(
+            self._h, _native.ptr(X), _native.ptr(G), _native.ptr(weights), npts,
+            1 if accumulate else 0, _native.ptr(out), _native.ptr(ws), nbytes,
+            self._stream()), 'wb_cosx_ozaki_k')
         return out
 
     def ao_eval(self, coords_rel, out=None):

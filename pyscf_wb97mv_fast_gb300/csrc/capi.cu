@@ -14,6 +14,7 @@
 
 #include "host.hpp"
 #include "launch.hpp"
+#include "ozaki.hpp"
 #include "wb97mv_gb300.h"
 
 namespace {
@@ -126,7 +127,7 @@ namespace {
 
 struct WsLayout {
     size_t om = 0, gh = 0, gl = 0, subcr = 0, msh = 0, counters = 0, work = 0;
-    size_t X = 0, F64 = 0, F32 = 0, G32 = 0, total = 0;
+    size_t X = 0, F64 = 0, F32 = 0, G32 = 0, oz = 0, total = 0;
 };
 
 WsLayout ws_layout(const wb_cosx* h, int64_t ldt, bool full) {
@@ -148,9 +149,15 @@ WsLayout ws_layout(const wb_cosx* h, int64_t ldt, bool full) {
     L.msh = take(sizeof(float) * (size_t)nsub * std::max(h->hp.nvshell, 1));
     if (full) {
         L.X = take(sizeof(double) * (size_t)nao * ldt);
-        L.F64 = take(sizeof(double) * (size_t)nao * ldt);
         L.F32 = take(sizeof(float) * (size_t)nao * ldt);
         L.G32 = take(sizeof(float) * (size_t)nao * ldt);
+        // scratch shared by the FP64 DGEMM path (F64 / w o G) and the
+        // bf16 Ozaki path (slices, level outputs): never live together
+        const size_t dg = sizeof(double) * (size_t)nao * ldt;
+        const size_t oz = std::max(wb::ozaki_f_bytes(nao, ldt),
+                                   wb::ozaki_k_bytes(nao, ldt));
+        L.F64 = take(std::max(dg, oz));
+        L.oz = L.F64;
     }
     L.total = off;
     return L;
@@ -458,7 +465,10 @@ int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
         return fail(WB_ERR_WORKSPACE, "wb_cosx_get_k: workspace needs " +
                                           std::to_string(L.total) + " bytes");
     WB_CUBLAS(cublasSetStream(h->cublas, s));
-    if (flags & WB_K_GEMM_EMULATED_FP64) {
+    const int gemm_mode = flags & 3;
+    const bool oz_f = gemm_mode == WB_K_GEMM_OZAKI_BF16 && wb::ozaki_f_supported(nao);
+    const bool oz_k = gemm_mode == WB_K_GEMM_OZAKI_BF16;
+    if (gemm_mode == WB_K_GEMM_EMULATED_FP64) {
         WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_FP64_EMULATED_FIXEDPOINT_MATH));
         WB_CUBLAS(cublasSetEmulationStrategy(h->cublas, CUBLAS_EMULATION_STRATEGY_EAGER));
     } else {
@@ -479,6 +489,22 @@ int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
     float* G32 = at<float>(workspace, L.G32);
     int64_t ntasks = 0;
     const double one = 1.0, zero = 0.0;
+    const bool prof = (flags & WB_K_PROFILE) && stats;
+    cudaEvent_t ev[7] = {};
+    double phase[6] = {0, 0, 0, 0, 0, 0};
+    if (prof)
+        for (int i = 0; i < 7; ++i) WB_CUDA(cudaEventCreate(&ev[i]));
+    auto mark = [&](int i) { if (prof) cudaEventRecord(ev[i], s); };
+    auto collect = [&]() -> int {
+        if (!prof) return WB_OK;
+        WB_CUDA(cudaEventSynchronize(ev[6]));
+        for (int i = 0; i < 6; ++i) {
+            float ms = 0.0f;
+            WB_CUDA(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+            phase[i] += ms;
+        }
+        return WB_OK;
+    };
     for (int64_t i0 = 0; i0 < npts; i0 += tile) {
         const int64_t nt = std::min(tile, npts - i0);
         const int64_t ldt = round32(nt);
@@ -490,26 +516,59 @@ int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
         ao.sh_eoff = h->sh_eoff; ao.sh_coff = h->sh_coff; ao.sh_ao0 = h->sh_ao0;
         ao.sh_ctr = h->sh_ctr; ao.exps = h->exps; ao.coeffs = h->coeffs; ao.X = X;
         ao.nao = nao;
+        mark(0);
         WB_CUDA(wb::launch_ao_eval(ao, s));
-        // F(g, mu) = sum_l X(g, l) QD(l, mu); QD row-major = col-major QD^T
-        WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)ldt, nao,
-                              nao, &one, X, (int)ldt, qd, nao, &zero, F64,
-                              (int)ldt));
-        WB_CUDA(wb::launch_f64_to_f32(F64, F32, (int64_t)nao * ldt, s));
-        launches += 3;
+        mark(1);
+        if (oz_f) {
+            const int r = wb::ozaki_f_gemm(h->cublas, X, qd, nao, ldt, F32,
+                                           at<void>(workspace, L.oz), s);
+            if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
+                               "ozaki F GEMM failed, code " + std::to_string(r));
+            mark(2);
+            launches += 2 + 5;
+        } else {
+            // F(g, mu) = sum_l X(g, l) QD(l, mu); QD row-major = col-major QD^T
+            WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)ldt,
+                                  nao, nao, &one, X, (int)ldt, qd, nao, &zero,
+                                  F64, (int)ldt));
+            mark(2);
+            WB_CUDA(wb::launch_f64_to_f32(F64, F32, (int64_t)nao * ldt, s));
+            launches += 2;
+        }
+        launches += 1;
+        mark(3);
         int st = run_g_tile(h, c, w, nt, ldt, F32, G32, tile_tol, workspace, L,
                             s, &launches);
         if (st != WB_OK) return st;
         ntasks += (ldt / 32) * (int64_t)h->hp.npairs;
-        WB_CUDA(wb::launch_weight_g(G32, w, nt, ldt, nao, F64, s));
-        // K(mu, nu) += sum_g X(g, mu) WG(g, nu); written row-major
-        const double* beta = i0 == 0 ? &zero : &one;
-        WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nao, nao,
-                              (int)ldt, &one, F64, (int)ldt, X, (int)ldt, beta,
-                              k_out, nao));
-        launches += 2;
+        mark(4);
+        if (oz_k) {
+            mark(5);
+            const int r = wb::ozaki_k_gemm(h->cublas, X, G32, w, nao, ldt, nt,
+                                           i0 == 0 ? 0 : 1, k_out,
+                                           at<void>(workspace, L.oz), s);
+            if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
+                               "ozaki K GEMM failed, code " + std::to_string(r));
+            launches += 2 + 5;
+        } else {
+            WB_CUDA(wb::launch_weight_g(G32, w, nt, ldt, nao, F64, s));
+            mark(5);
+            // K(mu, nu) += sum_g X(g, mu) WG(g, nu); written row-major
+            const double* beta = i0 == 0 ? &zero : &one;
+            WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nao, nao,
+                                  (int)ldt, &one, F64, (int)ldt, X, (int)ldt,
+                                  beta, k_out, nao));
+            launches += 2;
+        }
+        mark(6);
+        if ((st = collect()) != WB_OK) return st;
     }
-    return read_stats(h, workspace, L, ntasks, s, stats, launches);
+    if (prof)
+        for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
+    int st = read_stats(h, workspace, L, ntasks, s, stats, launches);
+    if (st == WB_OK && prof)
+        for (int i = 0; i < 6; ++i) stats->phase_ms[i] = phase[i];
+    return st;
 }
 
 int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
@@ -536,6 +595,51 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
     if (st != WB_OK) return st;
     return read_stats(h, workspace, L, (ldt / 32) * (int64_t)h->hp.npairs, s,
                       stats, launches);
+}
+
+size_t wb_ozaki_workspace_bytes(int nao, int64_t ld) {
+    if (nao <= 0 || ld <= 0) return 0;
+    return std::max(wb::ozaki_f_bytes(nao, ld), wb::ozaki_k_bytes(nao, ld));
+}
+
+int wb_cosx_ozaki_f(wb_cosx* h, const double* x, const double* qd,
+                    int64_t ld, float* f_out, void* workspace,
+                    size_t workspace_bytes, void* stream) {
+    if (!h || !x || !qd || !f_out || ld <= 0 || ld % 32)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_ozaki_f: bad arguments");
+    const int nao = h->hp.nao;
+    if (!wb::ozaki_f_supported(nao))
+        return fail(WB_ERR_UNSUPPORTED, "wb_cosx_ozaki_f: nao too large for one "
+                                        "exact FP32 level sum");
+    if (!workspace || workspace_bytes < wb::ozaki_f_bytes(nao, ld))
+        return fail(WB_ERR_WORKSPACE, "wb_cosx_ozaki_f: workspace too small");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    WB_CUBLAS(cublasSetStream(h->cublas, s));
+    WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+    const int r = wb::ozaki_f_gemm(h->cublas, x, qd, nao, ld, f_out, workspace, s);
+    if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
+                       "ozaki F GEMM failed, code " + std::to_string(r));
+    return WB_OK;
+}
+
+int wb_cosx_ozaki_k(wb_cosx* h, const double* x, const float* g,
+                    const double* weights, int64_t npts, int accumulate,
+                    double* k_out, void* workspace, size_t workspace_bytes,
+                    void* stream) {
+    if (!h || !x || !g || !weights || !k_out || npts <= 0)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_ozaki_k: bad arguments");
+    const int nao = h->hp.nao;
+    const int64_t ld = round32(npts);
+    if (!workspace || workspace_bytes < wb::ozaki_k_bytes(nao, ld))
+        return fail(WB_ERR_WORKSPACE, "wb_cosx_ozaki_k: workspace too small");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    WB_CUBLAS(cublasSetStream(h->cublas, s));
+    WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+    const int r = wb::ozaki_k_gemm(h->cublas, x, g, weights, nao, ld, npts,
+                                   accumulate, k_out, workspace, s);
+    if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
+                       "ozaki K GEMM failed, code " + std::to_string(r));
+    return WB_OK;
 }
 
 int wb_ao_eval(const wb_cosx* h, const double* coords, int64_t npts,

@@ -63,7 +63,7 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
                 gemm_dtype='float64', dtype='float32',
                 mem_fraction=DEFAULT_MEM_FRACTION, overlap=False,
                 semilocal=False, k=True, k_tile_tol=1e-11,
-                openblas_threads=None, vv10=True, k_gemm='native',
+                openblas_threads=None, vv10=True, k_gemm='ozaki',
                 sgx_jk_module=None):
     """Hook the GPU COSX K (and VV10) into mf; returns a HookSet.
 

@@ -63,19 +63,20 @@ class GpuKBuilder:
     blksize: grid points per native call (None: as many as the memory
     budget allows; the reference tiles by SMs x 32 warps x 32 points
     because its target cards have 8-24 GB).
-    gemm: 'native' (cuBLAS DGEMM) or 'emulated' (cuBLAS FP64 emulation).
+    gemm: 'ozaki' (FP64-accurate split on the bf16 tensor cores, default),
+    'native' (cuBLAS DGEMM) or 'emulated' (cuBLAS FP64 emulation).
     """
 
     def __init__(self, mol, device=None, tile_tol=1e-11, mem_budget=None,
-                 origin=None, blksize=None, gemm='native'):
+                 origin=None, blksize=None, gemm='ozaki'):
         self.mol = mol
         self.tile_tol = float(tile_tol)
         self.origin = origin
         self.device = device
         self.mem_budget = mem_budget
         self.blksize = None if blksize is None else int(blksize)
-        if gemm not in ('native', 'emulated'):
-            raise ValueError("gemm must be 'native' or 'emulated'")
+        if gemm not in ('ozaki', 'native', 'emulated'):
+            raise ValueError("gemm must be 'ozaki', 'native' or 'emulated'")
         self.gemm = gemm
         self.engine = None
         self._grids_states = {}
@@ -162,7 +163,7 @@ class GpuKBuilder:
         K = self.engine.get_k(state.coords, state.weights, qd, omega,
                               tile_tol=self.tile_tol,
                               tile_pts=self._tile(state.ngrids),
-                              emulated_gemm=(self.gemm == 'emulated'))
+                              gemm=self.gemm)
         if sym:
             K = proj_d.T @ K
         K = (K + K.T) * 0.5

@@ -153,14 +153,16 @@ def test_g_kernels_bitwise_reproducible():
 
 # -- full K build vs the oracle and the reference --------------------------------
 
-def _k_gpu(mol, coords, weights, dm, omega, tile_tol=0.0, tile_pts=0):
+def _k_gpu(mol, coords, weights, dm, omega, tile_tol=0.0, tile_pts=0,
+           gemm='ozaki'):
     torch = _torch()
     from pyscf_wb97mv_fast_gb300.cosx import CosxEngine
     eng = CosxEngine(mol)
     c = eng.relative(coords)
     w = torch.as_tensor(weights, device=eng.device)
     qd = torch.as_tensor(dm, device=eng.device)
-    K = eng.get_k(c, w, qd, omega, tile_tol=tile_tol, tile_pts=tile_pts)
+    K = eng.get_k(c, w, qd, omega, tile_tol=tile_tol, tile_pts=tile_pts,
+                  gemm=gemm)
     K = ((K + K.T) * 0.5).cpu().numpy()
     return K, eng.last_stats
 
@@ -272,19 +274,46 @@ def test_screening_error_dense_random_density():
     assert abs(0.25 * np.einsum('ij,ji->', dm, K1 - K0)) < 1e-8
 
 
+@pytest.mark.parametrize('gemm', ['ozaki', 'emulated'])
 @pytest.mark.parametrize('omega', [0.0, 0.3])
-def test_emulated_fp64_gemms_match_native(omega):
-    """cuBLAS FP64 fixed-point emulation for F = X QD and K = X^T (w G):
-    same K as the native DGEMMs to 1e-11 relative, and the oracle gate."""
-    torch = _torch()
-    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine
+def test_gemm_modes_match_native_fp64(omega, gemm):
+    """The Ozaki bf16 split (default) and cuBLAS FP64 emulation for
+    F = X QD and K = X^T (w G) give the K of the native DGEMMs: the F
+    roundings to FP32 agree except on rare ties (one ulp), so K agrees to
+    FP32-noise level, far inside the oracle gate."""
     mol = waters(4, 5.0, 4)
     coords, weights = grid_subset(mol, 1, 30000, 2)
     dm = density(mol.nao, 20, 2)
+    Kn, _ = _k_gpu(mol, coords, weights, dm, omega, gemm='native')
+    Ke, st = _k_gpu(mol, coords, weights, dm, omega, gemm=gemm)
+    assert np.max(np.abs(Ke - Kn)) < 1e-9 * np.abs(Kn).max()
+    assert abs(0.25 * np.einsum('ij,ji->', dm, Ke - Kn)) < 1e-10
+
+
+def test_ozaki_gemms_are_fp64_accurate():
+    """The two Ozaki GEMMs alone against FP64 torch GEMMs on the same
+    device operands: F bit-identical to fl32(X QD) on > 99.9 % of the
+    entries (the rest one ulp), K = X^T (w G) to 1e-12 relative."""
+    torch = _torch()
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine
+    mol = waters(6, 6.0, 6)
+    coords, weights = grid_subset(mol, 1, 40000, 3)
+    dm = density(mol.nao, 30, 3)
     eng = CosxEngine(mol)
     c = eng.relative(coords)
     w = torch.as_tensor(weights, device=eng.device)
     qd = torch.as_tensor(dm, device=eng.device)
-    Kn = eng.get_k(c, w, qd, omega, tile_tol=0.0).cpu().numpy()
-    Ke = eng.get_k(c, w, qd, omega, tile_tol=0.0, emulated_gemm=True).cpu().numpy()
-    assert np.max(np.abs(Ke - Kn)) < 1e-11 * np.abs(Kn).max()
+    X = eng.ao_eval(c)
+    F_ref = (qd.T @ X).to(torch.float32)
+    F_oz = eng.ozaki_f(X, qd)
+    same = (F_oz == F_ref).double().mean().item()
+    assert same > 0.999, same
+    ulp = (F_oz.view(torch.int32) - F_ref.view(torch.int32)).abs().max().item()
+    assert ulp <= 1
+    G = torch.randn(X.shape, dtype=torch.float32, device=eng.device)
+    n = c.shape[0]
+    G[:, n:] = 0
+    K_oz = eng.ozaki_k(X, G, w)
+    wG = G.double() * torch.nn.functional.pad(w, (0, X.shape[1] - n))[None, :]
+    K_ref = X @ wG.T
+    assert (K_oz - K_ref).abs().max().item() < 1e-12 * K_ref.abs().max().item()

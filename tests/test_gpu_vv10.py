@@ -32,9 +32,10 @@ def _points(n, seed):
 
 
 def test_kernel_sum_matches_fp64_bruteforce():
-    """Relative error <= 1e-6 on F, U, W; 1100 points: several 256-point
-    tiles and a ragged tail."""
-    c, q, w0, k = _points(1100, 0)
+    """Relative error <= 1e-6 on F, U, W against the FP64 sum of the same
+    (FP32-representable) inputs; 1100 points: several 256-point tiles and a
+    ragged tail."""
+    c, q, w0, k = (a.astype(np.float32).astype(np.float64) for a in _points(1100, 0))
     (F, U, W), kept = _kernel_sum(c, q, w0, k)
     ref = oracle.vv10_sum(c, q, w0, k)
     for got, r, name in zip((F, U, W), ref, 'FUW'):
