@@ -6,18 +6,20 @@
 // split (K. Ozaki et al., Numer. Algorithms 59 (2012) 95-118; on tensor
 // cores: H. Ootomo, K. Ozaki, R. Yokota, IJHPCA 2024):
 //
-//   x = 2^e sum_i d_i 2^(-6-7i),   d_i integer in [-64, 64]   (bf16-exact)
+//   x = 2^(e-W+1) sum_i d_i 2^(B (S-1-i)),  |d_i| <= 2^(B-1)  (bf16-exact)
 //
-// with e per row / column (chunk), digits by round-to-nearest, s slices.
+// with e per row / column (chunk), B = 6-bit balanced digits, S = 7 slices
+// (W = 42 bits), the digits cut from rint(x 2^(W-1-e)) with integer ops.
 // A product level l = i + j collects sum_{i+j=l} A_i B_j in ONE bf16 GEMM
 // with FP32 accumulation: storing the A slices ascending and the B slices
 // descending along K makes every level a prefix of A times a suffix of B.
-// Every product is an integer of magnitude <= 2^12 and a level sums at most
-// (l+1) * Kc of them, so with (l+1) Kc <= 4096 every partial sum is an
-// integer below 2^24: the FP32 accumulation is exact, whatever order the
-// tensor cores use.  Levels are combined in FP64 (ldexp, exact scaling).
-// The result carries ~7s bits relative to the per-row/column maxima; the
-// truncated products (i + j >= s) are below 2^(-7s) of them.
+// Every product is an integer of magnitude <= 2^(2B-2) = 1024 and a level
+// sums at most (l+1) * Kc of them, so with (l+1) Kc < 2^14 every partial
+// sum is an integer below 2^24: the FP32 accumulation is exact, whatever
+// order the tensor cores use.  Levels are combined exactly in int64 and
+// scaled once in FP64.  The result carries W = 42 bits relative to the
+// per-row / per-column maxima; the truncated products (i + j >= S) are
+// below 2^-W of them.
 //
 // The bf16 GEMMs themselves are plain library GEMMs (cuBLAS, bf16 in, FP32
 // accumulate); the slicing, the per-chunk scaling and the FP64 level
@@ -32,24 +34,52 @@
 
 namespace wb {
 
-__device__ __forceinline__ int exp_of_max(double m) {
-    // smallest e with m < 2^e (0 for m == 0)
-    if (!(m > 0.0)) return 0;
-    int e;
-    frexp(m, &e);          // m = f 2^e, f in [0.5, 1)
-    return e;
+// Fixed-point digits.  A value x with |x| < 2^e becomes the integer
+// q = rint(x 2^(W - 1 - e)), W = B S bits, |q| < 2^(W-1), written as
+// balanced base-2^B digits q = sum_i d_i 2^(B (S-1-i)), |d_i| <= 2^(B-1),
+// extracted from the least significant end with integer arithmetic only
+// (the one FP64 multiply by an exact power of two and one FP64 -> int64
+// conversion per element are the only FP64 operations).
+constexpr int kB = kOzBits;
+constexpr int kW = kOzBits * kOzSlices;
+
+__device__ __forceinline__ double pow2(int k) {
+    // exact 2^k for -1022 <= k <= 1023
+    return __longlong_as_double((long long)(1023 + k) << 52);
 }
 
-// digits of x (|x| < 2^e) -> s values in [-64, 64]
+__device__ __forceinline__ int exp_of_bits(unsigned long long absbits) {
+    // smallest e with |x| < 2^e from the bit pattern of |x|, clamped to
+    // [-400, 500]: rows whose largest entry is below 2^-400 are zero at this
+    // precision, and the clamp keeps every scale factor 2^k of the kernels
+    // (|k| <= 2 * 500 + 84) inside the normal FP64 range of pow2()
+    const int ebits = (int)(absbits >> 52);
+    int e = ebits - 1022;                           // |x| < 2^(ebits-1023+1)
+    if (absbits == 0ull || e < -400) e = -400;
+    return e > 500 ? 500 : e;
+}
+
 template<int S>
 __device__ __forceinline__ void digits(double x, int e, float* d) {
-    double r = ldexp(x, 6 - e);                 // |r| < 64
+    long long q = __double2ll_rn(x * pow2(kW - 1 - e));
+    const long long half = 1ll << (kB - 1), mask = (1ll << kB) - 1;
 #pragma unroll
-    for (int i = 0; i < S; ++i) {
-        const double q = rint(r);
-        d[i] = (float)q;
-        r = (r - q) * 128.0;
+    for (int i = S - 1; i >= 1; --i) {
+        const long long di = ((q + half) & mask) - half;
+        d[i] = (float)di;
+        q = (q - di) >> kB;
     }
+    d[0] = (float)q;
+}
+
+// value of the combined levels: sum_l C_l 2^(B (S-1-l)) as an exact int64
+template<int S>
+__device__ __forceinline__ long long combine_levels(const float* c) {
+    long long acc = 0;
+#pragma unroll
+    for (int l = 0; l < S; ++l)
+        acc += ((long long)__float2ll_rn(c[l])) << (kB * (S - 1 - l));
+    return acc;
 }
 
 // ---------------------------------------------------------------------------
@@ -65,9 +95,14 @@ __global__ void f_slice_x_kernel(const double* __restrict__ X, int nao,
                                  __nv_bfloat16* __restrict__ A) {
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ld) return;
-    double m = 0.0;
-    for (int l = 0; l < nao; ++l) m = fmax(m, fabs(X[(int64_t)l * ld + g]));
-    const int e = exp_of_max(m);
+    unsigned long long m = 0;
+    for (int l = 0; l < nao; ++l) {
+        const unsigned long long b =
+            (unsigned long long)__double_as_longlong(X[(int64_t)l * ld + g]) &
+            0x7fffffffffffffffull;
+        m = b > m ? b : m;
+    }
+    const int e = exp_of_bits(m);
     erow[g] = e;
     for (int l = 0; l < nao; ++l) {
         float d[S];
@@ -84,17 +119,22 @@ __global__ void f_slice_qd_kernel(const double* __restrict__ QD, int nao,
                                   __nv_bfloat16* __restrict__ B) {
     // one block per column mu of B = Q^T, i.e. QD(:, mu)
     const int mu = blockIdx.x;
-    __shared__ double red[256];
-    double m = 0.0;
-    for (int l = threadIdx.x; l < nao; l += blockDim.x)
-        m = fmax(m, fabs(QD[(int64_t)l * nao + mu]));
+    __shared__ unsigned long long red[256];
+    unsigned long long m = 0;
+    for (int l = threadIdx.x; l < nao; l += blockDim.x) {
+        const unsigned long long b =
+            (unsigned long long)__double_as_longlong(QD[(int64_t)l * nao + mu]) &
+            0x7fffffffffffffffull;
+        m = b > m ? b : m;
+    }
     red[threadIdx.x] = m;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        if (threadIdx.x < s && red[threadIdx.x + s] > red[threadIdx.x])
+            red[threadIdx.x] = red[threadIdx.x + s];
         __syncthreads();
     }
-    const int e = exp_of_max(red[0]);
+    const int e = exp_of_bits(red[0]);
     if (threadIdx.x == 0) ecol[mu] = e;
     const int64_t ldb = (int64_t)S * nao;
     for (int l = threadIdx.x; l < nao; l += blockDim.x) {
@@ -107,7 +147,8 @@ __global__ void f_slice_qd_kernel(const double* __restrict__ QD, int nao,
     }
 }
 
-// F32[mu, g] = fl32( sum_l C_l[mu, g] 2^(e_g + f_mu - 12 - 7 l) )
+// x y = 2^(e+f-2W+2) sum_l C_l 2^(B (2S-2-l))
+//     = 2^(e+f-2W+2+B(S-1)) * [sum_l C_l 2^(B (S-1-l))]
 template<int S>
 __global__ void f_combine_kernel(const float* __restrict__ C, int nao,
                                  int64_t ld, const int* __restrict__ erow,
@@ -117,12 +158,12 @@ __global__ void f_combine_kernel(const float* __restrict__ C, int nao,
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < plane;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t mu = i / ld, g = i - mu * ld;
-        const int base = erow[g] + ecol[mu] - 12;
-        double acc = 0.0;
+        float c[S];
 #pragma unroll
-        for (int l = S - 1; l >= 0; --l)
-            acc += ldexp((double)C[(int64_t)l * plane + i], base - 7 * l);
-        F[i] = __double2float_rn(acc);
+        for (int l = 0; l < S; ++l) c[l] = C[(int64_t)l * plane + i];
+        const long long acc = combine_levels<S>(c);
+        const int sc = erow[g] + ecol[mu] - 2 * kW + 2 + kB * (S - 1);
+        F[i] = __double2float_rn((double)acc * pow2(sc));
     }
 }
 
@@ -132,52 +173,67 @@ __global__ void f_combine_kernel(const float* __restrict__ C, int nao,
 // B_c(k, nu) = w_k G[nu, c KC + k]; layouts (col-major, ld = S KC):
 //   A: column mu = [slice 0 (KC) | slice 1 | ... ]     (ascending)
 //   B: column nu = [slice S-1 | ... | slice 0]          (descending)
-// chunk stride S KC nao.  One CTA per (chunk, column), KC threads.
+// chunk stride S KC nao.  One CTA of 256 threads per (chunk, column).
 // ---------------------------------------------------------------------------
 template<int S, int KC>
-__global__ void k_slice_kernel(const double* __restrict__ X,
-                               const float* __restrict__ G,
-                               const double* __restrict__ w, int nao,
-                               int64_t ld, int64_t npts, int nchunk,
-                               int* __restrict__ ex, int* __restrict__ ew,
-                               __nv_bfloat16* __restrict__ A,
-                               __nv_bfloat16* __restrict__ B) {
+__global__ void __launch_bounds__(256)
+k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
+               const double* __restrict__ w, int nao, int64_t ld,
+               int64_t npts, int* __restrict__ ex, int* __restrict__ ew,
+               __nv_bfloat16* __restrict__ A, __nv_bfloat16* __restrict__ B) {
+    constexpr int PER = KC / 256;
     const int c = blockIdx.x, col = blockIdx.y;
-    const int k = threadIdx.x;
-    const int64_t g = (int64_t)c * KC + k;
-    __shared__ double rx[KC], rw[KC];
-    double xv = 0.0, wv = 0.0;
-    if (g < npts) {
-        xv = X[(int64_t)col * ld + g];
-        wv = w[g] * (double)G[(int64_t)col * ld + g];
+    __shared__ unsigned long long rx[256], rw[256];
+    double xv[PER], wv[PER];
+    unsigned long long mx = 0, mw = 0;
+#pragma unroll
+    for (int r = 0; r < PER; ++r) {
+        const int k = r * 256 + threadIdx.x;
+        const int64_t g = (int64_t)c * KC + k;
+        xv[r] = 0.0;
+        wv[r] = 0.0;
+        if (g < npts) {
+            xv[r] = X[(int64_t)col * ld + g];
+            wv[r] = w[g] * (double)G[(int64_t)col * ld + g];
+        }
+        const unsigned long long bx =
+            (unsigned long long)__double_as_longlong(xv[r]) & 0x7fffffffffffffffull;
+        const unsigned long long bw =
+            (unsigned long long)__double_as_longlong(wv[r]) & 0x7fffffffffffffffull;
+        mx = bx > mx ? bx : mx;
+        mw = bw > mw ? bw : mw;
     }
-    rx[k] = fabs(xv);
-    rw[k] = fabs(wv);
+    rx[threadIdx.x] = mx;
+    rw[threadIdx.x] = mw;
     __syncthreads();
-    for (int s = KC / 2; s > 0; s >>= 1) {
-        if (k < s) {
-            rx[k] = fmax(rx[k], rx[k + s]);
-            rw[k] = fmax(rw[k], rw[k + s]);
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            if (rx[threadIdx.x + s] > rx[threadIdx.x]) rx[threadIdx.x] = rx[threadIdx.x + s];
+            if (rw[threadIdx.x + s] > rw[threadIdx.x]) rw[threadIdx.x] = rw[threadIdx.x + s];
         }
         __syncthreads();
     }
-    const int e1 = exp_of_max(rx[0]), e2 = exp_of_max(rw[0]);
-    if (k == 0) {
+    const int e1 = exp_of_bits(rx[0]), e2 = exp_of_bits(rw[0]);
+    if (threadIdx.x == 0) {
         ex[(int64_t)c * nao + col] = e1;
         ew[(int64_t)c * nao + col] = e2;
     }
-    float d1[S], d2[S];
-    digits<S>(xv, e1, d1);
-    digits<S>(wv, e2, d2);
     const int64_t colbase = (int64_t)c * S * KC * nao + (int64_t)col * S * KC;
 #pragma unroll
-    for (int i = 0; i < S; ++i) {
-        A[colbase + (int64_t)i * KC + k] = __float2bfloat16_rn(d1[i]);
-        B[colbase + (int64_t)(S - 1 - i) * KC + k] = __float2bfloat16_rn(d2[i]);
+    for (int r = 0; r < PER; ++r) {
+        const int k = r * 256 + threadIdx.x;
+        float d1[S], d2[S];
+        digits<S>(xv[r], e1, d1);
+        digits<S>(wv[r], e2, d2);
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
+            A[colbase + (int64_t)i * KC + k] = __float2bfloat16_rn(d1[i]);
+            B[colbase + (int64_t)(S - 1 - i) * KC + k] = __float2bfloat16_rn(d2[i]);
+        }
     }
 }
 
-// K[mu, nu] (+)= sum_c sum_l C[l][c](mu, nu) 2^(ex[c,mu] + ew[c,nu] - 12 - 7l)
+// K[mu, nu] (+)= sum_c 2^(ex+ew-2W+2+B(S-1)) [sum_l C[l][c] 2^(B (S-1-l))]
 template<int S>
 __global__ void k_combine_kernel(const float* __restrict__ C, int nao,
                                  int nchunk, const int* __restrict__ ex,
@@ -189,12 +245,13 @@ __global__ void k_combine_kernel(const float* __restrict__ C, int nao,
         const int mu = (int)(i % nao), nu = (int)(i / nao);   // C col-major
         double acc = 0.0;
         for (int c = 0; c < nchunk; ++c) {
-            const int base = ex[(int64_t)c * nao + mu] + ew[(int64_t)c * nao + nu] - 12;
-            double lv = 0.0;
+            float v[S];
 #pragma unroll
-            for (int l = S - 1; l >= 0; --l)
-                lv += ldexp((double)C[((int64_t)l * nchunk + c) * n2 + i], base - 7 * l);
-            acc += lv;
+            for (int l = 0; l < S; ++l) v[l] = C[((int64_t)l * nchunk + c) * n2 + i];
+            const long long lv = combine_levels<S>(v);
+            const int sc = ex[(int64_t)c * nao + mu] + ew[(int64_t)c * nao + nu] -
+                           2 * kW + 2 + kB * (S - 1);
+            acc += (double)lv * pow2(sc);
         }
         const int64_t o = (int64_t)mu * nao + nu;              // K row-major
         K[o] = accumulate ? K[o] + acc : acc;
@@ -279,8 +336,8 @@ int ozaki_k_gemm(cublasHandle_t hb, const double* X, const float* G,
     p += al(sizeof(__nv_bfloat16) * slab);
     float* C = reinterpret_cast<float*>(p);
     dim3 grid(nchunk, nao);
-    k_slice_kernel<S, KC><<<grid, KC, 0, s>>>(X, G, w, nao, ld, npts, nchunk,
-                                              ex, ew, A, B);
+    k_slice_kernel<S, KC><<<grid, 256, 0, s>>>(X, G, w, nao, ld, npts, ex, ew,
+                                               A, B);
     OZ_CUDA(cudaGetLastError());
     const float one = 1.0f, zero = 0.0f;
     const long long stride = (long long)S * KC * nao;

@@ -8,11 +8,12 @@
 
 namespace wb {
 
-constexpr int kOzSlices = 5;   // 7-bit slices per operand (~35 bits)
-constexpr int kOzKc = 768;     // K-GEMM chunk: (l + 1) * Kc < 4096 for l < 5
+constexpr int kOzBits = 6;     // balanced digits, |d| <= 32
+constexpr int kOzSlices = 7;   // 42 bits per operand
+constexpr int kOzKc = 2048;    // K-GEMM chunk: (l + 1) * Kc < 2^14 for l < 7
 
-// the F GEMM needs kOzSlices * nao < 4096 (exact FP32 level sums)
-inline bool ozaki_f_supported(int nao) { return kOzSlices * nao < 4096; }
+// exact FP32 level sums need kOzSlices * K < 2^14 along the inner dimension
+inline bool ozaki_f_supported(int nao) { return kOzSlices * nao < (1 << 14); }
 
 size_t ozaki_f_bytes(int nao, int64_t ld);
 size_t ozaki_k_bytes(int nao, int64_t ld);
