@@ -228,7 +228,12 @@ __device__ __forceinline__ void ao_shell(const AoArgs& A, int sh, int64_t g,
     const int ao0 = A.sh_ao0[sh];
     for (int ci = 0; ci < nc; ++ci) {
         double rad = 0.0;
-        for (int k = 0; k < np; ++k) rad += co[k * nc + ci] * exp(-ex[k] * r2);
+        for (int k = 0; k < np; ++k) {
+            // exp(-70) ~ 4e-31: such a primitive is zero at FP64 parity with
+            // any AO value of order one; skipping it avoids the FP64 exp
+            const double a = ex[k] * r2;
+            if (a < 70.0) rad += co[k * nc + ci] * exp(-a);
+        }
 #pragma unroll
         for (int m = 0; m < NS; ++m) {
             double v = 0.0;
@@ -285,7 +290,9 @@ __device__ __forceinline__ void ao_shell_d1(const AoArgs& A, int sh, int64_t g,
     for (int ci = 0; ci < nc; ++ci) {
         double rad0 = 0.0, rad1 = 0.0;
         for (int k = 0; k < np; ++k) {
-            const double e = co[k * nc + ci] * exp(-ex[k] * r2);
+            const double a = ex[k] * r2;
+            if (a >= 70.0) continue;          // below ~1e-30, see ao_shell
+            const double e = co[k * nc + ci] * exp(-a);
             rad0 += e;
             rad1 += -2.0 * ex[k] * e;
         }

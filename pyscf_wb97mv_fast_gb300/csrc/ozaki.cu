@@ -61,15 +61,27 @@ __device__ __forceinline__ int exp_of_bits(unsigned long long absbits) {
 
 template<int S>
 __device__ __forceinline__ void digits(double x, int e, float* d) {
-    long long q = __double2ll_rn(x * pow2(kW - 1 - e));
-    const long long half = 1ll << (kB - 1), mask = (1ll << kB) - 1;
+    // q (|q| < 2^(W-1) = 2^41) split as q = hi 2^24 + lo, lo in [0, 2^24):
+    // the four low digits come from lo, the carry goes into hi, the rest
+    // from hi -- 32-bit integer arithmetic throughout
+    static_assert(S == 7 && kB == 6, "digit split assumes 7 x 6 bits");
+    const long long q = __double2ll_rn(x * pow2(kW - 1 - e));
+    int lo = (int)(q & 0xFFFFFF);
+    int hi = (int)(q >> 24);
 #pragma unroll
-    for (int i = S - 1; i >= 1; --i) {
-        const long long di = ((q + half) & mask) - half;
+    for (int i = S - 1; i >= S - 4; --i) {
+        const int di = ((lo + 32) & 63) - 32;
         d[i] = (float)di;
-        q = (q - di) >> kB;
+        lo = (lo - di) >> 6;
     }
-    d[0] = (float)q;
+    hi += lo;
+#pragma unroll
+    for (int i = S - 5; i >= 1; --i) {
+        const int di = ((hi + 32) & 63) - 32;
+        d[i] = (float)di;
+        hi = (hi - di) >> 6;
+    }
+    d[0] = (float)hi;
 }
 
 // value of the combined levels: sum_l C_l 2^(B (S-1-l)) as an exact int64
