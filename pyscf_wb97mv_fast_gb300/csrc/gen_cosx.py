@@ -1,7 +1,7 @@
 """Generates csrc/generated/cosx_classes.cuh: one straight-line device
 function per shell-pair class (la >= lb, la <= 3) of the fused COSX kernel.
 
-For one task (shell pair A, B; one grid point g per thread) it computes
+For one task (shell pair A, B; one grid point g per thread) it adds
 
     G_B[nu] += sum_mu A^g_{mu nu} F_A[mu]        (always)
     G_A[mu] += sum_nu A^g_{mu nu} F_B[nu]        (A != B)
@@ -16,7 +16,11 @@ primitive prefactor), then for every primitive pair
     Ac[ca, cb]  = sum_t Ex sum_u Ey sum_v Ez R_tuv
     Y[cb]      += f0[ca] Ac[ca, cb],   X[ca] += Ac[ca, cb] h0[cb]
 
-and finally G_B += c2s^T Y, G_A += c2s^T X.  The recurrence and the
+and G_B += c2s^T Y at the end of the task.  The bra side is shared by a
+run of consecutive tasks with the same shell A (pairs are ordered by
+(A, B) within a class): f0 is formed once per run (cosx_begin) and X is
+carried across the run and added to G_A once (cosx_end).  The recurrence
+and the
 Hermite sum are the reference's math (pyscf_wb97mv_fast/gpu/sgx_k.py:
 200-307, gpu/shellpairs.py:447-485); the order of contraction (F first,
 no A block, no per-primitive contraction matrices) is this generator's.
@@ -219,9 +223,46 @@ def gen_transform_out(l, src, dst, ind, lines):
         lines.append('%sconst float %s%d = %s;' % (ind, dst, mu, expr))
 
 
+def gen_begin(la):
+    """f0 = c2s^T F_A of the run's A shell (loaded once per run)."""
+    na = 2 * la + 1
+    nca = (la + 1) * (la + 2) // 2
+    lines = ['template<> __device__ __forceinline__ void cosx_begin<%d>(' % la,
+             '    const CosxArgs& A, const int ia0, const long long g, float* f0)',
+             '{']
+    I = '    '
+    lines.append(I + 'const long long ld = A.ld;')
+    for mu in range(na):
+        lines.append(I + 'const float fa%d = A.F[(long long)(ia0 + %d) * ld + g];'
+                     % (mu, mu))
+    gen_transform_in(la, 'fa', 'c', I, lines)
+    for c in range(nca):
+        lines.append(I + 'f0[%d] = c%d;' % (c, c))
+    lines.append('}')
+    return '\n'.join(lines)
+
+
+def gen_end(la):
+    """G_A += c2s^T X at the end of a run."""
+    na = 2 * la + 1
+    nca = (la + 1) * (la + 2) // 2
+    lines = ['template<> __device__ __forceinline__ void cosx_end<%d>(' % la,
+             '    const CosxArgs& A, const int ia0, const long long g, const float* Xa)',
+             '{']
+    I = '    '
+    lines.append(I + 'const long long ld = A.ld;')
+    for c in range(nca):
+        lines.append(I + 'const float X%d = Xa[%d];' % (c, c))
+    gen_transform_out(la, 'X', 'ga', I, lines)
+    for mu in range(na):
+        lines.append(I + 'A.G[(long long)(ia0 + %d) * ld + g] += ga%d;' % (mu, mu))
+    lines.append('}')
+    return '\n'.join(lines)
+
+
 def gen_class(la, lb, diag):
     L = la + lb
-    na, nb = 2 * la + 1, 2 * lb + 1
+    nb = 2 * lb + 1
     ca = cart_components(la)
     cb = cart_components(lb)
     ents = e_entries(la, lb)
@@ -233,28 +274,22 @@ def gen_class(la, lb, diag):
     lines.append('    const CosxArgs& A, const int4 hdr, const long long g,')
     lines.append('    const float gxh, const float gyh, const float gzh,')
     lines.append('    const float gxl, const float gyl, const float gzl,')
-    lines.append('    const float4* __restrict__ stab)')
+    lines.append('    const float4* __restrict__ stab, const float* f0,')
+    lines.append('    const float* fb, float* Xa)')
     lines.append('{')
     lines.append(I + 'const long long ld = A.ld;')
-    lines.append(I + 'const float* __restrict__ Fp = A.F;')
-    lines.append(I + 'const int ia0 = hdr.x, ib0 = hdr.y, pp0 = hdr.z;')
+    lines.append(I + 'const int ib0 = hdr.y, pp0 = hdr.z;')
     lines.append(I + 'const int npp = hdr.w & 0xffff;')
-    # F loads
-    for mu in range(na):
-        lines.append(I + 'const float fa%d = Fp[(long long)(ia0 + %d) * ld + g];'
-                     % (mu, mu))
-    gen_transform_in(la, 'fa', 'f0_', I, lines)
+    for c in range(len(ca)):
+        lines.append(I + 'const float f0_%d = f0[%d];' % (c, c))
     if not diag:
         for nu in range(nb):
-            lines.append(I + 'const float fb%d = Fp[(long long)(ib0 + %d) * ld + g];'
-                         % (nu, nu))
+            lines.append(I + 'const float fb%d = fb[%d];' % (nu, nu))
         gen_transform_in(lb, 'fb', 'h0_', I, lines)
+        for c in range(len(ca)):
+            lines.append(I + 'float X%d = Xa[%d];' % (c, c))
     for c in range(len(cb)):
         lines.append(I + 'float Y%d = 0.0f;' % c)
-    if not diag:
-        for c in range(len(ca)):
-            lines.append(I + 'float X%d = 0.0f;' % c)
-    # R variables
     tuv = [(t, u, v) for t in range(L + 1) for u in range(L + 1 - t)
            for v in range(L + 1 - t - u)]
     lines.append(I + 'const float4* __restrict__ geo = A.geo;')
@@ -277,7 +312,6 @@ def gen_class(la, lb, diag):
     lines.append(J + 'const float T = fmaf(o0.x, r2, o0.y * r2);')
     lines.append(J + 'float Fb[%d];' % (L + 1))
     lines.append(J + 'boys_fp32<%d>(T, Fb, stab);' % L)
-    # c_n hi/lo: record floats [tp_hi, tp_lo, c0h, c0l, c1h, c1l, ...]
     comp = 'xyzw'
     for n in range(L + 1):
         fh = 2 + 2 * n
@@ -288,7 +322,6 @@ def gen_class(la, lb, diag):
                      % (n, ch, n, cl, n))
     lines.append(J + 'float ' + ', '.join(rname(*x) for x in tuv) + ';')
     gen_recurrence(L, lines, J)
-    # E loads
     if ents:
         nvec = est // 4
         lines.append(J + 'const float4* __restrict__ Em = Eb + (long long)(m - ppb) * %d;' % nvec)
@@ -304,7 +337,6 @@ def gen_class(la, lb, diag):
                 nm = flat[4 * q + c]
                 if nm is not None:
                     lines.append(J + 'const float %s = ev%d.%s;' % (nm, q, comp[c]))
-    # Hermite sums and accumulation
     for ia, cac in enumerate(ca):
         for ib, cbc in enumerate(cb):
             tag = '%d_%d' % (ia, ib)
@@ -313,23 +345,27 @@ def gen_class(la, lb, diag):
             if not diag:
                 lines.append(J + 'X%d = fmaf(%s, h0_%d, X%d);' % (ia, sv, ib, ia))
     lines.append(I + '}')
-    # outputs
     gen_transform_out(lb, 'Y', 'gb', I, lines)
-    lines.append(I + 'float* __restrict__ Gp = A.G;')
     for nu in range(nb):
-        lines.append(I + 'Gp[(long long)(ib0 + %d) * ld + g] += gb%d;' % (nu, nu))
+        lines.append(I + 'A.G[(long long)(ib0 + %d) * ld + g] += gb%d;' % (nu, nu))
     if not diag:
-        gen_transform_out(la, 'X', 'ga', I, lines)
-        for mu in range(na):
-            lines.append(I + 'Gp[(long long)(ia0 + %d) * ld + g] += ga%d;' % (mu, mu))
+        for c in range(len(ca)):
+            lines.append(I + 'Xa[%d] = X%d;' % (c, c))
     lines.append('}')
     return '\n'.join(lines)
 
 
 def source():
     out = ['// Generated by csrc/gen_cosx.py -- do not edit by hand.',
-           '// One straight-line task body per shell-pair class (la >= lb).',
+           '// One straight-line task body per shell-pair class (la >= lb),',
+           '// plus the per-run begin (F_A -> Cartesian f0) and end',
+           '// (G_A += c2s^T X) of each bra angular momentum.',
            '#pragma once', '']
+    for la in range(LMAX + 1):
+        out.append(gen_begin(la))
+        out.append('')
+        out.append(gen_end(la))
+        out.append('')
     for (la, lb) in classes():
         out.append(gen_class(la, lb, False))
         out.append('')

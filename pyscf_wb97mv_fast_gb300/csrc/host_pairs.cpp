@@ -312,8 +312,13 @@ int build_pairs(const wb_basis& b, const double origin[3], double cutoff,
             c.cls = class_of(out.vsh[c.A].l, out.vsh[c.B].l);
             kept.push_back(c);
         }
-    std::stable_sort(kept.begin(), kept.end(),
-                     [](const Cand& x, const Cand& y) { return x.cls < y.cls; });
+    // class-major, then bra shell A, then ket B: consecutive tasks of a
+    // class share A (the kernels keep F_A and G_A in registers per run)
+    std::stable_sort(kept.begin(), kept.end(), [](const Cand& x, const Cand& y) {
+        if (x.cls != y.cls) return x.cls < y.cls;
+        if (x.A != y.A) return x.A < y.A;
+        return x.B < y.B;
+    });
     out.npairs = (int)kept.size();
 
     // -- per pair / per primitive pair ---------------------------------------
