@@ -320,10 +320,21 @@ def test_ozaki_gemms_are_fp64_accurate():
     bound = (2.0 ** -38 * mol.nao * colmax[:, None] * rowmax[None, :]
              + F64.abs() * 2.0 ** -24)
     assert bool(((F_oz.double() - F64).abs() <= bound).all())
-    G = torch.randn(X.shape, dtype=torch.float32, device=eng.device)
+    # K: the G of the real kernels on this grid, against FP64 torch, within
+    # the split's bound: per 2048-point chunk c, 2^-40 Kc max_c|X_mu|
+    # max_c|w G_nu| (42-bit digits relative to the chunk-column maxima)
     n = c.shape[0]
-    G[:, n:] = 0
+    G = eng.g(c, w, F_oz, 0.0, 0.0)
     K_oz = eng.ozaki_k(X, G, w)
-    wG = G.double() * torch.nn.functional.pad(w, (0, X.shape[1] - n))[None, :]
+    wpad = torch.nn.functional.pad(w, (0, X.shape[1] - n))
+    wG = G.double() * wpad[None, :]
     K_ref = X @ wG.T
+    kc = 2048
+    ld = X.shape[1]
+    nch = (ld + kc - 1) // kc
+    pad = nch * kc - ld
+    xm = torch.nn.functional.pad(X.abs(), (0, pad)).view(mol.nao, nch, kc).max(dim=2).values
+    gm = torch.nn.functional.pad(wG.abs(), (0, pad)).view(mol.nao, nch, kc).max(dim=2).values
+    bound = 2.0 ** -40 * kc * (xm @ gm.T)
+    assert bool(((K_oz - K_ref).abs() <= bound).all())
     assert (K_oz - K_ref).abs().max().item() < 1e-10 * K_ref.abs().max().item()
