@@ -196,6 +196,27 @@ int wb_vv10_kernel_sum(const float* xyz, const float* q, const float* w0,
                        double* f_out, double* u_out, double* w_out,
                        void* stream, int64_t* pairs_kept);
 
+/* Allocation-free VV10 double sum: the same computation and results as
+ * wb_vv10_kernel_sum, for callers that cannot let the library allocate
+ * device memory (e.g. a host framework that reserves the whole GPU memory
+ * up front and hands out fixed arenas, where a cudaMalloc during a request
+ * would fail or stall the device).  Its scratch (tile statistics and the
+ * kept-pair counter) is a file-scope device array of fixed size, held by
+ * every GPU that loads the library until the process exits; n above
+ * WB_VV10_NOALLOC_MAX_POINTS is rejected with WB_ERR_INVALID_ARGUMENT.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  All calls on a device share the array and
+ * each call leaves its own contents there: calls whose work overlaps on
+ * the GPU (different streams, or different host threads) race.  No
+ * counterpart in the reference. */
+#define WB_VV10_NOALLOC_MAX_POINTS 1048576
+int wb_vv10_kernel_sum_noalloc(const float* xyz, const float* q,
+                               const float* w0, const float* kappa,
+                               int64_t n, double tile_tol, double* f_out,
+                               double* u_out, double* w_out, void* stream,
+                               int64_t* pairs_kept);
+
 /* Becke fuzzy-cell weights (host, FP64, OpenMP): for each point its
  * owner atom's cell weight.  Grid construction helper for the synthetic
  * workloads (PySCF builds the grids in the reference). */

@@ -22,6 +22,8 @@ WB_ERR_OUT_OF_MEMORY = 5
 WB_ERR_WORKSPACE = 6
 WB_ERR_NO_DEVICE = 7
 
+WB_VV10_NOALLOC_MAX_POINTS = 1048576
+
 WB_K_GEMM_NATIVE_FP64 = 0
 WB_K_GEMM_EMULATED_FP64 = 1
 WB_K_GEMM_OZAKI_BF16 = 2
@@ -40,6 +42,7 @@ EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_boys_fp32', 'wb_boys_f64_host', 'wb_vv10_kernel_sum',
             'wb_becke_partition', 'wb_fp32_fma_probe',
             'wb_ozaki_workspace_bytes', 'wb_cosx_ozaki_f', 'wb_cosx_ozaki_k',
+            'wb_vv10_kernel_sum_noalloc',
             'wb_status_string',
             'wb_last_error', 'wb_version')
 
@@ -130,6 +133,8 @@ def _declare(lib):
         'wb_vv10_kernel_sum': (_INT, [_P, _P, _P, _P, _I64, _D, _P, _P, _P, _P,
                                       ctypes.POINTER(_I64)]),
         'wb_becke_partition': (_INT, [_P, _I64, _P, _P, _INT, _P]),
+        'wb_vv10_kernel_sum_noalloc': (_INT, [_P, _P, _P, _P, _I64, _D, _P, _P,
+                                              _P, _P, ctypes.POINTER(_I64)]),
         'wb_fp32_fma_probe': (_INT, [_I64, _P, _I64, _P, ctypes.POINTER(_D)]),
         'wb_ozaki_workspace_bytes': (ctypes.c_size_t, [_INT, _I64]),
         'wb_cosx_ozaki_f': (_INT, [_P, _P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),

@@ -85,6 +85,10 @@ int upload_constants() {
 
 }  // namespace
 
+namespace wb {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace wb
+
 struct wb_cosx {
     int device = 0;
     int nsm = 1;

@@ -185,3 +185,112 @@ cudaError_t launch_vv10(const float* xyz, const float* q, const float* w0,
 }
 
 }  // namespace wb
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of wb_vv10_kernel_sum.
+//
+// Some callers of this library cannot let it allocate device memory: a
+// host framework that reserves all of the GPU memory up front and hands
+// out fixed arenas (a cudaMalloc in the middle of a request would fail or
+// stall the device), or a caller that must keep every CUDA call of the
+// hot loop free of the allocator.  For them the VV10 tile statistics and
+// the kept-pair counter live in this file-scope device array instead of a
+// cudaMallocAsync'd workspace.  Its size is fixed at build time, so the
+// entry point serves at most WB_VV10_NOALLOC_MAX_POINTS points, and every
+// GPU that loads the library holds it until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+#include <string>
+
+#include "wb97mv_gb300.h"
+
+namespace wb {
+// the calling thread's wb_last_error() message (defined with the C ABI)
+void set_last_error(const std::string& msg);
+}
+
+namespace {
+
+constexpr int64_t kNoallocMaxTiles =
+    (WB_VV10_NOALLOC_MAX_POINTS + wb::kVvTile - 1) / wb::kVvTile;
+constexpr size_t kNoallocBytes =
+    256 + sizeof(wb::VvTileStats) * (size_t)kNoallocMaxTiles;
+
+// [0, 256): kept-pair counter; [256, ...): one VvTileStats per tile
+static __device__ __align__(256) unsigned char g_vv10_scratch[kNoallocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+int noalloc_fail(int code, const char* msg, cudaError_t e = cudaSuccess) {
+    std::string m(msg);
+    if (e != cudaSuccess) m += std::string(": ") + cudaGetErrorString(e);
+    wb::set_last_error(m);
+    return code;
+}
+
+}  // namespace
+
+extern "C" int wb_vv10_kernel_sum_noalloc(const float* xyz, const float* q,
+                                          const float* w0, const float* kappa,
+                                          int64_t n, double tile_tol,
+                                          double* f_out, double* u_out,
+                                          double* w_out, void* stream,
+                                          int64_t* pairs_kept) {
+    if (n < 0 || !(tile_tol >= 0.0))
+        return noalloc_fail(WB_ERR_INVALID_ARGUMENT,
+                            "wb_vv10_kernel_sum_noalloc: n must be >= 0 and "
+                            "tile_tol >= 0");
+    if (n > WB_VV10_NOALLOC_MAX_POINTS)
+        return noalloc_fail(WB_ERR_INVALID_ARGUMENT,
+                            "wb_vv10_kernel_sum_noalloc: n exceeds "
+                            "WB_VV10_NOALLOC_MAX_POINTS (the size of its "
+                            "static scratch); use wb_vv10_kernel_sum");
+    if (n && (!xyz || !q || !w0 || !kappa || !f_out || !u_out || !w_out))
+        return noalloc_fail(WB_ERR_INVALID_ARGUMENT,
+                            "wb_vv10_kernel_sum_noalloc: null pointer");
+    if (n == 0) {
+        if (pairs_kept) *pairs_kept = 0;
+        return WB_OK;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return noalloc_fail(WB_ERR_CUDA, "wb_vv10_kernel_sum_noalloc: cudaGetDevice", e);
+    if (dev < 0 || dev >= kMaxDevices)
+        return noalloc_fail(WB_ERR_INVALID_ARGUMENT,
+                            "wb_vv10_kernel_sum_noalloc: device index too large");
+    void* scratch = nullptr;
+    {
+        // first call on this device: the device address of the array (the
+        // host-side name is only a stand-in), taken with the device current
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_vv10_scratch);
+            if (e != cudaSuccess || !p)
+                return noalloc_fail(WB_ERR_CUDA,
+                                    "wb_vv10_kernel_sum_noalloc: "
+                                    "cudaGetSymbolAddress", e);
+            g_noalloc_ptr[dev] = p;
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // launch_vv10 zeroes the counter and overwrites every tile record it
+    // reads; nothing else in the array must start at zero
+    e = wb::launch_vv10(xyz, q, w0, kappa, n, tile_tol, f_out, u_out, w_out,
+                        scratch, s);
+    if (e != cudaSuccess)
+        return noalloc_fail(WB_ERR_CUDA, "wb_vv10_kernel_sum_noalloc: launch", e);
+    if (pairs_kept) {
+        unsigned long long kept = 0;
+        e = cudaMemcpyAsync(&kept, scratch, sizeof(kept), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess)
+            return noalloc_fail(WB_ERR_CUDA, "wb_vv10_kernel_sum_noalloc: counter", e);
+        *pairs_kept = (int64_t)kept;
+    }
+    return WB_OK;
+}
