@@ -305,6 +305,8 @@ def main():
     torch.cuda.synchronize()
     flops_step, launches_step, kept, total = 0.0, 0, 0, 0
     phases = {}
+    kept_cls = [0] * 10
+    flops_cls = [0.0] * 10
     for i, w in enumerate(OMEGAS):
         eng.get_k(coords_d, w_d, qd_d, w, tile_tol=TILE_TOL,
                   gemm=args.gemm, out=K[i], stats=True, profile=True)
@@ -313,6 +315,9 @@ def main():
         launches_step += st['kernel_launches']
         kept += st['pairs_kept']
         total += st['pairs_total']
+        for c in range(10):
+            kept_cls[c] += st['kept_class'][c]
+            flops_cls[c] += st['flops_class'][c]
         for k, v in st['phase_ms'].items():
             phases[k] = phases.get(k, 0.0) + v
 
@@ -425,6 +430,11 @@ def main():
             'tasks_kept': kept, 'tasks_total': total,
             'model_flops_per_step': flops_step,
             'phases_ms_per_step': phases,
+            'classes': {'(%d,%d)' % (la, lb): {
+                'tasks_kept': kept_cls[la * (la + 1) // 2 + lb],
+                'model_gflop': round(flops_cls[la * (la + 1) // 2 + lb] / 1e9, 3)}
+                for la in range(4) for lb in range(la + 1)
+                if kept_cls[la * (la + 1) // 2 + lb]},
         }
         print(json.dumps(line))
     if world > 1:

@@ -75,6 +75,8 @@ def build(verbose=False, force=False, jobs=None):
     os.makedirs(LIBDIR, exist_ok=True)
     common = ['-std=c++17', '-O3', '-lineinfo', '-I', INCLUDE, '-I', CSRC,
               '-Xcompiler', '-fPIC,-fopenmp,-O2', '-Xptxas', '-v' if verbose else '-O3']
+    # extra nvcc flags, e.g. WB_NVCC_EXTRA=-DWB_COSX_MIN_BLOCKS=9766431111LL
+    common += os.environ.get('WB_NVCC_EXTRA', '').split()
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.splitext(src)[0] + '.o')

@@ -53,6 +53,36 @@ cudaError_t launch_omega(int npp, const double* p, const double* pref,
     return cudaGetLastError();
 }
 
+// Packed per-class primitive-pair records for the class kernels: one
+// contiguous record per pair (P hi, P lo, the first n_om float4 of the
+// omega record, the Hermite E block) so that a pair is one base address.
+__global__ void pack_records_kernel(const RecPack P, int npp,
+                                    const float4* __restrict__ geo,
+                                    const float4* __restrict__ om,
+                                    const float4* __restrict__ E,
+                                    float4* __restrict__ rec) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= npp) return;
+    int c = 0;
+    while (c < 9 && m >= P.pp_end[c]) ++c;
+    if (m < P.pp_begin[c] || m >= P.pp_end[c]) return;
+    const int ml = m - P.pp_begin[c];
+    float4* r = rec + P.rec_off[c] + (long long)ml * P.stride[c];
+    r[0] = geo[2 * (long long)m];
+    r[1] = geo[2 * (long long)m + 1];
+    for (int q = 0; q < P.nom[c]; ++q) r[2 + q] = om[4 * (long long)m + q];
+    const float4* e = E + P.e_off[c] + (long long)ml * P.ne[c];
+    for (int q = 0; q < P.ne[c]; ++q) r[2 + P.nom[c] + q] = e[q];
+}
+
+cudaError_t launch_pack_records(const RecPack& P, int npp, const float4* geo,
+                                const float4* om, const float4* E,
+                                float4* rec, cudaStream_t s) {
+    if (npp <= 0) return cudaSuccess;
+    pack_records_kernel<<<(npp + 127) / 128, 128, 0, s>>>(P, npp, geo, om, E, rec);
+    return cudaGetLastError();
+}
+
 // -- FP64 (npts, 3) -> FP32 SoA hi / lo, padded with zeros to ld ----------
 __global__ void grid_prep_kernel(const double* __restrict__ c, int64_t npts,
                                  int64_t ld, float* __restrict__ hi,
@@ -80,9 +110,11 @@ cudaError_t launch_grid_prep(const double* coords, int64_t npts, int64_t ld,
 }
 
 // -- sub-block statistics (gpu/sgx_k.py:866-903) ---------------------------
-// One warp per 32-point sub-block: FP64 centroid and radius of the valid
-// points (centroid rounded to nearest FP32, radius rounded up), and for
-// every (virtual) shell msh = max_g fl32(w_g) sum_{t in shell} |F_tg|.
+// One warp per block of BP = 32 or 64 consecutive points (32 is the
+// reference's sub-block): FP64 centroid and radius of the valid points
+// (centroid rounded to nearest FP32, radius rounded up), and for every
+// (virtual) shell msh = max_g fl32(w_g) sum_{t in shell} |F_tg|.
+template<int BP>
 __global__ void sub_stats_kernel(const double* __restrict__ coords,
                                  const double* __restrict__ w,
                                  const float* __restrict__ F, int64_t npts,
@@ -91,28 +123,43 @@ __global__ void sub_stats_kernel(const double* __restrict__ coords,
                                  const int* __restrict__ vs_nf,
                                  float4* __restrict__ sub_cr,
                                  float* __restrict__ msh) {
+    constexpr int Q = BP / 32;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    const int nsub = (int)(ld / 32);
-    if (warp >= nsub) return;
-    const int64_t g = (int64_t)warp * 32 + lane;
-    const bool valid = g < npts;
-    double cx = 0.0, cy = 0.0, cz = 0.0;
-    if (valid) { cx = coords[g * 3]; cy = coords[g * 3 + 1]; cz = coords[g * 3 + 2]; }
-    double sx = cx, sy = cy, sz = cz;
+    const int nblk = (int)((ld + BP - 1) / BP);
+    if (warp >= nblk) return;
+    int64_t g[Q];
+    bool valid[Q];
+    double cx[Q], cy[Q], cz[Q];
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        g[q] = (int64_t)warp * BP + 32 * q + lane;
+        valid[q] = g[q] < npts;
+        cx[q] = cy[q] = cz[q] = 0.0;
+        if (valid[q]) {
+            cx[q] = coords[g[q] * 3];
+            cy[q] = coords[g[q] * 3 + 1];
+            cz[q] = coords[g[q] * 3 + 2];
+        }
+        sx += cx[q]; sy += cy[q]; sz += cz[q];
+    }
     for (int o = 16; o > 0; o >>= 1) {
         sx += __shfl_xor_sync(0xffffffffu, sx, o);
         sy += __shfl_xor_sync(0xffffffffu, sy, o);
         sz += __shfl_xor_sync(0xffffffffu, sz, o);
     }
-    const int64_t rem = npts - (int64_t)warp * 32;
-    const int nvalid = rem >= 32 ? 32 : (rem > 0 ? (int)rem : 0);
+    const int64_t rem = npts - (int64_t)warp * BP;
+    const int nvalid = rem >= BP ? BP : (rem > 0 ? (int)rem : 0);
     double mx = 0.0, my = 0.0, mz = 0.0;
     if (nvalid > 0) { mx = sx / nvalid; my = sy / nvalid; mz = sz / nvalid; }
     double d = 0.0;
-    if (valid) {
-        const double ex = cx - mx, ey = cy - my, ez = cz - mz;
-        d = sqrt(ex * ex + ey * ey + ez * ez);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if (valid[q]) {
+            const double ex = cx[q] - mx, ey = cy[q] - my, ez = cz[q] - mz;
+            d = fmax(d, sqrt(ex * ex + ey * ey + ez * ez));
+        }
     }
     for (int o = 16; o > 0; o >>= 1) d = fmax(d, __shfl_xor_sync(0xffffffffu, d, o));
     if (lane == 0) {
@@ -120,27 +167,41 @@ __global__ void sub_stats_kernel(const double* __restrict__ coords,
         if ((double)r < d) r = nextafterf(r, INFINITY);
         sub_cr[warp] = make_float4((float)mx, (float)my, (float)mz, r);
     }
-    const float w32 = valid ? (float)w[g] : 0.0f;
+    float w32[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) w32[q] = valid[q] ? (float)w[g[q]] : 0.0f;
     for (int s = 0; s < nvshell; ++s) {
         const int a0 = vs_ao0[s], nf = vs_nf[s];
-        float acc = 0.0f;
-        for (int t = 0; t < nf; ++t)
-            acc += fabsf(F[(int64_t)(a0 + t) * ld + g]) * w32;
+        float best = 0.0f;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            if (!valid[q]) continue;
+            float acc = 0.0f;
+            for (int t = 0; t < nf; ++t)
+                acc += fabsf(F[(int64_t)(a0 + t) * ld + g[q]]) * w32[q];
+            best = fmaxf(best, acc);
+        }
         for (int o = 16; o > 0; o >>= 1)
-            acc = fmaxf(acc, __shfl_xor_sync(0xffffffffu, acc, o));
-        if (lane == 0) msh[(int64_t)warp * nvshell + s] = acc;
+            best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
+        if (lane == 0) msh[(int64_t)warp * nvshell + s] = best;
     }
 }
 
 cudaError_t launch_sub_stats(const double* coords, const double* weights,
                              const float* F, int64_t npts, int64_t ld,
                              int nvshell, const int* vs_ao0, const int* vs_nf,
-                             float4* sub_cr, float* msh, cudaStream_t s) {
-    const int64_t nsub = ld / 32;
-    if (nsub <= 0) return cudaSuccess;
+                             int block_pts, float4* sub_cr, float* msh,
+                             cudaStream_t s) {
+    const int64_t nblk = (ld + block_pts - 1) / block_pts;
+    if (nblk <= 0) return cudaSuccess;
     const int warps = 4;
-    sub_stats_kernel<<<(unsigned)((nsub + warps - 1) / warps), 32 * warps, 0, s>>>(
-        coords, weights, F, npts, ld, nvshell, vs_ao0, vs_nf, sub_cr, msh);
+    const unsigned grid = (unsigned)((nblk + warps - 1) / warps);
+    if (block_pts == 64)
+        sub_stats_kernel<64><<<grid, 32 * warps, 0, s>>>(
+            coords, weights, F, npts, ld, nvshell, vs_ao0, vs_nf, sub_cr, msh);
+    else
+        sub_stats_kernel<32><<<grid, 32 * warps, 0, s>>>(
+            coords, weights, F, npts, ld, nvshell, vs_ao0, vs_nf, sub_cr, msh);
     return cudaGetLastError();
 }
 
@@ -180,6 +241,36 @@ cudaError_t launch_weight_g(const float* G, const double* w, int64_t npts,
     int64_t blocks = (total + 255) / 256;
     if (blocks > 152 * 64) blocks = 152 * 64;
     weight_g_kernel<<<(unsigned)blocks, 256, 0, s>>>(G, w, npts, ld, total, out);
+    return cudaGetLastError();
+}
+
+// G[mu, g] = sum of the class partial-G rows src[mu] (ascending class
+// order, -1 = none): the fixed-order combination of the concurrently
+// filled class buffers.  Four points per thread (ld is a multiple of 32).
+__global__ void gsum_kernel(const float* __restrict__ gc,
+                            const int4* __restrict__ src, int64_t ld,
+                            float* __restrict__ G) {
+    const int mu = blockIdx.y;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (i >= ld) return;
+    const int4 sr = src[mu];
+    const int rows[4] = {sr.x, sr.y, sr.z, sr.w};
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (rows[j] < 0) continue;
+        const float4 v = *reinterpret_cast<const float4*>(gc + rows[j] * ld + i);
+        acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
+    }
+    *reinterpret_cast<float4*>(G + (int64_t)mu * ld + i) = acc;
+}
+
+cudaError_t launch_gsum(const float* gc, const int4* src, int nao, int64_t ld,
+                        float* G, cudaStream_t s) {
+    if (nao <= 0 || ld <= 0) return cudaSuccess;
+    const int64_t quads = ld / 4;
+    dim3 grid((unsigned)((quads + 255) / 256), (unsigned)nao);
+    gsum_kernel<<<grid, 256, 0, s>>>(gc, src, ld, G);
     return cudaGetLastError();
 }
 

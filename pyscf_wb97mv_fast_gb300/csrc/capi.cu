@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "host.hpp"
+#include "generated/cosx_layout.h"
 #include "launch.hpp"
 #include "ozaki.hpp"
 #include "wb97mv_gb300.h"
@@ -101,6 +102,8 @@ struct wb_cosx {
     double* pref = nullptr;
     float4* E = nullptr;
     int4* hdr = nullptr;
+    int4* khdr = nullptr;
+    int4* gsrc = nullptr;
     int2* pshell = nullptr;
     float2* ptau = nullptr;
     float4* bnd = nullptr;
@@ -125,12 +128,22 @@ struct wb_cosx {
     double* exps = nullptr;
     double* coeffs = nullptr;
     int blocks_per_sm[wb::NCLASS] = {0};
+    // class launches run concurrently on their own streams (fork / join by
+    // events on the caller's stream), largest estimated work first
+    cudaStream_t cstream[wb::NCLASS] = {};
+    cudaEvent_t cdone[wb::NCLASS] = {};
+    cudaEvent_t fork = nullptr;
+    int corder[wb::NCLASS] = {0};
+    int pts[wb::NCLASS] = {0};       // points per lane of each class kernel
+    bool uses_pts[2] = {false, false};
 };
 
 namespace {
 
 struct WsLayout {
-    size_t om = 0, gh = 0, gl = 0, subcr = 0, msh = 0, counters = 0, work = 0;
+    size_t om = 0, rec = 0, gh = 0, gl = 0, counters = 0, work = 0;
+    size_t subcr[2] = {0, 0}, msh[2] = {0, 0};     // 32- and 64-point blocks
+    size_t gcls = 0;
     size_t X = 0, F64 = 0, F32 = 0, G32 = 0, oz = 0, total = 0;
 };
 
@@ -142,15 +155,19 @@ WsLayout ws_layout(const wb_cosx* h, int64_t ldt, bool full) {
         off = align256(off + bytes);
         return o;
     };
-    const int64_t nsub = ldt / 32;
     const int nao = h->hp.nao;
     L.counters = take(sizeof(unsigned long long) * 3 * wb::NCLASS);
     L.work = take(sizeof(int) * wb::NCLASS);
     L.om = take(sizeof(float) * 16 * (size_t)std::max(h->hp.npp, 1));
+    L.rec = take(sizeof(float4) * (size_t)std::max<int64_t>(h->hp.nrec, 1));
     L.gh = take(sizeof(float) * 3 * (size_t)ldt);
     L.gl = take(sizeof(float) * 3 * (size_t)ldt);
-    L.subcr = take(sizeof(float4) * (size_t)nsub);
-    L.msh = take(sizeof(float) * (size_t)nsub * std::max(h->hp.nvshell, 1));
+    for (int b = 0; b < 2; ++b) {
+        const int64_t nblk = (ldt + 32 * (b + 1) - 1) / (32 * (b + 1));
+        L.subcr[b] = take(sizeof(float4) * (size_t)nblk);
+        L.msh[b] = take(sizeof(float) * (size_t)nblk * std::max(h->hp.nvshell, 1));
+    }
+    L.gcls = take(sizeof(float) * (size_t)std::max<int64_t>(h->hp.ncrow, 1) * ldt);
     if (full) {
         L.X = take(sizeof(double) * (size_t)nao * ldt);
         L.F32 = take(sizeof(float) * (size_t)nao * ldt);
@@ -173,12 +190,13 @@ T* at(void* base, size_t off) {
 }
 
 wb::CosxArgs make_args(const wb_cosx* h, void* ws, const WsLayout& L,
-                       int64_t ldt, int64_t npts_t, const float* F, float* G,
+                       int64_t ldt, int64_t npts_t, const float* F,
                        double tile_tol) {
     wb::CosxArgs a;
     std::memset(&a, 0, sizeof(a));
     a.F = F;
-    a.G = G;
+    for (int c = 0; c < wb::NCLASS; ++c)
+        a.Gcls[c] = at<float>(ws, L.gcls) + h->hp.crow_base[c] * ldt;
     a.ld = ldt;
     a.npts = (int)npts_t;
     a.nsub = (int)(ldt / 32);
@@ -187,14 +205,19 @@ wb::CosxArgs make_args(const wb_cosx* h, void* ws, const WsLayout& L,
     for (int c = 0; c < wb::NCLASS; ++c) {
         a.Ecls[c] = h->E + h->hp.cls[c].e_base / 4;
         a.pp_begin[c] = h->hp.cls[c].pp_begin;
+        a.rec[c] = at<float4>(ws, L.rec) + h->hp.rec_off[c];
     }
     a.hdr = h->hdr;
+    a.khdr = h->khdr;
     a.pshell = h->pshell;
     a.ptau = h->ptau;
     a.bnd = h->bnd;
     a.bpref = h->bpref;
-    a.sub_cr = at<float4>(ws, L.subcr);
-    a.msh = at<float>(ws, L.msh);
+    for (int b = 0; b < 2; ++b) {
+        a.blk_cr[b] = at<float4>(ws, L.subcr[b]);
+        a.blk_msh[b] = at<float>(ws, L.msh[b]);
+        a.nblk[b] = (int)((ldt + 32 * (b + 1) - 1) / (32 * (b + 1)));
+    }
     a.nvshell = h->hp.nvshell;
     a.tol = tile_tol > 0.0 ? (float)(tile_tol / 1.001) : 0.0f;
     if (tile_tol > 0.0 && a.tol <= 0.0f) a.tol = 1e-38f;
@@ -208,33 +231,66 @@ wb::CosxArgs make_args(const wb_cosx* h, void* ws, const WsLayout& L,
     return a;
 }
 
+// per-omega primitive-pair data: the omega record and the packed class
+// records the G kernels read
+int prepare_omega(wb_cosx* h, double omega, void* ws, const WsLayout& L,
+                  cudaStream_t s) {
+    WB_CUDA(wb::launch_omega(h->hp.npp, h->p, h->pref, omega,
+                             at<float4>(ws, L.om), s));
+    wb::RecPack P;
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        P.pp_begin[c] = h->hp.cls[c].pp_begin;
+        P.pp_end[c] = h->hp.cls[c].pp_end;
+        P.stride[c] = wb::kRecStride[c];
+        P.nom[c] = wb::kRecNom[c];
+        P.ne[c] = wb::kRecNe[c];
+        P.rec_off[c] = h->hp.rec_off[c];
+        P.e_off[c] = h->hp.cls[c].e_base / 4;
+    }
+    WB_CUDA(wb::launch_pack_records(P, h->hp.npp, h->geo, at<float4>(ws, L.om),
+                                    h->E, at<float4>(ws, L.rec), s));
+    return WB_OK;
+}
+
 // stats, sub-block prep and the class launches of one tile; F and G are
-// (nao, ldt) AO-major, G is zeroed here
+// (nao, ldt) AO-major.  The classes fill their own partial-G buffers
+// concurrently; G is their fixed-order sum.
 int run_g_tile(wb_cosx* h, const double* coords, const double* weights,
                int64_t npts_t, int64_t ldt, const float* F, float* G,
                double tile_tol, void* ws, const WsLayout& L, cudaStream_t s,
                int* launches) {
-    const wb::CosxArgs a = make_args(h, ws, L, ldt, npts_t, F, G, tile_tol);
+    const wb::CosxArgs a = make_args(h, ws, L, ldt, npts_t, F, tile_tol);
     WB_CUDA(wb::launch_grid_prep(coords, npts_t, ldt, at<float>(ws, L.gh),
                                  at<float>(ws, L.gl), s));
-    WB_CUDA(wb::launch_sub_stats(coords, weights, F, npts_t, ldt,
-                                 h->hp.nvshell, h->vs_ao0, h->vs_nf,
-                                 at<float4>(ws, L.subcr), at<float>(ws, L.msh),
-                                 s));
-    WB_CUDA(cudaMemsetAsync(G, 0, sizeof(float) * (size_t)h->hp.nao * ldt, s));
-    WB_CUDA(cudaMemsetAsync(at<int>(ws, L.work), 0, sizeof(int) * wb::NCLASS, s));
-    *launches += 2;
-    const int nsub = (int)(ldt / 32);
-    for (int c = 0; c < wb::NCLASS; ++c) {
-        const wb::ClassRange& r = h->hp.cls[c];
-        if (r.pair_end <= r.pair_begin) continue;
-        const int want = (nsub + 3) / 4;
-        const int cap = std::max(1, h->blocks_per_sm[c]) * h->nsm;
-        const int grid = std::max(1, std::min(want, cap));
-        WB_CUDA(wb::launch_cosx_class_range(c, a, r.pair_begin, r.pair_end,
-                                            grid, s));
+    for (int b = 0; b < 2; ++b) {
+        if (!h->uses_pts[b]) continue;
+        WB_CUDA(wb::launch_sub_stats(coords, weights, F, npts_t, ldt,
+                                     h->hp.nvshell, h->vs_ao0, h->vs_nf,
+                                     32 * (b + 1), at<float4>(ws, L.subcr[b]),
+                                     at<float>(ws, L.msh[b]), s));
         *launches += 1;
     }
+    WB_CUDA(cudaMemsetAsync(at<float>(ws, L.gcls), 0,
+                            sizeof(float) * (size_t)h->hp.ncrow * ldt, s));
+    WB_CUDA(cudaMemsetAsync(at<int>(ws, L.work), 0, sizeof(int) * wb::NCLASS, s));
+    *launches += 2;
+    WB_CUDA(cudaEventRecord(h->fork, s));
+    for (int i = 0; i < wb::NCLASS; ++i) {
+        const int c = h->corder[i];
+        const wb::ClassRange& r = h->hp.cls[c];
+        if (r.pair_end <= r.pair_begin) continue;
+        const int want = (a.nblk[h->pts[c] - 1] + 3) / 4;
+        const int cap = std::max(1, h->blocks_per_sm[c]) * h->nsm;
+        const int grid = std::max(1, std::min(want, cap));
+        WB_CUDA(cudaStreamWaitEvent(h->cstream[c], h->fork, 0));
+        WB_CUDA(wb::launch_cosx_class_range(c, a, r.pair_begin, r.pair_end,
+                                            grid, h->cstream[c]));
+        WB_CUDA(cudaEventRecord(h->cdone[c], h->cstream[c]));
+        WB_CUDA(cudaStreamWaitEvent(s, h->cdone[c], 0));
+        *launches += 1;
+    }
+    WB_CUDA(wb::launch_gsum(at<float>(ws, L.gcls), h->gsrc, h->hp.nao, ldt, G, s));
+    *launches += 1;
     return WB_OK;
 }
 
@@ -365,6 +421,8 @@ int wb_cosx_create(const wb_basis* basis, const double origin[3],
     add((void**)&h->pref, hp.pref.data(), hp.pref.size() * sizeof(double));
     add((void**)&h->E, hp.E.data(), hp.E.size() * sizeof(float));
     add((void**)&h->hdr, hp.hdr.data(), hp.hdr.size() * sizeof(int32_t));
+    add((void**)&h->khdr, hp.khdr.data(), hp.khdr.size() * sizeof(int32_t));
+    add((void**)&h->gsrc, hp.gsrc.data(), hp.gsrc.size() * sizeof(int32_t));
     add((void**)&h->pshell, hp.pshell.data(), hp.pshell.size() * sizeof(int32_t));
     add((void**)&h->ptau, hp.ptau.data(), hp.ptau.size() * sizeof(float));
     add((void**)&h->bnd, hp.bnd.data(), hp.bnd.size() * sizeof(float));
@@ -402,8 +460,30 @@ int wb_cosx_create(const wb_basis* basis, const double origin[3],
     }
     if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS)
         return cleanup(fail(WB_ERR_CUBLAS, "cublasCreate failed"));
-    for (int c = 0; c < wb::NCLASS; ++c)
+    for (int c = 0; c < wb::NCLASS; ++c) {
         h->blocks_per_sm[c] = wb::cosx_class_blocks_per_sm(c);
+        h->pts[c] = wb::cosx_class_pts(c);
+        if (hp.cls[c].pair_end > hp.cls[c].pair_begin)
+            h->uses_pts[h->pts[c] - 1] = true;
+    }
+    {   // launch order: model flops of all pairs of a class, descending
+        double work[wb::NCLASS] = {0};
+        for (int c = 0; c < wb::NCLASS; ++c) {
+            h->corder[c] = c;
+            for (int k = hp.cls[c].pair_begin; k < hp.cls[c].pair_end; ++k)
+                work[c] += (double)hp.pflops[k];
+        }
+        std::stable_sort(h->corder, h->corder + wb::NCLASS,
+                         [&](int x, int y) { return work[x] > work[y]; });
+    }
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        e = cudaStreamCreateWithFlags(&h->cstream[c], cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&h->cdone[c], cudaEventDisableTiming);
+        if (e != cudaSuccess) return cleanup(cuda_fail(e, "class streams"));
+    }
+    e = cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "class streams"));
     *out = h;
     return WB_OK;
 }
@@ -411,6 +491,11 @@ int wb_cosx_create(const wb_basis* basis, const double origin[3],
 int wb_cosx_destroy(wb_cosx* h) {
     if (!h) return WB_OK;
     if (h->cublas) cublasDestroy(h->cublas);
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        if (h->cstream[c]) cudaStreamDestroy(h->cstream[c]);
+        if (h->cdone[c]) cudaEventDestroy(h->cdone[c]);
+    }
+    if (h->fork) cudaEventDestroy(h->fork);
     if (h->block) cudaFree(h->block);
     delete h;
     return WB_OK;
@@ -480,9 +565,11 @@ int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
     }
     WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.counters), 0,
                             sizeof(unsigned long long) * 3 * wb::NCLASS, s));
-    WB_CUDA(wb::launch_omega(h->hp.npp, h->p, h->pref, omega,
-                             at<float4>(workspace, L.om), s));
-    int launches = 1;
+    {
+        const int st = prepare_omega(h, omega, workspace, L, s);
+        if (st != WB_OK) return st;
+    }
+    int launches = 2;
     if (npts == 0) {
         WB_CUDA(cudaMemsetAsync(k_out, 0, sizeof(double) * nao * nao, s));
         return read_stats(h, workspace, L, 0, s, stats, launches);
@@ -591,9 +678,11 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
                                           std::to_string(L.total) + " bytes");
     WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.counters), 0,
                             sizeof(unsigned long long) * 3 * wb::NCLASS, s));
-    WB_CUDA(wb::launch_omega(h->hp.npp, h->p, h->pref, omega,
-                             at<float4>(workspace, L.om), s));
-    int launches = 1;
+    {
+        const int st = prepare_omega(h, omega, workspace, L, s);
+        if (st != WB_OK) return st;
+    }
+    int launches = 2;
     int st = run_g_tile(h, coords, weights, npts, ldt, f, g_out, tile_tol,
                         workspace, L, s, &launches);
     if (st != WB_OK) return st;

@@ -11,25 +11,34 @@ constexpr int kClasses = 10;
 //   geo[2m], geo[2m+1]   P hi (xyz, 0), P lo (xyz, 0)      molecule frame
 //   om[4m .. 4m+3]       tp_hi, tp_lo, c0_hi, c0_lo, ..., c6_hi, c6_lo
 //   Ecls[c] + (m - pp_begin[c]) * stride_c/4   packed Hermite E
-// Per pair k: hdr[k] = (ia0, ib0, pp0, npp | diag << 16), pshell[k] =
-// (virtual shell A, B), ptau[k] = (tau, tau * sum pref).
+// Per pair k: hdr[k] = (ia0, ib0, pp0, npp | diag << 16), khdr[k] = (ia0 |
+// ga0 << 16, ib0 | gb0 << 16, pp0, npp | diag << 16) with ga0 / gb0 the
+// rows of A / B in the class's partial-G buffer, pshell[k] = (virtual shell
+// A, B), ptau[k] = (tau, tau * sum pref).
 struct CosxArgs {
     const float* F;            // (nao, ld) AO-major, FP32
-    float* G;                  // (nao, ld) AO-major, FP32, accumulated
+    float* Gcls[kClasses];     // per class (rows, ld) partial G, zeroed
     long long ld;              // padded point count (multiple of 32)
     int npts;                  // valid points
     int nsub;                  // ld / 32
     const float4* geo;
     const float4* om;
+    // per class, packed per primitive pair (class-local index m):
+    // rec[c] + m * stride_c = P hi, P lo, omega record (n_om float4), E
+    const float4* rec[kClasses];
     const float4* Ecls[kClasses];
     int pp_begin[kClasses];
     const int4* hdr;
+    const int4* khdr;
     const int2* pshell;
     const float2* ptau;
     const float4* bnd;         // per pp: P (FP32), p' = 0.75 p
     const float* bpref;        // per pp: bound prefactor (rounded up)
-    const float4* sub_cr;      // per sub-block: centroid (xyz), radius
-    const float* msh;          // (nsub, nvshell): max_g w_g sum_shell |F|
+    // per block of 32 * PTS points (index PTS - 1): centroid (xyz), radius
+    // and msh (nblk, nvshell) = max_g w_g sum_shell |F|
+    const float4* blk_cr[2];
+    const float* blk_msh[2];
+    int nblk[2];
     int nvshell;
     float tol;                 // tile_tol / 1.001, <= 0 keeps every task
     const float* gxyz_hi;      // (3, ld) SoA grid coordinates, hi

@@ -6,25 +6,37 @@
 
 namespace wb {
 
-// One task of class (LA, LB): primitive-pair loop, G_B update, bra-side
-// Cartesian accumulators Xa carried across the run of tasks with the same A.
-template<int LA, int LB, bool DIAG>
-__device__ __forceinline__ void cosx_task(
-    const CosxArgs& A, const int4 hdr, const long long g,
-    const float gxh, const float gyh, const float gzh,
-    const float gxl, const float gyl, const float gzl,
-    const float4* __restrict__ stab, const float* f0, const float* fb,
-    float* Xa);
+// The inputs of one primitive pair a class reads (geo, omega record and,
+// for small classes, the Hermite E record), held in registers one pair
+// ahead of the computation.
+template<int LA, int LB> struct CosxRec;
+
+template<int LA, int LB>
+__device__ __forceinline__ void cosx_rec_load(const CosxArgs& A, const int m,
+                                              CosxRec<LA, LB>& r);
+
+// One task of class (LA, LB) on PTS grid points per lane (arrays of PTS:
+// Gp = the point's column of the class buffer (row stride ld; points past
+// the array are clamped to its last column), ok = the point exists, its
+// coordinates): loop over the class-local primitive pairs pp0 .. pp0 +
+// npp - 1, G_B update in rows gb0 .. of the class buffer, bra-side
+// Cartesian accumulators Xa
+// (PTS x NCA) carried across the run of tasks with the same A.  rec holds
+// pair pp0's record on entry and pair nxt's on exit (the next task's first
+// pair).  The DIAG form (B = A) adds its ket accumulators to Xa instead of
+// writing G_B.  Specialised per (LA, LB, DIAG) with run() as the body.
+template<int LA, int LB, bool DIAG, int PTS> struct CosxTask;
 
 // Start of a run: f0 = c2s^T F_A (Cartesian components of F on shell A).
 template<int LA>
-__device__ __forceinline__ void cosx_begin(const CosxArgs& A, const int ia0,
-                                           const long long g, float* f0);
+__device__ __forceinline__ void cosx_begin(const float* fa, float* f0);
 
-// End of a run: G_A += c2s^T Xa.
+// End of a run: G_A = c2s^T Xa, stored to rows ga0 .. of the class buffer
+// at the point Gp points to (row stride ld), if the point exists.
 template<int LA>
-__device__ __forceinline__ void cosx_end(const CosxArgs& A, const int ia0,
-                                         const long long g, const float* Xa);
+__device__ __forceinline__ void cosx_end(float* __restrict__ Gp, const int ga0,
+                                         const int ld, const bool ok,
+                                         const float* Xa);
 
 }  // namespace wb
 

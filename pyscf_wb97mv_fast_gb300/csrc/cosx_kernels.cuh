@@ -3,14 +3,20 @@
 //
 // One warp owns one 32-point sub-block at a time (one grid point per lane)
 // and walks the class's shell pairs in ascending (A, B) order: 32 pairs at
-// a time every lane loads one pair header and evaluates its screening
-// bound, a ballot compacts the kept ones, and the warp then runs each kept
-// task with all lanes (headers by shuffle, the next task's F_B prefetched
-// while the current one computes).  Tasks with the same bra shell A form a
-// run: F_A is read and G_A written once per run.  A warp takes the next
-// sub-block from a per-class counter (dynamic load balance); every G
-// element is written by exactly one lane in a fixed order, so results do
-// not depend on the launch shape or scheduling.
+// a time every lane evaluates one pair's screening bound (its header, shell
+// maxima and tau were fetched one chunk ahead), a ballot compacts the kept
+// ones, and the warp then runs each kept task with all lanes.  Headers come
+// by shuffle; while one task computes, the next task's F_B (and its F_A
+// when it opens a new run) and its first primitive-pair record are already
+// in flight.  Tasks with the same bra shell A form a run: F_A is read and
+// G_A stored once per run.
+//
+// Each class writes its own partial G buffer (rows of its two angular
+// momenta), so classes can run concurrently; a fixed-order sum over the
+// class buffers forms G.  A warp takes the next sub-block from a per-class
+// counter (dynamic load balance); every element of a class buffer is
+// written by one lane in a fixed order, so results do not depend on the
+// launch shape, the scheduling or the overlap of classes.
 //
 // The bound is the reference's locked estimate (gpu/sgx_k.py:35-46,
 // :417-456): tau * sum_prim pref F_0(p' d_min^2) * max(msh_A, msh_B) with
@@ -24,18 +30,32 @@ namespace wb {
 constexpr int kCtaThreads = 128;
 constexpr int kBoysFloat4 = 145 * 5;
 
-__device__ __forceinline__ bool screen_pair(const CosxArgs& A, int sub, int k,
-                                            const float4 cr, const int4 hdr) {
-    const int2 sh = A.pshell[k];
-    const float* ms = A.msh + (long long)sub * A.nvshell;
-    const float f = fmaxf(ms[sh.x], ms[sh.y]);
-    const float2 tp = A.ptau[k];
+// Minimum resident CTAs per SM requested per class (register cap
+// 65536 / (128 * n)), one hex digit per class in class order (0,0), (1,0),
+// (1,1), (2,0), ...; a build may override it with
+// -DWB_COSX_MIN_BLOCKS=0x<10 hex digits>LL.
+#ifndef WB_COSX_MIN_BLOCKS
+#define WB_COSX_MIN_BLOCKS 0x6544331111LL
+#endif
+constexpr int min_blocks(int cls) {
+    long long v = WB_COSX_MIN_BLOCKS;
+    for (int i = cls; i < kClasses - 1; ++i) v >>= 4;
+    return (int)(v & 15) > 0 ? (int)(v & 15) : 1;
+}
+
+// tp = (tau, tau * sum pref), f = max(msh_A, msh_B) of the block; bnd and
+// bpref start at the class's first primitive pair (hdr.z is class-local)
+__device__ __forceinline__ bool screen_pair(const float tol,
+                                            const float4* __restrict__ bnd,
+                                            const float* __restrict__ bpref,
+                                            const float4 cr, const int4 hdr,
+                                            const float2 tp, const float f) {
     // F_0 <= 1: tau * sum(pref) * f bounds the full estimate from above
-    if (tp.y * f * 1.0001f < A.tol) return false;
+    if (tp.y * f * 1.0001f < tol) return false;
     const int pp0 = hdr.z, npp = hdr.w & 0xffff;
     float b = 0.0f;
     for (int m = pp0; m < pp0 + npp; ++m) {
-        const float4 bp = A.bnd[m];
+        const float4 bp = bnd[m];
         const float dx = bp.x - cr.x, dy = bp.y - cr.y, dz = bp.z - cr.z;
         const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
         float d = dist - cr.w - 1e-5f * (dist + cr.w) - 1e-6f;
@@ -43,9 +63,9 @@ __device__ __forceinline__ bool screen_pair(const CosxArgs& A, int sub, int k,
         const float T = bp.w * d * d;
         const float f0 = (T > 1e-12f)
             ? 0.88622692545f * erff(sqrtf(T)) * rsqrtf(T) : 1.0f;
-        b += A.bpref[m] * f0;
+        b += bpref[m] * f0;
     }
-    return tp.x * b * f >= A.tol;
+    return tp.x * b * f >= tol;
 }
 
 __device__ __forceinline__ int4 shfl_int4(const int4 v, int src) {
@@ -55,107 +75,203 @@ __device__ __forceinline__ int4 shfl_int4(const int4 v, int src) {
                      __shfl_sync(0xffffffffu, v.w, src));
 }
 
-template<int LB>
-__device__ __forceinline__ void load_fb(const CosxArgs& A, const int ib0,
-                                        const long long g, float* fb) {
+// F rows n0 .. n0 + N - 1 at the point Fp points to (row stride ld)
+template<int N>
+__device__ __forceinline__ void load_f(const float* __restrict__ Fp,
+                                       const int ld, const int n0, float* f) {
 #pragma unroll
-    for (int nu = 0; nu < 2 * LB + 1; ++nu)
-        fb[nu] = A.F[(long long)(ib0 + nu) * A.ld + g];
+    for (int nu = 0; nu < N; ++nu) f[nu] = Fp[(long long)(n0 + nu) * ld];
 }
 
+__device__ __forceinline__ int lo16(const int x) { return x & 0xffff; }
+__device__ __forceinline__ int hi16(const int x) {
+    return (int)((unsigned)x >> 16);
+}
+
+// Points per lane of each class: 2 for the light classes, whose tasks have
+// one to a few primitive pairs (the per-task and per-pair overhead is then
+// shared by two points), 1 for the register-heavy ones.
+template<int LA, int LB> struct ClassPts {
+    static constexpr int value = (LA + LB <= 2) ? 2 : 1;
+};
+
 template<int LA, int LB>
-__global__ void __launch_bounds__(kCtaThreads)
+__global__ void __launch_bounds__(kCtaThreads,
+                                  min_blocks(LA * (LA + 1) / 2 + LB))
 cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
     constexpr int CLS = LA * (LA + 1) / 2 + LB;
     constexpr int NCA = (LA + 1) * (LA + 2) / 2;
+    constexpr int NA = 2 * LA + 1;
     constexpr int NB = 2 * LB + 1;
+    constexpr int PTS = ClassPts<LA, LB>::value;
     __shared__ float4 stab[kBoysFloat4];
     for (int i = threadIdx.x; i < kBoysFloat4; i += blockDim.x)
         stab[i] = A.boys[i];
     __syncthreads();
     const int lane = threadIdx.x & 31;
+    float* __restrict__ Gc = A.Gcls[CLS];
+    const int ld = (int)A.ld;
+    const float tol = A.tol;
+    const float4* __restrict__ bnd = A.bnd + A.pp_begin[CLS];
+    const float* __restrict__ bpref = A.bpref + A.pp_begin[CLS];
+    const float4* __restrict__ blk_cr = A.blk_cr[PTS - 1];
+    const float* __restrict__ blk_msh = A.blk_msh[PTS - 1];
+    const int nblk = A.nblk[PTS - 1];
     unsigned long long kept = 0, flops = 0, ints = 0;
     for (;;) {
-        int sub = 0;
-        if (lane == 0) sub = atomicAdd(A.work + CLS, 1);
-        sub = __shfl_sync(0xffffffffu, sub, 0);
-        if (sub >= A.nsub) break;
-        const long long g = (long long)sub * 32 + lane;
-        const float gxh = A.gxyz_hi[g], gyh = A.gxyz_hi[A.ld + g],
-                    gzh = A.gxyz_hi[2 * A.ld + g];
-        const float gxl = A.gxyz_lo[g], gyl = A.gxyz_lo[A.ld + g],
-                    gzl = A.gxyz_lo[2 * A.ld + g];
-        const float4 cr = A.sub_cr[sub];
-        const int nvalid = min(32, A.npts - sub * 32);
-        // run state: the current bra shell (its first AO), f0 and Xa
-        int curA = -1;
-        float f0[NCA], Xa[NCA];
+        int blk = 0;
+        if (lane == 0) blk = atomicAdd(A.work + CLS, 1);
+        blk = __shfl_sync(0xffffffffu, blk, 0);
+        if (blk >= nblk) break;
+        // the lane's points: blk * 32 PTS + 32 p + lane (clamped to the
+        // arrays; ok marks the ones that exist)
+        const float* __restrict__ Fp[PTS];
+        float* Gp[PTS];
+        bool ok[PTS];
+        float gxh[PTS], gyh[PTS], gzh[PTS], gxl[PTS], gyl[PTS], gzl[PTS];
 #pragma unroll
-        for (int c = 0; c < NCA; ++c) { f0[c] = 0.0f; Xa[c] = 0.0f; }
+        for (int p = 0; p < PTS; ++p) {
+            const int g0 = blk * (32 * PTS) + 32 * p + lane;
+            ok[p] = g0 < ld;
+            const int g = ok[p] ? g0 : ld - 1;
+            Fp[p] = A.F + g;
+            Gp[p] = Gc + g;
+            gxh[p] = A.gxyz_hi[g];
+            gyh[p] = A.gxyz_hi[ld + g];
+            gzh[p] = A.gxyz_hi[2 * (long long)ld + g];
+            gxl[p] = A.gxyz_lo[g];
+            gyl[p] = A.gxyz_lo[ld + g];
+            gzl[p] = A.gxyz_lo[2 * (long long)ld + g];
+        }
+        const float4 cr = blk_cr[blk];
+        const float* __restrict__ ms = blk_msh + (long long)blk * A.nvshell;
+        const int rem = A.npts - blk * 32 * PTS;
+        const int nvalid = rem < 32 * PTS ? (rem > 0 ? rem : 0) : 32 * PTS;
+        const int nsb = (nvalid + 31) / 32;     // 32-point sub-blocks covered
+        // run state: the current bra shell (packed header word), its class
+        // buffer row, f0 and Xa; pendA / fan: F_A prefetched for a next run
+        int curA = -1, ga0 = 0, pendA = -1;
+        float f0[PTS * NCA], Xa[PTS * NCA], fan[PTS * NA];
+#pragma unroll
+        for (int c = 0; c < PTS * NCA; ++c) { f0[c] = 0.0f; Xa[c] = 0.0f; }
+#pragma unroll
+        for (int c = 0; c < PTS * NA; ++c) fan[c] = 0.0f;
+        // screen inputs of the first chunk
+        int4 nhl = make_int4(0, 0, 0, 0);
+        float2 ntp = make_float2(0.0f, 0.0f);
+        float nfm = 0.0f;
+        {
+            const int k = pair_begin + lane;
+            if (k < pair_end) {
+                nhl = A.khdr[k];
+                ntp = A.ptau[k];
+                const int2 sh = A.pshell[k];
+                nfm = fmaxf(ms[sh.x], ms[sh.y]);
+            }
+        }
         for (int c0 = pair_begin; c0 < pair_end; c0 += 32) {
-            // every lane fetches one pair header: the screen uses it, and
-            // the kept tasks get theirs by shuffle (no dependent load)
             const int k = c0 + lane;
+            const int4 hl = nhl;
+            const float2 tp = ntp;
+            const float fm = nfm;
+            // the next chunk's header, tau and shell pair, then (after this
+            // chunk's screen) its shell maxima
+            const int kn = k + 32;
+            int2 nsh = make_int2(0, 0);
+            if (kn < pair_end) {
+                nhl = A.khdr[kn];
+                ntp = A.ptau[kn];
+                nsh = A.pshell[kn];
+            }
             bool keep = k < pair_end;
-            int4 hl = make_int4(0, 0, 0, 0);
-            if (keep) hl = A.hdr[k];
-            if (keep && A.tol > 0.0f) keep = screen_pair(A, sub, k, cr, hl);
+            if (keep && tol > 0.0f)
+                keep = screen_pair(tol, bnd, bpref, cr, hl, tp, fm);
+            if (kn < pair_end) nfm = fmaxf(ms[nsh.x], ms[nsh.y]);
             unsigned mask = __ballot_sync(0xffffffffu, keep);
             if (!mask) continue;
-            int j = __ffs(mask) - 1;
-            int4 hdr = shfl_int4(hl, j);
-            float fb[NB];
-            load_fb<LB>(A, hdr.y, g, fb);
+            int4 hdr = shfl_int4(hl, __ffs(mask) - 1);
+            float fb[PTS * NB];
+#pragma unroll
+            for (int p = 0; p < PTS; ++p)
+                load_f<NB>(Fp[p], ld, lo16(hdr.y), fb + p * NB);
+            CosxRec<LA, LB> rec;
+            cosx_rec_load<LA, LB>(A, hdr.z, rec);
             while (true) {
+                if (hdr.x != curA) {
+                    if (curA >= 0) {
+#pragma unroll
+                        for (int p = 0; p < PTS; ++p)
+                            cosx_end<LA>(Gp[p], ga0, ld, ok[p], Xa + p * NCA);
+                    }
+                    curA = hdr.x;
+                    ga0 = hi16(hdr.x);
+                    if (pendA != curA) {
+#pragma unroll
+                        for (int p = 0; p < PTS; ++p)
+                            load_f<NA>(Fp[p], ld, lo16(hdr.x), fan + p * NA);
+                        pendA = curA;
+                    }
+#pragma unroll
+                    for (int p = 0; p < PTS; ++p)
+                        cosx_begin<LA>(fan + p * NA, f0 + p * NCA);
+#pragma unroll
+                    for (int c = 0; c < PTS * NCA; ++c) Xa[c] = 0.0f;
+                }
                 mask &= mask - 1;
-                // prefetch the next kept task of this chunk
+                // prefetch the next kept task of this chunk (fan is free:
+                // f0 of the current run is formed)
                 const bool more = mask != 0u;
                 int4 hn = hdr;
-                float fbn[NB];
+                float fbn[PTS * NB];
                 if (more) {
                     hn = shfl_int4(hl, __ffs(mask) - 1);
-                    load_fb<LB>(A, hn.y, g, fbn);
-                }
-                if (hdr.x != curA) {
-                    if (curA >= 0) cosx_end<LA>(A, curA, g, Xa);
-                    curA = hdr.x;
-                    cosx_begin<LA>(A, curA, g, f0);
 #pragma unroll
-                    for (int c = 0; c < NCA; ++c) Xa[c] = 0.0f;
+                    for (int p = 0; p < PTS; ++p)
+                        load_f<NB>(Fp[p], ld, lo16(hn.y), fbn + p * NB);
+                    if (hn.x != hdr.x) {
+#pragma unroll
+                        for (int p = 0; p < PTS; ++p)
+                            load_f<NA>(Fp[p], ld, lo16(hn.x), fan + p * NA);
+                        pendA = hn.x;
+                    }
                 }
+                const int gb0 = hi16(hdr.y), pp0 = hdr.z, npp = hdr.w & 0xffff;
+                const int nxt = more ? hn.z : pp0;
                 if constexpr (LA == LB) {
                     if (hdr.w >> 16)
-                        cosx_task<LA, LB, true>(A, hdr, g, gxh, gyh, gzh, gxl,
-                                                gyl, gzl, stab, f0, fb, Xa);
+                        CosxTask<LA, LB, true, PTS>::run(
+                            A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
+                            gxl, gyl, gzl, stab, f0, fb, Xa, rec);
                     else
-                        cosx_task<LA, LB, false>(A, hdr, g, gxh, gyh, gzh, gxl,
-                                                 gyl, gzl, stab, f0, fb, Xa);
+                        CosxTask<LA, LB, false, PTS>::run(
+                            A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
+                            gxl, gyl, gzl, stab, f0, fb, Xa, rec);
                 } else {
-                    cosx_task<LA, LB, false>(A, hdr, g, gxh, gyh, gzh, gxl,
-                                             gyl, gzl, stab, f0, fb, Xa);
+                    CosxTask<LA, LB, false, PTS>::run(
+                        A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
+                        gxl, gyl, gzl, stab, f0, fb, Xa, rec);
                 }
-                if (lane == 0) {
-                    // hdr.w holds npp | diag << 16; pair index from lane j
-                    kept += 1;
-                }
+                kept += nsb;
                 if (!more) break;
                 hdr = hn;
 #pragma unroll
-                for (int nu = 0; nu < NB; ++nu) fb[nu] = fbn[nu];
+                for (int nu = 0; nu < PTS * NB; ++nu) fb[nu] = fbn[nu];
             }
             // model flops / integrals of the kept tasks of this chunk
-            const unsigned km = __ballot_sync(0xffffffffu, keep);
             if (keep) {
-                const unsigned long long fl = (unsigned long long)A.pflops[k] * nvalid;
-                const unsigned long long it = (unsigned long long)A.pnint[k] * nvalid;
-                flops += fl;
-                ints += it;
+                flops += (unsigned long long)A.pflops[k] * nvalid;
+                ints += (unsigned long long)A.pnint[k] * nvalid;
             }
-            (void)km;
         }
-        if (curA >= 0) cosx_end<LA>(A, curA, g, Xa);
+        if (curA >= 0) {
+#pragma unroll
+            for (int p = 0; p < PTS; ++p)
+                cosx_end<LA>(Gp[p], ga0, ld, ok[p], Xa + p * NCA);
+        }
     }
-    // lane 0 counted the tasks, every lane its own pairs' flops / integrals
+    // lane 0 counted the tasks (every lane runs every task) in units of the
+    // 32-point sub-blocks they cover; every lane counted the flops /
+    // integrals of its own pairs
     for (int o = 16; o > 0; o >>= 1) {
         flops += __shfl_xor_sync(0xffffffffu, flops, o);
         ints += __shfl_xor_sync(0xffffffffu, ints, o);

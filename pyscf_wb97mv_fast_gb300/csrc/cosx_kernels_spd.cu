@@ -49,4 +49,19 @@ int cosx_class_blocks_per_sm(int cls) {
     }
 }
 
+int cosx_class_pts(int cls) {
+    switch (cls) {
+    case 0: return ClassPts<0, 0>::value;
+    case 1: return ClassPts<1, 0>::value;
+    case 2: return ClassPts<1, 1>::value;
+    case 3: return ClassPts<2, 0>::value;
+    case 4: return ClassPts<2, 1>::value;
+    case 5: return ClassPts<2, 2>::value;
+    case 6: return ClassPts<3, 0>::value;
+    case 7: return ClassPts<3, 1>::value;
+    case 8: return ClassPts<3, 2>::value;
+    default: return ClassPts<3, 3>::value;
+    }
+}
+
 }  // namespace wb

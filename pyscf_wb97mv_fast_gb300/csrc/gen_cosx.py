@@ -224,17 +224,15 @@ def gen_transform_out(l, src, dst, ind, lines):
 
 
 def gen_begin(la):
-    """f0 = c2s^T F_A of the run's A shell (loaded once per run)."""
+    """f0 = c2s^T F_A of the run's A shell (F_A loaded by the caller)."""
     na = 2 * la + 1
     nca = (la + 1) * (la + 2) // 2
     lines = ['template<> __device__ __forceinline__ void cosx_begin<%d>(' % la,
-             '    const CosxArgs& A, const int ia0, const long long g, float* f0)',
+             '    const float* fa_in, float* f0)',
              '{']
     I = '    '
-    lines.append(I + 'const long long ld = A.ld;')
     for mu in range(na):
-        lines.append(I + 'const float fa%d = A.F[(long long)(ia0 + %d) * ld + g];'
-                     % (mu, mu))
+        lines.append(I + 'const float fa%d = fa_in[%d];' % (mu, mu))
     gen_transform_in(la, 'fa', 'c', I, lines)
     for c in range(nca):
         lines.append(I + 'f0[%d] = c%d;' % (c, c))
@@ -243,88 +241,95 @@ def gen_begin(la):
 
 
 def gen_end(la):
-    """G_A += c2s^T X at the end of a run."""
+    """G_A = c2s^T X at the end of a run: a plain store into the class's
+    partial-G buffer (no other task of the class writes the row before)."""
     na = 2 * la + 1
     nca = (la + 1) * (la + 2) // 2
     lines = ['template<> __device__ __forceinline__ void cosx_end<%d>(' % la,
-             '    const CosxArgs& A, const int ia0, const long long g, const float* Xa)',
+             '    float* __restrict__ Gp, const int ga0, const int ld,',
+             '    const bool ok, const float* Xa)',
              '{']
     I = '    '
-    lines.append(I + 'const long long ld = A.ld;')
     for c in range(nca):
         lines.append(I + 'const float X%d = Xa[%d];' % (c, c))
-    gen_transform_out(la, 'X', 'ga', I, lines)
+    gen_transform_out(la, 'X', 'gv', I, lines)
+    lines.append(I + 'if (!ok) return;')
     for mu in range(na):
-        lines.append(I + 'A.G[(long long)(ia0 + %d) * ld + g] += ga%d;' % (mu, mu))
+        lines.append(I + 'Gp[(long long)(ga0 + %d) * ld] = gv%d;' % (mu, mu))
     lines.append('}')
     return '\n'.join(lines)
 
 
-def gen_class(la, lb, diag):
+def n_om(la, lb):
+    """float4 per primitive pair of the omega record a class reads."""
+    return 1 + (la + lb + 1) // 2
+
+
+def pipe_e(la, lb):
+    """Whether the Hermite E record is prefetched one primitive pair ahead
+    (small records only: the prefetch doubles its registers)."""
+    return e_stride(la, lb) // 4 <= 6 and (la + lb) >= 1
+
+
+def rec_stride(la, lb):
+    """float4 per primitive pair of a class's packed record: geo (P hi,
+    P lo), the omega record's first n_om float4, the Hermite E block."""
+    return 2 + n_om(la, lb) + e_stride(la, lb) // 4
+
+
+def gen_rec(la, lb):
+    """Per-class record of one primitive pair (geo, omega and, for small
+    classes, E) and its loader: the task loop keeps the next pair's record
+    in flight while it computes the current one.  m is class-local."""
+    nom = n_om(la, lb)
+    nvec = e_stride(la, lb) // 4 if pipe_e(la, lb) else 0
+    mem = ['g0', 'g1'] + ['o%d' % q for q in range(nom)] + \
+          ['e%d' % q for q in range(nvec)]
+    lines = ['template<> struct CosxRec<%d, %d> {' % (la, lb),
+             '    float4 %s;' % ', '.join(mem),
+             '};',
+             'template<> __device__ __forceinline__ void cosx_rec_load<%d, %d>(' % (la, lb),
+             '    const CosxArgs& A, const int m, CosxRec<%d, %d>& r)' % (la, lb),
+             '{']
+    I = '    '
+    lines.append(I + 'const float4* __restrict__ q = A.rec[%d] + (long long)m * %d;'
+                 % (class_id(la, lb), rec_stride(la, lb)))
+    lines.append(I + 'r.g0 = __ldg(q);')
+    lines.append(I + 'r.g1 = __ldg(q + 1);')
+    for k in range(nom):
+        lines.append(I + 'r.o%d = __ldg(q + %d);' % (k, 2 + k))
+    for k in range(nvec):
+        lines.append(I + 'r.e%d = __ldg(q + %d);' % (k, 2 + nom + k))
+    lines.append('}')
+    return '\n'.join(lines)
+
+
+def gen_prim_body(la, lb, diag, rv, J, lines):
+    """Work of primitive pair m with its record in variable rv, for each of
+    the PTS points of the lane: Boys, R recurrence, Hermite sums and the Y
+    (and X) accumulation.  The record and E are shared by the points."""
     L = la + lb
-    nb = 2 * lb + 1
     ca = cart_components(la)
     cb = cart_components(lb)
     ents = e_entries(la, lb)
     est = e_stride(la, lb)
-    lines = []
-    I = '    '
-    lines.append('template<> __device__ __forceinline__ void cosx_task<%d, %d, %s>('
-                 % (la, lb, 'true' if diag else 'false'))
-    lines.append('    const CosxArgs& A, const int4 hdr, const long long g,')
-    lines.append('    const float gxh, const float gyh, const float gzh,')
-    lines.append('    const float gxl, const float gyl, const float gzl,')
-    lines.append('    const float4* __restrict__ stab, const float* f0,')
-    lines.append('    const float* fb, float* Xa)')
-    lines.append('{')
-    lines.append(I + 'const long long ld = A.ld;')
-    lines.append(I + 'const int ib0 = hdr.y, pp0 = hdr.z;')
-    lines.append(I + 'const int npp = hdr.w & 0xffff;')
-    for c in range(len(ca)):
-        lines.append(I + 'const float f0_%d = f0[%d];' % (c, c))
-    if not diag:
-        for nu in range(nb):
-            lines.append(I + 'const float fb%d = fb[%d];' % (nu, nu))
-        gen_transform_in(lb, 'fb', 'h0_', I, lines)
-        for c in range(len(ca)):
-            lines.append(I + 'float X%d = Xa[%d];' % (c, c))
-    for c in range(len(cb)):
-        lines.append(I + 'float Y%d = 0.0f;' % c)
+    nom = n_om(la, lb)
+    nvec = est // 4
+    comp = 'xyzw'
     tuv = [(t, u, v) for t in range(L + 1) for u in range(L + 1 - t)
            for v in range(L + 1 - t - u)]
-    lines.append(I + 'const float4* __restrict__ geo = A.geo;')
-    lines.append(I + 'const float4* __restrict__ om = A.om;')
-    if ents:
-        lines.append(I + 'const float4* __restrict__ Eb = A.Ecls[%d];' % class_id(la, lb))
-        lines.append(I + 'const int ppb = A.pp_begin[%d];' % class_id(la, lb))
-    lines.append(I + '#pragma unroll 1')
-    lines.append(I + 'for (int m = pp0; m < pp0 + npp; ++m) {')
-    J = I * 2
-    lines.append(J + 'const float4 ph = __ldg(geo + 2 * m);')
-    lines.append(J + 'const float4 pl = __ldg(geo + 2 * m + 1);')
-    lines.append(J + 'const float dx = (ph.x - gxh) + (pl.x - gxl);')
-    lines.append(J + 'const float dy = (ph.y - gyh) + (pl.y - gyl);')
-    lines.append(J + 'const float dz = (ph.z - gzh) + (pl.z - gzl);')
-    lines.append(J + 'const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));')
-    nom = 1 + (L + 1) // 2
+    lines.append(J + 'const float4 ph = %s.g0, pl = %s.g1;' % (rv, rv))
     for q in range(nom):
-        lines.append(J + 'const float4 o%d = __ldg(om + 4 * (long long)m + %d);' % (q, q))
-    lines.append(J + 'const float T = fmaf(o0.x, r2, o0.y * r2);')
-    lines.append(J + 'float Fb[%d];' % (L + 1))
-    lines.append(J + 'boys_fp32<%d>(T, Fb, stab);' % L)
-    comp = 'xyzw'
-    for n in range(L + 1):
-        fh = 2 + 2 * n
-        fl = fh + 1
-        ch = 'o%d.%s' % (fh // 4, comp[fh % 4])
-        cl = 'o%d.%s' % (fl // 4, comp[fl % 4])
-        lines.append(J + 'const float R000_%d = fmaf(%s, Fb[%d], %s * Fb[%d]);'
-                     % (n, ch, n, cl, n))
-    lines.append(J + 'float ' + ', '.join(rname(*x) for x in tuv) + ';')
-    gen_recurrence(L, lines, J)
+        lines.append(J + 'const float4 o%d = %s.o%d;' % (q, rv, q))
     if ents:
-        nvec = est // 4
-        lines.append(J + 'const float4* __restrict__ Em = Eb + (long long)(m - ppb) * %d;' % nvec)
+        if pipe_e(la, lb):
+            for q in range(nvec):
+                lines.append(J + 'const float4 ev%d = %s.e%d;' % (q, rv, q))
+        else:
+            lines.append(J + 'const float4* __restrict__ Em = A.rec[%d] + (long long)m * %d + %d;'
+                         % (class_id(la, lb), rec_stride(la, lb), 2 + nom))
+            for q in range(nvec):
+                lines.append(J + 'const float4 ev%d = __ldg(Em + %d);' % (q, q))
         flat = []
         for ax in range(3):
             for (i, j, t) in ents:
@@ -332,39 +337,140 @@ def gen_class(la, lb, diag):
         while len(flat) % 4:
             flat.append(None)
         for q in range(nvec):
-            lines.append(J + 'const float4 ev%d = __ldg(Em + %d);' % (q, q))
             for c in range(4):
                 nm = flat[4 * q + c]
                 if nm is not None:
                     lines.append(J + 'const float %s = ev%d.%s;' % (nm, q, comp[c]))
+    lines.append(J + '#pragma unroll')
+    lines.append(J + 'for (int p = 0; p < PTS; ++p) {')
+    K = J + '    '
+    lines.append(K + 'const float dx = (ph.x - gxh[p]) + (pl.x - gxl[p]);')
+    lines.append(K + 'const float dy = (ph.y - gyh[p]) + (pl.y - gyl[p]);')
+    lines.append(K + 'const float dz = (ph.z - gzh[p]) + (pl.z - gzl[p]);')
+    lines.append(K + 'const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));')
+    lines.append(K + 'const float T = fmaf(o0.x, r2, o0.y * r2);')
+    lines.append(K + 'float Fb[%d];' % (L + 1))
+    lines.append(K + 'boys_fp32<%d>(T, Fb, stab);' % L)
+    for n in range(L + 1):
+        fh = 2 + 2 * n
+        fl = fh + 1
+        ch = 'o%d.%s' % (fh // 4, comp[fh % 4])
+        cl = 'o%d.%s' % (fl // 4, comp[fl % 4])
+        lines.append(K + 'const float R000_%d = fmaf(%s, Fb[%d], %s * Fb[%d]);'
+                     % (n, ch, n, cl, n))
+    lines.append(K + 'float ' + ', '.join(rname(*x) for x in tuv) + ';')
+    gen_recurrence(L, lines, K)
     for ia, cac in enumerate(ca):
         for ib, cbc in enumerate(cb):
             tag = '%d_%d' % (ia, ib)
-            sv = gen_hermite(la, lb, cac, cbc, J, lines, tag)
-            lines.append(J + 'Y%d = fmaf(f0_%d, %s, Y%d);' % (ib, ia, sv, ib))
+            sv = gen_hermite(la, lb, cac, cbc, K, lines, tag)
+            lines.append(K + 'Yv[p][%d] = fmaf(f0v[p][%d], %s, Yv[p][%d]);'
+                         % (ib, ia, sv, ib))
             if not diag:
-                lines.append(J + 'X%d = fmaf(%s, h0_%d, X%d);' % (ia, sv, ib, ia))
-    lines.append(I + '}')
-    gen_transform_out(lb, 'Y', 'gb', I, lines)
-    for nu in range(nb):
-        lines.append(I + 'A.G[(long long)(ib0 + %d) * ld + g] += gb%d;' % (nu, nu))
+                lines.append(K + 'Xv[p][%d] = fmaf(%s, h0v[p][%d], Xv[p][%d]);'
+                             % (ia, sv, ib, ia))
+    lines.append(J + '}')
+
+
+def gen_class(la, lb, diag):
+    nb = 2 * lb + 1
+    nca = (la + 1) * (la + 2) // 2
+    ncb = (lb + 1) * (lb + 2) // 2
+    ents = e_entries(la, lb)
+    lines = []
+    I = '    '
+    lines.append('template<int PTS> struct CosxTask<%d, %d, %s, PTS> {'
+                 % (la, lb, 'true' if diag else 'false'))
+    lines.append('static __device__ __forceinline__ void run(')
+    lines.append('    const CosxArgs& A, float* const* Gp, const int ld, const int gb0,')
+    lines.append('    const int pp0, const int npp, const int nxt, const bool* ok,')
+    lines.append('    const float* gxh, const float* gyh, const float* gzh,')
+    lines.append('    const float* gxl, const float* gyl, const float* gzl,')
+    lines.append('    const float4* __restrict__ stab, const float* f0,')
+    lines.append('    const float* fb, float* Xa, CosxRec<%d, %d>& rec)' % (la, lb))
+    lines.append('{')
+    lines.append(I + 'float f0v[PTS][%d], Yv[PTS][%d];' % (nca, ncb))
     if not diag:
-        for c in range(len(ca)):
-            lines.append(I + 'Xa[%d] = X%d;' % (c, c))
+        lines.append(I + 'float gbo[PTS][%d], h0v[PTS][%d], Xv[PTS][%d];'
+                     % (nb, ncb, nca))
+    lines.append(I + '#pragma unroll')
+    lines.append(I + 'for (int p = 0; p < PTS; ++p) {')
+    J = I * 2
+    if not diag:
+        # G_B read early: its latency overlaps the primitive loop
+        for nu in range(nb):
+            lines.append(J + 'gbo[p][%d] = Gp[p][(long long)(gb0 + %d) * ld];'
+                         % (nu, nu))
+        for nu in range(nb):
+            lines.append(J + 'const float fb%d = fb[p * %d + %d];' % (nu, nb, nu))
+        gen_transform_in(lb, 'fb', 'h0_', J, lines)
+        for c in range(ncb):
+            lines.append(J + 'h0v[p][%d] = h0_%d;' % (c, c))
+        for c in range(nca):
+            lines.append(J + 'Xv[p][%d] = Xa[p * %d + %d];' % (c, nca, c))
+    for c in range(nca):
+        lines.append(J + 'f0v[p][%d] = f0[p * %d + %d];' % (c, nca, c))
+    for c in range(ncb):
+        lines.append(J + 'Yv[p][%d] = 0.0f;' % c)
+    lines.append(I + '}')
+    lines.append(I + 'const int pend = pp0 + npp;')
+    # two register sets for the primitive-pair record (rec, rb) used in
+    # turn: while one pair computes, the next one loads into the other set
+    lines.append(I + 'CosxRec<%d, %d> rb;' % (la, lb))
+    lines.append(I + 'int m = pp0;')
+    lines.append(I + '#pragma unroll 1')
+    lines.append(I + 'while (true) {')
+    lines.append(J + 'cosx_rec_load<%d, %d>(A, m + 1 < pend ? m + 1 : nxt, rb);'
+                 % (la, lb))
+    lines.append(J + '{')
+    gen_prim_body(la, lb, diag, 'rec', J + I, lines)
+    lines.append(J + '}')
+    lines.append(J + 'if (++m == pend) { rec = rb; break; }')
+    lines.append(J + 'cosx_rec_load<%d, %d>(A, m + 1 < pend ? m + 1 : nxt, rec);'
+                 % (la, lb))
+    lines.append(J + '{')
+    gen_prim_body(la, lb, diag, 'rb', J + I, lines)
+    lines.append(J + '}')
+    lines.append(J + 'if (++m == pend) break;')
+    lines.append(I + '}')
+    lines.append(I + '#pragma unroll')
+    lines.append(I + 'for (int p = 0; p < PTS; ++p) {')
+    if diag:
+        # B = A: the ket contribution joins the run's bra accumulator, which
+        # cosx_end transforms and stores once
+        for c in range(ncb):
+            lines.append(J + 'Xa[p * %d + %d] += Yv[p][%d];' % (nca, c, c))
+    else:
+        for c in range(ncb):
+            lines.append(J + 'const float Y%d = Yv[p][%d];' % (c, c))
+        gen_transform_out(lb, 'Y', 'gy', J, lines)
+        lines.append(J + 'if (ok[p]) {')
+        for nu in range(nb):
+            lines.append(J + '    Gp[p][(long long)(gb0 + %d) * ld] = gbo[p][%d] + gy%d;'
+                         % (nu, nu, nu))
+        lines.append(J + '}')
+        for c in range(nca):
+            lines.append(J + 'Xa[p * %d + %d] = Xv[p][%d];' % (nca, c, c))
+    lines.append(I + '}')
     lines.append('}')
+    lines.append('};')
     return '\n'.join(lines)
 
 
 def source():
     out = ['// Generated by csrc/gen_cosx.py -- do not edit by hand.',
            '// One straight-line task body per shell-pair class (la >= lb),',
-           '// plus the per-run begin (F_A -> Cartesian f0) and end',
-           '// (G_A += c2s^T X) of each bra angular momentum.',
+           '// its primitive-pair record and loader, plus the per-run begin',
+           '// (F_A -> Cartesian f0) and end (G_A = c2s^T X) of each bra',
+           '// angular momentum.',
            '#pragma once', '']
     for la in range(LMAX + 1):
         out.append(gen_begin(la))
         out.append('')
         out.append(gen_end(la))
+        out.append('')
+    for (la, lb) in classes():
+        out.append(gen_rec(la, lb))
         out.append('')
     for (la, lb) in classes():
         out.append(gen_class(la, lb, False))
@@ -379,11 +485,23 @@ def source():
     return '\n'.join(out)
 
 
-def write(path=None):
-    if path is None:
-        path = os.path.join(HERE, 'generated', 'cosx_classes.cuh')
+def layout_source():
+    """Host-visible constants of the packed primitive-pair records."""
+    cl = classes()
+    return '\n'.join([
+        '// Generated by csrc/gen_cosx.py -- do not edit by hand.',
+        '// Packed primitive-pair record of each class (class order):',
+        '// float4 count = 2 (P hi, P lo) + n_om (omega record) + n_e (E).',
+        '#pragma once', '',
+        'namespace wb {',
+        'constexpr int kRecNom[10] = {%s};' % ', '.join(str(n_om(a, b)) for a, b in cl),
+        'constexpr int kRecNe[10] = {%s};' % ', '.join(str(e_stride(a, b) // 4) for a, b in cl),
+        'constexpr int kRecStride[10] = {%s};' % ', '.join(str(rec_stride(a, b)) for a, b in cl),
+        '}  // namespace wb', ''])
+
+
+def _write_if_changed(path, src):
     os.makedirs(os.path.dirname(path), exist_ok=True)
-    src = source()
     old = None
     if os.path.exists(path):
         with open(path) as fh:
@@ -391,6 +509,14 @@ def write(path=None):
     if old != src:
         with open(path, 'w') as fh:
             fh.write(src)
+
+
+def write(path=None):
+    if path is None:
+        path = os.path.join(HERE, 'generated', 'cosx_classes.cuh')
+    _write_if_changed(path, source())
+    _write_if_changed(os.path.join(os.path.dirname(path), 'cosx_layout.h'),
+                      layout_source())
     return path
 
 

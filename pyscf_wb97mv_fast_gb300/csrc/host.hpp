@@ -57,6 +57,9 @@ struct HostPairs {
     std::vector<VShell> vsh;
     // per pair (device order: sorted by class)
     std::vector<int32_t> hdr;       // 4 per pair: ia0, ib0, pp0, npp|diag<<16
+    // kernel form of hdr: ia0 | ga0 << 16, ib0 | gb0 << 16, pp0, npp|diag<<16
+    // with ga0 / gb0 the rows of A / B in the class's partial-G buffer
+    std::vector<int32_t> khdr;
     std::vector<int32_t> pshell;    // 2 per pair: vshell A, vshell B
     std::vector<float> ptau;        // 2 per pair: tau, tau * sum(pref)
     std::vector<int32_t> pclass, pish, pjsh;
@@ -69,6 +72,19 @@ struct HostPairs {
     std::vector<float> bpref;       // bound prefactor, rounded up
     std::vector<float> E;           // per class blocks, e_stride per pp
     ClassRange cls[NCLASS];
+    // per-class partial G buffers: class (la, lb) holds the AOs of the
+    // l = la shells (rows 0 ..) then, for lb != la, those of the l = lb
+    // shells, each group in AO order
+    int nlao[LMAX + 1] = {0, 0, 0, 0};   // AOs per angular momentum
+    int crow[NCLASS] = {0};              // rows of each class buffer
+    int64_t crow_base[NCLASS] = {0};     // first row of each class buffer
+    int64_t ncrow = 0;                   // rows of all class buffers
+    std::vector<int32_t> gsrc;           // 4 per AO: class-buffer rows that
+                                         // sum to G, ascending class, -1 pad
+    // packed per-class primitive-pair records (geo, omega record, E) that
+    // the class kernels read; rebuilt per omega
+    int64_t rec_off[NCLASS] = {0};       // float4 offset of each class
+    int64_t nrec = 0;                    // float4 in all classes
     // per virtual shell (for the sub-block statistics)
     std::vector<int32_t> vs_ao0, vs_nf;
 };

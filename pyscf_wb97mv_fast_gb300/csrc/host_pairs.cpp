@@ -19,6 +19,7 @@
 #include <numeric>
 
 #include "host.hpp"
+#include "generated/cosx_layout.h"
 
 namespace wb {
 
@@ -277,12 +278,21 @@ int build_pairs(const wb_basis& b, const double origin[3], double cutoff,
         }
         ao += nc * nsph(l);
     }
+    if (ao > 65535) {
+        err = "nao=" + std::to_string(ao) + " exceeds 65535 (16-bit packed rows)";
+        return WB_ERR_UNSUPPORTED;
+    }
     out.nao = ao;
     out.nbas_phys = b.nbas;
     out.nvshell = (int)out.vsh.size();
-    for (const VShell& v : out.vsh) {
+    // position of each virtual shell's first AO among the AOs of its l
+    std::vector<int> lrow(out.vsh.size());
+    for (size_t s = 0; s < out.vsh.size(); ++s) {
+        const VShell& v = out.vsh[s];
         out.vs_ao0.push_back(v.ao0);
         out.vs_nf.push_back(nsph(v.l));
+        lrow[s] = out.nlao[v.l];
+        out.nlao[v.l] += nsph(v.l);
     }
     const double s_fold[LMAX + 1] = {cart2sph(0)[0], cart2sph(1)[0], 1.0, 1.0};
     double tau_l[LMAX + 1];
@@ -355,6 +365,14 @@ int build_pairs(const wb_basis& b, const double origin[3], double cutoff,
         out.hdr.push_back(B.ao0);
         out.hdr.push_back(pp);
         out.hdr.push_back(npp | (diag ? (1 << 16) : 0));
+        {
+            const int ga0 = lrow[c.A];
+            const int gb0 = (la != lb ? out.nlao[la] : 0) + lrow[c.B];
+            out.khdr.push_back((int32_t)((uint32_t)A.ao0 | ((uint32_t)ga0 << 16)));
+            out.khdr.push_back((int32_t)((uint32_t)B.ao0 | ((uint32_t)gb0 << 16)));
+            out.khdr.push_back(pp - out.cls[c.cls].pp_begin);    // class-local
+            out.khdr.push_back(npp | (diag ? (1 << 16) : 0));
+        }
         out.pshell.push_back(c.A);
         out.pshell.push_back(c.B);
         out.pclass.push_back(c.cls);
@@ -436,6 +454,56 @@ int build_pairs(const wb_basis& b, const double origin[3], double cutoff,
             out.cls[c].pp_begin = out.cls[c].pp_end = 0;
         }
     out.npp = pp;
+    // class partial-G buffers and the rows each AO of G sums
+    int64_t base = 0;
+    for (int la = 0; la <= LMAX; ++la)
+        for (int lb = 0; lb <= la; ++lb) {
+            const int c = class_of(la, lb);
+            const bool used = out.cls[c].pair_end > out.cls[c].pair_begin;
+            out.crow[c] = used ? out.nlao[la] + (la != lb ? out.nlao[lb] : 0) : 0;
+            out.crow_base[c] = base;
+            base += out.crow[c];
+        }
+    out.ncrow = base;
+    // packed primitive-pair records (float4 offsets per class)
+    for (int la = 0; la <= LMAX; ++la)
+        for (int lb = 0; lb <= la; ++lb) {
+            const int c = class_of(la, lb);
+            if (kRecNe[c] * 4 != e_stride(la, lb) || kRecNom[c] != 1 + (la + lb + 1) / 2 ||
+                kRecStride[c] != 2 + kRecNom[c] + kRecNe[c]) {
+                err = "generated record layout does not match the pair tables";
+                return WB_ERR_UNSUPPORTED;
+            }
+        }
+    int64_t roff = 0;
+    for (int c = 0; c < NCLASS; ++c) {
+        out.rec_off[c] = roff;
+        roff += (int64_t)(out.cls[c].pp_end - out.cls[c].pp_begin) * kRecStride[c];
+    }
+    out.nrec = roff;
+    out.gsrc.assign(4 * (size_t)out.nao, -1);
+    for (size_t s = 0; s < out.vsh.size(); ++s) {
+        const VShell& v = out.vsh[s];
+        for (int comp = 0; comp < nsph(v.l); ++comp) {
+            int n = 0;
+            for (int c = 0; c < NCLASS; ++c) {
+                if (!out.crow[c]) continue;
+                int la = 0, lb = 0;
+                for (int x = 0; x <= LMAX; ++x)
+                    for (int y = 0; y <= x; ++y)
+                        if (class_of(x, y) == c) { la = x; lb = y; }
+                int64_t row = -1;
+                if (la == v.l) row = out.crow_base[c] + lrow[s] + comp;
+                else if (lb == v.l) row = out.crow_base[c] + out.nlao[la] + lrow[s] + comp;
+                if (row < 0) continue;
+                if (row > INT32_MAX) {
+                    err = "partial-G rows exceed 2^31";
+                    return WB_ERR_UNSUPPORTED;
+                }
+                out.gsrc[4 * (size_t)(v.ao0 + comp) + n++] = (int32_t)row;
+            }
+        }
+    }
     return WB_OK;
 }
 

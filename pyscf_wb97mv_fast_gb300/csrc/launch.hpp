@@ -36,16 +36,34 @@ cudaError_t upload_c2s_tables(const double* t0, const double* t1,
                               const double* t2, const double* t3);
 cudaError_t upload_c2s_f(const float* all /* 4 x 70 */);
 
+// class ranges and record layout for launch_pack_records (classes with no
+// primitive pairs have pp_begin == pp_end)
+struct RecPack {
+    int pp_begin[10], pp_end[10], stride[10], nom[10], ne[10];
+    long long rec_off[10];      // float4 offset of the class's records
+    long long e_off[10];        // float4 offset of the class's E block
+};
+cudaError_t launch_pack_records(const RecPack& P, int npp, const float4* geo,
+                                const float4* om, const float4* E,
+                                float4* rec, cudaStream_t s);
 cudaError_t launch_omega(int npp, const double* p, const double* pref,
                          double omega, float4* om, cudaStream_t s);
 cudaError_t launch_grid_prep(const double* coords, int64_t npts, int64_t ld,
                              float* hi, float* lo, cudaStream_t s);
+// centroid / radius and shell maxima per block of block_pts (32 or 64)
+// points: ceil(ld / block_pts) blocks
 cudaError_t launch_sub_stats(const double* coords, const double* weights,
                              const float* F, int64_t npts, int64_t ld,
                              int nvshell, const int* vs_ao0, const int* vs_nf,
-                             float4* sub_cr, float* msh, cudaStream_t s);
+                             int block_pts, float4* sub_cr, float* msh,
+                             cudaStream_t s);
+// points per lane (1 or 2) of a class kernel: its blocks hold 32 * pts
+int cosx_class_pts(int cls);
 cudaError_t launch_f64_to_f32(const double* in, float* out, int64_t n,
                               cudaStream_t s);
+// G = fixed-order sum of the class partial-G rows (4 source rows per AO)
+cudaError_t launch_gsum(const float* gc, const int4* src, int nao, int64_t ld,
+                        float* G, cudaStream_t s);
 cudaError_t launch_weight_g(const float* G, const double* w, int64_t npts,
                             int64_t ld, int nao, double* out, cudaStream_t s);
 cudaError_t launch_dense_impl(const CosxArgs& a, int npairs, const int* pclass,
