@@ -59,13 +59,40 @@ __device__ __forceinline__ int exp_of_bits(unsigned long long absbits) {
     return e > 500 ? 500 : e;
 }
 
+// q = rint(x 2^(W-1-e)) from the bit pattern of x with integer arithmetic:
+// |x| = m 2^p (m the 53-bit significand), shifted right with round half to
+// even -- the same integer as an exact FP64 scaling followed by
+// round-to-nearest, without the FP64 pipe (1/64 of the FP32 rate on GB300)
+__device__ __forceinline__ long long fixed_q(double x, int e) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((b >> 52) & 0x7ff);
+    unsigned long long m = b & 0xfffffffffffffull;
+    int p = -1074;
+    if (E) { m |= 1ull << 52; p = E - 1075; }
+    const int sh = p + kW - 1 - e;
+    unsigned long long q = 0;
+    if (m) {
+        if (sh >= 0) {
+            // only small m (|x| < 2^e keeps q below 2^(W-1))
+            q = m << (sh < 11 ? sh : 11);
+        } else if (sh > -64) {
+            const int r = -sh;
+            q = m >> r;
+            const unsigned long long rem = m & ((1ull << r) - 1);
+            const unsigned long long half = 1ull << (r - 1);
+            if (rem > half || (rem == half && (q & 1ull))) ++q;
+        }
+    }
+    return (b >> 63) ? -(long long)q : (long long)q;
+}
+
 template<int S>
 __device__ __forceinline__ void digits(double x, int e, float* d) {
     // q (|q| < 2^(W-1) = 2^41) split as q = hi 2^24 + lo, lo in [0, 2^24):
     // the four low digits come from lo, the carry goes into hi, the rest
     // from hi -- 32-bit integer arithmetic throughout
     static_assert(S == 7 && kB == 6, "digit split assumes 7 x 6 bits");
-    const long long q = __double2ll_rn(x * pow2(kW - 1 - e));
+    const long long q = fixed_q(x, e);
     int lo = (int)(q & 0xFFFFFF);
     int hi = (int)(q >> 24);
 #pragma unroll
@@ -84,13 +111,43 @@ __device__ __forceinline__ void digits(double x, int e, float* d) {
     d[0] = (float)hi;
 }
 
+// RN(v 2^sc) as FP32 from the int64 v with integer arithmetic (one
+// rounding); results outside the normal FP32 range take the FP64 path
+__device__ __forceinline__ float scaled_ll_to_float(long long v, int sc) {
+    if (v == 0) return 0.0f;
+    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v
+                                       : (unsigned long long)v;
+    const int nb = 64 - __clzll((long long)a);
+    unsigned long long q;
+    int e2;
+    if (nb > 24) {
+        int r = nb - 24;
+        q = a >> r;
+        const unsigned long long rem = a & ((1ull << r) - 1);
+        const unsigned long long half = 1ull << (r - 1);
+        if (rem > half || (rem == half && (q & 1ull))) ++q;
+        if (q == (1ull << 24)) { q >>= 1; ++r; }
+        e2 = r;
+    } else {
+        q = a << (24 - nb);
+        e2 = nb - 24;
+    }
+    const int E = e2 + sc + 23 + 127;
+    if (E <= 0 || E >= 255)
+        return __double2float_rn((double)v * pow2(sc < -1000 ? -1000 : (sc > 1000 ? 1000 : sc)));
+    const unsigned bits = ((unsigned)E << 23) | ((unsigned)q & 0x7fffffu) |
+                          (v < 0 ? 0x80000000u : 0u);
+    return __uint_as_float(bits);
+}
+
 // value of the combined levels: sum_l C_l 2^(B (S-1-l)) as an exact int64
+// (every level is an integer below 2^24 in magnitude: 32-bit conversion)
 template<int S>
 __device__ __forceinline__ long long combine_levels(const float* c) {
     long long acc = 0;
 #pragma unroll
     for (int l = 0; l < S; ++l)
-        acc += ((long long)__float2ll_rn(c[l])) << (kB * (S - 1 - l));
+        acc += ((long long)__float2int_rn(c[l])) << (kB * (S - 1 - l));
     return acc;
 }
 
@@ -101,28 +158,48 @@ __device__ __forceinline__ long long combine_levels(const float* c) {
 // A_all (ld x S*nao, col-major): column block i = slice i.
 // B_all (S*nao x nao, col-major): row block r = slice S-1-r.
 // ---------------------------------------------------------------------------
-template<int S>
-__global__ void f_slice_x_kernel(const double* __restrict__ X, int nao,
-                                 int64_t ld, int* __restrict__ erow,
-                                 __nv_bfloat16* __restrict__ A) {
+// exponent of max_l |X(l, g)| per point g: eight rows in flight per thread
+__global__ void f_rowmax_kernel(const double* __restrict__ X, int nao,
+                                int64_t ld, int* __restrict__ erow) {
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ld) return;
+    const unsigned long long* Xb = reinterpret_cast<const unsigned long long*>(X);
     unsigned long long m = 0;
-    for (int l = 0; l < nao; ++l) {
-        const unsigned long long b =
-            (unsigned long long)__double_as_longlong(X[(int64_t)l * ld + g]) &
-            0x7fffffffffffffffull;
-        m = b > m ? b : m;
-    }
-    const int e = exp_of_bits(m);
-    erow[g] = e;
-    for (int l = 0; l < nao; ++l) {
-        float d[S];
-        digits<S>(X[(int64_t)l * ld + g], e, d);
+    int l = 0;
+    for (; l + 8 <= nao; l += 8) {
+        unsigned long long b[8];
 #pragma unroll
-        for (int i = 0; i < S; ++i)
-            A[((int64_t)i * nao + l) * ld + g] = __float2bfloat16_rn(d[i]);
+        for (int u = 0; u < 8; ++u) b[u] = __ldg(Xb + (int64_t)(l + u) * ld + g);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const unsigned long long a = b[u] & 0x7fffffffffffffffull;
+            m = a > m ? a : m;
+        }
     }
+    for (; l < nao; ++l) {
+        const unsigned long long a = __ldg(Xb + (int64_t)l * ld + g) & 0x7fffffffffffffffull;
+        m = a > m ? a : m;
+    }
+    erow[g] = exp_of_bits(m);
+}
+
+// slices of X: one thread per (row l, two points); bf16 pairs per store
+template<int S>
+__global__ void f_slice_x_kernel(const double* __restrict__ X, int nao,
+                                 int64_t ld, const int* __restrict__ erow,
+                                 __nv_bfloat16* __restrict__ A) {
+    const int l = blockIdx.y;
+    const int64_t g = 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    if (g >= ld) return;                    // ld is even (a multiple of 32)
+    const double2 x = *reinterpret_cast<const double2*>(X + (int64_t)l * ld + g);
+    const int2 e = *reinterpret_cast<const int2*>(erow + g);
+    float d0[S], d1[S];
+    digits<S>(x.x, e.x, d0);
+    digits<S>(x.y, e.y, d1);
+#pragma unroll
+    for (int i = 0; i < S; ++i)
+        *reinterpret_cast<__nv_bfloat162*>(A + ((int64_t)i * nao + l) * ld + g) =
+            __floats2bfloat162_rn(d0[i], d1[i]);
 }
 
 template<int S>
@@ -166,17 +243,28 @@ __global__ void f_combine_kernel(const float* __restrict__ C, int nao,
                                  int64_t ld, const int* __restrict__ erow,
                                  const int* __restrict__ ecol,
                                  float* __restrict__ F) {
+    const int mu = blockIdx.y;
+    const int64_t g = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+    if (g >= ld) return;                    // ld is a multiple of 4
     const int64_t plane = (int64_t)nao * ld;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < plane;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t mu = i / ld, g = i - mu * ld;
-        float c[S];
+    const int64_t i = (int64_t)mu * ld + g;
+    float4 c[S];
 #pragma unroll
-        for (int l = 0; l < S; ++l) c[l] = C[(int64_t)l * plane + i];
-        const long long acc = combine_levels<S>(c);
-        const int sc = erow[g] + ecol[mu] - 2 * kW + 2 + kB * (S - 1);
-        F[i] = __double2float_rn((double)acc * pow2(sc));
+    for (int l = 0; l < S; ++l)
+        c[l] = __ldg(reinterpret_cast<const float4*>(C + (int64_t)l * plane + i));
+    const int4 er = *reinterpret_cast<const int4*>(erow + g);
+    const int base = ecol[mu] - 2 * kW + 2 + kB * (S - 1);
+    float v[4][S];
+#pragma unroll
+    for (int l = 0; l < S; ++l) {
+        v[0][l] = c[l].x; v[1][l] = c[l].y; v[2][l] = c[l].z; v[3][l] = c[l].w;
     }
+    float4 out;
+    out.x = scaled_ll_to_float(combine_levels<S>(v[0]), er.x + base);
+    out.y = scaled_ll_to_float(combine_levels<S>(v[1]), er.y + base);
+    out.z = scaled_ll_to_float(combine_levels<S>(v[2]), er.z + base);
+    out.w = scaled_ll_to_float(combine_levels<S>(v[3]), er.w + base);
+    *reinterpret_cast<float4*>(F + i) = out;
 }
 
 // ---------------------------------------------------------------------------
@@ -188,60 +276,92 @@ __global__ void f_combine_kernel(const float* __restrict__ C, int nao,
 // chunk stride S KC nao.  One CTA of 256 threads per (chunk, column).
 // ---------------------------------------------------------------------------
 template<int S, int KC>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(KC / 8)
 k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
                const double* __restrict__ w, int nao, int64_t ld,
                int64_t npts, int* __restrict__ ex, int* __restrict__ ew,
                __nv_bfloat16* __restrict__ A, __nv_bfloat16* __restrict__ B) {
-    constexpr int PER = KC / 256;
+    constexpr int T = KC / 8;               // threads: eight points each
     const int c = blockIdx.x, col = blockIdx.y;
-    __shared__ unsigned long long rx[256], rw[256];
-    double xv[PER], wv[PER];
+    __shared__ unsigned long long rx[T / 32], rw[T / 32];
+    const int k0 = 8 * threadIdx.x;
+    const int64_t g0 = (int64_t)c * KC + k0;
+    double xv[8], wv[8];
     unsigned long long mx = 0, mw = 0;
+    if (g0 + 8 <= npts) {
+        const double2* xp = reinterpret_cast<const double2*>(X + (int64_t)col * ld + g0);
+        const double2* wp = reinterpret_cast<const double2*>(w + g0);
+        const float4* gp = reinterpret_cast<const float4*>(G + (int64_t)col * ld + g0);
+        const float4 ga = __ldg(gp), gb = __ldg(gp + 1);
+        const float gv[8] = {ga.x, ga.y, ga.z, ga.w, gb.x, gb.y, gb.z, gb.w};
 #pragma unroll
-    for (int r = 0; r < PER; ++r) {
-        const int k = r * 256 + threadIdx.x;
-        const int64_t g = (int64_t)c * KC + k;
-        xv[r] = 0.0;
-        wv[r] = 0.0;
-        if (g < npts) {
-            xv[r] = X[(int64_t)col * ld + g];
-            wv[r] = w[g] * (double)G[(int64_t)col * ld + g];
+        for (int u = 0; u < 4; ++u) {
+            const double2 a = __ldg(xp + u), b = __ldg(wp + u);
+            xv[2 * u] = a.x; xv[2 * u + 1] = a.y;
+            wv[2 * u] = b.x * (double)gv[2 * u];
+            wv[2 * u + 1] = b.y * (double)gv[2 * u + 1];
         }
+    } else {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int64_t g = g0 + u;
+            xv[u] = 0.0;
+            wv[u] = 0.0;
+            if (g < npts) {
+                xv[u] = X[(int64_t)col * ld + g];
+                wv[u] = w[g] * (double)G[(int64_t)col * ld + g];
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
         const unsigned long long bx =
-            (unsigned long long)__double_as_longlong(xv[r]) & 0x7fffffffffffffffull;
+            (unsigned long long)__double_as_longlong(xv[u]) & 0x7fffffffffffffffull;
         const unsigned long long bw =
-            (unsigned long long)__double_as_longlong(wv[r]) & 0x7fffffffffffffffull;
+            (unsigned long long)__double_as_longlong(wv[u]) & 0x7fffffffffffffffull;
         mx = bx > mx ? bx : mx;
         mw = bw > mw ? bw : mw;
     }
-    rx[threadIdx.x] = mx;
-    rw[threadIdx.x] = mw;
-    __syncthreads();
-    for (int s = 128; s > 0; s >>= 1) {
-        if (threadIdx.x < s) {
-            if (rx[threadIdx.x + s] > rx[threadIdx.x]) rx[threadIdx.x] = rx[threadIdx.x + s];
-            if (rw[threadIdx.x + s] > rw[threadIdx.x]) rw[threadIdx.x] = rw[threadIdx.x + s];
-        }
-        __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ox = __shfl_xor_sync(0xffffffffu, mx, o);
+        const unsigned long long ow = __shfl_xor_sync(0xffffffffu, mw, o);
+        mx = ox > mx ? ox : mx;
+        mw = ow > mw ? ow : mw;
     }
-    const int e1 = exp_of_bits(rx[0]), e2 = exp_of_bits(rw[0]);
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { rx[warp] = mx; rw[warp] = mw; }
+    __syncthreads();
+    mx = 0;
+    mw = 0;
+#pragma unroll
+    for (int j = 0; j < T / 32; ++j) {
+        mx = rx[j] > mx ? rx[j] : mx;
+        mw = rw[j] > mw ? rw[j] : mw;
+    }
+    const int e1 = exp_of_bits(mx), e2 = exp_of_bits(mw);
     if (threadIdx.x == 0) {
         ex[(int64_t)c * nao + col] = e1;
         ew[(int64_t)c * nao + col] = e2;
     }
     const int64_t colbase = (int64_t)c * S * KC * nao + (int64_t)col * S * KC;
+    float d1[8][S], d2[8][S];
 #pragma unroll
-    for (int r = 0; r < PER; ++r) {
-        const int k = r * 256 + threadIdx.x;
-        float d1[S], d2[S];
-        digits<S>(xv[r], e1, d1);
-        digits<S>(wv[r], e2, d2);
+    for (int u = 0; u < 8; ++u) {
+        digits<S>(xv[u], e1, d1[u]);
+        digits<S>(wv[u], e2, d2[u]);
+    }
 #pragma unroll
-        for (int i = 0; i < S; ++i) {
-            A[colbase + (int64_t)i * KC + k] = __float2bfloat16_rn(d1[i]);
-            B[colbase + (int64_t)(S - 1 - i) * KC + k] = __float2bfloat16_rn(d2[i]);
+    for (int i = 0; i < S; ++i) {
+        __nv_bfloat162 pa[4], pb[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            pa[u] = __floats2bfloat162_rn(d1[2 * u][i], d1[2 * u + 1][i]);
+            pb[u] = __floats2bfloat162_rn(d2[2 * u][i], d2[2 * u + 1][i]);
         }
+        *reinterpret_cast<uint4*>(A + colbase + (int64_t)i * KC + k0) =
+            *reinterpret_cast<const uint4*>(pa);
+        *reinterpret_cast<uint4*>(B + colbase + (int64_t)(S - 1 - i) * KC + k0) =
+            *reinterpret_cast<const uint4*>(pb);
     }
 }
 
@@ -311,8 +431,13 @@ int ozaki_f_gemm(cublasHandle_t hb, const double* X, const double* QD,
     __nv_bfloat16* B = reinterpret_cast<__nv_bfloat16*>(p);
     p += al(sizeof(__nv_bfloat16) * (size_t)S * nao * nao);
     float* C = reinterpret_cast<float*>(p);
-    f_slice_x_kernel<S><<<(unsigned)((ld + 127) / 128), 128, 0, s>>>(X, nao, ld, erow, A);
+    f_rowmax_kernel<<<(unsigned)((ld + 255) / 256), 256, 0, s>>>(X, nao, ld, erow);
     OZ_CUDA(cudaGetLastError());
+    {
+        dim3 grid((unsigned)((ld / 2 + 255) / 256), (unsigned)nao);
+        f_slice_x_kernel<S><<<grid, 256, 0, s>>>(X, nao, ld, erow, A);
+        OZ_CUDA(cudaGetLastError());
+    }
     f_slice_qd_kernel<S><<<nao, 256, 0, s>>>(QD, nao, ecol, B);
     OZ_CUDA(cudaGetLastError());
     const float one = 1.0f, zero = 0.0f;
@@ -325,11 +450,11 @@ int ozaki_f_gemm(cublasHandle_t hb, const double* X, const double* QD,
                                CUDA_R_32F, (int)ld, CUBLAS_COMPUTE_32F,
                                CUBLAS_GEMM_DEFAULT));
     }
-    const int64_t plane = (int64_t)nao * ld;
-    int64_t blocks = (plane + 255) / 256;
-    if (blocks > 152 * 32) blocks = 152 * 32;
-    f_combine_kernel<S><<<(unsigned)blocks, 256, 0, s>>>(C, nao, ld, erow, ecol, F);
-    OZ_CUDA(cudaGetLastError());
+    {
+        dim3 grid((unsigned)((ld / 4 + 255) / 256), (unsigned)nao);
+        f_combine_kernel<S><<<grid, 256, 0, s>>>(C, nao, ld, erow, ecol, F);
+        OZ_CUDA(cudaGetLastError());
+    }
     return 0;
 }
 
@@ -348,8 +473,8 @@ int ozaki_k_gemm(cublasHandle_t hb, const double* X, const float* G,
     p += al(sizeof(__nv_bfloat16) * slab);
     float* C = reinterpret_cast<float*>(p);
     dim3 grid(nchunk, nao);
-    k_slice_kernel<S, KC><<<grid, 256, 0, s>>>(X, G, w, nao, ld, npts, ex, ew,
-                                               A, B);
+    k_slice_kernel<S, KC><<<grid, KC / 8, 0, s>>>(X, G, w, nao, ld, npts, ex,
+                                                  ew, A, B);
     OZ_CUDA(cudaGetLastError());
     const float one = 1.0f, zero = 0.0f;
     const long long stride = (long long)S * KC * nao;
