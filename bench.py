@@ -8,12 +8,14 @@
   screening k_tile_tol = 1e-11.
 
 One step = the two K builds of one SCF cycle (full 1/r and erf(w r)/r,
-w = 0.3), each: FP64 AO values -> F GEMM -> sub-block stats -> fused screen
-+ G kernels -> K GEMM, all on the device.  The metric is COSX G TFLOP/s:
-the algorithmic flop model of the kept (sub-block, shell pair) tasks
+w = 0.3) from one density: FP64 AO values -> F GEMM -> block stats, formed
+once, then per omega the fused screen + G kernels -> K GEMM, all on the
+device (wb_cosx_get_k_multi; --per-omega runs one wb_cosx_get_k per omega,
+forming AO values and F twice).  The metric is COSX G TFLOP/s: the
+algorithmic flop model of the kept (sub-block, shell pair) tasks
 (pyscf_wb97mv_fast_gb300/flops_model.py) divided by the step time.
 
-  value  : device-resident inputs, wb_cosx_get_k through the engine
+  value  : device-resident inputs, the K builds through the engine
   e2e    : host (pinned) coordinates, weights and density matrix copied in
            and both K matrices copied out every step, through
            GpuKBuilder/get_k_only_gpu-equivalent calls
@@ -250,6 +252,8 @@ def config_dict(mol, g, args):
             'basis': 'synthetic def2-SVP structure', 'nao': mol.nao,
             'grid_points': int(g.size), 'omegas': list(OMEGAS),
             'k_tile_tol': TILE_TOL, 'proj': 'identity',
+            'omega_builds': 'per-omega' if getattr(args, 'per_omega', False)
+                            else 'multi-omega (shared AO values and F)',
             'l2': 'inputs larger than L2 (X alone is %.1f GB)'
                   % (8.0 * mol.nao * g.size / 1e9),
             'gemm': args.gemm, 'parallelism': 'replicas'}
@@ -267,6 +271,9 @@ def main():
     ap.add_argument('--grid-level', type=int, default=None,
                     help='grid level (profiling captures of a smaller grid)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--per-omega', action='store_true',
+                    help='one get_k call per omega instead of one multi-omega '
+                         'call (AO values and F formed twice)')
     ap.add_argument('--ref-points', type=int, default=400)
     args = ap.parse_args()
     if args.impl == 'reference':
@@ -291,26 +298,35 @@ def main():
     coords_d = eng.relative(g.coords)
     w_d = torch.as_tensor(g.weights, device=dev)
     qd_d = torch.as_tensor(dm, device=dev)
-    K = [torch.empty((mol.nao, mol.nao), dtype=torch.float64, device=dev)
-         for _ in OMEGAS]
+    K = torch.empty((len(OMEGAS), mol.nao, mol.nao), dtype=torch.float64,
+                    device=dev)
+
+    def build_k(c, wt, q, stats=False, profile=False):
+        # both omegas of one density: one multi-omega call (AO values, F and
+        # block statistics shared), or one call per omega with --per-omega
+        if args.per_omega:
+            sts = []
+            for i, w in enumerate(OMEGAS):
+                eng.get_k(c, wt, q, w, tile_tol=TILE_TOL, gemm=args.gemm,
+                          out=K[i], stats=stats, profile=profile)
+                sts.append(eng.last_stats)
+            return sts
+        eng.get_k_multi(c, wt, q, OMEGAS, tile_tol=TILE_TOL, gemm=args.gemm,
+                        out=K, stats=stats, profile=profile)
+        return [eng.last_stats]
 
     def step():
-        for i, w in enumerate(OMEGAS):
-            eng.get_k(coords_d, w_d, qd_d, w, tile_tol=TILE_TOL,
-                      gemm=args.gemm, out=K[i], stats=False)
+        build_k(coords_d, w_d, qd_d)
 
     # warm the library (cuBLAS heuristics, first launches), then one counted
-    # and profiled call per omega: kept tasks, model flops, launches, phases
+    # and profiled build: kept tasks, model flops, launches, phases
     step()
     torch.cuda.synchronize()
     flops_step, launches_step, kept, total = 0.0, 0, 0, 0
     phases = {}
     kept_cls = [0] * 10
     flops_cls = [0.0] * 10
-    for i, w in enumerate(OMEGAS):
-        eng.get_k(coords_d, w_d, qd_d, w, tile_tol=TILE_TOL,
-                  gemm=args.gemm, out=K[i], stats=True, profile=True)
-        st = eng.last_stats
+    for st in build_k(coords_d, w_d, qd_d, stats=True, profile=True):
         flops_step += st['model_flops']
         launches_step += st['kernel_launches']
         kept += st['pairs_kept']
@@ -361,9 +377,8 @@ def main():
         c_d2.copy_(c_h, non_blocking=True)
         w_d2.copy_(w_h, non_blocking=True)
         q_d2.copy_(d_h, non_blocking=True)
-        for i, w in enumerate(OMEGAS):
-            eng.get_k(c_d2, w_d2, q_d2, w, tile_tol=TILE_TOL,
-                      gemm=args.gemm, out=K[i], stats=False)
+        build_k(c_d2, w_d2, q_d2)
+        for i in range(len(OMEGAS)):
             Ks = (K[i] + K[i].T) * 0.5
             k_h[i].copy_(Ks, non_blocking=True)
 

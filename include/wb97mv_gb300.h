@@ -134,6 +134,21 @@ int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
                   double* k_out, void* workspace, size_t workspace_bytes,
                   void* stream, wb_cosx_stats* stats);
 
+/* wb_cosx_get_k for nomega range-separation parameters and one density:
+ * the AO values, F = fl32(X QD) and the block statistics of each tile are
+ * formed once and serve every omega; k_out holds nomega (nao, nao)
+ * row-major matrices, omega j at k_out + j nao^2, each equal to what
+ * wb_cosx_get_k returns for omegas[j].  stats sum over the omegas.  The
+ * reference reaches the same pair of matrices (omega = 0 and the
+ * functional's omega, one density) through two get_k_only calls of one
+ * SCF cycle (gpu/sgx_k.py:983-990, via GpuKBuilder.get_k :663-751). */
+int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
+                        const double* weights, int64_t npts, const double* qd,
+                        int nomega, const double* omegas, double tile_tol,
+                        int64_t tile_pts, int flags, double* k_out,
+                        void* workspace, size_t workspace_bytes, void* stream,
+                        wb_cosx_stats* stats);
+
 /* The fused G kernels alone on one tile: f (nao, ldp) FP32 AO-major in,
  * g_out (nao, ldp) FP32 out (overwritten).  weights (npts,) FP64 feed the
  * screening estimate.  Replaces GpuKBuilder._tasks + _launch

@@ -154,6 +154,40 @@ class CosxEngine:
             self.last_stats = st.as_dict()
         return out
 
+    def get_k_multi(self, coords_rel, weights, qd, omegas, tile_tol=1e-11,
+                    tile_pts=0, gemm='ozaki', out=None, stats=True,
+                    profile=False):
+        """get_k for several omegas and one density in one call: the AO
+        values, F and the block statistics of each tile serve every omega.
+        Returns (len(omegas), nao, nao) FP64 on the device; out[j] is what
+        get_k(..., omegas[j]) returns."""
+        torch = _torch()
+        om = [float(w) for w in omegas]
+        if not om:
+            raise ValueError('omegas is empty')
+        npts = int(coords_rel.shape[0])
+        nbytes = self.workspace_bytes(npts, tile_pts)
+        ws = self.workspace(nbytes)
+        if out is None:
+            out = torch.empty((len(om), self.nao, self.nao), dtype=torch.float64,
+                              device=self.device)
+        if tuple(out.shape) != (len(om), self.nao, self.nao) or not out.is_contiguous():
+            raise ValueError('out must be a contiguous (%d, nao, nao) tensor' % len(om))
+        st = _native.WbCosxStats() if stats else None
+        flags = _native.GEMM_MODES[gemm]
+        if profile and stats:
+            flags |= _native.WB_K_PROFILE
+        arr = (_native.ctypes.c_double * len(om))(*om)
+        _native.check(_native.lib().wb_cosx_get_k_multi(
+            self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
+            _native.ptr(qd.contiguous()), len(om), arr, float(tile_tol),
+            int(tile_pts), flags, _native.ptr(out), _native.ptr(ws), nbytes,
+            self._stream(), _native.ctypes.byref(st) if st is not None else None),
+            'wb_cosx_get_k_multi')
+        if st is not None:
+            self.last_stats = st.as_dict()
+        return out
+
     def g(self, coords_rel, weights, f, omega, tile_tol=0.0, out=None,
           stats=True):
         """G (nao, ld) FP32 from F (nao, ld) FP32 AO-major, one tile."""

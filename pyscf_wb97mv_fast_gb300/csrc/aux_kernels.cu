@@ -110,98 +110,128 @@ cudaError_t launch_grid_prep(const double* coords, int64_t npts, int64_t ld,
 }
 
 // -- sub-block statistics (gpu/sgx_k.py:866-903) ---------------------------
-// One warp per block of BP = 32 or 64 consecutive points (32 is the
-// reference's sub-block): FP64 centroid and radius of the valid points
-// (centroid rounded to nearest FP32, radius rounded up), and for every
-// (virtual) shell msh = max_g fl32(w_g) sum_{t in shell} |F_tg|.
-template<int BP>
+// One warp per 64-point block (two points per lane: the block's two 32-point
+// halves, the reference's sub-block size): for each half and for the whole
+// block the FP64 centroid and radius of the valid points (centroid rounded
+// to nearest FP32, radius rounded up) and, for every (virtual) shell,
+// msh = max_g fl32(w_g) sum_{t in shell} |F_tg|.  One pass over F serves
+// the 32- and the 64-point class kernels.
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float4 centroid_radius(double sx, double sy, double sz,
+                                                  int n, double d) {
+    float r = (float)d;
+    if ((double)r < d) r = nextafterf(r, INFINITY);
+    if (n <= 0) return make_float4(0.0f, 0.0f, 0.0f, r);
+    return make_float4((float)(sx / n), (float)(sy / n), (float)(sz / n), r);
+}
+
 __global__ void sub_stats_kernel(const double* __restrict__ coords,
                                  const double* __restrict__ w,
                                  const float* __restrict__ F, int64_t npts,
                                  int64_t ld, int nvshell,
                                  const int* __restrict__ vs_ao0,
                                  const int* __restrict__ vs_nf,
-                                 float4* __restrict__ sub_cr,
-                                 float* __restrict__ msh) {
-    constexpr int Q = BP / 32;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+                                 float4* __restrict__ cr32,
+                                 float* __restrict__ msh32,
+                                 float4* __restrict__ cr64,
+                                 float* __restrict__ msh64) {
+    const int blk = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    const int nblk = (int)((ld + BP - 1) / BP);
-    if (warp >= nblk) return;
-    int64_t g[Q];
-    bool valid[Q];
-    double cx[Q], cy[Q], cz[Q];
-    double sx = 0.0, sy = 0.0, sz = 0.0;
+    const int nblk64 = (int)((ld + 63) / 64), nsub = (int)(ld / 32);
+    if (blk >= nblk64) return;
+    const bool half1 = 2 * blk + 1 < nsub;      // second half inside ld
+    int64_t g[2];
+    bool valid[2];
+    double c[2][3];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        g[q] = (int64_t)warp * BP + 32 * q + lane;
+    for (int q = 0; q < 2; ++q) {
+        g[q] = (int64_t)blk * 64 + 32 * q + lane;
         valid[q] = g[q] < npts;
-        cx[q] = cy[q] = cz[q] = 0.0;
-        if (valid[q]) {
-            cx[q] = coords[g[q] * 3];
-            cy[q] = coords[g[q] * 3 + 1];
-            cz[q] = coords[g[q] * 3 + 2];
-        }
-        sx += cx[q]; sy += cy[q]; sz += cz[q];
+        for (int x = 0; x < 3; ++x) c[q][x] = valid[q] ? coords[g[q] * 3 + x] : 0.0;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        sx += __shfl_xor_sync(0xffffffffu, sx, o);
-        sy += __shfl_xor_sync(0xffffffffu, sy, o);
-        sz += __shfl_xor_sync(0xffffffffu, sz, o);
-    }
-    const int64_t rem = npts - (int64_t)warp * BP;
-    const int nvalid = rem >= BP ? BP : (rem > 0 ? (int)rem : 0);
-    double mx = 0.0, my = 0.0, mz = 0.0;
-    if (nvalid > 0) { mx = sx / nvalid; my = sy / nvalid; mz = sz / nvalid; }
-    double d = 0.0;
+    // centroids: halves, then the block
+    double s[2][3];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        if (valid[q]) {
-            const double ex = cx[q] - mx, ey = cy[q] - my, ez = cz[q] - mz;
-            d = fmax(d, sqrt(ex * ex + ey * ey + ez * ez));
-        }
+    for (int q = 0; q < 2; ++q)
+        for (int x = 0; x < 3; ++x) s[q][x] = warp_sum_d(c[q][x]);
+    int nv[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int64_t rem = npts - ((int64_t)blk * 64 + 32 * q);
+        nv[q] = rem >= 32 ? 32 : (rem > 0 ? (int)rem : 0);
     }
-    for (int o = 16; o > 0; o >>= 1) d = fmax(d, __shfl_xor_sync(0xffffffffu, d, o));
+    const int nvb = nv[0] + nv[1];
+    double mh[2][3], mb[3];
+    for (int x = 0; x < 3; ++x) {
+        for (int q = 0; q < 2; ++q) mh[q][x] = nv[q] ? s[q][x] / nv[q] : 0.0;
+        mb[x] = nvb ? (s[0][x] + s[1][x]) / nvb : 0.0;
+    }
+    double dh[2] = {0.0, 0.0}, db = 0.0;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        if (!valid[q]) continue;
+        double e2 = 0.0, b2 = 0.0;
+        for (int x = 0; x < 3; ++x) {
+            const double e = c[q][x] - mh[q][x], b = c[q][x] - mb[x];
+            e2 += e * e;
+            b2 += b * b;
+        }
+        dh[q] = sqrt(e2);
+        db = fmax(db, sqrt(b2));
+    }
+    dh[0] = warp_max_d(dh[0]);
+    dh[1] = warp_max_d(dh[1]);
+    db = warp_max_d(db);
     if (lane == 0) {
-        float r = (float)d;
-        if ((double)r < d) r = nextafterf(r, INFINITY);
-        sub_cr[warp] = make_float4((float)mx, (float)my, (float)mz, r);
+        cr32[2 * blk] = centroid_radius(s[0][0], s[0][1], s[0][2], nv[0], dh[0]);
+        if (half1)
+            cr32[2 * blk + 1] = centroid_radius(s[1][0], s[1][1], s[1][2], nv[1], dh[1]);
+        cr64[blk] = centroid_radius(s[0][0] + s[1][0], s[0][1] + s[1][1],
+                                    s[0][2] + s[1][2], nvb, db);
     }
-    float w32[Q];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) w32[q] = valid[q] ? (float)w[g[q]] : 0.0f;
-    for (int s = 0; s < nvshell; ++s) {
-        const int a0 = vs_ao0[s], nf = vs_nf[s];
-        float best = 0.0f;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            if (!valid[q]) continue;
-            float acc = 0.0f;
-            for (int t = 0; t < nf; ++t)
-                acc += fabsf(F[(int64_t)(a0 + t) * ld + g[q]]) * w32[q];
-            best = fmaxf(best, acc);
+    const float w0 = valid[0] ? (float)w[g[0]] : 0.0f;
+    const float w1 = valid[1] ? (float)w[g[1]] : 0.0f;
+    float* m32a = msh32 + (int64_t)(2 * blk) * nvshell;
+    float* m32b = msh32 + (int64_t)(2 * blk + 1) * nvshell;
+    float* m64 = msh64 + (int64_t)blk * nvshell;
+    for (int sh = 0; sh < nvshell; ++sh) {
+        const int a0 = vs_ao0[sh], nf = vs_nf[sh];
+        float acc0 = 0.0f, acc1 = 0.0f;
+        for (int t = 0; t < nf; ++t) {
+            const int64_t row = (int64_t)(a0 + t) * ld;
+            if (valid[0]) acc0 += fabsf(F[row + g[0]]) * w0;
+            if (valid[1]) acc1 += fabsf(F[row + g[1]]) * w1;
         }
-        for (int o = 16; o > 0; o >>= 1)
-            best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
-        if (lane == 0) msh[(int64_t)warp * nvshell + s] = best;
+        for (int o = 16; o > 0; o >>= 1) {
+            acc0 = fmaxf(acc0, __shfl_xor_sync(0xffffffffu, acc0, o));
+            acc1 = fmaxf(acc1, __shfl_xor_sync(0xffffffffu, acc1, o));
+        }
+        if (lane == 0) {
+            m32a[sh] = acc0;
+            if (half1) m32b[sh] = acc1;
+            m64[sh] = fmaxf(acc0, acc1);
+        }
     }
 }
 
 cudaError_t launch_sub_stats(const double* coords, const double* weights,
                              const float* F, int64_t npts, int64_t ld,
                              int nvshell, const int* vs_ao0, const int* vs_nf,
-                             int block_pts, float4* sub_cr, float* msh,
-                             cudaStream_t s) {
-    const int64_t nblk = (ld + block_pts - 1) / block_pts;
+                             float4* cr32, float* msh32, float4* cr64,
+                             float* msh64, cudaStream_t s) {
+    const int64_t nblk = (ld + 63) / 64;
     if (nblk <= 0) return cudaSuccess;
     const int warps = 4;
-    const unsigned grid = (unsigned)((nblk + warps - 1) / warps);
-    if (block_pts == 64)
-        sub_stats_kernel<64><<<grid, 32 * warps, 0, s>>>(
-            coords, weights, F, npts, ld, nvshell, vs_ao0, vs_nf, sub_cr, msh);
-    else
-        sub_stats_kernel<32><<<grid, 32 * warps, 0, s>>>(
-            coords, weights, F, npts, ld, nvshell, vs_ao0, vs_nf, sub_cr, msh);
+    sub_stats_kernel<<<(unsigned)((nblk + warps - 1) / warps), 32 * warps, 0, s>>>(
+        coords, weights, F, npts, ld, nvshell, vs_ao0, vs_nf, cr32, msh32,
+        cr64, msh64);
     return cudaGetLastError();
 }
 

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -135,7 +136,6 @@ struct wb_cosx {
     cudaEvent_t fork = nullptr;
     int corder[wb::NCLASS] = {0};
     int pts[wb::NCLASS] = {0};       // points per lane of each class kernel
-    bool uses_pts[2] = {false, false};
 };
 
 namespace {
@@ -252,28 +252,32 @@ int prepare_omega(wb_cosx* h, double omega, void* ws, const WsLayout& L,
     return WB_OK;
 }
 
-// stats, sub-block prep and the class launches of one tile; F and G are
-// (nao, ldt) AO-major.  The classes fill their own partial-G buffers
-// concurrently; G is their fixed-order sum.
-int run_g_tile(wb_cosx* h, const double* coords, const double* weights,
-               int64_t npts_t, int64_t ldt, const float* F, float* G,
-               double tile_tol, void* ws, const WsLayout& L, cudaStream_t s,
-               int* launches) {
-    const wb::CosxArgs a = make_args(h, ws, L, ldt, npts_t, F, tile_tol);
+// grid coordinates (FP32 hi / lo) and block statistics of one tile: they
+// depend on the points and F only, so one pass serves every omega
+int tile_prep(wb_cosx* h, const double* coords, const double* weights,
+              int64_t npts_t, int64_t ldt, const float* F, void* ws,
+              const WsLayout& L, cudaStream_t s, int* launches) {
     WB_CUDA(wb::launch_grid_prep(coords, npts_t, ldt, at<float>(ws, L.gh),
                                  at<float>(ws, L.gl), s));
-    for (int b = 0; b < 2; ++b) {
-        if (!h->uses_pts[b]) continue;
-        WB_CUDA(wb::launch_sub_stats(coords, weights, F, npts_t, ldt,
-                                     h->hp.nvshell, h->vs_ao0, h->vs_nf,
-                                     32 * (b + 1), at<float4>(ws, L.subcr[b]),
-                                     at<float>(ws, L.msh[b]), s));
-        *launches += 1;
-    }
+    WB_CUDA(wb::launch_sub_stats(coords, weights, F, npts_t, ldt,
+                                 h->hp.nvshell, h->vs_ao0, h->vs_nf,
+                                 at<float4>(ws, L.subcr[0]), at<float>(ws, L.msh[0]),
+                                 at<float4>(ws, L.subcr[1]), at<float>(ws, L.msh[1]),
+                                 s));
+    *launches += 2;
+    return WB_OK;
+}
+
+// the class launches of one tile (after tile_prep and prepare_omega); F and
+// G are (nao, ldt) AO-major.  The classes fill their own partial-G buffers
+// concurrently; G is their fixed-order sum.
+int run_g_classes(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
+                  float* G, double tile_tol, void* ws, const WsLayout& L,
+                  cudaStream_t s, int* launches) {
+    const wb::CosxArgs a = make_args(h, ws, L, ldt, npts_t, F, tile_tol);
     WB_CUDA(cudaMemsetAsync(at<float>(ws, L.gcls), 0,
                             sizeof(float) * (size_t)h->hp.ncrow * ldt, s));
     WB_CUDA(cudaMemsetAsync(at<int>(ws, L.work), 0, sizeof(int) * wb::NCLASS, s));
-    *launches += 2;
     WB_CUDA(cudaEventRecord(h->fork, s));
     for (int i = 0; i < wb::NCLASS; ++i) {
         const int c = h->corder[i];
@@ -463,8 +467,6 @@ int wb_cosx_create(const wb_basis* basis, const double origin[3],
     for (int c = 0; c < wb::NCLASS; ++c) {
         h->blocks_per_sm[c] = wb::cosx_class_blocks_per_sm(c);
         h->pts[c] = wb::cosx_class_pts(c);
-        if (hp.cls[c].pair_end > hp.cls[c].pair_begin)
-            h->uses_pts[h->pts[c] - 1] = true;
     }
     {   // launch order: model flops of all pairs of a class, descending
         double work[wb::NCLASS] = {0};
@@ -541,14 +543,32 @@ int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
                   double tile_tol, int64_t tile_pts, int flags, double* k_out,
                   void* workspace, size_t workspace_bytes, void* stream,
                   wb_cosx_stats* stats) {
-    if (!h || !k_out || !qd || npts < 0 || (npts && (!coords || !weights)))
+    return wb_cosx_get_k_multi(h, coords, weights, npts, qd, 1, &omega,
+                               tile_tol, tile_pts, flags, k_out, workspace,
+                               workspace_bytes, stream, stats);
+}
+
+int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
+                        const double* weights, int64_t npts, const double* qd,
+                        int nomega, const double* omegas, double tile_tol,
+                        int64_t tile_pts, int flags, double* k_out,
+                        void* workspace, size_t workspace_bytes, void* stream,
+                        wb_cosx_stats* stats) {
+    if (!h || !k_out || !qd || npts < 0 || (npts && (!coords || !weights)) ||
+        nomega < 1 || !omegas)
         return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_get_k: bad arguments");
-    if (!(omega >= 0.0) || !(tile_tol >= 0.0))
-        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_get_k: omega and tile_tol must be >= 0");
+    for (int j = 0; j < nomega; ++j)
+        if (!(omegas[j] >= 0.0))
+            return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_get_k: omega must be >= 0");
+    if (!(tile_tol >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_get_k: tile_tol must be >= 0");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int nao = h->hp.nao;
+    const size_t kk = (size_t)nao * nao;
     int64_t tile = tile_pts > 0 ? round32(tile_pts) : round32(std::max<int64_t>(npts, 1));
     tile = std::max<int64_t>(std::min(tile, round32(std::max<int64_t>(npts, 1))), 32);
+    if (tile > INT32_MAX - 64)
+        return fail(WB_ERR_UNSUPPORTED, "wb_cosx_get_k: tile above 2^31 points");
     const WsLayout L = ws_layout(h, tile, true);
     if (!workspace || workspace_bytes < L.total)
         return fail(WB_ERR_WORKSPACE, "wb_cosx_get_k: workspace needs " +
@@ -565,13 +585,9 @@ int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
     }
     WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.counters), 0,
                             sizeof(unsigned long long) * 3 * wb::NCLASS, s));
-    {
-        const int st = prepare_omega(h, omega, workspace, L, s);
-        if (st != WB_OK) return st;
-    }
-    int launches = 2;
+    int launches = 1;
     if (npts == 0) {
-        WB_CUDA(cudaMemsetAsync(k_out, 0, sizeof(double) * nao * nao, s));
+        WB_CUDA(cudaMemsetAsync(k_out, 0, sizeof(double) * kk * nomega, s));
         return read_stats(h, workspace, L, 0, s, stats, launches);
     }
     double* X = at<double>(workspace, L.X);
@@ -581,21 +597,31 @@ int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
     int64_t ntasks = 0;
     const double one = 1.0, zero = 0.0;
     const bool prof = (flags & WB_K_PROFILE) && stats;
-    cudaEvent_t ev[7] = {};
+    // phase events: AO, F GEMM, F cast, tile prep + per omega (omega data,
+    // G, weight, K GEMM)
+    cudaEvent_t ev[2] = {};
     double phase[6] = {0, 0, 0, 0, 0, 0};
     if (prof)
-        for (int i = 0; i < 7; ++i) WB_CUDA(cudaEventCreate(&ev[i]));
-    auto mark = [&](int i) { if (prof) cudaEventRecord(ev[i], s); };
-    auto collect = [&]() -> int {
+        for (int i = 0; i < 2; ++i) WB_CUDA(cudaEventCreate(&ev[i]));
+    int cur = 0;
+    auto mark = [&]() -> int {
+        // closes the running phase `cur` (timed from the last mark)
         if (!prof) return WB_OK;
-        WB_CUDA(cudaEventSynchronize(ev[6]));
-        for (int i = 0; i < 6; ++i) {
-            float ms = 0.0f;
-            WB_CUDA(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
-            phase[i] += ms;
-        }
+        WB_CUDA(cudaEventRecord(ev[1], s));
+        WB_CUDA(cudaEventSynchronize(ev[1]));
+        float ms = 0.0f;
+        WB_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        phase[cur] += ms;
+        WB_CUDA(cudaEventRecord(ev[0], s));
         return WB_OK;
     };
+    auto phase_to = [&](int p) -> int {
+        const int st = mark();
+        cur = p;
+        return st;
+    };
+    if (prof) WB_CUDA(cudaEventRecord(ev[0], s));
+    int st = WB_OK;
     for (int64_t i0 = 0; i0 < npts; i0 += tile) {
         const int64_t nt = std::min(tile, npts - i0);
         const int64_t ldt = round32(nt);
@@ -607,56 +633,62 @@ int wb_cosx_get_k(wb_cosx* h, const double* coords, const double* weights,
         ao.sh_eoff = h->sh_eoff; ao.sh_coff = h->sh_coff; ao.sh_ao0 = h->sh_ao0;
         ao.sh_ctr = h->sh_ctr; ao.exps = h->exps; ao.coeffs = h->coeffs; ao.X = X;
         ao.nao = nao;
-        mark(0);
+        if ((st = phase_to(0)) != WB_OK) return st;
         WB_CUDA(wb::launch_ao_eval(ao, s));
-        mark(1);
+        launches += 1;
+        if ((st = phase_to(1)) != WB_OK) return st;
         if (oz_f) {
             const int r = wb::ozaki_f_gemm(h->cublas, X, qd, nao, ldt, F32,
                                            at<void>(workspace, L.oz), s);
             if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
                                "ozaki F GEMM failed, code " + std::to_string(r));
-            mark(2);
-            launches += 2 + 5;
+            launches += 4 + wb::kOzSlices;
         } else {
             // F(g, mu) = sum_l X(g, l) QD(l, mu); QD row-major = col-major QD^T
             WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)ldt,
                                   nao, nao, &one, X, (int)ldt, qd, nao, &zero,
                                   F64, (int)ldt));
-            mark(2);
+            if ((st = phase_to(2)) != WB_OK) return st;
             WB_CUDA(wb::launch_f64_to_f32(F64, F32, (int64_t)nao * ldt, s));
             launches += 2;
         }
-        launches += 1;
-        mark(3);
-        int st = run_g_tile(h, c, w, nt, ldt, F32, G32, tile_tol, workspace, L,
-                            s, &launches);
-        if (st != WB_OK) return st;
-        ntasks += (ldt / 32) * (int64_t)h->hp.npairs;
-        mark(4);
-        if (oz_k) {
-            mark(5);
-            const int r = wb::ozaki_k_gemm(h->cublas, X, G32, w, nao, ldt, nt,
-                                           i0 == 0 ? 0 : 1, k_out,
-                                           at<void>(workspace, L.oz), s);
-            if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
-                               "ozaki K GEMM failed, code " + std::to_string(r));
-            launches += 2 + 5;
-        } else {
-            WB_CUDA(wb::launch_weight_g(G32, w, nt, ldt, nao, F64, s));
-            mark(5);
-            // K(mu, nu) += sum_g X(g, mu) WG(g, nu); written row-major
-            const double* beta = i0 == 0 ? &zero : &one;
-            WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nao, nao,
-                                  (int)ldt, &one, F64, (int)ldt, X, (int)ldt,
-                                  beta, k_out, nao));
+        if ((st = phase_to(3)) != WB_OK) return st;
+        if ((st = tile_prep(h, c, w, nt, ldt, F32, workspace, L, s, &launches)) != WB_OK)
+            return st;
+        for (int j = 0; j < nomega; ++j) {
+            double* Kj = k_out + kk * j;
+            if ((st = prepare_omega(h, omegas[j], workspace, L, s)) != WB_OK) return st;
             launches += 2;
+            if ((st = run_g_classes(h, nt, ldt, F32, G32, tile_tol, workspace, L,
+                                    s, &launches)) != WB_OK)
+                return st;
+            ntasks += (ldt / 32) * (int64_t)h->hp.npairs;
+            if (oz_k) {
+                if ((st = phase_to(5)) != WB_OK) return st;
+                const int r = wb::ozaki_k_gemm(h->cublas, X, G32, w, nao, ldt, nt,
+                                               i0 == 0 ? 0 : 1, Kj,
+                                               at<void>(workspace, L.oz), s);
+                if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
+                                   "ozaki K GEMM failed, code " + std::to_string(r));
+                launches += 2 + wb::kOzSlices;
+            } else {
+                if ((st = phase_to(4)) != WB_OK) return st;
+                WB_CUDA(wb::launch_weight_g(G32, w, nt, ldt, nao, F64, s));
+                if ((st = phase_to(5)) != WB_OK) return st;
+                // K(mu, nu) += sum_g X(g, mu) WG(g, nu); written row-major
+                const double* beta = i0 == 0 ? &zero : &one;
+                WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nao, nao,
+                                      (int)ldt, &one, F64, (int)ldt, X, (int)ldt,
+                                      beta, Kj, nao));
+                launches += 2;
+            }
+            if ((st = phase_to(3)) != WB_OK) return st;
         }
-        mark(6);
-        if ((st = collect()) != WB_OK) return st;
     }
+    if ((st = mark()) != WB_OK) return st;
     if (prof)
-        for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
-    int st = read_stats(h, workspace, L, ntasks, s, stats, launches);
+        for (int i = 0; i < 2; ++i) cudaEventDestroy(ev[i]);
+    st = read_stats(h, workspace, L, ntasks, s, stats, launches);
     if (st == WB_OK && prof)
         for (int i = 0; i < 6; ++i) stats->phase_ms[i] = phase[i];
     return st;
@@ -683,8 +715,9 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
         if (st != WB_OK) return st;
     }
     int launches = 2;
-    int st = run_g_tile(h, coords, weights, npts, ldt, f, g_out, tile_tol,
-                        workspace, L, s, &launches);
+    int st = tile_prep(h, coords, weights, npts, ldt, f, workspace, L, s, &launches);
+    if (st != WB_OK) return st;
+    st = run_g_classes(h, npts, ldt, f, g_out, tile_tol, workspace, L, s, &launches);
     if (st != WB_OK) return st;
     return read_stats(h, workspace, L, (ldt / 32) * (int64_t)h->hp.npairs, s,
                       stats, launches);

@@ -50,13 +50,13 @@ cudaError_t launch_omega(int npp, const double* p, const double* pref,
                          double omega, float4* om, cudaStream_t s);
 cudaError_t launch_grid_prep(const double* coords, int64_t npts, int64_t ld,
                              float* hi, float* lo, cudaStream_t s);
-// centroid / radius and shell maxima per block of block_pts (32 or 64)
-// points: ceil(ld / block_pts) blocks
+// centroid / radius and shell maxima per 32-point sub-block (ld / 32) and
+// per 64-point block (ceil(ld / 64)), one pass over F
 cudaError_t launch_sub_stats(const double* coords, const double* weights,
                              const float* F, int64_t npts, int64_t ld,
                              int nvshell, const int* vs_ao0, const int* vs_nf,
-                             int block_pts, float4* sub_cr, float* msh,
-                             cudaStream_t s);
+                             float4* cr32, float* msh32, float4* cr64,
+                             float* msh64, cudaStream_t s);
 // points per lane (1 or 2) of a class kernel: its blocks hold 32 * pts
 int cosx_class_pts(int cls);
 cudaError_t launch_f64_to_f32(const double* in, float* out, int64_t n,

@@ -58,19 +58,40 @@ def _sgx_jk_module():
     return mod
 
 
+def rsh_omegas(mf):
+    """(0, omega) for a range-separated functional with omega > 0 and a
+    full-range exchange part, (omega,) when only the long-range part is
+    used, None otherwise or when the functional cannot be read
+    (pyscf.dft.numint rsh_and_hybrid_coeff)."""
+    try:
+        ni = mf._numint
+        omega, alpha, hyb = ni.rsh_and_hybrid_coeff(mf.xc, spin=mf.mol.spin)
+    except Exception:
+        return None
+    omega = float(omega)
+    if omega <= 0.0:
+        return None
+    if abs(float(hyb)) > 0.0:
+        return (0.0, omega)
+    return (omega,) if abs(float(alpha)) > 0.0 else None
+
+
 def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
                 functional_factory=None, verify_ao=True,
                 gemm_dtype='float64', dtype='float32',
                 mem_fraction=DEFAULT_MEM_FRACTION, overlap=False,
                 semilocal=False, k=True, k_tile_tol=1e-11,
                 openblas_threads=None, vv10=True, k_gemm='ozaki',
-                sgx_jk_module=None):
+                sgx_jk_module=None, k_omegas='auto'):
     """Hook the GPU COSX K (and VV10) into mf; returns a HookSet.
 
     The keyword names follow the reference; backend must be None or
     'cuda' (there is one backend).  semilocal=True is not part of this
     build and raises.  sgx_jk_module lets tests pass a stand-in for
-    pyscf.sgx.sgx_jk.
+    pyscf.sgx.sgx_jk.  k_omegas (an addition): the omegas one SCF cycle
+    asks K for with the same density, built together (GpuKBuilder
+    omegas); 'auto' reads them from the range-separated functional of mf
+    ((0, omega) when it has one), None builds one K per call.
     """
     if backend not in (None, 'cuda', 'cupy'):
         raise ValueError("backend must be None or 'cuda'")
@@ -94,8 +115,11 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
                     return orig(sgx, dm, hermi, direct_scf_tol)
                 b = holder.get('builder')
                 if b is None:
+                    oms = (rsh_omegas(mf) if isinstance(k_omegas, str)
+                           and k_omegas == 'auto' else k_omegas)
                     b = sgx_k_mod.GpuKBuilder(mf.mol, tile_tol=k_tile_tol,
-                                              blksize=blksize, gemm=k_gemm)
+                                              blksize=blksize, gemm=k_gemm,
+                                              omegas=oms)
                     b._build()
                     torch = sgx_k_mod._torch()
                     free, _ = torch.cuda.mem_get_info(b.engine.device)

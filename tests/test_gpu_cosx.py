@@ -265,6 +265,54 @@ def test_builder_api_and_out_of_scope():
         get_k_only_gpu(b, sgx, asym)
 
 
+def test_multi_omega_build_matches_single_builds():
+    """wb_cosx_get_k_multi shares AO values, F and the block statistics
+    between the omegas: each of its matrices is bitwise the single-omega
+    build; the builder's pending cache hands out the second omega for the
+    same density and drops it for another one."""
+    torch = _torch()
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine
+    from pyscf_wb97mv_fast_gb300.gpu.sgx_k import GpuKBuilder, SyntheticSGX
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    mol = waters(4, 6.0, 11)
+    coords, weights = grid_subset(mol, 1, 9000, 5)
+    dm = density(mol.nao, 12, 4)
+    eng = CosxEngine(mol)
+    c = eng.relative(coords)
+    w = torch.as_tensor(weights, device=eng.device)
+    qd = torch.as_tensor(dm, device=eng.device)
+    oms = (0.0, 0.3, 0.11)
+    Km = eng.get_k_multi(c, w, qd, oms, tile_tol=1e-11, tile_pts=4096)
+    st_m = eng.last_stats
+    kept = 0
+    for j, om in enumerate(oms):
+        Ks = eng.get_k(c, w, qd, om, tile_tol=1e-11, tile_pts=4096)
+        kept += eng.last_stats['pairs_kept']
+        assert torch.equal(Km[j], Ks), om
+    assert st_m['pairs_kept'] == kept
+    # builder: omega 0 builds both, omega 0.3 comes from the pending set
+    g = build_grids(mol, level=0)
+    sgx = SyntheticSGX(mol, g)
+    b = GpuKBuilder(mol, tile_tol=1e-11, omegas=(0.0, 0.3))
+    b1 = GpuKBuilder(mol, tile_tol=1e-11)
+    K0 = b.get_k(sgx, dm, 0.0)
+    assert b.last_stats['from_multi'] is False
+    K3 = b.get_k(sgx, dm, 0.3)
+    assert b.last_stats['from_multi'] is True
+    assert np.array_equal(K0, b1.get_k(sgx, dm, 0.0))
+    assert np.array_equal(K3, b1.get_k(sgx, dm, 0.3))
+    # a new density drops the pending set: no stale K
+    dm2 = dm * 1.5
+    b.get_k(sgx, dm2, 0.0)
+    K3b = b.get_k(sgx, dm2, 0.3)
+    assert b.last_stats['from_multi'] is True
+    assert np.array_equal(K3b, b1.get_k(sgx, dm2, 0.3))
+    b.get_k(sgx, dm2, 0.0)
+    K3c = b.get_k(sgx, dm, 0.3)          # other density: built afresh
+    assert b.last_stats['from_multi'] is False
+    assert np.array_equal(K3c, K3)
+
+
 def test_screening_error_dense_random_density():
     """A dense random density (F does not decay) is the hard case for the
     screen: the error stays below 1e-7 (K elements) and 1e-8 (energy)."""

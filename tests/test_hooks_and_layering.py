@@ -144,3 +144,50 @@ def test_import_has_no_side_effects():
     out = subprocess.run([sys.executable, '-c', code], capture_output=True,
                          text=True, check=True).stdout.split()
     assert out == ['False', 'False']
+
+
+def test_rsh_omegas_from_the_functional():
+    from pyscf_wb97mv_fast_gb300.gpu.install import rsh_omegas
+
+    class NumInt:
+        def __init__(self, coeff):
+            self.coeff = coeff
+
+        def rsh_and_hybrid_coeff(self, xc, spin=0):
+            if self.coeff is None:
+                raise KeyError(xc)
+            return self.coeff
+
+    def mf(coeff):
+        return types.SimpleNamespace(_numint=NumInt(coeff), xc='x',
+                                     mol=types.SimpleNamespace(spin=0))
+
+    assert rsh_omegas(mf((0.3, 1.0, 0.15))) == (0.0, 0.3)     # wB97M-V
+    assert rsh_omegas(mf((0.3, 1.0, 0.0))) == (0.3,)          # LR only
+    assert rsh_omegas(mf((0.0, 0.0, 0.25))) is None           # global hybrid
+    assert rsh_omegas(mf(None)) is None
+    assert rsh_omegas(types.SimpleNamespace()) is None
+
+
+def test_builder_pending_set_only_matches_same_inputs():
+    import numpy as np
+    from pyscf_wb97mv_fast_gb300.gpu.sgx_k import GpuKBuilder
+    b = GpuKBuilder.__new__(GpuKBuilder)
+    dm = np.arange(9.0).reshape(3, 3)
+    proj = np.eye(3)
+    key = ('grid', False, 1e-11, 'ozaki')
+    K = np.ones((3, 3))
+    b._pending = (key, dm.copy(), proj.copy(), {0.3: K})
+    assert b._take_pending(key, dm, proj, 0.0) is None        # omega miss
+    assert b._pending is None                                 # dropped
+    b._pending = (key, dm.copy(), proj.copy(), {0.3: K})
+    other = dm.copy()
+    other[0, 0] += 1.0
+    assert b._take_pending(key, other, proj, 0.3) is None     # density miss
+    b._pending = (key, dm.copy(), proj.copy(), {0.3: K})
+    assert b._take_pending(('g2',) + key[1:], dm, proj, 0.3) is None
+    b._pending = (key, dm.copy(), proj.copy(), {0.3: K})
+    assert b._take_pending(key, dm, 2 * proj, 0.3) is None    # projector miss
+    b._pending = (key, dm.copy(), proj.copy(), {0.3: K})
+    assert b._take_pending(key, dm, proj, 0.3) is K           # hit, consumed
+    assert b._pending is None
