@@ -29,21 +29,29 @@ __global__ void omega_kernel(int npp, const double* __restrict__ p,
     }
     const double tp = th * pm;
     const double q = -2.0 * pm * th;
-    float rec[16];
+    float rec[20];
     rec[0] = (float)tp;
     rec[1] = (float)(tp - (double)rec[0]);
     double c = pref[m] * sth;
+    // far field (T = tp r^2 >= 36, erf(sqrt T) = 1 in FP64): R000_n =
+    // (-1)^n (2n-1)!! K0 r^-(2n+1) with K0 = c_0 sqrt(pi) / (2 sqrt(tp))
+    const double k0 = c * 0.88622692545275801365 / sqrt(tp);
     for (int n = 0; n < 7; ++n) {
         const float hi = (float)c;
         rec[2 + 2 * n] = hi;
         rec[3 + 2 * n] = (float)(c - (double)hi);
         c *= q;
     }
-    float4* o = om + 4 * (long long)m;
+    rec[16] = (float)k0;
+    rec[17] = (float)(k0 - (double)rec[16]);
+    rec[18] = (float)(36.0 / tp);            // r^2 at which T reaches 36
+    rec[19] = 0.0f;
+    float4* o = om + 5 * (long long)m;
     o[0] = make_float4(rec[0], rec[1], rec[2], rec[3]);
     o[1] = make_float4(rec[4], rec[5], rec[6], rec[7]);
     o[2] = make_float4(rec[8], rec[9], rec[10], rec[11]);
     o[3] = make_float4(rec[12], rec[13], rec[14], rec[15]);
+    o[4] = make_float4(rec[16], rec[17], rec[18], rec[19]);
 }
 
 cudaError_t launch_omega(int npp, const double* p, const double* pref,
@@ -70,7 +78,10 @@ __global__ void pack_records_kernel(const RecPack P, int npp,
     float4* r = rec + P.rec_off[c] + (long long)ml * P.stride[c];
     r[0] = geo[2 * (long long)m];
     r[1] = geo[2 * (long long)m + 1];
-    for (int q = 0; q < P.nom[c]; ++q) r[2 + q] = om[4 * (long long)m + q];
+    // omega record: its first n_om - 1 float4 (theta p, c_n), then the
+    // far-field float4 (K0 hi, K0 lo, r^2 threshold)
+    for (int q = 0; q + 1 < P.nom[c]; ++q) r[2 + q] = om[5 * (long long)m + q];
+    r[1 + P.nom[c]] = om[5 * (long long)m + 4];
     const float4* e = E + P.e_off[c] + (long long)ml * P.ne[c];
     for (int q = 0; q < P.ne[c]; ++q) r[2 + P.nom[c] + q] = e[q];
 }
@@ -110,12 +121,13 @@ cudaError_t launch_grid_prep(const double* coords, int64_t npts, int64_t ld,
 }
 
 // -- sub-block statistics (gpu/sgx_k.py:866-903) ---------------------------
-// One warp per 64-point block (two points per lane: the block's two 32-point
-// halves, the reference's sub-block size): for each half and for the whole
-// block the FP64 centroid and radius of the valid points (centroid rounded
-// to nearest FP32, radius rounded up) and, for every (virtual) shell,
-// msh = max_g fl32(w_g) sum_{t in shell} |F_tg|.  One pass over F serves
-// the 32- and the 64-point class kernels.
+// One warp per 128-point block (four points per lane): for its 32-point
+// quarters (the reference's sub-block size), its 64-point halves and the
+// whole block, the FP64 centroid and radius of the valid points (centroid
+// rounded to nearest FP32, radius rounded up) and, for every (virtual)
+// shell, msh = max_g fl32(w_g) sum_{t in shell} |F_tg|.  One pass over F
+// serves the 32-, 64- and 128-point class kernels.  Block b of size 32 * 2^k
+// covers points [b 32 2^k, (b + 1) 32 2^k); blocks past ld are not written.
 __device__ __forceinline__ double warp_sum_d(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -124,99 +136,105 @@ __device__ __forceinline__ double warp_max_d(double v) {
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
-__device__ __forceinline__ float4 centroid_radius(double sx, double sy, double sz,
-                                                  int n, double d) {
+__device__ __forceinline__ float4 centroid_radius(const double* sum, int n,
+                                                  double d) {
     float r = (float)d;
     if ((double)r < d) r = nextafterf(r, INFINITY);
     if (n <= 0) return make_float4(0.0f, 0.0f, 0.0f, r);
-    return make_float4((float)(sx / n), (float)(sy / n), (float)(sz / n), r);
+    return make_float4((float)(sum[0] / n), (float)(sum[1] / n),
+                       (float)(sum[2] / n), r);
 }
 
-__global__ void sub_stats_kernel(const double* __restrict__ coords,
+__global__ void sub_stats_kernel(const BlockStatsOut O,
+                                 const double* __restrict__ coords,
                                  const double* __restrict__ w,
                                  const float* __restrict__ F, int64_t npts,
                                  int64_t ld, int nvshell,
                                  const int* __restrict__ vs_ao0,
-                                 const int* __restrict__ vs_nf,
-                                 float4* __restrict__ cr32,
-                                 float* __restrict__ msh32,
-                                 float4* __restrict__ cr64,
-                                 float* __restrict__ msh64) {
+                                 const int* __restrict__ vs_nf) {
     const int blk = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    const int nblk64 = (int)((ld + 63) / 64), nsub = (int)(ld / 32);
-    if (blk >= nblk64) return;
-    const bool half1 = 2 * blk + 1 < nsub;      // second half inside ld
-    int64_t g[2];
-    bool valid[2];
-    double c[2][3];
+    const int nblk128 = (int)((ld + 127) / 128);
+    if (blk >= nblk128) return;
+    // blocks of each level that exist: 32 * 2^k points starting inside ld
+    int64_t g[4];
+    bool valid[4];
+    double c[4][3];
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        g[q] = (int64_t)blk * 64 + 32 * q + lane;
+    for (int q = 0; q < 4; ++q) {
+        g[q] = (int64_t)blk * 128 + 32 * q + lane;
         valid[q] = g[q] < npts;
         for (int x = 0; x < 3; ++x) c[q][x] = valid[q] ? coords[g[q] * 3 + x] : 0.0;
     }
-    // centroids: halves, then the block
-    double s[2][3];
+    int nv[4];
 #pragma unroll
-    for (int q = 0; q < 2; ++q)
-        for (int x = 0; x < 3; ++x) s[q][x] = warp_sum_d(c[q][x]);
-    int nv[2];
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const int64_t rem = npts - ((int64_t)blk * 64 + 32 * q);
+    for (int q = 0; q < 4; ++q) {
+        const int64_t rem = npts - ((int64_t)blk * 128 + 32 * q);
         nv[q] = rem >= 32 ? 32 : (rem > 0 ? (int)rem : 0);
     }
-    const int nvb = nv[0] + nv[1];
-    double mh[2][3], mb[3];
-    for (int x = 0; x < 3; ++x) {
-        for (int q = 0; q < 2; ++q) mh[q][x] = nv[q] ? s[q][x] / nv[q] : 0.0;
-        mb[x] = nvb ? (s[0][x] + s[1][x]) / nvb : 0.0;
-    }
-    double dh[2] = {0.0, 0.0}, db = 0.0;
+    double s[4][3];
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        if (!valid[q]) continue;
-        double e2 = 0.0, b2 = 0.0;
-        for (int x = 0; x < 3; ++x) {
-            const double e = c[q][x] - mh[q][x], b = c[q][x] - mb[x];
-            e2 += e * e;
-            b2 += b * b;
+    for (int q = 0; q < 4; ++q)
+        for (int x = 0; x < 3; ++x) s[q][x] = warp_sum_d(c[q][x]);
+    // level k = 0, 1, 2: block j of the level covers quarters [j 2^k, (j+1) 2^k)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int span = 1 << k;
+#pragma unroll
+        for (int j = 0; j < 4 / span; ++j) {
+            double sum[3] = {0.0, 0.0, 0.0};
+            int n = 0;
+            for (int q = j * span; q < (j + 1) * span; ++q) {
+                for (int x = 0; x < 3; ++x) sum[x] += s[q][x];
+                n += nv[q];
+            }
+            double m[3];
+            for (int x = 0; x < 3; ++x) m[x] = n ? sum[x] / n : 0.0;
+            double d = 0.0;
+            for (int q = j * span; q < (j + 1) * span; ++q) {
+                if (!valid[q]) continue;
+                double e2 = 0.0;
+                for (int x = 0; x < 3; ++x) {
+                    const double e = c[q][x] - m[x];
+                    e2 += e * e;
+                }
+                d = fmax(d, sqrt(e2));
+            }
+            d = warp_max_d(d);
+            const int64_t b = (int64_t)blk * (4 / span) + j;
+            if (lane == 0 && b * 32 * span < ld) O.cr[k][b] = centroid_radius(sum, n, d);
         }
-        dh[q] = sqrt(e2);
-        db = fmax(db, sqrt(b2));
     }
-    dh[0] = warp_max_d(dh[0]);
-    dh[1] = warp_max_d(dh[1]);
-    db = warp_max_d(db);
-    if (lane == 0) {
-        cr32[2 * blk] = centroid_radius(s[0][0], s[0][1], s[0][2], nv[0], dh[0]);
-        if (half1)
-            cr32[2 * blk + 1] = centroid_radius(s[1][0], s[1][1], s[1][2], nv[1], dh[1]);
-        cr64[blk] = centroid_radius(s[0][0] + s[1][0], s[0][1] + s[1][1],
-                                    s[0][2] + s[1][2], nvb, db);
-    }
-    const float w0 = valid[0] ? (float)w[g[0]] : 0.0f;
-    const float w1 = valid[1] ? (float)w[g[1]] : 0.0f;
-    float* m32a = msh32 + (int64_t)(2 * blk) * nvshell;
-    float* m32b = msh32 + (int64_t)(2 * blk + 1) * nvshell;
-    float* m64 = msh64 + (int64_t)blk * nvshell;
+    float wq[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) wq[q] = valid[q] ? (float)w[g[q]] : 0.0f;
     for (int sh = 0; sh < nvshell; ++sh) {
         const int a0 = vs_ao0[sh], nf = vs_nf[sh];
-        float acc0 = 0.0f, acc1 = 0.0f;
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         for (int t = 0; t < nf; ++t) {
             const int64_t row = (int64_t)(a0 + t) * ld;
-            if (valid[0]) acc0 += fabsf(F[row + g[0]]) * w0;
-            if (valid[1]) acc1 += fabsf(F[row + g[1]]) * w1;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (valid[q]) acc[q] += fabsf(F[row + g[q]]) * wq[q];
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            acc0 = fmaxf(acc0, __shfl_xor_sync(0xffffffffu, acc0, o));
-            acc1 = fmaxf(acc1, __shfl_xor_sync(0xffffffffu, acc1, o));
-        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            for (int o = 16; o > 0; o >>= 1)
+                acc[q] = fmaxf(acc[q], __shfl_xor_sync(0xffffffffu, acc[q], o));
         if (lane == 0) {
-            m32a[sh] = acc0;
-            if (half1) m32b[sh] = acc1;
-            m64[sh] = fmaxf(acc0, acc1);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int64_t b = (int64_t)blk * 4 + q;
+                if (b * 32 < ld) O.msh[0][b * nvshell + sh] = acc[q];
+            }
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int64_t b = (int64_t)blk * 2 + j;
+                if (b * 64 < ld)
+                    O.msh[1][b * nvshell + sh] = fmaxf(acc[2 * j], acc[2 * j + 1]);
+            }
+            O.msh[2][(int64_t)blk * nvshell + sh] =
+                fmaxf(fmaxf(acc[0], acc[1]), fmaxf(acc[2], acc[3]));
         }
     }
 }
@@ -224,14 +242,12 @@ __global__ void sub_stats_kernel(const double* __restrict__ coords,
 cudaError_t launch_sub_stats(const double* coords, const double* weights,
                              const float* F, int64_t npts, int64_t ld,
                              int nvshell, const int* vs_ao0, const int* vs_nf,
-                             float4* cr32, float* msh32, float4* cr64,
-                             float* msh64, cudaStream_t s) {
-    const int64_t nblk = (ld + 63) / 64;
+                             const BlockStatsOut& out, cudaStream_t s) {
+    const int64_t nblk = (ld + 127) / 128;
     if (nblk <= 0) return cudaSuccess;
     const int warps = 4;
     sub_stats_kernel<<<(unsigned)((nblk + warps - 1) / warps), 32 * warps, 0, s>>>(
-        coords, weights, F, npts, ld, nvshell, vs_ao0, vs_nf, cr32, msh32,
-        cr64, msh64);
+        out, coords, weights, F, npts, ld, nvshell, vs_ao0, vs_nf);
     return cudaGetLastError();
 }
 
@@ -584,7 +600,7 @@ __global__ void dense_kernel(const DenseArgs D) {
         const float dy = (ph.y - gyh) + (pl.y - gyl);
         const float dz = (ph.z - gzh) + (pl.z - gzl);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float* o = (const float*)(A.om + 4 * (int64_t)m);
+        const float* o = (const float*)(A.om + 5 * (int64_t)m);
         const float T = fmaf(o[0], r2, o[1] * r2);
         float Fb[7];
         boys_dyn<6>(L, T, Fb, A.boys);

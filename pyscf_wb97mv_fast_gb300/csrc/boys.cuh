@@ -20,6 +20,86 @@ namespace wb {
 // ---------------------------------------------------------------------------
 #define WB_BOYS_TSWITCH 36.0f
 
+// The T < 36 branch alone (T in [0, 36.06)): Taylor about the nearest node.
+template<int L>
+__device__ __forceinline__ void boys_taylor(float T, float* F,
+                                            const float4* __restrict__ tab) {
+    T = fmaxf(T, 0.0f);
+    const int k = __float2int_rn(T * 4.0f);
+    const float mh = fmaf(0.25f, (float)k, -T);           // -h, exact
+    const float q1 = mh;
+    const float q2 = q1 * mh * 0.5f;
+    const float q3 = q2 * mh * (1.0f / 3.0f);
+    const float q4 = q3 * mh * 0.25f;
+    const float q5 = q4 * mh * 0.2f;
+    const float q6 = q5 * mh * (1.0f / 6.0f);
+    const float4* row = tab + k * 5;
+    float hv[13], lv[7];
+    {
+        const float4 a = row[0], b = row[1];
+        hv[0] = a.x; hv[1] = a.y; hv[2] = a.z; hv[3] = a.w;
+        hv[4] = b.x; hv[5] = b.y; hv[6] = b.z; lv[0] = b.w;
+    }
+    if (L >= 1) {
+        const float4 c = row[2];
+        hv[7] = c.x; lv[1] = c.y; hv[8] = c.z; lv[2] = c.w;
+    }
+    if (L >= 3) {
+        const float4 d = row[3];
+        hv[9] = d.x; lv[3] = d.y; hv[10] = d.z; lv[4] = d.w;
+    }
+    if (L >= 5) {
+        const float4 e = row[4];
+        hv[11] = e.x; lv[5] = e.y; hv[12] = e.z; lv[6] = e.w;
+    }
+#pragma unroll
+    for (int n = 0; n <= L; ++n) {
+        float s = q6 * hv[n + 6];
+        s = fmaf(q5, hv[n + 5], s);
+        s = fmaf(q4, hv[n + 4], s);
+        s = fmaf(q3, hv[n + 3], s);
+        s = fmaf(q2, hv[n + 2], s);
+        s = fmaf(q1, hv[n + 1], s);
+        s = s + lv[n];
+        F[n] = hv[n] + s;
+    }
+}
+
+// Far field, T >= 36 (erf(sqrt T) = 1 to FP64 precision): the Hermite
+// sources R000_n = c_n F_n(T) are (-1)^n (2n-1)!! K0 r^-(2n+1), K0 = c_0
+// sqrt(pi) / (2 sqrt(theta p)) per primitive pair (hi + lo).  1/r is carried
+// in double-float (rsqrt and one Newton correction), the powers and the
+// odd double factorials in double-float, one rounding per R000_n -- the
+// same accuracy as c_n times the asymptotic F_n in double-float.
+template<int L>
+__device__ __forceinline__ void far_r000(const float r2, const float k0h,
+                                         const float k0l, float* R) {
+    const float s0 = rsqrtf(r2);
+    const float a = s0 * s0;
+    const float a_lo = fmaf(s0, s0, -a);
+    const float rr = fmaf(-r2, a, 1.0f) - r2 * a_lo;
+    const float sh = s0, sl = 0.5f * s0 * rr;
+    R[0] = fmaf(k0h, sh, fmaf(k0h, sl, k0l * sh));
+    if (L >= 1) {
+        const float uh = sh * sh;
+        const float ul = fmaf(sh, sh, -uh) + 2.0f * sh * sl;
+        float th = k0h * sh;
+        float tl = fmaf(k0h, sh, -th) + fmaf(k0h, sl, k0l * sh);
+#pragma unroll
+        for (int n = 1; n <= L; ++n) {
+            // t *= u, then R000_n = t (-(2n-1)!!)
+            const float p = th * uh;
+            const float e = fmaf(th, uh, -p) + fmaf(th, ul, tl * uh);
+            th = p + e;
+            tl = e - (th - p);
+            float df = 1.0f;
+            for (int j = 1; j <= n; ++j) df *= -(float)(2 * j - 1);
+            const float q = th * df;
+            R[n] = q + (fmaf(th, df, -q) + tl * df);
+        }
+    }
+}
+
 template<int L>
 __device__ __forceinline__ void boys_fp32(float T, float* F,
                                           const float4* __restrict__ tab) {

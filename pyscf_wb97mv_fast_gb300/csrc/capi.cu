@@ -128,7 +128,7 @@ struct wb_cosx {
     double* sh_ctr = nullptr;
     double* exps = nullptr;
     double* coeffs = nullptr;
-    int blocks_per_sm[wb::NCLASS] = {0};
+    int blocks_per_sm[wb::NCLASS][2] = {};   // [class][far variant]
     // class launches run concurrently on their own streams (fork / join by
     // events on the caller's stream), largest estimated work first
     cudaStream_t cstream[wb::NCLASS] = {};
@@ -142,7 +142,7 @@ namespace {
 
 struct WsLayout {
     size_t om = 0, rec = 0, gh = 0, gl = 0, counters = 0, work = 0;
-    size_t subcr[2] = {0, 0}, msh[2] = {0, 0};     // 32- and 64-point blocks
+    size_t subcr[3] = {0, 0, 0}, msh[3] = {0, 0, 0};  // 32/64/128-point blocks
     size_t gcls = 0;
     size_t X = 0, F64 = 0, F32 = 0, G32 = 0, oz = 0, total = 0;
 };
@@ -158,12 +158,13 @@ WsLayout ws_layout(const wb_cosx* h, int64_t ldt, bool full) {
     const int nao = h->hp.nao;
     L.counters = take(sizeof(unsigned long long) * 3 * wb::NCLASS);
     L.work = take(sizeof(int) * wb::NCLASS);
-    L.om = take(sizeof(float) * 16 * (size_t)std::max(h->hp.npp, 1));
+    L.om = take(sizeof(float) * wb::OMEGA_REC * (size_t)std::max(h->hp.npp, 1));
     L.rec = take(sizeof(float4) * (size_t)std::max<int64_t>(h->hp.nrec, 1));
     L.gh = take(sizeof(float) * 3 * (size_t)ldt);
     L.gl = take(sizeof(float) * 3 * (size_t)ldt);
-    for (int b = 0; b < 2; ++b) {
-        const int64_t nblk = (ldt + 32 * (b + 1) - 1) / (32 * (b + 1));
+    for (int b = 0; b < 3; ++b) {
+        const int64_t bp = 32 << b;
+        const int64_t nblk = (ldt + bp - 1) / bp;
         L.subcr[b] = take(sizeof(float4) * (size_t)nblk);
         L.msh[b] = take(sizeof(float) * (size_t)nblk * std::max(h->hp.nvshell, 1));
     }
@@ -213,10 +214,11 @@ wb::CosxArgs make_args(const wb_cosx* h, void* ws, const WsLayout& L,
     a.ptau = h->ptau;
     a.bnd = h->bnd;
     a.bpref = h->bpref;
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < 3; ++b) {
+        const int64_t bp = 32 << b;
         a.blk_cr[b] = at<float4>(ws, L.subcr[b]);
         a.blk_msh[b] = at<float>(ws, L.msh[b]);
-        a.nblk[b] = (int)((ldt + 32 * (b + 1) - 1) / (32 * (b + 1)));
+        a.nblk[b] = (int)((ldt + bp - 1) / bp);
     }
     a.nvshell = h->hp.nvshell;
     a.tol = tile_tol > 0.0 ? (float)(tile_tol / 1.001) : 0.0f;
@@ -259,11 +261,13 @@ int tile_prep(wb_cosx* h, const double* coords, const double* weights,
               const WsLayout& L, cudaStream_t s, int* launches) {
     WB_CUDA(wb::launch_grid_prep(coords, npts_t, ldt, at<float>(ws, L.gh),
                                  at<float>(ws, L.gl), s));
-    WB_CUDA(wb::launch_sub_stats(coords, weights, F, npts_t, ldt,
-                                 h->hp.nvshell, h->vs_ao0, h->vs_nf,
-                                 at<float4>(ws, L.subcr[0]), at<float>(ws, L.msh[0]),
-                                 at<float4>(ws, L.subcr[1]), at<float>(ws, L.msh[1]),
-                                 s));
+    wb::BlockStatsOut bo;
+    for (int b = 0; b < 3; ++b) {
+        bo.cr[b] = at<float4>(ws, L.subcr[b]);
+        bo.msh[b] = at<float>(ws, L.msh[b]);
+    }
+    WB_CUDA(wb::launch_sub_stats(coords, weights, F, npts_t, ldt, h->hp.nvshell,
+                                 h->vs_ao0, h->vs_nf, bo, s));
     *launches += 2;
     return WB_OK;
 }
@@ -272,9 +276,12 @@ int tile_prep(wb_cosx* h, const double* coords, const double* weights,
 // G are (nao, ldt) AO-major.  The classes fill their own partial-G buffers
 // concurrently; G is their fixed-order sum.
 int run_g_classes(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
-                  float* G, double tile_tol, void* ws, const WsLayout& L,
-                  cudaStream_t s, int* launches) {
+                  float* G, double omega, double tile_tol, void* ws,
+                  const WsLayout& L, cudaStream_t s, int* launches) {
     const wb::CosxArgs a = make_args(h, ws, L, ldt, npts_t, F, tile_tol);
+    // the far-field R000 variant pays where T = theta p r^2 >= 36 is common:
+    // the full-range operator (theta = 1); long-range omegas keep T small
+    const bool far = omega == 0.0;
     WB_CUDA(cudaMemsetAsync(at<float>(ws, L.gcls), 0,
                             sizeof(float) * (size_t)h->hp.ncrow * ldt, s));
     WB_CUDA(cudaMemsetAsync(at<int>(ws, L.work), 0, sizeof(int) * wb::NCLASS, s));
@@ -283,12 +290,13 @@ int run_g_classes(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
         const int c = h->corder[i];
         const wb::ClassRange& r = h->hp.cls[c];
         if (r.pair_end <= r.pair_begin) continue;
-        const int want = (a.nblk[h->pts[c] - 1] + 3) / 4;
-        const int cap = std::max(1, h->blocks_per_sm[c]) * h->nsm;
+        const int lvl = h->pts[c] == 4 ? 2 : h->pts[c] - 1;
+        const int want = (a.nblk[lvl] + 3) / 4;
+        const int cap = std::max(1, h->blocks_per_sm[c][far ? 1 : 0]) * h->nsm;
         const int grid = std::max(1, std::min(want, cap));
         WB_CUDA(cudaStreamWaitEvent(h->cstream[c], h->fork, 0));
         WB_CUDA(wb::launch_cosx_class_range(c, a, r.pair_begin, r.pair_end,
-                                            grid, h->cstream[c]));
+                                            grid, h->cstream[c], far));
         WB_CUDA(cudaEventRecord(h->cdone[c], h->cstream[c]));
         WB_CUDA(cudaStreamWaitEvent(s, h->cdone[c], 0));
         *launches += 1;
@@ -465,7 +473,8 @@ int wb_cosx_create(const wb_basis* basis, const double origin[3],
     if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS)
         return cleanup(fail(WB_ERR_CUBLAS, "cublasCreate failed"));
     for (int c = 0; c < wb::NCLASS; ++c) {
-        h->blocks_per_sm[c] = wb::cosx_class_blocks_per_sm(c);
+        h->blocks_per_sm[c][0] = wb::cosx_class_blocks_per_sm(c, false);
+        h->blocks_per_sm[c][1] = wb::cosx_class_blocks_per_sm(c, true);
         h->pts[c] = wb::cosx_class_pts(c);
     }
     {   // launch order: model flops of all pairs of a class, descending
@@ -659,8 +668,8 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
             double* Kj = k_out + kk * j;
             if ((st = prepare_omega(h, omegas[j], workspace, L, s)) != WB_OK) return st;
             launches += 2;
-            if ((st = run_g_classes(h, nt, ldt, F32, G32, tile_tol, workspace, L,
-                                    s, &launches)) != WB_OK)
+            if ((st = run_g_classes(h, nt, ldt, F32, G32, omegas[j], tile_tol,
+                                    workspace, L, s, &launches)) != WB_OK)
                 return st;
             ntasks += (ldt / 32) * (int64_t)h->hp.npairs;
             if (oz_k) {
@@ -717,7 +726,8 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
     int launches = 2;
     int st = tile_prep(h, coords, weights, npts, ldt, f, workspace, L, s, &launches);
     if (st != WB_OK) return st;
-    st = run_g_classes(h, npts, ldt, f, g_out, tile_tol, workspace, L, s, &launches);
+    st = run_g_classes(h, npts, ldt, f, g_out, omega, tile_tol, workspace, L, s,
+                       &launches);
     if (st != WB_OK) return st;
     return read_stats(h, workspace, L, (ldt / 32) * (int64_t)h->hp.npairs, s,
                       stats, launches);
@@ -802,7 +812,7 @@ int wb_int3c1e_dense(const wb_cosx* h, const double* coords, int64_t npts,
         return fail(WB_ERR_INVALID_ARGUMENT, "wb_int3c1e_dense: bad arguments");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int64_t ldt = round32(npts);
-    const size_t om_bytes = align256(sizeof(float) * 16 * (size_t)std::max(h->hp.npp, 1));
+    const size_t om_bytes = align256(sizeof(float) * wb::OMEGA_REC * (size_t)std::max(h->hp.npp, 1));
     const size_t g_bytes = align256(sizeof(float) * 3 * (size_t)ldt);
     void* tmp = nullptr;
     WB_CUDA(cudaMallocAsync(&tmp, om_bytes + 2 * g_bytes, s));

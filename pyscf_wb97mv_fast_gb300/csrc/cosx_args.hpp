@@ -9,7 +9,8 @@ constexpr int kClasses = 10;
 
 // Everything one class launch reads.  Per primitive pair m (global index):
 //   geo[2m], geo[2m+1]   P hi (xyz, 0), P lo (xyz, 0)      molecule frame
-//   om[4m .. 4m+3]       tp_hi, tp_lo, c0_hi, c0_lo, ..., c6_hi, c6_lo
+//   om[5m .. 5m+4]       tp_hi, tp_lo, c0_hi, c0_lo, ..., c6_hi, c6_lo,
+//                        K0_hi, K0_lo, r^2 far-field threshold, 0
 //   Ecls[c] + (m - pp_begin[c]) * stride_c/4   packed Hermite E
 // Per pair k: hdr[k] = (ia0, ib0, pp0, npp | diag << 16), khdr[k] = (ia0 |
 // ga0 << 16, ib0 | gb0 << 16, pp0, npp | diag << 16) with ga0 / gb0 the
@@ -34,11 +35,11 @@ struct CosxArgs {
     const float2* ptau;
     const float4* bnd;         // per pp: P (FP32), p' = 0.75 p
     const float* bpref;        // per pp: bound prefactor (rounded up)
-    // per block of 32 * PTS points (index PTS - 1): centroid (xyz), radius
+    // per block of 32 * PTS points (index log2 PTS): centroid (xyz), radius
     // and msh (nblk, nvshell) = max_g w_g sum_shell |F|
-    const float4* blk_cr[2];
-    const float* blk_msh[2];
-    int nblk[2];
+    const float4* blk_cr[3];
+    const float* blk_msh[3];
+    int nblk[3];
     int nvshell;
     float tol;                 // tile_tol / 1.001, <= 0 keeps every task
     const float* gxyz_hi;      // (3, ld) SoA grid coordinates, hi

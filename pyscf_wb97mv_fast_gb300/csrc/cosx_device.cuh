@@ -10,10 +10,7 @@ namespace wb {
 // for small classes, the Hermite E record), held in registers one pair
 // ahead of the computation.
 template<int LA, int LB> struct CosxRec;
-
-template<int LA, int LB>
-__device__ __forceinline__ void cosx_rec_load(const CosxArgs& A, const int m,
-                                              CosxRec<LA, LB>& r);
+// (one overload per class, generated: cosx_rec_load<FAR>(A, m, rec))
 
 // One task of class (LA, LB) on PTS grid points per lane (arrays of PTS:
 // Gp = the point's column of the class buffer (row stride ld; points past
@@ -24,8 +21,11 @@ __device__ __forceinline__ void cosx_rec_load(const CosxArgs& A, const int m,
 // (PTS x NCA) carried across the run of tasks with the same A.  rec holds
 // pair pp0's record on entry and pair nxt's on exit (the next task's first
 // pair).  The DIAG form (B = A) adds its ket accumulators to Xa instead of
-// writing G_B.  Specialised per (LA, LB, DIAG) with run() as the body.
-template<int LA, int LB, bool DIAG, int PTS> struct CosxTask;
+// writing G_B.  FAR selects the R000 form: the far-field expression under
+// warp-uniform branches (T >= 36 common: omega = 0) or boys_fp32 per point
+// (long-range omegas).  Specialised per (LA, LB, DIAG, FAR) with run() as
+// the body.
+template<int LA, int LB, bool DIAG, int PTS, bool FAR> struct CosxTask;
 
 // Start of a run: f0 = c2s^T F_A (Cartesian components of F on shell A).
 template<int LA>

@@ -88,14 +88,25 @@ __device__ __forceinline__ int hi16(const int x) {
     return (int)((unsigned)x >> 16);
 }
 
-// Points per lane of each class: 2 for the light classes, whose tasks have
-// one to a few primitive pairs (the per-task and per-pair overhead is then
-// shared by two points), 1 for the register-heavy ones.
+// Points per lane of each class (1, 2 or 4), one hex digit per class in
+// class order: more points share the per-task and per-primitive-pair
+// overhead of the light classes (tasks of one to a few primitive pairs) at
+// the cost of registers and of a screen over larger blocks.  A build may
+// override it with -DWB_COSX_PTS=0x<10 hex digits>LL.
+#ifndef WB_COSX_PTS
+#define WB_COSX_PTS 0x2222111111LL
+#endif
+constexpr int class_pts(int cls) {
+    long long v = WB_COSX_PTS;
+    for (int i = cls; i < kClasses - 1; ++i) v >>= 4;
+    const int p = (int)(v & 15);
+    return p >= 4 ? 4 : (p >= 2 ? 2 : 1);
+}
 template<int LA, int LB> struct ClassPts {
-    static constexpr int value = (LA + LB <= 2) ? 2 : 1;
+    static constexpr int value = class_pts(LA * (LA + 1) / 2 + LB);
 };
 
-template<int LA, int LB>
+template<int LA, int LB, bool FAR>
 __global__ void __launch_bounds__(kCtaThreads,
                                   min_blocks(LA * (LA + 1) / 2 + LB))
 cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
@@ -114,9 +125,10 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
     const float tol = A.tol;
     const float4* __restrict__ bnd = A.bnd + A.pp_begin[CLS];
     const float* __restrict__ bpref = A.bpref + A.pp_begin[CLS];
-    const float4* __restrict__ blk_cr = A.blk_cr[PTS - 1];
-    const float* __restrict__ blk_msh = A.blk_msh[PTS - 1];
-    const int nblk = A.nblk[PTS - 1];
+    constexpr int LVL = PTS == 4 ? 2 : PTS - 1;
+    const float4* __restrict__ blk_cr = A.blk_cr[LVL];
+    const float* __restrict__ blk_msh = A.blk_msh[LVL];
+    const int nblk = A.nblk[LVL];
     unsigned long long kept = 0, flops = 0, ints = 0;
     for (;;) {
         int blk = 0;
@@ -195,7 +207,7 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
             for (int p = 0; p < PTS; ++p)
                 load_f<NB>(Fp[p], ld, lo16(hdr.y), fb + p * NB);
             CosxRec<LA, LB> rec;
-            cosx_rec_load<LA, LB>(A, hdr.z, rec);
+            cosx_rec_load<FAR>(A, hdr.z, rec);
             while (true) {
                 if (hdr.x != curA) {
                     if (curA >= 0) {
@@ -239,15 +251,15 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
                 const int nxt = more ? hn.z : pp0;
                 if constexpr (LA == LB) {
                     if (hdr.w >> 16)
-                        CosxTask<LA, LB, true, PTS>::run(
+                        CosxTask<LA, LB, true, PTS, FAR>::run(
                             A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
                             gxl, gyl, gzl, stab, f0, fb, Xa, rec);
                     else
-                        CosxTask<LA, LB, false, PTS>::run(
+                        CosxTask<LA, LB, false, PTS, FAR>::run(
                             A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
                             gxl, gyl, gzl, stab, f0, fb, Xa, rec);
                 } else {
-                    CosxTask<LA, LB, false, PTS>::run(
+                    CosxTask<LA, LB, false, PTS, FAR>::run(
                         A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
                         gxl, gyl, gzl, stab, f0, fb, Xa, rec);
                 }

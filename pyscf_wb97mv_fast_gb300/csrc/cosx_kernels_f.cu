@@ -5,37 +5,43 @@ namespace wb {
 
 template<int LA, int LB>
 static cudaError_t run(const CosxArgs& a, int pb, int pe, int grid,
-                       cudaStream_t s) {
-    cosx_class_kernel<LA, LB><<<grid, kCtaThreads, 0, s>>>(a, pb, pe);
+                       cudaStream_t s, bool far) {
+    if (far)
+        cosx_class_kernel<LA, LB, true><<<grid, kCtaThreads, 0, s>>>(a, pb, pe);
+    else
+        cosx_class_kernel<LA, LB, false><<<grid, kCtaThreads, 0, s>>>(a, pb, pe);
     return cudaGetLastError();
 }
 
 template<int LA, int LB>
-static int occ() {
+static int occ(bool far) {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &n, cosx_class_kernel<LA, LB>, kCtaThreads, 0) != cudaSuccess)
-        return 1;
+    const cudaError_t e = far
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &n, cosx_class_kernel<LA, LB, true>, kCtaThreads, 0)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+              &n, cosx_class_kernel<LA, LB, false>, kCtaThreads, 0);
+    if (e != cudaSuccess) return 1;
     return n > 0 ? n : 1;
 }
 
 cudaError_t launch_cosx_f_class(int cls, const CosxArgs& a, int pb, int pe,
-                                int grid, cudaStream_t s) {
+                                int grid, cudaStream_t s, bool far) {
     switch (cls) {
-    case 6: return run<3, 0>(a, pb, pe, grid, s);
-    case 7: return run<3, 1>(a, pb, pe, grid, s);
-    case 8: return run<3, 2>(a, pb, pe, grid, s);
-    case 9: return run<3, 3>(a, pb, pe, grid, s);
+    case 6: return run<3, 0>(a, pb, pe, grid, s, far);
+    case 7: return run<3, 1>(a, pb, pe, grid, s, far);
+    case 8: return run<3, 2>(a, pb, pe, grid, s, far);
+    case 9: return run<3, 3>(a, pb, pe, grid, s, far);
     default: return cudaErrorInvalidValue;
     }
 }
 
-int cosx_f_class_blocks_per_sm(int cls) {
+int cosx_f_class_blocks_per_sm(int cls, bool far) {
     switch (cls) {
-    case 6: return occ<3, 0>();
-    case 7: return occ<3, 1>();
-    case 8: return occ<3, 2>();
-    case 9: return occ<3, 3>();
+    case 6: return occ<3, 0>(far);
+    case 7: return occ<3, 1>(far);
+    case 8: return occ<3, 2>(far);
+    case 9: return occ<3, 3>(far);
     default: return 1;
     }
 }

@@ -261,8 +261,10 @@ def gen_end(la):
 
 
 def n_om(la, lb):
-    """float4 per primitive pair of the omega record a class reads."""
-    return 1 + (la + lb + 1) // 2
+    """float4 per primitive pair of the omega record a class reads: theta p
+    and c_0..c_L (hi + lo), then the far-field float4 (K0 hi, K0 lo, r^2
+    threshold)."""
+    return 2 + (la + lb + 1) // 2
 
 
 def pipe_e(la, lb):
@@ -280,7 +282,9 @@ def rec_stride(la, lb):
 def gen_rec(la, lb):
     """Per-class record of one primitive pair (geo, omega and, for small
     classes, E) and its loader: the task loop keeps the next pair's record
-    in flight while it computes the current one.  m is class-local."""
+    in flight while it computes the current one.  m is class-local; the
+    far-field float4 (last omega float4) is loaded by the FAR variant
+    only."""
     nom = n_om(la, lb)
     nvec = e_stride(la, lb) // 4 if pipe_e(la, lb) else 0
     mem = ['g0', 'g1'] + ['o%d' % q for q in range(nom)] + \
@@ -288,7 +292,7 @@ def gen_rec(la, lb):
     lines = ['template<> struct CosxRec<%d, %d> {' % (la, lb),
              '    float4 %s;' % ', '.join(mem),
              '};',
-             'template<> __device__ __forceinline__ void cosx_rec_load<%d, %d>(' % (la, lb),
+             'template<bool FAR> __device__ __forceinline__ void cosx_rec_load(',
              '    const CosxArgs& A, const int m, CosxRec<%d, %d>& r)' % (la, lb),
              '{']
     I = '    '
@@ -296,15 +300,16 @@ def gen_rec(la, lb):
                  % (class_id(la, lb), rec_stride(la, lb)))
     lines.append(I + 'r.g0 = __ldg(q);')
     lines.append(I + 'r.g1 = __ldg(q + 1);')
-    for k in range(nom):
+    for k in range(nom - 1):
         lines.append(I + 'r.o%d = __ldg(q + %d);' % (k, 2 + k))
+    lines.append(I + 'if (FAR) r.o%d = __ldg(q + %d);' % (nom - 1, 1 + nom))
     for k in range(nvec):
         lines.append(I + 'r.e%d = __ldg(q + %d);' % (k, 2 + nom + k))
     lines.append('}')
     return '\n'.join(lines)
 
 
-def gen_prim_body(la, lb, diag, rv, J, lines):
+def gen_prim_body(la, lb, diag, rv, J, lines, far=True):
     """Work of primitive pair m with its record in variable rv, for each of
     the PTS points of the lane: Boys, R recurrence, Hermite sums and the Y
     (and X) accumulation.  The record and E are shared by the points."""
@@ -341,23 +346,84 @@ def gen_prim_body(la, lb, diag, rv, J, lines):
                 nm = flat[4 * q + c]
                 if nm is not None:
                     lines.append(J + 'const float %s = ev%d.%s;' % (nm, q, comp[c]))
+    if not far:
+        # Boys by boys_fp32 per point (Taylor / asymptotic / zero branches):
+        # the form for long-range omegas, where T >= 36 is rare
+        lines.append(J + 'float dxv[PTS], dyv[PTS], dzv[PTS], R0[PTS][%d];' % (L + 1))
+        lines.append(J + '#pragma unroll')
+        lines.append(J + 'for (int p = 0; p < PTS; ++p) {')
+        lines.append(J + '    dxv[p] = (ph.x - gxh[p]) + (pl.x - gxl[p]);')
+        lines.append(J + '    dyv[p] = (ph.y - gyh[p]) + (pl.y - gyl[p]);')
+        lines.append(J + '    dzv[p] = (ph.z - gzh[p]) + (pl.z - gzl[p]);')
+        lines.append(J + '    const float r2 = fmaf(dxv[p], dxv[p], fmaf(dyv[p], dyv[p], dzv[p] * dzv[p]));')
+        lines.append(J + '    const float T = fmaf(o0.x, r2, o0.y * r2);')
+        lines.append(J + '    float Fb[%d];' % (L + 1))
+        lines.append(J + '    boys_fp32<%d>(T, Fb, stab);' % L)
+        for n in range(L + 1):
+            fh = 2 + 2 * n
+            fl = fh + 1
+            ch = 'o%d.%s' % (fh // 4, comp[fh % 4])
+            cl = 'o%d.%s' % (fl // 4, comp[fl % 4])
+            lines.append(J + '    R0[p][%d] = fmaf(%s, Fb[%d], %s * Fb[%d]);'
+                         % (n, ch, n, cl, n))
+        lines.append(J + '}')
+    else:
+        of = 'o%d' % (nom - 1)          # far-field float4: K0 hi, K0 lo, thr
+        # distances, then R000 for every point: the far-field form when the
+        # whole warp is far (a uniform branch), else per point
+        lines.append(J + 'float dxv[PTS], dyv[PTS], dzv[PTS], r2v[PTS];')
+        lines.append(J + 'bool allfar = true, anyfar = false;')
+        lines.append(J + '#pragma unroll')
+        lines.append(J + 'for (int p = 0; p < PTS; ++p) {')
+        lines.append(J + '    dxv[p] = (ph.x - gxh[p]) + (pl.x - gxl[p]);')
+        lines.append(J + '    dyv[p] = (ph.y - gyh[p]) + (pl.y - gyl[p]);')
+        lines.append(J + '    dzv[p] = (ph.z - gzh[p]) + (pl.z - gzl[p]);')
+        lines.append(J + '    r2v[p] = fmaf(dxv[p], dxv[p], fmaf(dyv[p], dyv[p], dzv[p] * dzv[p]));')
+        lines.append(J + '    const bool f = r2v[p] >= %s.z;' % of)
+        lines.append(J + '    allfar = allfar && f;')
+        lines.append(J + '    anyfar = anyfar || f;')
+        lines.append(J + '}')
+        lines.append(J + 'float R0[PTS][%d];' % (L + 1))
+
+        def near(ind, p):
+            lines.append(ind + 'const float T = fmaf(o0.x, r2v[%s], o0.y * r2v[%s]);' % (p, p))
+            lines.append(ind + 'float Fb[%d];' % (L + 1))
+            lines.append(ind + 'boys_taylor<%d>(T, Fb, stab);' % L)
+            for n in range(L + 1):
+                fh = 2 + 2 * n
+                fl = fh + 1
+                ch = 'o%d.%s' % (fh // 4, comp[fh % 4])
+                cl = 'o%d.%s' % (fl // 4, comp[fl % 4])
+                lines.append(ind + 'R0[%s][%d] = fmaf(%s, Fb[%d], %s * Fb[%d]);'
+                             % (p, n, ch, n, cl, n))
+
+        # uniform branches when the whole warp is far (T >= 36) or near; the
+        # per-point branch only for mixed warps
+        lines.append(J + 'if (__all_sync(0xffffffffu, allfar)) {')
+        lines.append(J + '    #pragma unroll')
+        lines.append(J + '    for (int p = 0; p < PTS; ++p)')
+        lines.append(J + '        far_r000<%d>(r2v[p], %s.x, %s.y, R0[p]);' % (L, of, of))
+        lines.append(J + '} else if (!__any_sync(0xffffffffu, anyfar)) {')
+        lines.append(J + '    #pragma unroll')
+        lines.append(J + '    for (int p = 0; p < PTS; ++p) {')
+        near(J + '        ', 'p')
+        lines.append(J + '    }')
+        lines.append(J + '} else {')
+        lines.append(J + '    #pragma unroll')
+        lines.append(J + '    for (int p = 0; p < PTS; ++p) {')
+        lines.append(J + '        if (r2v[p] >= %s.z) {' % of)
+        lines.append(J + '            far_r000<%d>(r2v[p], %s.x, %s.y, R0[p]);' % (L, of, of))
+        lines.append(J + '        } else {')
+        near(J + '            ', 'p')
+        lines.append(J + '        }')
+        lines.append(J + '    }')
+        lines.append(J + '}')
     lines.append(J + '#pragma unroll')
     lines.append(J + 'for (int p = 0; p < PTS; ++p) {')
     K = J + '    '
-    lines.append(K + 'const float dx = (ph.x - gxh[p]) + (pl.x - gxl[p]);')
-    lines.append(K + 'const float dy = (ph.y - gyh[p]) + (pl.y - gyl[p]);')
-    lines.append(K + 'const float dz = (ph.z - gzh[p]) + (pl.z - gzl[p]);')
-    lines.append(K + 'const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));')
-    lines.append(K + 'const float T = fmaf(o0.x, r2, o0.y * r2);')
-    lines.append(K + 'float Fb[%d];' % (L + 1))
-    lines.append(K + 'boys_fp32<%d>(T, Fb, stab);' % L)
+    lines.append(K + 'const float dx = dxv[p], dy = dyv[p], dz = dzv[p];')
     for n in range(L + 1):
-        fh = 2 + 2 * n
-        fl = fh + 1
-        ch = 'o%d.%s' % (fh // 4, comp[fh % 4])
-        cl = 'o%d.%s' % (fl // 4, comp[fl % 4])
-        lines.append(K + 'const float R000_%d = fmaf(%s, Fb[%d], %s * Fb[%d]);'
-                     % (n, ch, n, cl, n))
+        lines.append(K + 'const float R000_%d = R0[p][%d];' % (n, n))
     lines.append(K + 'float ' + ', '.join(rname(*x) for x in tuv) + ';')
     gen_recurrence(L, lines, K)
     for ia, cac in enumerate(ca):
@@ -372,15 +438,15 @@ def gen_prim_body(la, lb, diag, rv, J, lines):
     lines.append(J + '}')
 
 
-def gen_class(la, lb, diag):
+def gen_class(la, lb, diag, far):
     nb = 2 * lb + 1
     nca = (la + 1) * (la + 2) // 2
     ncb = (lb + 1) * (lb + 2) // 2
     ents = e_entries(la, lb)
     lines = []
     I = '    '
-    lines.append('template<int PTS> struct CosxTask<%d, %d, %s, PTS> {'
-                 % (la, lb, 'true' if diag else 'false'))
+    lines.append('template<int PTS> struct CosxTask<%d, %d, %s, PTS, %s> {'
+                 % (la, lb, 'true' if diag else 'false', 'true' if far else 'false'))
     lines.append('static __device__ __forceinline__ void run(')
     lines.append('    const CosxArgs& A, float* const* Gp, const int ld, const int gb0,')
     lines.append('    const int pp0, const int npp, const int nxt, const bool* ok,')
@@ -420,16 +486,16 @@ def gen_class(la, lb, diag):
     lines.append(I + 'int m = pp0;')
     lines.append(I + '#pragma unroll 1')
     lines.append(I + 'while (true) {')
-    lines.append(J + 'cosx_rec_load<%d, %d>(A, m + 1 < pend ? m + 1 : nxt, rb);'
-                 % (la, lb))
+    lines.append(J + 'cosx_rec_load<%s>(A, m + 1 < pend ? m + 1 : nxt, rb);'
+                 % ('true' if far else 'false'))
     lines.append(J + '{')
-    gen_prim_body(la, lb, diag, 'rec', J + I, lines)
+    gen_prim_body(la, lb, diag, 'rec', J + I, lines, far)
     lines.append(J + '}')
     lines.append(J + 'if (++m == pend) { rec = rb; break; }')
-    lines.append(J + 'cosx_rec_load<%d, %d>(A, m + 1 < pend ? m + 1 : nxt, rec);'
-                 % (la, lb))
+    lines.append(J + 'cosx_rec_load<%s>(A, m + 1 < pend ? m + 1 : nxt, rec);'
+                 % ('true' if far else 'false'))
     lines.append(J + '{')
-    gen_prim_body(la, lb, diag, 'rb', J + I, lines)
+    gen_prim_body(la, lb, diag, 'rb', J + I, lines, far)
     lines.append(J + '}')
     lines.append(J + 'if (++m == pend) break;')
     lines.append(I + '}')
@@ -473,11 +539,12 @@ def source():
         out.append(gen_rec(la, lb))
         out.append('')
     for (la, lb) in classes():
-        out.append(gen_class(la, lb, False))
-        out.append('')
-        if la == lb:
-            out.append(gen_class(la, lb, True))
+        for far in (False, True):
+            out.append(gen_class(la, lb, False, far))
             out.append('')
+            if la == lb:
+                out.append(gen_class(la, lb, True, far))
+                out.append('')
     # E strides table for the host
     out.append('#define WB_E_STRIDES {%s}' % ', '.join(
         str(e_stride(la, lb)) for (la, lb) in classes()))

@@ -4,7 +4,7 @@
 #pragma once
 
 namespace wb {
-constexpr int kRecNom[10] = {1, 2, 2, 2, 3, 3, 3, 3, 4, 4};
+constexpr int kRecNom[10] = {2, 3, 3, 3, 4, 4, 4, 4, 5, 5};
 constexpr int kRecNe[10] = {0, 2, 6, 4, 11, 20, 7, 18, 31, 48};
-constexpr int kRecStride[10] = {3, 6, 10, 8, 16, 25, 12, 23, 37, 54};
+constexpr int kRecStride[10] = {4, 7, 11, 9, 17, 26, 13, 24, 38, 55};
 }  // namespace wb

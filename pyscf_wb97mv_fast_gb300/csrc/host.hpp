@@ -13,7 +13,7 @@ constexpr int LMAX = 3;
 constexpr int NCLASS = 10;          // (la >= lb) classes, la, lb <= 3
 constexpr int BOYS_NODES = 145;     // T_k = k / 4, k = 0..144 (T < 36)
 constexpr int BOYS_ROW = 20;        // floats per table row (kernel layout)
-constexpr int OMEGA_REC = 16;       // floats per primitive pair per omega
+constexpr int OMEGA_REC = 20;       // floats per primitive pair per omega
 constexpr int NIA_MAX = 16;         // functions per shell (reference cap)
 constexpr int PPR_MAX = 16;         // primitives per shell (reference cap)
 

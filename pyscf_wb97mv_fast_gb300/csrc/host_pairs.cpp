@@ -469,7 +469,7 @@ int build_pairs(const wb_basis& b, const double origin[3], double cutoff,
     for (int la = 0; la <= LMAX; ++la)
         for (int lb = 0; lb <= la; ++lb) {
             const int c = class_of(la, lb);
-            if (kRecNe[c] * 4 != e_stride(la, lb) || kRecNom[c] != 1 + (la + lb + 1) / 2 ||
+            if (kRecNe[c] * 4 != e_stride(la, lb) || kRecNom[c] != 2 + (la + lb + 1) / 2 ||
                 kRecStride[c] != 2 + kRecNom[c] + kRecNe[c]) {
                 err = "generated record layout does not match the pair tables";
                 return WB_ERR_UNSUPPORTED;

@@ -7,11 +7,12 @@
 
 namespace wb {
 
-// per-class fused screen + G kernels (cosx_kernels_*.cu)
+// per-class fused screen + G kernels (cosx_kernels_*.cu); far selects the
+// variant with the far-field R000 form (omega = 0, where T >= 36 is common)
 cudaError_t launch_cosx_class_range(int cls, const CosxArgs& a, int pb,
-                                    int pe, int grid, cudaStream_t s);
+                                    int pe, int grid, cudaStream_t s, bool far);
 // max resident CTAs per SM of a class kernel (128 threads each)
-int cosx_class_blocks_per_sm(int cls);
+int cosx_class_blocks_per_sm(int cls, bool far);
 
 struct AoArgs {
     const double* coords;       // (npts, 3) molecule frame
@@ -50,14 +51,17 @@ cudaError_t launch_omega(int npp, const double* p, const double* pref,
                          double omega, float4* om, cudaStream_t s);
 cudaError_t launch_grid_prep(const double* coords, int64_t npts, int64_t ld,
                              float* hi, float* lo, cudaStream_t s);
-// centroid / radius and shell maxima per 32-point sub-block (ld / 32) and
-// per 64-point block (ceil(ld / 64)), one pass over F
+// centroid / radius and shell maxima per block of 32, 64 and 128 points
+// (level k = 0, 1, 2: ceil(ld / (32 2^k)) blocks), one pass over F
+struct BlockStatsOut {
+    float4* cr[3];
+    float* msh[3];
+};
 cudaError_t launch_sub_stats(const double* coords, const double* weights,
                              const float* F, int64_t npts, int64_t ld,
                              int nvshell, const int* vs_ao0, const int* vs_nf,
-                             float4* cr32, float* msh32, float4* cr64,
-                             float* msh64, cudaStream_t s);
-// points per lane (1 or 2) of a class kernel: its blocks hold 32 * pts
+                             const BlockStatsOut& out, cudaStream_t s);
+// points per lane (1, 2 or 4) of a class kernel: its blocks hold 32 * pts
 int cosx_class_pts(int cls);
 cudaError_t launch_f64_to_f32(const double* in, float* out, int64_t n,
                               cudaStream_t s);
