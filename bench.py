@@ -394,8 +394,7 @@ def main():
     n = g.size
     ld = round32(n)
     X = eng.ao_eval(coords_d)
-    F = (qd_d.T @ X).to(torch.float32)          # F^T = (X QD)^T, AO-major
-    F = F.contiguous()
+    F = eng.ozaki_f(X, qd_d)                    # fl32(X QD), AO-major
     Gt = torch.empty((mol.nao, ld), dtype=torch.float32, device=dev)
     g_flops = 0.0
     for w in OMEGAS:
@@ -412,7 +411,8 @@ def main():
     prof = traffic_from_profile()
     roofline = {'bound': 'fp32', 'achieved': achieved, 'peak': peak,
                 'unit': 'TFLOP/s', 'frac': achieved / peak if peak else None,
-                'traffic': prof.get('bytes_per_launch') if prof else None,
+                'traffic': prof.get('bytes_per_g_phase') if prof else None,
+                'traffic_source': prof.get('source') if prof else None,
                 'peak_source': 'measured in this run: wb_fp32_fma_probe '
                                '(FFMA-only kernel, all SMs)',
                 'kernel': 'fused screen + G kernels (10 class launches) of '
