@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -52,6 +53,11 @@ int cuda_fail(cudaError_t e, const char* where) {
     } while (0)
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// largest dynamic shared memory per CTA for staged primitive-pair records
+constexpr size_t kStageMaxBytes = 96 * 1024;
+// default staged classes: (0,0) (1,0) (1,1) (2,1)
+constexpr long long kStageClasses = 0x1110100000LL;
 inline int64_t round32(int64_t x) { return (x + 31) / 32 * 32; }
 
 // Boys table per device, built once per process
@@ -129,6 +135,9 @@ struct wb_cosx {
     double* exps = nullptr;
     double* coeffs = nullptr;
     int blocks_per_sm[wb::NCLASS][2] = {};   // [class][far variant]
+    int recmax[wb::NCLASS] = {0};            // float4 of the largest task record
+    size_t stage_smem[wb::NCLASS] = {0};     // dynamic smem of the staged variant
+                                             // (0: register-prefetch variant)
     // class launches run concurrently on their own streams (fork / join by
     // events on the caller's stream), largest estimated work first
     cudaStream_t cstream[wb::NCLASS] = {};
@@ -207,6 +216,7 @@ wb::CosxArgs make_args(const wb_cosx* h, void* ws, const WsLayout& L,
         a.Ecls[c] = h->E + h->hp.cls[c].e_base / 4;
         a.pp_begin[c] = h->hp.cls[c].pp_begin;
         a.rec[c] = at<float4>(ws, L.rec) + h->hp.rec_off[c];
+        a.recmax[c] = h->recmax[c];
     }
     a.hdr = h->hdr;
     a.khdr = h->khdr;
@@ -296,7 +306,8 @@ int run_g_classes(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
         const int grid = std::max(1, std::min(want, cap));
         WB_CUDA(cudaStreamWaitEvent(h->cstream[c], h->fork, 0));
         WB_CUDA(wb::launch_cosx_class_range(c, a, r.pair_begin, r.pair_end,
-                                            grid, h->cstream[c], far));
+                                            grid, h->cstream[c], far,
+                                            h->stage_smem[c]));
         WB_CUDA(cudaEventRecord(h->cdone[c], h->cstream[c]));
         WB_CUDA(cudaStreamWaitEvent(s, h->cdone[c], 0));
         *launches += 1;
@@ -472,9 +483,34 @@ int wb_cosx_create(const wb_basis* basis, const double origin[3],
     }
     if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS)
         return cleanup(fail(WB_ERR_CUBLAS, "cublasCreate failed"));
+    // classes whose records are staged in shared memory: one hex digit per
+    // class in class order (measured per class on the water27 workload:
+    // staging wins where the register-carried record cost moves and
+    // uniform-register traffic, loses where it raises spills); the
+    // environment variable WB_COSX_STAGE (same digits) overrides it
+    long long stage_mask = kStageClasses;
+    if (const char* env = std::getenv("WB_COSX_STAGE"))
+        stage_mask = std::strtoll(env, nullptr, 16);
     for (int c = 0; c < wb::NCLASS; ++c) {
-        h->blocks_per_sm[c][0] = wb::cosx_class_blocks_per_sm(c, false);
-        h->blocks_per_sm[c][1] = wb::cosx_class_blocks_per_sm(c, true);
+        // primitive-pair records staged in shared memory (two buffers per
+        // warp of the largest task's record) for the classes of the mask,
+        // unless that needs more than kStageMaxBytes per CTA
+        int rm = 0;
+        for (int k = hp.cls[c].pair_begin; k < hp.cls[c].pair_end; ++k)
+            rm = std::max(rm, (hp.hdr[4 * k + 3] & 0xffff) * wb::kRecStride[c]);
+        h->recmax[c] = rm;
+        const size_t smem = (size_t)(128 / 32) * 2 * rm * sizeof(float4);
+        const bool stage_on = ((stage_mask >> (4 * (wb::NCLASS - 1 - c))) & 15) != 0;
+        h->stage_smem[c] = (stage_on && rm > 0 && smem <= kStageMaxBytes) ? smem : 0;
+        int n[2];
+        for (int f = 0; f < 2; ++f)
+            n[f] = wb::cosx_class_blocks_per_sm(c, f == 1, h->stage_smem[c]);
+        if (h->stage_smem[c] && (n[0] == 0 || n[1] == 0)) {
+            h->stage_smem[c] = 0;
+            for (int f = 0; f < 2; ++f)
+                n[f] = wb::cosx_class_blocks_per_sm(c, f == 1, 0);
+        }
+        for (int f = 0; f < 2; ++f) h->blocks_per_sm[c][f] = std::max(n[f], 1);
         h->pts[c] = wb::cosx_class_pts(c);
     }
     {   // launch order: model flops of all pairs of a class, descending

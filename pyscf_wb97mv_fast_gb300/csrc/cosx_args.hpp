@@ -27,6 +27,7 @@ struct CosxArgs {
     // per class, packed per primitive pair (class-local index m):
     // rec[c] + m * stride_c = P hi, P lo, omega record (n_om float4), E
     const float4* rec[kClasses];
+    int recmax[kClasses];      // float4 of the largest task record per class
     const float4* Ecls[kClasses];
     int pp_begin[kClasses];
     const int4* hdr;

@@ -23,9 +23,11 @@ template<int LA, int LB> struct CosxRec;
 // pair).  The DIAG form (B = A) adds its ket accumulators to Xa instead of
 // writing G_B.  FAR selects the R000 form: the far-field expression under
 // warp-uniform branches (T >= 36 common: omega = 0) or boys_fp32 per point
-// (long-range omegas).  Specialised per (LA, LB, DIAG, FAR) with run() as
-// the body.
-template<int LA, int LB, bool DIAG, int PTS, bool FAR> struct CosxTask;
+// (long-range omegas).  STAGE: the task's primitive-pair records were
+// copied to shared memory (rp, stride per class) instead of being carried
+// in registers one pair ahead.  Specialised per (LA, LB, DIAG, FAR,
+// STAGE) with run() as the body.
+template<int LA, int LB, bool DIAG, int PTS, bool FAR, bool STAGE> struct CosxTask;
 
 // Start of a run: f0 = c2s^T F_A (Cartesian components of F on shell A).
 template<int LA>

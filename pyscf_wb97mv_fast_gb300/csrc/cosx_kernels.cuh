@@ -24,6 +24,7 @@
 #pragma once
 #include "launch.hpp"
 #include "cosx_device.cuh"
+#include "generated/cosx_layout.h"
 
 namespace wb {
 
@@ -83,6 +84,23 @@ __device__ __forceinline__ void load_f(const float* __restrict__ Fp,
     for (int nu = 0; nu < N; ++nu) f[nu] = Fp[(long long)(n0 + nu) * ld];
 }
 
+// per-lane asynchronous 16-byte global -> shared copies (cp.async; the
+// wait is the hardware's, no polling): lanes split the n float4
+__device__ __forceinline__ void stage_records(float4* dst,
+                                              const float4* __restrict__ src,
+                                              const int n, const int lane) {
+    for (int j = lane; j < n; j += 32) {
+        const unsigned d = (unsigned)__cvta_generic_to_shared(dst + j);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n"
+                     :: "r"(d), "l"(src + j) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void stage_wait() {
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncwarp();
+}
+
 __device__ __forceinline__ int lo16(const int x) { return x & 0xffff; }
 __device__ __forceinline__ int hi16(const int x) {
     return (int)((unsigned)x >> 16);
@@ -106,7 +124,7 @@ template<int LA, int LB> struct ClassPts {
     static constexpr int value = class_pts(LA * (LA + 1) / 2 + LB);
 };
 
-template<int LA, int LB, bool FAR>
+template<int LA, int LB, bool FAR, bool STAGE>
 __global__ void __launch_bounds__(kCtaThreads,
                                   min_blocks(LA * (LA + 1) / 2 + LB))
 cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
@@ -120,6 +138,13 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
         stab[i] = A.boys[i];
     __syncthreads();
     const int lane = threadIdx.x & 31;
+    // STAGE: per warp, two record buffers of recmax float4 (dynamic smem)
+    extern __shared__ float4 s_stage[];
+    constexpr int RS = kRecStride[CLS];
+    const int rmax = A.recmax[CLS];
+    float4* wstage = s_stage + (threadIdx.x >> 5) * 2 * rmax;
+    const float4* __restrict__ recc = A.rec[CLS];
+    int sbuf = 0;
     float* __restrict__ Gc = A.Gcls[CLS];
     const int ld = (int)A.ld;
     const float tol = A.tol;
@@ -207,7 +232,14 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
             for (int p = 0; p < PTS; ++p)
                 load_f<NB>(Fp[p], ld, lo16(hdr.y), fb + p * NB);
             CosxRec<LA, LB> rec;
-            cosx_rec_load<FAR>(A, hdr.z, rec);
+            if constexpr (STAGE) {
+                __syncwarp();       // the previous chunk's reads of the buffer
+                stage_records(wstage + sbuf * rmax, recc + (long long)hdr.z * RS,
+                              (hdr.w & 0xffff) * RS, lane);
+                stage_wait();
+            } else {
+                cosx_rec_load<FAR>(A, hdr.z, rec);
+            }
             while (true) {
                 if (hdr.x != curA) {
                     if (curA >= 0) {
@@ -246,25 +278,51 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
                             load_f<NA>(Fp[p], ld, lo16(hn.x), fan + p * NA);
                         pendA = hn.x;
                     }
+                    // the next task's records into the other buffer (the
+                    // last reads of it ended before the previous wait)
+                    if constexpr (STAGE)
+                        stage_records(wstage + (sbuf ^ 1) * rmax,
+                                      recc + (long long)hn.z * RS,
+                                      (hn.w & 0xffff) * RS, lane);
                 }
                 const int gb0 = hi16(hdr.y), pp0 = hdr.z, npp = hdr.w & 0xffff;
                 const int nxt = more ? hn.z : pp0;
-                if constexpr (LA == LB) {
+                if constexpr (STAGE) {
+                    const float4* rp = wstage + sbuf * rmax;
+                    if constexpr (LA == LB) {
+                        if (hdr.w >> 16)
+                            CosxTask<LA, LB, true, PTS, FAR, true>::run(
+                                A, Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                                gxl, gyl, gzl, stab, f0, fb, Xa);
+                        else
+                            CosxTask<LA, LB, false, PTS, FAR, true>::run(
+                                A, Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                                gxl, gyl, gzl, stab, f0, fb, Xa);
+                    } else {
+                        CosxTask<LA, LB, false, PTS, FAR, true>::run(
+                            A, Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                            gxl, gyl, gzl, stab, f0, fb, Xa);
+                    }
+                } else if constexpr (LA == LB) {
                     if (hdr.w >> 16)
-                        CosxTask<LA, LB, true, PTS, FAR>::run(
+                        CosxTask<LA, LB, true, PTS, FAR, false>::run(
                             A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
                             gxl, gyl, gzl, stab, f0, fb, Xa, rec);
                     else
-                        CosxTask<LA, LB, false, PTS, FAR>::run(
+                        CosxTask<LA, LB, false, PTS, FAR, false>::run(
                             A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
                             gxl, gyl, gzl, stab, f0, fb, Xa, rec);
                 } else {
-                    CosxTask<LA, LB, false, PTS, FAR>::run(
+                    CosxTask<LA, LB, false, PTS, FAR, false>::run(
                         A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
                         gxl, gyl, gzl, stab, f0, fb, Xa, rec);
                 }
                 kept += nsb;
                 if (!more) break;
+                if constexpr (STAGE) {
+                    stage_wait();
+                    sbuf ^= 1;
+                }
                 hdr = hn;
 #pragma unroll
                 for (int nu = 0; nu < PTS * NB; ++nu) fb[nu] = fbn[nu];

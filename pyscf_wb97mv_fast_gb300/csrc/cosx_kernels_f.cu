@@ -3,46 +3,68 @@
 
 namespace wb {
 
-template<int LA, int LB>
-static cudaError_t run(const CosxArgs& a, int pb, int pe, int grid,
-                       cudaStream_t s, bool far) {
-    if (far)
-        cosx_class_kernel<LA, LB, true><<<grid, kCtaThreads, 0, s>>>(a, pb, pe);
-    else
-        cosx_class_kernel<LA, LB, false><<<grid, kCtaThreads, 0, s>>>(a, pb, pe);
+template<int LA, int LB, bool FAR, bool STAGE>
+static cudaError_t run1(const CosxArgs& a, int pb, int pe, int grid,
+                        size_t smem, cudaStream_t s) {
+    auto k = cosx_class_kernel<LA, LB, FAR, STAGE>;
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(
+            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k<<<grid, kCtaThreads, smem, s>>>(a, pb, pe);
     return cudaGetLastError();
 }
 
 template<int LA, int LB>
-static int occ(bool far) {
+static cudaError_t run(const CosxArgs& a, int pb, int pe, int grid,
+                       cudaStream_t s, bool far, size_t smem) {
+    if (smem)
+        return far ? run1<LA, LB, true, true>(a, pb, pe, grid, smem, s)
+                   : run1<LA, LB, false, true>(a, pb, pe, grid, smem, s);
+    return far ? run1<LA, LB, true, false>(a, pb, pe, grid, 0, s)
+               : run1<LA, LB, false, false>(a, pb, pe, grid, 0, s);
+}
+
+template<int LA, int LB, bool FAR, bool STAGE>
+static int occ1(size_t smem) {
+    auto k = cosx_class_kernel<LA, LB, FAR, STAGE>;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+        return 0;
     int n = 0;
-    const cudaError_t e = far
-        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-              &n, cosx_class_kernel<LA, LB, true>, kCtaThreads, 0)
-        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-              &n, cosx_class_kernel<LA, LB, false>, kCtaThreads, 0);
-    if (e != cudaSuccess) return 1;
-    return n > 0 ? n : 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kCtaThreads, smem) !=
+        cudaSuccess)
+        return 0;
+    return n;
+}
+
+template<int LA, int LB>
+static int occ(bool far, size_t smem) {
+    if (smem)
+        return far ? occ1<LA, LB, true, true>(smem) : occ1<LA, LB, false, true>(smem);
+    return far ? occ1<LA, LB, true, false>(0) : occ1<LA, LB, false, false>(0);
 }
 
 cudaError_t launch_cosx_f_class(int cls, const CosxArgs& a, int pb, int pe,
-                                int grid, cudaStream_t s, bool far) {
+                                int grid, cudaStream_t s, bool far, size_t smem) {
     switch (cls) {
-    case 6: return run<3, 0>(a, pb, pe, grid, s, far);
-    case 7: return run<3, 1>(a, pb, pe, grid, s, far);
-    case 8: return run<3, 2>(a, pb, pe, grid, s, far);
-    case 9: return run<3, 3>(a, pb, pe, grid, s, far);
+    case 6: return run<3, 0>(a, pb, pe, grid, s, far, smem);
+    case 7: return run<3, 1>(a, pb, pe, grid, s, far, smem);
+    case 8: return run<3, 2>(a, pb, pe, grid, s, far, smem);
+    case 9: return run<3, 3>(a, pb, pe, grid, s, far, smem);
     default: return cudaErrorInvalidValue;
     }
 }
 
-int cosx_f_class_blocks_per_sm(int cls, bool far) {
+int cosx_f_class_blocks_per_sm(int cls, bool far, size_t smem) {
     switch (cls) {
-    case 6: return occ<3, 0>(far);
-    case 7: return occ<3, 1>(far);
-    case 8: return occ<3, 2>(far);
-    case 9: return occ<3, 3>(far);
-    default: return 1;
+    case 6: return occ<3, 0>(far, smem);
+    case 7: return occ<3, 1>(far, smem);
+    case 8: return occ<3, 2>(far, smem);
+    case 9: return occ<3, 3>(far, smem);
+    default: return 0;
     }
 }
 

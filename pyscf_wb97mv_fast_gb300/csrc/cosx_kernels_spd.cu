@@ -5,53 +5,76 @@
 namespace wb {
 
 cudaError_t launch_cosx_f_class(int cls, const CosxArgs& a, int pb, int pe,
-                                int grid, cudaStream_t s, bool far);
-int cosx_f_class_blocks_per_sm(int cls, bool far);
+                                int grid, cudaStream_t s, bool far, size_t smem);
+int cosx_f_class_blocks_per_sm(int cls, bool far, size_t smem);
 
-template<int LA, int LB>
-static cudaError_t run(const CosxArgs& a, int pb, int pe, int grid,
-                       cudaStream_t s, bool far) {
-    if (far)
-        cosx_class_kernel<LA, LB, true><<<grid, kCtaThreads, 0, s>>>(a, pb, pe);
-    else
-        cosx_class_kernel<LA, LB, false><<<grid, kCtaThreads, 0, s>>>(a, pb, pe);
+template<int LA, int LB, bool FAR, bool STAGE>
+static cudaError_t run1(const CosxArgs& a, int pb, int pe, int grid,
+                        size_t smem, cudaStream_t s) {
+    auto k = cosx_class_kernel<LA, LB, FAR, STAGE>;
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(
+            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k<<<grid, kCtaThreads, smem, s>>>(a, pb, pe);
     return cudaGetLastError();
 }
 
 template<int LA, int LB>
-static int occ(bool far) {
+static cudaError_t run(const CosxArgs& a, int pb, int pe, int grid,
+                       cudaStream_t s, bool far, size_t smem) {
+    if (smem)
+        return far ? run1<LA, LB, true, true>(a, pb, pe, grid, smem, s)
+                   : run1<LA, LB, false, true>(a, pb, pe, grid, smem, s);
+    return far ? run1<LA, LB, true, false>(a, pb, pe, grid, 0, s)
+               : run1<LA, LB, false, false>(a, pb, pe, grid, 0, s);
+}
+
+template<int LA, int LB, bool FAR, bool STAGE>
+static int occ1(size_t smem) {
+    auto k = cosx_class_kernel<LA, LB, FAR, STAGE>;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+        return 0;
     int n = 0;
-    const cudaError_t e = far
-        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-              &n, cosx_class_kernel<LA, LB, true>, kCtaThreads, 0)
-        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-              &n, cosx_class_kernel<LA, LB, false>, kCtaThreads, 0);
-    if (e != cudaSuccess) return 1;
-    return n > 0 ? n : 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kCtaThreads, smem) !=
+        cudaSuccess)
+        return 0;
+    return n;
+}
+
+template<int LA, int LB>
+static int occ(bool far, size_t smem) {
+    if (smem)
+        return far ? occ1<LA, LB, true, true>(smem) : occ1<LA, LB, false, true>(smem);
+    return far ? occ1<LA, LB, true, false>(0) : occ1<LA, LB, false, false>(0);
 }
 
 cudaError_t launch_cosx_class_range(int cls, const CosxArgs& a, int pb,
-                                    int pe, int grid, cudaStream_t s, bool far) {
+                                    int pe, int grid, cudaStream_t s, bool far,
+                                    size_t smem) {
     switch (cls) {
-    case 0: return run<0, 0>(a, pb, pe, grid, s, far);
-    case 1: return run<1, 0>(a, pb, pe, grid, s, far);
-    case 2: return run<1, 1>(a, pb, pe, grid, s, far);
-    case 3: return run<2, 0>(a, pb, pe, grid, s, far);
-    case 4: return run<2, 1>(a, pb, pe, grid, s, far);
-    case 5: return run<2, 2>(a, pb, pe, grid, s, far);
-    default: return launch_cosx_f_class(cls, a, pb, pe, grid, s, far);
+    case 0: return run<0, 0>(a, pb, pe, grid, s, far, smem);
+    case 1: return run<1, 0>(a, pb, pe, grid, s, far, smem);
+    case 2: return run<1, 1>(a, pb, pe, grid, s, far, smem);
+    case 3: return run<2, 0>(a, pb, pe, grid, s, far, smem);
+    case 4: return run<2, 1>(a, pb, pe, grid, s, far, smem);
+    case 5: return run<2, 2>(a, pb, pe, grid, s, far, smem);
+    default: return launch_cosx_f_class(cls, a, pb, pe, grid, s, far, smem);
     }
 }
 
-int cosx_class_blocks_per_sm(int cls, bool far) {
+int cosx_class_blocks_per_sm(int cls, bool far, size_t smem) {
     switch (cls) {
-    case 0: return occ<0, 0>(far);
-    case 1: return occ<1, 0>(far);
-    case 2: return occ<1, 1>(far);
-    case 3: return occ<2, 0>(far);
-    case 4: return occ<2, 1>(far);
-    case 5: return occ<2, 2>(far);
-    default: return cosx_f_class_blocks_per_sm(cls, far);
+    case 0: return occ<0, 0>(far, smem);
+    case 1: return occ<1, 0>(far, smem);
+    case 2: return occ<1, 1>(far, smem);
+    case 3: return occ<2, 0>(far, smem);
+    case 4: return occ<2, 1>(far, smem);
+    case 5: return occ<2, 2>(far, smem);
+    default: return cosx_f_class_blocks_per_sm(cls, far, smem);
     }
 }
 

@@ -309,8 +309,9 @@ def gen_rec(la, lb):
     return '\n'.join(lines)
 
 
-def gen_prim_body(la, lb, diag, rv, J, lines, far=True):
-    """Work of primitive pair m with its record in variable rv, for each of
+def gen_prim_body(la, lb, diag, rv, J, lines, far=True, stage=False):
+    """Work of primitive pair m with its record in variable rv (a CosxRec,
+    or with stage a pointer to the record in shared memory), for each of
     the PTS points of the lane: Boys, R recurrence, Hermite sums and the Y
     (and X) accumulation.  The record and E are shared by the points."""
     L = la + lb
@@ -323,11 +324,19 @@ def gen_prim_body(la, lb, diag, rv, J, lines, far=True):
     comp = 'xyzw'
     tuv = [(t, u, v) for t in range(L + 1) for u in range(L + 1 - t)
            for v in range(L + 1 - t - u)]
-    lines.append(J + 'const float4 ph = %s.g0, pl = %s.g1;' % (rv, rv))
-    for q in range(nom):
-        lines.append(J + 'const float4 o%d = %s.o%d;' % (q, rv, q))
+    if stage:
+        lines.append(J + 'const float4 ph = %s[0], pl = %s[1];' % (rv, rv))
+        for q in range(nom):
+            lines.append(J + 'const float4 o%d = %s[%d];' % (q, rv, 2 + q))
+    else:
+        lines.append(J + 'const float4 ph = %s.g0, pl = %s.g1;' % (rv, rv))
+        for q in range(nom):
+            lines.append(J + 'const float4 o%d = %s.o%d;' % (q, rv, q))
     if ents:
-        if pipe_e(la, lb):
+        if stage:
+            for q in range(nvec):
+                lines.append(J + 'const float4 ev%d = %s[%d];' % (q, rv, 2 + nom + q))
+        elif pipe_e(la, lb):
             for q in range(nvec):
                 lines.append(J + 'const float4 ev%d = %s.e%d;' % (q, rv, q))
         else:
@@ -438,22 +447,29 @@ def gen_prim_body(la, lb, diag, rv, J, lines, far=True):
     lines.append(J + '}')
 
 
-def gen_class(la, lb, diag, far):
+def gen_class(la, lb, diag, far, stage=False):
     nb = 2 * lb + 1
     nca = (la + 1) * (la + 2) // 2
     ncb = (lb + 1) * (lb + 2) // 2
     ents = e_entries(la, lb)
     lines = []
     I = '    '
-    lines.append('template<int PTS> struct CosxTask<%d, %d, %s, PTS, %s> {'
-                 % (la, lb, 'true' if diag else 'false', 'true' if far else 'false'))
+    lines.append('template<int PTS> struct CosxTask<%d, %d, %s, PTS, %s, %s> {'
+                 % (la, lb, 'true' if diag else 'false', 'true' if far else 'false',
+                    'true' if stage else 'false'))
     lines.append('static __device__ __forceinline__ void run(')
     lines.append('    const CosxArgs& A, float* const* Gp, const int ld, const int gb0,')
-    lines.append('    const int pp0, const int npp, const int nxt, const bool* ok,')
+    if stage:
+        lines.append('    const float4* __restrict__ rp, const int npp, const bool* ok,')
+    else:
+        lines.append('    const int pp0, const int npp, const int nxt, const bool* ok,')
     lines.append('    const float* gxh, const float* gyh, const float* gzh,')
     lines.append('    const float* gxl, const float* gyl, const float* gzl,')
     lines.append('    const float4* __restrict__ stab, const float* f0,')
-    lines.append('    const float* fb, float* Xa, CosxRec<%d, %d>& rec)' % (la, lb))
+    if stage:
+        lines.append('    const float* fb, float* Xa)')
+    else:
+        lines.append('    const float* fb, float* Xa, CosxRec<%d, %d>& rec)' % (la, lb))
     lines.append('{')
     lines.append(I + 'float f0v[PTS][%d], Yv[PTS][%d];' % (nca, ncb))
     if not diag:
@@ -479,26 +495,36 @@ def gen_class(la, lb, diag, far):
     for c in range(ncb):
         lines.append(J + 'Yv[p][%d] = 0.0f;' % c)
     lines.append(I + '}')
-    lines.append(I + 'const int pend = pp0 + npp;')
-    # two register sets for the primitive-pair record (rec, rb) used in
-    # turn: while one pair computes, the next one loads into the other set
-    lines.append(I + 'CosxRec<%d, %d> rb;' % (la, lb))
-    lines.append(I + 'int m = pp0;')
-    lines.append(I + '#pragma unroll 1')
-    lines.append(I + 'while (true) {')
-    lines.append(J + 'cosx_rec_load<%s>(A, m + 1 < pend ? m + 1 : nxt, rb);'
-                 % ('true' if far else 'false'))
-    lines.append(J + '{')
-    gen_prim_body(la, lb, diag, 'rec', J + I, lines, far)
-    lines.append(J + '}')
-    lines.append(J + 'if (++m == pend) { rec = rb; break; }')
-    lines.append(J + 'cosx_rec_load<%s>(A, m + 1 < pend ? m + 1 : nxt, rec);'
-                 % ('true' if far else 'false'))
-    lines.append(J + '{')
-    gen_prim_body(la, lb, diag, 'rb', J + I, lines, far)
-    lines.append(J + '}')
-    lines.append(J + 'if (++m == pend) break;')
-    lines.append(I + '}')
+    if stage:
+        # records staged in shared memory by the caller: one base address
+        lines.append(I + '#pragma unroll 1')
+        lines.append(I + 'for (int m = 0; m < npp; ++m) {')
+        lines.append(J + 'const float4* __restrict__ q = rp + m * %d;' % rec_stride(la, lb))
+        lines.append(J + '{')
+        gen_prim_body(la, lb, diag, 'q', J + I, lines, far, stage=True)
+        lines.append(J + '}')
+        lines.append(I + '}')
+    else:
+        lines.append(I + 'const int pend = pp0 + npp;')
+        # two register sets for the primitive-pair record (rec, rb) used in
+        # turn: while one pair computes, the next one loads into the other set
+        lines.append(I + 'CosxRec<%d, %d> rb;' % (la, lb))
+        lines.append(I + 'int m = pp0;')
+        lines.append(I + '#pragma unroll 1')
+        lines.append(I + 'while (true) {')
+        lines.append(J + 'cosx_rec_load<%s>(A, m + 1 < pend ? m + 1 : nxt, rb);'
+                     % ('true' if far else 'false'))
+        lines.append(J + '{')
+        gen_prim_body(la, lb, diag, 'rec', J + I, lines, far)
+        lines.append(J + '}')
+        lines.append(J + 'if (++m == pend) { rec = rb; break; }')
+        lines.append(J + 'cosx_rec_load<%s>(A, m + 1 < pend ? m + 1 : nxt, rec);'
+                     % ('true' if far else 'false'))
+        lines.append(J + '{')
+        gen_prim_body(la, lb, diag, 'rb', J + I, lines, far)
+        lines.append(J + '}')
+        lines.append(J + 'if (++m == pend) break;')
+        lines.append(I + '}')
     lines.append(I + '#pragma unroll')
     lines.append(I + 'for (int p = 0; p < PTS; ++p) {')
     if diag:
@@ -540,11 +566,12 @@ def source():
         out.append('')
     for (la, lb) in classes():
         for far in (False, True):
-            out.append(gen_class(la, lb, False, far))
-            out.append('')
-            if la == lb:
-                out.append(gen_class(la, lb, True, far))
+            for stage in (False, True):
+                out.append(gen_class(la, lb, False, far, stage))
                 out.append('')
+                if la == lb:
+                    out.append(gen_class(la, lb, True, far, stage))
+                    out.append('')
     # E strides table for the host
     out.append('#define WB_E_STRIDES {%s}' % ', '.join(
         str(e_stride(la, lb)) for (la, lb) in classes()))

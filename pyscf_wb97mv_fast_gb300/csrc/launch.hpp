@@ -8,11 +8,15 @@
 namespace wb {
 
 // per-class fused screen + G kernels (cosx_kernels_*.cu); far selects the
-// variant with the far-field R000 form (omega = 0, where T >= 36 is common)
+// variant with the far-field R000 form (omega = 0, where T >= 36 is common);
+// stage_smem > 0 selects the variant that stages each task's primitive-pair
+// records in shared memory (stage_smem bytes of dynamic smem per CTA)
 cudaError_t launch_cosx_class_range(int cls, const CosxArgs& a, int pb,
-                                    int pe, int grid, cudaStream_t s, bool far);
-// max resident CTAs per SM of a class kernel (128 threads each)
-int cosx_class_blocks_per_sm(int cls, bool far);
+                                    int pe, int grid, cudaStream_t s, bool far,
+                                    size_t stage_smem);
+// max resident CTAs per SM of a class kernel (128 threads each); 0 if the
+// kernel cannot run with that much dynamic shared memory
+int cosx_class_blocks_per_sm(int cls, bool far, size_t stage_smem);
 
 struct AoArgs {
     const double* coords;       // (npts, 3) molecule frame
