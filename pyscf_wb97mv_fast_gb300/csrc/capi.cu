@@ -710,9 +710,10 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
             ntasks += (ldt / 32) * (int64_t)h->hp.npairs;
             if (oz_k) {
                 if ((st = phase_to(5)) != WB_OK) return st;
+                // the X slices of this tile serve every omega
                 const int r = wb::ozaki_k_gemm(h->cublas, X, G32, w, nao, ldt, nt,
                                                i0 == 0 ? 0 : 1, Kj,
-                                               at<void>(workspace, L.oz), s);
+                                               at<void>(workspace, L.oz), s, j > 0);
                 if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
                                    "ozaki K GEMM failed, code " + std::to_string(r));
                 launches += 2 + wb::kOzSlices;

@@ -21,9 +21,10 @@ template<int LA, int LB> struct CosxRec;
 // (PTS x NCA) carried across the run of tasks with the same A.  rec holds
 // pair pp0's record on entry and pair nxt's on exit (the next task's first
 // pair).  The DIAG form (B = A) adds its ket accumulators to Xa instead of
-// writing G_B.  FAR selects the R000 form: the far-field expression under
-// warp-uniform branches (T >= 36 common: omega = 0) or boys_fp32 per point
-// (long-range omegas).  STAGE: the task's primitive-pair records were
+// writing G_B.  FAR selects the order of the warp-uniform R000 branches:
+// all-far first (T >= 36 common: omega = 0) or all-near first (long-range
+// omegas, where theta p <= omega^2 keeps T small); mixed warps choose per
+// point between the far-field form and the Boys Taylor form.  STAGE: the task's primitive-pair records were
 // copied to shared memory (rp, stride per class) instead of being carried
 // in registers one pair ahead.  Specialised per (LA, LB, DIAG, FAR,
 // STAGE) with run() as the body.

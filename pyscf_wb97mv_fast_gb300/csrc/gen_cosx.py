@@ -282,9 +282,7 @@ def rec_stride(la, lb):
 def gen_rec(la, lb):
     """Per-class record of one primitive pair (geo, omega and, for small
     classes, E) and its loader: the task loop keeps the next pair's record
-    in flight while it computes the current one.  m is class-local; the
-    far-field float4 (last omega float4) is loaded by the FAR variant
-    only."""
+    in flight while it computes the current one.  m is class-local."""
     nom = n_om(la, lb)
     nvec = e_stride(la, lb) // 4 if pipe_e(la, lb) else 0
     mem = ['g0', 'g1'] + ['o%d' % q for q in range(nom)] + \
@@ -302,7 +300,7 @@ def gen_rec(la, lb):
     lines.append(I + 'r.g1 = __ldg(q + 1);')
     for k in range(nom - 1):
         lines.append(I + 'r.o%d = __ldg(q + %d);' % (k, 2 + k))
-    lines.append(I + 'if (FAR) r.o%d = __ldg(q + %d);' % (nom - 1, 1 + nom))
+    lines.append(I + 'r.o%d = __ldg(q + %d);' % (nom - 1, 1 + nom))
     for k in range(nvec):
         lines.append(I + 'r.e%d = __ldg(q + %d);' % (k, 2 + nom + k))
     lines.append('}')
@@ -356,25 +354,47 @@ def gen_prim_body(la, lb, diag, rv, J, lines, far=True, stage=False):
                 if nm is not None:
                     lines.append(J + 'const float %s = ev%d.%s;' % (nm, q, comp[c]))
     if not far:
-        # Boys by boys_fp32 per point (Taylor / asymptotic / zero branches):
-        # the form for long-range omegas, where T >= 36 is rare
-        lines.append(J + 'float dxv[PTS], dyv[PTS], dzv[PTS], R0[PTS][%d];' % (L + 1))
+        # long-range omegas: T = theta p r^2 stays below 36 almost always,
+        # so one warp vote selects the branch-free Taylor form for every
+        # point; mixed warps take the far-field form where T >= 36
+        of = 'o%d' % (nom - 1)
+        lines.append(J + 'float dxv[PTS], dyv[PTS], dzv[PTS], r2v[PTS], R0[PTS][%d];' % (L + 1))
+        lines.append(J + 'bool allnear = true;')
         lines.append(J + '#pragma unroll')
         lines.append(J + 'for (int p = 0; p < PTS; ++p) {')
         lines.append(J + '    dxv[p] = (ph.x - gxh[p]) + (pl.x - gxl[p]);')
         lines.append(J + '    dyv[p] = (ph.y - gyh[p]) + (pl.y - gyl[p]);')
         lines.append(J + '    dzv[p] = (ph.z - gzh[p]) + (pl.z - gzl[p]);')
-        lines.append(J + '    const float r2 = fmaf(dxv[p], dxv[p], fmaf(dyv[p], dyv[p], dzv[p] * dzv[p]));')
-        lines.append(J + '    const float T = fmaf(o0.x, r2, o0.y * r2);')
-        lines.append(J + '    float Fb[%d];' % (L + 1))
-        lines.append(J + '    boys_fp32<%d>(T, Fb, stab);' % L)
-        for n in range(L + 1):
-            fh = 2 + 2 * n
-            fl = fh + 1
-            ch = 'o%d.%s' % (fh // 4, comp[fh % 4])
-            cl = 'o%d.%s' % (fl // 4, comp[fl % 4])
-            lines.append(J + '    R0[p][%d] = fmaf(%s, Fb[%d], %s * Fb[%d]);'
-                         % (n, ch, n, cl, n))
+        lines.append(J + '    r2v[p] = fmaf(dxv[p], dxv[p], fmaf(dyv[p], dyv[p], dzv[p] * dzv[p]));')
+        lines.append(J + '    allnear = allnear && r2v[p] < %s.z;' % of)
+        lines.append(J + '}')
+
+        def near_n(ind, p):
+            lines.append(ind + 'const float T = fmaf(o0.x, r2v[%s], o0.y * r2v[%s]);' % (p, p))
+            lines.append(ind + 'float Fb[%d];' % (L + 1))
+            lines.append(ind + 'boys_taylor<%d>(T, Fb, stab);' % L)
+            for n in range(L + 1):
+                fh = 2 + 2 * n
+                fl = fh + 1
+                ch = 'o%d.%s' % (fh // 4, comp[fh % 4])
+                cl = 'o%d.%s' % (fl // 4, comp[fl % 4])
+                lines.append(ind + 'R0[%s][%d] = fmaf(%s, Fb[%d], %s * Fb[%d]);'
+                             % (p, n, ch, n, cl, n))
+
+        lines.append(J + 'if (__all_sync(0xffffffffu, allnear)) {')
+        lines.append(J + '    #pragma unroll')
+        lines.append(J + '    for (int p = 0; p < PTS; ++p) {')
+        near_n(J + '        ', 'p')
+        lines.append(J + '    }')
+        lines.append(J + '} else {')
+        lines.append(J + '    #pragma unroll')
+        lines.append(J + '    for (int p = 0; p < PTS; ++p) {')
+        lines.append(J + '        if (r2v[p] >= %s.z) {' % of)
+        lines.append(J + '            far_r000<%d>(r2v[p], %s.x, %s.y, R0[p]);' % (L, of, of))
+        lines.append(J + '        } else {')
+        near_n(J + '            ', 'p')
+        lines.append(J + '        }')
+        lines.append(J + '    }')
         lines.append(J + '}')
     else:
         of = 'o%d' % (nom - 1)          # far-field float4: K0 hi, K0 lo, thr

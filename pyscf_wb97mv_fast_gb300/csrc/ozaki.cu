@@ -275,7 +275,9 @@ __global__ void f_combine_kernel(const float* __restrict__ C, int nao,
 //   B: column nu = [slice S-1 | ... | slice 0]          (descending)
 // chunk stride S KC nao.  One CTA of 256 threads per (chunk, column).
 // ---------------------------------------------------------------------------
-template<int S, int KC>
+// DOX = false: the X slices and exponents of this tile are already in A /
+// ex (an earlier omega of the same tile); only w o G is sliced
+template<int S, int KC, bool DOX>
 __global__ void __launch_bounds__(KC / 8)
 k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
                const double* __restrict__ w, int nao, int64_t ld,
@@ -296,8 +298,13 @@ k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
         const float gv[8] = {ga.x, ga.y, ga.z, ga.w, gb.x, gb.y, gb.z, gb.w};
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const double2 a = __ldg(xp + u), b = __ldg(wp + u);
-            xv[2 * u] = a.x; xv[2 * u + 1] = a.y;
+            const double2 b = __ldg(wp + u);
+            if (DOX) {
+                const double2 a = __ldg(xp + u);
+                xv[2 * u] = a.x; xv[2 * u + 1] = a.y;
+            } else {
+                xv[2 * u] = 0.0; xv[2 * u + 1] = 0.0;
+            }
             wv[2 * u] = b.x * (double)gv[2 * u];
             wv[2 * u + 1] = b.y * (double)gv[2 * u + 1];
         }
@@ -308,7 +315,7 @@ k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
             xv[u] = 0.0;
             wv[u] = 0.0;
             if (g < npts) {
-                xv[u] = X[(int64_t)col * ld + g];
+                if (DOX) xv[u] = X[(int64_t)col * ld + g];
                 wv[u] = w[g] * (double)G[(int64_t)col * ld + g];
             }
         }
@@ -340,14 +347,14 @@ k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
     }
     const int e1 = exp_of_bits(mx), e2 = exp_of_bits(mw);
     if (threadIdx.x == 0) {
-        ex[(int64_t)c * nao + col] = e1;
+        if (DOX) ex[(int64_t)c * nao + col] = e1;
         ew[(int64_t)c * nao + col] = e2;
     }
     const int64_t colbase = (int64_t)c * S * KC * nao + (int64_t)col * S * KC;
     float d1[8][S], d2[8][S];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-        digits<S>(xv[u], e1, d1[u]);
+        if (DOX) digits<S>(xv[u], e1, d1[u]);
         digits<S>(wv[u], e2, d2[u]);
     }
 #pragma unroll
@@ -355,11 +362,12 @@ k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
         __nv_bfloat162 pa[4], pb[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            pa[u] = __floats2bfloat162_rn(d1[2 * u][i], d1[2 * u + 1][i]);
+            if (DOX) pa[u] = __floats2bfloat162_rn(d1[2 * u][i], d1[2 * u + 1][i]);
             pb[u] = __floats2bfloat162_rn(d2[2 * u][i], d2[2 * u + 1][i]);
         }
-        *reinterpret_cast<uint4*>(A + colbase + (int64_t)i * KC + k0) =
-            *reinterpret_cast<const uint4*>(pa);
+        if (DOX)
+            *reinterpret_cast<uint4*>(A + colbase + (int64_t)i * KC + k0) =
+                *reinterpret_cast<const uint4*>(pa);
         *reinterpret_cast<uint4*>(B + colbase + (int64_t)(S - 1 - i) * KC + k0) =
             *reinterpret_cast<const uint4*>(pb);
     }
@@ -460,7 +468,8 @@ int ozaki_f_gemm(cublasHandle_t hb, const double* X, const double* QD,
 
 int ozaki_k_gemm(cublasHandle_t hb, const double* X, const float* G,
                  const double* w, int nao, int64_t ld, int64_t npts,
-                 int accumulate, double* K, void* ws, cudaStream_t s) {
+                 int accumulate, double* K, void* ws, cudaStream_t s,
+                 bool x_sliced) {
     constexpr int S = kOzSlices, KC = kOzKc;
     const int nchunk = (int)((ld + KC - 1) / KC);
     char* p = static_cast<char*>(ws);
@@ -473,8 +482,12 @@ int ozaki_k_gemm(cublasHandle_t hb, const double* X, const float* G,
     p += al(sizeof(__nv_bfloat16) * slab);
     float* C = reinterpret_cast<float*>(p);
     dim3 grid(nchunk, nao);
-    k_slice_kernel<S, KC><<<grid, KC / 8, 0, s>>>(X, G, w, nao, ld, npts, ex,
-                                                  ew, A, B);
+    if (x_sliced)
+        k_slice_kernel<S, KC, false><<<grid, KC / 8, 0, s>>>(X, G, w, nao, ld, npts,
+                                                            ex, ew, A, B);
+    else
+        k_slice_kernel<S, KC, true><<<grid, KC / 8, 0, s>>>(X, G, w, nao, ld, npts,
+                                                           ex, ew, A, B);
     OZ_CUDA(cudaGetLastError());
     const float one = 1.0f, zero = 0.0f;
     const long long stride = (long long)S * KC * nao;

@@ -25,8 +25,12 @@ int ozaki_f_gemm(cublasHandle_t hb, const double* X, const double* QD,
                  int nao, int64_t ld, float* F, void* ws, cudaStream_t s);
 
 // K (nao, nao) row-major (+)= X^T (w o G) over the npts valid points.
+// x_sliced: ws already holds the slices of this X (an earlier call on the
+// same X and workspace, e.g. another omega of the same tile), which are
+// reused.
 int ozaki_k_gemm(cublasHandle_t hb, const double* X, const float* G,
                  const double* w, int nao, int64_t ld, int64_t npts,
-                 int accumulate, double* K, void* ws, cudaStream_t s);
+                 int accumulate, double* K, void* ws, cudaStream_t s,
+                 bool x_sliced = false);
 
 }  // namespace wb
