@@ -94,6 +94,40 @@ cudaError_t launch_pack_records(const RecPack& P, int npp, const float4* geo,
     return cudaGetLastError();
 }
 
+__global__ void pack_records2_kernel(const RecPack P, int npp,
+                                     const float4* __restrict__ geo,
+                                     const float4* __restrict__ oma,
+                                     const float4* __restrict__ omb,
+                                     const float4* __restrict__ E,
+                                     float4* __restrict__ rec) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= npp) return;
+    int c = 0;
+    while (c < 9 && m >= P.pp_end[c]) ++c;
+    if (m < P.pp_begin[c] || m >= P.pp_end[c]) return;
+    const int ml = m - P.pp_begin[c];
+    const int nom = P.nom[c];
+    float4* r = rec + P.rec_off[c] + (long long)ml * P.stride[c];
+    r[0] = geo[2 * (long long)m];
+    r[1] = geo[2 * (long long)m + 1];
+    const float4* om[2] = {oma, omb};
+    for (int w = 0; w < 2; ++w) {
+        for (int q = 0; q + 1 < nom; ++q) r[2 + w * nom + q] = om[w][5 * (long long)m + q];
+        r[1 + (w + 1) * nom] = om[w][5 * (long long)m + 4];
+    }
+    const float4* e = E + P.e_off[c] + (long long)ml * P.ne[c];
+    for (int q = 0; q < P.ne[c]; ++q) r[2 + 2 * nom + q] = e[q];
+}
+
+cudaError_t launch_pack_records2(const RecPack& P, int npp, const float4* geo,
+                                 const float4* om_a, const float4* om_b,
+                                 const float4* E, float4* rec, cudaStream_t s) {
+    if (npp <= 0) return cudaSuccess;
+    pack_records2_kernel<<<(npp + 127) / 128, 128, 0, s>>>(P, npp, geo, om_a, om_b,
+                                                         E, rec);
+    return cudaGetLastError();
+}
+
 // -- FP64 (npts, 3) -> FP32 SoA hi / lo, padded with zeros to ld ----------
 __global__ void grid_prep_kernel(const double* __restrict__ c, int64_t npts,
                                  int64_t ld, float* __restrict__ hi,

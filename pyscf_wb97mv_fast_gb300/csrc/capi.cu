@@ -58,6 +58,8 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kStageMaxBytes = 96 * 1024;
 // default staged classes: (0,0) (1,0) (1,1) (2,1)
 constexpr long long kStageClasses = 0x1110100000LL;
+// default classes with a dual-omega kernel: (0,0) (1,0) (2,0) (2,1)
+constexpr long long kDualClasses = 0x1101100000LL;
 inline int64_t round32(int64_t x) { return (x + 31) / 32 * 32; }
 
 // Boys table per device, built once per process
@@ -138,6 +140,13 @@ struct wb_cosx {
     int recmax[wb::NCLASS] = {0};            // float4 of the largest task record
     size_t stage_smem[wb::NCLASS] = {0};     // dynamic smem of the staged variant
                                              // (0: register-prefetch variant)
+    // dual-omega variant (two omegas per launch): record size, dynamic smem,
+    // occupancy; usable when every class with pairs supports it
+    int recmax2[wb::NCLASS] = {0};
+    size_t stage_smem2[wb::NCLASS] = {0};
+    int blocks_per_sm2[wb::NCLASS] = {0};
+    bool dual_cls[wb::NCLASS] = {false};   // class runs its dual-omega kernel
+    bool dual_ok = false;                  // two-omega passes are on
     // class launches run concurrently on their own streams (fork / join by
     // events on the caller's stream), largest estimated work first
     cudaStream_t cstream[wb::NCLASS] = {};
@@ -150,10 +159,11 @@ struct wb_cosx {
 namespace {
 
 struct WsLayout {
-    size_t om = 0, rec = 0, gh = 0, gl = 0, counters = 0, work = 0;
+    size_t om = 0, rec = 0, om2 = 0, rec2 = 0, recb = 0, gh = 0, gl = 0;
+    size_t counters = 0, work = 0;
     size_t subcr[3] = {0, 0, 0}, msh[3] = {0, 0, 0};  // 32/64/128-point blocks
-    size_t gcls = 0;
-    size_t X = 0, F64 = 0, F32 = 0, G32 = 0, oz = 0, total = 0;
+    size_t gcls = 0, gcls2 = 0;
+    size_t X = 0, F64 = 0, F32 = 0, G32 = 0, G32b = 0, oz = 0, total = 0;
 };
 
 WsLayout ws_layout(const wb_cosx* h, int64_t ldt, bool full) {
@@ -166,9 +176,14 @@ WsLayout ws_layout(const wb_cosx* h, int64_t ldt, bool full) {
     };
     const int nao = h->hp.nao;
     L.counters = take(sizeof(unsigned long long) * 3 * wb::NCLASS);
-    L.work = take(sizeof(int) * wb::NCLASS);
+    L.work = take(sizeof(int) * 2 * wb::NCLASS);     // per class, per omega slot
     L.om = take(sizeof(float) * wb::OMEGA_REC * (size_t)std::max(h->hp.npp, 1));
     L.rec = take(sizeof(float4) * (size_t)std::max<int64_t>(h->hp.nrec, 1));
+    // second omega of a dual-omega build: its omega record, the dual
+    // records and its class buffers (and G below)
+    L.om2 = take(sizeof(float) * wb::OMEGA_REC * (size_t)std::max(h->hp.npp, 1));
+    L.rec2 = take(sizeof(float4) * (size_t)std::max<int64_t>(h->hp.nrec2, 1));
+    L.recb = take(sizeof(float4) * (size_t)std::max<int64_t>(h->hp.nrec, 1));
     L.gh = take(sizeof(float) * 3 * (size_t)ldt);
     L.gl = take(sizeof(float) * 3 * (size_t)ldt);
     for (int b = 0; b < 3; ++b) {
@@ -178,10 +193,12 @@ WsLayout ws_layout(const wb_cosx* h, int64_t ldt, bool full) {
         L.msh[b] = take(sizeof(float) * (size_t)nblk * std::max(h->hp.nvshell, 1));
     }
     L.gcls = take(sizeof(float) * (size_t)std::max<int64_t>(h->hp.ncrow, 1) * ldt);
+    L.gcls2 = take(sizeof(float) * (size_t)std::max<int64_t>(h->hp.ncrow, 1) * ldt);
     if (full) {
         L.X = take(sizeof(double) * (size_t)nao * ldt);
         L.F32 = take(sizeof(float) * (size_t)nao * ldt);
         L.G32 = take(sizeof(float) * (size_t)nao * ldt);
+        L.G32b = take(sizeof(float) * (size_t)nao * ldt);
         // scratch shared by the FP64 DGEMM path (F64 / w o G) and the
         // bf16 Ozaki path (slices, level outputs): never live together
         const size_t dg = sizeof(double) * (size_t)nao * ldt;
@@ -217,6 +234,9 @@ wb::CosxArgs make_args(const wb_cosx* h, void* ws, const WsLayout& L,
         a.pp_begin[c] = h->hp.cls[c].pp_begin;
         a.rec[c] = at<float4>(ws, L.rec) + h->hp.rec_off[c];
         a.recmax[c] = h->recmax[c];
+        a.rec2[c] = at<float4>(ws, L.rec2) + h->hp.rec_off2[c];
+        a.recmax2[c] = h->recmax2[c];
+        a.Gcls2[c] = at<float>(ws, L.gcls2) + h->hp.crow_base[c] * ldt;
     }
     a.hdr = h->hdr;
     a.khdr = h->khdr;
@@ -261,6 +281,46 @@ int prepare_omega(wb_cosx* h, double omega, void* ws, const WsLayout& L,
     }
     WB_CUDA(wb::launch_pack_records(P, h->hp.npp, h->geo, at<float4>(ws, L.om),
                                     h->E, at<float4>(ws, L.rec), s));
+    return WB_OK;
+}
+
+// the same for two omegas at once: both omega records and the dual-layout
+// class records (slot a first)
+int prepare_omega_dual(wb_cosx* h, double omega_a, double omega_b, void* ws,
+                       const WsLayout& L, cudaStream_t s) {
+    WB_CUDA(wb::launch_omega(h->hp.npp, h->p, h->pref, omega_a,
+                             at<float4>(ws, L.om), s));
+    WB_CUDA(wb::launch_omega(h->hp.npp, h->p, h->pref, omega_b,
+                             at<float4>(ws, L.om2), s));
+    wb::RecPack P;
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        P.pp_begin[c] = h->hp.cls[c].pp_begin;
+        P.pp_end[c] = h->hp.cls[c].pp_end;
+        P.stride[c] = wb::kRecStride2[c];
+        P.nom[c] = wb::kRecNom[c];
+        P.ne[c] = wb::kRecNe[c];
+        P.rec_off[c] = h->hp.rec_off2[c];
+        P.e_off[c] = h->hp.cls[c].e_base / 4;
+    }
+    WB_CUDA(wb::launch_pack_records2(P, h->hp.npp, h->geo, at<float4>(ws, L.om),
+                                     at<float4>(ws, L.om2), h->E,
+                                     at<float4>(ws, L.rec2), s));
+    // single-omega records of both slots for the classes without a dual
+    // kernel
+    bool singles = false;
+    for (int c = 0; c < wb::NCLASS; ++c)
+        singles = singles || (h->hp.cls[c].pair_end > h->hp.cls[c].pair_begin &&
+                              !h->dual_cls[c]);
+    if (singles) {
+        for (int c = 0; c < wb::NCLASS; ++c) {
+            P.stride[c] = wb::kRecStride[c];
+            P.rec_off[c] = h->hp.rec_off[c];
+        }
+        WB_CUDA(wb::launch_pack_records(P, h->hp.npp, h->geo, at<float4>(ws, L.om),
+                                        h->E, at<float4>(ws, L.rec), s));
+        WB_CUDA(wb::launch_pack_records(P, h->hp.npp, h->geo, at<float4>(ws, L.om2),
+                                        h->E, at<float4>(ws, L.recb), s));
+    }
     return WB_OK;
 }
 
@@ -314,6 +374,62 @@ int run_g_classes(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
     }
     WB_CUDA(wb::launch_gsum(at<float>(ws, L.gcls), h->gsrc, h->hp.nao, ldt, G, s));
     *launches += 1;
+    return WB_OK;
+}
+
+// the class launches of one tile for two omegas at once (after tile_prep
+// and prepare_omega_dual): slot a fills the class buffers and G_a, slot b
+// the second buffers and G_b
+int run_g_classes_dual(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
+                       float* Ga, float* Gb, double omega_a, double omega_b,
+                       double tile_tol, void* ws, const WsLayout& L,
+                       cudaStream_t s, int* launches) {
+    const wb::CosxArgs a = make_args(h, ws, L, ldt, npts_t, F, tile_tol);
+    // slot b of the single-omega kernels: its records, buffers, counters
+    wb::CosxArgs b = a;
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        b.rec[c] = at<float4>(ws, L.recb) + h->hp.rec_off[c];
+        b.Gcls[c] = a.Gcls2[c];
+    }
+    b.work = a.work + wb::NCLASS;
+    const size_t gbytes = sizeof(float) * (size_t)h->hp.ncrow * ldt;
+    WB_CUDA(cudaMemsetAsync(at<float>(ws, L.gcls), 0, gbytes, s));
+    WB_CUDA(cudaMemsetAsync(at<float>(ws, L.gcls2), 0, gbytes, s));
+    WB_CUDA(cudaMemsetAsync(at<int>(ws, L.work), 0, sizeof(int) * 2 * wb::NCLASS, s));
+    WB_CUDA(cudaEventRecord(h->fork, s));
+    for (int i = 0; i < wb::NCLASS; ++i) {
+        const int c = h->corder[i];
+        const wb::ClassRange& r = h->hp.cls[c];
+        if (r.pair_end <= r.pair_begin) continue;
+        const int lvl = h->pts[c] == 4 ? 2 : h->pts[c] - 1;
+        const int want = (a.nblk[lvl] + 3) / 4;
+        WB_CUDA(cudaStreamWaitEvent(h->cstream[c], h->fork, 0));
+        if (h->dual_cls[c]) {
+            const int cap = std::max(1, h->blocks_per_sm2[c]) * h->nsm;
+            WB_CUDA(wb::launch_cosx_class_range(c, a, r.pair_begin, r.pair_end,
+                                                std::max(1, std::min(want, cap)),
+                                                h->cstream[c], false,
+                                                h->stage_smem2[c], true));
+            *launches += 1;
+        } else {
+            const double om[2] = {omega_a, omega_b};
+            for (int w = 0; w < 2; ++w) {
+                const bool far = om[w] == 0.0;
+                const int cap = std::max(1, h->blocks_per_sm[c][far ? 1 : 0]) * h->nsm;
+                WB_CUDA(wb::launch_cosx_class_range(c, w ? b : a, r.pair_begin,
+                                                    r.pair_end,
+                                                    std::max(1, std::min(want, cap)),
+                                                    h->cstream[c], far,
+                                                    h->stage_smem[c]));
+                *launches += 1;
+            }
+        }
+        WB_CUDA(cudaEventRecord(h->cdone[c], h->cstream[c]));
+        WB_CUDA(cudaStreamWaitEvent(s, h->cdone[c], 0));
+    }
+    WB_CUDA(wb::launch_gsum(at<float>(ws, L.gcls), h->gsrc, h->hp.nao, ldt, Ga, s));
+    WB_CUDA(wb::launch_gsum(at<float>(ws, L.gcls2), h->gsrc, h->hp.nao, ldt, Gb, s));
+    *launches += 2;
     return WB_OK;
 }
 
@@ -511,7 +627,34 @@ int wb_cosx_create(const wb_basis* basis, const double origin[3],
                 n[f] = wb::cosx_class_blocks_per_sm(c, f == 1, 0);
         }
         for (int f = 0; f < 2; ++f) h->blocks_per_sm[c][f] = std::max(n[f], 1);
+        // dual-omega variant: always staged, dual record layout
+        int rm2 = 0;
+        for (int k = hp.cls[c].pair_begin; k < hp.cls[c].pair_end; ++k)
+            rm2 = std::max(rm2, (hp.hdr[4 * k + 3] & 0xffff) * wb::kRecStride2[c]);
+        h->recmax2[c] = rm2;
+        const size_t smem2 = (size_t)(128 / 32) * 2 * rm2 * sizeof(float4);
+        if (rm2 > 0 && smem2 <= kStageMaxBytes) {
+            h->stage_smem2[c] = smem2;
+            h->blocks_per_sm2[c] = wb::cosx_class_blocks_per_sm(c, false, smem2, true);
+        }
         h->pts[c] = wb::cosx_class_pts(c);
+    }
+    {
+        // classes that run the dual-omega kernel in a two-omega pass (one
+        // hex digit per class, measured per class on the water27 workload:
+        // fused wins where the shared per-task work dominates, loses where
+        // two sets of accumulators spill); the others run their single-omega
+        // kernel twice in the same pass.  WB_COSX_DUAL overrides the digits
+        // (0 turns two-omega passes off).
+        long long mask = kDualClasses;
+        h->dual_ok = true;
+        if (const char* env = std::getenv("WB_COSX_DUAL")) {
+            mask = std::strtoll(env, nullptr, 16);
+            h->dual_ok = mask != 0;
+        }
+        for (int c = 0; c < wb::NCLASS; ++c)
+            h->dual_cls[c] = ((mask >> (4 * (wb::NCLASS - 1 - c))) & 15) != 0 &&
+                             h->blocks_per_sm2[c] >= 1;
     }
     {   // launch order: model flops of all pairs of a class, descending
         double work[wb::NCLASS] = {0};
@@ -639,6 +782,7 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
     double* F64 = at<double>(workspace, L.F64);
     float* F32 = at<float>(workspace, L.F32);
     float* G32 = at<float>(workspace, L.G32);
+    float* G32b = at<float>(workspace, L.G32b);
     int64_t ntasks = 0;
     const double one = 1.0, zero = 0.0;
     const bool prof = (flags & WB_K_PROFILE) && stats;
@@ -700,27 +844,25 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
         if ((st = phase_to(3)) != WB_OK) return st;
         if ((st = tile_prep(h, c, w, nt, ldt, F32, workspace, L, s, &launches)) != WB_OK)
             return st;
-        for (int j = 0; j < nomega; ++j) {
+        // K += X^T (w o G) of omega j from the G in Gsrc; the X slices of
+        // this tile serve every omega after the first
+        bool x_sliced = false;
+        auto k_gemm = [&](int j, const float* Gsrc) -> int {
             double* Kj = k_out + kk * j;
-            if ((st = prepare_omega(h, omegas[j], workspace, L, s)) != WB_OK) return st;
-            launches += 2;
-            if ((st = run_g_classes(h, nt, ldt, F32, G32, omegas[j], tile_tol,
-                                    workspace, L, s, &launches)) != WB_OK)
-                return st;
-            ntasks += (ldt / 32) * (int64_t)h->hp.npairs;
+            int rs;
             if (oz_k) {
-                if ((st = phase_to(5)) != WB_OK) return st;
-                // the X slices of this tile serve every omega
-                const int r = wb::ozaki_k_gemm(h->cublas, X, G32, w, nao, ldt, nt,
+                if ((rs = phase_to(5)) != WB_OK) return rs;
+                const int r = wb::ozaki_k_gemm(h->cublas, X, Gsrc, w, nao, ldt, nt,
                                                i0 == 0 ? 0 : 1, Kj,
-                                               at<void>(workspace, L.oz), s, j > 0);
+                                               at<void>(workspace, L.oz), s, x_sliced);
                 if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
                                    "ozaki K GEMM failed, code " + std::to_string(r));
+                x_sliced = true;
                 launches += 2 + wb::kOzSlices;
             } else {
-                if ((st = phase_to(4)) != WB_OK) return st;
-                WB_CUDA(wb::launch_weight_g(G32, w, nt, ldt, nao, F64, s));
-                if ((st = phase_to(5)) != WB_OK) return st;
+                if ((rs = phase_to(4)) != WB_OK) return rs;
+                WB_CUDA(wb::launch_weight_g(Gsrc, w, nt, ldt, nao, F64, s));
+                if ((rs = phase_to(5)) != WB_OK) return rs;
                 // K(mu, nu) += sum_g X(g, mu) WG(g, nu); written row-major
                 const double* beta = i0 == 0 ? &zero : &one;
                 WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nao, nao,
@@ -728,7 +870,36 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
                                       beta, Kj, nao));
                 launches += 2;
             }
-            if ((st = phase_to(3)) != WB_OK) return st;
+            return phase_to(3);
+        };
+        for (int j = 0; j < nomega;) {
+            if (h->dual_ok && j + 1 < nomega) {
+                // two omegas in one pass of the class kernels; slot a (the
+                // all-far-first branch order) takes the smaller omega
+                int ja = j, jb = j + 1;
+                if (omegas[jb] < omegas[ja]) std::swap(ja, jb);
+                if ((st = prepare_omega_dual(h, omegas[ja], omegas[jb], workspace, L,
+                                             s)) != WB_OK)
+                    return st;
+                launches += 3;
+                if ((st = run_g_classes_dual(h, nt, ldt, F32, G32, G32b, omegas[ja],
+                                             omegas[jb], tile_tol, workspace, L, s,
+                                             &launches)) != WB_OK)
+                    return st;
+                ntasks += 2 * (ldt / 32) * (int64_t)h->hp.npairs;
+                if ((st = k_gemm(ja, G32)) != WB_OK) return st;
+                if ((st = k_gemm(jb, G32b)) != WB_OK) return st;
+                j += 2;
+                continue;
+            }
+            if ((st = prepare_omega(h, omegas[j], workspace, L, s)) != WB_OK) return st;
+            launches += 2;
+            if ((st = run_g_classes(h, nt, ldt, F32, G32, omegas[j], tile_tol,
+                                    workspace, L, s, &launches)) != WB_OK)
+                return st;
+            ntasks += (ldt / 32) * (int64_t)h->hp.npairs;
+            if ((st = k_gemm(j, G32)) != WB_OK) return st;
+            j += 1;
         }
     }
     if ((st = mark()) != WB_OK) return st;

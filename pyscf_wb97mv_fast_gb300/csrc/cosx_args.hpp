@@ -28,6 +28,11 @@ struct CosxArgs {
     // rec[c] + m * stride_c = P hi, P lo, omega record (n_om float4), E
     const float4* rec[kClasses];
     int recmax[kClasses];      // float4 of the largest task record per class
+    // dual-omega launches: records of two omegas per pair (stride 2 + 2 n_om
+    // + n_e), and the second omega's class buffers
+    const float4* rec2[kClasses];
+    int recmax2[kClasses];
+    float* Gcls2[kClasses];
     const float4* Ecls[kClasses];
     int pp_begin[kClasses];
     const int4* hdr;

@@ -30,6 +30,11 @@ template<int LA, int LB> struct CosxRec;
 // STAGE) with run() as the body.
 template<int LA, int LB, bool DIAG, int PTS, bool FAR, bool STAGE> struct CosxTask;
 
+// The same task for two omegas at once (records staged in shared memory,
+// dual layout): distances, headers and F shared; integrals, accumulators
+// and G_B per omega slot w (Gp[w * PTS + p], Xa[(w * PTS + p) * NCA ..]).
+template<int LA, int LB, bool DIAG, int PTS> struct CosxTask2;
+
 // Start of a run: f0 = c2s^T F_A (Cartesian components of F on shell A).
 template<int LA>
 __device__ __forceinline__ void cosx_begin(const float* fa, float* f0);

@@ -38,8 +38,13 @@ constexpr int kBoysFloat4 = 145 * 5;
 #ifndef WB_COSX_MIN_BLOCKS
 #define WB_COSX_MIN_BLOCKS 0x6544331111LL
 #endif
-constexpr int min_blocks(int cls) {
-    long long v = WB_COSX_MIN_BLOCKS;
+// the same for the dual-omega kernels (two sets of integrals and
+// accumulators per lane): -DWB_COSX_MIN_BLOCKS2=0x<10 hex digits>LL
+#ifndef WB_COSX_MIN_BLOCKS2
+#define WB_COSX_MIN_BLOCKS2 0x4333221111LL
+#endif
+constexpr int min_blocks(int cls, int nw = 1) {
+    long long v = nw == 2 ? WB_COSX_MIN_BLOCKS2 : WB_COSX_MIN_BLOCKS;
     for (int i = cls; i < kClasses - 1; ++i) v >>= 4;
     return (int)(v & 15) > 0 ? (int)(v & 15) : 1;
 }
@@ -124,10 +129,11 @@ template<int LA, int LB> struct ClassPts {
     static constexpr int value = class_pts(LA * (LA + 1) / 2 + LB);
 };
 
-template<int LA, int LB, bool FAR, bool STAGE>
+template<int LA, int LB, bool FAR, bool STAGE, int NW>
 __global__ void __launch_bounds__(kCtaThreads,
-                                  min_blocks(LA * (LA + 1) / 2 + LB))
+                                  min_blocks(LA * (LA + 1) / 2 + LB, NW))
 cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
+    static_assert(NW == 1 || (NW == 2 && STAGE), "dual-omega needs staging");
     constexpr int CLS = LA * (LA + 1) / 2 + LB;
     constexpr int NCA = (LA + 1) * (LA + 2) / 2;
     constexpr int NA = 2 * LA + 1;
@@ -140,12 +146,12 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
     const int lane = threadIdx.x & 31;
     // STAGE: per warp, two record buffers of recmax float4 (dynamic smem)
     extern __shared__ float4 s_stage[];
-    constexpr int RS = kRecStride[CLS];
-    const int rmax = A.recmax[CLS];
+    constexpr int RS = NW == 2 ? kRecStride2[CLS] : kRecStride[CLS];
+    const int rmax = NW == 2 ? A.recmax2[CLS] : A.recmax[CLS];
     float4* wstage = s_stage + (threadIdx.x >> 5) * 2 * rmax;
-    const float4* __restrict__ recc = A.rec[CLS];
+    const float4* __restrict__ recc = NW == 2 ? A.rec2[CLS] : A.rec[CLS];
     int sbuf = 0;
-    float* __restrict__ Gc = A.Gcls[CLS];
+    float* Gcw[2] = {A.Gcls[CLS], NW == 2 ? A.Gcls2[CLS] : A.Gcls[CLS]};
     const int ld = (int)A.ld;
     const float tol = A.tol;
     const float4* __restrict__ bnd = A.bnd + A.pp_begin[CLS];
@@ -163,7 +169,7 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
         // the lane's points: blk * 32 PTS + 32 p + lane (clamped to the
         // arrays; ok marks the ones that exist)
         const float* __restrict__ Fp[PTS];
-        float* Gp[PTS];
+        float* Gp[NW * PTS];
         bool ok[PTS];
         float gxh[PTS], gyh[PTS], gzh[PTS], gxl[PTS], gyl[PTS], gzl[PTS];
 #pragma unroll
@@ -172,7 +178,8 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
             ok[p] = g0 < ld;
             const int g = ok[p] ? g0 : ld - 1;
             Fp[p] = A.F + g;
-            Gp[p] = Gc + g;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) Gp[w * PTS + p] = Gcw[w] + g;
             gxh[p] = A.gxyz_hi[g];
             gyh[p] = A.gxyz_hi[ld + g];
             gzh[p] = A.gxyz_hi[2 * (long long)ld + g];
@@ -188,9 +195,11 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
         // run state: the current bra shell (packed header word), its class
         // buffer row, f0 and Xa; pendA / fan: F_A prefetched for a next run
         int curA = -1, ga0 = 0, pendA = -1;
-        float f0[PTS * NCA], Xa[PTS * NCA], fan[PTS * NA];
+        float f0[PTS * NCA], Xa[NW * PTS * NCA], fan[PTS * NA];
 #pragma unroll
-        for (int c = 0; c < PTS * NCA; ++c) { f0[c] = 0.0f; Xa[c] = 0.0f; }
+        for (int c = 0; c < PTS * NCA; ++c) f0[c] = 0.0f;
+#pragma unroll
+        for (int c = 0; c < NW * PTS * NCA; ++c) Xa[c] = 0.0f;
 #pragma unroll
         for (int c = 0; c < PTS * NA; ++c) fan[c] = 0.0f;
         // screen inputs of the first chunk
@@ -244,8 +253,8 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
                 if (hdr.x != curA) {
                     if (curA >= 0) {
 #pragma unroll
-                        for (int p = 0; p < PTS; ++p)
-                            cosx_end<LA>(Gp[p], ga0, ld, ok[p], Xa + p * NCA);
+                        for (int c = 0; c < NW * PTS; ++c)
+                            cosx_end<LA>(Gp[c], ga0, ld, ok[c % PTS], Xa + c * NCA);
                     }
                     curA = hdr.x;
                     ga0 = hi16(hdr.x);
@@ -259,7 +268,7 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
                     for (int p = 0; p < PTS; ++p)
                         cosx_begin<LA>(fan + p * NA, f0 + p * NCA);
 #pragma unroll
-                    for (int c = 0; c < PTS * NCA; ++c) Xa[c] = 0.0f;
+                    for (int c = 0; c < NW * PTS * NCA; ++c) Xa[c] = 0.0f;
                 }
                 mask &= mask - 1;
                 // prefetch the next kept task of this chunk (fan is free:
@@ -287,7 +296,23 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
                 }
                 const int gb0 = hi16(hdr.y), pp0 = hdr.z, npp = hdr.w & 0xffff;
                 const int nxt = more ? hn.z : pp0;
-                if constexpr (STAGE) {
+                if constexpr (NW == 2) {
+                    const float4* rp = wstage + sbuf * rmax;
+                    if constexpr (LA == LB) {
+                        if (hdr.w >> 16)
+                            CosxTask2<LA, LB, true, PTS>::run(
+                                Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                                gxl, gyl, gzl, stab, f0, fb, Xa);
+                        else
+                            CosxTask2<LA, LB, false, PTS>::run(
+                                Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                                gxl, gyl, gzl, stab, f0, fb, Xa);
+                    } else {
+                        CosxTask2<LA, LB, false, PTS>::run(
+                            Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                            gxl, gyl, gzl, stab, f0, fb, Xa);
+                    }
+                } else if constexpr (STAGE) {
                     const float4* rp = wstage + sbuf * rmax;
                     if constexpr (LA == LB) {
                         if (hdr.w >> 16)
@@ -317,7 +342,7 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
                         A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
                         gxl, gyl, gzl, stab, f0, fb, Xa, rec);
                 }
-                kept += nsb;
+                kept += nsb * NW;
                 if (!more) break;
                 if constexpr (STAGE) {
                     stage_wait();
@@ -329,14 +354,14 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
             }
             // model flops / integrals of the kept tasks of this chunk
             if (keep) {
-                flops += (unsigned long long)A.pflops[k] * nvalid;
-                ints += (unsigned long long)A.pnint[k] * nvalid;
+                flops += (unsigned long long)A.pflops[k] * nvalid * NW;
+                ints += (unsigned long long)A.pnint[k] * nvalid * NW;
             }
         }
         if (curA >= 0) {
 #pragma unroll
-            for (int p = 0; p < PTS; ++p)
-                cosx_end<LA>(Gp[p], ga0, ld, ok[p], Xa + p * NCA);
+            for (int c = 0; c < NW * PTS; ++c)
+                cosx_end<LA>(Gp[c], ga0, ld, ok[c % PTS], Xa + c * NCA);
         }
     }
     // lane 0 counted the tasks (every lane runs every task) in units of the

@@ -5,13 +5,14 @@
 namespace wb {
 
 cudaError_t launch_cosx_f_class(int cls, const CosxArgs& a, int pb, int pe,
-                                int grid, cudaStream_t s, bool far, size_t smem);
-int cosx_f_class_blocks_per_sm(int cls, bool far, size_t smem);
+                                int grid, cudaStream_t s, bool far, size_t smem,
+                                bool dual);
+int cosx_f_class_blocks_per_sm(int cls, bool far, size_t smem, bool dual);
 
-template<int LA, int LB, bool FAR, bool STAGE>
+template<int LA, int LB, bool FAR, bool STAGE, int NW = 1>
 static cudaError_t run1(const CosxArgs& a, int pb, int pe, int grid,
                         size_t smem, cudaStream_t s) {
-    auto k = cosx_class_kernel<LA, LB, FAR, STAGE>;
+    auto k = cosx_class_kernel<LA, LB, FAR, STAGE, NW>;
     if (smem > 48 * 1024) {
         const cudaError_t e = cudaFuncSetAttribute(
             k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -23,7 +24,8 @@ static cudaError_t run1(const CosxArgs& a, int pb, int pe, int grid,
 
 template<int LA, int LB>
 static cudaError_t run(const CosxArgs& a, int pb, int pe, int grid,
-                       cudaStream_t s, bool far, size_t smem) {
+                       cudaStream_t s, bool far, size_t smem, bool dual) {
+    if (dual) return run1<LA, LB, false, true, 2>(a, pb, pe, grid, smem, s);
     if (smem)
         return far ? run1<LA, LB, true, true>(a, pb, pe, grid, smem, s)
                    : run1<LA, LB, false, true>(a, pb, pe, grid, smem, s);
@@ -31,9 +33,9 @@ static cudaError_t run(const CosxArgs& a, int pb, int pe, int grid,
                : run1<LA, LB, false, false>(a, pb, pe, grid, 0, s);
 }
 
-template<int LA, int LB, bool FAR, bool STAGE>
+template<int LA, int LB, bool FAR, bool STAGE, int NW = 1>
 static int occ1(size_t smem) {
-    auto k = cosx_class_kernel<LA, LB, FAR, STAGE>;
+    auto k = cosx_class_kernel<LA, LB, FAR, STAGE, NW>;
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
@@ -46,7 +48,8 @@ static int occ1(size_t smem) {
 }
 
 template<int LA, int LB>
-static int occ(bool far, size_t smem) {
+static int occ(bool far, size_t smem, bool dual) {
+    if (dual) return occ1<LA, LB, false, true, 2>(smem);
     if (smem)
         return far ? occ1<LA, LB, true, true>(smem) : occ1<LA, LB, false, true>(smem);
     return far ? occ1<LA, LB, true, false>(0) : occ1<LA, LB, false, false>(0);
@@ -54,27 +57,27 @@ static int occ(bool far, size_t smem) {
 
 cudaError_t launch_cosx_class_range(int cls, const CosxArgs& a, int pb,
                                     int pe, int grid, cudaStream_t s, bool far,
-                                    size_t smem) {
+                                    size_t smem, bool dual) {
     switch (cls) {
-    case 0: return run<0, 0>(a, pb, pe, grid, s, far, smem);
-    case 1: return run<1, 0>(a, pb, pe, grid, s, far, smem);
-    case 2: return run<1, 1>(a, pb, pe, grid, s, far, smem);
-    case 3: return run<2, 0>(a, pb, pe, grid, s, far, smem);
-    case 4: return run<2, 1>(a, pb, pe, grid, s, far, smem);
-    case 5: return run<2, 2>(a, pb, pe, grid, s, far, smem);
-    default: return launch_cosx_f_class(cls, a, pb, pe, grid, s, far, smem);
+    case 0: return run<0, 0>(a, pb, pe, grid, s, far, smem, dual);
+    case 1: return run<1, 0>(a, pb, pe, grid, s, far, smem, dual);
+    case 2: return run<1, 1>(a, pb, pe, grid, s, far, smem, dual);
+    case 3: return run<2, 0>(a, pb, pe, grid, s, far, smem, dual);
+    case 4: return run<2, 1>(a, pb, pe, grid, s, far, smem, dual);
+    case 5: return run<2, 2>(a, pb, pe, grid, s, far, smem, dual);
+    default: return launch_cosx_f_class(cls, a, pb, pe, grid, s, far, smem, dual);
     }
 }
 
-int cosx_class_blocks_per_sm(int cls, bool far, size_t smem) {
+int cosx_class_blocks_per_sm(int cls, bool far, size_t smem, bool dual) {
     switch (cls) {
-    case 0: return occ<0, 0>(far, smem);
-    case 1: return occ<1, 0>(far, smem);
-    case 2: return occ<1, 1>(far, smem);
-    case 3: return occ<2, 0>(far, smem);
-    case 4: return occ<2, 1>(far, smem);
-    case 5: return occ<2, 2>(far, smem);
-    default: return cosx_f_class_blocks_per_sm(cls, far, smem);
+    case 0: return occ<0, 0>(far, smem, dual);
+    case 1: return occ<1, 0>(far, smem, dual);
+    case 2: return occ<1, 1>(far, smem, dual);
+    case 3: return occ<2, 0>(far, smem, dual);
+    case 4: return occ<2, 1>(far, smem, dual);
+    case 5: return occ<2, 2>(far, smem, dual);
+    default: return cosx_f_class_blocks_per_sm(cls, far, smem, dual);
     }
 }
 

@@ -569,6 +569,215 @@ def gen_class(la, lb, diag, far, stage=False):
     return '\n'.join(lines)
 
 
+def rec_stride2(la, lb):
+    """float4 per primitive pair of a class's dual-omega packed record: geo,
+    the two omegas' records (n_om float4 each), E."""
+    return 2 + 2 * n_om(la, lb) + e_stride(la, lb) // 4
+
+
+def gen_r000(la, lb, J, lines, of_prefix, near_first, slot):
+    """R0[slot][p][n] for every point from the distances r2v, with the
+    omega record fields named <of_prefix><q>: warp-uniform all-far /
+    all-near branches (the likelier one tested first), per point for mixed
+    warps."""
+    L = la + lb
+    nom = n_om(la, lb)
+    comp = 'xyzw'
+    o = lambda q: '%s%d' % (of_prefix, q)
+    of = o(nom - 1)
+
+    def near(ind):
+        lines.append(ind + 'const float T = fmaf(%s.x, r2v[p], %s.y * r2v[p]);' % (o(0), o(0)))
+        lines.append(ind + 'float Fb[%d];' % (L + 1))
+        lines.append(ind + 'boys_taylor<%d>(T, Fb, stab);' % L)
+        for n in range(L + 1):
+            fh = 2 + 2 * n
+            fl = fh + 1
+            ch = '%s.%s' % (o(fh // 4), comp[fh % 4])
+            cl = '%s.%s' % (o(fl // 4), comp[fl % 4])
+            lines.append(ind + 'R0[%d][p][%d] = fmaf(%s, Fb[%d], %s * Fb[%d]);'
+                         % (slot, n, ch, n, cl, n))
+
+    def far(ind):
+        lines.append(ind + 'far_r000<%d>(r2v[p], %s.x, %s.y, R0[%d][p]);' % (L, of, of, slot))
+
+    lines.append(J + '{')
+    K = J + '    '
+    lines.append(K + 'bool allfar = true, allnear = true;')
+    lines.append(K + '#pragma unroll')
+    lines.append(K + 'for (int p = 0; p < PTS; ++p) {')
+    lines.append(K + '    const bool f = r2v[p] >= %s.z;' % of)
+    lines.append(K + '    allfar = allfar && f;')
+    lines.append(K + '    allnear = allnear && !f;')
+    lines.append(K + '}')
+    first, second = (('allnear', near), ('allfar', far)) if near_first else (('allfar', far), ('allnear', near))
+    lines.append(K + 'if (__all_sync(0xffffffffu, %s)) {' % first[0])
+    lines.append(K + '    #pragma unroll')
+    lines.append(K + '    for (int p = 0; p < PTS; ++p) {')
+    first[1](K + '        ')
+    lines.append(K + '    }')
+    lines.append(K + '} else if (__all_sync(0xffffffffu, %s)) {' % second[0])
+    lines.append(K + '    #pragma unroll')
+    lines.append(K + '    for (int p = 0; p < PTS; ++p) {')
+    second[1](K + '        ')
+    lines.append(K + '    }')
+    lines.append(K + '} else {')
+    lines.append(K + '    #pragma unroll')
+    lines.append(K + '    for (int p = 0; p < PTS; ++p) {')
+    lines.append(K + '        if (r2v[p] >= %s.z) {' % of)
+    far(K + '            ')
+    lines.append(K + '        } else {')
+    near(K + '            ')
+    lines.append(K + '        }')
+    lines.append(K + '    }')
+    lines.append(K + '}')
+    lines.append(J + '}')
+
+
+def gen_prim_body_dual(la, lb, diag, J, lines):
+    """Dual-omega work of one primitive pair whose record is at q (shared
+    memory): the distances once, then for each omega slot the R000 sources
+    (slot 0: all-far tested first, slot 1: all-near first), the R
+    recurrence, the Hermite sums and the Y (and X) accumulation."""
+    L = la + lb
+    ca = cart_components(la)
+    cb = cart_components(lb)
+    ents = e_entries(la, lb)
+    nom = n_om(la, lb)
+    nvec = e_stride(la, lb) // 4
+    comp = 'xyzw'
+    tuv = [(t, u, v) for t in range(L + 1) for u in range(L + 1 - t)
+           for v in range(L + 1 - t - u)]
+    lines.append(J + 'const float4 ph = q[0], pl = q[1];')
+    for w, pre in enumerate(('oa', 'ob')):
+        for k in range(nom):
+            lines.append(J + 'const float4 %s%d = q[%d];' % (pre, k, 2 + w * nom + k))
+    if ents:
+        for k in range(nvec):
+            lines.append(J + 'const float4 ev%d = q[%d];' % (k, 2 + 2 * nom + k))
+        flat = []
+        for ax in range(3):
+            for (i, j, t) in ents:
+                flat.append(ename(ax, i, j, t))
+        while len(flat) % 4:
+            flat.append(None)
+        for k in range(nvec):
+            for c in range(4):
+                nm = flat[4 * k + c]
+                if nm is not None:
+                    lines.append(J + 'const float %s = ev%d.%s;' % (nm, k, comp[c]))
+    lines.append(J + 'float dxv[PTS], dyv[PTS], dzv[PTS], r2v[PTS], R0[2][PTS][%d];' % (L + 1))
+    lines.append(J + '#pragma unroll')
+    lines.append(J + 'for (int p = 0; p < PTS; ++p) {')
+    lines.append(J + '    dxv[p] = (ph.x - gxh[p]) + (pl.x - gxl[p]);')
+    lines.append(J + '    dyv[p] = (ph.y - gyh[p]) + (pl.y - gyl[p]);')
+    lines.append(J + '    dzv[p] = (ph.z - gzh[p]) + (pl.z - gzl[p]);')
+    lines.append(J + '    r2v[p] = fmaf(dxv[p], dxv[p], fmaf(dyv[p], dyv[p], dzv[p] * dzv[p]));')
+    lines.append(J + '}')
+    gen_r000(la, lb, J, lines, 'oa', False, 0)
+    gen_r000(la, lb, J, lines, 'ob', True, 1)
+    lines.append(J + '#pragma unroll')
+    lines.append(J + 'for (int w = 0; w < 2; ++w) {')
+    lines.append(J + '#pragma unroll')
+    lines.append(J + 'for (int p = 0; p < PTS; ++p) {')
+    K = J + '    '
+    lines.append(K + 'const float dx = dxv[p], dy = dyv[p], dz = dzv[p];')
+    for n in range(L + 1):
+        lines.append(K + 'const float R000_%d = R0[w][p][%d];' % (n, n))
+    lines.append(K + 'float ' + ', '.join(rname(*x) for x in tuv) + ';')
+    gen_recurrence(L, lines, K)
+    for ia, cac in enumerate(ca):
+        for ib, cbc in enumerate(cb):
+            tag = '%d_%d' % (ia, ib)
+            sv = gen_hermite(la, lb, cac, cbc, K, lines, tag)
+            lines.append(K + 'Yv[w][p][%d] = fmaf(f0v[p][%d], %s, Yv[w][p][%d]);'
+                         % (ib, ia, sv, ib))
+            if not diag:
+                lines.append(K + 'Xv[w][p][%d] = fmaf(%s, h0v[p][%d], Xv[w][p][%d]);'
+                             % (ia, sv, ib, ia))
+    lines.append(J + '}')
+    lines.append(J + '}')
+
+
+def gen_class_dual(la, lb, diag):
+    """Task body for two omegas at once (records staged in shared memory):
+    the screen, headers, F loads and distances are shared, the integrals,
+    accumulators and G_B updates are per omega slot (Gp[w * PTS + p],
+    Xa[w * PTS * NCA + ...])."""
+    nb = 2 * lb + 1
+    nca = (la + 1) * (la + 2) // 2
+    ncb = (lb + 1) * (lb + 2) // 2
+    lines = []
+    I = '    '
+    J = I * 2
+    lines.append('template<int PTS> struct CosxTask2<%d, %d, %s, PTS> {'
+                 % (la, lb, 'true' if diag else 'false'))
+    lines.append('static __device__ __forceinline__ void run(')
+    lines.append('    float* const* Gp, const int ld, const int gb0,')
+    lines.append('    const float4* __restrict__ rp, const int npp, const bool* ok,')
+    lines.append('    const float* gxh, const float* gyh, const float* gzh,')
+    lines.append('    const float* gxl, const float* gyl, const float* gzl,')
+    lines.append('    const float4* __restrict__ stab, const float* f0,')
+    lines.append('    const float* fb, float* Xa)')
+    lines.append('{')
+    lines.append(I + 'float f0v[PTS][%d], Yv[2][PTS][%d];' % (nca, ncb))
+    if not diag:
+        lines.append(I + 'float gbo[2][PTS][%d], h0v[PTS][%d], Xv[2][PTS][%d];'
+                     % (nb, ncb, nca))
+    lines.append(I + '#pragma unroll')
+    lines.append(I + 'for (int p = 0; p < PTS; ++p) {')
+    if not diag:
+        lines.append(J + '#pragma unroll')
+        lines.append(J + 'for (int w = 0; w < 2; ++w) {')
+        for nu in range(nb):
+            lines.append(J + '    gbo[w][p][%d] = Gp[w * PTS + p][(long long)(gb0 + %d) * ld];'
+                         % (nu, nu))
+        for c in range(nca):
+            lines.append(J + '    Xv[w][p][%d] = Xa[(w * PTS + p) * %d + %d];' % (c, nca, c))
+        lines.append(J + '}')
+        for nu in range(nb):
+            lines.append(J + 'const float fb%d = fb[p * %d + %d];' % (nu, nb, nu))
+        gen_transform_in(lb, 'fb', 'h0_', J, lines)
+        for c in range(ncb):
+            lines.append(J + 'h0v[p][%d] = h0_%d;' % (c, c))
+    for c in range(nca):
+        lines.append(J + 'f0v[p][%d] = f0[p * %d + %d];' % (c, nca, c))
+    for c in range(ncb):
+        lines.append(J + 'Yv[0][p][%d] = 0.0f;' % c)
+        lines.append(J + 'Yv[1][p][%d] = 0.0f;' % c)
+    lines.append(I + '}')
+    lines.append(I + '#pragma unroll 1')
+    lines.append(I + 'for (int m = 0; m < npp; ++m) {')
+    lines.append(J + 'const float4* __restrict__ q = rp + m * %d;' % rec_stride2(la, lb))
+    lines.append(J + '{')
+    gen_prim_body_dual(la, lb, diag, J + I, lines)
+    lines.append(J + '}')
+    lines.append(I + '}')
+    lines.append(I + '#pragma unroll')
+    lines.append(I + 'for (int w = 0; w < 2; ++w) {')
+    lines.append(I + '#pragma unroll')
+    lines.append(I + 'for (int p = 0; p < PTS; ++p) {')
+    if diag:
+        for c in range(ncb):
+            lines.append(J + 'Xa[(w * PTS + p) * %d + %d] += Yv[w][p][%d];' % (nca, c, c))
+    else:
+        for c in range(ncb):
+            lines.append(J + 'const float Y%d = Yv[w][p][%d];' % (c, c))
+        gen_transform_out(lb, 'Y', 'gy', J, lines)
+        lines.append(J + 'if (ok[p]) {')
+        for nu in range(nb):
+            lines.append(J + '    Gp[w * PTS + p][(long long)(gb0 + %d) * ld] = gbo[w][p][%d] + gy%d;'
+                         % (nu, nu, nu))
+        lines.append(J + '}')
+        for c in range(nca):
+            lines.append(J + 'Xa[(w * PTS + p) * %d + %d] = Xv[w][p][%d];' % (nca, c, c))
+    lines.append(I + '}')
+    lines.append(I + '}')
+    lines.append('}')
+    lines.append('};')
+    return '\n'.join(lines)
+
+
 def source():
     out = ['// Generated by csrc/gen_cosx.py -- do not edit by hand.',
            '// One straight-line task body per shell-pair class (la >= lb),',
@@ -592,6 +801,11 @@ def source():
                 if la == lb:
                     out.append(gen_class(la, lb, True, far, stage))
                     out.append('')
+        out.append(gen_class_dual(la, lb, False))
+        out.append('')
+        if la == lb:
+            out.append(gen_class_dual(la, lb, True))
+            out.append('')
     # E strides table for the host
     out.append('#define WB_E_STRIDES {%s}' % ', '.join(
         str(e_stride(la, lb)) for (la, lb) in classes()))
@@ -611,6 +825,8 @@ def layout_source():
         'constexpr int kRecNom[10] = {%s};' % ', '.join(str(n_om(a, b)) for a, b in cl),
         'constexpr int kRecNe[10] = {%s};' % ', '.join(str(e_stride(a, b) // 4) for a, b in cl),
         'constexpr int kRecStride[10] = {%s};' % ', '.join(str(rec_stride(a, b)) for a, b in cl),
+        '// dual-omega record: 2 + 2 n_om + n_e',
+        'constexpr int kRecStride2[10] = {%s};' % ', '.join(str(rec_stride2(a, b)) for a, b in cl),
         '}  // namespace wb', ''])
 
 

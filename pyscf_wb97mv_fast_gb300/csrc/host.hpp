@@ -85,6 +85,8 @@ struct HostPairs {
     // the class kernels read; rebuilt per omega
     int64_t rec_off[NCLASS] = {0};       // float4 offset of each class
     int64_t nrec = 0;                    // float4 in all classes
+    int64_t rec_off2[NCLASS] = {0};      // the same for the dual-omega layout
+    int64_t nrec2 = 0;
     // per virtual shell (for the sub-block statistics)
     std::vector<int32_t> vs_ao0, vs_nf;
 };

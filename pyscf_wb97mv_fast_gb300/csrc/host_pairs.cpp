@@ -470,17 +470,22 @@ int build_pairs(const wb_basis& b, const double origin[3], double cutoff,
         for (int lb = 0; lb <= la; ++lb) {
             const int c = class_of(la, lb);
             if (kRecNe[c] * 4 != e_stride(la, lb) || kRecNom[c] != 2 + (la + lb + 1) / 2 ||
-                kRecStride[c] != 2 + kRecNom[c] + kRecNe[c]) {
+                kRecStride[c] != 2 + kRecNom[c] + kRecNe[c] ||
+                kRecStride2[c] != 2 + 2 * kRecNom[c] + kRecNe[c]) {
                 err = "generated record layout does not match the pair tables";
                 return WB_ERR_UNSUPPORTED;
             }
         }
-    int64_t roff = 0;
+    int64_t roff = 0, roff2 = 0;
     for (int c = 0; c < NCLASS; ++c) {
         out.rec_off[c] = roff;
-        roff += (int64_t)(out.cls[c].pp_end - out.cls[c].pp_begin) * kRecStride[c];
+        out.rec_off2[c] = roff2;
+        const int64_t n = out.cls[c].pp_end - out.cls[c].pp_begin;
+        roff += n * kRecStride[c];
+        roff2 += n * kRecStride2[c];
     }
     out.nrec = roff;
+    out.nrec2 = roff2;
     out.gsrc.assign(4 * (size_t)out.nao, -1);
     for (size_t s = 0; s < out.vsh.size(); ++s) {
         const VShell& v = out.vsh[s];

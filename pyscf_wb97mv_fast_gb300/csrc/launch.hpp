@@ -11,12 +11,15 @@ namespace wb {
 // variant with the far-field R000 form (omega = 0, where T >= 36 is common);
 // stage_smem > 0 selects the variant that stages each task's primitive-pair
 // records in shared memory (stage_smem bytes of dynamic smem per CTA)
+// dual runs the dual-omega variant (two omegas per launch, staged records
+// of the dual layout; far is then unused)
 cudaError_t launch_cosx_class_range(int cls, const CosxArgs& a, int pb,
                                     int pe, int grid, cudaStream_t s, bool far,
-                                    size_t stage_smem);
+                                    size_t stage_smem, bool dual = false);
 // max resident CTAs per SM of a class kernel (128 threads each); 0 if the
 // kernel cannot run with that much dynamic shared memory
-int cosx_class_blocks_per_sm(int cls, bool far, size_t stage_smem);
+int cosx_class_blocks_per_sm(int cls, bool far, size_t stage_smem,
+                             bool dual = false);
 
 struct AoArgs {
     const double* coords;       // (npts, 3) molecule frame
@@ -51,6 +54,11 @@ struct RecPack {
 cudaError_t launch_pack_records(const RecPack& P, int npp, const float4* geo,
                                 const float4* om, const float4* E,
                                 float4* rec, cudaStream_t s);
+// dual-omega records: geo, the first n_om - 1 float4 and the far-field
+// float4 of om_a, then the same of om_b, then E (P.stride = dual stride)
+cudaError_t launch_pack_records2(const RecPack& P, int npp, const float4* geo,
+                                 const float4* om_a, const float4* om_b,
+                                 const float4* E, float4* rec, cudaStream_t s);
 cudaError_t launch_omega(int npp, const double* p, const double* pref,
                          double omega, float4* om, cudaStream_t s);
 cudaError_t launch_grid_prep(const double* coords, int64_t npts, int64_t ld,
