@@ -203,7 +203,7 @@ WsLayout ws_layout(const wb_cosx* h, int64_t ldt, bool full) {
         // bf16 Ozaki path (slices, level outputs): never live together
         const size_t dg = sizeof(double) * (size_t)nao * ldt;
         const size_t oz = std::max(wb::ozaki_f_bytes(nao, ldt),
-                                   wb::ozaki_k_bytes(nao, ldt));
+                                   wb::ozaki_k_bytes(nao, ldt, 2));
         L.F64 = take(std::max(dg, oz));
         L.oz = L.F64;
     }
@@ -887,8 +887,23 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
                                              &launches)) != WB_OK)
                     return st;
                 ntasks += 2 * (ldt / 32) * (int64_t)h->hp.npairs;
-                if ((st = k_gemm(ja, G32)) != WB_OK) return st;
-                if ((st = k_gemm(jb, G32b)) != WB_OK) return st;
+                if (oz_k) {
+                    // both omegas' w o G against the same X in one split
+                    if ((st = phase_to(5)) != WB_OK) return st;
+                    const float* Gs[2] = {G32, G32b};
+                    double* Ks[2] = {k_out + kk * ja, k_out + kk * jb};
+                    const int r = wb::ozaki_k_gemm_multi(
+                        h->cublas, X, Gs, 2, w, nao, ldt, nt, i0 == 0 ? 0 : 1, Ks,
+                        at<void>(workspace, L.oz), s, x_sliced);
+                    if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
+                                       "ozaki K GEMM failed, code " + std::to_string(r));
+                    x_sliced = true;
+                    launches += 3 + wb::kOzSlices;
+                    if ((st = phase_to(3)) != WB_OK) return st;
+                } else {
+                    if ((st = k_gemm(ja, G32)) != WB_OK) return st;
+                    if ((st = k_gemm(jb, G32b)) != WB_OK) return st;
+                }
                 j += 2;
                 continue;
             }

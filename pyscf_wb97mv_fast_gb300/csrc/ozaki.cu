@@ -276,13 +276,16 @@ __global__ void f_combine_kernel(const float* __restrict__ C, int nao,
 // chunk stride S KC nao.  One CTA of 256 threads per (chunk, column).
 // ---------------------------------------------------------------------------
 // DOX = false: the X slices and exponents of this tile are already in A /
-// ex (an earlier omega of the same tile); only w o G is sliced
+// ex (an earlier omega of the same tile); only w o G is sliced.  B holds nb
+// columns per chunk (several right-hand sides side by side); this launch
+// fills columns boff .. boff + nao - 1.
 template<int S, int KC, bool DOX>
 __global__ void __launch_bounds__(KC / 8)
 k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
                const double* __restrict__ w, int nao, int64_t ld,
                int64_t npts, int* __restrict__ ex, int* __restrict__ ew,
-               __nv_bfloat16* __restrict__ A, __nv_bfloat16* __restrict__ B) {
+               __nv_bfloat16* __restrict__ A, __nv_bfloat16* __restrict__ B,
+               int nb, int boff) {
     constexpr int T = KC / 8;               // threads: eight points each
     const int c = blockIdx.x, col = blockIdx.y;
     __shared__ unsigned long long rx[T / 32], rw[T / 32];
@@ -348,9 +351,10 @@ k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
     const int e1 = exp_of_bits(mx), e2 = exp_of_bits(mw);
     if (threadIdx.x == 0) {
         if (DOX) ex[(int64_t)c * nao + col] = e1;
-        ew[(int64_t)c * nao + col] = e2;
+        ew[(int64_t)c * nb + boff + col] = e2;
     }
     const int64_t colbase = (int64_t)c * S * KC * nao + (int64_t)col * S * KC;
+    const int64_t colbase_b = (int64_t)c * S * KC * nb + (int64_t)(boff + col) * S * KC;
     float d1[8][S], d2[8][S];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -368,32 +372,38 @@ k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
         if (DOX)
             *reinterpret_cast<uint4*>(A + colbase + (int64_t)i * KC + k0) =
                 *reinterpret_cast<const uint4*>(pa);
-        *reinterpret_cast<uint4*>(B + colbase + (int64_t)(S - 1 - i) * KC + k0) =
+        *reinterpret_cast<uint4*>(B + colbase_b + (int64_t)(S - 1 - i) * KC + k0) =
             *reinterpret_cast<const uint4*>(pb);
     }
 }
 
-// K[mu, nu] (+)= sum_c 2^(ex+ew-2W+2+B(S-1)) [sum_l C[l][c] 2^(B (S-1-l))]
+// K_r[mu, nu] (+)= sum_c 2^(ex+ew-2W+2+B(S-1)) [sum_l C[l][c] 2^(B (S-1-l))]
+// for the nb / nao right-hand sides r (column r nao + nu of C)
+struct KOut {
+    double* k[8];
+};
+
 template<int S>
-__global__ void k_combine_kernel(const float* __restrict__ C, int nao,
+__global__ void k_combine_kernel(const float* __restrict__ C, int nao, int nb,
                                  int nchunk, const int* __restrict__ ex,
                                  const int* __restrict__ ew, int accumulate,
-                                 double* __restrict__ K) {
-    const int64_t n2 = (int64_t)nao * nao;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2;
+                                 const KOut Ks) {
+    const int64_t nc = (int64_t)nao * nb;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nc;
          i += (int64_t)gridDim.x * blockDim.x) {
-        const int mu = (int)(i % nao), nu = (int)(i / nao);   // C col-major
+        const int mu = (int)(i % nao), col = (int)(i / nao);   // C col-major
         double acc = 0.0;
         for (int c = 0; c < nchunk; ++c) {
             float v[S];
 #pragma unroll
-            for (int l = 0; l < S; ++l) v[l] = C[((int64_t)l * nchunk + c) * n2 + i];
+            for (int l = 0; l < S; ++l) v[l] = C[((int64_t)l * nchunk + c) * nc + i];
             const long long lv = combine_levels<S>(v);
-            const int sc = ex[(int64_t)c * nao + mu] + ew[(int64_t)c * nao + nu] -
+            const int sc = ex[(int64_t)c * nao + mu] + ew[(int64_t)c * nb + col] -
                            2 * kW + 2 + kB * (S - 1);
             acc += (double)lv * pow2(sc);
         }
-        const int64_t o = (int64_t)mu * nao + nu;              // K row-major
+        double* K = Ks.k[col / nao];
+        const int64_t o = (int64_t)mu * nao + col % nao;       // K row-major
         K[o] = accumulate ? K[o] + acc : acc;
     }
 }
@@ -409,12 +419,13 @@ size_t ozaki_f_bytes(int nao, int64_t ld) {
            al(sizeof(float) * S * nao * ld);
 }
 
-size_t ozaki_k_bytes(int nao, int64_t ld) {
+size_t ozaki_k_bytes(int nao, int64_t ld, int nrhs) {
     const size_t S = kOzSlices;
     const int64_t nchunk = (ld + kOzKc - 1) / kOzKc;
-    return 2 * al(sizeof(int) * nchunk * nao) +
-           2 * al(sizeof(__nv_bfloat16) * S * kOzKc * nchunk * nao) +
-           al(sizeof(float) * S * nchunk * (size_t)nao * nao);
+    return al(sizeof(int) * nchunk * nao) + al(sizeof(int) * nchunk * nao * nrhs) +
+           al(sizeof(__nv_bfloat16) * S * kOzKc * nchunk * nao) +
+           al(sizeof(__nv_bfloat16) * S * kOzKc * nchunk * nao * nrhs) +
+           al(sizeof(float) * S * nchunk * (size_t)nao * nao * nrhs);
 }
 
 #define OZ_CUBLAS(call)                                        \
@@ -466,46 +477,63 @@ int ozaki_f_gemm(cublasHandle_t hb, const double* X, const double* QD,
     return 0;
 }
 
+int ozaki_k_gemm_multi(cublasHandle_t hb, const double* X, const float* const* G,
+                       int nrhs, const double* w, int nao, int64_t ld,
+                       int64_t npts, int accumulate, double* const* K, void* ws,
+                       cudaStream_t s, bool x_sliced) {
+    constexpr int S = kOzSlices, KC = kOzKc;
+    if (nrhs < 1 || nrhs > 8) return (int)cudaErrorInvalidValue;
+    const int nchunk = (int)((ld + KC - 1) / KC);
+    const int nb = nrhs * nao;
+    // the X side (ex, A) first, at offsets independent of nrhs, so that a
+    // later call with x_sliced finds them whatever its nrhs
+    char* p = static_cast<char*>(ws);
+    int* ex = reinterpret_cast<int*>(p); p += al(sizeof(int) * (size_t)nchunk * nao);
+    const size_t slab = (size_t)S * KC * nchunk * nao;
+    __nv_bfloat16* A = reinterpret_cast<__nv_bfloat16*>(p);
+    p += al(sizeof(__nv_bfloat16) * slab);
+    int* ew = reinterpret_cast<int*>(p); p += al(sizeof(int) * (size_t)nchunk * nb);
+    __nv_bfloat16* B = reinterpret_cast<__nv_bfloat16*>(p);
+    p += al(sizeof(__nv_bfloat16) * slab * nrhs);
+    float* C = reinterpret_cast<float*>(p);
+    KOut Kd = {};
+    for (int r = 0; r < nrhs; ++r) Kd.k[r] = K[r];
+    dim3 grid(nchunk, nao);
+    for (int r = 0; r < nrhs; ++r) {
+        if (x_sliced || r > 0)
+            k_slice_kernel<S, KC, false><<<grid, KC / 8, 0, s>>>(
+                X, G[r], w, nao, ld, npts, ex, ew, A, B, nb, r * nao);
+        else
+            k_slice_kernel<S, KC, true><<<grid, KC / 8, 0, s>>>(
+                X, G[r], w, nao, ld, npts, ex, ew, A, B, nb, r * nao);
+        OZ_CUDA(cudaGetLastError());
+    }
+    const float one = 1.0f, zero = 0.0f;
+    const long long stride_a = (long long)S * KC * nao;
+    const long long stride_b = (long long)S * KC * nb;
+    const long long nc = (long long)nao * nb;
+    for (int l = 0; l < S; ++l) {
+        OZ_CUBLAS(cublasGemmStridedBatchedEx(
+            hb, CUBLAS_OP_T, CUBLAS_OP_N, nao, nb, (l + 1) * KC, &one, A,
+            CUDA_R_16BF, S * KC, stride_a, B + (size_t)(S - 1 - l) * KC,
+            CUDA_R_16BF, S * KC, stride_b, &zero, C + (size_t)l * nchunk * nc,
+            CUDA_R_32F, nao, nc, nchunk, CUBLAS_COMPUTE_32F,
+            CUBLAS_GEMM_DEFAULT));
+    }
+    int64_t blocks = (nc + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    k_combine_kernel<S><<<(unsigned)blocks, 256, 0, s>>>(C, nao, nb, nchunk, ex, ew,
+                                                        accumulate, Kd);
+    OZ_CUDA(cudaGetLastError());
+    return 0;
+}
+
 int ozaki_k_gemm(cublasHandle_t hb, const double* X, const float* G,
                  const double* w, int nao, int64_t ld, int64_t npts,
                  int accumulate, double* K, void* ws, cudaStream_t s,
                  bool x_sliced) {
-    constexpr int S = kOzSlices, KC = kOzKc;
-    const int nchunk = (int)((ld + KC - 1) / KC);
-    char* p = static_cast<char*>(ws);
-    int* ex = reinterpret_cast<int*>(p); p += al(sizeof(int) * (size_t)nchunk * nao);
-    int* ew = reinterpret_cast<int*>(p); p += al(sizeof(int) * (size_t)nchunk * nao);
-    const size_t slab = (size_t)S * KC * nchunk * nao;
-    __nv_bfloat16* A = reinterpret_cast<__nv_bfloat16*>(p);
-    p += al(sizeof(__nv_bfloat16) * slab);
-    __nv_bfloat16* B = reinterpret_cast<__nv_bfloat16*>(p);
-    p += al(sizeof(__nv_bfloat16) * slab);
-    float* C = reinterpret_cast<float*>(p);
-    dim3 grid(nchunk, nao);
-    if (x_sliced)
-        k_slice_kernel<S, KC, false><<<grid, KC / 8, 0, s>>>(X, G, w, nao, ld, npts,
-                                                            ex, ew, A, B);
-    else
-        k_slice_kernel<S, KC, true><<<grid, KC / 8, 0, s>>>(X, G, w, nao, ld, npts,
-                                                           ex, ew, A, B);
-    OZ_CUDA(cudaGetLastError());
-    const float one = 1.0f, zero = 0.0f;
-    const long long stride = (long long)S * KC * nao;
-    const long long n2 = (long long)nao * nao;
-    for (int l = 0; l < S; ++l) {
-        OZ_CUBLAS(cublasGemmStridedBatchedEx(
-            hb, CUBLAS_OP_T, CUBLAS_OP_N, nao, nao, (l + 1) * KC, &one, A,
-            CUDA_R_16BF, S * KC, stride, B + (size_t)(S - 1 - l) * KC,
-            CUDA_R_16BF, S * KC, stride, &zero, C + (size_t)l * nchunk * n2,
-            CUDA_R_32F, nao, n2, nchunk, CUBLAS_COMPUTE_32F,
-            CUBLAS_GEMM_DEFAULT));
-    }
-    int64_t blocks = (n2 + 255) / 256;
-    if (blocks > 152 * 32) blocks = 152 * 32;
-    k_combine_kernel<S><<<(unsigned)blocks, 256, 0, s>>>(C, nao, nchunk, ex, ew,
-                                                        accumulate, K);
-    OZ_CUDA(cudaGetLastError());
-    return 0;
+    return ozaki_k_gemm_multi(hb, X, &G, 1, w, nao, ld, npts, accumulate, &K, ws,
+                              s, x_sliced);
 }
 
 }  // namespace wb

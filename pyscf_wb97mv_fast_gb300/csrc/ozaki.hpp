@@ -16,7 +16,9 @@ constexpr int kOzKc = 2048;    // K-GEMM chunk: (l + 1) * Kc < 2^14 for l < 7
 inline bool ozaki_f_supported(int nao) { return kOzSlices * nao < (1 << 14); }
 
 size_t ozaki_f_bytes(int nao, int64_t ld);
-size_t ozaki_k_bytes(int nao, int64_t ld);
+// workspace of the K split for nrhs right-hand sides (w o G of several
+// omegas against the same X)
+size_t ozaki_k_bytes(int nao, int64_t ld, int nrhs = 1);
 
 // F (nao, ld) FP32 AO-major = fl32(X QD); X (nao, ld) FP64 AO-major, QD
 // (nao, nao) row-major FP64.  Returns 0, a cudaError_t, or 1000 + cuBLAS
@@ -32,5 +34,12 @@ int ozaki_k_gemm(cublasHandle_t hb, const double* X, const float* G,
                  const double* w, int nao, int64_t ld, int64_t npts,
                  int accumulate, double* K, void* ws, cudaStream_t s,
                  bool x_sliced = false);
+
+// K_r (+)= X^T (w o G_r) for r < nrhs (<= 8) in one split: X sliced once,
+// the w o G_r side by side (N = nrhs nao per level GEMM), one combine.
+int ozaki_k_gemm_multi(cublasHandle_t hb, const double* X, const float* const* G,
+                       int nrhs, const double* w, int nao, int64_t ld,
+                       int64_t npts, int accumulate, double* const* K, void* ws,
+                       cudaStream_t s, bool x_sliced = false);
 
 }  // namespace wb
