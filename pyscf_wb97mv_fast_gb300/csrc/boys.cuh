@@ -20,19 +20,20 @@ namespace wb {
 // ---------------------------------------------------------------------------
 #define WB_BOYS_TSWITCH 36.0f
 
-// The T < 36 branch alone (T in [0, 36.06)): Taylor about the nearest node.
+// The T < 36 branch alone (T in [0, 36.06)): Taylor about the nearest node,
+// F_n(T) = sum_j F_{n+j}(T_k) (-h)^j / j!, in nested form:
+//   t = F_{n+6};  t = F_{n+j} + t (-h) / (j + 1)  for j = 5 .. 1;
+//   F_n = F_n,hi + (F_n,lo + (-h) t)
+// (the (-h)/(j+1) are formed once for every order; one dependent FMA chain
+// per order; the lo part joins before the single final addition).
 template<int L>
 __device__ __forceinline__ void boys_taylor(float T, float* F,
                                             const float4* __restrict__ tab) {
     T = fmaxf(T, 0.0f);
     const int k = __float2int_rn(T * 4.0f);
     const float mh = fmaf(0.25f, (float)k, -T);           // -h, exact
-    const float q1 = mh;
-    const float q2 = q1 * mh * 0.5f;
-    const float q3 = q2 * mh * (1.0f / 3.0f);
-    const float q4 = q3 * mh * 0.25f;
-    const float q5 = q4 * mh * 0.2f;
-    const float q6 = q5 * mh * (1.0f / 6.0f);
+    const float m2 = mh * 0.5f, m3 = mh * (1.0f / 3.0f), m4 = mh * 0.25f;
+    const float m5 = mh * 0.2f, m6 = mh * (1.0f / 6.0f);
     const float4* row = tab + k * 5;
     float hv[13], lv[7];
     {
@@ -54,14 +55,12 @@ __device__ __forceinline__ void boys_taylor(float T, float* F,
     }
 #pragma unroll
     for (int n = 0; n <= L; ++n) {
-        float s = q6 * hv[n + 6];
-        s = fmaf(q5, hv[n + 5], s);
-        s = fmaf(q4, hv[n + 4], s);
-        s = fmaf(q3, hv[n + 3], s);
-        s = fmaf(q2, hv[n + 2], s);
-        s = fmaf(q1, hv[n + 1], s);
-        s = s + lv[n];
-        F[n] = hv[n] + s;
+        float t = fmaf(hv[n + 6], m6, hv[n + 5]);
+        t = fmaf(t, m5, hv[n + 4]);
+        t = fmaf(t, m4, hv[n + 3]);
+        t = fmaf(t, m3, hv[n + 2]);
+        t = fmaf(t, m2, hv[n + 1]);
+        F[n] = hv[n] + fmaf(mh, t, lv[n]);
     }
 }
 
@@ -105,44 +104,7 @@ __device__ __forceinline__ void boys_fp32(float T, float* F,
                                           const float4* __restrict__ tab) {
     if (!(T > 0.0f)) T = 0.0f;
     if (T < WB_BOYS_TSWITCH) {
-        const int k = __float2int_rn(T * 4.0f);
-        const float mh = fmaf(0.25f, (float)k, -T);       // -h, exact
-        const float q1 = mh;
-        const float q2 = q1 * mh * 0.5f;
-        const float q3 = q2 * mh * (1.0f / 3.0f);
-        const float q4 = q3 * mh * 0.25f;
-        const float q5 = q4 * mh * 0.2f;
-        const float q6 = q5 * mh * (1.0f / 6.0f);
-        const float4* row = tab + k * 5;
-        float hv[13], lv[7];
-        {
-            const float4 a = row[0], b = row[1];
-            hv[0] = a.x; hv[1] = a.y; hv[2] = a.z; hv[3] = a.w;
-            hv[4] = b.x; hv[5] = b.y; hv[6] = b.z; lv[0] = b.w;
-        }
-        if (L >= 1) {
-            const float4 c = row[2];
-            hv[7] = c.x; lv[1] = c.y; hv[8] = c.z; lv[2] = c.w;
-        }
-        if (L >= 3) {
-            const float4 d = row[3];
-            hv[9] = d.x; lv[3] = d.y; hv[10] = d.z; lv[4] = d.w;
-        }
-        if (L >= 5) {
-            const float4 e = row[4];
-            hv[11] = e.x; lv[5] = e.y; hv[12] = e.z; lv[6] = e.w;
-        }
-#pragma unroll
-        for (int n = 0; n <= L; ++n) {
-            float s = q6 * hv[n + 6];
-            s = fmaf(q5, hv[n + 5], s);
-            s = fmaf(q4, hv[n + 4], s);
-            s = fmaf(q3, hv[n + 3], s);
-            s = fmaf(q2, hv[n + 2], s);
-            s = fmaf(q1, hv[n + 1], s);
-            s = s + lv[n];
-            F[n] = hv[n] + s;
-        }
+        boys_taylor<L>(T, F, tab);
     } else if (T > 1e30f) {
 #pragma unroll
         for (int n = 0; n <= L; ++n) F[n] = 0.0f;

@@ -674,8 +674,33 @@ def gen_prim_body_dual(la, lb, diag, J, lines):
     lines.append(J + '    dzv[p] = (ph.z - gzh[p]) + (pl.z - gzl[p]);')
     lines.append(J + '    r2v[p] = fmaf(dxv[p], dxv[p], fmaf(dyv[p], dyv[p], dzv[p] * dzv[p]));')
     lines.append(J + '}')
-    gen_r000(la, lb, J, lines, 'oa', False, 0)
-    gen_r000(la, lb, J, lines, 'ob', True, 1)
+    # the common case of a full-range + long-range pair: slot a far and slot
+    # b near for the whole warp -- one vote, both slots in one basic block
+    ofa, ofb = 'oa%d' % (nom - 1), 'ob%d' % (nom - 1)
+    lines.append(J + 'bool farnear = true;')
+    lines.append(J + '#pragma unroll')
+    lines.append(J + 'for (int p = 0; p < PTS; ++p)')
+    lines.append(J + '    farnear = farnear && r2v[p] >= %s.z && r2v[p] < %s.z;' % (ofa, ofb))
+    lines.append(J + 'if (__all_sync(0xffffffffu, farnear)) {')
+    K = J + '    '
+    lines.append(K + '#pragma unroll')
+    lines.append(K + 'for (int p = 0; p < PTS; ++p) {')
+    lines.append(K + '    far_r000<%d>(r2v[p], %s.x, %s.y, R0[0][p]);' % (L, ofa, ofa))
+    lines.append(K + '    const float T = fmaf(ob0.x, r2v[p], ob0.y * r2v[p]);')
+    lines.append(K + '    float Fb[%d];' % (L + 1))
+    lines.append(K + '    boys_taylor<%d>(T, Fb, stab);' % L)
+    for n in range(L + 1):
+        fh = 2 + 2 * n
+        fl = fh + 1
+        ch = 'ob%d.%s' % (fh // 4, comp[fh % 4])
+        cl = 'ob%d.%s' % (fl // 4, comp[fl % 4])
+        lines.append(K + '    R0[1][p][%d] = fmaf(%s, Fb[%d], %s * Fb[%d]);'
+                     % (n, ch, n, cl, n))
+    lines.append(K + '}')
+    lines.append(J + '} else {')
+    gen_r000(la, lb, K, lines, 'oa', False, 0)
+    gen_r000(la, lb, K, lines, 'ob', True, 1)
+    lines.append(J + '}')
     lines.append(J + '#pragma unroll')
     lines.append(J + 'for (int w = 0; w < 2; ++w) {')
     lines.append(J + '#pragma unroll')
