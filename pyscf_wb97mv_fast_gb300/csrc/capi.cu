@@ -154,6 +154,7 @@ struct wb_cosx {
     cudaEvent_t fork = nullptr;
     int corder[wb::NCLASS] = {0};
     int pts[wb::NCLASS] = {0};       // points per lane of each class kernel
+    int pts2[wb::NCLASS] = {0};      // the same for the dual-omega kernels
 };
 
 namespace {
@@ -401,7 +402,8 @@ int run_g_classes_dual(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
         const int c = h->corder[i];
         const wb::ClassRange& r = h->hp.cls[c];
         if (r.pair_end <= r.pair_begin) continue;
-        const int lvl = h->pts[c] == 4 ? 2 : h->pts[c] - 1;
+        const int pc = h->dual_cls[c] ? h->pts2[c] : h->pts[c];
+        const int lvl = pc == 4 ? 2 : pc - 1;
         const int want = (a.nblk[lvl] + 3) / 4;
         WB_CUDA(cudaStreamWaitEvent(h->cstream[c], h->fork, 0));
         if (h->dual_cls[c]) {
@@ -638,6 +640,7 @@ int wb_cosx_create(const wb_basis* basis, const double origin[3],
             h->blocks_per_sm2[c] = wb::cosx_class_blocks_per_sm(c, false, smem2, true);
         }
         h->pts[c] = wb::cosx_class_pts(c);
+        h->pts2[c] = wb::cosx_class_pts(c, true);
     }
     {
         // classes that run the dual-omega kernel in a two-omega pass (one

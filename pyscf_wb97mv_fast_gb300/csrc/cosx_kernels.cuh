@@ -125,8 +125,19 @@ constexpr int class_pts(int cls) {
     const int p = (int)(v & 15);
     return p >= 4 ? 4 : (p >= 2 ? 2 : 1);
 }
-template<int LA, int LB> struct ClassPts {
-    static constexpr int value = class_pts(LA * (LA + 1) / 2 + LB);
+// the same for the dual-omega kernels: -DWB_COSX_PTS2=0x<10 hex digits>LL
+#ifndef WB_COSX_PTS2
+#define WB_COSX_PTS2 0x2222111111LL
+#endif
+constexpr int class_pts2(int cls) {
+    long long v = WB_COSX_PTS2;
+    for (int i = cls; i < kClasses - 1; ++i) v >>= 4;
+    const int p = (int)(v & 15);
+    return p >= 4 ? 4 : (p >= 2 ? 2 : 1);
+}
+template<int LA, int LB, int NW = 1> struct ClassPts {
+    static constexpr int value = NW == 2 ? class_pts2(LA * (LA + 1) / 2 + LB)
+                                         : class_pts(LA * (LA + 1) / 2 + LB);
 };
 
 template<int LA, int LB, bool FAR, bool STAGE, int NW>
@@ -138,7 +149,7 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
     constexpr int NCA = (LA + 1) * (LA + 2) / 2;
     constexpr int NA = 2 * LA + 1;
     constexpr int NB = 2 * LB + 1;
-    constexpr int PTS = ClassPts<LA, LB>::value;
+    constexpr int PTS = ClassPts<LA, LB, NW>::value;
     __shared__ float4 stab[kBoysFloat4];
     for (int i = threadIdx.x; i < kBoysFloat4; i += blockDim.x)
         stab[i] = A.boys[i];

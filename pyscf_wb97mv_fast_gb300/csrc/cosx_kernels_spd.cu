@@ -81,18 +81,18 @@ int cosx_class_blocks_per_sm(int cls, bool far, size_t smem, bool dual) {
     }
 }
 
-int cosx_class_pts(int cls) {
+int cosx_class_pts(int cls, bool dual) {
     switch (cls) {
-    case 0: return ClassPts<0, 0>::value;
-    case 1: return ClassPts<1, 0>::value;
-    case 2: return ClassPts<1, 1>::value;
-    case 3: return ClassPts<2, 0>::value;
-    case 4: return ClassPts<2, 1>::value;
-    case 5: return ClassPts<2, 2>::value;
-    case 6: return ClassPts<3, 0>::value;
-    case 7: return ClassPts<3, 1>::value;
-    case 8: return ClassPts<3, 2>::value;
-    default: return ClassPts<3, 3>::value;
+    case 0: return dual ? ClassPts<0, 0, 2>::value : ClassPts<0, 0>::value;
+    case 1: return dual ? ClassPts<1, 0, 2>::value : ClassPts<1, 0>::value;
+    case 2: return dual ? ClassPts<1, 1, 2>::value : ClassPts<1, 1>::value;
+    case 3: return dual ? ClassPts<2, 0, 2>::value : ClassPts<2, 0>::value;
+    case 4: return dual ? ClassPts<2, 1, 2>::value : ClassPts<2, 1>::value;
+    case 5: return dual ? ClassPts<2, 2, 2>::value : ClassPts<2, 2>::value;
+    case 6: return dual ? ClassPts<3, 0, 2>::value : ClassPts<3, 0>::value;
+    case 7: return dual ? ClassPts<3, 1, 2>::value : ClassPts<3, 1>::value;
+    case 8: return dual ? ClassPts<3, 2, 2>::value : ClassPts<3, 2>::value;
+    default: return dual ? ClassPts<3, 3, 2>::value : ClassPts<3, 3>::value;
     }
 }
 

@@ -74,7 +74,7 @@ cudaError_t launch_sub_stats(const double* coords, const double* weights,
                              int nvshell, const int* vs_ao0, const int* vs_nf,
                              const BlockStatsOut& out, cudaStream_t s);
 // points per lane (1, 2 or 4) of a class kernel: its blocks hold 32 * pts
-int cosx_class_pts(int cls);
+int cosx_class_pts(int cls, bool dual = false);
 cudaError_t launch_f64_to_f32(const double* in, float* out, int64_t n,
                               cudaStream_t s);
 // G = fixed-order sum of the class partial-G rows (4 source rows per AO)
