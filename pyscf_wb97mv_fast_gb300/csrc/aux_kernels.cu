@@ -371,6 +371,39 @@ __device__ __forceinline__ const double* c2s_ptr() {
     else return c_c2s3;
 }
 
+// exp(-a) for 0 <= a < 70 in FP64, table-driven after P. T. P. Tang,
+// "Table-driven implementation of the exponential function in IEEE
+// floating-point arithmetic", ACM TOMS 15 (1989) 144-157:
+//   a = n ln2/64 + r, n = rint(64 a / ln2), |r| <= ln2/128, r from a
+//   two-constant (Cody-Waite) reduction with n C1 exact (C1 has 40
+//   significant bits, n <= 6464);
+//   exp(-a) = 2^-(n >> 6) 2^-((n & 63)/64) exp(-r), the middle factor from
+//   a 64-entry table, exp(-r) by its degree-5 Taylor polynomial (truncation
+//   below 4e-17), the power of two applied to the exponent field.
+// About 2 ulp; the AO values feed 42-bit splits.
+__constant__ double c_exp2m[64];            // 2^(-j/64), j = 0..63
+
+__device__ __forceinline__ double exp_neg(const double a,
+                                          const double* __restrict__ tab) {
+    const double C1 = 0.010830424696237628;     // ln2/64, high 40 bits
+    const double C2 = 1.1517191508074686e-14;   // ln2/64 - C1
+    const double t = a * 92.33248261689366;      // 64 / ln2
+    const int n = __double2int_rn(t);
+    const double dn = (double)n;
+    double r = fma(-dn, C1, a);
+    r = fma(-dn, C2, r);
+    const double x = -r;
+    double p = fma(x, 1.0 / 120.0, 1.0 / 24.0);
+    p = fma(x, p, 1.0 / 6.0);
+    p = fma(x, p, 0.5);
+    p = fma(x, p, 1.0);
+    p = fma(x, p, 1.0);
+    // 2^-(n >> 6) 2^-(j/64): subtract from the table entry's exponent field
+    const double tj = tab[n & 63];
+    const long long bits = __double_as_longlong(tj) - ((long long)(n >> 6) << 52);
+    return __longlong_as_double(bits) * p;
+}
+
 __device__ __forceinline__ double ipow(double x, int n) {
     double r = 1.0;
     for (int i = 0; i < n; ++i) r *= x;
@@ -380,7 +413,7 @@ __device__ __forceinline__ double ipow(double x, int n) {
 template<int L>
 __device__ __forceinline__ void ao_shell(const AoArgs& A, int sh, int64_t g,
                                          double dx, double dy, double dz,
-                                         double r2) {
+                                         double r2, const double* etab) {
     constexpr int NC = (L + 1) * (L + 2) / 2, NS = 2 * L + 1;
     double mono[NC];
     {
@@ -403,7 +436,7 @@ __device__ __forceinline__ void ao_shell(const AoArgs& A, int sh, int64_t g,
             // exp(-70) ~ 4e-31: such a primitive is zero at FP64 parity with
             // any AO value of order one; skipping it avoids the FP64 exp
             const double a = ex[k] * r2;
-            if (a < 70.0) rad += co[k * nc + ci] * exp(-a);
+            if (a < 70.0) rad += co[k * nc + ci] * exp_neg(a, etab);
         }
 #pragma unroll
         for (int m = 0; m < NS; ++m) {
@@ -416,6 +449,9 @@ __device__ __forceinline__ void ao_shell(const AoArgs& A, int sh, int64_t g,
 }
 
 __global__ void ao_eval_kernel(const AoArgs A) {
+    __shared__ double etab[64];
+    if (threadIdx.x < 64) etab[threadIdx.x] = c_exp2m[threadIdx.x];
+    __syncthreads();
     const int sh = blockIdx.y;
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= A.ld) return;
@@ -430,10 +466,10 @@ __global__ void ao_eval_kernel(const AoArgs A) {
     const double dz = A.coords[g * 3 + 2] - A.sh_ctr[sh * 3 + 2];
     const double r2 = dx * dx + dy * dy + dz * dz;
     switch (l) {
-    case 0: ao_shell<0>(A, sh, g, dx, dy, dz, r2); break;
-    case 1: ao_shell<1>(A, sh, g, dx, dy, dz, r2); break;
-    case 2: ao_shell<2>(A, sh, g, dx, dy, dz, r2); break;
-    default: ao_shell<3>(A, sh, g, dx, dy, dz, r2); break;
+    case 0: ao_shell<0>(A, sh, g, dx, dy, dz, r2, etab); break;
+    case 1: ao_shell<1>(A, sh, g, dx, dy, dz, r2, etab); break;
+    case 2: ao_shell<2>(A, sh, g, dx, dy, dz, r2, etab); break;
+    default: ao_shell<3>(A, sh, g, dx, dy, dz, r2, etab); break;
     }
 }
 
@@ -444,7 +480,7 @@ __global__ void ao_eval_kernel(const AoArgs A) {
 template<int L>
 __device__ __forceinline__ void ao_shell_d1(const AoArgs& A, int sh, int64_t g,
                                             double dx, double dy, double dz,
-                                            double r2) {
+                                            double r2, const double* etab) {
     constexpr int NC = (L + 1) * (L + 2) / 2, NS = 2 * L + 1;
     double px[L + 2], py[L + 2], pz[L + 2];
     px[0] = py[0] = pz[0] = 1.0;
@@ -463,7 +499,7 @@ __device__ __forceinline__ void ao_shell_d1(const AoArgs& A, int sh, int64_t g,
         for (int k = 0; k < np; ++k) {
             const double a = ex[k] * r2;
             if (a >= 70.0) continue;          // below ~1e-30, see ao_shell
-            const double e = co[k * nc + ci] * exp(-a);
+            const double e = co[k * nc + ci] * exp_neg(a, etab);
             rad0 += e;
             rad1 += -2.0 * ex[k] * e;
         }
@@ -504,6 +540,9 @@ __device__ __forceinline__ void ao_shell_d1(const AoArgs& A, int sh, int64_t g,
 }
 
 __global__ void ao_eval_d1_kernel(const AoArgs A) {
+    __shared__ double etab[64];
+    if (threadIdx.x < 64) etab[threadIdx.x] = c_exp2m[threadIdx.x];
+    __syncthreads();
     const int sh = blockIdx.y;
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= A.ld) return;
@@ -521,10 +560,10 @@ __global__ void ao_eval_d1_kernel(const AoArgs A) {
     const double dz = A.coords[g * 3 + 2] - A.sh_ctr[sh * 3 + 2];
     const double r2 = dx * dx + dy * dy + dz * dz;
     switch (l) {
-    case 0: ao_shell_d1<0>(A, sh, g, dx, dy, dz, r2); break;
-    case 1: ao_shell_d1<1>(A, sh, g, dx, dy, dz, r2); break;
-    case 2: ao_shell_d1<2>(A, sh, g, dx, dy, dz, r2); break;
-    default: ao_shell_d1<3>(A, sh, g, dx, dy, dz, r2); break;
+    case 0: ao_shell_d1<0>(A, sh, g, dx, dy, dz, r2, etab); break;
+    case 1: ao_shell_d1<1>(A, sh, g, dx, dy, dz, r2, etab); break;
+    case 2: ao_shell_d1<2>(A, sh, g, dx, dy, dz, r2, etab); break;
+    default: ao_shell_d1<3>(A, sh, g, dx, dy, dz, r2, etab); break;
     }
 }
 
@@ -543,6 +582,10 @@ cudaError_t launch_ao_eval(const AoArgs& a, cudaStream_t s) {
 }
 
 // c2s tables filled by the host (same formula as the host pair builder)
+cudaError_t upload_exp_table(const double* t64) {
+    return cudaMemcpyToSymbol(c_exp2m, t64, sizeof(double) * 64);
+}
+
 cudaError_t upload_c2s_tables(const double* t0, const double* t1,
                               const double* t2, const double* t3) {
     cudaError_t e;

@@ -90,6 +90,10 @@ int upload_constants() {
     for (int l = 0; l < 4; ++l)
         for (size_t i = 0; i < c[l].size(); ++i) f[l][i] = (float)c[l][i];
     WB_CUDA(wb::upload_c2s_f(&f[0][0]));
+    double t64[64];
+    for (int j = 0; j < 64; ++j)
+        t64[j] = (double)std::exp2l(-(long double)j / 64.0L);   // rounded once
+    WB_CUDA(wb::upload_exp_table(t64));
     return WB_OK;
 }
 

@@ -43,6 +43,8 @@ cudaError_t launch_ao_eval_d1(const AoArgs& a, cudaStream_t s);
 cudaError_t upload_c2s_tables(const double* t0, const double* t1,
                               const double* t2, const double* t3);
 cudaError_t upload_c2s_f(const float* all /* 4 x 70 */);
+// 2^(-j/64), j = 0..63, for the AO kernels' exp
+cudaError_t upload_exp_table(const double* t64);
 
 // class ranges and record layout for launch_pack_records (classes with no
 // primitive pairs have pp_begin == pp_end)
