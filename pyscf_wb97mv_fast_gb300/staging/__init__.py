@@ -1,1 +1,1 @@
-"""Subpackage of pyscf_wb97mv_fast_gb300."""
+"""Staged SCF driver (``schedule.StagedSCF``, ``schedule.run_staged``)."""

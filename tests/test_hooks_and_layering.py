@@ -138,7 +138,8 @@ def test_oom_retry_halves_tile_then_reraises():
 
 def test_import_has_no_side_effects():
     code = ('import sys, pyscf_wb97mv_fast_gb300, pyscf_wb97mv_fast_gb300.gpu.install, '
-            'pyscf_wb97mv_fast_gb300.gpu.sgx_k;'
+            'pyscf_wb97mv_fast_gb300.gpu.sgx_k, pyscf_wb97mv_fast_gb300.core.sgx_patch, '
+            'pyscf_wb97mv_fast_gb300.staging.schedule;'
             'print(any(m == "pyscf" or m.startswith("pyscf.") for m in sys.modules),'
             ' "torch" in sys.modules)')
     out = subprocess.run([sys.executable, '-c', code], capture_output=True,
