@@ -19,9 +19,11 @@ algorithmic flop model of the kept (sub-block, shell pair) tasks
   e2e    : host (pinned) coordinates, weights and density matrix copied in
            and both K matrices copied out every step, through
            GpuKBuilder/get_k_only_gpu-equivalent calls
-  roofline: the fused G kernels alone (wb_cosx_g), CUDA events on the
-           launching stream, against the FP32 FMA peak measured in the same
-           run (wb_fp32_fma_probe)
+  roofline: the G phase alone (wb_cosx_g_multi: block statistics, the
+           fused screen + G class kernels of both omegas in one two-omega
+           pass, the class-buffer sums), CUDA events on the launching
+           stream, against the FP32 FMA peak measured in the same run
+           (wb_fp32_fma_probe)
   cpu_baseline: the FP64 OpenMP oracle on a bounded sample of the points
 
 --impl reference times the reference's CPU path for this workload on the
@@ -390,20 +392,21 @@ def main():
     h2d = c_h.numel() * 8 + w_h.numel() * 8 + d_h.numel() * 8
     d2h = sum(k.numel() * 8 for k in k_h)
 
-    # -- roofline of the fused G kernels (wb_cosx_g on the same F) -----------------
+    # -- roofline of the G phase (wb_cosx_g_multi on the same F) -----------------
     n = g.size
     ld = round32(n)
     X = eng.ao_eval(coords_d)
     F = eng.ozaki_f(X, qd_d)                    # fl32(X QD), AO-major
-    Gt = torch.empty((mol.nao, ld), dtype=torch.float32, device=dev)
-    g_flops = 0.0
-    for w in OMEGAS:
-        eng.g(coords_d, w_d, F, w, TILE_TOL, out=Gt, stats=True)
-        g_flops += eng.last_stats['model_flops']
+    Gt = torch.empty((len(OMEGAS), mol.nao, ld), dtype=torch.float32,
+                     device=dev)
+    # both omegas in one call, as in the step: block statistics once, the
+    # omega pair in one pass of the two-omega class kernels
+    eng.g_multi(coords_d, w_d, F, OMEGAS, TILE_TOL, out=Gt, stats=True)
+    g_flops = eng.last_stats['model_flops']
+    g_launches = eng.last_stats['kernel_launches']
 
     def g_step():
-        for w in OMEGAS:
-            eng.g(coords_d, w_d, F, w, TILE_TOL, out=Gt, stats=False)
+        eng.g_multi(coords_d, w_d, F, OMEGAS, TILE_TOL, out=Gt, stats=False)
     t_g = timed(g_step, max(2, args.steps), 1)
     del X
     peak = fp32_peak(torch)
@@ -415,8 +418,9 @@ def main():
                 'traffic_source': prof.get('source') if prof else None,
                 'peak_source': 'measured in this run: wb_fp32_fma_probe '
                                '(FFMA-only kernel, all SMs)',
-                'kernel': 'fused screen + G kernels (10 class launches) of '
-                          'both omegas',
+                'kernel': 'block statistics + fused screen + G class kernels '
+                          '+ class-buffer sums of both omegas in one call '
+                          '(wb_cosx_g_multi, %d launches)' % g_launches,
                 'ms': t_g * 1e3}
     mp = measured_peaks()
     if mp:

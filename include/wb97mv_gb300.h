@@ -158,6 +158,20 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
               float* g_out, void* workspace, size_t workspace_bytes,
               void* stream, wb_cosx_stats* stats);
 
+/* wb_cosx_g for nomega omegas and one F: the block statistics are formed
+ * once, and omegas are taken in pairs by the two-omega class kernels (one
+ * screen, F loads and distances per pair of omegas), as in
+ * wb_cosx_get_k_multi.  g_out holds nomega (nao, ldp) FP32 arrays, omega j
+ * at g_out + j nao ldp, each equal to what wb_cosx_g returns for
+ * omegas[j].  Same workspace as wb_cosx_g.  Replaces the _tasks + _launch
+ * part (gpu/sgx_k.py:754-781, :813-843) of the reference's two K builds of
+ * one SCF cycle. */
+int wb_cosx_g_multi(wb_cosx* h, const double* coords, const double* weights,
+                    int64_t npts, const float* f, int nomega,
+                    const double* omegas, double tile_tol, float* g_out,
+                    void* workspace, size_t workspace_bytes, void* stream,
+                    wb_cosx_stats* stats);
+
 /* The two FP64-accurate GEMMs of the K build on the bf16 tensor cores
  * (Ozaki split, WB_K_GEMM_OZAKI_BF16), callable alone:
  *   wb_cosx_ozaki_f: f_out (nao, ld) FP32 = fl32(X QD), x (nao, ld) FP64

@@ -37,7 +37,8 @@ NCLASS = 10
 
 EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_cosx_export_pairs', 'wb_cosx_workspace_bytes',
-            'wb_cosx_get_k', 'wb_cosx_get_k_multi', 'wb_cosx_g', 'wb_ao_eval',
+            'wb_cosx_get_k', 'wb_cosx_get_k_multi', 'wb_cosx_g',
+            'wb_cosx_g_multi', 'wb_ao_eval',
             'wb_ao_eval_deriv1',
             'wb_int3c1e_dense',
             'wb_boys_fp32', 'wb_boys_f64_host', 'wb_vv10_kernel_sum',
@@ -129,6 +130,9 @@ def _declare(lib):
                                        ctypes.POINTER(WbCosxStats)]),
         'wb_cosx_g': (_INT, [_P, _P, _P, _I64, _P, _D, _D, _P, _P,
                              ctypes.c_size_t, _P, ctypes.POINTER(WbCosxStats)]),
+        'wb_cosx_g_multi': (_INT, [_P, _P, _P, _I64, _P, _INT, _P, _D, _P, _P,
+                                   ctypes.c_size_t, _P,
+                                   ctypes.POINTER(WbCosxStats)]),
         'wb_ao_eval': (_INT, [_P, _P, _I64, _P, _P]),
         'wb_ao_eval_deriv1': (_INT, [_P, _P, _I64, _P, _P]),
         'wb_int3c1e_dense': (_INT, [_P, _P, _I64, _D, _P, _P]),

@@ -212,6 +212,39 @@ class CosxEngine:
             self.last_stats = st.as_dict()
         return out
 
+    def g_multi(self, coords_rel, weights, f, omegas, tile_tol=0.0, out=None,
+                stats=True):
+        """G for several omegas from one F: (len(omegas), nao, ld) FP32,
+        out[j] equal to g(..., omegas[j]); omega pairs share one pass of
+        the two-omega class kernels."""
+        torch = _torch()
+        om = [float(w) for w in omegas]
+        if not om:
+            raise ValueError('omegas is empty')
+        npts = int(coords_rel.shape[0])
+        ld = round32(npts)
+        if f.shape != (self.nao, ld) or f.dtype != torch.float32:
+            raise ValueError('f must be (nao, %d) float32' % ld)
+        nbytes = self.workspace_bytes(npts)
+        ws = self.workspace(nbytes)
+        if out is None:
+            out = torch.empty((len(om), self.nao, ld), dtype=torch.float32,
+                              device=self.device)
+        if tuple(out.shape) != (len(om), self.nao, ld) or not out.is_contiguous():
+            raise ValueError('out must be a contiguous (%d, nao, %d) tensor'
+                             % (len(om), ld))
+        st = _native.WbCosxStats() if stats else None
+        arr = (_native.ctypes.c_double * len(om))(*om)
+        _native.check(_native.lib().wb_cosx_g_multi(
+            self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
+            _native.ptr(f.contiguous()), len(om), arr, float(tile_tol),
+            _native.ptr(out), _native.ptr(ws), nbytes, self._stream(),
+            _native.ctypes.byref(st) if st is not None else None),
+            'wb_cosx_g_multi')
+        if st is not None:
+            self.last_stats = st.as_dict()
+        return out
+
     def ozaki_f(self, X, qd):
         """F (nao, ld) FP32 = fl32(X QD) through the bf16 Ozaki split."""
         torch = _torch()

@@ -963,6 +963,60 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
                       stats, launches);
 }
 
+int wb_cosx_g_multi(wb_cosx* h, const double* coords, const double* weights,
+                    int64_t npts, const float* f, int nomega,
+                    const double* omegas, double tile_tol, float* g_out,
+                    void* workspace, size_t workspace_bytes, void* stream,
+                    wb_cosx_stats* stats) {
+    if (!h || !f || !g_out || npts <= 0 || !coords || !weights || nomega < 1 ||
+        !omegas)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_g_multi: bad arguments");
+    for (int j = 0; j < nomega; ++j)
+        if (!(omegas[j] >= 0.0))
+            return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_g_multi: omega must be >= 0");
+    if (!(tile_tol >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_g_multi: tile_tol must be >= 0");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t ldt = round32(npts);
+    const WsLayout L = ws_layout(h, ldt, false);
+    if (!workspace || workspace_bytes < L.total)
+        return fail(WB_ERR_WORKSPACE, "wb_cosx_g_multi: workspace needs " +
+                                          std::to_string(L.total) + " bytes");
+    WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.counters), 0,
+                            sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+    int launches = 1;
+    int st = tile_prep(h, coords, weights, npts, ldt, f, workspace, L, s, &launches);
+    if (st != WB_OK) return st;
+    const size_t gsz = (size_t)h->hp.nao * ldt;
+    int64_t ntasks = 0;
+    // the omega loop of wb_cosx_get_k_multi: a dual pass per omega pair
+    for (int j = 0; j < nomega;) {
+        if (h->dual_ok && j + 1 < nomega) {
+            int ja = j, jb = j + 1;
+            if (omegas[jb] < omegas[ja]) std::swap(ja, jb);
+            if ((st = prepare_omega_dual(h, omegas[ja], omegas[jb], workspace, L,
+                                         s)) != WB_OK)
+                return st;
+            launches += 3;
+            if ((st = run_g_classes_dual(h, npts, ldt, f, g_out + gsz * ja,
+                                         g_out + gsz * jb, omegas[ja], omegas[jb],
+                                         tile_tol, workspace, L, s, &launches)) != WB_OK)
+                return st;
+            ntasks += 2 * (ldt / 32) * (int64_t)h->hp.npairs;
+            j += 2;
+            continue;
+        }
+        if ((st = prepare_omega(h, omegas[j], workspace, L, s)) != WB_OK) return st;
+        launches += 2;
+        if ((st = run_g_classes(h, npts, ldt, f, g_out + gsz * j, omegas[j], tile_tol,
+                                workspace, L, s, &launches)) != WB_OK)
+            return st;
+        ntasks += (ldt / 32) * (int64_t)h->hp.npairs;
+        j += 1;
+    }
+    return read_stats(h, workspace, L, ntasks, s, stats, launches);
+}
+
 size_t wb_ozaki_workspace_bytes(int nao, int64_t ld) {
     if (nao <= 0 || ld <= 0) return 0;
     return std::max(wb::ozaki_f_bytes(nao, ld), wb::ozaki_k_bytes(nao, ld));

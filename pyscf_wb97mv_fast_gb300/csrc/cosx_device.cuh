@@ -46,6 +46,20 @@ __device__ __forceinline__ void cosx_end(float* __restrict__ Gp, const int ga0,
                                          const int ld, const bool ok,
                                          const float* Xa);
 
+// G_B += y for the ket rows of a task: a reduction in L2 (red.global.add,
+// no value returned), so the task neither waits for nor holds the old
+// value.  Every element of a class buffer has one writer lane, whose
+// operations on one address take effect in program order: the sum order,
+// and so the result, is the same as a load-add-store (the reduction
+// flushes subnormal results to zero).  -DWB_COSX_GB_RED=0 selects the
+// load-add-store.
+#ifndef WB_COSX_GB_RED
+#define WB_COSX_GB_RED 1
+#endif
+__device__ __forceinline__ void gb_add(float* p, const float y) {
+    atomicAdd(p, y);
+}
+
 }  // namespace wb
 
 namespace wb {

@@ -499,10 +499,13 @@ def gen_class(la, lb, diag, far, stage=False):
     lines.append(I + 'for (int p = 0; p < PTS; ++p) {')
     J = I * 2
     if not diag:
-        # G_B read early: its latency overlaps the primitive loop
+        # WB_COSX_GB_RED = 0: G_B read early (its latency overlaps the
+        # primitive loop), added to and stored at the end
+        lines.append('#if !WB_COSX_GB_RED')
         for nu in range(nb):
             lines.append(J + 'gbo[p][%d] = Gp[p][(long long)(gb0 + %d) * ld];'
                          % (nu, nu))
+        lines.append('#endif')
         for nu in range(nb):
             lines.append(J + 'const float fb%d = fb[p * %d + %d];' % (nu, nb, nu))
         gen_transform_in(lb, 'fb', 'h0_', J, lines)
@@ -558,8 +561,13 @@ def gen_class(la, lb, diag, far, stage=False):
         gen_transform_out(lb, 'Y', 'gy', J, lines)
         lines.append(J + 'if (ok[p]) {')
         for nu in range(nb):
+            lines.append('#if WB_COSX_GB_RED')
+            lines.append(J + '    gb_add(Gp[p] + (long long)(gb0 + %d) * ld, gy%d);'
+                         % (nu, nu))
+            lines.append('#else')
             lines.append(J + '    Gp[p][(long long)(gb0 + %d) * ld] = gbo[p][%d] + gy%d;'
                          % (nu, nu, nu))
+            lines.append('#endif')
         lines.append(J + '}')
         for c in range(nca):
             lines.append(J + 'Xa[p * %d + %d] = Xv[p][%d];' % (nca, c, c))
@@ -754,9 +762,11 @@ def gen_class_dual(la, lb, diag):
     if not diag:
         lines.append(J + '#pragma unroll')
         lines.append(J + 'for (int w = 0; w < 2; ++w) {')
+        lines.append('#if !WB_COSX_GB_RED')
         for nu in range(nb):
             lines.append(J + '    gbo[w][p][%d] = Gp[w * PTS + p][(long long)(gb0 + %d) * ld];'
                          % (nu, nu))
+        lines.append('#endif')
         for c in range(nca):
             lines.append(J + '    Xv[w][p][%d] = Xa[(w * PTS + p) * %d + %d];' % (c, nca, c))
         lines.append(J + '}')
@@ -791,8 +801,13 @@ def gen_class_dual(la, lb, diag):
         gen_transform_out(lb, 'Y', 'gy', J, lines)
         lines.append(J + 'if (ok[p]) {')
         for nu in range(nb):
+            lines.append('#if WB_COSX_GB_RED')
+            lines.append(J + '    gb_add(Gp[w * PTS + p] + (long long)(gb0 + %d) * ld, gy%d);'
+                         % (nu, nu))
+            lines.append('#else')
             lines.append(J + '    Gp[w * PTS + p][(long long)(gb0 + %d) * ld] = gbo[w][p][%d] + gy%d;'
                          % (nu, nu, nu))
+            lines.append('#endif')
         lines.append(J + '}')
         for c in range(nca):
             lines.append(J + 'Xa[(w * PTS + p) * %d + %d] = Xv[w][p][%d];' % (nca, c, c))

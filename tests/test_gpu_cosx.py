@@ -290,6 +290,16 @@ def test_multi_omega_build_matches_single_builds():
         kept += eng.last_stats['pairs_kept']
         assert torch.equal(Km[j], Ks), om
     assert st_m['pairs_kept'] == kept
+    # the G-only entry point: one pass of the two-omega kernels per omega
+    # pair, bitwise the single-omega G, the same tasks kept
+    F = eng.ozaki_f(eng.ao_eval(c), qd)
+    Gm = eng.g_multi(c, w, F, oms, 1e-11)
+    kept_gm, kept_g = eng.last_stats['pairs_kept'], 0
+    for j, om in enumerate(oms):
+        Gs = eng.g(c, w, F, om, 1e-11)
+        kept_g += eng.last_stats['pairs_kept']
+        assert torch.equal(Gm[j], Gs), om
+    assert kept_gm == kept_g
     # builder: omega 0 builds both, omega 0.3 comes from the pending set
     g = build_grids(mol, level=0)
     sgx = SyntheticSGX(mol, g)
