@@ -345,6 +345,48 @@ __global__ void gsum_kernel(const float* __restrict__ gc,
     *reinterpret_cast<float4*>(G + (int64_t)mu * ld + i) = acc;
 }
 
+// Longest-processing-time order of the point blocks of each class (one
+// CTA per class): a counting sort of the blocks by their measured cost in
+// 2^(1/8) steps, costliest first.  Each kernel hands its blocks out in this
+// order, so the last blocks taken -- the tail of the launch -- are the
+// cheap ones.  Within a step the order is arbitrary; results do not depend
+// on it (a block's G columns are written by one warp in fixed pair order).
+__global__ void block_order_kernel(const BlockOrderArgs P) {
+    const int c = blockIdx.x;
+    const int n = P.n[c];
+    if (n <= 0) return;
+    const float* __restrict__ cost = P.cost + (long long)c * P.stride;
+    int* __restrict__ order = P.order + (long long)c * P.stride;
+    __shared__ unsigned cnt[256];
+    for (int b = threadIdx.x; b < 256; b += blockDim.x) cnt[b] = 0u;
+    __syncthreads();
+    auto bucket = [](float x) {
+        // 255 - 8 log2(1 + cost), clamped: bucket 0 holds the costliest
+        const float l = 8.0f * __log2f(1.0f + fmaxf(x, 0.0f));
+        const int b = 255 - (int)fminf(l, 255.0f);
+        return b < 0 ? 0 : b;
+    };
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        atomicAdd(&cnt[bucket(cost[i])], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned run = 0;
+        for (int b = 0; b < 256; ++b) {
+            const unsigned t = cnt[b];
+            cnt[b] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        order[atomicAdd(&cnt[bucket(cost[i])], 1u)] = i;
+}
+
+cudaError_t launch_block_order(const BlockOrderArgs& P, cudaStream_t s) {
+    block_order_kernel<<<kClasses, 1024, 0, s>>>(P);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_gsum(const float* gc, const int4* src, int nao, int64_t ld,
                         float* G, cudaStream_t s) {
     if (nao <= 0 || ld <= 0) return cudaSuccess;

@@ -159,6 +159,13 @@ struct wb_cosx {
     int corder[wb::NCLASS] = {0};
     int pts[wb::NCLASS] = {0};       // points per lane of each class kernel
     int pts2[wb::NCLASS] = {0};      // the same for the dual-omega kernels
+    // block order (costliest first) learnt from the previous launch on a
+    // grid of the same padded size: per class, stride floats of block
+    // costs and ints of order; bo_n[c] = blocks of the order held (0: none)
+    float* bcost = nullptr;
+    int* border = nullptr;
+    int64_t bo_stride = 0, bo_ld = -1;
+    int bo_n[wb::NCLASS] = {0};
 };
 
 namespace {
@@ -347,13 +354,79 @@ int tile_prep(wb_cosx* h, const double* coords, const double* weights,
     return WB_OK;
 }
 
+#ifndef WB_COSX_BLOCK_ORDER
+#define WB_COSX_BLOCK_ORDER 1
+#endif
+
+// blocks of the class kernel that runs for class c (its points per lane)
+int class_nblk(const wb_cosx* h, const wb::CosxArgs& a, int c, bool dual) {
+    const int pc = dual ? h->pts2[c] : h->pts[c];
+    return a.nblk[pc == 4 ? 2 : pc - 1];
+}
+
+// cost / order arrays for a tile of ldt points (grown on demand; a new
+// padded size drops the orders held), then the per-class pointers of a:
+// every class records its block costs, and takes its blocks in the held
+// order when that order covers the same blocks
+int block_order_args(wb_cosx* h, int64_t ldt, wb::CosxArgs& a,
+                     const bool* dual, cudaStream_t s) {
+    if (!WB_COSX_BLOCK_ORDER) return WB_OK;
+    const int64_t stride = (ldt + 31) / 32;
+    if (stride > h->bo_stride) {
+        WB_CUDA(cudaStreamSynchronize(s));
+        if (h->bcost) cudaFree(h->bcost);
+        if (h->border) cudaFree(h->border);
+        h->bcost = nullptr;
+        h->border = nullptr;
+        h->bo_stride = 0;
+        WB_CUDA(cudaMalloc(&h->bcost, sizeof(float) * wb::NCLASS * stride));
+        WB_CUDA(cudaMalloc(&h->border, sizeof(int) * wb::NCLASS * stride));
+        h->bo_stride = stride;
+        h->bo_ld = -1;
+    }
+    if (h->bo_ld != ldt) {
+        for (int c = 0; c < wb::NCLASS; ++c) h->bo_n[c] = 0;
+        h->bo_ld = ldt;
+    }
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        a.bcost[c] = h->bcost + c * h->bo_stride;
+        a.border[c] = h->bo_n[c] == class_nblk(h, a, c, dual[c])
+                          ? h->border + c * h->bo_stride : nullptr;
+    }
+    return WB_OK;
+}
+
+// after the class launches: the order of the next launch from the costs
+// just recorded (classes that ran)
+int block_order_update(wb_cosx* h, const wb::CosxArgs& a, const bool* ran,
+                       const bool* dual, cudaStream_t s, int* launches) {
+    if (!WB_COSX_BLOCK_ORDER) return WB_OK;
+    wb::BlockOrderArgs P;
+    P.cost = h->bcost;
+    P.order = h->border;
+    P.stride = h->bo_stride;
+    for (int c = 0; c < wb::NCLASS; ++c)
+        P.n[c] = ran[c] ? class_nblk(h, a, c, dual[c]) : 0;
+    WB_CUDA(wb::launch_block_order(P, s));
+    for (int c = 0; c < wb::NCLASS; ++c)
+        if (ran[c]) h->bo_n[c] = P.n[c];
+    *launches += 1;
+    return WB_OK;
+}
+
 // the class launches of one tile (after tile_prep and prepare_omega); F and
 // G are (nao, ldt) AO-major.  The classes fill their own partial-G buffers
 // concurrently; G is their fixed-order sum.
 int run_g_classes(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
                   float* G, double omega, double tile_tol, void* ws,
                   const WsLayout& L, cudaStream_t s, int* launches) {
-    const wb::CosxArgs a = make_args(h, ws, L, ldt, npts_t, F, tile_tol);
+    wb::CosxArgs a = make_args(h, ws, L, ldt, npts_t, F, tile_tol);
+    const bool single[wb::NCLASS] = {};
+    bool ran[wb::NCLASS] = {};
+    {
+        const int st = block_order_args(h, ldt, a, single, s);
+        if (st != WB_OK) return st;
+    }
     // the far-field R000 variant pays where T = theta p r^2 >= 36 is common:
     // the full-range operator (theta = 1); long-range omegas keep T small
     const bool far = omega == 0.0;
@@ -375,7 +448,12 @@ int run_g_classes(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
                                             h->stage_smem[c]));
         WB_CUDA(cudaEventRecord(h->cdone[c], h->cstream[c]));
         WB_CUDA(cudaStreamWaitEvent(s, h->cdone[c], 0));
+        ran[c] = true;
         *launches += 1;
+    }
+    {
+        const int st = block_order_update(h, a, ran, single, s, launches);
+        if (st != WB_OK) return st;
     }
     WB_CUDA(wb::launch_gsum(at<float>(ws, L.gcls), h->gsrc, h->hp.nao, ldt, G, s));
     *launches += 1;
@@ -389,7 +467,12 @@ int run_g_classes_dual(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
                        float* Ga, float* Gb, double omega_a, double omega_b,
                        double tile_tol, void* ws, const WsLayout& L,
                        cudaStream_t s, int* launches) {
-    const wb::CosxArgs a = make_args(h, ws, L, ldt, npts_t, F, tile_tol);
+    wb::CosxArgs a = make_args(h, ws, L, ldt, npts_t, F, tile_tol);
+    bool ran[wb::NCLASS] = {};
+    {
+        const int st = block_order_args(h, ldt, a, h->dual_cls, s);
+        if (st != WB_OK) return st;
+    }
     // slot b of the single-omega kernels: its records, buffers, counters
     wb::CosxArgs b = a;
     for (int c = 0; c < wb::NCLASS; ++c) {
@@ -432,6 +515,11 @@ int run_g_classes_dual(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
         }
         WB_CUDA(cudaEventRecord(h->cdone[c], h->cstream[c]));
         WB_CUDA(cudaStreamWaitEvent(s, h->cdone[c], 0));
+        ran[c] = true;
+    }
+    {
+        const int st = block_order_update(h, a, ran, h->dual_cls, s, launches);
+        if (st != WB_OK) return st;
     }
     WB_CUDA(wb::launch_gsum(at<float>(ws, L.gcls), h->gsrc, h->hp.nao, ldt, Ga, s));
     WB_CUDA(wb::launch_gsum(at<float>(ws, L.gcls2), h->gsrc, h->hp.nao, ldt, Gb, s));
@@ -694,6 +782,8 @@ int wb_cosx_destroy(wb_cosx* h) {
     }
     if (h->fork) cudaEventDestroy(h->fork);
     if (h->block) cudaFree(h->block);
+    if (h->bcost) cudaFree(h->bcost);
+    if (h->border) cudaFree(h->border);
     delete h;
     return WB_OK;
 }

@@ -55,6 +55,12 @@ struct CosxArgs {
     const int* pnint;          // per pair nfi * nfj
     unsigned long long* counters;  // per class: kept, flops, ints (3 each)
     int* work;                 // per class dynamic sub-block counter
+    // block order: the i-th block a class kernel takes is border[c][i]
+    // (a permutation of its blocks, costliest first; nullptr = ascending),
+    // and bcost[c][blk] receives the model flops of the tasks block blk
+    // kept (the order of the next call on the same grid)
+    const int* border[kClasses];
+    float* bcost[kClasses];
 };
 
 }  // namespace wb

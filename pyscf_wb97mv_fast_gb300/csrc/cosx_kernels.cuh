@@ -172,11 +172,19 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
     const float* __restrict__ blk_msh = A.blk_msh[LVL];
     const int nblk = A.nblk[LVL];
     unsigned long long kept = 0, flops = 0, ints = 0;
+    const int* __restrict__ order = A.border[CLS];
     for (;;) {
-        int blk = 0;
-        if (lane == 0) blk = atomicAdd(A.work + CLS, 1);
-        blk = __shfl_sync(0xffffffffu, blk, 0);
-        if (blk >= nblk) break;
+        int item = 0;
+        if (lane == 0) item = atomicAdd(A.work + CLS, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nblk) break;
+        // costliest blocks first (the order is a permutation of 0 .. nblk-1)
+        int blk = item;
+        if (order) {
+            const int b = order[item];
+            blk = b >= 0 && b < nblk ? b : item;
+        }
+        unsigned long long bfl = 0;     // model flops kept in this block
         // the lane's points: blk * 32 PTS + 32 p + lane (clamped to the
         // arrays; ok marks the ones that exist)
         const float* __restrict__ Fp[PTS];
@@ -365,7 +373,10 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
             }
             // model flops / integrals of the kept tasks of this chunk
             if (keep) {
-                flops += (unsigned long long)A.pflops[k] * nvalid * NW;
+                const unsigned long long fk =
+                    (unsigned long long)A.pflops[k] * nvalid * NW;
+                flops += fk;
+                bfl += fk;
                 ints += (unsigned long long)A.pnint[k] * nvalid * NW;
             }
         }
@@ -374,6 +385,8 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
             for (int c = 0; c < NW * PTS; ++c)
                 cosx_end<LA>(Gp[c], ga0, ld, ok[c % PTS], Xa + c * NCA);
         }
+        for (int o = 16; o > 0; o >>= 1) bfl += __shfl_xor_sync(0xffffffffu, bfl, o);
+        if (lane == 0 && A.bcost[CLS]) A.bcost[CLS][blk] = (float)bfl;
     }
     // lane 0 counted the tasks (every lane runs every task) in units of the
     // 32-point sub-blocks they cover; every lane counted the flops /

@@ -80,6 +80,16 @@ int cosx_class_pts(int cls, bool dual = false);
 cudaError_t launch_f64_to_f32(const double* in, float* out, int64_t n,
                               cudaStream_t s);
 // G = fixed-order sum of the class partial-G rows (4 source rows per AO)
+// block order of each class from the per-block costs of a previous launch
+// (cost / order: kClasses rows of stride floats / ints; n[c] blocks of class
+// c, 0 = leave the class alone)
+struct BlockOrderArgs {
+    const float* cost;
+    int* order;
+    long long stride;
+    int n[kClasses];
+};
+cudaError_t launch_block_order(const BlockOrderArgs& P, cudaStream_t s);
 cudaError_t launch_gsum(const float* gc, const int4* src, int nao, int64_t ld,
                         float* G, cudaStream_t s);
 cudaError_t launch_weight_g(const float* G, const double* w, int64_t npts,
