@@ -197,6 +197,54 @@ def cpu_baseline(mol, g, dm, engine, budget_s=15.0):
             'seconds': dt}
 
 
+class SlaterGgaTau:
+    """Host stand-in for the functional of the semilocal flow timing
+    (PySCF's libxc is not installed): Slater exchange plus a gradient and a
+    kinetic-energy-density term, libxc convention."""
+
+    def eval(self, rho):
+        r = np.maximum(rho[0], 1e-12)
+        sigma = (rho[1:4] ** 2).sum(axis=0)
+        ex = np.exp(-r)
+        cx = 0.7385587663820224
+        e = -cx * r ** (4.0 / 3.0) + 0.05 * sigma * ex + 0.2 * rho[4] * r / (1.0 + r)
+        vrho = (-4.0 / 3.0 * cx * r ** (1.0 / 3.0) - 0.05 * sigma * ex
+                + 0.2 * rho[4] / (1.0 + r) ** 2)
+        return e / r, vrho, 0.05 * ex, 0.2 * r / (1.0 + r)
+
+
+def xc_flow_timing(mol, g, dm, eng, torch, calls=3):
+    """Wall time of one semilocal XC flow (gpu_nr_rks, MGGA) on the bench
+    molecule and grid, device synchronised; the host functional is the
+    stand-in above."""
+    import types
+    from pyscf_wb97mv_fast_gb300.gpu.xc import XcContext, gpu_nr_rks
+
+    class Ni:
+        @staticmethod
+        def _xc_type(xc_code):
+            return 'MGGA'
+    ctx = XcContext(mol, functional_factory=lambda xc, ni: SlaterGgaTau())
+    ctx.engine = eng
+    grids = types.SimpleNamespace(coords=g.coords, weights=g.weights)
+    out = gpu_nr_rks(ctx, Ni(), mol, grids, 'mgga', dm)     # warm-up
+    ts = []
+    for _ in range(calls):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = gpu_nr_rks(ctx, Ni(), mol, grids, 'mgga', dm)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    return {'ms_per_call': 1e3 * statistics.median(ts), 'calls': calls,
+            'npts': int(g.size), 'nao': int(mol.nao), 'xctype': 'MGGA',
+            'nelec': out[0],
+            'functional': 'host stand-in (Slater exchange + gradient + tau '
+                          'terms; PySCF libxc not installed)',
+            'note': 'wall time per gpu_nr_rks call: AO values and gradients, '
+                    '4 F-type GEMM splits, density pass, host functional, '
+                    'Fock-side pass, 4 K-type GEMM splits'}
+
+
 def run_sample(oracle, mol, g, dm, idx):
     coords = g.coords[idx]
     X = oracle.ao_eval(mol, coords)
@@ -277,6 +325,8 @@ def main():
                     help='one get_k call per omega instead of one multi-omega '
                          'call (AO values and F formed twice)')
     ap.add_argument('--ref-points', type=int, default=400)
+    ap.add_argument('--no-xc', action='store_true',
+                    help='skip the semilocal XC flow timing')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -427,6 +477,8 @@ def main():
         roofline['measured_peaks_file'] = {'hbm_gbs': mp.get('hbm_gbs'),
                                            'bf16_tflops': mp.get('bf16_tflops')}
 
+    xc_flow = None if args.no_xc else xc_flow_timing(mol, g, dm, eng, torch)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(mol, g, dm, eng)
@@ -444,6 +496,7 @@ def main():
                     'd2h_bytes_per_step': d2h},
             'roofline': roofline,
             'cpu_baseline': cpu,
+            'xc_flow': xc_flow,
             'clocks': clocks.summary(),
             'gpu_launches': launches_step * args.steps,
             'tasks_kept': kept, 'tasks_total': total,

@@ -201,6 +201,24 @@ int wb_ao_eval(const wb_cosx* h, const double* coords, int64_t npts,
 int wb_ao_eval_deriv1(const wb_cosx* h, const double* coords, int64_t npts,
                       double* x_out, void* stream);
 
+/* Semilocal XC flow (NumInt.nr_rks for one RKS density; the reference's
+ * gpu_nr_rks, gpu/xc.py:130-201), the two pointwise passes around the host
+ * functional.  x (4, nao, ld) FP64 from wb_ao_eval_deriv1; ld a multiple of
+ * 32 and >= npts.
+ *   wb_xc_rho: t (1 or 4, nao, ld) FP32 = fl32(dm^T x_d) (wb_cosx_ozaki_f on
+ *     each plane; plane 0 only unless mgga); rho_out (5, ld) FP64 = (rho,
+ *     grad x/y/z, tau) -- gpu/xc.py:158-172.
+ *   wb_xc_aow: v (5, ld) FP64, the density-parameter derivatives (chain
+ *     rule applied, gpu/xc.py:96-116); g_out (1 or 4, nao, ld) FP32: plane 0
+ *     = 1/2 v0 x0 + sum_d v_d x_d, planes 1..3 (mgga) = 1/2 vtau x_d.  Then
+ *     vmat = K + K^T + sum_d K_d with K = wb_cosx_ozaki_k(x0, plane 0, w)
+ *     and K_d = wb_cosx_ozaki_k(x_d, plane d, w) -- gpu/xc.py:179-201.
+ * Points at or past npts get 0 in both. */
+int wb_xc_rho(const wb_cosx* h, const double* x, const float* t, int64_t npts,
+              int64_t ld, int mgga, double* rho_out, void* stream);
+int wb_xc_aow(const wb_cosx* h, const double* x, const double* v, int64_t npts,
+              int64_t ld, int mgga, float* g_out, void* stream);
+
 /* Dense contracted spherical A[g, mu, nu] (npts, nao, nao) FP32 for small
  * validation systems.  Replaces int3c1e_fp32 (gpu/int3c1e.py:284-314). */
 int wb_int3c1e_dense(const wb_cosx* h, const double* coords, int64_t npts,

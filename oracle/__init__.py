@@ -162,6 +162,52 @@ def nlc_vxc(mol, coords, weights, dm, nlc_coefs, thresh=1e-8):
     return nelec, excsum, vmat + vmat.T
 
 
+def xc_chain_rule(rho, exc, vrho, vsigma, vtau):
+    """libxc derivatives -> density-parameter derivatives v (5, P): vrho,
+    2 vsigma grad rho, vtau (reference gpu/xc.py:96-116; zero rows for an
+    absent vsigma / vtau)."""
+    v = np.zeros((5, rho.shape[1]))
+    v[0] = vrho
+    if vsigma is not None:
+        v[1:4] = 2.0 * np.asarray(vsigma)[None] * rho[1:4]
+    if vtau is not None:
+        v[4] = vtau
+    return np.asarray(exc, dtype=np.float64), v
+
+
+def nr_rks(mol, coords, weights, dm, functional, xctype, ao=None):
+    """FP64 restatement of the reference's semilocal XC flow
+    (gpu/xc.py:130-201 = NumInt.nr_rks for one RKS density):
+    (nelec, excsum, vmat).  functional.eval(rho (5, P)) returns (exc, vrho,
+    vsigma, vtau) in the libxc convention; xctype 'LDA', 'GGA' or 'MGGA';
+    ao: the AO values and gradients (4, P, nao) when already evaluated."""
+    if ao is None:
+        ao = ao_eval_deriv1(mol, coords)
+    w = np.asarray(weights, dtype=np.float64)
+    n = len(w)
+    T = ao[0] @ dm
+    rho = np.zeros((5, n))
+    rho[0] = (T * ao[0]).sum(axis=1)
+    rho[1:4] = 2.0 * np.einsum('pm,dpm->dp', T, ao[1:4])
+    if xctype == 'MGGA':
+        for d in range(1, 4):
+            rho[4] += 0.5 * ((ao[d] @ dm) * ao[d]).sum(axis=1)
+    exc, vrho, vsigma, vtau = functional.eval(rho)
+    exc, v = xc_chain_rule(rho, exc, vrho, vsigma, vtau)
+    nelec = float((rho[0] * w).sum())
+    excsum = float((rho[0] * w * exc).sum())
+    wv = v * w[None]
+    wv[0] *= 0.5
+    aow = np.einsum('dpm,dp->pm', ao, wv[:4])
+    vmat = ao[0].T @ aow
+    vmat = vmat + vmat.T
+    if xctype == 'MGGA':
+        wtau = 0.5 * wv[4]
+        for d in range(1, 4):
+            vmat += (ao[d] * wtau[:, None]).T @ ao[d]
+    return nelec, excsum, vmat
+
+
 def vv10_sum(coords, q, w0, kappa):
     """FP64 brute-force F (x -1.5), U, W."""
     c = np.ascontiguousarray(coords, dtype=np.float64)

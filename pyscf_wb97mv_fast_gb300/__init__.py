@@ -2,9 +2,12 @@
 SCF, behind the removable PySCF-hook API of pyscf-wb97mv-fast.
 
     core.hooks      HookSet, reset_diis, track_residual
+    core.sgx_patch  the RSH-branch fix of PySCF's SGX.get_jk
     gpu.install     install_gpu(mf, k=True) -> HookSet
     gpu.sgx_k       GpuKBuilder, get_k_only_gpu
     gpu.vv10        VV10 kernel sum and the nr_nlc_vxc flow
+    gpu.xc          the semilocal nr_rks flow
+    staging         StagedSCF, run_staged
     cosx            CosxEngine: the native handle driven from PyTorch
     basis, systems, grids   synthetic inputs (no PySCF needed)
 

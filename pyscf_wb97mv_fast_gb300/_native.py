@@ -39,7 +39,7 @@ EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_cosx_export_pairs', 'wb_cosx_workspace_bytes',
             'wb_cosx_get_k', 'wb_cosx_get_k_multi', 'wb_cosx_g',
             'wb_cosx_g_multi', 'wb_ao_eval',
-            'wb_ao_eval_deriv1',
+            'wb_ao_eval_deriv1', 'wb_xc_rho', 'wb_xc_aow',
             'wb_int3c1e_dense',
             'wb_boys_fp32', 'wb_boys_f64_host', 'wb_vv10_kernel_sum',
             'wb_becke_partition', 'wb_fp32_fma_probe',
@@ -135,6 +135,8 @@ def _declare(lib):
                                    ctypes.POINTER(WbCosxStats)]),
         'wb_ao_eval': (_INT, [_P, _P, _I64, _P, _P]),
         'wb_ao_eval_deriv1': (_INT, [_P, _P, _I64, _P, _P]),
+        'wb_xc_rho': (_INT, [_P, _P, _P, _I64, _I64, _INT, _P, _P]),
+        'wb_xc_aow': (_INT, [_P, _P, _P, _I64, _I64, _INT, _P, _P]),
         'wb_int3c1e_dense': (_INT, [_P, _P, _I64, _D, _P, _P]),
         'wb_boys_fp32': (_INT, [_P, _I64, _INT, _P, _P]),
         'wb_boys_f64_host': (_INT, [_INT, _D, _P]),

@@ -298,6 +298,29 @@ class CosxEngine:
             self._stream()), 'wb_ao_eval_deriv1')
         return out
 
+    def xc_rho(self, X, T, npts, mgga):
+        """Semilocal XC density parameters (5, ld) FP64 (rho, grad, tau) from
+        X (4, nao, ld) FP64 and T (1 or 4, nao, ld) FP32 = fl32(dm^T X_d)."""
+        torch = _torch()
+        ld = int(X.shape[2])
+        out = torch.empty((5, ld), dtype=torch.float64, device=self.device)
+        _native.check(_native.lib().wb_xc_rho(
+            self._h, _native.ptr(X), _native.ptr(T.contiguous()), int(npts), ld,
+            1 if mgga else 0, _native.ptr(out), self._stream()), 'wb_xc_rho')
+        return out
+
+    def xc_aow(self, X, v, npts, mgga):
+        """Fock-side planes (1 or 4, nao, ld) FP32 from X and the
+        density-parameter derivatives v (5, ld) FP64."""
+        torch = _torch()
+        ld = int(X.shape[2])
+        out = torch.empty((4 if mgga else 1, self.nao, ld), dtype=torch.float32,
+                          device=self.device)
+        _native.check(_native.lib().wb_xc_aow(
+            self._h, _native.ptr(X), _native.ptr(v.contiguous()), int(npts), ld,
+            1 if mgga else 0, _native.ptr(out), self._stream()), 'wb_xc_aow')
+        return out
+
     def int3c1e_dense(self, coords_rel, omega=0.0):
         """Dense (npts, nao, nao) FP32 contracted spherical integrals
         (validation only; refuses more than 2 GiB)."""

@@ -387,6 +387,97 @@ cudaError_t launch_block_order(const BlockOrderArgs& P, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// -- semilocal XC flow (reference gpu/xc.py:130-201) -------------------------
+// Density parameters at every point: rho = sum_mu T0 X0, grad_d = 2 sum_mu
+// T0 X_d and, for MGGA, tau = 1/2 sum_d sum_mu T_d X_d, with X (4, nao, ld)
+// the FP64 AO values and gradients and T (1 or 4, nao, ld) = fl32(D^T X_d)
+// from the FP64-accurate F GEMM.  Products in FP32 (the reference's flow is
+// FP32 throughout), summed in FP32 over 8 AOs and in FP64 across groups.
+// One thread per point, rows read coalesced.  Points at or past npts: 0.
+__global__ void xc_rho_kernel(const double* __restrict__ X,
+                              const float* __restrict__ T, int nao, int64_t ld,
+                              int64_t npts, int mgga, double* __restrict__ rho) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ld) return;
+    double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (g < npts) {
+        const int64_t pl = (int64_t)nao * ld;
+        for (int m0 = 0; m0 < nao; m0 += 8) {
+            float part[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            const int m1 = min(nao, m0 + 8);
+            for (int mu = m0; mu < m1; ++mu) {
+                const int64_t o = (int64_t)mu * ld + g;
+                const float t0 = T[o];
+                part[0] = fmaf(t0, (float)X[o], part[0]);
+                part[1] = fmaf(t0, (float)X[pl + o], part[1]);
+                part[2] = fmaf(t0, (float)X[2 * pl + o], part[2]);
+                part[3] = fmaf(t0, (float)X[3 * pl + o], part[3]);
+                if (mgga) {
+                    part[4] = fmaf(T[pl + o], (float)X[pl + o], part[4]);
+                    part[4] = fmaf(T[2 * pl + o], (float)X[2 * pl + o], part[4]);
+                    part[4] = fmaf(T[3 * pl + o], (float)X[3 * pl + o], part[4]);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) acc[k] += (double)part[k];
+        }
+    }
+    rho[g] = acc[0];
+    rho[ld + g] = 2.0 * acc[1];
+    rho[2 * ld + g] = 2.0 * acc[2];
+    rho[3 * ld + g] = 2.0 * acc[3];
+    rho[4 * ld + g] = 0.5 * acc[4];
+}
+
+cudaError_t launch_xc_rho(const double* X, const float* T, int nao, int64_t ld,
+                          int64_t npts, int mgga, double* rho, cudaStream_t s) {
+    if (ld <= 0) return cudaSuccess;
+    xc_rho_kernel<<<(unsigned)((ld + 255) / 256), 256, 0, s>>>(X, T, nao, ld, npts,
+                                                              mgga, rho);
+    return cudaGetLastError();
+}
+
+// The Fock-side planes, FP32 (nao, ld) each: G0 = 1/2 v0 X0 + sum_d v_d X_d
+// (the reference's aow without the weights, which the K GEMM applies) and,
+// for MGGA, G_d = 1/2 vtau X_d (d = x, y, z); v (5, ld) FP64 are the
+// density-parameter derivatives (chain rule applied).  Points at or past
+// npts: 0.
+__global__ void xc_aow_kernel(const double* __restrict__ X,
+                              const double* __restrict__ v, int nao, int64_t ld,
+                              int64_t npts, int mgga, float* __restrict__ G) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    if (g >= ld) return;
+    const int64_t pl = (int64_t)nao * ld;
+    const int64_t o = (int64_t)mu * ld + g;
+    float g0 = 0.0f, gt[3] = {0.0f, 0.0f, 0.0f};
+    if (g < npts) {
+        const float u0 = (float)(0.5 * v[g]);
+        g0 = u0 * (float)X[o];
+#pragma unroll
+        for (int d = 1; d < 4; ++d)
+            g0 = fmaf((float)v[d * ld + g], (float)X[d * pl + o], g0);
+        if (mgga) {
+            const float ut = (float)(0.5 * v[4 * ld + g]);
+#pragma unroll
+            for (int d = 1; d < 4; ++d) gt[d - 1] = ut * (float)X[d * pl + o];
+        }
+    }
+    G[o] = g0;
+    if (mgga) {
+#pragma unroll
+        for (int d = 1; d < 4; ++d) G[d * pl + o] = gt[d - 1];
+    }
+}
+
+cudaError_t launch_xc_aow(const double* X, const double* v, int nao, int64_t ld,
+                          int64_t npts, int mgga, float* G, cudaStream_t s) {
+    if (ld <= 0 || nao <= 0) return cudaSuccess;
+    dim3 grid((unsigned)((ld + 255) / 256), (unsigned)nao);
+    xc_aow_kernel<<<grid, 256, 0, s>>>(X, v, nao, ld, npts, mgga, G);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_gsum(const float* gc, const int4* src, int nao, int64_t ld,
                         float* G, cudaStream_t s) {
     if (nao <= 0 || ld <= 0) return cudaSuccess;

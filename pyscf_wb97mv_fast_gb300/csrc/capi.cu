@@ -1180,6 +1180,24 @@ int wb_ao_eval_deriv1(const wb_cosx* h, const double* coords, int64_t npts,
     return WB_OK;
 }
 
+int wb_xc_rho(const wb_cosx* h, const double* x, const float* t, int64_t npts,
+              int64_t ld, int mgga, double* rho_out, void* stream) {
+    if (!h || !x || !t || !rho_out || npts < 0 || ld < npts || ld % 32 != 0)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_xc_rho: bad arguments");
+    WB_CUDA(wb::launch_xc_rho(x, t, h->hp.nao, ld, npts, mgga ? 1 : 0, rho_out,
+                              static_cast<cudaStream_t>(stream)));
+    return WB_OK;
+}
+
+int wb_xc_aow(const wb_cosx* h, const double* x, const double* v, int64_t npts,
+              int64_t ld, int mgga, float* g_out, void* stream) {
+    if (!h || !x || !v || !g_out || npts < 0 || ld < npts || ld % 32 != 0)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_xc_aow: bad arguments");
+    WB_CUDA(wb::launch_xc_aow(x, v, h->hp.nao, ld, npts, mgga ? 1 : 0, g_out,
+                              static_cast<cudaStream_t>(stream)));
+    return WB_OK;
+}
+
 int wb_int3c1e_dense(const wb_cosx* h, const double* coords, int64_t npts,
                      double omega, float* out, void* stream) {
     if (!h || !out || npts <= 0 || !coords || !(omega >= 0.0))

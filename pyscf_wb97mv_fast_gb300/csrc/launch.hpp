@@ -90,6 +90,11 @@ struct BlockOrderArgs {
     int n[kClasses];
 };
 cudaError_t launch_block_order(const BlockOrderArgs& P, cudaStream_t s);
+// semilocal XC: density parameters (5, ld) FP64 and the Fock-side planes
+cudaError_t launch_xc_rho(const double* X, const float* T, int nao, int64_t ld,
+                          int64_t npts, int mgga, double* rho, cudaStream_t s);
+cudaError_t launch_xc_aow(const double* X, const double* v, int nao, int64_t ld,
+                          int64_t npts, int mgga, float* G, cudaStream_t s);
 cudaError_t launch_gsum(const float* gc, const int4* src, int nao, int64_t ld,
                         float* G, cudaStream_t s);
 cudaError_t launch_weight_g(const float* G, const double* w, int64_t npts,

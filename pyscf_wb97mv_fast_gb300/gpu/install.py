@@ -80,14 +80,16 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
                 functional_factory=None, verify_ao=True,
                 gemm_dtype='float64', dtype='float32',
                 mem_fraction=DEFAULT_MEM_FRACTION, overlap=False,
-                semilocal=False, k=True, k_tile_tol=1e-11,
+                semilocal=True, k=True, k_tile_tol=1e-11,
                 openblas_threads=None, vv10=True, k_gemm='ozaki',
                 sgx_jk_module=None, k_omegas='auto'):
     """Hook the GPU COSX K (and VV10) into mf; returns a HookSet.
 
     The keyword names follow the reference; backend must be None or
-    'cuda' (there is one backend).  semilocal=True is not part of this
-    build and raises.  sgx_jk_module lets tests pass a stand-in for
+    'cuda' (there is one backend).  semilocal=True replaces
+    ``mf._numint.nr_rks`` by the GPU semilocal flow (gpu/xc.py), with
+    functional_factory(xc_code, ni) -> XcFunctional (default: PySCF's
+    libxc on the host).  sgx_jk_module lets tests pass a stand-in for
     pyscf.sgx.sgx_jk.  k_omegas (an addition): the omegas one SCF cycle
     asks K for with the same density, built together (GpuKBuilder
     omegas); 'auto' reads them from the range-separated functional of mf
@@ -95,10 +97,6 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
     """
     if backend not in (None, 'cuda', 'cupy'):
         raise ValueError("backend must be None or 'cuda'")
-    if semilocal:
-        raise NotImplementedError(
-            'the semilocal XC hook (nr_rks) is not part of this build; '
-            'install with semilocal=False (stock PySCF keeps nr_rks)')
     hooks = HookSet()
     hooks.k_stats = []
     hooks.timings = []
@@ -138,6 +136,20 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
             return get_k_only
 
         hooks.wrap(mod, 'get_k_only', k_factory)
+    if semilocal:
+        ni = getattr(mf, '_numint', None)
+        if ni is None:
+            raise TypeError('mf has no _numint; not a DFT object?')
+        from pyscf_wb97mv_fast_gb300.gpu import xc as xc_mod
+        xctx = xc_mod.XcContext(mf.mol, functional_factory=functional_factory)
+
+        def rks_factory(orig):
+            def nr_rks(mol, grids, xc_code, dms, relativity=0, hermi=1,
+                       max_memory=2000, verbose=None):
+                return xc_mod.gpu_nr_rks(xctx, ni, mol, grids, xc_code, dms,
+                                         relativity, hermi, max_memory, verbose)
+            return nr_rks
+        hooks.wrap(ni, 'nr_rks', rks_factory)
     if vv10:
         ni = getattr(mf, '_numint', None)
         if ni is None:
@@ -154,8 +166,9 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
             return nr_nlc_vxc
         hooks.wrap(ni, 'nr_nlc_vxc', nlc_factory)
     if overlap:
-        warnings.warn('overlap=True has no effect: the XC flows are not '
-                      'hooked in this build', RuntimeWarning)
+        warnings.warn('overlap=True has no effect: the K, XC and VV10 '
+                      'flows run one after another on the device',
+                      RuntimeWarning)
     return hooks
 
 

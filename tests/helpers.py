@@ -48,3 +48,46 @@ def local_density(mol, atoms_per_unit=3, nocc_per_unit=5, seed=0):
         cols.append(c)
     c = np.hstack(cols)
     return 2.0 * c @ c.T
+
+
+class ToyFunctional:
+    """Stand-in XcFunctional (libxc convention) for the semilocal flow tests,
+    PySCF's libxc being absent:  e(rho, sigma, tau) = -Cx rho^(4/3)
+    + a sigma exp(-rho) + b tau rho / (1 + rho), exc = e / rho, and
+    vrho, vsigma, vtau its partial derivatives; a = b = 0 for LDA (no
+    vsigma, vtau), b = 0 for GGA (no vtau).  Points with rho < 1e-12 give
+    zeros, like libxc's density threshold."""
+
+    CX = 0.7385587663820224
+
+    def __init__(self, xctype='MGGA', a=0.05, b=0.2):
+        self.xctype = xctype
+        self.a = a if xctype in ('GGA', 'MGGA') else 0.0
+        self.b = b if xctype == 'MGGA' else 0.0
+
+    def eval(self, rho):
+        rho = np.asarray(rho, dtype=np.float64)
+        r = rho[0]
+        ok = r >= 1e-12
+        rr = np.where(ok, r, 1.0)
+        sigma = (rho[1:4] ** 2).sum(axis=0)
+        tau = rho[4]
+        ex = np.exp(-rr)
+        e = -self.CX * rr ** (4.0 / 3.0) + self.a * sigma * ex + self.b * tau * rr / (1.0 + rr)
+        vrho = (-4.0 / 3.0 * self.CX * rr ** (1.0 / 3.0) - self.a * sigma * ex
+                + self.b * tau / (1.0 + rr) ** 2)
+        exc = np.where(ok, e / rr, 0.0)
+        vrho = np.where(ok, vrho, 0.0)
+        vsigma = np.where(ok, self.a * ex, 0.0) if self.xctype != 'LDA' else None
+        vtau = np.where(ok, self.b * rr / (1.0 + rr), 0.0) if self.xctype == 'MGGA' else None
+        return exc, vrho, vsigma, vtau
+
+
+class ToyNumInt:
+    """The two NumInt pieces the flow reads: the xc type."""
+
+    def __init__(self, xctype):
+        self.xctype = xctype
+
+    def _xc_type(self, xc_code):
+        return self.xctype

@@ -86,7 +86,8 @@ def test_install_routes_only_this_mf_and_restores():
     calls = []
     mod.get_k_only = lambda sgx, dm, hermi=1, tol=1e-13: calls.append(sgx) or 'cpu'
     orig = mod.get_k_only
-    hooks = install_gpu(mf, k=True, vv10=False, sgx_jk_module=mod)
+    hooks = install_gpu(mf, k=True, vv10=False, semilocal=False,
+                        sgx_jk_module=mod)
     assert mod.get_k_only is not orig
     other = Sgx()
     assert mod.get_k_only(other, None) == 'cpu'   # foreign SGX object: original
@@ -95,13 +96,22 @@ def test_install_routes_only_this_mf_and_restores():
     assert mod.get_k_only is orig
 
 
-def test_install_rejects_what_this_build_does_not_hook():
+def test_install_semilocal_hook_wraps_and_restores_nr_rks():
     from pyscf_wb97mv_fast_gb300.gpu.install import install_gpu
     mf, _ = _fake_mf()
-    with pytest.raises(NotImplementedError):
-        install_gpu(mf, semilocal=True, k=False, vv10=False)
+    stock = lambda *a, **k: 'cpu'
+    mf._numint.nr_rks = stock
+    hooks = install_gpu(mf, semilocal=True, k=False, vv10=False,
+                        functional_factory=lambda xc, ni: None)
+    assert mf._numint.nr_rks is not stock
+    assert mf._numint.nr_rks.__name__ == 'nr_rks'
+    hooks.restore_all()
+    assert mf._numint.nr_rks is stock
     with pytest.raises(ValueError):
         install_gpu(mf, backend='numpy', k=False, vv10=False)
+    with pytest.raises(TypeError):
+        install_gpu(types.SimpleNamespace(mol=None), semilocal=True, k=False,
+                    vv10=False)
 
 
 def test_oom_retry_halves_tile_then_reraises():
@@ -139,7 +149,7 @@ def test_oom_retry_halves_tile_then_reraises():
 def test_import_has_no_side_effects():
     code = ('import sys, pyscf_wb97mv_fast_gb300, pyscf_wb97mv_fast_gb300.gpu.install, '
             'pyscf_wb97mv_fast_gb300.gpu.sgx_k, pyscf_wb97mv_fast_gb300.core.sgx_patch, '
-            'pyscf_wb97mv_fast_gb300.staging.schedule;'
+            'pyscf_wb97mv_fast_gb300.staging.schedule, pyscf_wb97mv_fast_gb300.gpu.xc;'
             'print(any(m == "pyscf" or m.startswith("pyscf.") for m in sys.modules),'
             ' "torch" in sys.modules)')
     out = subprocess.run([sys.executable, '-c', code], capture_output=True,
