@@ -167,6 +167,14 @@ _SYNTH = {
               (1, 3, 13.0, 4.3), (1, 1, 0.22, 1.0), (2, 1, 0.85, 1.0)],
         'O': [(0, 5, 2200.0, 4.6), (0, 1, 0.75, 1.0), (0, 1, 0.23, 1.0),
               (1, 3, 16.0, 4.3), (1, 1, 0.27, 1.0), (2, 1, 1.20, 1.0)],
+        'F': [(0, 5, 2900.0, 4.6), (0, 1, 0.95, 1.0), (0, 1, 0.29, 1.0),
+              (1, 3, 20.0, 4.3), (1, 1, 0.33, 1.0), (2, 1, 1.40, 1.0)],
+        'S': [(0, 5, 40000.0, 5.5), (0, 3, 40.0, 3.0), (0, 1, 0.45, 1.0),
+              (0, 1, 0.17, 1.0), (1, 5, 300.0, 3.5), (1, 1, 0.35, 1.0),
+              (1, 1, 0.12, 1.0), (2, 1, 0.48, 1.0)],
+        'Cl': [(0, 5, 48000.0, 5.5), (0, 3, 50.0, 3.0), (0, 1, 0.55, 1.0),
+               (0, 1, 0.21, 1.0), (1, 5, 360.0, 3.5), (1, 1, 0.42, 1.0),
+               (1, 1, 0.14, 1.0), (2, 1, 0.65, 1.0)],
     },
     'synthetic-tzvp': {
         'H': [(0, 3, 34.0, 5.0), (0, 1, 0.32, 1.0), (0, 1, 0.10, 1.0),
@@ -183,6 +191,20 @@ _SYNTH = {
               (0, 1, 0.42, 1.0), (0, 1, 0.16, 1.0),
               (1, 4, 63.0, 4.0), (1, 1, 0.64, 1.0), (1, 1, 0.19, 1.0),
               (2, 1, 2.30, 1.0), (2, 1, 0.65, 1.0), (3, 1, 1.43, 1.0)],
+        'F': [(0, 6, 35000.0, 6.0), (0, 2, 45.0, 3.0), (0, 1, 1.40, 1.0),
+              (0, 1, 0.53, 1.0), (0, 1, 0.20, 1.0),
+              (1, 4, 80.0, 4.0), (1, 1, 0.80, 1.0), (1, 1, 0.24, 1.0),
+              (2, 1, 3.00, 1.0), (2, 1, 0.85, 1.0), (3, 1, 1.85, 1.0)],
+        'S': [(0, 6, 100000.0, 6.0), (0, 3, 160.0, 3.5), (0, 1, 2.00, 1.0),
+              (0, 1, 0.55, 1.0), (0, 1, 0.20, 1.0),
+              (1, 5, 600.0, 4.0), (1, 2, 4.00, 3.0), (1, 1, 0.45, 1.0),
+              (1, 1, 0.15, 1.0), (2, 1, 1.50, 1.0), (2, 1, 0.40, 1.0),
+              (3, 1, 0.56, 1.0)],
+        'Cl': [(0, 6, 120000.0, 6.0), (0, 3, 190.0, 3.5), (0, 1, 2.40, 1.0),
+               (0, 1, 0.66, 1.0), (0, 1, 0.24, 1.0),
+               (1, 5, 700.0, 4.0), (1, 2, 4.80, 3.0), (1, 1, 0.55, 1.0),
+               (1, 1, 0.18, 1.0), (2, 1, 1.90, 1.0), (2, 1, 0.52, 1.0),
+               (3, 1, 0.70, 1.0)],
     },
 }
 

@@ -7,6 +7,9 @@
   ``pyscf_wb97mv_fast/core/testsystems.py:39-45``).
 * ``alkane(n)``: all-trans CnH(2n+2), C-C 1.53 A, C-H 1.09 A, tetrahedral
   angles, zig-zag backbone in the xy plane.
+* ``drug_like(seed)``: a seeded drug-like test molecule with the elements of
+  small-molecule drugs (C, N, O, S, F, Cl, H): a benzene ring carrying the
+  halogens and a side chain of C, N, O and S, filled with hydrogens.
 
 All coordinates are returned in Angstrom as [(symbol, (x, y, z))].
 """
@@ -90,3 +93,102 @@ def alkane(n, cc=1.53, ch=1.09):
 def water_dimer(seed=1):
     """Two waters in a 3.2 A box (the small parity system)."""
     return water_cluster(2, box=3.2, seed=seed)
+
+
+# single-bond lengths (Angstrom) and valences for drug_like
+_BOND = {('C', 'C'): 1.51, ('C', 'N'): 1.47, ('C', 'O'): 1.43, ('C', 'S'): 1.82,
+         ('C', 'F'): 1.35, ('C', 'Cl'): 1.75, ('N', 'N'): 1.45, ('N', 'O'): 1.40,
+         ('N', 'S'): 1.70, ('O', 'S'): 1.57, ('O', 'O'): 1.48, ('S', 'S'): 2.05}
+_XH = {'C': 1.09, 'N': 1.01, 'O': 0.96, 'S': 1.34}
+_VALENCE = {'C': 4, 'N': 3, 'O': 2, 'S': 2}
+
+
+def _bond(a, b):
+    return _BOND.get((a, b)) or _BOND[(b, a)]
+
+
+def _unit(v):
+    return v / np.linalg.norm(v)
+
+
+def drug_like(seed=0, chain=('C', 'N', 'C', 'O', 'C', 'S', 'C'),
+              halogens=('F', 'Cl'), max_tries=300):
+    """Seeded drug-like molecule (Angstrom).  A planar benzene ring (C-C
+    1.39 A) carries the halogens (C-F 1.35, C-Cl 1.75 A, radial) and, at
+    ring carbon 0, a side chain with the elements of ``chain`` in seeded
+    order, each single-bonded to the previous one (bond angle >= 100 deg,
+    non-bonded heavy atoms >= 2.4 A apart).  Hydrogens fill the remaining
+    valences (ring C: one; C 4, N 3, O 2, S 2) at X-H bond lengths, at
+    >= 100 deg from the atom's other bonds and clear of the other atoms.
+    Meant for integral tests, not chemistry."""
+    rng = np.random.default_rng(seed)
+    sym, pos, nbr = [], [], []
+
+    def add(s, p, parent=None):
+        sym.append(s)
+        pos.append(np.asarray(p, dtype=np.float64))
+        nbr.append([])
+        if parent is not None:
+            nbr[-1].append(parent)
+            nbr[parent].append(len(sym) - 1)
+        return len(sym) - 1
+
+    for k in range(6):
+        a = k * math.pi / 3.0
+        add('C', (1.39 * math.cos(a), 1.39 * math.sin(a), 0.0))
+    for k in range(6):
+        nbr[k] += [(k + 1) % 6, (k + 5) % 6]
+    for k, x in zip((2, 4), halogens):
+        add(x, pos[k] * (1.0 + _bond('C', x) / 1.39), k)
+
+    def clear(p, skip, heavy_min, h_min):
+        for i, q in enumerate(pos):
+            if i in skip:
+                continue
+            d = np.linalg.norm(p - q)
+            if d < (h_min if sym[i] == 'H' else heavy_min):
+                return False
+        return True
+
+    def direction(i, tries):
+        bonds = [_unit(pos[j] - pos[i]) for j in nbr[i]]
+        for _ in range(tries):
+            v = _unit(rng.normal(size=3))
+            if all(np.dot(v, b) <= math.cos(math.radians(100.0)) for b in bonds):
+                return v
+        return None
+
+    order = list(chain)
+    rng.shuffle(order)
+    prev = 0
+    for x in order:
+        placed = False
+        for _ in range(200):
+            v = direction(prev, 200) if prev != 0 else _unit(pos[0])
+            if v is None:
+                break
+            p = pos[prev] + _bond(sym[prev], x) * v
+            if clear(p, {prev}, 2.4, 1.5):
+                prev = add(x, p, prev)
+                placed = True
+                break
+            if prev == 0:
+                break
+        if not placed:
+            break
+    heavy = len(sym)
+    for i in range(heavy):
+        s = sym[i]
+        if s not in _VALENCE:
+            continue
+        free = (3 if i < 6 else _VALENCE[s]) - len(nbr[i])
+        for _ in range(max(free, 0)):
+            for t in range(max_tries):
+                v = _unit(pos[i]) if (i < 6 and t == 0) else direction(i, 50)
+                if v is None:
+                    continue
+                p = pos[i] + _XH[s] * v
+                if clear(p, {i}, 1.9 if t < max_tries // 2 else 1.5, 1.4):
+                    add('H', p, i)
+                    break
+    return [(s, tuple(float(c) for c in p)) for s, p in zip(sym, pos)]

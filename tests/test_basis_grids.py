@@ -7,7 +7,7 @@ import pytest
 from pyscf_wb97mv_fast_gb300.basis import (Molecule, cart2sph, cart_components,
                                            gto_norm)
 from pyscf_wb97mv_fast_gb300.grids import angular_grid, build_grids, radial_grid
-from pyscf_wb97mv_fast_gb300.systems import alkane, water_cluster
+from pyscf_wb97mv_fast_gb300.systems import alkane, drug_like, water_cluster
 
 
 def test_cart2sph_orthonormal_on_the_sphere():
@@ -20,8 +20,12 @@ def test_cart2sph_orthonormal_on_the_sphere():
         assert np.allclose(G, np.eye(2 * l + 1), atol=1e-12)
 
 
-def test_contracted_functions_are_normalised():
-    mol = Molecule.build(water_cluster(1, 1.0, seed=0), 'synthetic-tzvp')
+@pytest.mark.parametrize('basis', ['synthetic-svp', 'synthetic-tzvp'])
+def test_contracted_functions_are_normalised(basis):
+    atoms = water_cluster(1, 1.0, seed=0) + [('F', (3.0, 0, 0)), ('S', (6.0, 0, 0)),
+                                             ('Cl', (9.0, 0, 0)), ('C', (12.0, 0, 0)),
+                                             ('N', (15.0, 0, 0))]
+    mol = Molecule.build(atoms, basis)
     r, w = radial_grid(400, 1.0)
     for sh in mol.shells:
         for c in range(sh.nctr):
@@ -85,3 +89,23 @@ def test_gto_norm():
         r, w = radial_grid(300, 1.0)
         v = (gto_norm(l, a) * r ** l * np.exp(-a * r * r)) ** 2
         assert (v * w).sum() == pytest.approx(1.0, rel=1e-8)
+
+
+def test_drug_like_molecule():
+    """Seeded; the drug elements present; bonded distances only between
+    bonded atoms; SVP / TZVP sizes (f shells on the heavy atoms)."""
+    atoms = drug_like(0)
+    assert drug_like(0) == atoms
+    sym = [a[0] for a in atoms]
+    for x in ('C', 'N', 'O', 'S', 'F', 'Cl', 'H'):
+        assert x in sym
+    xyz = np.array([a[1] for a in atoms])
+    d = np.linalg.norm(xyz[:, None] - xyz[None], axis=2) + np.eye(len(sym)) * 99
+    assert d.min() > 0.9
+    heavy = [i for i, s in enumerate(sym) if s != 'H']
+    dh = d[np.ix_(heavy, heavy)]
+    assert dh.min() > 1.3
+    svp = Molecule.build(atoms, 'synthetic-svp')
+    tz = Molecule.build(atoms, 'synthetic-tzvp')
+    assert tz.nao > 1.9 * svp.nao
+    assert max(sh.l for sh in tz.shells) == 3

@@ -191,6 +191,40 @@ def test_k_matches_oracle(basis, gen, omega):
     assert st['pairs_kept'] == st['pairs_total']
 
 
+def _drug(seed, basis):
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.systems import drug_like
+    return Molecule.build(drug_like(seed), basis)
+
+
+@pytest.mark.parametrize('basis,npts', [('synthetic-svp', 3000),
+                                        ('synthetic-tzvp', 1500)])
+@pytest.mark.parametrize('omega', [0.0, 0.3])
+def test_k_matches_oracle_drug_like(basis, npts, omega):
+    """The K gates on a seeded drug-like molecule (C, N, O, S, F, Cl, H;
+    f shells on every heavy atom in TZVP): the reference validates on drug
+    molecules (README.md:118-128); here with synthetic molecules and basis
+    data."""
+    mol = _drug(0, basis)
+    coords, weights = grid_subset(mol, 1, npts, 4)
+    dm = density(mol.nao, 30, 5)
+    K, st = _k_gpu(mol, coords, weights, dm, omega)
+    Kref = oracle.cosx_k(mol, coords, weights, dm, omega)
+    assert np.array_equal(K, K.T)
+    rel = np.max(np.abs(K - Kref)) / np.abs(Kref).max()
+    assert rel < 1e-6, rel
+    gate = 3e-7 if omega == 0.0 else 1e-7
+    de = abs(0.25 * np.einsum('ij,ji->', dm, K - Kref))
+    assert de < gate, de
+
+
+@pytest.mark.parametrize('omega', [0.0, 0.3])
+def test_g_kernels_match_oracle_drug_like(omega):
+    mol = _drug(1, 'synthetic-tzvp')
+    _, G, Gref, _ = _g_case(mol, 600, 6, omega)
+    assert np.max(np.abs(G - Gref)) < 2e-6 * np.abs(Gref).max()
+
+
 @pytest.mark.parametrize('omega', [0.0, 0.3])
 def test_k_matches_reference_golden(omega):
     """The reference's own FP64 K on the same 160 points (dense A from

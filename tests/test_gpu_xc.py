@@ -42,6 +42,20 @@ def test_nr_rks_matches_oracle_flow(xctype):
     assert np.array_equal(v, v.T)
 
 
+def test_nr_rks_drug_like_tzvp():
+    """Heavier elements and f shells (a seeded drug-like molecule)."""
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.systems import drug_like
+    mol = Molecule.build(drug_like(2), 'synthetic-tzvp')
+    coords, weights = grid_subset(mol, 1, 4000, 9)
+    dm = density(mol.nao, 30, 4)
+    n, e, v = _flow(mol, coords, weights, dm, 'MGGA')
+    n0, e0, v0 = oracle.nr_rks(mol, coords, weights, dm, ToyFunctional('MGGA'), 'MGGA')
+    assert abs(n - n0) / n0 < 1e-6
+    assert abs(e - e0) <= 1e-6 * abs(e0)
+    assert np.max(np.abs(v - v0)) <= 1e-6 * np.abs(v0).max()
+
+
 def test_tiles_give_the_one_tile_result():
     """Several tiles (a ragged last one) sum to the one-tile result up to
     the order of the FP64 sums."""
