@@ -234,8 +234,10 @@ wb::CosxArgs make_args(const wb_cosx* h, void* ws, const WsLayout& L,
     wb::CosxArgs a;
     std::memset(&a, 0, sizeof(a));
     a.F = F;
-    for (int c = 0; c < wb::NCLASS; ++c)
+    for (int c = 0; c < wb::NCLASS; ++c) {
         a.Gcls[c] = at<float>(ws, L.gcls) + h->hp.crow_base[c] * ldt;
+        a.crow[c] = (int)h->hp.crow[c];
+    }
     a.ld = ldt;
     a.npts = (int)npts_t;
     a.nsub = (int)(ldt / 32);
@@ -430,8 +432,7 @@ int run_g_classes(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
     // the far-field R000 variant pays where T = theta p r^2 >= 36 is common:
     // the full-range operator (theta = 1); long-range omegas keep T small
     const bool far = omega == 0.0;
-    WB_CUDA(cudaMemsetAsync(at<float>(ws, L.gcls), 0,
-                            sizeof(float) * (size_t)h->hp.ncrow * ldt, s));
+    // (the class kernels zero their buffers block by block)
     WB_CUDA(cudaMemsetAsync(at<int>(ws, L.work), 0, sizeof(int) * wb::NCLASS, s));
     WB_CUDA(cudaEventRecord(h->fork, s));
     for (int i = 0; i < wb::NCLASS; ++i) {
@@ -480,9 +481,7 @@ int run_g_classes_dual(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
         b.Gcls[c] = a.Gcls2[c];
     }
     b.work = a.work + wb::NCLASS;
-    const size_t gbytes = sizeof(float) * (size_t)h->hp.ncrow * ldt;
-    WB_CUDA(cudaMemsetAsync(at<float>(ws, L.gcls), 0, gbytes, s));
-    WB_CUDA(cudaMemsetAsync(at<float>(ws, L.gcls2), 0, gbytes, s));
+    // (the class kernels zero their buffers block by block)
     WB_CUDA(cudaMemsetAsync(at<int>(ws, L.work), 0, sizeof(int) * 2 * wb::NCLASS, s));
     WB_CUDA(cudaEventRecord(h->fork, s));
     for (int i = 0; i < wb::NCLASS; ++i) {

@@ -18,7 +18,9 @@ constexpr int kClasses = 10;
 // A, B), ptau[k] = (tau, tau * sum pref).
 struct CosxArgs {
     const float* F;            // (nao, ld) AO-major, FP32
-    float* Gcls[kClasses];     // per class (rows, ld) partial G, zeroed
+    float* Gcls[kClasses];     // per class (rows, ld) partial G; each class
+                               // kernel zeroes its block's columns first
+    int crow[kClasses];        // rows of each class buffer
     long long ld;              // padded point count (multiple of 32)
     int npts;                  // valid points
     int nsub;                  // ld / 32

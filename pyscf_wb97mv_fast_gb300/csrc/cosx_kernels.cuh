@@ -207,6 +207,17 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
             gzl[p] = A.gxyz_lo[2 * (long long)ld + g];
         }
         const float4 cr = blk_cr[blk];
+        // zero this block's columns of the class buffer(s) (each element
+        // has this lane as its one writer, so later stores and reductions
+        // follow in program order; replaces a memset pass over the buffers)
+        {
+            const int nrow = A.crow[CLS];
+            for (int r = 0; r < nrow; ++r) {
+#pragma unroll
+                for (int c = 0; c < NW * PTS; ++c)
+                    if (ok[c % PTS]) Gp[c][(long long)r * ld] = 0.0f;
+            }
+        }
         const float* __restrict__ ms = blk_msh + (long long)blk * A.nvshell;
         const int rem = A.npts - blk * 32 * PTS;
         const int nvalid = rem < 32 * PTS ? (rem > 0 ? rem : 0) : 32 * PTS;
