@@ -232,6 +232,14 @@ int wb_boys_fp32(const float* t, int64_t n, int nmax, float* out,
 /* Host FP64 Boys F_0..F_nmax at one argument (used to build the table). */
 int wb_boys_f64_host(int nmax, double t, double* out);
 
+/* Host only (no device): model flops per grid point summed over the shell
+ * pairs the COSX kernels keep for this basis -- the reference's pair
+ * enumeration and magnitude cut (gpu/shellpairs.py:287-294) and the flop
+ * model of the G kernels, i.e. the work of one grid point with no task
+ * screening.  npairs_out (may be NULL) receives the number of pairs. */
+int wb_model_flops_per_point(const wb_basis* basis, double pair_cutoff,
+                             double* flops_out, int64_t* npairs_out);
+
 /* VV10 double sum over n points (FP32 pair terms, FP64 per-point sums):
  *   F_i = -1.5 sum_j q_j / (g gp (g + gp)),  U_i = sum_j T (1/g + 1/(g+gp)),
  *   W_i = sum_j T (1/g + 1/(g+gp)) R^2,  g = R^2 w0_i + kappa_i, gp likewise.

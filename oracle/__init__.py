@@ -51,7 +51,7 @@ def _load():
         basis = [I, I] + [P] * 9 + [P] * 4
         _lib.oracle_boys.argtypes = [I, D, P]
         _lib.oracle_int3c1e.argtypes = basis + [P, I64, D, P]
-        _lib.oracle_cosx_g.argtypes = basis + [P, I64, D, P, P]
+        _lib.oracle_cosx_g.argtypes = basis + [P, I64, D, D, P, P]
         _lib.oracle_ao_eval.argtypes = basis + [P, I64, P]
         _lib.oracle_vv10_sum.argtypes = [P, P, P, P, I64, P, P, P]
         _lib.oracle_ao_eval_deriv1.argtypes = basis + [P, I64, P]
@@ -95,13 +95,14 @@ def int3c1e(mol, coords, omega=0.0):
     return out
 
 
-def cosx_g(mol, coords, F, omega=0.0):
+def cosx_g(mol, coords, F, omega=0.0, pair_cutoff=1e-14):
     """G (ng, nao) FP64 for F (ng, nao)."""
     b = _Basis(mol)
     c = np.ascontiguousarray(coords, dtype=np.float64)
     F = np.ascontiguousarray(F, dtype=np.float64)
     G = np.zeros_like(F)
-    _load().oracle_cosx_g(*b.args, _p(c), len(c), float(omega), _p(F), _p(G))
+    _load().oracle_cosx_g(*b.args, _p(c), len(c), float(omega),
+                          float(pair_cutoff), _p(F), _p(G))
     return G
 
 

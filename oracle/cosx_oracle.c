@@ -21,7 +21,8 @@
  * Inputs are the packed basis arrays of Molecule.packed() plus the
  * Cartesian -> spherical matrices (ncart, nsph) row-major for l = 0..3.
  * Pairs are enumerated as in the reference (ish >= jsh, all primitive
- * pairs, no magnitude cut).
+ * pairs); oracle_cosx_g applies the reference's shell-pair magnitude cut
+ * (gpu/shellpairs.py:287-294) when given a cutoff > 0.
  */
 #include <math.h>
 #include <stdint.h>
@@ -261,14 +262,48 @@ int oracle_int3c1e(OBASIS_ARGS, const double* coords, int64_t ng, double omega,
     return 0;
 }
 
-/* F, G (ng, nao) point-major; G overwritten.  Optionally restricted to the
- * pairs with keep[pair] != 0 (pair index of the ish >= jsh enumeration). */
+/* The reference's shell-pair cut (gpu/shellpairs.py:287-294): a pair
+ * (ish >= jsh) is kept when sum_ab exp(-a b / (a + b) |A - B|^2) times the
+ * two shells' largest |contraction coefficient| exceeds cutoff (0 keeps
+ * every pair).  keep (nbas, nbas), lower triangle used. */
+static unsigned char* pair_keep(const obasis* b, double cutoff) {
+    const int n = b->nbas;
+    unsigned char* keep = (unsigned char*)malloc((size_t)n * n);
+    double* cmax = (double*)calloc((size_t)n, sizeof(double));
+    for (int s = 0; s < n; ++s) {
+        const int np = b->shell_nprim[s], nc = b->shell_nctr[s];
+        for (int k = 0; k < np * nc; ++k)
+            cmax[s] = fmax(cmax[s], fabs(b->coeffs[b->shell_coef_off[s] + k]));
+    }
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j <= i; ++j) {
+            const double* A = b->atom_coords + 3 * b->shell_atom[i];
+            const double* B = b->atom_coords + 3 * b->shell_atom[j];
+            const double d2 = (A[0] - B[0]) * (A[0] - B[0]) +
+                              (A[1] - B[1]) * (A[1] - B[1]) +
+                              (A[2] - B[2]) * (A[2] - B[2]);
+            double mag = 0.0;
+            for (int a = 0; a < b->shell_nprim[i]; ++a)
+                for (int c = 0; c < b->shell_nprim[j]; ++c) {
+                    const double al = b->exps[b->shell_exp_off[i] + a];
+                    const double be = b->exps[b->shell_exp_off[j] + c];
+                    mag += exp(-al * be / (al + be) * d2);
+                }
+            keep[(size_t)i * n + j] = cutoff <= 0.0 || mag * cmax[i] * cmax[j] > cutoff;
+        }
+    free(cmax);
+    return keep;
+}
+
+/* F, G (ng, nao) point-major; G overwritten.  Only the shell pairs that
+ * pair_keep keeps contribute. */
 int oracle_cosx_g(OBASIS_ARGS, const double* coords, int64_t ng, double omega,
-                  const double* F, double* G) {
+                  double cutoff, const double* F, double* G) {
     obasis b;
     make_basis(&b, OBASIS_PASS);
     int* ao = ao_offsets(&b);
     const int nao = ao[nbas];
+    unsigned char* keep = pair_keep(&b, cutoff);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int64_t g = 0; g < ng; ++g) {
         double A[256];
@@ -277,6 +312,7 @@ int oracle_cosx_g(OBASIS_ARGS, const double* coords, int64_t ng, double omega,
         for (int i = 0; i < nao; ++i) Gg[i] = 0.0;
         for (int ish = 0; ish < nbas; ++ish)
             for (int jsh = 0; jsh <= ish; ++jsh) {
+                if (!keep[(size_t)ish * nbas + jsh]) continue;
                 int ni, nj;
                 pair_block(&b, ish, jsh, coords + 3 * g, omega, A, &ni, &nj);
                 const int i0 = ao[ish], j0 = ao[jsh];
@@ -293,6 +329,7 @@ int oracle_cosx_g(OBASIS_ARGS, const double* coords, int64_t ng, double omega,
                     }
             }
     }
+    free(keep);
     free(ao);
     return 0;
 }

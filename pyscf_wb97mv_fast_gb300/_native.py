@@ -41,7 +41,8 @@ EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_cosx_g_multi', 'wb_ao_eval',
             'wb_ao_eval_deriv1', 'wb_xc_rho', 'wb_xc_aow',
             'wb_int3c1e_dense',
-            'wb_boys_fp32', 'wb_boys_f64_host', 'wb_vv10_kernel_sum',
+            'wb_boys_fp32', 'wb_boys_f64_host', 'wb_model_flops_per_point',
+            'wb_vv10_kernel_sum',
             'wb_becke_partition', 'wb_fp32_fma_probe',
             'wb_ozaki_workspace_bytes', 'wb_cosx_ozaki_f', 'wb_cosx_ozaki_k',
             'wb_vv10_kernel_sum_noalloc',
@@ -140,6 +141,7 @@ def _declare(lib):
         'wb_int3c1e_dense': (_INT, [_P, _P, _I64, _D, _P, _P]),
         'wb_boys_fp32': (_INT, [_P, _I64, _INT, _P, _P]),
         'wb_boys_f64_host': (_INT, [_INT, _D, _P]),
+        'wb_model_flops_per_point': (_INT, [_P, _D, _P, _P]),
         'wb_vv10_kernel_sum': (_INT, [_P, _P, _P, _P, _I64, _D, _P, _P, _P, _P,
                                       ctypes.POINTER(_I64)]),
         'wb_becke_partition': (_INT, [_P, _I64, _P, _P, _INT, _P]),

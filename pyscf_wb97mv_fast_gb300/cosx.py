@@ -51,13 +51,7 @@ class CosxEngine:
             device = torch.device(device).index or 0
         self.device = torch.device('cuda', device)
         self._packed = self.mol.packed()
-        p = self._packed
-        self._basis = _native.WbBasis(
-            p['natm'], p['nbas'], _native.ptr(p['atom_coords']),
-            _native.ptr(p['shell_atom']), _native.ptr(p['shell_l']),
-            _native.ptr(p['shell_nprim']), _native.ptr(p['shell_nctr']),
-            _native.ptr(p['shell_exp_off']), _native.ptr(p['shell_coef_off']),
-            _native.ptr(p['exps']), _native.ptr(p['coeffs']))
+        self._basis = _wb_basis(self._packed)
         self._origin_c = np.ascontiguousarray(self.origin, dtype=np.float64)
         lib = _native.lib()
         handle = _native.ctypes.c_void_p()
@@ -335,6 +329,29 @@ class CosxEngine:
             self._h, _native.ptr(coords_rel), npts, float(omega),
             _native.ptr(out), self._stream()), 'wb_int3c1e_dense')
         return out
+
+
+def _wb_basis(p):
+    """The C-ABI basis view of Molecule.packed() p (p must outlive it)."""
+    return _native.WbBasis(
+        p['natm'], p['nbas'], _native.ptr(p['atom_coords']),
+        _native.ptr(p['shell_atom']), _native.ptr(p['shell_l']),
+        _native.ptr(p['shell_nprim']), _native.ptr(p['shell_nctr']),
+        _native.ptr(p['shell_exp_off']), _native.ptr(p['shell_coef_off']),
+        _native.ptr(p['exps']), _native.ptr(p['coeffs']))
+
+
+def model_flops_per_point(mol, pair_cutoff=1e-14):
+    """(model flops per grid point over the kept shell pairs, number of
+    pairs) -- the work of one point with no task screening, on the host."""
+    p = as_molecule(mol).packed()
+    b = _wb_basis(p)
+    out = _native.ctypes.c_double()
+    n = _native.ctypes.c_int64()
+    _native.check(_native.lib().wb_model_flops_per_point(
+        _native.ctypes.byref(b), float(pair_cutoff), _native.ctypes.byref(out),
+        _native.ctypes.byref(n)), 'wb_model_flops_per_point')
+    return float(out.value), int(n.value)
 
 
 def boys_eval(T, nmax):

@@ -576,6 +576,22 @@ int wb_boys_f64_host(int nmax, double t, double* out) {
     return WB_OK;
 }
 
+int wb_model_flops_per_point(const wb_basis* basis, double pair_cutoff,
+                             double* flops_out, int64_t* npairs_out) {
+    if (!basis || !flops_out || !(pair_cutoff >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_model_flops_per_point: bad arguments");
+    wb::HostPairs hp;
+    std::string err;
+    const double origin[3] = {0.0, 0.0, 0.0};
+    const int st = wb::build_pairs(*basis, origin, pair_cutoff, hp, err);
+    if (st != WB_OK) return fail(st, err);
+    double sum = 0.0;
+    for (const int64_t f : hp.pflops) sum += (double)f;
+    *flops_out = sum;
+    if (npairs_out) *npairs_out = hp.npairs;
+    return WB_OK;
+}
+
 int wb_becke_partition(const double* points, int64_t n, const int* owner,
                        const double* atom_coords, int natm, double* out) {
     if (n < 0 || natm <= 0 || (!points && n) || (!owner && n) || !atom_coords ||
