@@ -249,6 +249,50 @@ def xc_flow_timing(mol, g, dm, eng, torch, calls=3):
                     'Fock-side pass, 4 K-type GEMM splits'}
 
 
+def vv10_timing(mol, dm, eng, torch, peak, calls=2):
+    """The VV10 double sum (Vv10Kernel.kernel_sum, every pair kept) on the
+    bench density's own VV10 terms over the level-1 grid: pairs/s and the
+    27-operations-per-pair work (24 flops + 3 reciprocals) against the FP32
+    peak measured in the same run."""
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    from pyscf_wb97mv_fast_gb300.gpu.vv10 import THRESH, Vv10Kernel, vv10_pointwise
+    g1 = build_grids(mol, level=1)
+    c = eng.relative(g1.coords)
+    n = int(g1.size)
+    ao = eng.ao_eval_deriv1(c)[:, :, :n]
+    D = torch.as_tensor(dm, device=eng.device)
+    T = D @ ao[0]
+    rho0 = (T * ao[0]).sum(dim=0)
+    grad = 2.0 * torch.einsum('mp,dmp->dp', T, ao[1:4])
+    del ao, T
+    w = torch.as_tensor(g1.weights, device=eng.device)
+    ind = rho0 >= THRESH
+    q, W0, kappa = vv10_pointwise(rho0[ind], grad[:, ind], w[ind], (6.0, 0.01))[:3]
+    xyz = c[ind].to(torch.float32)
+    kern = Vv10Kernel(0.0)
+    kern.kernel_sum(xyz, q, W0, kappa)
+    ts = []
+    for _ in range(calls):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        kern.kernel_sum(xyz, q, W0, kappa)
+        e1.record()
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    t = min(ts)
+    m = int(xyz.shape[0])
+    pairs = float(m) * m
+    tflops = 27.0 * pairs / t / 1e12
+    return {'points': m, 'grid': 'level 1 (%d points, rho >= %g kept)' % (n, THRESH),
+            'ms_per_call': t * 1e3, 'pairs_per_s': pairs / t,
+            'achieved_tflops': tflops, 'peak_tflops': peak,
+            'frac': tflops / peak if peak else None,
+            'work': '27 operations per pair (24 flops + 3 reciprocals), '
+                    'every pair kept (tile_tol 0)',
+            'parameters': 'b = 6.0, C = 0.01 (the wB97M-V VV10 set)'}
+
+
 def run_sample(oracle, mol, g, dm, idx):
     coords = g.coords[idx]
     X = oracle.ao_eval(mol, coords)
@@ -483,6 +527,7 @@ def main():
                                            'bf16_tflops': mp.get('bf16_tflops')}
 
     xc_flow = None if args.no_xc else xc_flow_timing(mol, g, dm, eng, torch)
+    vv10 = None if args.no_xc else vv10_timing(mol, dm, eng, torch, peak)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -502,6 +547,7 @@ def main():
             'roofline': roofline,
             'cpu_baseline': cpu,
             'xc_flow': xc_flow,
+            'vv10': vv10,
             'clocks': clocks.summary(),
             'gpu_launches': launches_step * args.steps,
             'tasks_kept': kept, 'tasks_total': total,

@@ -8,8 +8,8 @@
 // One thread per outer point, inner points staged through shared memory in
 // 256-point tiles.  Inside a tile the three sums are FP32 with Kahan
 // compensation, across tiles they accumulate in FP64 in a fixed order: no
-// atomics, bitwise reproducible.  Reciprocals are IEEE round-to-nearest
-// (__frcp_rn): T = q rcp(g gp gt), Tu = T (rcp(g) + rcp(gt)).
+// atomics, bitwise reproducible.  One reciprocal per pair (rcp.approx plus
+// one Newton step): T = q / (g gp gt), Tu = T (g + gt) gp / (g gp gt).
 //
 // Distance pruning on the device: per 256-point tile the centroid, radius,
 // sum q, min w0 and min kappa (FP64); a (block, tile) pair is skipped when
@@ -24,6 +24,12 @@
 namespace wb {
 
 constexpr int kVvTile = 256;
+
+// WB_VV10_FAST = 1: one reciprocal per pair and 16-pair partial sums (the
+// default); 0: three IEEE reciprocals and a Kahan step per pair
+#ifndef WB_VV10_FAST
+#define WB_VV10_FAST 1
+#endif
 
 struct VvTileStats {
     double cx, cy, cz, rad, qsum, w0min, kmin, pad;
@@ -125,6 +131,43 @@ vv10_sum_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
         }
         __syncthreads();
         const int m = (int)min((int64_t)kVvTile, n - jt * kVvTile);
+#if WB_VV10_FAST
+        if (active) {
+            // one reciprocal per pair: inv = 1/(g gp gt) from rcp.approx and
+            // one Newton step, T = q inv and, with 1/g + 1/gt = (g + gt) gp
+            // inv, Tu = T (g + gt) gp inv.  Plain FP32 sums over 16 pairs,
+            // merged into Kahan-compensated tile sums once per 16 pairs.
+            float fs = 0.f, fc = 0.f, us = 0.f, uc = 0.f, ws = 0.f, wc = 0.f;
+            for (int t0 = 0; t0 < m; t0 += 16) {
+                const int t1 = min(m, t0 + 16);
+                float pf = 0.f, pu = 0.f, pw = 0.f;
+                for (int t = t0; t < t1; ++t) {
+                    const float4 pj = sp[t];
+                    const float2 kj = sk[t];
+                    const float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const float g = fmaf(r2, w0i, ki);
+                    const float gp = fmaf(r2, kj.x, kj.y);
+                    const float gt = g + gp;
+                    const float pr = g * gp * gt;
+                    float inv;
+                    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(pr));
+                    inv = fmaf(inv, fmaf(-pr, inv, 1.0f), inv);
+                    const float T = pj.w * inv;
+                    const float Tu = T * ((g + gt) * gp * inv);
+                    pf += T;
+                    pu += Tu;
+                    pw = fmaf(Tu, r2, pw);
+                }
+                float y, z;
+                y = pf - fc; z = fs + y; fc = (z - fs) - y; fs = z;
+                y = pu - uc; z = us + y; uc = (z - us) - y; us = z;
+                y = pw - wc; z = ws + y; wc = (z - ws) - y; ws = z;
+            }
+            f64 += (double)fs; u64 += (double)us; w64 += (double)ws;
+            nkept += (unsigned long long)m;
+        }
+#else
         if (active) {
             float fs = 0.f, fc = 0.f, us = 0.f, uc = 0.f, ws = 0.f, wc = 0.f;
             for (int t = 0; t < m; ++t) {
@@ -146,6 +189,7 @@ vv10_sum_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
             f64 += (double)fs; u64 += (double)us; w64 += (double)ws;
             nkept += (unsigned long long)m;
         }
+#endif
         __syncthreads();
     }
     if (active) { F[i] = -1.5 * f64; U[i] = u64; W[i] = w64; }
