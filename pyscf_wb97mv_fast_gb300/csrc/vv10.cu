@@ -30,6 +30,10 @@ constexpr int kVvTile = 256;
 #ifndef WB_VV10_FAST
 #define WB_VV10_FAST 1
 #endif
+// one Newton step on the approximate reciprocal (1 = on)
+#ifndef WB_VV10_NEWTON
+#define WB_VV10_NEWTON 1
+#endif
 
 struct VvTileStats {
     double cx, cy, cz, rad, qsum, w0min, kmin, pad;
@@ -138,26 +142,31 @@ vv10_sum_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
             // inv, Tu = T (g + gt) gp inv.  Plain FP32 sums over 16 pairs,
             // merged into Kahan-compensated tile sums once per 16 pairs.
             float fs = 0.f, fc = 0.f, us = 0.f, uc = 0.f, ws = 0.f, wc = 0.f;
+            auto pair = [&](const int t, float& pf, float& pu, float& pw) {
+                const float4 pj = sp[t];
+                const float2 kj = sk[t];
+                const float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                const float g = fmaf(r2, w0i, ki);
+                const float gp = fmaf(r2, kj.x, kj.y);
+                const float gt = g + gp;
+                const float pr = g * gp * gt;
+                float inv;
+                asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(pr));
+                if (WB_VV10_NEWTON) inv = fmaf(inv, fmaf(-pr, inv, 1.0f), inv);
+                const float T = pj.w * inv;
+                const float Tu = T * ((g + gt) * gp * inv);
+                pf += T;
+                pu += Tu;
+                pw = fmaf(Tu, r2, pw);
+            };
             for (int t0 = 0; t0 < m; t0 += 16) {
-                const int t1 = min(m, t0 + 16);
                 float pf = 0.f, pu = 0.f, pw = 0.f;
-                for (int t = t0; t < t1; ++t) {
-                    const float4 pj = sp[t];
-                    const float2 kj = sk[t];
-                    const float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    const float g = fmaf(r2, w0i, ki);
-                    const float gp = fmaf(r2, kj.x, kj.y);
-                    const float gt = g + gp;
-                    const float pr = g * gp * gt;
-                    float inv;
-                    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(pr));
-                    inv = fmaf(inv, fmaf(-pr, inv, 1.0f), inv);
-                    const float T = pj.w * inv;
-                    const float Tu = T * ((g + gt) * gp * inv);
-                    pf += T;
-                    pu += Tu;
-                    pw = fmaf(Tu, r2, pw);
+                if (t0 + 16 <= m) {
+#pragma unroll
+                    for (int t = 0; t < 16; ++t) pair(t0 + t, pf, pu, pw);
+                } else {
+                    for (int t = t0; t < m; ++t) pair(t, pf, pu, pw);
                 }
                 float y, z;
                 y = pf - fc; z = fs + y; fc = (z - fs) - y; fs = z;

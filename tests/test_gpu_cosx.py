@@ -151,6 +151,31 @@ def test_g_kernels_bitwise_reproducible():
     assert np.array_equal(G1, G2)
 
 
+def test_block_order_does_not_change_g():
+    """The first G launch on a grid takes the point blocks in ascending
+    order, later ones costliest first (learnt from the previous launch):
+    bitwise the same G and the same kept tasks, on one handle."""
+    torch = _torch()
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine, round32
+    mol = waters(4, 6.0, 12)
+    eng = CosxEngine(mol)
+    coords, weights = grid_subset(mol, 1, 20000, 9)
+    n = len(coords)
+    dm = density(mol.nao, 12, 9)
+    F = (oracle.ao_eval(mol, coords) @ dm).astype(np.float32)
+    Fd = torch.zeros((mol.nao, round32(n)), dtype=torch.float32, device=eng.device)
+    Fd[:, :n] = torch.as_tensor(F.T, device=eng.device)
+    c = eng.relative(coords)
+    w = torch.as_tensor(weights, device=eng.device)
+    runs = []
+    for _ in range(3):
+        G = eng.g_multi(c, w, Fd, (0.0, 0.3), 1e-11)
+        runs.append((G.clone(), eng.last_stats['pairs_kept']))
+    for G, kept in runs[1:]:
+        assert torch.equal(G, runs[0][0])
+        assert kept == runs[0][1]
+
+
 # -- full K build vs the oracle and the reference --------------------------------
 
 def _k_gpu(mol, coords, weights, dm, omega, tile_tol=0.0, tile_pts=0,
