@@ -293,6 +293,40 @@ def vv10_timing(mol, dm, eng, torch, peak, calls=2):
             'parameters': 'b = 6.0, C = 0.01 (the wB97M-V VV10 set)'}
 
 
+def fp64_form_timing(eng, coords_d, w_d, qd_d, K_mixed, t_mixed, dm, torch,
+                     calls=2):
+    """The plain FP64 form of the same step (wb_cosx_get_k_fp64: FP64 AO
+    values, F kept in FP64, the same screen, FP64 G kernels, cuBLAS DGEMMs)
+    on the same inputs: its time per step, its model-flop rate, the
+    mixed-precision step's speed-up over it, and the mixed-precision K's
+    deviation from it (max |dK| / max |K| and 1/4 tr(D dK) per omega)."""
+    eng.get_k_fp64(coords_d, w_d, qd_d, OMEGAS, tile_tol=TILE_TOL)   # tables, warm-up
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(calls):
+        K64 = eng.get_k_fp64(coords_d, w_d, qd_d, OMEGAS, tile_tol=TILE_TOL,
+                             stats=False)
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / calls
+    eng.get_k_fp64(coords_d, w_d, qd_d, OMEGAS, tile_tol=TILE_TOL)
+    st = eng.last_stats
+    dev = {}
+    for i, w in enumerate(OMEGAS):
+        a = ((K_mixed[i] + K_mixed[i].T) * 0.5).cpu().numpy()
+        b = ((K64[i] + K64[i].T) * 0.5).cpu().numpy()
+        dev['omega=%g' % w] = {
+            'max_abs_dK_rel': float(np.abs(a - b).max() / np.abs(b).max()),
+            'quarter_tr_D_dK': float(0.25 * np.einsum('ij,ji->', dm, a - b))}
+    return {'ms_per_step': t * 1e3, 'model_flops_per_step': st['model_flops'],
+            'tflops': st['model_flops'] / t / 1e12,
+            'tasks_kept': st['pairs_kept'], 'tasks_total': st['pairs_total'],
+            'mixed_speedup': t / t_mixed, 'mixed_vs_fp64': dev,
+            'what': 'wb_cosx_get_k_fp64, both omegas, tile_tol %g, same inputs' % TILE_TOL}
+
+
 def run_sample(oracle, mol, g, dm, idx):
     coords = g.coords[idx]
     X = oracle.ao_eval(mol, coords)
@@ -376,6 +410,8 @@ def main():
     ap.add_argument('--ref-points', type=int, default=400)
     ap.add_argument('--no-xc', action='store_true',
                     help='skip the semilocal XC flow timing')
+    ap.add_argument('--no-fp64', action='store_true',
+                    help='skip the plain FP64 form timing')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -528,6 +564,9 @@ def main():
 
     xc_flow = None if args.no_xc else xc_flow_timing(mol, g, dm, eng, torch)
     vv10 = None if args.no_xc else vv10_timing(mol, dm, eng, torch, peak)
+    build_k(coords_d, w_d, qd_d)
+    fp64_form = None if args.no_fp64 else fp64_form_timing(
+        eng, coords_d, w_d, qd_d, K, t_step, dm, torch)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -548,6 +587,7 @@ def main():
             'cpu_baseline': cpu,
             'xc_flow': xc_flow,
             'vv10': vv10,
+            'fp64_form': fp64_form,
             'clocks': clocks.summary(),
             'gpu_launches': launches_step * args.steps,
             'tasks_kept': kept, 'tasks_total': total,

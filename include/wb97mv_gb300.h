@@ -149,6 +149,28 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
                         void* workspace, size_t workspace_bytes, void* stream,
                         wb_cosx_stats* stats);
 
+/* Plain FP64 form of the K build: the same steps as wb_cosx_get_k_multi
+ * with every step in FP64 and nothing rounded to FP32.  X (FP64 AO values)
+ * -> F = X QD (cuBLAS DGEMM, kept FP64) -> the same screen (block
+ * statistics of fl32(F), 32-point blocks, tile_tol) -> G by FP64 class
+ * kernels (FP64 Boys, McMurchie-Davidson recurrences, Hermite sums and
+ * contraction; G accumulated in FP64) -> K = X^T (w o G) (cuBLAS DGEMM).
+ * The whole grid is one tile.  k_out holds nomega (nao, nao) row-major
+ * unsymmetrised K, as wb_cosx_get_k_multi.  It is the comparison point of
+ * the mixed-precision path and an FP64 operator for the SCF tail; the
+ * reference's FP64 tail takes the hooks off and runs stock PySCF's
+ * get_k_only on the CPU (staging/schedule.py:329-334), so this entry has
+ * no GPU counterpart there.  The first call on a handle builds and uploads
+ * the FP64 pair tables (synchronous device allocation and copies), so it
+ * must not be inside a stream capture.  Workspace:
+ * wb_cosx_fp64_workspace_bytes(h, npts) (36 B per point and AO). */
+size_t wb_cosx_fp64_workspace_bytes(const wb_cosx* h, int64_t npts);
+int wb_cosx_get_k_fp64(wb_cosx* h, const double* coords, const double* weights,
+                       int64_t npts, const double* qd, int nomega,
+                       const double* omegas, double tile_tol, double* k_out,
+                       void* workspace, size_t workspace_bytes, void* stream,
+                       wb_cosx_stats* stats);
+
 /* The fused G kernels alone on one tile: f (nao, ldp) FP32 AO-major in,
  * g_out (nao, ldp) FP32 out (overwritten).  weights (npts,) FP64 feed the
  * screening estimate.  Replaces GpuKBuilder._tasks + _launch

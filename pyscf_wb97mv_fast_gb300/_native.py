@@ -46,6 +46,7 @@ EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_becke_partition', 'wb_fp32_fma_probe',
             'wb_ozaki_workspace_bytes', 'wb_cosx_ozaki_f', 'wb_cosx_ozaki_k',
             'wb_vv10_kernel_sum_noalloc',
+            'wb_cosx_fp64_workspace_bytes', 'wb_cosx_get_k_fp64',
             'wb_status_string',
             'wb_last_error', 'wb_version')
 
@@ -152,6 +153,10 @@ def _declare(lib):
         'wb_cosx_ozaki_f': (_INT, [_P, _P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
         'wb_cosx_ozaki_k': (_INT, [_P, _P, _P, _P, _I64, _INT, _P, _P,
                                    ctypes.c_size_t, _P]),
+        'wb_cosx_fp64_workspace_bytes': (ctypes.c_size_t, [_P, _I64]),
+        'wb_cosx_get_k_fp64': (_INT, [_P, _P, _P, _I64, _P, _INT, _P, _D, _P, _P,
+                                      ctypes.c_size_t, _P,
+                                      ctypes.POINTER(WbCosxStats)]),
         'wb_status_string': (ctypes.c_char_p, [_INT]),
         'wb_last_error': (ctypes.c_char_p, []),
         'wb_version': (_INT, []),

@@ -182,6 +182,38 @@ class CosxEngine:
             self.last_stats = st.as_dict()
         return out
 
+    def get_k_fp64(self, coords_rel, weights, qd, omegas, tile_tol=1e-11,
+                   out=None, stats=True):
+        """The plain FP64 form of get_k_multi: FP64 AO values, F = X QD kept
+        in FP64 (cuBLAS DGEMM), the same screen, G from the FP64 class
+        kernels (accumulated in FP64), K = X^T (w o G) by cuBLAS DGEMM; the
+        whole grid is one tile.  Returns (len(omegas), nao, nao) FP64 on
+        the device, unsymmetrised.  The first call on an engine uploads the
+        FP64 pair tables (synchronous)."""
+        torch = _torch()
+        om = [float(w) for w in omegas]
+        if not om:
+            raise ValueError('omegas is empty')
+        npts = int(coords_rel.shape[0])
+        nbytes = int(_native.lib().wb_cosx_fp64_workspace_bytes(self._h, npts))
+        ws = self.workspace(nbytes)
+        if out is None:
+            out = torch.empty((len(om), self.nao, self.nao), dtype=torch.float64,
+                              device=self.device)
+        if tuple(out.shape) != (len(om), self.nao, self.nao) or not out.is_contiguous():
+            raise ValueError('out must be a contiguous (%d, nao, nao) tensor' % len(om))
+        st = _native.WbCosxStats() if stats else None
+        arr = (_native.ctypes.c_double * len(om))(*om)
+        _native.check(_native.lib().wb_cosx_get_k_fp64(
+            self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
+            _native.ptr(qd.contiguous()), len(om), arr, float(tile_tol),
+            _native.ptr(out), _native.ptr(ws), nbytes, self._stream(),
+            _native.ctypes.byref(st) if st is not None else None),
+            'wb_cosx_get_k_fp64')
+        if st is not None:
+            self.last_stats = st.as_dict()
+        return out
+
     def g(self, coords_rel, weights, f, omega, tile_tol=0.0, out=None,
           stats=True):
         """G (nao, ld) FP32 from F (nao, ld) FP32 AO-major, one tile."""

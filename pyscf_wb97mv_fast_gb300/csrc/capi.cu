@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "host.hpp"
+#include "cosx_fp64.hpp"
 #include "generated/cosx_layout.h"
 #include "launch.hpp"
 #include "ozaki.hpp"
@@ -166,6 +167,13 @@ struct wb_cosx {
     int* border = nullptr;
     int64_t bo_stride = 0, bo_ld = -1;
     int bo_n[wb::NCLASS] = {0};
+    // FP64 pair data of the plain FP64 form (wb_cosx_get_k_fp64), uploaded
+    // on its first call: P per primitive pair, the class E blocks, the FP64
+    // Boys table followed by the FP64 c2s tables of l = 2, 3
+    double* f64_P = nullptr;
+    double* f64_E = nullptr;
+    double* f64_boys = nullptr;
+    long long f64_ebase[wb::NCLASS] = {0};
 };
 
 namespace {
@@ -547,6 +555,75 @@ int read_stats(wb_cosx* h, void* ws, const WsLayout& L, int64_t ntasks_total,
     return WB_OK;
 }
 
+// FP64 pair data, FP64 Boys table and the FP64 c2s constants of the plain
+// FP64 form, built and uploaded on its first call (synchronous copies)
+int ensure_fp64(wb_cosx* h) {
+    if (h->f64_P) return WB_OK;
+    wb::HostPairs64 hp64;
+    wb::build_pairs64(h->hp, hp64);
+    std::vector<double> tab((size_t)wb::kBoys64Nodes * wb::kBoys64Cols);
+    for (int k = 0; k < wb::kBoys64Nodes; ++k)
+        wb::boys_f64(wb::kBoys64Cols - 1, 0.25 * k,
+                     tab.data() + (size_t)k * wb::kBoys64Cols);
+    // the FP64 c2s tables after the Boys table: l = 2 (6 x 5), l = 3 (10 x 7)
+    const std::vector<double> d = wb::cart2sph(2), f = wb::cart2sph(3);
+    tab.insert(tab.end(), d.begin(), d.end());
+    tab.insert(tab.end(), f.begin(), f.end());
+    double *P = nullptr, *E = nullptr, *B = nullptr;
+    auto upload = [](double** dst, const std::vector<double>& v) -> cudaError_t {
+        cudaError_t e = cudaMalloc(dst, sizeof(double) * std::max<size_t>(v.size(), 1));
+        if (e != cudaSuccess) return e;
+        if (v.empty()) return cudaSuccess;
+        return cudaMemcpy(*dst, v.data(), sizeof(double) * v.size(),
+                          cudaMemcpyHostToDevice);
+    };
+    cudaError_t e = upload(&P, hp64.P);
+    if (e == cudaSuccess) e = upload(&E, hp64.E);
+    if (e == cudaSuccess) e = upload(&B, tab);
+    if (e != cudaSuccess) {
+        if (P) cudaFree(P);
+        if (E) cudaFree(E);
+        if (B) cudaFree(B);
+        return cuda_fail(e, "FP64 pair tables");
+    }
+    h->f64_P = P;
+    h->f64_E = E;
+    h->f64_boys = B;
+    for (int c = 0; c < wb::NCLASS; ++c) h->f64_ebase[c] = hp64.e_base[c];
+    return WB_OK;
+}
+
+struct WsLayout64 {
+    WsLayout base;                  // counters, work, block statistics
+    size_t X = 0, F64 = 0, F32 = 0, G64 = 0, WG = 0, total = 0;
+};
+
+WsLayout64 ws_layout_fp64(const wb_cosx* h, int64_t ld) {
+    WsLayout64 L;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align256(off + bytes);
+        return o;
+    };
+    L.base.counters = take(sizeof(unsigned long long) * 3 * wb::NCLASS);
+    L.base.work = take(sizeof(int) * 2 * wb::NCLASS);
+    for (int b = 0; b < 3; ++b) {
+        const int64_t bp = 32 << b;
+        const int64_t nblk = (ld + bp - 1) / bp;
+        L.base.subcr[b] = take(sizeof(float4) * (size_t)nblk);
+        L.base.msh[b] = take(sizeof(float) * (size_t)nblk * std::max(h->hp.nvshell, 1));
+    }
+    const size_t n = (size_t)h->hp.nao * ld;
+    L.X = take(sizeof(double) * n);
+    L.F64 = take(sizeof(double) * n);
+    L.F32 = take(sizeof(float) * n);
+    L.G64 = take(sizeof(double) * n);
+    L.WG = take(sizeof(double) * n);
+    L.total = off;
+    return L;
+}
+
 }  // namespace
 
 extern "C" {
@@ -799,6 +876,9 @@ int wb_cosx_destroy(wb_cosx* h) {
     if (h->block) cudaFree(h->block);
     if (h->bcost) cudaFree(h->bcost);
     if (h->border) cudaFree(h->border);
+    if (h->f64_P) cudaFree(h->f64_P);
+    if (h->f64_E) cudaFree(h->f64_E);
+    if (h->f64_boys) cudaFree(h->f64_boys);
     delete h;
     return WB_OK;
 }
@@ -1036,6 +1116,125 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
     if (st == WB_OK && prof)
         for (int i = 0; i < 6; ++i) stats->phase_ms[i] = phase[i];
     return st;
+}
+
+size_t wb_cosx_fp64_workspace_bytes(const wb_cosx* h, int64_t npts) {
+    if (!h || npts < 0) return 0;
+    return ws_layout_fp64(h, round32(std::max<int64_t>(npts, 1))).total;
+}
+
+int wb_cosx_get_k_fp64(wb_cosx* h, const double* coords, const double* weights,
+                       int64_t npts, const double* qd, int nomega,
+                       const double* omegas, double tile_tol, double* k_out,
+                       void* workspace, size_t workspace_bytes, void* stream,
+                       wb_cosx_stats* stats) {
+    if (!h || !k_out || !qd || npts < 0 || (npts && (!coords || !weights)) ||
+        nomega < 1 || !omegas)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_get_k_fp64: bad arguments");
+    for (int j = 0; j < nomega; ++j)
+        if (!(omegas[j] >= 0.0))
+            return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_get_k_fp64: omega must be >= 0");
+    if (!(tile_tol >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_get_k_fp64: tile_tol must be >= 0");
+    const int64_t ld = round32(std::max<int64_t>(npts, 1));
+    if (ld > INT32_MAX - 64)
+        return fail(WB_ERR_UNSUPPORTED, "wb_cosx_get_k_fp64: above 2^31 points");
+    const WsLayout64 L = ws_layout_fp64(h, ld);
+    if (!workspace || workspace_bytes < L.total)
+        return fail(WB_ERR_WORKSPACE, "wb_cosx_get_k_fp64: workspace needs " +
+                                          std::to_string(L.total) + " bytes");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int nao = h->hp.nao;
+    const size_t kk = (size_t)nao * nao;
+    WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.base.counters), 0,
+                            sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+    int launches = 1;
+    if (npts == 0) {
+        WB_CUDA(cudaMemsetAsync(k_out, 0, sizeof(double) * kk * nomega, s));
+        return read_stats(h, workspace, L.base, 0, s, stats, launches);
+    }
+    int st = ensure_fp64(h);
+    if (st != WB_OK) return st;
+    WB_CUBLAS(cublasSetStream(h->cublas, s));
+    WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+    double* X = at<double>(workspace, L.X);
+    double* F64 = at<double>(workspace, L.F64);
+    float* F32 = at<float>(workspace, L.F32);
+    double* G64 = at<double>(workspace, L.G64);
+    double* WG = at<double>(workspace, L.WG);
+    const double one = 1.0, zero = 0.0;
+    wb::AoArgs ao;
+    ao.coords = coords; ao.npts = npts; ao.ld = ld; ao.nbas = h->nbas;
+    ao.sh_l = h->sh_l; ao.sh_np = h->sh_np; ao.sh_nc = h->sh_nc;
+    ao.sh_eoff = h->sh_eoff; ao.sh_coff = h->sh_coff; ao.sh_ao0 = h->sh_ao0;
+    ao.sh_ctr = h->sh_ctr; ao.exps = h->exps; ao.coeffs = h->coeffs; ao.X = X;
+    ao.nao = nao;
+    WB_CUDA(wb::launch_ao_eval(ao, s));
+    // F = X QD in FP64 (no rounding); its FP32 copy feeds only the block
+    // statistics of the screen, as in the mixed-precision path
+    WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)ld, nao, nao,
+                          &one, X, (int)ld, qd, nao, &zero, F64, (int)ld));
+    WB_CUDA(wb::launch_f64_to_f32(F64, F32, (int64_t)nao * ld, s));
+    wb::BlockStatsOut bo;
+    for (int b = 0; b < 3; ++b) {
+        bo.cr[b] = at<float4>(workspace, L.base.subcr[b]);
+        bo.msh[b] = at<float>(workspace, L.base.msh[b]);
+    }
+    WB_CUDA(wb::launch_sub_stats(coords, weights, F32, npts, ld, h->hp.nvshell,
+                                 h->vs_ao0, h->vs_nf, bo, s));
+    launches += 4;
+    wb::CosxF64Args a;
+    std::memset(&a, 0, sizeof(a));
+    a.F = F64;
+    a.G = G64;
+    a.coords = coords;
+    a.ld = ld;
+    a.npts = (int)npts;
+    a.khdr = h->khdr;
+    a.pshell = h->pshell;
+    a.ptau = h->ptau;
+    a.bnd = h->bnd;
+    a.bpref = h->bpref;
+    a.blk_cr = bo.cr[0];
+    a.blk_msh = bo.msh[0];
+    a.nblk = (int)(ld / 32);
+    a.nvshell = h->hp.nvshell;
+    a.tol = tile_tol > 0.0 ? (float)(tile_tol / 1.001) : 0.0f;
+    if (tile_tol > 0.0 && a.tol <= 0.0f) a.tol = 1e-38f;
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        a.pp_begin[c] = h->hp.cls[c].pp_begin;
+        a.e_base[c] = h->f64_ebase[c];
+    }
+    a.P = h->f64_P;
+    a.p = h->p;
+    a.pref = h->pref;
+    a.E = h->f64_E;
+    a.boys = h->f64_boys;
+    a.c2s = h->f64_boys + (size_t)wb::kBoys64Nodes * wb::kBoys64Cols;
+    a.pflops = h->pflops;
+    a.pnint = h->pnint;
+    a.counters = at<unsigned long long>(workspace, L.base.counters);
+    a.work = at<int>(workspace, L.base.work);
+    int64_t ntasks = 0;
+    for (int j = 0; j < nomega; ++j) {
+        a.omega = omegas[j];
+        WB_CUDA(cudaMemsetAsync(G64, 0, sizeof(double) * (size_t)nao * ld, s));
+        WB_CUDA(cudaMemsetAsync(a.work, 0, sizeof(int) * wb::NCLASS, s));
+        launches += 2;
+        for (int c = 0; c < wb::NCLASS; ++c) {
+            const int pb = h->hp.cls[c].pair_begin, pe = h->hp.cls[c].pair_end;
+            if (pe <= pb) continue;
+            WB_CUDA(wb::launch_cosx_fp64_class(c, a, pb, pe, h->nsm, s));
+            ++launches;
+        }
+        ntasks += (ld / 32) * (int64_t)h->hp.npairs;
+        WB_CUDA(wb::launch_weight_g64(G64, weights, npts, ld, nao, WG, s));
+        WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nao, nao, (int)ld,
+                              &one, WG, (int)ld, X, (int)ld, &zero, k_out + kk * j,
+                              nao));
+        launches += 2;
+    }
+    return read_stats(h, workspace, L.base, ntasks, s, stats, launches);
 }
 
 int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,

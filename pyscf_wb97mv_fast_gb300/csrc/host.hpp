@@ -95,6 +95,18 @@ struct HostPairs {
 int build_pairs(const wb_basis& b, const double origin[3], double cutoff,
                 HostPairs& out, std::string& err);
 
+// FP64 pair data of the plain FP64 G kernels (cosx_fp64.cu), per primitive
+// pair in the order of the pair tables: P (3 per pair, molecule frame) and,
+// in one block per class, the Hermite E^{i,j}_t of the three axes laid out
+// [axis][i][j][t] (i <= la, j <= lb, t <= i + j, E^{00}_0 = 1 included).
+int e64_axis(int la, int lb);        // sum_{i <= la, j <= lb} (i + j + 1)
+struct HostPairs64 {
+    std::vector<double> P;
+    std::vector<double> E;
+    int64_t e_base[NCLASS] = {0};    // double offset of each class's E block
+};
+void build_pairs64(const HostPairs& hp, HostPairs64& out);
+
 // FLOP model of one (bra ish, ket jsh) task per grid point.
 int64_t model_flops(int la, int lb, int npi, int npj, bool diag);
 

@@ -215,6 +215,50 @@ static double bound_c(int la, int lb, double p, double a, double b) {
     return f * 1.01;
 }
 
+int e64_axis(int la, int lb) { return e_count_axis(la, lb) + 1; }
+
+void build_pairs64(const HostPairs& hp, HostPairs64& out) {
+    out = HostPairs64();
+    int lofc[NCLASS][2];
+    for (int x = 0; x <= LMAX; ++x)
+        for (int y = 0; y <= x; ++y) {
+            lofc[class_of(x, y)][0] = x;
+            lofc[class_of(x, y)][1] = y;
+        }
+    int64_t base = 0;
+    for (int c = 0; c < NCLASS; ++c) {
+        out.e_base[c] = base;
+        base += (int64_t)(hp.cls[c].pp_end - hp.cls[c].pp_begin) * 3 *
+                e64_axis(lofc[c][0], lofc[c][1]);
+    }
+    out.P.resize(3 * (size_t)hp.npp);
+    out.E.resize((size_t)base);
+    // primitive pairs follow the pair order, bra primitive outer (as in
+    // build_pairs), so pair k's first one is hdr[4k + 2]
+    for (int k = 0; k < hp.npairs; ++k) {
+        const VShell& A = hp.vsh[hp.pshell[2 * k]];
+        const VShell& B = hp.vsh[hp.pshell[2 * k + 1]];
+        const int c = hp.pclass[k], la = A.l, lb = B.l, nax = e64_axis(la, lb);
+        int pp = hp.hdr[4 * k + 2];
+        for (int a = 0; a < A.nprim; ++a)
+            for (int bb = 0; bb < B.nprim; ++bb, ++pp) {
+                const double al = A.exps[a], be = B.exps[bb], p = al + be;
+                double* e = out.E.data() + out.e_base[c] +
+                            (int64_t)(pp - hp.cls[c].pp_begin) * 3 * nax;
+                for (int x = 0; x < 3; ++x) {
+                    const double P = (al * A.A[x] + be * B.A[x]) / p;
+                    out.P[3 * (size_t)pp + x] = P;
+                    double E[4][4][7];
+                    hermite_axis(la, lb, p, P - A.A[x], P - B.A[x], E);
+                    int q = 0;
+                    for (int i = 0; i <= la; ++i)
+                        for (int j = 0; j <= lb; ++j)
+                            for (int t = 0; t <= i + j; ++t) e[x * nax + q++] = E[i][j][t];
+                }
+            }
+    }
+}
+
 int64_t model_flops(int la, int lb, int npi, int npj, bool diag) {
     const int L = la + lb;
     const int NA = nsph(la), NB = nsph(lb);
