@@ -327,6 +327,81 @@ def fp64_form_timing(eng, coords_d, w_d, qd_d, K_mixed, t_mixed, dm, torch,
             'what': 'wb_cosx_get_k_fp64, both omegas, tile_tol %g, same inputs' % TILE_TOL}
 
 
+def serving_requests(n_solves=16, cycles=3, seed=5):
+    """Seeded SCF-shaped requests of uneven size: water clusters of 4-32
+    waters (synthetic def2-SVP) and all-trans alkanes C6-C14 (synthetic
+    def2-TZVP, f shells), level-0 grids, `cycles` exchange builds each with
+    seeded densities (D = 2 C C^T, C orthonormal with the molecule's
+    occupied count)."""
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    from pyscf_wb97mv_fast_gb300.systems import alkane, water_cluster
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_solves):
+        if rng.random() < 0.5:
+            n = int(rng.integers(4, 33))
+            mol = Molecule.build(water_cluster(n, box=max(5.0, 3.2 * n ** (1.0 / 3.0)),
+                                               seed=100 + i), 'synthetic-svp')
+            nocc, name = 5 * n, 'water%d/svp' % n
+        else:
+            n = int(rng.integers(6, 15))
+            mol = Molecule.build(alkane(n), 'synthetic-tzvp')
+            nocc, name = 4 * n + 1, 'C%dH%d/tzvp' % (n, 2 * n + 2)
+        g = build_grids(mol, level=0)
+        dms = []
+        for c in range(cycles):
+            r = np.random.default_rng(seed * 1000 + i * 10 + c)
+            q, _ = np.linalg.qr(r.normal(size=(mol.nao, nocc)))
+            dms.append(2.0 * q @ q.T)
+        out.append((name, mol, g.coords, g.weights, dms))
+    return out
+
+
+def serving_timing(torch, rates=(4.0, 16.0), slots=4, seed=5):
+    """Continuous batching of SCF-shaped requests (serving.ExchangeServer):
+    the plain per-request form (one request at a time, back to back) and
+    seeded Poisson arrivals at each rate with `slots` builds in flight;
+    solves/s and p50/p99 time-to-result, and whether every served result is
+    bitwise the result of the plain form."""
+    from pyscf_wb97mv_fast_gb300.serving import (ExchangeServer, Solve,
+                                                 poisson_arrivals, solve_summary)
+    reqs = serving_requests(seed=seed)
+    # warm-up: library, cuBLAS heuristics, pinned-memory pool
+    srv = ExchangeServer(slots=1)
+    Solve(srv, *reqs[0][1:4], reqs[0][4][:1]).run()
+    srv.close()
+    srv = ExchangeServer(slots=1)
+    plain = [Solve(srv, m, c, w, d, tag=nm) for nm, m, c, w, d in reqs]
+    for s in plain:
+        s.run()
+    srv.close()
+    out = {'requests': [r[0] for r in reqs], 'cycles_per_solve': len(reqs[0][4]),
+           'grid': 'level 0', 'omegas': list(OMEGAS), 'k_tile_tol': TILE_TOL,
+           'plain': solve_summary(plain), 'served': {}}
+    for rate in rates:
+        srv = ExchangeServer(slots=slots)
+        arr = poisson_arrivals(len(reqs), rate, seed)
+        solves = [Solve(srv, m, c, w, d, tag=nm) for nm, m, c, w, d in reqs]
+        t0 = time.perf_counter()
+        for s, t in zip(solves, arr):
+            dt = t0 + t - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            s.start()
+        for s in solves:
+            s.join()
+        srv.close()
+        same = all(all(np.array_equal(a, b) for a, b in zip(s.results, p.results))
+                   for s, p in zip(solves, plain))
+        summ = solve_summary(solves)
+        summ.update({'rate_per_s': rate, 'slots': slots,
+                     'max_concurrent_builds': srv.scheduler.max_running,
+                     'bitwise_equal_to_plain': bool(same)})
+        out['served']['rate=%g' % rate] = summ
+    return out
+
+
 def run_sample(oracle, mol, g, dm, idx):
     coords = g.coords[idx]
     X = oracle.ao_eval(mol, coords)
@@ -412,6 +487,8 @@ def main():
                     help='skip the semilocal XC flow timing')
     ap.add_argument('--no-fp64', action='store_true',
                     help='skip the plain FP64 form timing')
+    ap.add_argument('--no-serving', action='store_true',
+                    help='skip the continuous-batching serving leg')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -567,6 +644,7 @@ def main():
     build_k(coords_d, w_d, qd_d)
     fp64_form = None if args.no_fp64 else fp64_form_timing(
         eng, coords_d, w_d, qd_d, K, t_step, dm, torch)
+    serving = None if (args.no_serving or world > 1) else serving_timing(torch)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -588,6 +666,7 @@ def main():
             'xc_flow': xc_flow,
             'vv10': vv10,
             'fp64_form': fp64_form,
+            'serving': serving,
             'clocks': clocks.summary(),
             'gpu_launches': launches_step * args.steps,
             'tasks_kept': kept, 'tasks_total': total,

@@ -1,0 +1,435 @@
+"""Continuous batching of COSX exchange builds on one GPU.
+
+The reference runs one SCF at a time.  Batch throughput is an explicit
+non-goal there (docs/design.en.md:44), and its K builder serves one
+molecule per call (gpu/sgx_k.py:663-751).  This module serves many
+molecules at once.
+
+* A *session* is one molecule whose state stays on the device between
+  requests: the engine's packed shell pairs (the C-ABI handle) and the
+  grid coordinates and weights.  This is the state an SCF keeps across
+  cycles.
+* A *request* is one exchange build of a session: a new density in, K for
+  every omega of the session out (wb_cosx_get_k_multi).  This is the K
+  work of one SCF cycle.
+
+Requests that arrive while others run on the GPU are admitted as soon as a
+slot and enough device memory are free.  Admission scans the queue in
+arrival order and takes the first request that fits (first fit), so a
+large request at the head does not stall small ones behind it.  A session
+runs one request at a time, in submission order.  Each slot is a host
+thread with its own CUDA stream, so the builds of different slots overlap
+on the device.
+
+Memory.  A running request holds its build's workspace
+(wb_cosx_workspace_bytes), its density and its K buffers.  An open session
+holds its pair tables and grid.  Admission keeps the sum of running
+footprints plus the resident session bytes under the budget (default 60 %
+of the free device memory, the reference's mem_fraction,
+gpu/install.py:209).  A request whose session could never fit is rejected
+at submit time.
+
+Determinism.  Every kernel of a build has a fixed summation order that
+does not depend on launch shape, block order or what else runs on the
+device.  So a request returns bitwise the same K alone and in a mix.
+
+The scheduling core (Scheduler) is plain Python with no GPU.  The GPU
+executor (ExchangeServer) plugs CosxEngine calls into it.
+"""
+import collections
+import threading
+import time
+
+import numpy as np
+
+
+class Rejected(ValueError):
+    """A request that can never be admitted (its footprint exceeds the
+    budget) or a server that is closed."""
+
+
+class Future:
+    """Result handle of one request."""
+
+    def __init__(self, tag=None):
+        self.tag = tag
+        self._ev = threading.Event()
+        self._value = None
+        self._error = None
+        self.t_submit = time.perf_counter()
+        self.t_start = None
+        self.t_done = None
+
+    def _finish(self, value=None, error=None):
+        self._value, self._error = value, error
+        self.t_done = time.perf_counter()
+        self._ev.set()
+
+    def done(self):
+        return self._ev.is_set()
+
+    def result(self, timeout=None):
+        if not self._ev.wait(timeout):
+            raise TimeoutError('request not finished')
+        if self._error is not None:
+            raise self._error
+        return self._value
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.t_submit
+
+    @property
+    def queued(self):
+        return None if self.t_start is None else self.t_start - self.t_submit
+
+
+class Scheduler:
+    """Slots, a memory budget and a queue; GPU-free.
+
+    run_fn(job, slot) executes one admitted job on worker `slot` (0 ..
+    slots - 1) and returns its value.  Jobs carry .footprint (bytes while
+    running) and .key (jobs with the same key run one at a time, in
+    submission order).
+    """
+
+    def __init__(self, run_fn, slots=4, budget=None):
+        if slots < 1:
+            raise ValueError('slots must be >= 1')
+        self.run_fn = run_fn
+        self.slots = int(slots)
+        self.budget = None if budget is None else int(budget)
+        self.resident = 0                # bytes held outside running jobs
+        self._queue = collections.deque()
+        self._busy_keys = set()
+        self._used = 0
+        self._running = 0
+        self._closed = False
+        self._cv = threading.Condition()
+        self.max_running = 0             # high-water marks (tests, reports)
+        self.max_used = 0
+        self._workers = [threading.Thread(target=self._worker, args=(i,),
+                                          daemon=True, name='cosx-slot-%d' % i)
+                         for i in range(self.slots)]
+        for t in self._workers:
+            t.start()
+
+    # -- resident bytes (sessions) ------------------------------------------
+    def reserve(self, nbytes):
+        with self._cv:
+            if self.budget is not None and self.resident + nbytes > self.budget:
+                raise Rejected('resident state of %d bytes exceeds the budget '
+                               '(%d of %d bytes held)' % (nbytes, self.resident,
+                                                           self.budget))
+            self.resident += int(nbytes)
+
+    def release(self, nbytes):
+        with self._cv:
+            self.resident -= int(nbytes)
+            self._cv.notify_all()
+
+    # -- jobs ------------------------------------------------------------------
+    def submit(self, job, tag=None):
+        fut = Future(tag)
+        with self._cv:
+            if self._closed:
+                raise Rejected('scheduler is closed')
+            if self.budget is not None and job.footprint + self.resident > self.budget:
+                raise Rejected('request footprint %d bytes (+ %d resident) exceeds '
+                               'the budget of %d bytes' % (job.footprint,
+                                                           self.resident, self.budget))
+            self._queue.append((job, fut))
+            self._cv.notify_all()
+        return fut
+
+    def _fits(self, job):
+        if job.key in self._busy_keys:
+            return False
+        if self.budget is None:
+            return True
+        return self._used + job.footprint + self.resident <= self.budget
+
+    def _take(self):
+        # first fit in arrival order; a key's jobs keep their order (an
+        # earlier job of a busy or waiting key blocks its later ones)
+        blocked = set()
+        for i, (job, fut) in enumerate(self._queue):
+            if job.key in blocked:
+                continue
+            if self._fits(job):
+                del self._queue[i]
+                return job, fut
+            blocked.add(job.key)
+        return None
+
+    def _worker(self, slot):
+        while True:
+            with self._cv:
+                item = None
+                while not self._closed or self._queue:
+                    item = self._take()
+                    if item is not None:
+                        break
+                    if self._closed and not self._queue:
+                        break
+                    self._cv.wait()
+                if item is None:
+                    return
+                job, fut = item
+                self._busy_keys.add(job.key)
+                self._used += job.footprint
+                self._running += 1
+                self.max_running = max(self.max_running, self._running)
+                self.max_used = max(self.max_used, self._used + self.resident)
+                fut.t_start = time.perf_counter()
+            value, error = None, None
+            try:
+                value = self.run_fn(job, slot)
+            except BaseException as e:           # noqa: BLE001 -- handed to the caller
+                error = e
+            with self._cv:
+                self._busy_keys.discard(job.key)
+                self._used -= job.footprint
+                self._running -= 1
+                self._cv.notify_all()
+            fut._finish(value, error)
+
+    def close(self, wait=True):
+        """No more submissions; the queued jobs still run."""
+        with self._cv:
+            self._closed = True
+            self._cv.notify_all()
+        if wait:
+            for t in self._workers:
+                t.join()
+
+
+def latency_summary(futures):
+    """p50 / p99 / mean latency (s), requests per second over the span
+    from the first submit to the last completion."""
+    lat = np.array([f.latency for f in futures if f.latency is not None])
+    if not len(lat):
+        return {'requests': 0}
+    t0 = min(f.t_submit for f in futures)
+    t1 = max(f.t_done for f in futures if f.t_done is not None)
+    q = np.array([f.queued for f in futures if f.queued is not None])
+    return {'requests': int(len(lat)),
+            'p50_s': float(np.percentile(lat, 50)),
+            'p99_s': float(np.percentile(lat, 99)),
+            'mean_s': float(lat.mean()),
+            'queued_p50_s': float(np.percentile(q, 50)) if len(q) else None,
+            'span_s': float(t1 - t0),
+            'requests_per_s': float(len(lat) / (t1 - t0)) if t1 > t0 else None}
+
+
+class _Job:
+    __slots__ = ('session', 'dm', 'footprint', 'key')
+
+    def __init__(self, session, dm, footprint):
+        self.session = session
+        self.dm = dm
+        self.footprint = footprint
+        self.key = id(session)
+
+
+class Session:
+    """One molecule resident on the device: its engine (packed shell
+    pairs) and grid.  Open through ExchangeServer.open_session."""
+
+    def __init__(self, server, mol, coords, weights, omegas, tile_tol):
+        import torch
+        from .cosx import CosxEngine
+        self.server = server
+        self.engine = CosxEngine(mol, device=server.device.index)
+        self.coords = self.engine.relative(coords)
+        self.weights = torch.as_tensor(np.ascontiguousarray(weights, dtype=np.float64),
+                                       device=server.device)
+        self.omegas = tuple(float(w) for w in omegas)
+        self.tile_tol = float(tile_tol)
+        self.nao = self.engine.nao
+        self.npts = int(self.coords.shape[0])
+        nom = len(self.omegas)
+        kb = 8 * nom * self.nao * self.nao
+        # running footprint: the build's workspace, D, K and its symmetrised
+        # copy; resident: the pair tables are small next to the grid arrays
+        self.footprint = (self.engine.workspace_bytes(self.npts) +
+                          8 * self.nao * self.nao + 2 * kb)
+        self.resident = 32 * self.npts + kb
+        self.closed = False
+
+    def submit(self, dm):
+        """One exchange build with density dm (nao, nao) FP64 (host):
+        returns a Future whose result is K (len(omegas), nao, nao) FP64 on
+        the host, symmetrised as the reference returns it."""
+        return self.server._submit(self, dm)
+
+    def close(self):
+        if not self.closed:
+            self.closed = True
+            self.server._close_session(self)
+
+
+class ExchangeServer:
+    """Continuous-batching exchange builds on one GPU (module docstring).
+
+    slots: builds in flight at once (one host thread + CUDA stream each).
+    budget: device bytes for running builds + open sessions (default: 60 %
+    of the free device memory at start-up).  gemm: the K build's GEMM mode.
+    """
+
+    def __init__(self, device=0, slots=4, budget=None, gemm='ozaki'):
+        import torch
+        self.device = torch.device('cuda', device if isinstance(device, int)
+                                   else torch.device(device).index or 0)
+        if budget is None:
+            free, _ = torch.cuda.mem_get_info(self.device)
+            budget = int(0.6 * free)
+        self.gemm = gemm
+        self._streams = [torch.cuda.Stream(device=self.device) for _ in range(slots)]
+        self._sched = Scheduler(self._run, slots=slots, budget=budget)
+        self.futures = []
+
+    @property
+    def scheduler(self):
+        return self._sched
+
+    def open_session(self, mol, coords, weights, omegas=(0.0, 0.3), tile_tol=1e-11):
+        s = Session(self, mol, coords, weights, omegas, tile_tol)
+        try:
+            self._sched.reserve(s.resident)
+        except Rejected:
+            s.engine.close()
+            raise
+        return s
+
+    def _close_session(self, s):
+        self._sched.release(s.resident)
+        s.engine.close()
+
+    def _submit(self, session, dm):
+        if session.closed:
+            raise Rejected('session is closed')
+        dm = np.ascontiguousarray(dm, dtype=np.float64)
+        if dm.shape != (session.nao, session.nao):
+            raise ValueError('dm must be (%d, %d)' % (session.nao, session.nao))
+        fut = self._sched.submit(_Job(session, dm, session.footprint))
+        self.futures.append(fut)
+        return fut
+
+    def _run(self, job, slot):
+        import torch
+        s = job.session
+        eng = s.engine
+        stream = self._streams[slot]
+        nom = len(s.omegas)
+        with torch.cuda.device(self.device), torch.cuda.stream(stream):
+            dm_h = torch.from_numpy(job.dm).pin_memory()
+            dm_d = torch.empty((s.nao, s.nao), dtype=torch.float64, device=self.device)
+            dm_d.copy_(dm_h, non_blocking=True)
+            K = eng.get_k_multi(s.coords, s.weights, dm_d, s.omegas,
+                                tile_tol=s.tile_tol, gemm=self.gemm, stats=False)
+            Ks = (K + K.transpose(1, 2)) * 0.5
+            out = torch.empty((nom, s.nao, s.nao), dtype=torch.float64).pin_memory()
+            out.copy_(Ks, non_blocking=True)
+            done = torch.cuda.Event()
+            done.record(stream)
+        done.synchronize()
+        # the workspace goes back to the allocator's cache for other builds
+        eng._ws = None
+        del K, Ks, dm_d
+        return out.numpy()
+
+    def close(self):
+        self._sched.close(wait=True)
+
+    def summary(self):
+        out = latency_summary(self.futures)
+        out['slots'] = self._sched.slots
+        out['budget_bytes'] = self._sched.budget
+        out['max_concurrent'] = self._sched.max_running
+        out['max_bytes_admitted'] = self._sched.max_used
+        return out
+
+
+def poisson_arrivals(n, rate, seed):
+    """n arrival times (s) of a Poisson process of the given rate."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))
+
+
+def replay(submit_fns, arrivals):
+    """Calls submit_fns[i]() at arrivals[i] seconds after the start (real
+    time, one thread); returns the futures in order."""
+    t0 = time.perf_counter()
+    futs = []
+    for fn, t in zip(submit_fns, arrivals):
+        dt = t0 + t - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        futs.append(fn())
+    return futs
+
+
+class Solve:
+    """One SCF-shaped request: open a session for a molecule and run its
+    exchange builds one after another (each cycle's density depends on the
+    previous cycle's result in an SCF, so a solve's builds never overlap
+    each other; different solves overlap freely).  run() returns the K of
+    every cycle; t_arrival / t_done bracket the whole solve."""
+
+    def __init__(self, server, mol, coords, weights, densities, omegas=(0.0, 0.3),
+                 tile_tol=1e-11, tag=None):
+        self.server = server
+        self.mol, self.coords, self.weights = mol, coords, weights
+        self.densities = list(densities)
+        self.omegas, self.tile_tol, self.tag = omegas, tile_tol, tag
+        self.t_arrival = self.t_done = None
+        self.results = None
+        self.error = None
+        self._thread = None
+
+    def run(self):
+        self.t_arrival = time.perf_counter()
+        sess = self.server.open_session(self.mol, self.coords, self.weights,
+                                        self.omegas, self.tile_tol)
+        try:
+            self.results = [sess.submit(dm).result() for dm in self.densities]
+        finally:
+            sess.close()
+            self.t_done = time.perf_counter()
+        return self.results
+
+    def start(self):
+        """run() on a client thread (errors kept in .error)."""
+        def body():
+            try:
+                self.run()
+            except BaseException as e:            # noqa: BLE001
+                self.error = e
+        self._thread = threading.Thread(target=body, daemon=True)
+        self._thread.start()
+        return self
+
+    def join(self, timeout=None):
+        self._thread.join(timeout)
+        if self.error is not None:
+            raise self.error
+        return self.results
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.t_arrival
+
+
+def solve_summary(solves):
+    """Time-to-result of whole solves: p50 / p99 (s) and solves per second
+    over the span from the first arrival to the last completion."""
+    lat = np.array([s.latency for s in solves if s.latency is not None])
+    if not len(lat):
+        return {'solves': 0}
+    t0 = min(s.t_arrival for s in solves)
+    t1 = max(s.t_done for s in solves if s.t_done is not None)
+    return {'solves': int(len(lat)), 'p50_s': float(np.percentile(lat, 50)),
+            'p99_s': float(np.percentile(lat, 99)), 'mean_s': float(lat.mean()),
+            'span_s': float(t1 - t0),
+            'solves_per_s': float(len(lat) / (t1 - t0)) if t1 > t0 else None}

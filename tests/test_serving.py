@@ -1,0 +1,129 @@
+"""The continuous-batching scheduler (serving.Scheduler) on the CPU: slots,
+memory budget, first-fit admission, per-session order, errors.  The GPU
+executor is covered by tests/test_gpu_serving.py."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from pyscf_wb97mv_fast_gb300.serving import (Rejected, Scheduler, latency_summary,
+                                             poisson_arrivals, replay)
+
+
+class Job:
+    def __init__(self, name, footprint, key, dur=0.02):
+        self.name, self.footprint, self.key, self.dur = name, footprint, key, dur
+
+
+class Recorder:
+    def __init__(self):
+        self.lock = threading.Lock()
+        self.running = {}
+        self.max_running = 0
+        self.max_bytes = 0
+        self.order = []
+        self.overlaps = []
+
+    def __call__(self, job, slot):
+        with self.lock:
+            for other in self.running.values():
+                assert other.key != job.key, 'two jobs of one key at once'
+            self.running[job.name] = job
+            self.max_running = max(self.max_running, len(self.running))
+            self.max_bytes = max(self.max_bytes,
+                                 sum(j.footprint for j in self.running.values()))
+            self.order.append(job.name)
+        time.sleep(job.dur)
+        with self.lock:
+            del self.running[job.name]
+        return job.name, slot
+
+
+def test_slots_and_budget_are_never_exceeded():
+    rec = Recorder()
+    s = Scheduler(rec, slots=3, budget=100)
+    futs = [s.submit(Job('j%d' % i, 30 + (i % 3) * 10, key=i)) for i in range(24)]
+    s.close()
+    assert [f.result()[0] for f in futs] == ['j%d' % i for i in range(24)]
+    assert rec.max_running <= 3
+    assert rec.max_bytes <= 100
+    assert rec.max_running >= 2            # work did overlap
+    assert s.max_running == rec.max_running
+
+
+def test_first_fit_lets_small_jobs_pass_a_large_one():
+    rec = Recorder()
+    s = Scheduler(rec, slots=4, budget=100)
+    a = s.submit(Job('a', 60, key='a', dur=0.2))
+    time.sleep(0.05)                       # a is running
+    big = s.submit(Job('big', 80, key='big', dur=0.01))   # waits for a
+    small = s.submit(Job('small', 30, key='small', dur=0.01))
+    small.result(5)
+    assert not big.done()                  # small passed big
+    s.close()
+    assert big.result() and a.result()
+    assert rec.order.index('small') < rec.order.index('big')
+
+
+def test_jobs_of_one_key_run_in_submission_order():
+    rec = Recorder()
+    s = Scheduler(rec, slots=4, budget=None)
+    futs = [s.submit(Job('s%d' % i, 1, key='same', dur=0.005)) for i in range(10)]
+    futs += [s.submit(Job('o%d' % i, 1, key='o%d' % i, dur=0.005)) for i in range(5)]
+    s.close()
+    for f in futs:
+        f.result()
+    same = [n for n in rec.order if n.startswith('s')]
+    assert same == ['s%d' % i for i in range(10)]
+
+
+def test_rejections_and_errors():
+    def boom(job, slot):
+        raise RuntimeError('kernel failed: ' + job.name)
+    s = Scheduler(boom, slots=2, budget=50)
+    with pytest.raises(Rejected):
+        s.submit(Job('huge', 51, key=1))
+    s.reserve(20)
+    with pytest.raises(Rejected):
+        s.submit(Job('now too big', 40, key=2))
+    with pytest.raises(Rejected):
+        s.reserve(40)
+    f = s.submit(Job('x', 10, key=3))
+    with pytest.raises(RuntimeError, match='kernel failed: x'):
+        f.result(5)
+    s.release(20)
+    s.close()
+    with pytest.raises(Rejected):
+        s.submit(Job('late', 1, key=4))
+    with pytest.raises(ValueError):
+        Scheduler(boom, slots=0)
+
+
+def test_resident_bytes_count_against_admission():
+    rec = Recorder()
+    s = Scheduler(rec, slots=4, budget=100)
+    s.reserve(50)
+    futs = [s.submit(Job('j%d' % i, 25, key=i, dur=0.03)) for i in range(6)]
+    for f in futs:
+        f.result(5)
+    assert rec.max_bytes <= 50             # two jobs at a time next to 50 resident
+    assert s.max_used <= 100
+    s.close()
+
+
+def test_latency_summary_and_arrivals():
+    a = poisson_arrivals(200, rate=50.0, seed=3)
+    b = poisson_arrivals(200, rate=50.0, seed=3)
+    assert np.array_equal(a, b) and np.all(np.diff(a) > 0)
+    assert 2.5 < a[-1] < 6.0               # 200 arrivals at 50/s
+    s = Scheduler(lambda job, slot: job.name, slots=2)
+    jobs = [Job('r%d' % i, 1, key=i, dur=0) for i in range(8)]
+    futs = replay([lambda j=j: s.submit(j) for j in jobs],
+                  np.linspace(0.0, 0.07, 8))
+    s.close()
+    summ = latency_summary(futs)
+    assert summ['requests'] == 8
+    assert 0 <= summ['p50_s'] <= summ['p99_s']
+    assert summ['span_s'] >= 0.07
+    assert latency_summary([])['requests'] == 0
