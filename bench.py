@@ -358,6 +358,57 @@ def serving_requests(n_solves=16, cycles=3, seed=5):
     return out
 
 
+def graph_timing(torch, sizes=(4, 8, 16, 32), reps=10):
+    """Per-build time of a multi-omega K build (both omegas, level-0 grid,
+    synthetic def2-SVP water clusters) launched directly vs replayed from
+    its CUDA graph (CosxEngine.capture_k_multi), symmetrisation included."""
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    from pyscf_wb97mv_fast_gb300.systems import water_cluster
+    out = {}
+    for n in sizes:
+        mol = Molecule.build(water_cluster(n, box=max(5.0, 3.2 * n ** (1.0 / 3.0)),
+                                           seed=200 + n), 'synthetic-svp')
+        g = build_grids(mol, level=0)
+        eng = CosxEngine(mol)
+        c = eng.relative(g.coords)
+        w = torch.as_tensor(g.weights, device=eng.device)
+        r = np.random.default_rng(n)
+        q, _ = np.linalg.qr(r.normal(size=(mol.nao, 5 * n)))
+        qd = torch.as_tensor(2.0 * q @ q.T, device=eng.device)
+        K = torch.empty((len(OMEGAS), mol.nao, mol.nao), dtype=torch.float64,
+                        device=eng.device)
+
+        def direct():
+            eng.get_k_multi(c, w, qd, OMEGAS, tile_tol=TILE_TOL, out=K, stats=False)
+            return (K + K.transpose(1, 2)) * 0.5
+
+        for _ in range(3):
+            direct()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            direct()
+        torch.cuda.synchronize()
+        t_direct = (time.perf_counter() - t0) / reps
+        kg = eng.capture_k_multi(c, w, OMEGAS, tile_tol=TILE_TOL)
+        for _ in range(3):
+            kg.run(qd)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            kg.run(qd)
+        torch.cuda.synchronize()
+        t_graph = (time.perf_counter() - t0) / reps
+        same = bool(torch.equal(kg.run(qd), direct()))
+        out['water%d' % n] = {'nao': mol.nao, 'points': int(g.size),
+                              'direct_ms': t_direct * 1e3, 'graph_ms': t_graph * 1e3,
+                              'bitwise_equal': same}
+        del kg, eng
+    return out
+
+
 def serving_timing(torch, rates=(4.0, 16.0), slots=4, seed=5):
     """Continuous batching of SCF-shaped requests (serving.ExchangeServer):
     the plain per-request form (one request at a time, back to back) and
@@ -399,6 +450,28 @@ def serving_timing(torch, rates=(4.0, 16.0), slots=4, seed=5):
                      'max_concurrent_builds': srv.scheduler.max_running,
                      'bitwise_equal_to_plain': bool(same)})
         out['served']['rate=%g' % rate] = summ
+    # the highest rate again with every session's builds captured in CUDA
+    # graphs (first cycle captures, later cycles replay)
+    rate = rates[-1]
+    srv = ExchangeServer(slots=slots)
+    arr = poisson_arrivals(len(reqs), rate, seed)
+    solves = [Solve(srv, m, c, w, d, tag=nm, graphs=True) for nm, m, c, w, d in reqs]
+    t0 = time.perf_counter()
+    for s, t in zip(solves, arr):
+        dt = t0 + t - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        s.start()
+    for s in solves:
+        s.join()
+    srv.close()
+    same = all(all(np.array_equal(a, b) for a, b in zip(s.results, p.results))
+               for s, p in zip(solves, plain))
+    summ = solve_summary(solves)
+    summ.update({'rate_per_s': rate, 'slots': slots, 'cuda_graphs': True,
+                 'max_concurrent_builds': srv.scheduler.max_running,
+                 'bitwise_equal_to_plain': bool(same)})
+    out['served']['rate=%g,graphs' % rate] = summ
     return out
 
 
@@ -645,6 +718,7 @@ def main():
     fp64_form = None if args.no_fp64 else fp64_form_timing(
         eng, coords_d, w_d, qd_d, K, t_step, dm, torch)
     serving = None if (args.no_serving or world > 1) else serving_timing(torch)
+    graphs = None if (args.no_serving or world > 1) else graph_timing(torch)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -667,6 +741,7 @@ def main():
             'vv10': vv10,
             'fp64_form': fp64_form,
             'serving': serving,
+            'cuda_graphs': graphs,
             'clocks': clocks.summary(),
             'gpu_launches': launches_step * args.steps,
             'tasks_kept': kept, 'tasks_total': total,

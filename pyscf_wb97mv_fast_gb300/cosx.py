@@ -182,6 +182,18 @@ class CosxEngine:
             self.last_stats = st.as_dict()
         return out
 
+    def capture_k_multi(self, coords_rel, weights, omegas, tile_tol=1e-11,
+                        gemm='ozaki'):
+        """A get_k_multi build captured in a CUDA graph on fixed buffers:
+        returns a KBuildGraph whose run(dm) copies dm into its density
+        buffer, replays the graph and returns the symmetrised K
+        (len(omegas), nao, nao) on the device (its own output buffer,
+        overwritten by the next run).  coords_rel and weights must stay
+        alive and unchanged.  One warm-up build runs first (it allocates
+        the workspace and the block-order arrays, which a capture must
+        not)."""
+        return KBuildGraph(self, coords_rel, weights, omegas, tile_tol, gemm)
+
     def get_k_fp64(self, coords_rel, weights, qd, omegas, tile_tol=1e-11,
                    out=None, stats=True):
         """The plain FP64 form of get_k_multi: FP64 AO values, F = X QD kept
@@ -361,6 +373,46 @@ class CosxEngine:
             self._h, _native.ptr(coords_rel), npts, float(omega),
             _native.ptr(out), self._stream()), 'wb_int3c1e_dense')
         return out
+
+
+class KBuildGraph:
+    """One multi-omega K build of an engine captured in a CUDA graph (see
+    CosxEngine.capture_k_multi).  Every launch of the build (AO values,
+    the F split, block statistics, the class kernels on the engine's class
+    streams, the class-buffer sums, the K split) and the symmetrisation
+    replay with one graph launch; the block order of each replay is the
+    one the previous replay's kernels recorded on the device.  Not
+    thread-safe: one run at a time per graph (and per engine)."""
+
+    def __init__(self, eng, coords_rel, weights, omegas, tile_tol, gemm):
+        torch = _torch()
+        self.eng = eng
+        self.omegas = tuple(float(w) for w in omegas)
+        self._coords, self._weights = coords_rel, weights
+        self.qd = torch.zeros((eng.nao, eng.nao), dtype=torch.float64,
+                              device=eng.device)
+        self._k = torch.empty((len(self.omegas), eng.nao, eng.nao),
+                              dtype=torch.float64, device=eng.device)
+        args = dict(tile_tol=tile_tol, gemm=gemm, out=self._k, stats=False)
+        side = torch.cuda.Stream(device=eng.device)
+        side.wait_stream(torch.cuda.current_stream(eng.device))
+        with torch.cuda.stream(side):
+            # warm-up: workspace, block-order arrays, cuBLAS kernel choice
+            eng.get_k_multi(coords_rel, weights, self.qd, self.omegas, **args)
+        torch.cuda.current_stream(eng.device).wait_stream(side)
+        side.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, capture_error_mode='thread_local'):
+            eng.get_k_multi(coords_rel, weights, self.qd, self.omegas, **args)
+            self.out = (self._k + self._k.transpose(1, 2)) * 0.5
+
+    def run(self, dm):
+        """dm (nao, nao) FP64, host or device -> symmetrised K on the device
+        (this graph's output buffer)."""
+        torch = _torch()
+        self.qd.copy_(torch.as_tensor(dm, dtype=torch.float64), non_blocking=True)
+        self.graph.replay()
+        return self.out
 
 
 def _wb_basis(p):

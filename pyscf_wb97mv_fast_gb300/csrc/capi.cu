@@ -57,6 +57,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // largest dynamic shared memory per CTA for staged primitive-pair records
 constexpr size_t kStageMaxBytes = 96 * 1024;
+constexpr size_t kCublasWorkspace = 32u << 20;    // bytes per handle
 // default staged classes: (0,0) (1,0) (1,1) (2,1)
 constexpr long long kStageClasses = 0x1110100000LL;
 // default classes with a dual-omega kernel: (0,0) (1,0) (2,0) (2,1)
@@ -170,6 +171,7 @@ struct wb_cosx {
     // FP64 pair data of the plain FP64 form (wb_cosx_get_k_fp64), uploaded
     // on its first call: P per primitive pair, the class E blocks, the FP64
     // Boys table followed by the FP64 c2s tables of l = 2, 3
+    void* cublas_ws = nullptr;       // fixed cuBLAS workspace (kCublasWorkspace)
     double* f64_P = nullptr;
     double* f64_E = nullptr;
     double* f64_boys = nullptr;
@@ -785,6 +787,15 @@ int wb_cosx_create(const wb_basis* basis, const double origin[3],
     }
     if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS)
         return cleanup(fail(WB_ERR_CUBLAS, "cublasCreate failed"));
+    // a fixed cuBLAS workspace owned by the handle: no cuBLAS call of a
+    // build allocates, so a build can be captured in a CUDA graph
+    {
+        const cudaError_t we = cudaMalloc(&h->cublas_ws, kCublasWorkspace);
+        if (we != cudaSuccess) return cleanup(cuda_fail(we, "cuBLAS workspace"));
+        if (cublasSetWorkspace(h->cublas, h->cublas_ws, kCublasWorkspace) !=
+            CUBLAS_STATUS_SUCCESS)
+            return cleanup(fail(WB_ERR_CUBLAS, "cublasSetWorkspace failed"));
+    }
     // classes whose records are staged in shared memory: one hex digit per
     // class in class order (measured per class on the water27 workload:
     // staging wins where the register-carried record cost moves and
@@ -876,6 +887,7 @@ int wb_cosx_destroy(wb_cosx* h) {
     if (h->block) cudaFree(h->block);
     if (h->bcost) cudaFree(h->bcost);
     if (h->border) cudaFree(h->border);
+    if (h->cublas_ws) cudaFree(h->cublas_ws);
     if (h->f64_P) cudaFree(h->f64_P);
     if (h->f64_E) cudaFree(h->f64_E);
     if (h->f64_boys) cudaFree(h->f64_boys);

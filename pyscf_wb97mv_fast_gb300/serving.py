@@ -115,12 +115,23 @@ class Scheduler:
             t.start()
 
     # -- resident bytes (sessions) ------------------------------------------
-    def reserve(self, nbytes):
+    def reserve(self, nbytes, wait=False, timeout=None):
+        """Hold nbytes outside running jobs (an open session).  wait: block
+        until running jobs and other sessions leave room (a size above the
+        whole budget is rejected at once); otherwise reject if it does not
+        fit now."""
         with self._cv:
-            if self.budget is not None and self.resident + nbytes > self.budget:
-                raise Rejected('resident state of %d bytes exceeds the budget '
-                               '(%d of %d bytes held)' % (nbytes, self.resident,
-                                                           self.budget))
+            if self.budget is not None:
+                if nbytes > self.budget or not wait:
+                    if self.resident + nbytes > self.budget:
+                        raise Rejected('resident state of %d bytes exceeds the '
+                                       'budget (%d of %d bytes held)'
+                                       % (nbytes, self.resident, self.budget))
+                elif not self._cv.wait_for(
+                        lambda: self._used + self.resident + nbytes <= self.budget,
+                        timeout):
+                    raise Rejected('no room for %d resident bytes within %s s'
+                                   % (nbytes, timeout))
             self.resident += int(nbytes)
 
     def release(self, nbytes):
@@ -222,6 +233,61 @@ def latency_summary(futures):
             'requests_per_s': float(len(lat) / (t1 - t0)) if t1 > t0 else None}
 
 
+class _SharedLock:
+    """Many holders in shared mode, or one in exclusive mode.  The server
+    runs its host-side CUDA work (builds, session set-up and tear-down) in
+    shared mode and CUDA-graph captures in exclusive mode: a capture must
+    not overlap a device-wide synchronisation or allocation of another
+    thread."""
+
+    def __init__(self):
+        self._cv = threading.Condition()
+        self._shared = 0
+        self._excl = False
+        self._waiting_excl = 0
+
+    def acquire_shared(self):
+        with self._cv:
+            # waiting exclusive holders go first (captures are rare and short)
+            self._cv.wait_for(lambda: not self._excl and not self._waiting_excl)
+            self._shared += 1
+
+    def release_shared(self):
+        with self._cv:
+            self._shared -= 1
+            self._cv.notify_all()
+
+    def acquire_exclusive(self):
+        with self._cv:
+            self._waiting_excl += 1
+            self._cv.wait_for(lambda: not self._excl and self._shared == 0)
+            self._waiting_excl -= 1
+            self._excl = True
+
+    def release_exclusive(self):
+        with self._cv:
+            self._excl = False
+            self._cv.notify_all()
+
+    def shared(self):
+        return _Held(self.acquire_shared, self.release_shared)
+
+    def exclusive(self):
+        return _Held(self.acquire_exclusive, self.release_exclusive)
+
+
+class _Held:
+    def __init__(self, acq, rel):
+        self._acq, self._rel = acq, rel
+
+    def __enter__(self):
+        self._acq()
+        return self
+
+    def __exit__(self, *exc):
+        self._rel()
+
+
 class _Job:
     __slots__ = ('session', 'dm', 'footprint', 'key')
 
@@ -236,10 +302,15 @@ class Session:
     """One molecule resident on the device: its engine (packed shell
     pairs) and grid.  Open through ExchangeServer.open_session."""
 
-    def __init__(self, server, mol, coords, weights, omegas, tile_tol):
+    def __init__(self, server, mol, coords, weights, omegas, tile_tol,
+                 graphs=False):
         import torch
         from .cosx import CosxEngine
         self.server = server
+        # graphs: the first build captures the session's build in a CUDA
+        # graph (KBuildGraph) and later builds replay it
+        self.graphs = bool(graphs)
+        self.kgraph = None
         self.engine = CosxEngine(mol, device=server.device.index)
         self.coords = self.engine.relative(coords)
         self.weights = torch.as_tensor(np.ascontiguousarray(weights, dtype=np.float64),
@@ -255,6 +326,11 @@ class Session:
         self.footprint = (self.engine.workspace_bytes(self.npts) +
                           8 * self.nao * self.nao + 2 * kb)
         self.resident = 32 * self.npts + kb
+        if self.graphs:
+            # a captured build keeps its workspace and buffers for the
+            # session's life: held as resident, not per request
+            self.resident += self.footprint + kb
+            self.footprint = 0
         self.closed = False
 
     def submit(self, dm):
@@ -287,24 +363,31 @@ class ExchangeServer:
         self.gemm = gemm
         self._streams = [torch.cuda.Stream(device=self.device) for _ in range(slots)]
         self._sched = Scheduler(self._run, slots=slots, budget=budget)
+        self._cuda = _SharedLock()
         self.futures = []
 
     @property
     def scheduler(self):
         return self._sched
 
-    def open_session(self, mol, coords, weights, omegas=(0.0, 0.3), tile_tol=1e-11):
-        s = Session(self, mol, coords, weights, omegas, tile_tol)
+    def open_session(self, mol, coords, weights, omegas=(0.0, 0.3), tile_tol=1e-11,
+                     graphs=False):
+        with self._cuda.shared():
+            s = Session(self, mol, coords, weights, omegas, tile_tol, graphs)
         try:
-            self._sched.reserve(s.resident)
+            self._sched.reserve(s.resident, wait=True)
         except Rejected:
-            s.engine.close()
+            with self._cuda.shared():
+                s.engine.close()
             raise
         return s
 
     def _close_session(self, s):
+        with self._cuda.shared():
+            s.kgraph = None
+            s.engine._ws = None
+            s.engine.close()
         self._sched.release(s.resident)
-        s.engine.close()
 
     def _submit(self, session, dm):
         if session.closed:
@@ -322,21 +405,32 @@ class ExchangeServer:
         eng = s.engine
         stream = self._streams[slot]
         nom = len(s.omegas)
-        with torch.cuda.device(self.device), torch.cuda.stream(stream):
+        if s.graphs and s.kgraph is None:
+            # the session keeps its workspace while its graph lives; the
+            # capture (with its warm-up build) runs alone
+            with self._cuda.exclusive(), torch.cuda.device(self.device), \
+                    torch.cuda.stream(stream):
+                s.kgraph = eng.capture_k_multi(s.coords, s.weights, s.omegas,
+                                               tile_tol=s.tile_tol, gemm=self.gemm)
+        with self._cuda.shared(), torch.cuda.device(self.device), \
+                torch.cuda.stream(stream):
             dm_h = torch.from_numpy(job.dm).pin_memory()
-            dm_d = torch.empty((s.nao, s.nao), dtype=torch.float64, device=self.device)
-            dm_d.copy_(dm_h, non_blocking=True)
-            K = eng.get_k_multi(s.coords, s.weights, dm_d, s.omegas,
-                                tile_tol=s.tile_tol, gemm=self.gemm, stats=False)
-            Ks = (K + K.transpose(1, 2)) * 0.5
             out = torch.empty((nom, s.nao, s.nao), dtype=torch.float64).pin_memory()
-            out.copy_(Ks, non_blocking=True)
+            if s.graphs:
+                out.copy_(s.kgraph.run(dm_h), non_blocking=True)
+            else:
+                dm_d = torch.empty((s.nao, s.nao), dtype=torch.float64,
+                                   device=self.device)
+                dm_d.copy_(dm_h, non_blocking=True)
+                K = eng.get_k_multi(s.coords, s.weights, dm_d, s.omegas,
+                                    tile_tol=s.tile_tol, gemm=self.gemm, stats=False)
+                out.copy_((K + K.transpose(1, 2)) * 0.5, non_blocking=True)
             done = torch.cuda.Event()
             done.record(stream)
-        done.synchronize()
-        # the workspace goes back to the allocator's cache for other builds
-        eng._ws = None
-        del K, Ks, dm_d
+            done.synchronize()
+        if not s.graphs:
+            # the workspace goes back to the allocator's cache for other builds
+            eng._ws = None
         return out.numpy()
 
     def close(self):
@@ -378,8 +472,9 @@ class Solve:
     every cycle; t_arrival / t_done bracket the whole solve."""
 
     def __init__(self, server, mol, coords, weights, densities, omegas=(0.0, 0.3),
-                 tile_tol=1e-11, tag=None):
+                 tile_tol=1e-11, tag=None, graphs=False):
         self.server = server
+        self.graphs = graphs
         self.mol, self.coords, self.weights = mol, coords, weights
         self.densities = list(densities)
         self.omegas, self.tile_tol, self.tag = omegas, tile_tol, tag
@@ -391,7 +486,7 @@ class Solve:
     def run(self):
         self.t_arrival = time.perf_counter()
         sess = self.server.open_session(self.mol, self.coords, self.weights,
-                                        self.omegas, self.tile_tol)
+                                        self.omegas, self.tile_tol, self.graphs)
         try:
             self.results = [sess.submit(dm).result() for dm in self.densities]
         finally:

@@ -70,3 +70,37 @@ def test_budget_rejects_what_can_never_fit():
     s.close()
     srv.close()
     assert srv.scheduler.resident == 0
+
+
+def test_captured_build_replays_match_direct_builds():
+    """A K build captured in a CUDA graph replays bitwise the direct build,
+    for each new density."""
+    import torch
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine
+    mol, coords, weights, dms = _cases()[1]
+    eng = CosxEngine(mol)
+    c = eng.relative(coords)
+    w = torch.as_tensor(weights, device=eng.device)
+    kg = eng.capture_k_multi(c, w, (0.0, 0.3), tile_tol=1e-11)
+    for dm in (dms[0], dms[1], dms[0]):
+        Kg = kg.run(dm).cpu().numpy()
+        Kd = eng.get_k_multi(c, w, torch.as_tensor(dm, device=eng.device),
+                             (0.0, 0.3), tile_tol=1e-11)
+        Kd = ((Kd + Kd.transpose(1, 2)) * 0.5).cpu().numpy()
+        assert np.array_equal(Kg, Kd)
+
+
+def test_served_with_graphs_equal_plain():
+    from pyscf_wb97mv_fast_gb300.serving import ExchangeServer, Solve
+    cases = _cases()
+    srv1 = ExchangeServer(slots=1)
+    alone = [Solve(srv1, m, c, w, d + d[:1]).run() for m, c, w, d in cases]
+    srv1.close()
+    srv = ExchangeServer(slots=3)
+    solves = [Solve(srv, m, c, w, d + d[:1], graphs=True).start()
+              for m, c, w, d in cases]
+    got = [s.join(120) for s in solves]
+    srv.close()
+    for a, b in zip(alone, got):
+        for ka, kb in zip(a, b):
+            assert np.array_equal(ka, kb)

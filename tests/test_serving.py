@@ -127,3 +127,19 @@ def test_latency_summary_and_arrivals():
     assert 0 <= summ['p50_s'] <= summ['p99_s']
     assert summ['span_s'] >= 0.07
     assert latency_summary([])['requests'] == 0
+
+
+def test_reserve_waits_for_room():
+    rec = Recorder()
+    s = Scheduler(rec, slots=2, budget=100)
+    f = s.submit(Job('long', 70, key='a', dur=0.2))
+    time.sleep(0.05)                       # 70 bytes running
+    t0 = time.perf_counter()
+    s.reserve(50, wait=True, timeout=5)    # waits for the job to end
+    assert time.perf_counter() - t0 > 0.05 and f.done()
+    with pytest.raises(Rejected):
+        s.reserve(60, wait=True, timeout=0.05)   # 50 + 60 > 100, nothing ends
+    with pytest.raises(Rejected):
+        s.reserve(101, wait=True)                # above the whole budget
+    s.release(50)
+    s.close()
