@@ -409,6 +409,105 @@ def graph_timing(torch, sizes=(4, 8, 16, 32), reps=10):
     return out
 
 
+def batched_timing(torch, nmol=64, seed=4, iters=3):
+    """Config-4 shape: nmol seeded water clusters of n in {4..32} waters
+    (uniform), synthetic def2-SVP, level-0 grids, both omegas.  One SCF
+    iteration's K builds of all molecules: one molecule per call
+    (wb_cosx_get_k_multi, back to back on one stream) vs batched
+    (wb_cosx_batch_run: one launch per class over the molecules of a wave;
+    waves fill half of the free device memory with workspaces)."""
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.cosx import CosxBatch, CosxEngine, batch_workspace_bytes
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    from pyscf_wb97mv_fast_gb300.systems import water_cluster
+    rng = np.random.default_rng(seed)
+    sizes = [int(x) for x in rng.integers(4, 33, size=nmol)]
+    engines, grids, qds = [], [], []
+    for i, n in enumerate(sizes):
+        mol = Molecule.build(water_cluster(n, box=max(5.0, 3.2 * n ** (1.0 / 3.0)),
+                                           seed=300 + i), 'synthetic-svp')
+        g = build_grids(mol, level=0)
+        eng = CosxEngine(mol)
+        engines.append(eng)
+        grids.append((eng.relative(g.coords), torch.as_tensor(g.weights, device=eng.device)))
+        r = np.random.default_rng(seed * 1000 + i)
+        q, _ = np.linalg.qr(r.normal(size=(mol.nao, 5 * n)))
+        qds.append(torch.as_tensor(2.0 * q @ q.T, device=eng.device))
+    wsb = [e.workspace_bytes(int(c.shape[0])) for e, (c, _) in zip(engines, grids)]
+    wsb_batch, scratch = batch_workspace_bytes(engines, [int(c.shape[0]) for c, _ in grids])
+    # one molecule per call, one shared workspace
+    shared = torch.empty(max(wsb), dtype=torch.uint8, device=engines[0].device)
+    outs = [torch.empty((len(OMEGAS), e.nao, e.nao), dtype=torch.float64,
+                        device=e.device) for e in engines]
+    for e in engines:
+        e._ws = shared
+
+    def per_molecule():
+        for e, (c, w), q, o in zip(engines, grids, qds, outs):
+            e.get_k_multi(c, w, q, OMEGAS, tile_tol=TILE_TOL, out=o, stats=False)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(iters):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / iters
+
+    t_single = timed(per_molecule)
+    ref = [o.clone() for o in outs]
+    flops = 0.0
+    for e, (c, w), q, o in zip(engines, grids, qds, outs):
+        e.get_k_multi(c, w, q, OMEGAS, tile_tol=TILE_TOL, out=o, stats=True)
+        flops += e.last_stats['model_flops']
+    for e in engines:
+        e._ws = None
+    del shared
+    torch.cuda.empty_cache()
+    free, _ = torch.cuda.mem_get_info(engines[0].device)
+    budget = 0.6 * free
+    waves, cur, used = [], [], scratch
+    for i, b in enumerate(wsb_batch):
+        if cur and used + b > budget:
+            waves.append(cur)
+            cur, used = [], scratch
+        cur.append(i)
+        used += b
+    waves.append(cur)
+    batches = [CosxBatch([engines[i] for i in wv], [grids[i] for i in wv], OMEGAS,
+                         tile_tol=TILE_TOL) for wv in waves]
+    bouts = [[outs[i] for i in wv] for wv in waves]
+
+    def batched():
+        for bt, wv, bo in zip(batches, waves, bouts):
+            bt.run([qds[i] for i in wv], out=bo)
+
+    t_batch = timed(batched)
+    same = all(torch.equal(a, b) for a, b in zip(outs, ref))
+    kernel_launches = 0
+    for bt, wv, bo in zip(batches, waves, bouts):
+        bt.run([qds[i] for i in wv], out=bo, stats=True)
+        kernel_launches += bt.last_stats['kernel_launches']
+    for bt in batches:
+        bt.close()
+    for e in engines:
+        e._ws = None
+        e.close()
+    return {'molecules': nmol, 'waters_per_cluster': sizes,
+            'grid': 'level 0', 'points_total': int(sum(int(c.shape[0]) for c, _ in grids)),
+            'waves': len(waves), 'workspace_gb': (sum(wsb_batch) + scratch) / 1e9,
+            'per_molecule_ms_per_iteration': t_single,
+            'batched_ms_per_iteration': t_batch, 'speedup': t_single / t_batch,
+            'model_flops_per_iteration': flops,
+            'tflops_batched': flops / (t_batch * 1e-3) / 1e12,
+            'kernel_launches_batched': kernel_launches,
+            'bitwise_equal_to_per_molecule': bool(same)}
+
+
 def serving_timing(torch, rates=(4.0, 16.0), slots=4, seed=5):
     """Continuous batching of SCF-shaped requests (serving.ExchangeServer):
     the plain per-request form (one request at a time, back to back) and
@@ -562,6 +661,8 @@ def main():
                     help='skip the plain FP64 form timing')
     ap.add_argument('--no-serving', action='store_true',
                     help='skip the continuous-batching serving leg')
+    ap.add_argument('--no-batched', action='store_true',
+                    help='skip the batched (many molecules per launch) leg')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -719,6 +820,9 @@ def main():
         eng, coords_d, w_d, qd_d, K, t_step, dm, torch)
     serving = None if (args.no_serving or world > 1) else serving_timing(torch)
     graphs = None if (args.no_serving or world > 1) else graph_timing(torch)
+    eng._ws = None
+    torch.cuda.empty_cache()
+    batched = None if (args.no_batched or world > 1) else batched_timing(torch)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -742,6 +846,7 @@ def main():
             'fp64_form': fp64_form,
             'serving': serving,
             'cuda_graphs': graphs,
+            'batched': batched,
             'clocks': clocks.summary(),
             'gpu_launches': launches_step * args.steps,
             'tasks_kept': kept, 'tasks_total': total,

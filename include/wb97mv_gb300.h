@@ -171,6 +171,41 @@ int wb_cosx_get_k_fp64(wb_cosx* h, const double* coords, const double* weights,
                        void* workspace, size_t workspace_bytes, void* stream,
                        wb_cosx_stats* stats);
 
+/* Batched K builds: the K of several molecules per call, with one launch
+ * per class kernel over all of them (a class with no two-omega kernel:
+ * one per omega).  A plan fixes the molecules (handles, each used by this
+ * plan only while it lives), their grids (coords, weights, npts; device
+ * memory that must stay unchanged), their workspaces (owned by the plan
+ * while it lives), the omegas (1 or 2) and tile_tol.  wb_cosx_batch_create
+ * evaluates the AO values, the grid coordinates and the omega records
+ * once (on `stream`, synchronised before it returns).  The F / K split
+ * scratch is one buffer shared by the molecules (they use it one after
+ * another): each molecule's workspace needs wb_cosx_batch_workspace_bytes
+ * bytes and the scratch the largest *scratch_bytes it reports.  Each
+ * wb_cosx_batch_run takes one density per molecule (qd[m], (nao_m,
+ * nao_m) row-major) and writes nomega unsymmetrised K matrices per
+ * molecule to k_out[m], as wb_cosx_get_k_multi does (omega j at k_out[m]
+ * + j nao_m^2).  A run makes no allocation and, with stats == NULL, no
+ * host synchronisation, so it can be captured in a CUDA graph.  Each
+ * molecule's K equals its wb_cosx_get_k_multi result when the handles
+ * agree on the kernel variant of every class (the same elements and
+ * basis).  The reference builds one molecule's K per call
+ * (GpuKBuilder.get_k, gpu/sgx_k.py:663-751) and has no batched form
+ * (batch throughput is a non-goal, docs/design.en.md:44). */
+typedef struct wb_cosx_batch wb_cosx_batch;
+size_t wb_cosx_batch_workspace_bytes(const wb_cosx* h, int64_t npts,
+                                     size_t* scratch_bytes);
+int wb_cosx_batch_create(int nmol, wb_cosx* const* handles,
+                         const double* const* coords, const double* const* weights,
+                         const int64_t* npts, void* const* workspaces,
+                         const size_t* workspace_bytes, void* scratch,
+                         size_t scratch_bytes, int nomega, const double* omegas,
+                         double tile_tol, int flags, void* stream,
+                         wb_cosx_batch** out);
+int wb_cosx_batch_run(wb_cosx_batch* b, const double* const* qd,
+                      double* const* k_out, void* stream, wb_cosx_stats* stats);
+int wb_cosx_batch_destroy(wb_cosx_batch* b);
+
 /* The fused G kernels alone on one tile: f (nao, ldp) FP32 AO-major in,
  * g_out (nao, ldp) FP32 out (overwritten).  weights (npts,) FP64 feed the
  * screening estimate.  Replaces GpuKBuilder._tasks + _launch

@@ -47,6 +47,8 @@ EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_ozaki_workspace_bytes', 'wb_cosx_ozaki_f', 'wb_cosx_ozaki_k',
             'wb_vv10_kernel_sum_noalloc',
             'wb_cosx_fp64_workspace_bytes', 'wb_cosx_get_k_fp64',
+            'wb_cosx_batch_workspace_bytes', 'wb_cosx_batch_create',
+            'wb_cosx_batch_run', 'wb_cosx_batch_destroy',
             'wb_status_string',
             'wb_last_error', 'wb_version')
 
@@ -157,6 +159,13 @@ def _declare(lib):
         'wb_cosx_get_k_fp64': (_INT, [_P, _P, _P, _I64, _P, _INT, _P, _D, _P, _P,
                                       ctypes.c_size_t, _P,
                                       ctypes.POINTER(WbCosxStats)]),
+        'wb_cosx_batch_workspace_bytes': (ctypes.c_size_t, [_P, _I64,
+                                                            ctypes.POINTER(ctypes.c_size_t)]),
+        'wb_cosx_batch_create': (_INT, [_INT, _P, _P, _P, _P, _P, _P, _P,
+                                        ctypes.c_size_t, _INT, _P, _D, _INT, _P,
+                                        ctypes.POINTER(_P)]),
+        'wb_cosx_batch_run': (_INT, [_P, _P, _P, _P, ctypes.POINTER(WbCosxStats)]),
+        'wb_cosx_batch_destroy': (_INT, [_P]),
         'wb_status_string': (ctypes.c_char_p, [_INT]),
         'wb_last_error': (ctypes.c_char_p, []),
         'wb_version': (_INT, []),

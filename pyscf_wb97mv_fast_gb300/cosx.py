@@ -415,6 +415,101 @@ class KBuildGraph:
         return self.out
 
 
+def batch_workspace_bytes(engines, npts):
+    """Per-molecule workspace bytes of a CosxBatch and the bytes of its
+    shared scratch."""
+    lib = _native.lib()
+    ws, scr = [], 0
+    for e, n in zip(engines, npts):
+        s = _native.ctypes.c_size_t(0)
+        ws.append(int(lib.wb_cosx_batch_workspace_bytes(e._h, int(n),
+                                                        _native.ctypes.byref(s))))
+        scr = max(scr, int(s.value))
+    return ws, scr
+
+
+class CosxBatch:
+    """K builds of several molecules per call (wb_cosx_batch_*): one launch
+    per class kernel over all molecules.  engines: one CosxEngine per
+    molecule (each used only by this batch while it lives; its workspace
+    is sized for its grid); grids: (coords_rel, weights) device tensors per
+    molecule, kept alive and unchanged.  The AO values, grid coordinates
+    and omega records are formed once here; run(qds) builds every K."""
+
+    def __init__(self, engines, grids, omegas=(0.0, 0.3), tile_tol=1e-11,
+                 gemm='ozaki'):
+        torch = _torch()
+        if not engines or len(engines) != len(grids):
+            raise ValueError('one (coords_rel, weights) per engine')
+        self.engines = list(engines)
+        self.omegas = tuple(float(w) for w in omegas)
+        if len(self.omegas) not in (1, 2):
+            raise ValueError('1 or 2 omegas')
+        self._grids = [(c.contiguous(), w.contiguous()) for c, w in grids]
+        n = len(self.engines)
+        dev = self.engines[0].device
+        P = _native.ctypes.c_void_p
+        npts = [int(c.shape[0]) for c, _ in self._grids]
+        wsb, scr = batch_workspace_bytes(self.engines, npts)
+        ws = [e.workspace(b) for e, b in zip(self.engines, wsb)]
+        self._scratch = torch.empty(max(scr, 1), dtype=torch.uint8, device=dev)
+        self._hold = ws
+        handles = (P * n)(*[e._h.value for e in self.engines])
+        coords = (P * n)(*[c.data_ptr() for c, _ in self._grids])
+        weights = (P * n)(*[w.data_ptr() for _, w in self._grids])
+        npts_a = (_native.ctypes.c_int64 * n)(*npts)
+        ws_a = (P * n)(*[t.data_ptr() for t in ws])
+        wsb_a = (_native.ctypes.c_size_t * n)(*wsb)
+        om = (_native.ctypes.c_double * len(self.omegas))(*self.omegas)
+        out = P()
+        with torch.cuda.device(dev):
+            _native.check(_native.lib().wb_cosx_batch_create(
+                n, handles, coords, weights, npts_a, ws_a, wsb_a,
+                self._scratch.data_ptr(), self._scratch.numel(), len(self.omegas),
+                om, float(tile_tol), _native.GEMM_MODES[gemm],
+                CosxEngine._stream(), _native.ctypes.byref(out)),
+                'wb_cosx_batch_create')
+        self._b = out
+        self.device = dev
+        self.last_stats = {}
+
+    def run(self, qds, out=None, stats=False):
+        """qds: one (nao, nao) FP64 device tensor per molecule -> a list of
+        (len(omegas), nao, nao) unsymmetrised K (out: the same, to reuse)."""
+        torch = _torch()
+        n = len(self.engines)
+        if len(qds) != n:
+            raise ValueError('one density per molecule')
+        if out is None:
+            out = [torch.empty((len(self.omegas), e.nao, e.nao), dtype=torch.float64,
+                               device=self.device) for e in self.engines]
+        P = _native.ctypes.c_void_p
+        qd_c = [q.contiguous() for q in qds]
+        for q, e in zip(qd_c, self.engines):
+            if tuple(q.shape) != (e.nao, e.nao):
+                raise ValueError('density of the wrong shape')
+        st = _native.WbCosxStats() if stats else None
+        _native.check(_native.lib().wb_cosx_batch_run(
+            self._b, (P * n)(*[q.data_ptr() for q in qd_c]),
+            (P * n)(*[k.data_ptr() for k in out]), CosxEngine._stream(),
+            _native.ctypes.byref(st) if st is not None else None),
+            'wb_cosx_batch_run')
+        if st is not None:
+            self.last_stats = st.as_dict()
+        return out
+
+    def close(self):
+        if getattr(self, '_b', None):
+            _native.lib().wb_cosx_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:                       # noqa: BLE001
+            pass
+
+
 def _wb_basis(p):
     """The C-ABI basis view of Molecule.packed() p (p must outlive it)."""
     return _native.WbBasis(

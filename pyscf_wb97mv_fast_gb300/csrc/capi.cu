@@ -284,6 +284,10 @@ wb::CosxArgs make_args(const wb_cosx* h, void* ws, const WsLayout& L,
     a.pnint = h->pnint;
     a.counters = at<unsigned long long>(ws, L.counters);
     a.work = at<int>(ws, L.work);
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        a.cls_pb[c] = h->hp.cls[c].pair_begin;
+        a.cls_pe[c] = h->hp.cls[c].pair_end;
+    }
     return a;
 }
 
@@ -627,6 +631,39 @@ WsLayout64 ws_layout_fp64(const wb_cosx* h, int64_t ld) {
 }
 
 }  // namespace
+
+// -- batched K builds: several molecules, one launch per class -------------
+
+struct wb_cosx_batch {
+    int nmol = 0;
+    int nom = 0;                        // omegas: 1, or 2 (slot a <= slot b)
+    double om[2] = {0.0, 0.0};
+    int kidx[2] = {0, 1};               // k_out matrix of slot a / b
+    double tol = 0.0;
+    int gemm = WB_K_GEMM_OZAKI_BF16;
+    std::vector<wb_cosx*> h;
+    std::vector<const double*> coords, weights;
+    std::vector<int64_t> npts, ld;
+    std::vector<void*> ws;
+    std::vector<WsLayout> L;
+    void* scratch = nullptr;            // the F / K split scratch, shared
+    bool has[wb::NCLASS] = {};          // some molecule has pairs of the class
+    bool dual[wb::NCLASS] = {};         // the two-omega kernel, every molecule
+    size_t smem[wb::NCLASS] = {};       // staged single-omega kernel (0: prefetch)
+    size_t smem2[wb::NCLASS] = {};
+    int rmax[wb::NCLASS] = {}, rmax2[wb::NCLASS] = {};
+    int items[wb::NCLASS] = {};         // blocks of the class over the molecules
+    int order[wb::NCLASS] = {};
+    void* block = nullptr;              // device: args (2 nmol), offsets, counters
+    wb::CosxArgs* d_args = nullptr;
+    int* d_off = nullptr;               // NCLASS x (nmol + 1)
+    int* d_work = nullptr;              // NCLASS x 2
+};
+
+static int batch_fail(wb_cosx_batch* b, int code) {
+    wb_cosx_batch_destroy(b);
+    return code;
+}
 
 extern "C" {
 
@@ -1247,6 +1284,343 @@ int wb_cosx_get_k_fp64(wb_cosx* h, const double* coords, const double* weights,
         launches += 2;
     }
     return read_stats(h, workspace, L.base, ntasks, s, stats, launches);
+}
+
+size_t wb_cosx_batch_workspace_bytes(const wb_cosx* h, int64_t npts,
+                                     size_t* scratch_bytes) {
+    if (!h || npts < 1) return 0;
+    const WsLayout L = ws_layout(h, round32(npts), true);
+    if (scratch_bytes) *scratch_bytes = L.total - L.oz;
+    return L.oz;
+}
+
+int wb_cosx_batch_create(int nmol, wb_cosx* const* handles,
+                         const double* const* coords, const double* const* weights,
+                         const int64_t* npts, void* const* workspaces,
+                         const size_t* workspace_bytes, void* scratch,
+                         size_t scratch_bytes, int nomega, const double* omegas,
+                         double tile_tol, int flags, void* stream,
+                         wb_cosx_batch** out) {
+    if (!out || nmol < 1 || !handles || !coords || !weights || !npts || !workspaces ||
+        !workspace_bytes || !scratch || !omegas || nomega < 1 || nomega > 2 ||
+        !(tile_tol >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_batch_create: bad arguments");
+    *out = nullptr;
+    for (int j = 0; j < nomega; ++j)
+        if (!(omegas[j] >= 0.0))
+            return fail(WB_ERR_INVALID_ARGUMENT,
+                        "wb_cosx_batch_create: omega must be >= 0");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    wb_cosx_batch* b = new wb_cosx_batch();
+    b->nmol = nmol;
+    b->nom = nomega;
+    b->om[0] = omegas[0];
+    if (nomega == 2) {
+        b->om[1] = omegas[1];
+        if (omegas[1] < omegas[0]) {
+            std::swap(b->om[0], b->om[1]);
+            b->kidx[0] = 1;
+            b->kidx[1] = 0;
+        }
+    }
+    b->tol = tile_tol;
+    b->gemm = flags & 3;
+    b->scratch = scratch;
+    for (int m = 0; m < nmol; ++m) {
+        wb_cosx* h = handles[m];
+        if (!h || !coords[m] || !weights[m] || npts[m] < 1 || !workspaces[m])
+            return batch_fail(b, fail(WB_ERR_INVALID_ARGUMENT,
+                                      "wb_cosx_batch_create: molecule " +
+                                          std::to_string(m) + ": bad arguments"));
+        if (h->device != handles[0]->device)
+            return batch_fail(b, fail(WB_ERR_INVALID_ARGUMENT,
+                                      "wb_cosx_batch_create: handles on different devices"));
+        for (int k = 0; k < m; ++k)
+            if (handles[k] == h)
+                return batch_fail(b, fail(WB_ERR_INVALID_ARGUMENT,
+                                          "wb_cosx_batch_create: a handle appears twice"));
+        const int64_t ld = round32(npts[m]);
+        if (ld > INT32_MAX - 64)
+            return batch_fail(b, fail(WB_ERR_UNSUPPORTED,
+                                      "wb_cosx_batch_create: above 2^31 points"));
+        const WsLayout L = ws_layout(h, ld, true);
+        if (workspace_bytes[m] < L.oz || scratch_bytes < L.total - L.oz)
+            return batch_fail(b, fail(WB_ERR_WORKSPACE,
+                                      "wb_cosx_batch_create: molecule " +
+                                          std::to_string(m) + " needs " +
+                                          std::to_string(L.oz) + " workspace and " +
+                                          std::to_string(L.total - L.oz) +
+                                          " scratch bytes"));
+        b->h.push_back(h);
+        b->coords.push_back(coords[m]);
+        b->weights.push_back(weights[m]);
+        b->npts.push_back(npts[m]);
+        b->ld.push_back(ld);
+        b->ws.push_back(workspaces[m]);
+        b->L.push_back(L);
+    }
+    // per class: the kernel variant every molecule runs, the largest task
+    // record, the blocks (items) over the molecules
+    double work[wb::NCLASS] = {0};
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        bool dual = nomega == 2, staged = true;
+        for (int m = 0; m < nmol; ++m) {
+            const wb_cosx* h = b->h[m];
+            if (h->hp.cls[c].pair_end <= h->hp.cls[c].pair_begin) continue;
+            b->has[c] = true;
+            dual = dual && h->dual_ok && h->dual_cls[c];
+            staged = staged && h->stage_smem[c] > 0;
+            b->rmax[c] = std::max(b->rmax[c], h->recmax[c]);
+            b->rmax2[c] = std::max(b->rmax2[c], h->recmax2[c]);
+            for (int k = h->hp.cls[c].pair_begin; k < h->hp.cls[c].pair_end; ++k)
+                work[c] += (double)h->hp.pflops[k] * (double)b->npts[m];
+        }
+        const size_t sm = (size_t)(128 / 32) * 2 * b->rmax[c] * sizeof(float4);
+        const size_t sm2 = (size_t)(128 / 32) * 2 * b->rmax2[c] * sizeof(float4);
+        b->dual[c] = b->has[c] && dual && sm2 <= kStageMaxBytes;
+        b->smem2[c] = b->dual[c] ? sm2 : 0;
+        b->smem[c] = (b->has[c] && staged && sm <= kStageMaxBytes) ? sm : 0;
+        b->order[c] = c;
+    }
+    std::stable_sort(b->order, b->order + wb::NCLASS,
+                     [&](int x, int y) { return work[x] > work[y]; });
+    // host argument blocks (slot a, slot b) and item offsets
+    std::vector<wb::CosxArgs> args(2 * (size_t)nmol);
+    std::vector<int> off((size_t)wb::NCLASS * (nmol + 1), 0);
+    for (int m = 0; m < nmol; ++m) {
+        wb_cosx* h = b->h[m];
+        const WsLayout& L = b->L[m];
+        wb::CosxArgs a = make_args(h, b->ws[m], L, b->ld[m], b->npts[m],
+                                   at<float>(b->ws[m], L.F32), tile_tol);
+        wb::CosxArgs bb = a;
+        for (int c = 0; c < wb::NCLASS; ++c) {
+            bb.rec[c] = at<float4>(b->ws[m], L.recb) + h->hp.rec_off[c];
+            bb.Gcls[c] = a.Gcls2[c];
+        }
+        args[m] = a;
+        args[nmol + m] = bb;
+    }
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        int* o = off.data() + (size_t)c * (nmol + 1);
+        for (int m = 0; m < nmol; ++m) {
+            const wb_cosx* h = b->h[m];
+            int n = 0;
+            if (h->hp.cls[c].pair_end > h->hp.cls[c].pair_begin) {
+                const int pc = b->dual[c] ? h->pts2[c] : h->pts[c];
+                n = args[m].nblk[pc == 4 ? 2 : pc - 1];
+            }
+            if ((int64_t)o[m] + n > INT32_MAX)
+                return batch_fail(b, fail(WB_ERR_UNSUPPORTED,
+                                          "wb_cosx_batch_create: too many blocks"));
+            o[m + 1] = o[m] + n;
+        }
+        b->items[c] = o[nmol];
+    }
+    const size_t args_b = align256(sizeof(wb::CosxArgs) * args.size());
+    const size_t off_b = align256(sizeof(int) * off.size());
+    const size_t work_b = sizeof(int) * 2 * wb::NCLASS;
+    cudaError_t e = cudaMalloc(&b->block, args_b + off_b + work_b);
+    if (e != cudaSuccess) return batch_fail(b, cuda_fail(e, "wb_cosx_batch_create"));
+    b->d_args = static_cast<wb::CosxArgs*>(b->block);
+    b->d_off = reinterpret_cast<int*>(static_cast<char*>(b->block) + args_b);
+    b->d_work = reinterpret_cast<int*>(static_cast<char*>(b->block) + args_b + off_b);
+    e = cudaMemcpy(b->d_args, args.data(), sizeof(wb::CosxArgs) * args.size(),
+                   cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_off, off.data(), sizeof(int) * off.size(),
+                       cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return batch_fail(b, cuda_fail(e, "wb_cosx_batch_create"));
+    // what stays fixed for the plan's life: AO values, grid coordinates
+    // (hi / lo), the omega records of both slots
+    for (int m = 0; m < nmol; ++m) {
+        wb_cosx* h = b->h[m];
+        const WsLayout& L = b->L[m];
+        void* ws = b->ws[m];
+        wb::AoArgs ao;
+        ao.coords = b->coords[m]; ao.npts = b->npts[m]; ao.ld = b->ld[m];
+        ao.nbas = h->nbas; ao.sh_l = h->sh_l; ao.sh_np = h->sh_np;
+        ao.sh_nc = h->sh_nc; ao.sh_eoff = h->sh_eoff; ao.sh_coff = h->sh_coff;
+        ao.sh_ao0 = h->sh_ao0; ao.sh_ctr = h->sh_ctr; ao.exps = h->exps;
+        ao.coeffs = h->coeffs; ao.X = at<double>(ws, L.X); ao.nao = h->hp.nao;
+        e = wb::launch_ao_eval(ao, s);
+        if (e == cudaSuccess)
+            e = wb::launch_grid_prep(b->coords[m], b->npts[m], b->ld[m],
+                                     at<float>(ws, L.gh), at<float>(ws, L.gl), s);
+        if (e != cudaSuccess) return batch_fail(b, cuda_fail(e, "wb_cosx_batch_create"));
+        wb::RecPack P;
+        for (int c = 0; c < wb::NCLASS; ++c) {
+            P.pp_begin[c] = h->hp.cls[c].pp_begin;
+            P.pp_end[c] = h->hp.cls[c].pp_end;
+            P.stride[c] = wb::kRecStride[c];
+            P.nom[c] = wb::kRecNom[c];
+            P.ne[c] = wb::kRecNe[c];
+            P.rec_off[c] = h->hp.rec_off[c];
+            P.e_off[c] = h->hp.cls[c].e_base / 4;
+        }
+        const size_t slot_rec[2] = {L.rec, L.recb};
+        const size_t slot_om[2] = {L.om, L.om2};
+        for (int w = 0; w < nomega && e == cudaSuccess; ++w) {
+            e = wb::launch_omega(h->hp.npp, h->p, h->pref, b->om[w],
+                                 at<float4>(ws, slot_om[w]), s);
+            if (e == cudaSuccess)
+                e = wb::launch_pack_records(P, h->hp.npp, h->geo,
+                                            at<float4>(ws, slot_om[w]), h->E,
+                                            at<float4>(ws, slot_rec[w]), s);
+        }
+        if (e == cudaSuccess && nomega == 2) {
+            for (int c = 0; c < wb::NCLASS; ++c) {
+                P.stride[c] = wb::kRecStride2[c];
+                P.rec_off[c] = h->hp.rec_off2[c];
+            }
+            e = wb::launch_pack_records2(P, h->hp.npp, h->geo, at<float4>(ws, L.om),
+                                         at<float4>(ws, L.om2), h->E,
+                                         at<float4>(ws, L.rec2), s);
+        }
+        if (e != cudaSuccess) return batch_fail(b, cuda_fail(e, "wb_cosx_batch_create"));
+    }
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return batch_fail(b, cuda_fail(e, "wb_cosx_batch_create"));
+    *out = b;
+    return WB_OK;
+}
+
+int wb_cosx_batch_run(wb_cosx_batch* b, const double* const* qd,
+                      double* const* k_out, void* stream, wb_cosx_stats* stats) {
+    if (!b || !qd || !k_out)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_batch_run: bad arguments");
+    for (int m = 0; m < b->nmol; ++m)
+        if (!qd[m] || !k_out[m])
+            return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_batch_run: null matrix");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int nmol = b->nmol;
+    int launches = 0;
+    const double one = 1.0, zero = 0.0;
+    // per molecule: F = fl32(X QD) and the block statistics
+    for (int m = 0; m < nmol; ++m) {
+        wb_cosx* h = b->h[m];
+        const WsLayout& L = b->L[m];
+        void* ws = b->ws[m];
+        const int nao = h->hp.nao;
+        const int64_t ld = b->ld[m];
+        WB_CUBLAS(cublasSetStream(h->cublas, s));
+        WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+        if (stats)
+            WB_CUDA(cudaMemsetAsync(at<void>(ws, L.counters), 0,
+                                    sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+        const double* X = at<double>(ws, L.X);
+        float* F32 = at<float>(ws, L.F32);
+        if (b->gemm == WB_K_GEMM_OZAKI_BF16 && wb::ozaki_f_supported(nao)) {
+            const int r = wb::ozaki_f_gemm(h->cublas, X, qd[m], nao, ld, F32,
+                                           b->scratch, s);
+            if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
+                               "ozaki F GEMM failed, code " + std::to_string(r));
+            launches += 4 + wb::kOzSlices;
+        } else {
+            double* F64 = static_cast<double*>(b->scratch);
+            WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)ld, nao, nao,
+                                  &one, X, (int)ld, qd[m], nao, &zero, F64, (int)ld));
+            WB_CUDA(wb::launch_f64_to_f32(F64, F32, (int64_t)nao * ld, s));
+            launches += 2;
+        }
+        wb::BlockStatsOut bo;
+        for (int k = 0; k < 3; ++k) {
+            bo.cr[k] = at<float4>(ws, L.subcr[k]);
+            bo.msh[k] = at<float>(ws, L.msh[k]);
+        }
+        WB_CUDA(wb::launch_sub_stats(b->coords[m], b->weights[m], F32, b->npts[m], ld,
+                                     h->hp.nvshell, h->vs_ao0, h->vs_nf, bo, s));
+        launches += 1;
+    }
+    // every class: one launch over all molecules (two for the classes
+    // without a two-omega kernel)
+    WB_CUDA(cudaMemsetAsync(b->d_work, 0, sizeof(int) * 2 * wb::NCLASS, s));
+    launches += 1;
+    const wb_cosx* h0 = b->h[0];
+    for (int i = 0; i < wb::NCLASS; ++i) {
+        const int c = b->order[i];
+        if (!b->has[c] || b->items[c] == 0) continue;
+        const int want = (b->items[c] + 3) / 4;
+        const int* off = b->d_off + (size_t)c * (nmol + 1);
+        if (b->dual[c]) {
+            const int cap = std::max(1, h0->blocks_per_sm2[c]) * h0->nsm;
+            WB_CUDA(wb::launch_cosx_class_batch(c, b->d_args, off, nmol,
+                                                b->d_work + 2 * c, b->rmax2[c],
+                                                std::max(1, std::min(want, cap)), s,
+                                                false, b->smem2[c], true));
+            launches += 1;
+        } else {
+            for (int w = 0; w < b->nom; ++w) {
+                const bool far = b->om[w] == 0.0;
+                const int cap = std::max(1, h0->blocks_per_sm[c][far ? 1 : 0]) * h0->nsm;
+                WB_CUDA(wb::launch_cosx_class_batch(
+                    c, b->d_args + (size_t)w * nmol, off, nmol, b->d_work + 2 * c + w,
+                    b->rmax[c], std::max(1, std::min(want, cap)), s, far, b->smem[c],
+                    false));
+                launches += 1;
+            }
+        }
+    }
+    // per molecule: G of each slot, then K
+    for (int m = 0; m < nmol; ++m) {
+        wb_cosx* h = b->h[m];
+        const WsLayout& L = b->L[m];
+        void* ws = b->ws[m];
+        const int nao = h->hp.nao;
+        const int64_t ld = b->ld[m];
+        const size_t kk = (size_t)nao * nao;
+        const double* X = at<double>(ws, L.X);
+        float* Gs[2] = {at<float>(ws, L.G32), at<float>(ws, L.G32b)};
+        const size_t gcl[2] = {L.gcls, L.gcls2};
+        double* Ks[2] = {k_out[m] + kk * b->kidx[0], k_out[m] + kk * b->kidx[1]};
+        for (int w = 0; w < b->nom; ++w)
+            WB_CUDA(wb::launch_gsum(at<float>(ws, gcl[w]), h->gsrc, nao, ld, Gs[w], s));
+        launches += b->nom;
+        if (b->gemm == WB_K_GEMM_OZAKI_BF16) {
+            const float* Gc[2] = {Gs[0], Gs[1]};
+            const int r = wb::ozaki_k_gemm_multi(h->cublas, X, Gc, b->nom, b->weights[m],
+                                                 nao, ld, b->npts[m], 0, Ks,
+                                                 b->scratch, s, false);
+            if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
+                               "ozaki K GEMM failed, code " + std::to_string(r));
+            launches += 3 + wb::kOzSlices;
+        } else {
+            double* WG = static_cast<double*>(b->scratch);
+            for (int w = 0; w < b->nom; ++w) {
+                WB_CUDA(wb::launch_weight_g(Gs[w], b->weights[m], b->npts[m], ld, nao,
+                                            WG, s));
+                WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nao, nao,
+                                      (int)ld, &one, WG, (int)ld, X, (int)ld, &zero,
+                                      Ks[w], nao));
+                launches += 2;
+            }
+        }
+    }
+    if (!stats) return WB_OK;
+    std::memset(stats, 0, sizeof(*stats));
+    for (int m = 0; m < nmol; ++m) {
+        wb_cosx_stats st;
+        const int r = read_stats(b->h[m], b->ws[m], b->L[m],
+                                 b->nom * (b->ld[m] / 32) * (int64_t)b->h[m]->hp.npairs,
+                                 s, &st, 0);
+        if (r != WB_OK) return r;
+        stats->tasks_total += st.tasks_total;
+        stats->tasks_kept += st.tasks_kept;
+        stats->integrals += st.integrals;
+        stats->model_flops += st.model_flops;
+        for (int c = 0; c < wb::NCLASS; ++c) {
+            stats->tasks_kept_class[c] += st.tasks_kept_class[c];
+            stats->model_flops_class[c] += st.model_flops_class[c];
+        }
+    }
+    stats->kernel_launches = launches;
+    return WB_OK;
+}
+
+int wb_cosx_batch_destroy(wb_cosx_batch* b) {
+    if (!b) return WB_OK;
+    if (b->block) cudaFree(b->block);
+    delete b;
+    return WB_OK;
 }
 
 int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,

@@ -63,6 +63,9 @@ struct CosxArgs {
     // kept (the order of the next call on the same grid)
     const int* border[kClasses];
     float* bcost[kClasses];
+    // the class pair ranges (the batched kernels read them from here)
+    int cls_pb[kClasses];
+    int cls_pe[kClasses];
 };
 
 }  // namespace wb

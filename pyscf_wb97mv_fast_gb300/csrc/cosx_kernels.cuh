@@ -140,28 +140,25 @@ template<int LA, int LB, int NW = 1> struct ClassPts {
                                          : class_pts(LA * (LA + 1) / 2 + LB);
 };
 
+// One block (32 * PTS points) of one class kernel: every pair of the class
+// (screen, tasks, G) for the points of block blk.  A is the argument block
+// of the block's molecule; wstage / rmax the warp's record buffers (two of
+// rmax float4) and sbuf the one in use; kept / flops / ints accumulate the
+// counters of the warp.
 template<int LA, int LB, bool FAR, bool STAGE, int NW>
-__global__ void __launch_bounds__(kCtaThreads,
-                                  min_blocks(LA * (LA + 1) / 2 + LB, NW))
-cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
-    static_assert(NW == 1 || (NW == 2 && STAGE), "dual-omega needs staging");
+__device__ __forceinline__ void cosx_class_block(
+    const CosxArgs& A, const int pair_begin, const int pair_end, const int blk,
+    const float4* __restrict__ stab, float4* wstage, const int rmax, int& sbuf,
+    unsigned long long& kept, unsigned long long& flops,
+    unsigned long long& ints) {
     constexpr int CLS = LA * (LA + 1) / 2 + LB;
     constexpr int NCA = (LA + 1) * (LA + 2) / 2;
     constexpr int NA = 2 * LA + 1;
     constexpr int NB = 2 * LB + 1;
     constexpr int PTS = ClassPts<LA, LB, NW>::value;
-    __shared__ float4 stab[kBoysFloat4];
-    for (int i = threadIdx.x; i < kBoysFloat4; i += blockDim.x)
-        stab[i] = A.boys[i];
-    __syncthreads();
     const int lane = threadIdx.x & 31;
-    // STAGE: per warp, two record buffers of recmax float4 (dynamic smem)
-    extern __shared__ float4 s_stage[];
     constexpr int RS = NW == 2 ? kRecStride2[CLS] : kRecStride[CLS];
-    const int rmax = NW == 2 ? A.recmax2[CLS] : A.recmax[CLS];
-    float4* wstage = s_stage + (threadIdx.x >> 5) * 2 * rmax;
     const float4* __restrict__ recc = NW == 2 ? A.rec2[CLS] : A.rec[CLS];
-    int sbuf = 0;
     float* Gcw[2] = {A.Gcls[CLS], NW == 2 ? A.Gcls2[CLS] : A.Gcls[CLS]};
     const int ld = (int)A.ld;
     const float tol = A.tol;
@@ -170,6 +167,240 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
     constexpr int LVL = PTS == 4 ? 2 : PTS - 1;
     const float4* __restrict__ blk_cr = A.blk_cr[LVL];
     const float* __restrict__ blk_msh = A.blk_msh[LVL];
+    unsigned long long bfl = 0;     // model flops kept in this block
+    // the lane's points: blk * 32 PTS + 32 p + lane (clamped to the
+    // arrays; ok marks the ones that exist)
+    const float* __restrict__ Fp[PTS];
+    float* Gp[NW * PTS];
+    bool ok[PTS];
+    float gxh[PTS], gyh[PTS], gzh[PTS], gxl[PTS], gyl[PTS], gzl[PTS];
+#pragma unroll
+    for (int p = 0; p < PTS; ++p) {
+        const int g0 = blk * (32 * PTS) + 32 * p + lane;
+        ok[p] = g0 < ld;
+        const int g = ok[p] ? g0 : ld - 1;
+        Fp[p] = A.F + g;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) Gp[w * PTS + p] = Gcw[w] + g;
+        gxh[p] = A.gxyz_hi[g];
+        gyh[p] = A.gxyz_hi[ld + g];
+        gzh[p] = A.gxyz_hi[2 * (long long)ld + g];
+        gxl[p] = A.gxyz_lo[g];
+        gyl[p] = A.gxyz_lo[ld + g];
+        gzl[p] = A.gxyz_lo[2 * (long long)ld + g];
+    }
+    const float4 cr = blk_cr[blk];
+    // zero this block's columns of the class buffer(s) (each element
+    // has this lane as its one writer, so later stores and reductions
+    // follow in program order; replaces a memset pass over the buffers)
+    {
+        const int nrow = A.crow[CLS];
+        for (int r = 0; r < nrow; ++r) {
+#pragma unroll
+            for (int c = 0; c < NW * PTS; ++c)
+                if (ok[c % PTS]) Gp[c][(long long)r * ld] = 0.0f;
+        }
+    }
+    const float* __restrict__ ms = blk_msh + (long long)blk * A.nvshell;
+    const int rem = A.npts - blk * 32 * PTS;
+    const int nvalid = rem < 32 * PTS ? (rem > 0 ? rem : 0) : 32 * PTS;
+    const int nsb = (nvalid + 31) / 32;     // 32-point sub-blocks covered
+    // run state: the current bra shell (packed header word), its class
+    // buffer row, f0 and Xa; pendA / fan: F_A prefetched for a next run
+    int curA = -1, ga0 = 0, pendA = -1;
+    float f0[PTS * NCA], Xa[NW * PTS * NCA], fan[PTS * NA];
+#pragma unroll
+    for (int c = 0; c < PTS * NCA; ++c) f0[c] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < NW * PTS * NCA; ++c) Xa[c] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < PTS * NA; ++c) fan[c] = 0.0f;
+    // screen inputs of the first chunk
+    int4 nhl = make_int4(0, 0, 0, 0);
+    float2 ntp = make_float2(0.0f, 0.0f);
+    float nfm = 0.0f;
+    {
+        const int k = pair_begin + lane;
+        if (k < pair_end) {
+            nhl = A.khdr[k];
+            ntp = A.ptau[k];
+            const int2 sh = A.pshell[k];
+            nfm = fmaxf(ms[sh.x], ms[sh.y]);
+        }
+    }
+    for (int c0 = pair_begin; c0 < pair_end; c0 += 32) {
+        const int k = c0 + lane;
+        const int4 hl = nhl;
+        const float2 tp = ntp;
+        const float fm = nfm;
+        // the next chunk's header, tau and shell pair, then (after this
+        // chunk's screen) its shell maxima
+        const int kn = k + 32;
+        int2 nsh = make_int2(0, 0);
+        if (kn < pair_end) {
+            nhl = A.khdr[kn];
+            ntp = A.ptau[kn];
+            nsh = A.pshell[kn];
+        }
+        bool keep = k < pair_end;
+        if (keep && tol > 0.0f)
+            keep = screen_pair(tol, bnd, bpref, cr, hl, tp, fm);
+        if (kn < pair_end) nfm = fmaxf(ms[nsh.x], ms[nsh.y]);
+        unsigned mask = __ballot_sync(0xffffffffu, keep);
+        if (!mask) continue;
+        int4 hdr = shfl_int4(hl, __ffs(mask) - 1);
+        float fb[PTS * NB];
+#pragma unroll
+        for (int p = 0; p < PTS; ++p)
+            load_f<NB>(Fp[p], ld, lo16(hdr.y), fb + p * NB);
+        CosxRec<LA, LB> rec;
+        if constexpr (STAGE) {
+            __syncwarp();       // the previous chunk's reads of the buffer
+            stage_records(wstage + sbuf * rmax, recc + (long long)hdr.z * RS,
+                          (hdr.w & 0xffff) * RS, lane);
+            stage_wait();
+        } else {
+            cosx_rec_load<FAR>(A, hdr.z, rec);
+        }
+        while (true) {
+            if (hdr.x != curA) {
+                if (curA >= 0) {
+#pragma unroll
+                    for (int c = 0; c < NW * PTS; ++c)
+                        cosx_end<LA>(Gp[c], ga0, ld, ok[c % PTS], Xa + c * NCA);
+                }
+                curA = hdr.x;
+                ga0 = hi16(hdr.x);
+                if (pendA != curA) {
+#pragma unroll
+                    for (int p = 0; p < PTS; ++p)
+                        load_f<NA>(Fp[p], ld, lo16(hdr.x), fan + p * NA);
+                    pendA = curA;
+                }
+#pragma unroll
+                for (int p = 0; p < PTS; ++p)
+                    cosx_begin<LA>(fan + p * NA, f0 + p * NCA);
+#pragma unroll
+                for (int c = 0; c < NW * PTS * NCA; ++c) Xa[c] = 0.0f;
+            }
+            mask &= mask - 1;
+            // prefetch the next kept task of this chunk (fan is free:
+            // f0 of the current run is formed)
+            const bool more = mask != 0u;
+            int4 hn = hdr;
+            float fbn[PTS * NB];
+            if (more) {
+                hn = shfl_int4(hl, __ffs(mask) - 1);
+#pragma unroll
+                for (int p = 0; p < PTS; ++p)
+                    load_f<NB>(Fp[p], ld, lo16(hn.y), fbn + p * NB);
+                if (hn.x != hdr.x) {
+#pragma unroll
+                    for (int p = 0; p < PTS; ++p)
+                        load_f<NA>(Fp[p], ld, lo16(hn.x), fan + p * NA);
+                    pendA = hn.x;
+                }
+                // the next task's records into the other buffer (the
+                // last reads of it ended before the previous wait)
+                if constexpr (STAGE)
+                    stage_records(wstage + (sbuf ^ 1) * rmax,
+                                  recc + (long long)hn.z * RS,
+                                  (hn.w & 0xffff) * RS, lane);
+            }
+            const int gb0 = hi16(hdr.y), pp0 = hdr.z, npp = hdr.w & 0xffff;
+            const int nxt = more ? hn.z : pp0;
+            if constexpr (NW == 2) {
+                const float4* rp = wstage + sbuf * rmax;
+                if constexpr (LA == LB) {
+                    if (hdr.w >> 16)
+                        CosxTask2<LA, LB, true, PTS>::run(
+                            Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                            gxl, gyl, gzl, stab, f0, fb, Xa);
+                    else
+                        CosxTask2<LA, LB, false, PTS>::run(
+                            Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                            gxl, gyl, gzl, stab, f0, fb, Xa);
+                } else {
+                    CosxTask2<LA, LB, false, PTS>::run(
+                        Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                        gxl, gyl, gzl, stab, f0, fb, Xa);
+                }
+            } else if constexpr (STAGE) {
+                const float4* rp = wstage + sbuf * rmax;
+                if constexpr (LA == LB) {
+                    if (hdr.w >> 16)
+                        CosxTask<LA, LB, true, PTS, FAR, true>::run(
+                            A, Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                            gxl, gyl, gzl, stab, f0, fb, Xa);
+                    else
+                        CosxTask<LA, LB, false, PTS, FAR, true>::run(
+                            A, Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                            gxl, gyl, gzl, stab, f0, fb, Xa);
+                } else {
+                    CosxTask<LA, LB, false, PTS, FAR, true>::run(
+                        A, Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
+                        gxl, gyl, gzl, stab, f0, fb, Xa);
+                }
+            } else if constexpr (LA == LB) {
+                if (hdr.w >> 16)
+                    CosxTask<LA, LB, true, PTS, FAR, false>::run(
+                        A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
+                        gxl, gyl, gzl, stab, f0, fb, Xa, rec);
+                else
+                    CosxTask<LA, LB, false, PTS, FAR, false>::run(
+                        A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
+                        gxl, gyl, gzl, stab, f0, fb, Xa, rec);
+            } else {
+                CosxTask<LA, LB, false, PTS, FAR, false>::run(
+                    A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
+                    gxl, gyl, gzl, stab, f0, fb, Xa, rec);
+            }
+            kept += nsb * NW;
+            if (!more) break;
+            if constexpr (STAGE) {
+                stage_wait();
+                sbuf ^= 1;
+            }
+            hdr = hn;
+#pragma unroll
+            for (int nu = 0; nu < PTS * NB; ++nu) fb[nu] = fbn[nu];
+        }
+        // model flops / integrals of the kept tasks of this chunk
+        if (keep) {
+            const unsigned long long fk =
+                (unsigned long long)A.pflops[k] * nvalid * NW;
+            flops += fk;
+            bfl += fk;
+            ints += (unsigned long long)A.pnint[k] * nvalid * NW;
+        }
+    }
+    if (curA >= 0) {
+#pragma unroll
+        for (int c = 0; c < NW * PTS; ++c)
+            cosx_end<LA>(Gp[c], ga0, ld, ok[c % PTS], Xa + c * NCA);
+    }
+    for (int o = 16; o > 0; o >>= 1) bfl += __shfl_xor_sync(0xffffffffu, bfl, o);
+    if (lane == 0 && A.bcost[CLS]) A.bcost[CLS][blk] = (float)bfl;
+}
+
+template<int LA, int LB, bool FAR, bool STAGE, int NW>
+__global__ void __launch_bounds__(kCtaThreads,
+                                  min_blocks(LA * (LA + 1) / 2 + LB, NW))
+cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
+    static_assert(NW == 1 || (NW == 2 && STAGE), "dual-omega needs staging");
+    constexpr int CLS = LA * (LA + 1) / 2 + LB;
+    constexpr int PTS = ClassPts<LA, LB, NW>::value;
+    __shared__ float4 stab[kBoysFloat4];
+    for (int i = threadIdx.x; i < kBoysFloat4; i += blockDim.x)
+        stab[i] = A.boys[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    // STAGE: per warp, two record buffers of recmax float4 (dynamic smem)
+    extern __shared__ float4 s_stage[];
+    const int rmax = NW == 2 ? A.recmax2[CLS] : A.recmax[CLS];
+    float4* wstage = s_stage + (threadIdx.x >> 5) * 2 * rmax;
+    int sbuf = 0;
+    constexpr int LVL = PTS == 4 ? 2 : PTS - 1;
     const int nblk = A.nblk[LVL];
     unsigned long long kept = 0, flops = 0, ints = 0;
     const int* __restrict__ order = A.border[CLS];
@@ -184,220 +415,9 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
             const int b = order[item];
             blk = b >= 0 && b < nblk ? b : item;
         }
-        unsigned long long bfl = 0;     // model flops kept in this block
-        // the lane's points: blk * 32 PTS + 32 p + lane (clamped to the
-        // arrays; ok marks the ones that exist)
-        const float* __restrict__ Fp[PTS];
-        float* Gp[NW * PTS];
-        bool ok[PTS];
-        float gxh[PTS], gyh[PTS], gzh[PTS], gxl[PTS], gyl[PTS], gzl[PTS];
-#pragma unroll
-        for (int p = 0; p < PTS; ++p) {
-            const int g0 = blk * (32 * PTS) + 32 * p + lane;
-            ok[p] = g0 < ld;
-            const int g = ok[p] ? g0 : ld - 1;
-            Fp[p] = A.F + g;
-#pragma unroll
-            for (int w = 0; w < NW; ++w) Gp[w * PTS + p] = Gcw[w] + g;
-            gxh[p] = A.gxyz_hi[g];
-            gyh[p] = A.gxyz_hi[ld + g];
-            gzh[p] = A.gxyz_hi[2 * (long long)ld + g];
-            gxl[p] = A.gxyz_lo[g];
-            gyl[p] = A.gxyz_lo[ld + g];
-            gzl[p] = A.gxyz_lo[2 * (long long)ld + g];
-        }
-        const float4 cr = blk_cr[blk];
-        // zero this block's columns of the class buffer(s) (each element
-        // has this lane as its one writer, so later stores and reductions
-        // follow in program order; replaces a memset pass over the buffers)
-        {
-            const int nrow = A.crow[CLS];
-            for (int r = 0; r < nrow; ++r) {
-#pragma unroll
-                for (int c = 0; c < NW * PTS; ++c)
-                    if (ok[c % PTS]) Gp[c][(long long)r * ld] = 0.0f;
-            }
-        }
-        const float* __restrict__ ms = blk_msh + (long long)blk * A.nvshell;
-        const int rem = A.npts - blk * 32 * PTS;
-        const int nvalid = rem < 32 * PTS ? (rem > 0 ? rem : 0) : 32 * PTS;
-        const int nsb = (nvalid + 31) / 32;     // 32-point sub-blocks covered
-        // run state: the current bra shell (packed header word), its class
-        // buffer row, f0 and Xa; pendA / fan: F_A prefetched for a next run
-        int curA = -1, ga0 = 0, pendA = -1;
-        float f0[PTS * NCA], Xa[NW * PTS * NCA], fan[PTS * NA];
-#pragma unroll
-        for (int c = 0; c < PTS * NCA; ++c) f0[c] = 0.0f;
-#pragma unroll
-        for (int c = 0; c < NW * PTS * NCA; ++c) Xa[c] = 0.0f;
-#pragma unroll
-        for (int c = 0; c < PTS * NA; ++c) fan[c] = 0.0f;
-        // screen inputs of the first chunk
-        int4 nhl = make_int4(0, 0, 0, 0);
-        float2 ntp = make_float2(0.0f, 0.0f);
-        float nfm = 0.0f;
-        {
-            const int k = pair_begin + lane;
-            if (k < pair_end) {
-                nhl = A.khdr[k];
-                ntp = A.ptau[k];
-                const int2 sh = A.pshell[k];
-                nfm = fmaxf(ms[sh.x], ms[sh.y]);
-            }
-        }
-        for (int c0 = pair_begin; c0 < pair_end; c0 += 32) {
-            const int k = c0 + lane;
-            const int4 hl = nhl;
-            const float2 tp = ntp;
-            const float fm = nfm;
-            // the next chunk's header, tau and shell pair, then (after this
-            // chunk's screen) its shell maxima
-            const int kn = k + 32;
-            int2 nsh = make_int2(0, 0);
-            if (kn < pair_end) {
-                nhl = A.khdr[kn];
-                ntp = A.ptau[kn];
-                nsh = A.pshell[kn];
-            }
-            bool keep = k < pair_end;
-            if (keep && tol > 0.0f)
-                keep = screen_pair(tol, bnd, bpref, cr, hl, tp, fm);
-            if (kn < pair_end) nfm = fmaxf(ms[nsh.x], ms[nsh.y]);
-            unsigned mask = __ballot_sync(0xffffffffu, keep);
-            if (!mask) continue;
-            int4 hdr = shfl_int4(hl, __ffs(mask) - 1);
-            float fb[PTS * NB];
-#pragma unroll
-            for (int p = 0; p < PTS; ++p)
-                load_f<NB>(Fp[p], ld, lo16(hdr.y), fb + p * NB);
-            CosxRec<LA, LB> rec;
-            if constexpr (STAGE) {
-                __syncwarp();       // the previous chunk's reads of the buffer
-                stage_records(wstage + sbuf * rmax, recc + (long long)hdr.z * RS,
-                              (hdr.w & 0xffff) * RS, lane);
-                stage_wait();
-            } else {
-                cosx_rec_load<FAR>(A, hdr.z, rec);
-            }
-            while (true) {
-                if (hdr.x != curA) {
-                    if (curA >= 0) {
-#pragma unroll
-                        for (int c = 0; c < NW * PTS; ++c)
-                            cosx_end<LA>(Gp[c], ga0, ld, ok[c % PTS], Xa + c * NCA);
-                    }
-                    curA = hdr.x;
-                    ga0 = hi16(hdr.x);
-                    if (pendA != curA) {
-#pragma unroll
-                        for (int p = 0; p < PTS; ++p)
-                            load_f<NA>(Fp[p], ld, lo16(hdr.x), fan + p * NA);
-                        pendA = curA;
-                    }
-#pragma unroll
-                    for (int p = 0; p < PTS; ++p)
-                        cosx_begin<LA>(fan + p * NA, f0 + p * NCA);
-#pragma unroll
-                    for (int c = 0; c < NW * PTS * NCA; ++c) Xa[c] = 0.0f;
-                }
-                mask &= mask - 1;
-                // prefetch the next kept task of this chunk (fan is free:
-                // f0 of the current run is formed)
-                const bool more = mask != 0u;
-                int4 hn = hdr;
-                float fbn[PTS * NB];
-                if (more) {
-                    hn = shfl_int4(hl, __ffs(mask) - 1);
-#pragma unroll
-                    for (int p = 0; p < PTS; ++p)
-                        load_f<NB>(Fp[p], ld, lo16(hn.y), fbn + p * NB);
-                    if (hn.x != hdr.x) {
-#pragma unroll
-                        for (int p = 0; p < PTS; ++p)
-                            load_f<NA>(Fp[p], ld, lo16(hn.x), fan + p * NA);
-                        pendA = hn.x;
-                    }
-                    // the next task's records into the other buffer (the
-                    // last reads of it ended before the previous wait)
-                    if constexpr (STAGE)
-                        stage_records(wstage + (sbuf ^ 1) * rmax,
-                                      recc + (long long)hn.z * RS,
-                                      (hn.w & 0xffff) * RS, lane);
-                }
-                const int gb0 = hi16(hdr.y), pp0 = hdr.z, npp = hdr.w & 0xffff;
-                const int nxt = more ? hn.z : pp0;
-                if constexpr (NW == 2) {
-                    const float4* rp = wstage + sbuf * rmax;
-                    if constexpr (LA == LB) {
-                        if (hdr.w >> 16)
-                            CosxTask2<LA, LB, true, PTS>::run(
-                                Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
-                                gxl, gyl, gzl, stab, f0, fb, Xa);
-                        else
-                            CosxTask2<LA, LB, false, PTS>::run(
-                                Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
-                                gxl, gyl, gzl, stab, f0, fb, Xa);
-                    } else {
-                        CosxTask2<LA, LB, false, PTS>::run(
-                            Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
-                            gxl, gyl, gzl, stab, f0, fb, Xa);
-                    }
-                } else if constexpr (STAGE) {
-                    const float4* rp = wstage + sbuf * rmax;
-                    if constexpr (LA == LB) {
-                        if (hdr.w >> 16)
-                            CosxTask<LA, LB, true, PTS, FAR, true>::run(
-                                A, Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
-                                gxl, gyl, gzl, stab, f0, fb, Xa);
-                        else
-                            CosxTask<LA, LB, false, PTS, FAR, true>::run(
-                                A, Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
-                                gxl, gyl, gzl, stab, f0, fb, Xa);
-                    } else {
-                        CosxTask<LA, LB, false, PTS, FAR, true>::run(
-                            A, Gp, ld, gb0, rp, npp, ok, gxh, gyh, gzh,
-                            gxl, gyl, gzl, stab, f0, fb, Xa);
-                    }
-                } else if constexpr (LA == LB) {
-                    if (hdr.w >> 16)
-                        CosxTask<LA, LB, true, PTS, FAR, false>::run(
-                            A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
-                            gxl, gyl, gzl, stab, f0, fb, Xa, rec);
-                    else
-                        CosxTask<LA, LB, false, PTS, FAR, false>::run(
-                            A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
-                            gxl, gyl, gzl, stab, f0, fb, Xa, rec);
-                } else {
-                    CosxTask<LA, LB, false, PTS, FAR, false>::run(
-                        A, Gp, ld, gb0, pp0, npp, nxt, ok, gxh, gyh, gzh,
-                        gxl, gyl, gzl, stab, f0, fb, Xa, rec);
-                }
-                kept += nsb * NW;
-                if (!more) break;
-                if constexpr (STAGE) {
-                    stage_wait();
-                    sbuf ^= 1;
-                }
-                hdr = hn;
-#pragma unroll
-                for (int nu = 0; nu < PTS * NB; ++nu) fb[nu] = fbn[nu];
-            }
-            // model flops / integrals of the kept tasks of this chunk
-            if (keep) {
-                const unsigned long long fk =
-                    (unsigned long long)A.pflops[k] * nvalid * NW;
-                flops += fk;
-                bfl += fk;
-                ints += (unsigned long long)A.pnint[k] * nvalid * NW;
-            }
-        }
-        if (curA >= 0) {
-#pragma unroll
-            for (int c = 0; c < NW * PTS; ++c)
-                cosx_end<LA>(Gp[c], ga0, ld, ok[c % PTS], Xa + c * NCA);
-        }
-        for (int o = 16; o > 0; o >>= 1) bfl += __shfl_xor_sync(0xffffffffu, bfl, o);
-        if (lane == 0 && A.bcost[CLS]) A.bcost[CLS][blk] = (float)bfl;
+        cosx_class_block<LA, LB, FAR, STAGE, NW>(A, pair_begin, pair_end, blk, stab,
+                                                 wstage, rmax, sbuf, kept, flops,
+                                                 ints);
     }
     // lane 0 counted the tasks (every lane runs every task) in units of the
     // 32-point sub-blocks they cover; every lane counted the flops /
@@ -411,6 +431,86 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
         atomicAdd(A.counters + 3 * CLS + 1, flops);
         atomicAdd(A.counters + 3 * CLS + 2, ints);
     }
+}
+
+// Batched form: the blocks of one class over several molecules in one
+// launch.  args[m] is molecule m's argument block (its class pair range in
+// cls_pb / cls_pe); its blocks of this class are the items item_off[m] ..
+// item_off[m + 1] - 1 (ascending).  Warps take items from one counter
+// (*work) and copy the argument block of the molecule they work on into
+// shared memory; rmax is the largest task record of the class over the
+// molecules (the dynamic shared memory holds two per warp).  The Boys table
+// is the same for every molecule.  Each molecule's counters receive its own
+// tasks; every element of every class buffer keeps one writer lane and its
+// summation order, so each molecule's G equals its single-molecule G.
+template<int LA, int LB, bool FAR, bool STAGE, int NW>
+__global__ void __launch_bounds__(kCtaThreads,
+                                  min_blocks(LA * (LA + 1) / 2 + LB, NW))
+cosx_class_kernel_batch(const CosxArgs* __restrict__ args,
+                        const int* __restrict__ item_off, const int nmol,
+                        int* __restrict__ work, const int rmax) {
+    static_assert(NW == 1 || (NW == 2 && STAGE), "dual-omega needs staging");
+    constexpr int CLS = LA * (LA + 1) / 2 + LB;
+    constexpr int NWARP = kCtaThreads / 32;
+    static_assert(sizeof(CosxArgs) % 4 == 0, "argument block copied as words");
+    __shared__ float4 stab[kBoysFloat4];
+    __shared__ CosxArgs sA[NWARP];
+    const float4* __restrict__ boys = args[0].boys;
+    for (int i = threadIdx.x; i < kBoysFloat4; i += blockDim.x) stab[i] = boys[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    extern __shared__ float4 s_stage[];
+    float4* wstage = s_stage + warp * 2 * rmax;
+    int sbuf = 0;
+    const int total = item_off[nmol];
+    int cur = -1;
+    unsigned long long kept = 0, flops = 0, ints = 0;
+    auto flush = [&]() {
+        unsigned long long f = flops, n = ints;
+        for (int o = 16; o > 0; o >>= 1) {
+            f += __shfl_xor_sync(0xffffffffu, f, o);
+            n += __shfl_xor_sync(0xffffffffu, n, o);
+        }
+        if (lane == 0 && kept) {
+            unsigned long long* c = sA[warp].counters + 3 * CLS;
+            atomicAdd(c + 0, kept);
+            atomicAdd(c + 1, f);
+            atomicAdd(c + 2, n);
+        }
+        kept = flops = ints = 0;
+    };
+    for (;;) {
+        int item = 0, m = 0;
+        if (lane == 0) {
+            item = atomicAdd(work, 1);
+            if (item < total) {
+                int lo = 0, hi = nmol;          // item_off[lo] <= item < item_off[hi]
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (item_off[mid] <= item) lo = mid; else hi = mid;
+                }
+                m = lo;
+            }
+        }
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        m = __shfl_sync(0xffffffffu, m, 0);
+        if (m != cur) {
+            if (cur >= 0) flush();
+            __syncwarp();
+            const int* src = reinterpret_cast<const int*>(args + m);
+            int* dst = reinterpret_cast<int*>(sA + warp);
+            for (int i = lane; i < (int)(sizeof(CosxArgs) / 4); i += 32) dst[i] = src[i];
+            __syncwarp();
+            cur = m;
+        }
+        const CosxArgs& Am = sA[warp];
+        cosx_class_block<LA, LB, FAR, STAGE, NW>(Am, Am.cls_pb[CLS], Am.cls_pe[CLS],
+                                                 item - item_off[m], stab, wstage,
+                                                 rmax, sbuf, kept, flops, ints);
+    }
+    if (cur >= 0) flush();
 }
 
 }  // namespace wb

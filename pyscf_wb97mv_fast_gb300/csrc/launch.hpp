@@ -16,6 +16,14 @@ namespace wb {
 cudaError_t launch_cosx_class_range(int cls, const CosxArgs& a, int pb,
                                     int pe, int grid, cudaStream_t s, bool far,
                                     size_t stage_smem, bool dual = false);
+// the batched form: one launch over the class's blocks of nmol molecules
+// (args: nmol device argument blocks; off: nmol + 1 item offsets; work: a
+// zeroed counter; rmax: the largest task record of the class over the
+// molecules, smem = 4 warps x 2 x rmax float4 when staged)
+cudaError_t launch_cosx_class_batch(int cls, const CosxArgs* args, const int* off,
+                                    int nmol, int* work, int rmax, int grid,
+                                    cudaStream_t s, bool far, size_t smem,
+                                    bool dual);
 // max resident CTAs per SM of a class kernel (128 threads each); 0 if the
 // kernel cannot run with that much dynamic shared memory
 int cosx_class_blocks_per_sm(int cls, bool far, size_t stage_smem,
