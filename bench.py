@@ -661,6 +661,8 @@ def main():
                     help='skip the plain FP64 form timing')
     ap.add_argument('--no-serving', action='store_true',
                     help='skip the continuous-batching serving leg')
+    ap.add_argument('--no-autotune', action='store_true',
+                    help='keep the compiled-in per-class kernel variants')
     ap.add_argument('--no-batched', action='store_true',
                     help='skip the batched (many molecules per launch) leg')
     args = ap.parse_args()
@@ -686,6 +688,12 @@ def main():
     coords_d = eng.relative(g.coords)
     w_d = torch.as_tensor(g.weights, device=dev)
     qd_d = torch.as_tensor(dm, device=dev)
+    # per-class kernel variants tuned on this grid and density (untimed set-up)
+    tuned = None
+    if not args.no_autotune:
+        from pyscf_wb97mv_fast_gb300.autotune import autotune_classes
+        tuned = autotune_classes(eng, coords_d, w_d, qd_d, OMEGAS, tile_tol=TILE_TOL)
+        torch.cuda.empty_cache()
     K = torch.empty((len(OMEGAS), mol.nao, mol.nao), dtype=torch.float64,
                     device=dev)
 
@@ -847,6 +855,7 @@ def main():
             'serving': serving,
             'cuda_graphs': graphs,
             'batched': batched,
+            'autotune': tuned,
             'clocks': clocks.summary(),
             'gpu_launches': launches_step * args.steps,
             'tasks_kept': kept, 'tasks_total': total,

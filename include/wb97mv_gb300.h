@@ -149,6 +149,19 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
                         void* workspace, size_t workspace_bytes, void* stream,
                         wb_cosx_stats* stats);
 
+/* Kernel variant of one class on this handle (the knobs of the autotuner,
+ * pyscf_wb97mv_fast_gb300/autotune.py): dual = 1 runs the class's
+ * two-omega kernel in two-omega passes (else one single-omega launch per
+ * omega); staged = 1 stages each task's primitive-pair records in shared
+ * memory (else they are prefetched into registers).  A variant the
+ * molecule cannot run (records too large for shared memory, no two-omega
+ * kernel) returns WB_ERR_UNSUPPORTED and leaves the class as it was.
+ * Results are the same to FP32 rounding whatever the variant; each variant
+ * is deterministic.  The reference has one kernel per class
+ * (gpu/sgx_k.py:165-400) and no autotuner. */
+int wb_cosx_set_class_variant(wb_cosx* h, int cls, int dual, int staged);
+int wb_cosx_get_class_variant(const wb_cosx* h, int cls, int* dual, int* staged);
+
 /* Plain FP64 form of the K build: the same steps as wb_cosx_get_k_multi
  * with every step in FP64 and nothing rounded to FP32.  X (FP64 AO values)
  * -> F = X QD (cuBLAS DGEMM, kept FP64) -> the same screen (block

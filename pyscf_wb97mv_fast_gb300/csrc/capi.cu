@@ -1167,6 +1167,41 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
     return st;
 }
 
+int wb_cosx_set_class_variant(wb_cosx* h, int cls, int dual, int staged) {
+    if (!h || cls < 0 || cls >= wb::NCLASS || dual < 0 || dual > 1 || staged < 0 ||
+        staged > 1)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_set_class_variant: bad arguments");
+    const int c = cls;
+    if (dual && !(h->stage_smem2[c] > 0 && h->blocks_per_sm2[c] >= 1))
+        return fail(WB_ERR_UNSUPPORTED, "wb_cosx_set_class_variant: class " +
+                                            std::to_string(c) +
+                                            " has no two-omega kernel for this molecule");
+    size_t smem = 0;
+    if (staged) {
+        smem = (size_t)(128 / 32) * 2 * h->recmax[c] * sizeof(float4);
+        if (h->recmax[c] <= 0 || smem > kStageMaxBytes)
+            return fail(WB_ERR_UNSUPPORTED, "wb_cosx_set_class_variant: class " +
+                                                std::to_string(c) +
+                                                " records do not fit the staged kernel");
+    }
+    int n[2];
+    for (int f = 0; f < 2; ++f) n[f] = wb::cosx_class_blocks_per_sm(c, f == 1, smem);
+    if (n[0] == 0 || n[1] == 0)
+        return fail(WB_ERR_UNSUPPORTED, "wb_cosx_set_class_variant: no occupancy");
+    h->stage_smem[c] = smem;
+    for (int f = 0; f < 2; ++f) h->blocks_per_sm[c][f] = n[f];
+    h->dual_cls[c] = dual != 0;
+    return WB_OK;
+}
+
+int wb_cosx_get_class_variant(const wb_cosx* h, int cls, int* dual, int* staged) {
+    if (!h || cls < 0 || cls >= wb::NCLASS || !dual || !staged)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_get_class_variant: bad arguments");
+    *dual = h->dual_cls[cls] ? 1 : 0;
+    *staged = h->stage_smem[cls] > 0 ? 1 : 0;
+    return WB_OK;
+}
+
 size_t wb_cosx_fp64_workspace_bytes(const wb_cosx* h, int64_t npts) {
     if (!h || npts < 0) return 0;
     return ws_layout_fp64(h, round32(std::max<int64_t>(npts, 1))).total;
