@@ -409,6 +409,33 @@ def graph_timing(torch, sizes=(4, 8, 16, 32), reps=10):
     return out
 
 
+def grad_timing(torch, calls=2):
+    """The COSX exchange nuclear gradient (wb_cosx_k_grad, FP64, grid
+    response off) of the bench molecule and density on its level-0 grid,
+    omega = 0, k_tile_tol as the K builds: ms per call after one warm-up
+    call."""
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    mol, _, dm = workload()
+    g0 = build_grids(mol, level=0)
+    eng = CosxEngine(mol)
+    c = eng.relative(g0.coords)
+    w = torch.as_tensor(g0.weights, device=eng.device)
+    grad = eng.k_grad(c, w, dm, 0.0, tile_tol=TILE_TOL)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        grad = eng.k_grad(c, w, dm, 0.0, tile_tol=TILE_TOL)
+    t = (time.perf_counter() - t0) / calls
+    eng._ws = None
+    eng.close()
+    return {'ms_per_call': t * 1e3, 'points': int(g0.size), 'natm': mol.natm,
+            'omega': 0.0, 'k_tile_tol': TILE_TOL,
+            'max_abs_grad': float(np.abs(grad).max()),
+            'what': 'AO values and gradients, F = X D, FP64 G, the AO-side '
+                    'contraction, FP64 integral-derivative kernels'}
+
+
 def batched_timing(torch, nmol=64, seed=4, iters=3):
     """Config-4 shape: nmol seeded water clusters of n in {4..32} waters
     (uniform), synthetic def2-SVP, level-0 grids, both omegas.  One SCF
@@ -661,6 +688,8 @@ def main():
                     help='skip the plain FP64 form timing')
     ap.add_argument('--no-serving', action='store_true',
                     help='skip the continuous-batching serving leg')
+    ap.add_argument('--no-grad', action='store_true',
+                    help='skip the exchange-gradient timing')
     ap.add_argument('--no-autotune', action='store_true',
                     help='keep the compiled-in per-class kernel variants')
     ap.add_argument('--no-batched', action='store_true',
@@ -831,6 +860,7 @@ def main():
     eng._ws = None
     torch.cuda.empty_cache()
     batched = None if (args.no_batched or world > 1) else batched_timing(torch)
+    k_grad = None if (args.no_grad or world > 1) else grad_timing(torch)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -856,6 +886,7 @@ def main():
             'cuda_graphs': graphs,
             'batched': batched,
             'autotune': tuned,
+            'k_grad': k_grad,
             'clocks': clocks.summary(),
             'gpu_launches': launches_step * args.steps,
             'tasks_kept': kept, 'tasks_total': total,

@@ -149,6 +149,25 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
                         void* workspace, size_t workspace_bytes, void* stream,
                         wb_cosx_stats* stats);
 
+/* COSX exchange nuclear gradient with the grid response off, in FP64:
+ * grad_out (natm, 3) = dE/dR of E = -1/4 tr(D K(omega)) at fixed D, fixed
+ * grid points and weights (the SGX gradient with grid response off), for
+ * the plain SGX K (no PJS projector: dm is the symmetric density).  Two
+ * parts: the AO-value side 1/2 sum_g w_g sum_{mu on C} grad X_g,mu (G D)_g,mu
+ * with G from the FP64 class kernels, and the integral side
+ * -1/2 sum_g w_g sum_{nu on C, lam} F_g,nu F_g,lam d(nu lam|g)/dR_nu from
+ * FP64 derivative kernels (d/dA = 2 alpha (a+1) - a_x (a-1); the ket side
+ * by translational invariance).  tile_tol screens tasks as the K build
+ * does.  Bitwise reproducible.  The reference computes gradients with
+ * stock PySCF (pyscf.sgx.grad, grid response off; README.md:134-137) and
+ * has no GPU gradient of its own (README.md:168).  Calls the same lazy
+ * FP64 table upload as wb_cosx_get_k_fp64. */
+size_t wb_cosx_k_grad_workspace_bytes(const wb_cosx* h, int64_t npts, int natm);
+int wb_cosx_k_grad(wb_cosx* h, const double* coords, const double* weights,
+                   int64_t npts, const double* dm, double omega, double tile_tol,
+                   int natm, double* grad_out, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
 /* Kernel variant of one class on this handle (the knobs of the autotuner,
  * pyscf_wb97mv_fast_gb300/autotune.py): dual = 1 runs the class's
  * two-omega kernel in two-omega passes (else one single-omega launch per

@@ -48,6 +48,7 @@ EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_vv10_kernel_sum_noalloc',
             'wb_cosx_fp64_workspace_bytes', 'wb_cosx_get_k_fp64',
             'wb_cosx_set_class_variant', 'wb_cosx_get_class_variant',
+            'wb_cosx_k_grad_workspace_bytes', 'wb_cosx_k_grad',
             'wb_cosx_batch_workspace_bytes', 'wb_cosx_batch_create',
             'wb_cosx_batch_run', 'wb_cosx_batch_destroy',
             'wb_status_string',
@@ -158,6 +159,9 @@ def _declare(lib):
                                    ctypes.c_size_t, _P]),
         'wb_cosx_fp64_workspace_bytes': (ctypes.c_size_t, [_P, _I64]),
         'wb_cosx_set_class_variant': (_INT, [_P, _INT, _INT, _INT]),
+        'wb_cosx_k_grad_workspace_bytes': (ctypes.c_size_t, [_P, _I64, _INT]),
+        'wb_cosx_k_grad': (_INT, [_P, _P, _P, _I64, _P, _D, _D, _INT, _P, _P,
+                                  ctypes.c_size_t, _P]),
         'wb_cosx_get_class_variant': (_INT, [_P, _INT, ctypes.POINTER(_INT),
                                              ctypes.POINTER(_INT)]),
         'wb_cosx_get_k_fp64': (_INT, [_P, _P, _P, _I64, _P, _INT, _P, _D, _P, _P,

@@ -182,6 +182,24 @@ class CosxEngine:
             self.last_stats = st.as_dict()
         return out
 
+    def k_grad(self, coords_rel, weights, dm, omega, tile_tol=0.0):
+        """Nuclear gradient (natm, 3) FP64 (host) of E = -1/4 tr(D K(omega))
+        at fixed D, grid points and weights (SGX with the grid response
+        off), for the plain SGX K (dm the symmetric density, no projector);
+        FP64 throughout (wb_cosx_k_grad)."""
+        torch = _torch()
+        npts = int(coords_rel.shape[0])
+        natm = int(self.mol.natm)
+        nbytes = int(_native.lib().wb_cosx_k_grad_workspace_bytes(self._h, npts, natm))
+        ws = self.workspace(nbytes)
+        out = torch.empty((natm, 3), dtype=torch.float64, device=self.device)
+        d = torch.as_tensor(dm, dtype=torch.float64, device=self.device).contiguous()
+        _native.check(_native.lib().wb_cosx_k_grad(
+            self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
+            _native.ptr(d), float(omega), float(tile_tol), natm, _native.ptr(out),
+            _native.ptr(ws), nbytes, self._stream()), 'wb_cosx_k_grad')
+        return out.cpu().numpy()
+
     def capture_k_multi(self, coords_rel, weights, omegas, tile_tol=1e-11,
                         gemm='ozaki'):
         """A get_k_multi build captured in a CUDA graph on fixed buffers:

@@ -16,6 +16,7 @@
 
 #include "host.hpp"
 #include "cosx_fp64.hpp"
+#include "cosx_grad64.hpp"
 #include "generated/cosx_layout.h"
 #include "launch.hpp"
 #include "ozaki.hpp"
@@ -176,6 +177,9 @@ struct wb_cosx {
     double* f64_E = nullptr;
     double* f64_boys = nullptr;
     long long f64_ebase[wb::NCLASS] = {0};
+    double* f64_alpha = nullptr;     // bra exponent per primitive pair
+    double* f64_vsxyz = nullptr;     // virtual shell centres (3 each)
+    int* vs_atom = nullptr;          // virtual shell atoms
 };
 
 namespace {
@@ -592,9 +596,30 @@ int ensure_fp64(wb_cosx* h) {
         if (B) cudaFree(B);
         return cuda_fail(e, "FP64 pair tables");
     }
+    std::vector<double> vxyz;
+    std::vector<int> vat;
+    for (const wb::VShell& v : h->hp.vsh) {
+        for (int x = 0; x < 3; ++x) vxyz.push_back(v.A[x]);
+        vat.push_back(v.atom);
+    }
+    double *AL = nullptr, *VX = nullptr;
+    int* VA = nullptr;
+    e = upload(&AL, hp64.alpha);
+    if (e == cudaSuccess) e = upload(&VX, vxyz);
+    if (e == cudaSuccess) e = cudaMalloc(&VA, sizeof(int) * std::max<size_t>(vat.size(), 1));
+    if (e == cudaSuccess && !vat.empty())
+        e = cudaMemcpy(VA, vat.data(), sizeof(int) * vat.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        for (void* q : {(void*)P, (void*)E, (void*)B, (void*)AL, (void*)VX, (void*)VA})
+            if (q) cudaFree(q);
+        return cuda_fail(e, "FP64 pair tables");
+    }
     h->f64_P = P;
     h->f64_E = E;
     h->f64_boys = B;
+    h->f64_alpha = AL;
+    h->f64_vsxyz = VX;
+    h->vs_atom = VA;
     for (int c = 0; c < wb::NCLASS; ++c) h->f64_ebase[c] = hp64.e_base[c];
     return WB_OK;
 }
@@ -928,6 +953,9 @@ int wb_cosx_destroy(wb_cosx* h) {
     if (h->f64_P) cudaFree(h->f64_P);
     if (h->f64_E) cudaFree(h->f64_E);
     if (h->f64_boys) cudaFree(h->f64_boys);
+    if (h->f64_alpha) cudaFree(h->f64_alpha);
+    if (h->f64_vsxyz) cudaFree(h->f64_vsxyz);
+    if (h->vs_atom) cudaFree(h->vs_atom);
     delete h;
     return WB_OK;
 }
@@ -1655,6 +1683,125 @@ int wb_cosx_batch_destroy(wb_cosx_batch* b) {
     if (!b) return WB_OK;
     if (b->block) cudaFree(b->block);
     delete b;
+    return WB_OK;
+}
+
+size_t wb_cosx_k_grad_workspace_bytes(const wb_cosx* h, int64_t npts, int natm) {
+    if (!h || npts < 0 || natm < 1) return 0;
+    const int64_t ld = round32(std::max<int64_t>(npts, 1));
+    const WsLayout64 L = ws_layout_fp64(h, ld);
+    const size_t n = (size_t)h->hp.nao * ld;
+    return align256(L.total + sizeof(double) * 4 * n) +
+           align256(sizeof(double) * (size_t)(ld / 32) * natm * 3) +
+           align256(sizeof(double) * 3 * (size_t)h->hp.nao);
+}
+
+int wb_cosx_k_grad(wb_cosx* h, const double* coords, const double* weights,
+                   int64_t npts, const double* dm, double omega, double tile_tol,
+                   int natm, double* grad_out, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+    if (!h || !dm || !grad_out || npts < 1 || !coords || !weights || natm < 1 ||
+        !(omega >= 0.0) || !(tile_tol >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_k_grad: bad arguments");
+    for (const wb::VShell& v : h->hp.vsh)
+        if (v.atom >= natm)
+            return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_k_grad: natm below the basis atoms");
+    const int64_t ld = round32(npts);
+    if (ld > INT32_MAX - 64)
+        return fail(WB_ERR_UNSUPPORTED, "wb_cosx_k_grad: above 2^31 points");
+    const size_t need = wb_cosx_k_grad_workspace_bytes(h, npts, natm);
+    if (!workspace || workspace_bytes < need)
+        return fail(WB_ERR_WORKSPACE, "wb_cosx_k_grad: workspace needs " +
+                                          std::to_string(need) + " bytes");
+    int st = ensure_fp64(h);
+    if (st != WB_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int nao = h->hp.nao;
+    const size_t n = (size_t)nao * ld;
+    // the FP64 form's layout, then the AO values and their x, y, z
+    // gradients (4, nao, ld), the per-block gradient rows and the AO sums
+    const WsLayout64 L = ws_layout_fp64(h, ld);
+    char* base = static_cast<char*>(workspace);
+    double* Xd = reinterpret_cast<double*>(base + L.total);     // (4, nao, ld)
+    double* gbuf = reinterpret_cast<double*>(base + align256(L.total + sizeof(double) * 4 * n));
+    const int nblk = (int)(ld / 32);
+    double* aodot = reinterpret_cast<double*>(
+        reinterpret_cast<char*>(gbuf) + align256(sizeof(double) * (size_t)nblk * natm * 3));
+    double* F64 = at<double>(workspace, L.F64);
+    float* F32 = at<float>(workspace, L.F32);
+    double* G64 = at<double>(workspace, L.G64);
+    double* H = at<double>(workspace, L.WG);
+    WB_CUBLAS(cublasSetStream(h->cublas, s));
+    WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+    const double one = 1.0, zero = 0.0;
+    wb::AoArgs ao;
+    ao.coords = coords; ao.npts = npts; ao.ld = ld; ao.nbas = h->nbas;
+    ao.sh_l = h->sh_l; ao.sh_np = h->sh_np; ao.sh_nc = h->sh_nc;
+    ao.sh_eoff = h->sh_eoff; ao.sh_coff = h->sh_coff; ao.sh_ao0 = h->sh_ao0;
+    ao.sh_ctr = h->sh_ctr; ao.exps = h->exps; ao.coeffs = h->coeffs; ao.X = Xd;
+    ao.nao = nao;
+    WB_CUDA(wb::launch_ao_eval_d1(ao, s));
+    // F = X D (FP64); fl32(F) feeds the screen's block statistics only
+    WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)ld, nao, nao, &one,
+                          Xd, (int)ld, dm, nao, &zero, F64, (int)ld));
+    WB_CUDA(wb::launch_f64_to_f32(F64, F32, (int64_t)n, s));
+    wb::BlockStatsOut bo;
+    for (int b = 0; b < 3; ++b) {
+        bo.cr[b] = at<float4>(workspace, L.base.subcr[b]);
+        bo.msh[b] = at<float>(workspace, L.base.msh[b]);
+    }
+    WB_CUDA(wb::launch_sub_stats(coords, weights, F32, npts, ld, h->hp.nvshell,
+                                 h->vs_ao0, h->vs_nf, bo, s));
+    const float tol = tile_tol > 0.0 ? std::max((float)(tile_tol / 1.001), 1e-38f) : 0.0f;
+    int* work = at<int>(workspace, L.base.work);
+    // G = A F by the FP64 class kernels
+    wb::CosxF64Args a;
+    std::memset(&a, 0, sizeof(a));
+    a.F = F64; a.G = G64; a.coords = coords; a.ld = ld; a.npts = (int)npts;
+    a.omega = omega; a.khdr = h->khdr; a.pshell = h->pshell; a.ptau = h->ptau;
+    a.bnd = h->bnd; a.bpref = h->bpref; a.blk_cr = bo.cr[0]; a.blk_msh = bo.msh[0];
+    a.nblk = nblk; a.nvshell = h->hp.nvshell; a.tol = tol;
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        a.pp_begin[c] = h->hp.cls[c].pp_begin;
+        a.e_base[c] = h->f64_ebase[c];
+    }
+    a.P = h->f64_P; a.p = h->p; a.pref = h->pref; a.E = h->f64_E; a.boys = h->f64_boys;
+    a.c2s = h->f64_boys + (size_t)wb::kBoys64Nodes * wb::kBoys64Cols;
+    a.pflops = h->pflops; a.pnint = h->pnint;
+    a.counters = at<unsigned long long>(workspace, L.base.counters);
+    a.work = work;
+    WB_CUDA(cudaMemsetAsync(a.counters, 0, sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+    WB_CUDA(cudaMemsetAsync(G64, 0, sizeof(double) * n, s));
+    WB_CUDA(cudaMemsetAsync(work, 0, sizeof(int) * wb::NCLASS, s));
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        const int pb = h->hp.cls[c].pair_begin, pe = h->hp.cls[c].pair_end;
+        if (pe > pb) WB_CUDA(wb::launch_cosx_fp64_class(c, a, pb, pe, h->nsm, s));
+    }
+    // X side: 1/2 sum_g w_g sum_{mu on C} grad X_g,mu (G D)_g,mu
+    WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)ld, nao, nao, &one,
+                          G64, (int)ld, dm, nao, &zero, H, (int)ld));
+    WB_CUDA(cudaMemsetAsync(grad_out, 0, sizeof(double) * 3 * (size_t)natm, s));
+    WB_CUDA(wb::launch_ao_dot(Xd, H, weights, npts, ld, nao, aodot, s));
+    WB_CUDA(wb::launch_atom_sum(aodot, h->vs_ao0, h->vs_nf, h->vs_atom, h->hp.nvshell,
+                                natm, 0.5, grad_out, s));
+    // integral side
+    wb::CosxGradArgs g;
+    std::memset(&g, 0, sizeof(g));
+    g.F = F64; g.coords = coords; g.weights = weights; g.ld = ld; g.npts = (int)npts;
+    g.omega = omega; g.khdr = h->khdr; g.pshell = h->pshell; g.ptau = h->ptau;
+    g.bnd = h->bnd; g.bpref = h->bpref; g.blk_cr = bo.cr[0]; g.blk_msh = bo.msh[0];
+    g.nblk = nblk; g.nvshell = h->hp.nvshell; g.tol = tol;
+    for (int c = 0; c < wb::NCLASS; ++c) g.pp_begin[c] = h->hp.cls[c].pp_begin;
+    g.P = h->f64_P; g.p = h->p; g.pref = h->pref; g.alpha = h->f64_alpha;
+    g.vs_xyz = h->f64_vsxyz; g.vs_atom = h->vs_atom; g.boys = h->f64_boys;
+    g.c2s = a.c2s; g.gbuf = gbuf; g.natm = natm; g.work = work;
+    WB_CUDA(cudaMemsetAsync(gbuf, 0, sizeof(double) * (size_t)nblk * natm * 3, s));
+    WB_CUDA(cudaMemsetAsync(work, 0, sizeof(int) * wb::NCLASS, s));
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        const int pb = h->hp.cls[c].pair_begin, pe = h->hp.cls[c].pair_end;
+        if (pe > pb) WB_CUDA(wb::launch_cosx_grad64_class(c, g, pb, pe, h->nsm, s));
+    }
+    WB_CUDA(wb::launch_grad_rows_sum(gbuf, nblk, natm, grad_out, s));
     return WB_OK;
 }
 

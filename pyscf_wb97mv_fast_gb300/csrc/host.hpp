@@ -102,6 +102,7 @@ int build_pairs(const wb_basis& b, const double origin[3], double cutoff,
 int e64_axis(int la, int lb);        // sum_{i <= la, j <= lb} (i + j + 1)
 struct HostPairs64 {
     std::vector<double> P;
+    std::vector<double> alpha;       // bra (shell A) exponent per primitive pair
     std::vector<double> E;
     int64_t e_base[NCLASS] = {0};    // double offset of each class's E block
 };

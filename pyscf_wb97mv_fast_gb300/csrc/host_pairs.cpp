@@ -232,6 +232,7 @@ void build_pairs64(const HostPairs& hp, HostPairs64& out) {
                 e64_axis(lofc[c][0], lofc[c][1]);
     }
     out.P.resize(3 * (size_t)hp.npp);
+    out.alpha.resize((size_t)hp.npp);
     out.E.resize((size_t)base);
     // primitive pairs follow the pair order, bra primitive outer (as in
     // build_pairs), so pair k's first one is hdr[4k + 2]
@@ -243,6 +244,7 @@ void build_pairs64(const HostPairs& hp, HostPairs64& out) {
         for (int a = 0; a < A.nprim; ++a)
             for (int bb = 0; bb < B.nprim; ++bb, ++pp) {
                 const double al = A.exps[a], be = B.exps[bb], p = al + be;
+                out.alpha[(size_t)pp] = al;
                 double* e = out.E.data() + out.e_base[c] +
                             (int64_t)(pp - hp.cls[c].pp_begin) * 3 * nax;
                 for (int x = 0; x < 3; ++x) {
