@@ -59,6 +59,9 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // largest dynamic shared memory per CTA for staged primitive-pair records
 constexpr size_t kStageMaxBytes = 96 * 1024;
 constexpr size_t kCublasWorkspace = 32u << 20;    // bytes per handle
+// per-class counters (kept, flops, ints) and one status word (a record
+// staging wait of a class kernel that gave up)
+constexpr int kCounterWords = 3 * wb::NCLASS + 1;
 // default staged classes: (0,0) (1,0) (1,1) (2,1)
 constexpr long long kStageClasses = 0x1110100000LL;
 // default classes with a dual-omega kernel: (0,0) (1,0) (2,0) (2,1)
@@ -201,7 +204,7 @@ WsLayout ws_layout(const wb_cosx* h, int64_t ldt, bool full) {
         return o;
     };
     const int nao = h->hp.nao;
-    L.counters = take(sizeof(unsigned long long) * 3 * wb::NCLASS);
+    L.counters = take(sizeof(unsigned long long) * kCounterWords);
     L.work = take(sizeof(int) * 2 * wb::NCLASS);     // per class, per omega slot
     L.om = take(sizeof(float) * wb::OMEGA_REC * (size_t)std::max(h->hp.npp, 1));
     L.rec = take(sizeof(float4) * (size_t)std::max<int64_t>(h->hp.nrec, 1));
@@ -287,6 +290,7 @@ wb::CosxArgs make_args(const wb_cosx* h, void* ws, const WsLayout& L,
     a.pflops = h->pflops;
     a.pnint = h->pnint;
     a.counters = at<unsigned long long>(ws, L.counters);
+    a.status = a.counters + 3 * wb::NCLASS;
     a.work = at<int>(ws, L.work);
     for (int c = 0; c < wb::NCLASS; ++c) {
         a.cls_pb[c] = h->hp.cls[c].pair_begin;
@@ -547,10 +551,12 @@ int run_g_classes_dual(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
 int read_stats(wb_cosx* h, void* ws, const WsLayout& L, int64_t ntasks_total,
                cudaStream_t s, wb_cosx_stats* stats, int launches) {
     if (!stats) return WB_OK;
-    unsigned long long c[3 * wb::NCLASS];
+    unsigned long long c[kCounterWords];
     WB_CUDA(cudaMemcpyAsync(c, at<unsigned long long>(ws, L.counters),
                             sizeof(c), cudaMemcpyDeviceToHost, s));
     WB_CUDA(cudaStreamSynchronize(s));
+    if (c[3 * wb::NCLASS])
+        return fail(WB_ERR_CUDA, "a class kernel's record staging timed out");
     std::memset(stats, 0, sizeof(*stats));
     stats->tasks_total = ntasks_total;
     for (int k = 0; k < wb::NCLASS; ++k) {
@@ -637,7 +643,7 @@ WsLayout64 ws_layout_fp64(const wb_cosx* h, int64_t ld) {
         off = align256(off + bytes);
         return o;
     };
-    L.base.counters = take(sizeof(unsigned long long) * 3 * wb::NCLASS);
+    L.base.counters = take(sizeof(unsigned long long) * kCounterWords);
     L.base.work = take(sizeof(int) * 2 * wb::NCLASS);
     for (int b = 0; b < 3; ++b) {
         const int64_t bp = 32 << b;
@@ -1041,7 +1047,7 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
         WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
     }
     WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.counters), 0,
-                            sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+                            sizeof(unsigned long long) * kCounterWords, s));
     int launches = 1;
     if (npts == 0) {
         WB_CUDA(cudaMemsetAsync(k_out, 0, sizeof(double) * kk * nomega, s));
@@ -1259,7 +1265,7 @@ int wb_cosx_get_k_fp64(wb_cosx* h, const double* coords, const double* weights,
     const int nao = h->hp.nao;
     const size_t kk = (size_t)nao * nao;
     WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.base.counters), 0,
-                            sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+                            sizeof(unsigned long long) * kCounterWords, s));
     int launches = 1;
     if (npts == 0) {
         WB_CUDA(cudaMemsetAsync(k_out, 0, sizeof(double) * kk * nomega, s));
@@ -1569,7 +1575,7 @@ int wb_cosx_batch_run(wb_cosx_batch* b, const double* const* qd,
         WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
         if (stats)
             WB_CUDA(cudaMemsetAsync(at<void>(ws, L.counters), 0,
-                                    sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+                                    sizeof(unsigned long long) * kCounterWords, s));
         const double* X = at<double>(ws, L.X);
         float* F32 = at<float>(ws, L.F32);
         if (b->gemm == WB_K_GEMM_OZAKI_BF16 && wb::ozaki_f_supported(nao)) {
@@ -1770,7 +1776,7 @@ int wb_cosx_k_grad(wb_cosx* h, const double* coords, const double* weights,
     a.pflops = h->pflops; a.pnint = h->pnint;
     a.counters = at<unsigned long long>(workspace, L.base.counters);
     a.work = work;
-    WB_CUDA(cudaMemsetAsync(a.counters, 0, sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+    WB_CUDA(cudaMemsetAsync(a.counters, 0, sizeof(unsigned long long) * kCounterWords, s));
     WB_CUDA(cudaMemsetAsync(G64, 0, sizeof(double) * n, s));
     WB_CUDA(cudaMemsetAsync(work, 0, sizeof(int) * wb::NCLASS, s));
     for (int c = 0; c < wb::NCLASS; ++c) {
@@ -1820,7 +1826,7 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
         return fail(WB_ERR_WORKSPACE, "wb_cosx_g: workspace needs " +
                                           std::to_string(L.total) + " bytes");
     WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.counters), 0,
-                            sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+                            sizeof(unsigned long long) * kCounterWords, s));
     {
         const int st = prepare_omega(h, omega, workspace, L, s);
         if (st != WB_OK) return st;
@@ -1855,7 +1861,7 @@ int wb_cosx_g_multi(wb_cosx* h, const double* coords, const double* weights,
         return fail(WB_ERR_WORKSPACE, "wb_cosx_g_multi: workspace needs " +
                                           std::to_string(L.total) + " bytes");
     WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.counters), 0,
-                            sizeof(unsigned long long) * 3 * wb::NCLASS, s));
+                            sizeof(unsigned long long) * kCounterWords, s));
     int launches = 1;
     int st = tile_prep(h, coords, weights, npts, ldt, f, workspace, L, s, &launches);
     if (st != WB_OK) return st;

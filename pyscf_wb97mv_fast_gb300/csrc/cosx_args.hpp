@@ -66,6 +66,7 @@ struct CosxArgs {
     // the class pair ranges (the batched kernels read them from here)
     int cls_pb[kClasses];
     int cls_pe[kClasses];
+    unsigned long long* status;    // nonzero: a record staging wait gave up
 };
 
 }  // namespace wb

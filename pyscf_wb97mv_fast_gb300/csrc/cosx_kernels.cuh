@@ -89,8 +89,16 @@ __device__ __forceinline__ void load_f(const float* __restrict__ Fp,
     for (int nu = 0; nu < N; ++nu) f[nu] = Fp[(long long)(n0 + nu) * ld];
 }
 
-// per-lane asynchronous 16-byte global -> shared copies (cp.async; the
-// wait is the hardware's, no polling): lanes split the n float4
+// Record staging of one warp: two shared-memory buffers.  Lane form (the
+// default): per-lane asynchronous 16-byte global -> shared copies
+// (cp.async; the wait is the hardware's, no polling), lanes split the n
+// float4.  TMA form (-DWB_COSX_TMA=1, two-omega kernels only): each buffer
+// is filled with one TMA bulk copy (cp.async.bulk, global -> shared) that
+// completes on the buffer's own mbarrier (expect_tx by lane 0, every lane
+// waits on the phase parity).  Measured on the water27 bench step, the TMA
+// form made the G phase 2-3 % slower (73.6 vs 71.5 ms): a task's records
+// are a few hundred bytes, below the size where one bulk copy beats 32
+// lanes' 16-byte copies, and the bounded wait loop adds instructions.
 __device__ __forceinline__ void stage_records(float4* dst,
                                               const float4* __restrict__ src,
                                               const int n, const int lane) {
@@ -105,6 +113,90 @@ __device__ __forceinline__ void stage_wait() {
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncwarp();
 }
+
+#ifndef WB_COSX_TMA
+#define WB_COSX_TMA 0
+#endif
+#if WB_COSX_TMA
+// A wait gives up after kStageSpins polls: it sets *status, and the warp
+// stops waiting (its results are then wrong and the host reports the
+// failure), so a lost completion cannot hang the kernel.
+constexpr int kStageSpins = 1 << 16;
+
+// the two mbarriers of each warp of a CTA (8 B each)
+__shared__ unsigned long long g_stage_mbar[kCtaThreads / 32][2];
+
+// bits 0, 1: the phase parity buffer 0 / 1 completes next; bit 2: a wait
+// gave up
+struct RecStager {
+    unsigned state;
+};
+
+__device__ __forceinline__ unsigned stage_bar(const int b) {
+    return (unsigned)__cvta_generic_to_shared(&g_stage_mbar[threadIdx.x >> 5][b]);
+}
+
+// lane 0 of each warp initialises its two mbarriers (count 1); the CTA's
+// __syncthreads after the Boys table load publishes them
+__device__ __forceinline__ RecStager stager_init(const int lane) {
+    RecStager st;
+    st.state = 0u;
+    if (lane == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n"
+                     :: "r"(stage_bar(0)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n"
+                     :: "r"(stage_bar(1)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    return st;
+}
+
+// n float4 from src (16-byte aligned) into dst = buffer b, one bulk copy
+__device__ __forceinline__ void tma_stage_records(const int b, float4* dst,
+                                                  const float4* __restrict__ src,
+                                                  const int n, const int lane) {
+    if (lane == 0) {
+        const unsigned bar = stage_bar(b);
+        const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+        const unsigned bytes = 16u * (unsigned)n;
+        // the warp's earlier reads of this buffer (ordered by the caller's
+        // __syncwarp) come before the async-proxy write
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("{\n\t.reg .b64 st;\n\t"
+                     "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}\n"
+                     :: "r"(bar), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes"
+                     " [%0], [%1], %2, [%3];\n"
+                     :: "r"(d), "l"(src), "r"(bytes), "r"(bar) : "memory");
+    }
+}
+
+// wait until buffer b's copy has landed
+__device__ __forceinline__ void tma_stage_wait(RecStager& st, const int b,
+                                               unsigned long long* status) {
+    if (!(st.state & 4u)) {
+        const unsigned bar = stage_bar(b);
+        const unsigned par = (st.state >> b) & 1u;
+        unsigned done = 0;
+        for (int i = 0; i < kStageSpins && !done; ++i)
+            asm volatile("{\n\t.reg .pred p;\n\t"
+                         "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                         "selp.u32 %0, 1, 0, p;\n\t}\n"
+                         : "=r"(done) : "r"(bar), "r"(par) : "memory");
+        if (!done) {
+            st.state |= 4u;
+            if (status) atomicOr(status, 1ull);
+        }
+    }
+    st.state ^= 1u << b;
+    __syncwarp();
+}
+#define WB_STAGER_PARAM , RecStager& stg
+#define WB_STAGER_ARG , stg
+#else
+#define WB_STAGER_PARAM
+#define WB_STAGER_ARG
+#endif
 
 __device__ __forceinline__ int lo16(const int x) { return x & 0xffff; }
 __device__ __forceinline__ int hi16(const int x) {
@@ -144,13 +236,14 @@ template<int LA, int LB, int NW = 1> struct ClassPts {
 // (screen, tasks, G) for the points of block blk.  A is the argument block
 // of the block's molecule; wstage / rmax the warp's record buffers (two of
 // rmax float4) and sbuf the one in use; kept / flops / ints accumulate the
-// counters of the warp.
+// counters of the warp (with the TMA form, stg holds the buffers' copy
+// state).
 template<int LA, int LB, bool FAR, bool STAGE, int NW>
 __device__ __forceinline__ void cosx_class_block(
     const CosxArgs& A, const int pair_begin, const int pair_end, const int blk,
     const float4* __restrict__ stab, float4* wstage, const int rmax, int& sbuf,
     unsigned long long& kept, unsigned long long& flops,
-    unsigned long long& ints) {
+    unsigned long long& ints WB_STAGER_PARAM) {
     constexpr int CLS = LA * (LA + 1) / 2 + LB;
     constexpr int NCA = (LA + 1) * (LA + 2) / 2;
     constexpr int NA = 2 * LA + 1;
@@ -256,9 +349,19 @@ __device__ __forceinline__ void cosx_class_block(
         CosxRec<LA, LB> rec;
         if constexpr (STAGE) {
             __syncwarp();       // the previous chunk's reads of the buffer
-            stage_records(wstage + sbuf * rmax, recc + (long long)hdr.z * RS,
-                          (hdr.w & 0xffff) * RS, lane);
-            stage_wait();
+#if WB_COSX_TMA
+            if constexpr (NW == 2) {
+                tma_stage_records(sbuf, wstage + sbuf * rmax,
+                                  recc + (long long)hdr.z * RS, (hdr.w & 0xffff) * RS,
+                                  lane);
+                tma_stage_wait(stg, sbuf, A.status);
+            } else
+#endif
+            {
+                stage_records(wstage + sbuf * rmax, recc + (long long)hdr.z * RS,
+                              (hdr.w & 0xffff) * RS, lane);
+                stage_wait();
+            }
         } else {
             cosx_rec_load<FAR>(A, hdr.z, rec);
         }
@@ -302,10 +405,18 @@ __device__ __forceinline__ void cosx_class_block(
                 }
                 // the next task's records into the other buffer (the
                 // last reads of it ended before the previous wait)
-                if constexpr (STAGE)
-                    stage_records(wstage + (sbuf ^ 1) * rmax,
-                                  recc + (long long)hn.z * RS,
-                                  (hn.w & 0xffff) * RS, lane);
+                if constexpr (STAGE) {
+#if WB_COSX_TMA
+                    if constexpr (NW == 2)
+                        tma_stage_records(sbuf ^ 1, wstage + (sbuf ^ 1) * rmax,
+                                          recc + (long long)hn.z * RS,
+                                          (hn.w & 0xffff) * RS, lane);
+                    else
+#endif
+                        stage_records(wstage + (sbuf ^ 1) * rmax,
+                                      recc + (long long)hn.z * RS,
+                                      (hn.w & 0xffff) * RS, lane);
+                }
             }
             const int gb0 = hi16(hdr.y), pp0 = hdr.z, npp = hdr.w & 0xffff;
             const int nxt = more ? hn.z : pp0;
@@ -358,7 +469,12 @@ __device__ __forceinline__ void cosx_class_block(
             kept += nsb * NW;
             if (!more) break;
             if constexpr (STAGE) {
-                stage_wait();
+#if WB_COSX_TMA
+                if constexpr (NW == 2)
+                    tma_stage_wait(stg, sbuf ^ 1, A.status);
+                else
+#endif
+                    stage_wait();
                 sbuf ^= 1;
             }
             hdr = hn;
@@ -391,6 +507,9 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
     constexpr int CLS = LA * (LA + 1) / 2 + LB;
     constexpr int PTS = ClassPts<LA, LB, NW>::value;
     __shared__ float4 stab[kBoysFloat4];
+#if WB_COSX_TMA
+    RecStager stg = stager_init(threadIdx.x & 31);
+#endif
     for (int i = threadIdx.x; i < kBoysFloat4; i += blockDim.x)
         stab[i] = A.boys[i];
     __syncthreads();
@@ -417,7 +536,7 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
         }
         cosx_class_block<LA, LB, FAR, STAGE, NW>(A, pair_begin, pair_end, blk, stab,
                                                  wstage, rmax, sbuf, kept, flops,
-                                                 ints);
+                                                 ints WB_STAGER_ARG);
     }
     // lane 0 counted the tasks (every lane runs every task) in units of the
     // 32-point sub-blocks they cover; every lane counted the flops /
@@ -455,11 +574,14 @@ cosx_class_kernel_batch(const CosxArgs* __restrict__ args,
     static_assert(sizeof(CosxArgs) % 4 == 0, "argument block copied as words");
     __shared__ float4 stab[kBoysFloat4];
     __shared__ CosxArgs sA[NWARP];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+#if WB_COSX_TMA
+    RecStager stg = stager_init(lane);
+#endif
     const float4* __restrict__ boys = args[0].boys;
     for (int i = threadIdx.x; i < kBoysFloat4; i += blockDim.x) stab[i] = boys[i];
     __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
     extern __shared__ float4 s_stage[];
     float4* wstage = s_stage + warp * 2 * rmax;
     int sbuf = 0;
@@ -508,7 +630,8 @@ cosx_class_kernel_batch(const CosxArgs* __restrict__ args,
         const CosxArgs& Am = sA[warp];
         cosx_class_block<LA, LB, FAR, STAGE, NW>(Am, Am.cls_pb[CLS], Am.cls_pe[CLS],
                                                  item - item_off[m], stab, wstage,
-                                                 rmax, sbuf, kept, flops, ints);
+                                                 rmax, sbuf, kept, flops,
+                                                 ints WB_STAGER_ARG);
     }
     if (cur >= 0) flush();
 }
