@@ -143,25 +143,33 @@ def measured_peaks():
     return None
 
 
+FP32_PROBES = {}
+
+
 def fp32_peak(torch):
-    """FP32 FMA throughput of this GPU (TFLOP/s), best of 5 probe launches."""
+    """FP32 FMA throughput of this GPU (TFLOP/s): best of 5 launches of the
+    scalar-FMA probe and of the packed-FMA (fma.rn.f32x2) probe, the larger
+    of the two (both kept in FP32_PROBES)."""
     from pyscf_wb97mv_fast_gb300 import _native
     lib = _native.lib()
     nsm = torch.cuda.get_device_properties(0).multi_processor_count
     out = torch.empty(nsm * 2048, dtype=torch.float32, device='cuda')
     flops = _native.ctypes.c_double()
     stream = _native.ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    best = 0.0
-    for it in range(7):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        _native.check(lib.wb_fp32_fma_probe(20000, _native.ptr(out), out.numel(),
-                                            stream, _native.ctypes.byref(flops)))
-        e1.record()
-        e1.synchronize()
-        if it >= 2:
-            best = max(best, flops.value / (e0.elapsed_time(e1) * 1e-3) / 1e12)
-    return best
+    for name, fn in (('ffma', lib.wb_fp32_fma_probe), ('ffma2', lib.wb_fp32x2_fma_probe)):
+        best = 0.0
+        for it in range(7):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _native.check(fn(20000, _native.ptr(out), out.numel(), stream,
+                             _native.ctypes.byref(flops)))
+            e1.record()
+            e1.synchronize()
+            if it >= 2:
+                best = max(best, flops.value / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+        FP32_PROBES[name] = best
+    return max(FP32_PROBES.values())
 
 
 def traffic_from_profile():
@@ -839,8 +847,10 @@ def main():
                 'unit': 'TFLOP/s', 'frac': achieved / peak if peak else None,
                 'traffic': prof.get('bytes_per_g_phase') if prof else None,
                 'traffic_source': prof.get('source') if prof else None,
-                'peak_source': 'measured in this run: wb_fp32_fma_probe '
-                               '(FFMA-only kernel, all SMs)',
+                'peak_source': 'measured in this run: the larger of '
+                               'wb_fp32_fma_probe (scalar FMAs) and '
+                               'wb_fp32x2_fma_probe (packed f32x2 FMAs), all SMs',
+                'fp32_probes_tflops': dict(FP32_PROBES),
                 'kernel': 'block statistics + fused screen + G class kernels '
                           '+ class-buffer sums of both omegas in one call '
                           '(wb_cosx_g_multi, %d launches)' % g_launches,

@@ -375,6 +375,11 @@ int wb_becke_partition(const double* points, int64_t n, const int* owner,
  * (the reference reports no roofline). */
 int wb_fp32_fma_probe(int64_t iters, float* out, int64_t out_len,
                       void* stream, double* flops);
+/* The same with packed FMAs (fma.rn.f32x2, two FP32 FMAs per instruction,
+ * sm_100+): *flops counts both halves.  The FP32 peak of a roofline is the
+ * larger of the two probes. */
+int wb_fp32x2_fma_probe(int64_t iters, float* out, int64_t out_len, void* stream,
+                        double* flops);
 
 const char* wb_status_string(int status);
 const char* wb_last_error(void);

@@ -43,7 +43,7 @@ EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_int3c1e_dense',
             'wb_boys_fp32', 'wb_boys_f64_host', 'wb_model_flops_per_point',
             'wb_vv10_kernel_sum',
-            'wb_becke_partition', 'wb_fp32_fma_probe',
+            'wb_becke_partition', 'wb_fp32_fma_probe', 'wb_fp32x2_fma_probe',
             'wb_ozaki_workspace_bytes', 'wb_cosx_ozaki_f', 'wb_cosx_ozaki_k',
             'wb_vv10_kernel_sum_noalloc',
             'wb_cosx_fp64_workspace_bytes', 'wb_cosx_get_k_fp64',
@@ -153,6 +153,7 @@ def _declare(lib):
         'wb_vv10_kernel_sum_noalloc': (_INT, [_P, _P, _P, _P, _I64, _D, _P, _P,
                                               _P, _P, ctypes.POINTER(_I64)]),
         'wb_fp32_fma_probe': (_INT, [_I64, _P, _I64, _P, ctypes.POINTER(_D)]),
+        'wb_fp32x2_fma_probe': (_INT, [_I64, _P, _I64, _P, ctypes.POINTER(_D)]),
         'wb_ozaki_workspace_bytes': (ctypes.c_size_t, [_INT, _I64]),
         'wb_cosx_ozaki_f': (_INT, [_P, _P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
         'wb_cosx_ozaki_k': (_INT, [_P, _P, _P, _P, _I64, _INT, _P, _P,

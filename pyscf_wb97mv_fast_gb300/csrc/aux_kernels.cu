@@ -947,9 +947,40 @@ __global__ void fma_probe_kernel(int64_t iters, float* __restrict__ out) {
         a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
+// the same with packed FMAs (fma.rn.f32x2: two FP32 FMAs per instruction)
+__global__ void fma2_probe_kernel(int64_t iters, float* __restrict__ out) {
+    unsigned long long a[8];
+    const float b0 = threadIdx.x * 1e-7f;
+    for (int k = 0; k < 8; ++k) {
+        const float lo = b0 + 2 * k * 1e-7f, hi = lo + 1e-7f;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(a[k]) : "f"(lo), "f"(hi));
+    }
+    unsigned long long m, c;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(m) : "f"(0.999999f));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(c) : "f"(1e-7f));
+    for (int64_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                asm volatile("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(a[r]) : "l"(m), "l"(c));
+        }
+    }
+    float s = 0.0f;
+    for (int k = 0; k < 8; ++k) {
+        float lo, hi;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a[k]));
+        s += lo + hi;
+    }
+    out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 cudaError_t launch_fma_probe(int64_t iters, int blocks, int threads,
-                             float* out, cudaStream_t s) {
-    fma_probe_kernel<<<blocks, threads, 0, s>>>(iters, out);
+                             float* out, cudaStream_t s, bool packed) {
+    if (packed)
+        fma2_probe_kernel<<<blocks, threads, 0, s>>>(iters, out);
+    else
+        fma_probe_kernel<<<blocks, threads, 0, s>>>(iters, out);
     return cudaGetLastError();
 }
 

@@ -2080,4 +2080,19 @@ int wb_fp32_fma_probe(int64_t iters, float* out, int64_t out_len,
     return WB_OK;
 }
 
+int wb_fp32x2_fma_probe(int64_t iters, float* out, int64_t out_len, void* stream,
+                        double* flops) {
+    int dev = 0, nsm = 1;
+    WB_CUDA(cudaGetDevice(&dev));
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = 256, blocks = nsm * 8;
+    if (!out || out_len < (int64_t)threads * blocks || iters <= 0)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_fp32x2_fma_probe: out needs "
+                    + std::to_string((int64_t)threads * blocks) + " floats");
+    WB_CUDA(wb::launch_fma_probe(iters, blocks, threads, out,
+                                 static_cast<cudaStream_t>(stream), true));
+    if (flops) *flops = 2.0 * 2.0 * 8.0 * 16.0 * (double)iters * threads * blocks;
+    return WB_OK;
+}
+
 }  // extern "C"

@@ -114,8 +114,9 @@ cudaError_t launch_boys(const float* t, int64_t n, int nmax,
                         const float4* tab, float* out, cudaStream_t s);
 // VV10 double sum; ws must hold vv10_workspace_bytes(n) bytes
 size_t vv10_workspace_bytes(int64_t n);
+// packed: fma.rn.f32x2 (two FP32 FMAs per instruction) instead of fmaf
 cudaError_t launch_fma_probe(int64_t iters, int blocks, int threads,
-                             float* out, cudaStream_t s);
+                             float* out, cudaStream_t s, bool packed = false);
 cudaError_t launch_vv10(const float* xyz, const float* q, const float* w0,
                         const float* kap, int64_t n, double tile_tol,
                         double* F, double* U, double* W, void* ws,
