@@ -114,3 +114,30 @@ def test_fp64_empty_grid_and_bad_arguments():
     assert torch.count_nonzero(K).item() == 0
     with pytest.raises(_native.NativeError):
         eng.get_k_fp64(c, w, qd, (-1.0,))
+
+
+def test_mixed_path_against_fp64_form_water27():
+    """The bench molecule at full size (27 waters, synthetic def2-SVP, 648
+    AOs, level-1 grid): the mixed-precision multi-omega build against the
+    plain FP64 form on the same screen setting.  Gates: max|dK| < 1e-6
+    max|K| and |1/4 tr(D dK)| below the reference's water27 floor of an
+    FP32 full-K build (3e-6; README.md known issue 1)."""
+    import torch
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    from pyscf_wb97mv_fast_gb300.systems import water_cluster
+    mol = Molecule.build(water_cluster(27, box=10.0, seed=27), 'synthetic-svp')
+    g = build_grids(mol, level=1)
+    dm = local_density(mol, seed=27)
+    eng = CosxEngine(mol)
+    c = eng.relative(g.coords)
+    w = torch.as_tensor(g.weights, device=eng.device)
+    qd = torch.as_tensor(dm, device=eng.device)
+    Km = eng.get_k_multi(c, w, qd, (0.0, 0.3), tile_tol=1e-11)
+    Km = ((Km + Km.transpose(1, 2)) * 0.5).cpu().numpy()
+    K64, _ = _k64(mol, g.coords, g.weights, dm, (0.0, 0.3), tile_tol=1e-11, eng=eng)
+    for j in range(2):
+        scale = np.abs(K64[j]).max()
+        assert np.max(np.abs(Km[j] - K64[j])) < 1e-6 * scale
+        assert abs(0.25 * np.einsum('ij,ji->', dm, Km[j] - K64[j])) < 3e-6
