@@ -340,6 +340,19 @@ int wb_vv10_kernel_sum(const float* xyz, const float* q, const float* w0,
                        double* f_out, double* u_out, double* w_out,
                        void* stream, int64_t* pairs_kept);
 
+/* wb_vv10_kernel_sum for several molecules in one launch: the points of
+ * molecule m are offsets[m] .. offsets[m + 1] - 1 of the concatenated
+ * arrays (offsets: nmol + 1 host int64, offsets[0] = 0), and each point's
+ * double sum runs over its own molecule's points only.  Every molecule's
+ * F, U, W are bitwise what wb_vv10_kernel_sum returns for it alone.
+ * *pairs_kept sums over the molecules.  Synchronises `stream` before it
+ * returns (the host tile tables are copied).  The reference sums one
+ * molecule per call (Vv10Kernel.kernel_sum, gpu/vv10.py:167-240). */
+int wb_vv10_kernel_sum_batch(int nmol, const int64_t* offsets, const float* xyz,
+                             const float* q, const float* w0, const float* kappa,
+                             double tile_tol, double* f_out, double* u_out,
+                             double* w_out, void* stream, int64_t* pairs_kept);
+
 /* Allocation-free VV10 double sum: the same computation and results as
  * wb_vv10_kernel_sum, for callers that cannot let the library allocate
  * device memory (e.g. a host framework that reserves the whole GPU memory

@@ -2065,6 +2065,84 @@ int wb_vv10_kernel_sum(const float* xyz, const float* q, const float* w0,
     return WB_OK;
 }
 
+int wb_vv10_kernel_sum_batch(int nmol, const int64_t* offsets, const float* xyz,
+                             const float* q, const float* w0, const float* kappa,
+                             double tile_tol, double* f_out, double* u_out,
+                             double* w_out, void* stream, int64_t* pairs_kept) {
+    if (nmol < 1 || !offsets || !(tile_tol >= 0.0) || offsets[0] != 0)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_vv10_kernel_sum_batch: bad arguments");
+    for (int m = 0; m < nmol; ++m)
+        if (offsets[m + 1] < offsets[m])
+            return fail(WB_ERR_INVALID_ARGUMENT,
+                        "wb_vv10_kernel_sum_batch: offsets must not decrease");
+    const int64_t n = offsets[nmol];
+    if (n && (!xyz || !q || !w0 || !kappa || !f_out || !u_out || !w_out))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_vv10_kernel_sum_batch: null pointer");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // tiles of 256 points inside each molecule
+    std::vector<long long> tstart;
+    std::vector<int> tlen, tmol, mtile(nmol + 1, 0);
+    for (int m = 0; m < nmol; ++m) {
+        mtile[m] = (int)tstart.size();
+        for (int64_t i = offsets[m]; i < offsets[m + 1]; i += 256) {
+            tstart.push_back(i);
+            tlen.push_back((int)std::min<int64_t>(256, offsets[m + 1] - i));
+            tmol.push_back(m);
+        }
+    }
+    const int64_t nt = (int64_t)tstart.size();
+    mtile[nmol] = (int)nt;
+    if (nt > INT32_MAX / 2)
+        return fail(WB_ERR_UNSUPPORTED, "wb_vv10_kernel_sum_batch: too many tiles");
+    if (nt == 0) {
+        if (pairs_kept) *pairs_kept = 0;
+        return WB_OK;
+    }
+    const size_t b_start = align256(sizeof(long long) * nt);
+    const size_t b_len = align256(sizeof(int) * nt);
+    const size_t b_mol = align256(sizeof(int) * nt);
+    const size_t b_mt = align256(sizeof(int) * (nmol + 1));
+    const size_t b_st = align256(wb::vv10_tile_stats_bytes(nt));
+    char* ws = nullptr;
+    WB_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&ws),
+                            256 + b_start + b_len + b_mol + b_mt + b_st, s));
+    unsigned long long* kept = reinterpret_cast<unsigned long long*>(ws);
+    wb::VvSeg sg;
+    char* p = ws + 256;
+    sg.tstart = reinterpret_cast<const long long*>(p); p += b_start;
+    sg.tlen = reinterpret_cast<const int*>(p); p += b_len;
+    sg.tmol = reinterpret_cast<const int*>(p); p += b_mol;
+    sg.mtile = reinterpret_cast<const int*>(p); p += b_mt;
+    void* stats = p;
+    sg.ntiles = nt;
+    cudaError_t e = cudaMemsetAsync(kept, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(const_cast<long long*>(sg.tstart), tstart.data(),
+                            sizeof(long long) * nt, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(const_cast<int*>(sg.tlen), tlen.data(), sizeof(int) * nt,
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(const_cast<int*>(sg.tmol), tmol.data(), sizeof(int) * nt,
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(const_cast<int*>(sg.mtile), mtile.data(),
+                            sizeof(int) * (nmol + 1), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = wb::launch_vv10_seg(xyz, q, w0, kappa, sg, tile_tol, f_out, u_out, w_out,
+                                stats, kept, s);
+    unsigned long long kept_h = 0;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&kept_h, kept, sizeof(kept_h), cudaMemcpyDeviceToHost, s);
+    // the host tables must outlive the copies that read them
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaError_t e2 = cudaFreeAsync(ws, s);
+    if (e != cudaSuccess) return cuda_fail(e, "wb_vv10_kernel_sum_batch");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync");
+    if (pairs_kept) *pairs_kept = (int64_t)kept_h;
+    return WB_OK;
+}
+
 int wb_fp32_fma_probe(int64_t iters, float* out, int64_t out_len,
                       void* stream, double* flops) {
     int dev = 0, nsm = 1;

@@ -117,6 +117,20 @@ size_t vv10_workspace_bytes(int64_t n);
 // packed: fma.rn.f32x2 (two FP32 FMAs per instruction) instead of fmaf
 cudaError_t launch_fma_probe(int64_t iters, int blocks, int threads,
                              float* out, cudaStream_t s, bool packed = false);
+// batched VV10: tiles of several molecules (see vv10.cu); device arrays
+struct VvSeg {
+    const long long* tstart;    // first point of each tile
+    const int* tlen;            // points of each tile (1 .. 256)
+    const int* tmol;            // molecule of each tile
+    const int* mtile;           // nmol + 1: first tile of each molecule
+    long long ntiles;
+};
+size_t vv10_tile_stats_bytes(int64_t ntiles);
+// stats: vv10_tile_stats_bytes(ntiles) bytes; kept: a zeroed counter or null
+cudaError_t launch_vv10_seg(const float* xyz, const float* q, const float* w0,
+                            const float* kap, const VvSeg& sg, double tile_tol,
+                            double* F, double* U, double* W, void* stats,
+                            unsigned long long* kept, cudaStream_t s);
 cudaError_t launch_vv10(const float* xyz, const float* q, const float* w0,
                         const float* kap, int64_t n, double tile_tol,
                         double* F, double* U, double* W, void* ws,

@@ -103,6 +103,53 @@ __device__ __forceinline__ bool vv10_keep(const VvTileStats& a,
     return fmax(fmax(bf, bu), bw) >= tol;
 }
 
+// The pairs of one outer point with one staged inner tile (m points), the
+// one-reciprocal form: inv = 1/(g gp gt) from rcp.approx and one Newton
+// step, T = q inv and, with 1/g + 1/gt = (g + gt) gp inv, Tu = T (g + gt)
+// gp inv.  Plain FP32 sums over 16 pairs, merged into Kahan-compensated
+// tile sums once per 16 pairs; the tile sums join the FP64 totals.  Shared
+// by the single-molecule and the batched kernels (same arithmetic, same
+// order).
+__device__ __forceinline__ void vv10_tile_fast(
+    const float xi, const float yi, const float zi, const float w0i, const float ki,
+    const float4* sp, const float2* sk, const int m, double& f64, double& u64,
+    double& w64, unsigned long long& nkept) {
+    float fs = 0.f, fc = 0.f, us = 0.f, uc = 0.f, ws = 0.f, wc = 0.f;
+    auto pair = [&](const int t, float& pf, float& pu, float& pw) {
+        const float4 pj = sp[t];
+        const float2 kj = sk[t];
+        const float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float g = fmaf(r2, w0i, ki);
+        const float gp = fmaf(r2, kj.x, kj.y);
+        const float gt = g + gp;
+        const float pr = g * gp * gt;
+        float inv;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(pr));
+        if (WB_VV10_NEWTON) inv = fmaf(inv, fmaf(-pr, inv, 1.0f), inv);
+        const float T = pj.w * inv;
+        const float Tu = T * ((g + gt) * gp * inv);
+        pf += T;
+        pu += Tu;
+        pw = fmaf(Tu, r2, pw);
+    };
+    for (int t0 = 0; t0 < m; t0 += 16) {
+        float pf = 0.f, pu = 0.f, pw = 0.f;
+        if (t0 + 16 <= m) {
+#pragma unroll
+            for (int t = 0; t < 16; ++t) pair(t0 + t, pf, pu, pw);
+        } else {
+            for (int t = t0; t < m; ++t) pair(t, pf, pu, pw);
+        }
+        float y, z;
+        y = pf - fc; z = fs + y; fc = (z - fs) - y; fs = z;
+        y = pu - uc; z = us + y; uc = (z - us) - y; us = z;
+        y = pw - wc; z = ws + y; wc = (z - ws) - y; ws = z;
+    }
+    f64 += (double)fs; u64 += (double)us; w64 += (double)ws;
+    nkept += (unsigned long long)m;
+}
+
 __global__ void __launch_bounds__(kVvTile)
 vv10_sum_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
                 const float* __restrict__ w0, const float* __restrict__ kap,
@@ -136,46 +183,8 @@ vv10_sum_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
         __syncthreads();
         const int m = (int)min((int64_t)kVvTile, n - jt * kVvTile);
 #if WB_VV10_FAST
-        if (active) {
-            // one reciprocal per pair: inv = 1/(g gp gt) from rcp.approx and
-            // one Newton step, T = q inv and, with 1/g + 1/gt = (g + gt) gp
-            // inv, Tu = T (g + gt) gp inv.  Plain FP32 sums over 16 pairs,
-            // merged into Kahan-compensated tile sums once per 16 pairs.
-            float fs = 0.f, fc = 0.f, us = 0.f, uc = 0.f, ws = 0.f, wc = 0.f;
-            auto pair = [&](const int t, float& pf, float& pu, float& pw) {
-                const float4 pj = sp[t];
-                const float2 kj = sk[t];
-                const float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                const float g = fmaf(r2, w0i, ki);
-                const float gp = fmaf(r2, kj.x, kj.y);
-                const float gt = g + gp;
-                const float pr = g * gp * gt;
-                float inv;
-                asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(pr));
-                if (WB_VV10_NEWTON) inv = fmaf(inv, fmaf(-pr, inv, 1.0f), inv);
-                const float T = pj.w * inv;
-                const float Tu = T * ((g + gt) * gp * inv);
-                pf += T;
-                pu += Tu;
-                pw = fmaf(Tu, r2, pw);
-            };
-            for (int t0 = 0; t0 < m; t0 += 16) {
-                float pf = 0.f, pu = 0.f, pw = 0.f;
-                if (t0 + 16 <= m) {
-#pragma unroll
-                    for (int t = 0; t < 16; ++t) pair(t0 + t, pf, pu, pw);
-                } else {
-                    for (int t = t0; t < m; ++t) pair(t, pf, pu, pw);
-                }
-                float y, z;
-                y = pf - fc; z = fs + y; fc = (z - fs) - y; fs = z;
-                y = pu - uc; z = us + y; uc = (z - us) - y; us = z;
-                y = pw - wc; z = ws + y; wc = (z - ws) - y; ws = z;
-            }
-            f64 += (double)fs; u64 += (double)us; w64 += (double)ws;
-            nkept += (unsigned long long)m;
-        }
+        if (active)
+            vv10_tile_fast(xi, yi, zi, w0i, ki, sp, sk, m, f64, u64, w64, nkept);
 #else
         if (active) {
             float fs = 0.f, fc = 0.f, us = 0.f, uc = 0.f, ws = 0.f, wc = 0.f;
@@ -386,6 +395,129 @@ vv10_sum_packed_kernel(const float* __restrict__ xyz, const float* __restrict__ 
 }
 
 }  // namespace
+
+// -- batched form: several molecules' point sets in one launch -------------
+// The points of molecule m are [off_m, off_m+1) of the concatenated arrays
+// and are cut into 256-point tiles that never straddle two molecules:
+// tile t covers [tstart[t], tstart[t] + tlen[t]) of molecule tmol[t], and
+// molecule m owns tiles mtile[m] .. mtile[m + 1] - 1.  One block per outer
+// tile; its inner tiles are those of its own molecule, in order, so every
+// molecule's sums are bitwise those of its single-molecule call.
+
+__global__ void vv10_tile_stats_seg_kernel(const float* __restrict__ xyz,
+                                           const float* __restrict__ q,
+                                           const float* __restrict__ w0,
+                                           const float* __restrict__ kap,
+                                           const VvSeg sg, VvTileStats* __restrict__ st) {
+    const int64_t tile = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (tile >= sg.ntiles) return;
+    const int64_t i0 = sg.tstart[tile];
+    const int64_t i1 = i0 + sg.tlen[tile];
+    double sx = 0, sy = 0, sz = 0, sq = 0, mw = INFINITY, mk = INFINITY;
+    for (int64_t i = i0 + lane; i < i1; i += 32) {
+        sx += xyz[3 * i]; sy += xyz[3 * i + 1]; sz += xyz[3 * i + 2];
+        sq += q[i];
+        mw = fmin(mw, (double)w0[i]);
+        mk = fmin(mk, (double)kap[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        sz += __shfl_xor_sync(0xffffffffu, sz, o);
+        sq += __shfl_xor_sync(0xffffffffu, sq, o);
+        mw = fmin(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+        mk = fmin(mk, __shfl_xor_sync(0xffffffffu, mk, o));
+    }
+    const double cnt = (double)(i1 - i0);
+    const double cx = sx / cnt, cy = sy / cnt, cz = sz / cnt;
+    double r = 0.0;
+    for (int64_t i = i0 + lane; i < i1; i += 32) {
+        const double dx = xyz[3 * i] - cx, dy = xyz[3 * i + 1] - cy,
+                     dz = xyz[3 * i + 2] - cz;
+        r = fmax(r, sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    for (int o = 16; o > 0; o >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, o));
+    if (lane == 0) {
+        VvTileStats s;
+        s.cx = cx; s.cy = cy; s.cz = cz; s.rad = r * (1.0 + 1e-12) + 1e-12;
+        s.qsum = sq; s.w0min = mw; s.kmin = mk; s.pad = 0.0;
+        st[tile] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kVvTile)
+vv10_sum_seg_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
+                    const float* __restrict__ w0, const float* __restrict__ kap,
+                    const VvSeg sg, double tol, const VvTileStats* __restrict__ st,
+                    double* __restrict__ F, double* __restrict__ U,
+                    double* __restrict__ W, unsigned long long* __restrict__ kept) {
+    __shared__ float4 sp[kVvTile];      // x, y, z, q
+    __shared__ float2 sk[kVvTile];      // w0, kappa
+    __shared__ int s_keep[2];
+    const int64_t t = blockIdx.x;
+    const int mol = sg.tmol[t];
+    const int64_t i = sg.tstart[t] + threadIdx.x;
+    const bool active = (int)threadIdx.x < sg.tlen[t];
+    float xi = 0.f, yi = 0.f, zi = 0.f, w0i = 0.f, ki = 1.f;
+    if (active) {
+        xi = xyz[3 * i]; yi = xyz[3 * i + 1]; zi = xyz[3 * i + 2];
+        w0i = w0[i]; ki = kap[i];
+    }
+    double f64 = 0.0, u64 = 0.0, w64 = 0.0;
+    unsigned long long nkept = 0;
+    const int jt0 = sg.mtile[mol], jt1 = sg.mtile[mol + 1];
+    for (int jt = jt0; jt < jt1; ++jt) {
+        if (threadIdx.x == 0)
+            s_keep[jt & 1] = vv10_keep(st[t], st[jt], tol);
+        const int m = sg.tlen[jt];
+        const int64_t j = sg.tstart[jt] + threadIdx.x;
+        __syncthreads();
+        if (!s_keep[jt & 1]) continue;  // uniform across the block
+        if ((int)threadIdx.x < m) {
+            sp[threadIdx.x] = make_float4(xyz[3 * j], xyz[3 * j + 1],
+                                          xyz[3 * j + 2], q[j]);
+            sk[threadIdx.x] = make_float2(w0[j], kap[j]);
+        }
+        __syncthreads();
+        if (active)
+            vv10_tile_fast(xi, yi, zi, w0i, ki, sp, sk, m, f64, u64, w64, nkept);
+        __syncthreads();
+    }
+    if (active) { F[i] = -1.5 * f64; U[i] = u64; W[i] = w64; }
+    if (kept) {
+        __shared__ unsigned long long red[kVvTile / 32];
+        unsigned long long v = nkept;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long tot = 0;
+            for (int w = 0; w < kVvTile / 32; ++w) tot += red[w];
+            atomicAdd(kept, tot);
+        }
+    }
+}
+
+cudaError_t launch_vv10_seg(const float* xyz, const float* q, const float* w0,
+                            const float* kap, const VvSeg& sg, double tile_tol,
+                            double* F, double* U, double* W, void* stats,
+                            unsigned long long* kept, cudaStream_t s) {
+    if (sg.ntiles <= 0) return cudaSuccess;
+    VvTileStats* st = static_cast<VvTileStats*>(stats);
+    vv10_tile_stats_seg_kernel<<<(unsigned)((sg.ntiles * 32 + 127) / 128), 128, 0, s>>>(
+        xyz, q, w0, kap, sg, st);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    vv10_sum_seg_kernel<<<(unsigned)sg.ntiles, kVvTile, 0, s>>>(xyz, q, w0, kap, sg,
+                                                               tile_tol, st, F, U, W,
+                                                               kept);
+    return cudaGetLastError();
+}
+
+size_t vv10_tile_stats_bytes(int64_t ntiles) {
+    return (size_t)ntiles * sizeof(VvTileStats);
+}
 
 cudaError_t launch_vv10(const float* xyz, const float* q, const float* w0,
                         const float* kap, int64_t n, double tile_tol,

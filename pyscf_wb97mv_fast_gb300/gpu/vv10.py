@@ -62,6 +62,35 @@ class Vv10Kernel:
         return F, U, W
 
 
+    def kernel_sum_batch(self, coords, q, W0, kappa):
+        """The double sums of several molecules in one launch: lists of
+        per-molecule device arrays as kernel_sum takes them -> lists of F,
+        U, W (each molecule's sums over its own points only; bitwise equal
+        to kernel_sum per molecule)."""
+        torch = _torch()
+        sizes = [int(c.shape[0]) for c in coords]
+        dev = coords[0].device
+        offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        n = int(offsets[-1])
+        xyz = torch.cat([c.to(torch.float32) for c in coords]).contiguous()
+        q32, w32, k32 = (torch.cat([torch.as_tensor(a, device=dev).to(torch.float32)
+                                    for a in arrs]).contiguous()
+                         for arrs in (q, W0, kappa))
+        F = torch.zeros(n, dtype=torch.float64, device=dev)
+        U = torch.zeros_like(F)
+        W = torch.zeros_like(F)
+        kept = _native.ctypes.c_int64()
+        stream = _native.ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        _native.check(_native.lib().wb_vv10_kernel_sum_batch(
+            len(sizes), offsets.ctypes.data_as(_native.ctypes.c_void_p),
+            _native.ptr(xyz), _native.ptr(q32), _native.ptr(w32), _native.ptr(k32),
+            self.tile_tol, _native.ptr(F), _native.ptr(U), _native.ptr(W), stream,
+            _native.ctypes.byref(kept)), 'wb_vv10_kernel_sum_batch')
+        self.last_pairs_kept = (int(kept.value), int(sum(m * m for m in sizes)))
+        sl = [slice(int(offsets[i]), int(offsets[i + 1])) for i in range(len(sizes))]
+        return [F[x] for x in sl], [U[x] for x in sl], [W[x] for x in sl]
+
+
 def vv10_pointwise(rho0, grad, weights, nlc_pars):
     """Per-point FP64 terms on the thresholded set: q, W0, kappa, dW0/dR,
     dW0/dG, dK/dR, Beta (torch tensors; Beta a float)."""
