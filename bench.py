@@ -735,6 +735,8 @@ def main():
                     help='keep the compiled-in per-class kernel variants')
     ap.add_argument('--no-batched', action='store_true',
                     help='skip the batched (many molecules per launch) leg')
+    ap.add_argument('--batched-molecules', type=int, default=64,
+                    help='water clusters in the batched leg (profiling: fewer)')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -902,7 +904,8 @@ def main():
     graphs = None if (args.no_serving or world > 1) else graph_timing(torch)
     eng._ws = None
     torch.cuda.empty_cache()
-    batched = None if (args.no_batched or world > 1) else batched_timing(torch)
+    batched = None if (args.no_batched or world > 1) else batched_timing(
+        torch, nmol=args.batched_molecules)
     k_grad = None if (args.no_grad or world > 1) else grad_timing(torch)
 
     cpu = None
