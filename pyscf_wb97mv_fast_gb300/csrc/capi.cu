@@ -685,10 +685,15 @@ struct wb_cosx_batch {
     int rmax[wb::NCLASS] = {}, rmax2[wb::NCLASS] = {};
     int items[wb::NCLASS] = {};         // blocks of the class over the molecules
     int order[wb::NCLASS] = {};
-    void* block = nullptr;              // device: args (2 nmol), offsets, counters
+    void* block = nullptr;              // device: args (2 nmol), offsets, counters,
+                                        // item costs and orders
     wb::CosxArgs* d_args = nullptr;
     int* d_off = nullptr;               // NCLASS x (nmol + 1)
     int* d_work = nullptr;              // NCLASS x 2
+    float* d_cost = nullptr;            // NCLASS x stride: model flops per item
+    int* d_order = nullptr;             // NCLASS x stride: costliest first
+    int64_t stride = 0;
+    bool ordered = false;               // the orders hold a previous run's costs
 };
 
 static int batch_fail(wb_cosx_batch* b, int code) {
@@ -1485,14 +1490,30 @@ int wb_cosx_batch_create(int nmol, wb_cosx* const* handles,
         }
         b->items[c] = o[nmol];
     }
+    int64_t stride = 1;
+    for (int c = 0; c < wb::NCLASS; ++c) stride = std::max<int64_t>(stride, b->items[c]);
+    b->stride = stride;
     const size_t args_b = align256(sizeof(wb::CosxArgs) * args.size());
     const size_t off_b = align256(sizeof(int) * off.size());
-    const size_t work_b = sizeof(int) * 2 * wb::NCLASS;
-    cudaError_t e = cudaMalloc(&b->block, args_b + off_b + work_b);
+    const size_t work_b = align256(sizeof(int) * 2 * wb::NCLASS);
+    const size_t cost_b = align256(sizeof(float) * wb::NCLASS * stride);
+    const size_t order_b = align256(sizeof(int) * wb::NCLASS * stride);
+    cudaError_t e = cudaMalloc(&b->block, args_b + off_b + work_b + cost_b + order_b);
     if (e != cudaSuccess) return batch_fail(b, cuda_fail(e, "wb_cosx_batch_create"));
-    b->d_args = static_cast<wb::CosxArgs*>(b->block);
-    b->d_off = reinterpret_cast<int*>(static_cast<char*>(b->block) + args_b);
-    b->d_work = reinterpret_cast<int*>(static_cast<char*>(b->block) + args_b + off_b);
+    char* blk = static_cast<char*>(b->block);
+    b->d_args = reinterpret_cast<wb::CosxArgs*>(blk);
+    b->d_off = reinterpret_cast<int*>(blk + args_b);
+    b->d_work = reinterpret_cast<int*>(blk + args_b + off_b);
+    b->d_cost = reinterpret_cast<float*>(blk + args_b + off_b + work_b);
+    b->d_order = reinterpret_cast<int*>(blk + args_b + off_b + work_b + cost_b);
+    // every block records its kept model flops at its item index, the
+    // order of the next run
+    for (int m = 0; m < nmol; ++m)
+        for (int c = 0; c < wb::NCLASS; ++c) {
+            float* row = b->d_cost + (size_t)c * stride + off[(size_t)c * (nmol + 1) + m];
+            args[m].bcost[c] = row;
+            args[nmol + m].bcost[c] = row;
+        }
     e = cudaMemcpy(b->d_args, args.data(), sizeof(wb::CosxArgs) * args.size(),
                    cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -1610,10 +1631,11 @@ int wb_cosx_batch_run(wb_cosx_batch* b, const double* const* qd,
         if (!b->has[c] || b->items[c] == 0) continue;
         const int want = (b->items[c] + 3) / 4;
         const int* off = b->d_off + (size_t)c * (nmol + 1);
+        const int* order = b->ordered ? b->d_order + (size_t)c * b->stride : nullptr;
         if (b->dual[c]) {
             const int cap = std::max(1, h0->blocks_per_sm2[c]) * h0->nsm;
             WB_CUDA(wb::launch_cosx_class_batch(c, b->d_args, off, nmol,
-                                                b->d_work + 2 * c, b->rmax2[c],
+                                                b->d_work + 2 * c, b->rmax2[c], order,
                                                 std::max(1, std::min(want, cap)), s,
                                                 false, b->smem2[c], true));
             launches += 1;
@@ -1623,11 +1645,21 @@ int wb_cosx_batch_run(wb_cosx_batch* b, const double* const* qd,
                 const int cap = std::max(1, h0->blocks_per_sm[c][far ? 1 : 0]) * h0->nsm;
                 WB_CUDA(wb::launch_cosx_class_batch(
                     c, b->d_args + (size_t)w * nmol, off, nmol, b->d_work + 2 * c + w,
-                    b->rmax[c], std::max(1, std::min(want, cap)), s, far, b->smem[c],
-                    false));
+                    b->rmax[c], order, std::max(1, std::min(want, cap)), s, far,
+                    b->smem[c], false));
                 launches += 1;
             }
         }
+    }
+    {   // the next run takes each class's items costliest first
+        wb::BlockOrderArgs P;
+        P.cost = b->d_cost;
+        P.order = b->d_order;
+        P.stride = b->stride;
+        for (int c = 0; c < wb::NCLASS; ++c) P.n[c] = b->has[c] ? b->items[c] : 0;
+        WB_CUDA(wb::launch_block_order(P, s));
+        launches += 1;
+        b->ordered = true;
     }
     // per molecule: G of each slot, then K
     for (int m = 0; m < nmol; ++m) {

@@ -558,7 +558,10 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
 // item_off[m + 1] - 1 (ascending).  Warps take items from one counter
 // (*work) and copy the argument block of the molecule they work on into
 // shared memory; rmax is the largest task record of the class over the
-// molecules (the dynamic shared memory holds two per warp).  The Boys table
+// molecules (the dynamic shared memory holds two per warp).  order, if not
+// null, is the order in which the items are taken (costliest first, from
+// the block costs the previous launch recorded through each molecule's
+// bcost).  The Boys table
 // is the same for every molecule.  Each molecule's counters receive its own
 // tasks; every element of every class buffer keeps one writer lane and its
 // summation order, so each molecule's G equals its single-molecule G.
@@ -567,7 +570,8 @@ __global__ void __launch_bounds__(kCtaThreads,
                                   min_blocks(LA * (LA + 1) / 2 + LB, NW))
 cosx_class_kernel_batch(const CosxArgs* __restrict__ args,
                         const int* __restrict__ item_off, const int nmol,
-                        int* __restrict__ work, const int rmax) {
+                        int* __restrict__ work, const int rmax,
+                        const int* __restrict__ order) {
     static_assert(NW == 1 || (NW == 2 && STAGE), "dual-omega needs staging");
     constexpr int CLS = LA * (LA + 1) / 2 + LB;
     constexpr int NWARP = kCtaThreads / 32;
@@ -607,6 +611,11 @@ cosx_class_kernel_batch(const CosxArgs* __restrict__ args,
         if (lane == 0) {
             item = atomicAdd(work, 1);
             if (item < total) {
+                // costliest items first (a permutation of 0 .. total - 1)
+                if (order) {
+                    const int o = order[item];
+                    item = o >= 0 && o < total ? o : item;
+                }
                 int lo = 0, hi = nmol;          // item_off[lo] <= item < item_off[hi]
                 while (hi - lo > 1) {
                     const int mid = (lo + hi) >> 1;

@@ -19,10 +19,11 @@ cudaError_t launch_cosx_class_range(int cls, const CosxArgs& a, int pb,
 // the batched form: one launch over the class's blocks of nmol molecules
 // (args: nmol device argument blocks; off: nmol + 1 item offsets; work: a
 // zeroed counter; rmax: the largest task record of the class over the
-// molecules, smem = 4 warps x 2 x rmax float4 when staged)
+// molecules, smem = 4 warps x 2 x rmax float4 when staged; order: the item
+// order, costliest first, or null for ascending)
 cudaError_t launch_cosx_class_batch(int cls, const CosxArgs* args, const int* off,
-                                    int nmol, int* work, int rmax, int grid,
-                                    cudaStream_t s, bool far, size_t smem,
+                                    int nmol, int* work, int rmax, const int* order,
+                                    int grid, cudaStream_t s, bool far, size_t smem,
                                     bool dual);
 // max resident CTAs per SM of a class kernel (128 threads each); 0 if the
 // kernel cannot run with that much dynamic shared memory
