@@ -82,7 +82,7 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
                 mem_fraction=DEFAULT_MEM_FRACTION, overlap=False,
                 semilocal=True, k=True, k_tile_tol=1e-11,
                 openblas_threads=None, vv10=True, k_gemm='ozaki',
-                sgx_jk_module=None, k_omegas='auto'):
+                sgx_jk_module=None, k_omegas='auto', k_precision='fp32'):
     """Hook the GPU COSX K (and VV10) into mf; returns a HookSet.
 
     The keyword names follow the reference; backend must be None or
@@ -94,6 +94,8 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
     asks K for with the same density, built together (GpuKBuilder
     omegas); 'auto' reads them from the range-separated functional of mf
     ((0, omega) when it has one), None builds one K per call.
+    k_precision (an addition): 'fp32' (the mixed-precision K) or 'fp64'
+    (the plain FP64 GPU form, for an FP64 tail on the GPU).
     """
     if backend not in (None, 'cuda', 'cupy'):
         raise ValueError("backend must be None or 'cuda'")
@@ -117,6 +119,7 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
                            and k_omegas == 'auto' else k_omegas)
                     b = sgx_k_mod.GpuKBuilder(mf.mol, tile_tol=k_tile_tol,
                                               blksize=blksize, gemm=k_gemm,
+                                              precision=k_precision,
                                               omegas=oms)
                     b._build()
                     torch = sgx_k_mod._torch()

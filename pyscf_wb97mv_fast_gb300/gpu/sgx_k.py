@@ -78,10 +78,15 @@ class GpuKBuilder:
     one native call (AO values and F shared) and the others are kept until
     asked for with the same density, grid and projector; any other call
     drops them.  None (default): one K per call.
+    precision (an addition): 'fp32' (default: the fused FP32 G kernels,
+    F rounded once to FP32) or 'fp64' (the plain FP64 form,
+    wb_cosx_get_k_fp64: FP64 F, FP64 G kernels, DGEMMs; the whole grid in
+    one call) -- the operator of an FP64 tail on the GPU.
     """
 
     def __init__(self, mol, device=None, tile_tol=1e-11, mem_budget=None,
-                 origin=None, blksize=None, gemm='ozaki', omegas=None):
+                 origin=None, blksize=None, gemm='ozaki', omegas=None,
+                 precision='fp32'):
         self.mol = mol
         self.tile_tol = float(tile_tol)
         self.origin = origin
@@ -92,6 +97,9 @@ class GpuKBuilder:
             raise ValueError("gemm must be 'ozaki', 'native' or 'emulated'")
         self.gemm = gemm
         self.omegas = None if omegas is None else tuple(float(w) for w in omegas)
+        if precision not in ('fp32', 'fp64'):
+            raise ValueError("precision must be 'fp32' or 'fp64'")
+        self.precision = precision
         self._pending = None       # (key, dm copy, {omega: K host}) of a multi build
         self.engine = None
         self._grids_states = {}
@@ -171,7 +179,7 @@ class GpuKBuilder:
         proj = np.asarray(pjs._overlap_correction_matrix, dtype=np.float64)
         sym = bool(pjs.sym_ovlp)
         state = self._grid_state(grids)
-        key = (state.fingerprint, sym, self.tile_tol, self.gemm)
+        key = (state.fingerprint, sym, self.tile_tol, self.gemm, self.precision)
         omega = float(omega)
         hit = self._take_pending(key, dm, proj, omega)
         if hit is not None:
@@ -186,7 +194,11 @@ class GpuKBuilder:
         qd = proj_d @ torch.as_tensor(dm, dtype=torch.float64, device=dev)
         tk0 = time.perf_counter()
         multi = self.omegas is not None and omega in self.omegas and len(self.omegas) > 1
-        if multi:
+        if self.precision == 'fp64':
+            Ks = self.engine.get_k_fp64(state.coords, state.weights, qd,
+                                        self.omegas if multi else (omega,),
+                                        tile_tol=self.tile_tol)
+        elif multi:
             Ks = self.engine.get_k_multi(state.coords, state.weights, qd,
                                          self.omegas, tile_tol=self.tile_tol,
                                          tile_pts=self._tile(state.ngrids),

@@ -21,7 +21,9 @@ after max_fp32_s2_cycles), the GPU hooks come off for the remaining cycles
 -- again with a DIIS reset and a full Fock rebuild, since the energy
 functional changes by the FP32 error -- and convergence is never declared
 before that switch.  ``fp64_final_vv10='gpu'`` keeps VV10 (only) on the GPU
-for the FP64 tail; ``'cpu'`` moves it back too.  ``fp64_conv_tol`` is the
+for the FP64 tail; ``'cpu'`` moves it back too.  ``fp64_final_k='gpu'``
+(an addition; the reference's tail always runs K on the CPU) keeps K on
+the GPU for the tail in its plain FP64 form (``k_precision='fp64'``).  ``fp64_conv_tol`` is the
 |dE| threshold of the FP64 tail alone (the |g| threshold stays
 conv_tol_grad or sqrt(conv_tol)); setting it also turns mf.conv_check off
 while attached.
@@ -146,7 +148,8 @@ class StagedSCF:
                  nlc_production_level=3, gpu_stages=(), gpu_kwargs=None,
                  fp64_final=False, tau_fp64=None, fp64_final_vv10='gpu',
                  tau_fp64_g=5e-5, max_fp32_s2_cycles=8, tau2_g=math.inf,
-                 max_s1_cycles=8, fp64_conv_tol=None, installer=None):
+                 max_s1_cycles=8, fp64_conv_tol=None, installer=None,
+                 fp64_final_k='cpu'):
         df = getattr(mf, 'with_df', None)
         if df is None or not hasattr(df, 'grids_level_i'):
             raise TypeError('StagedSCF needs a COSX (SGX) mf, got %s'
@@ -158,6 +161,8 @@ class StagedSCF:
                              'needs 2 in gpu_stages')
         if fp64_final_vv10 not in ('gpu', 'cpu'):
             raise ValueError("fp64_final_vv10 must be 'gpu' or 'cpu'")
+        if fp64_final_k not in ('gpu', 'cpu'):
+            raise ValueError("fp64_final_k must be 'gpu' or 'cpu'")
         if fp64_conv_tol is not None and not fp64_final:
             raise ValueError('fp64_conv_tol applies to the FP64 tail: '
                              'needs fp64_final=True')
@@ -181,6 +186,7 @@ class StagedSCF:
         self.gpu_stages = tuple(sorted(set(gpu_stages)))
         self.gpu_kwargs = dict(gpu_kwargs or {})
         self.fp64_final_vv10 = fp64_final_vv10
+        self.fp64_final_k = fp64_final_k
         self.fp64_conv_tol = (None if fp64_conv_tol is None
                               else float(fp64_conv_tol))
         self.plan = StagePlan(tau1=tau1, tau2=tau2, tau2_g=tau2_g,
@@ -325,10 +331,17 @@ class StagedSCF:
             self.switches.append(dict(_from=old, to=old, cycle=cycle, t=t,
                                       precision='fp64', forced=decision[1]))
             self._set_gpu(False)
-            if self.fp64_final_vv10 == 'gpu':
-                # VV10 stays FP32 on the GPU; K goes back to the FP64 code
-                self._gpu_hooks = self._installer(
-                    self.mf, **dict(self.gpu_kwargs, semilocal=False, k=False))
+            k_gpu = self.fp64_final_k == 'gpu'
+            if self.fp64_final_vv10 == 'gpu' or k_gpu:
+                # VV10 stays FP32 on the GPU (or goes back to the CPU); K
+                # goes back to the FP64 CPU code, or with fp64_final_k='gpu'
+                # runs in the plain FP64 form on the GPU
+                kw = dict(self.gpu_kwargs, semilocal=False, k=k_gpu)
+                if self.fp64_final_vv10 != 'gpu':
+                    kw['vv10'] = False
+                if k_gpu:
+                    kw['k_precision'] = 'fp64'
+                self._gpu_hooks = self._installer(self.mf, **kw)
             self.mf._nsteps_direct = 0
             reset_diis(envs.get('mf_diis'))
             _note(self.mf, 'StagedSCF precision switch FP32 -> FP64 in %s at '

@@ -141,3 +141,31 @@ def test_mixed_path_against_fp64_form_water27():
         scale = np.abs(K64[j]).max()
         assert np.max(np.abs(Km[j] - K64[j])) < 1e-6 * scale
         assert abs(0.25 * np.einsum('ij,ji->', dm, Km[j] - K64[j])) < 3e-6
+
+
+def test_builder_fp64_precision_for_the_tail():
+    """GpuKBuilder(precision='fp64'), the K of an FP64 tail on the GPU
+    (install_gpu(k_precision='fp64'), StagedSCF(fp64_final_k='gpu')): the
+    reference's get_k contract, FP64 agreement with the oracle, and the
+    second omega of a cycle served from the multi-omega build."""
+    from pyscf_wb97mv_fast_gb300.gpu.sgx_k import (GpuKBuilder, SyntheticSGX,
+                                                   get_k_only_gpu)
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    mol = dimer('synthetic-svp')
+    g = build_grids(mol, level=0)
+    sgx = SyntheticSGX(mol, g)
+    dm = density(mol.nao, 10, 9)
+    b = GpuKBuilder(mol, tile_tol=0.0, precision='fp64', omegas=(0.0, 0.3))
+    K0 = get_k_only_gpu(b, sgx, dm)
+    assert np.array_equal(K0, K0.T)
+    mol.omega = 0.3
+    try:
+        K3 = get_k_only_gpu(b, sgx, dm)
+        assert b.last_stats['from_multi']
+    finally:
+        mol.omega = 0.0
+    for K, om in ((K0, 0.0), (K3, 0.3)):
+        ref = oracle.cosx_k(mol, g.coords, g.weights, dm, om)
+        assert np.max(np.abs(K - ref)) < 1e-11 * np.abs(ref).max()
+    with pytest.raises(ValueError):
+        GpuKBuilder(mol, precision='fp16')

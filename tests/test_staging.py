@@ -291,6 +291,30 @@ def test_gpu_stages_with_fp64_tail():
     assert mf.gpu is None          # hooks off after restore
 
 
+@pytest.mark.parametrize('vv10', ['gpu', 'cpu'])
+def test_fp64_tail_on_the_gpu(vv10):
+    """fp64_final_k='gpu' (an addition): the FP64 tail keeps K on the GPU in
+    its plain FP64 form; VV10 stays on the GPU only with
+    fp64_final_vv10='gpu'."""
+    mf = FakeMF()
+    calls = []
+    st = StagedSCF(mf, gpu_stages=(0, 1, 2), fp64_final=True, fp64_final_k='gpu',
+                   fp64_final_vv10=vv10, gpu_kwargs=dict(k=True, k_tile_tol=1e-11),
+                   installer=installer(calls))
+    with st:
+        mf.kernel()
+    tail = dict(k=True, k_tile_tol=1e-11, semilocal=False, k_precision='fp64')
+    if vv10 == 'cpu':
+        tail['vv10'] = False
+    assert calls == [dict(k=True, k_tile_tol=1e-11), tail]
+    i = next(i for i, h in enumerate(st.history) if h['fp64'])
+    assert mf.veff_log[i]['full'] and mf.veff_log[i]['gpu']['k'] is True
+    assert st.history[-1]['fp64'] and mf.converged
+    assert mf.gpu is None
+    with pytest.raises(ValueError):
+        StagedSCF(FakeMF(), fp64_final=True, fp64_final_k='x')
+
+
 def test_fp64_conv_tol_and_steps_mode_turn_conv_check_off():
     mf = FakeMF()
     seen = []
