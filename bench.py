@@ -135,6 +135,25 @@ class ClockSampler:
                 'samples': len(sm)}
 
 
+def max_over_ranks(t, world, device):
+    """The job's time: the slowest rank's (all-reduce MAX over the ranks of
+    the default process group; the local time when world is 1)."""
+    if world <= 1:
+        return float(t)
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([float(t)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_throughput(work_per_rank, t_max, world):
+    """Whole-job throughput of world replicas that each did
+    work_per_rank in at most t_max seconds (weak scaling: the path does not
+    shard, every rank runs the full workload on its own GPU)."""
+    return world * float(work_per_rank) / float(t_max)
+
+
 def measured_peaks():
     path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
     if os.path.exists(path):
@@ -824,11 +843,8 @@ def main():
 
     with ClockSampler(local) as clocks:
         t_step = timed(step, args.steps, args.warmup)
-    if world > 1:
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
-    value = world * flops_step / t_step / 1e12
+    t_step = max_over_ranks(t_step, world, dev)
+    value = replica_throughput(flops_step, t_step, world) / 1e12
 
     # -- e2e: pinned host inputs in, K out, every step ----------------------------
     coords_rel_h = (g.coords - eng.origin).astype(np.float64)
@@ -851,10 +867,7 @@ def main():
             k_h[i].copy_(Ks, non_blocking=True)
 
     t_e2e = timed(e2e_step, args.steps, 1)
-    if world > 1:
-        tt = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    t_e2e = max_over_ranks(t_e2e, world, dev)
     h2d = c_h.numel() * 8 + w_h.numel() * 8 + d_h.numel() * 8
     d2h = sum(k.numel() * 8 for k in k_h)
 
@@ -920,7 +933,8 @@ def main():
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
             'data': 'synthetic (seeded generators; no PySCF grids or basis)',
             'config': config_dict(mol, g, args),
-            'e2e': {'value': world * flops_step / t_e2e / 1e12, 'unit': UNIT,
+            'e2e': {'value': replica_throughput(flops_step, t_e2e, world) / 1e12,
+                    'unit': UNIT,
                     'ms_per_step': t_e2e * 1e3, 'h2d_bytes_per_step': h2d,
                     'd2h_bytes_per_step': d2h},
             'roofline': roofline,
