@@ -345,6 +345,30 @@ __global__ void gsum_kernel(const float* __restrict__ gc,
     *reinterpret_cast<float4*>(G + (int64_t)mu * ld + i) = acc;
 }
 
+// the same over two buffer sets (the two halves of split blocks): the
+// first set's rows, then the second's, in fixed order
+__global__ void gsum2_kernel(const float* __restrict__ gc0,
+                             const float* __restrict__ gc1,
+                             const int4* __restrict__ src, int64_t ld,
+                             float* __restrict__ G) {
+    const int mu = blockIdx.y;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (i >= ld) return;
+    const int4 sr = src[mu];
+    const int rows[4] = {sr.x, sr.y, sr.z, sr.w};
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int h = 0; h < 2; ++h) {
+        const float* gc = h ? gc1 : gc0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (rows[j] < 0) continue;
+            const float4 v = *reinterpret_cast<const float4*>(gc + rows[j] * ld + i);
+            acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
+        }
+    }
+    *reinterpret_cast<float4*>(G + (int64_t)mu * ld + i) = acc;
+}
+
 // Longest-processing-time order of the point blocks of each class (one
 // CTA per class): a counting sort of the blocks by their measured cost in
 // 2^(1/8) steps, costliest first.  Each kernel hands its blocks out in this
@@ -484,6 +508,14 @@ cudaError_t launch_gsum(const float* gc, const int4* src, int nao, int64_t ld,
     const int64_t quads = ld / 4;
     dim3 grid((unsigned)((quads + 255) / 256), (unsigned)nao);
     gsum_kernel<<<grid, 256, 0, s>>>(gc, src, ld, G);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gsum2(const float* gc0, const float* gc1, const int4* src, int nao,
+                         int64_t ld, float* G, cudaStream_t s) {
+    const int64_t quads = ld / 4;
+    dim3 grid((unsigned)((quads + 255) / 256), (unsigned)nao);
+    gsum2_kernel<<<grid, 256, 0, s>>>(gc0, gc1, src, ld, G);
     return cudaGetLastError();
 }
 

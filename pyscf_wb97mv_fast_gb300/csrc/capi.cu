@@ -172,6 +172,9 @@ struct wb_cosx {
     int* border = nullptr;
     int64_t bo_stride = 0, bo_ld = -1;
     int bo_n[wb::NCLASS] = {0};
+    // first pair of the second half of each class's blocks (WB_COSX_SPLIT):
+    // a run boundary near the middle of the class's model flops
+    int split[wb::NCLASS] = {0};
     // FP64 pair data of the plain FP64 form (wb_cosx_get_k_fp64), uploaded
     // on its first call: P per primitive pair, the class E blocks, the FP64
     // Boys table followed by the FP64 c2s tables of l = 2, 3
@@ -191,7 +194,7 @@ struct WsLayout {
     size_t om = 0, rec = 0, om2 = 0, rec2 = 0, recb = 0, gh = 0, gl = 0;
     size_t counters = 0, work = 0;
     size_t subcr[3] = {0, 0, 0}, msh[3] = {0, 0, 0};  // 32/64/128-point blocks
-    size_t gcls = 0, gcls2 = 0;
+    size_t gcls = 0, gcls2 = 0, gclsH = 0, gcls2H = 0;
     size_t X = 0, F64 = 0, F32 = 0, G32 = 0, G32b = 0, oz = 0, total = 0;
 };
 
@@ -223,6 +226,10 @@ WsLayout ws_layout(const wb_cosx* h, int64_t ldt, bool full) {
     }
     L.gcls = take(sizeof(float) * (size_t)std::max<int64_t>(h->hp.ncrow, 1) * ldt);
     L.gcls2 = take(sizeof(float) * (size_t)std::max<int64_t>(h->hp.ncrow, 1) * ldt);
+#if WB_COSX_SPLIT
+    L.gclsH = take(sizeof(float) * (size_t)std::max<int64_t>(h->hp.ncrow, 1) * ldt);
+    L.gcls2H = take(sizeof(float) * (size_t)std::max<int64_t>(h->hp.ncrow, 1) * ldt);
+#endif
     if (full) {
         L.X = take(sizeof(double) * (size_t)nao * ldt);
         L.F32 = take(sizeof(float) * (size_t)nao * ldt);
@@ -296,6 +303,13 @@ wb::CosxArgs make_args(const wb_cosx* h, void* ws, const WsLayout& L,
         a.cls_pb[c] = h->hp.cls[c].pair_begin;
         a.cls_pe[c] = h->hp.cls[c].pair_end;
     }
+#if WB_COSX_SPLIT
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        a.GclsH[c] = at<float>(ws, L.gclsH) + h->hp.crow_base[c] * ldt;
+        a.Gcls2H[c] = at<float>(ws, L.gcls2H) + h->hp.crow_base[c] * ldt;
+        a.cls_split[c] = h->split[c];
+    }
+#endif
     return a;
 }
 
@@ -385,7 +399,8 @@ int tile_prep(wb_cosx* h, const double* coords, const double* weights,
 // blocks of the class kernel that runs for class c (its points per lane)
 int class_nblk(const wb_cosx* h, const wb::CosxArgs& a, int c, bool dual) {
     const int pc = dual ? h->pts2[c] : h->pts[c];
-    return a.nblk[pc == 4 ? 2 : pc - 1];
+    // with WB_COSX_SPLIT a block is two items
+    return (WB_COSX_SPLIT ? 2 : 1) * a.nblk[pc == 4 ? 2 : pc - 1];
 }
 
 // cost / order arrays for a tile of ldt points (grown on demand; a new
@@ -395,7 +410,7 @@ int class_nblk(const wb_cosx* h, const wb::CosxArgs& a, int c, bool dual) {
 int block_order_args(wb_cosx* h, int64_t ldt, wb::CosxArgs& a,
                      const bool* dual, cudaStream_t s) {
     if (!WB_COSX_BLOCK_ORDER) return WB_OK;
-    const int64_t stride = (ldt + 31) / 32;
+    const int64_t stride = (WB_COSX_SPLIT ? 2 : 1) * ((ldt + 31) / 32);
     if (stride > h->bo_stride) {
         WB_CUDA(cudaStreamSynchronize(s));
         if (h->bcost) cudaFree(h->bcost);
@@ -462,7 +477,7 @@ int run_g_classes(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
         const wb::ClassRange& r = h->hp.cls[c];
         if (r.pair_end <= r.pair_begin) continue;
         const int lvl = h->pts[c] == 4 ? 2 : h->pts[c] - 1;
-        const int want = (a.nblk[lvl] + 3) / 4;
+        const int want = ((WB_COSX_SPLIT ? 2 : 1) * a.nblk[lvl] + 3) / 4;
         const int cap = std::max(1, h->blocks_per_sm[c][far ? 1 : 0]) * h->nsm;
         const int grid = std::max(1, std::min(want, cap));
         WB_CUDA(cudaStreamWaitEvent(h->cstream[c], h->fork, 0));
@@ -478,7 +493,12 @@ int run_g_classes(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
         const int st = block_order_update(h, a, ran, single, s, launches);
         if (st != WB_OK) return st;
     }
+#if WB_COSX_SPLIT
+    WB_CUDA(wb::launch_gsum2(at<float>(ws, L.gcls), at<float>(ws, L.gclsH), h->gsrc,
+                             h->hp.nao, ldt, G, s));
+#else
     WB_CUDA(wb::launch_gsum(at<float>(ws, L.gcls), h->gsrc, h->hp.nao, ldt, G, s));
+#endif
     *launches += 1;
     return WB_OK;
 }
@@ -501,6 +521,9 @@ int run_g_classes_dual(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
     for (int c = 0; c < wb::NCLASS; ++c) {
         b.rec[c] = at<float4>(ws, L.recb) + h->hp.rec_off[c];
         b.Gcls[c] = a.Gcls2[c];
+#if WB_COSX_SPLIT
+        b.GclsH[c] = a.Gcls2H[c];
+#endif
     }
     b.work = a.work + wb::NCLASS;
     // (the class kernels zero their buffers block by block)
@@ -512,7 +535,7 @@ int run_g_classes_dual(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
         if (r.pair_end <= r.pair_begin) continue;
         const int pc = h->dual_cls[c] ? h->pts2[c] : h->pts[c];
         const int lvl = pc == 4 ? 2 : pc - 1;
-        const int want = (a.nblk[lvl] + 3) / 4;
+        const int want = ((WB_COSX_SPLIT ? 2 : 1) * a.nblk[lvl] + 3) / 4;
         WB_CUDA(cudaStreamWaitEvent(h->cstream[c], h->fork, 0));
         if (h->dual_cls[c]) {
             const int cap = std::max(1, h->blocks_per_sm2[c]) * h->nsm;
@@ -542,8 +565,15 @@ int run_g_classes_dual(wb_cosx* h, int64_t npts_t, int64_t ldt, const float* F,
         const int st = block_order_update(h, a, ran, h->dual_cls, s, launches);
         if (st != WB_OK) return st;
     }
+#if WB_COSX_SPLIT
+    WB_CUDA(wb::launch_gsum2(at<float>(ws, L.gcls), at<float>(ws, L.gclsH), h->gsrc,
+                             h->hp.nao, ldt, Ga, s));
+    WB_CUDA(wb::launch_gsum2(at<float>(ws, L.gcls2), at<float>(ws, L.gcls2H), h->gsrc,
+                             h->hp.nao, ldt, Gb, s));
+#else
     WB_CUDA(wb::launch_gsum(at<float>(ws, L.gcls), h->gsrc, h->hp.nao, ldt, Ga, s));
     WB_CUDA(wb::launch_gsum(at<float>(ws, L.gcls2), h->gsrc, h->hp.nao, ldt, Gb, s));
+#endif
     *launches += 2;
     return WB_OK;
 }
@@ -926,6 +956,18 @@ int wb_cosx_create(const wb_basis* basis, const double origin[3],
         for (int c = 0; c < wb::NCLASS; ++c)
             h->dual_cls[c] = ((mask >> (4 * (wb::NCLASS - 1 - c))) & 15) != 0 &&
                              h->blocks_per_sm2[c] >= 1;
+    }
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        // the split pair of each class: past half of its model flops, moved
+        // on to the next run boundary (a bra shell's run stays in one half,
+        // so its G_A rows have one writer)
+        const int pb = hp.cls[c].pair_begin, pe = hp.cls[c].pair_end;
+        double tot = 0.0, acc = 0.0;
+        for (int k = pb; k < pe; ++k) tot += (double)hp.pflops[k];
+        int k = pb;
+        while (k < pe && acc + (double)hp.pflops[k] <= 0.5 * tot) acc += (double)hp.pflops[k++];
+        while (k > pb && k < pe && hp.pshell[2 * k] == hp.pshell[2 * (k - 1)]) ++k;
+        h->split[c] = k;
     }
     {   // launch order: model flops of all pairs of a class, descending
         double work[wb::NCLASS] = {0};

@@ -3,6 +3,16 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+// -DWB_COSX_SPLIT=1: each point block of a class is two work items, its
+// pair range cut at a run boundary near the middle of the class's model
+// flops; the second half writes a second set of class buffers, summed
+// after the first.  Twice the items per warp for the load balance of the
+// heavy classes, bitwise reproducible.  Off by default: compiled, not yet
+// measured.
+#ifndef WB_COSX_SPLIT
+#define WB_COSX_SPLIT 0
+#endif
+
 namespace wb {
 
 constexpr int kClasses = 10;
@@ -67,6 +77,11 @@ struct CosxArgs {
     int cls_pb[kClasses];
     int cls_pe[kClasses];
     unsigned long long* status;    // nonzero: a record staging wait gave up
+#if WB_COSX_SPLIT
+    float* GclsH[kClasses];    // class buffers of the second half of each block
+    float* Gcls2H[kClasses];
+    int cls_split[kClasses];   // first pair of the second half
+#endif
 };
 
 }  // namespace wb

@@ -197,6 +197,13 @@ __device__ __forceinline__ void tma_stage_wait(RecStager& st, const int b,
 #define WB_STAGER_PARAM
 #define WB_STAGER_ARG
 #endif
+// with WB_COSX_SPLIT: the buffer set a block item writes (0, 1) and the
+// index its cost is recorded at
+#if WB_COSX_SPLIT
+#define WB_SPLIT_PARAM , const int hset, const int citem
+#else
+#define WB_SPLIT_PARAM
+#endif
 
 __device__ __forceinline__ int lo16(const int x) { return x & 0xffff; }
 __device__ __forceinline__ int hi16(const int x) {
@@ -243,7 +250,7 @@ __device__ __forceinline__ void cosx_class_block(
     const CosxArgs& A, const int pair_begin, const int pair_end, const int blk,
     const float4* __restrict__ stab, float4* wstage, const int rmax, int& sbuf,
     unsigned long long& kept, unsigned long long& flops,
-    unsigned long long& ints WB_STAGER_PARAM) {
+    unsigned long long& ints WB_STAGER_PARAM WB_SPLIT_PARAM) {
     constexpr int CLS = LA * (LA + 1) / 2 + LB;
     constexpr int NCA = (LA + 1) * (LA + 2) / 2;
     constexpr int NA = 2 * LA + 1;
@@ -252,7 +259,13 @@ __device__ __forceinline__ void cosx_class_block(
     const int lane = threadIdx.x & 31;
     constexpr int RS = NW == 2 ? kRecStride2[CLS] : kRecStride[CLS];
     const float4* __restrict__ recc = NW == 2 ? A.rec2[CLS] : A.rec[CLS];
+#if WB_COSX_SPLIT
+    float* const g1 = hset ? A.GclsH[CLS] : A.Gcls[CLS];
+    float* const g2 = hset ? A.Gcls2H[CLS] : A.Gcls2[CLS];
+    float* Gcw[2] = {g1, NW == 2 ? g2 : g1};
+#else
     float* Gcw[2] = {A.Gcls[CLS], NW == 2 ? A.Gcls2[CLS] : A.Gcls[CLS]};
+#endif
     const int ld = (int)A.ld;
     const float tol = A.tol;
     const float4* __restrict__ bnd = A.bnd + A.pp_begin[CLS];
@@ -496,7 +509,11 @@ __device__ __forceinline__ void cosx_class_block(
             cosx_end<LA>(Gp[c], ga0, ld, ok[c % PTS], Xa + c * NCA);
     }
     for (int o = 16; o > 0; o >>= 1) bfl += __shfl_xor_sync(0xffffffffu, bfl, o);
+#if WB_COSX_SPLIT
+    if (lane == 0 && A.bcost[CLS]) A.bcost[CLS][citem] = (float)bfl;
+#else
     if (lane == 0 && A.bcost[CLS]) A.bcost[CLS][blk] = (float)bfl;
+#endif
 }
 
 template<int LA, int LB, bool FAR, bool STAGE, int NW>
@@ -523,6 +540,27 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
     const int nblk = A.nblk[LVL];
     unsigned long long kept = 0, flops = 0, ints = 0;
     const int* __restrict__ order = A.border[CLS];
+#if WB_COSX_SPLIT
+    // items 2 blk + h: half h of block blk
+    const int nitem = 2 * nblk;
+    const int split = A.cls_split[CLS];
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(A.work + CLS, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nitem) break;
+        int it = item;
+        if (order) {
+            const int b = order[item];
+            it = b >= 0 && b < nitem ? b : item;
+        }
+        const int blk = it >> 1, h = it & 1;
+        cosx_class_block<LA, LB, FAR, STAGE, NW>(A, h ? split : pair_begin,
+                                                 h ? pair_end : split, blk, stab,
+                                                 wstage, rmax, sbuf, kept, flops,
+                                                 ints WB_STAGER_ARG, h, it);
+    }
+#else
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(A.work + CLS, 1);
@@ -538,6 +576,7 @@ cosx_class_kernel(const CosxArgs A, const int pair_begin, const int pair_end) {
                                                  wstage, rmax, sbuf, kept, flops,
                                                  ints WB_STAGER_ARG);
     }
+#endif
     // lane 0 counted the tasks (every lane runs every task) in units of the
     // 32-point sub-blocks they cover; every lane counted the flops /
     // integrals of its own pairs
@@ -637,10 +676,19 @@ cosx_class_kernel_batch(const CosxArgs* __restrict__ args,
             cur = m;
         }
         const CosxArgs& Am = sA[warp];
+#if WB_COSX_SPLIT
+        // the batched form does not split: one item per block, buffer set 0
+        cosx_class_block<LA, LB, FAR, STAGE, NW>(Am, Am.cls_pb[CLS], Am.cls_pe[CLS],
+                                                 item - item_off[m], stab, wstage,
+                                                 rmax, sbuf, kept, flops,
+                                                 ints WB_STAGER_ARG, 0,
+                                                 item - item_off[m]);
+#else
         cosx_class_block<LA, LB, FAR, STAGE, NW>(Am, Am.cls_pb[CLS], Am.cls_pe[CLS],
                                                  item - item_off[m], stab, wstage,
                                                  rmax, sbuf, kept, flops,
                                                  ints WB_STAGER_ARG);
+#endif
     }
     if (cur >= 0) flush();
 }

@@ -106,6 +106,9 @@ cudaError_t launch_xc_aow(const double* X, const double* v, int nao, int64_t ld,
                           int64_t npts, int mgga, float* G, cudaStream_t s);
 cudaError_t launch_gsum(const float* gc, const int4* src, int nao, int64_t ld,
                         float* G, cudaStream_t s);
+// the same over two buffer sets (the halves of split blocks), gc0 first
+cudaError_t launch_gsum2(const float* gc0, const float* gc1, const int4* src, int nao,
+                         int64_t ld, float* G, cudaStream_t s);
 cudaError_t launch_weight_g(const float* G, const double* w, int64_t npts,
                             int64_t ld, int nao, double* out, cudaStream_t s);
 cudaError_t launch_dense_impl(const CosxArgs& a, int npairs, const int* pclass,
