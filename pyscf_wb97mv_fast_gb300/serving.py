@@ -27,7 +27,9 @@ holds its pair tables and grid.  Admission keeps the sum of running
 footprints plus the resident session bytes under the budget (default 60 %
 of the free device memory, the reference's mem_fraction,
 gpu/install.py:209).  A request whose session could never fit is rejected
-at submit time.
+at submit time.  A session is admitted only when one of its own requests
+fits on top of it, so open sessions can never hold the whole budget while
+their requests wait.
 
 Determinism.  Every kernel of a build has a fixed summation order that
 does not depend on launch shape, block order or what else runs on the
@@ -115,20 +117,26 @@ class Scheduler:
             t.start()
 
     # -- resident bytes (sessions) ------------------------------------------
-    def reserve(self, nbytes, wait=False, timeout=None):
-        """Hold nbytes outside running jobs (an open session).  wait: block
+    def reserve(self, nbytes, wait=False, timeout=None, headroom=0):
+        """Hold nbytes outside running jobs (an open session).  headroom:
+        bytes that must fit on top of it at admission -- the footprint of
+        the session's own requests -- so that the most recently admitted
+        session can always run once the others' jobs end, and sessions
+        waiting on each other cannot starve every request.  wait: block
         until running jobs and other sessions leave room (a size above the
         whole budget is rejected at once); otherwise reject if it does not
         fit now."""
+        need = int(nbytes) + int(headroom)
         with self._cv:
             if self.budget is not None:
-                if nbytes > self.budget or not wait:
-                    if self.resident + nbytes > self.budget:
-                        raise Rejected('resident state of %d bytes exceeds the '
-                                       'budget (%d of %d bytes held)'
-                                       % (nbytes, self.resident, self.budget))
+                if need > self.budget or not wait:
+                    if self.resident + need > self.budget:
+                        raise Rejected('resident state of %d bytes (+ %d headroom) '
+                                       'exceeds the budget (%d of %d bytes held)'
+                                       % (nbytes, headroom, self.resident,
+                                          self.budget))
                 elif not self._cv.wait_for(
-                        lambda: self._used + self.resident + nbytes <= self.budget,
+                        lambda: self._used + self.resident + need <= self.budget,
                         timeout):
                     raise Rejected('no room for %d resident bytes within %s s'
                                    % (nbytes, timeout))
@@ -375,7 +383,7 @@ class ExchangeServer:
         with self._cuda.shared():
             s = Session(self, mol, coords, weights, omegas, tile_tol, graphs)
         try:
-            self._sched.reserve(s.resident, wait=True)
+            self._sched.reserve(s.resident, wait=True, headroom=s.footprint)
         except Rejected:
             with self._cuda.shared():
                 s.engine.close()

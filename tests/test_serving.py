@@ -143,3 +143,34 @@ def test_reserve_waits_for_room():
         s.reserve(101, wait=True)                # above the whole budget
     s.release(50)
     s.close()
+
+
+def test_session_headroom_prevents_starvation():
+    """Sessions hold resident bytes while their requests queue.  Admitting
+    a session only with room for its own request on top (headroom) keeps
+    the most recent session runnable: here three sessions of 20 resident +
+    50 per request share a budget of 100; without headroom the third
+    admission (60 resident) would leave no room for any request."""
+    rec = Recorder()
+    s = Scheduler(rec, slots=4, budget=100)
+    done = []
+
+    def session(name):
+        s.reserve(20, wait=True, timeout=10, headroom=50)
+        try:
+            for i in range(2):
+                s.submit(Job('%s%d' % (name, i), 50, key=name, dur=0.02)).result(10)
+        finally:
+            s.release(20)
+        done.append(name)
+
+    ts = [threading.Thread(target=session, args=(n,)) for n in 'abc']
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join(20)
+    assert sorted(done) == ['a', 'b', 'c']
+    assert s.max_used <= 100 and s.resident == 0
+    with pytest.raises(Rejected):
+        s.reserve(60, wait=True, headroom=50)       # can never fit
+    s.close()
