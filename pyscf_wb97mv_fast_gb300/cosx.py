@@ -23,6 +23,38 @@ def round32(n):
     return (int(n) + KSUB - 1) // KSUB * KSUB
 
 
+def device_arg(t, name, dtype, device, shape=None):
+    """t checked before its raw pointer goes to a native call, returned
+    contiguous: a torch tensor of dtype on device whose shape matches
+    (None entries match any extent).  The native calls read and write as
+    many elements as their size arguments say, so a host tensor, another
+    dtype or a short array must stop here with a Python error, not become
+    an out-of-bounds access in a kernel."""
+    torch = _torch()
+    if not isinstance(t, torch.Tensor):
+        raise TypeError('%s: a torch tensor on %s expected, got %s'
+                        % (name, device, type(t).__name__))
+    if t.device != device:
+        raise ValueError('%s is on %s, expected %s' % (name, t.device, device))
+    if t.dtype != dtype:
+        raise TypeError('%s is %s, expected %s' % (name, t.dtype, dtype))
+    if shape is not None and (t.dim() != len(shape) or any(
+            s is not None and int(a) != int(s) for a, s in zip(t.shape, shape))):
+        raise ValueError('%s has shape %s, expected (%s)'
+                         % (name, tuple(t.shape),
+                            ', '.join('*' if s is None else str(int(s)) for s in shape)))
+    return t.contiguous()
+
+
+def device_out(t, name, dtype, device, shape):
+    """An output buffer: as device_arg, and already contiguous (a copy
+    would not receive the result)."""
+    device_arg(t, name, dtype, device, shape)
+    if not t.is_contiguous():
+        raise ValueError('%s must be contiguous' % name)
+    return t
+
+
 def as_molecule(mol):
     """A Molecule from a Molecule or a PySCF Mole."""
     if isinstance(mol, Molecule):
@@ -118,6 +150,18 @@ class CosxEngine:
     def _stream():
         return _native.ctypes.c_void_p(_torch().cuda.current_stream().cuda_stream)
 
+    def _grid_args(self, coords_rel, weights):
+        """(coords_rel (npts, 3), weights (npts,)) FP64 on this engine's
+        device, checked and contiguous, and npts."""
+        torch = _torch()
+        c = device_arg(coords_rel, 'coords_rel', torch.float64, self.device, (None, 3))
+        n = int(c.shape[0])
+        w = device_arg(weights, 'weights', torch.float64, self.device, (n,))
+        return c, w, n
+
+    def _dm_arg(self, qd, name='qd'):
+        return device_arg(qd, name, _torch().float64, self.device, (self.nao, self.nao))
+
     # -- entry points ---------------------------------------------------------
     def get_k(self, coords_rel, weights, qd, omega, tile_tol=1e-11,
               tile_pts=0, gemm='ozaki', out=None, stats=True,
@@ -128,19 +172,21 @@ class CosxEngine:
         (FP64-accurate split on the bf16 tensor cores, default), 'native'
         (cuBLAS DGEMM) or 'emulated' (cuBLAS FP64 emulation)."""
         torch = _torch()
-        npts = int(coords_rel.shape[0])
+        coords_rel, weights, npts = self._grid_args(coords_rel, weights)
+        qd = self._dm_arg(qd)
         nbytes = self.workspace_bytes(npts, tile_pts)
         ws = self.workspace(nbytes)
         if out is None:
             out = torch.empty((self.nao, self.nao), dtype=torch.float64,
                               device=self.device)
+        device_out(out, 'out', torch.float64, self.device, (self.nao, self.nao))
         st = _native.WbCosxStats() if stats else None
         flags = _native.GEMM_MODES[gemm]
         if profile and stats:
             flags |= _native.WB_K_PROFILE
         _native.check(_native.lib().wb_cosx_get_k(
             self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
-            _native.ptr(qd.contiguous()), float(omega), float(tile_tol),
+            _native.ptr(qd), float(omega), float(tile_tol),
             int(tile_pts), flags, _native.ptr(out), _native.ptr(ws), nbytes,
             self._stream(), _native.ctypes.byref(st) if st is not None else None),
             'wb_cosx_get_k')
@@ -159,14 +205,14 @@ class CosxEngine:
         om = [float(w) for w in omegas]
         if not om:
             raise ValueError('omegas is empty')
-        npts = int(coords_rel.shape[0])
+        coords_rel, weights, npts = self._grid_args(coords_rel, weights)
+        qd = self._dm_arg(qd)
         nbytes = self.workspace_bytes(npts, tile_pts)
         ws = self.workspace(nbytes)
         if out is None:
             out = torch.empty((len(om), self.nao, self.nao), dtype=torch.float64,
                               device=self.device)
-        if tuple(out.shape) != (len(om), self.nao, self.nao) or not out.is_contiguous():
-            raise ValueError('out must be a contiguous (%d, nao, nao) tensor' % len(om))
+        device_out(out, 'out', torch.float64, self.device, (len(om), self.nao, self.nao))
         st = _native.WbCosxStats() if stats else None
         flags = _native.GEMM_MODES[gemm]
         if profile and stats:
@@ -174,7 +220,7 @@ class CosxEngine:
         arr = (_native.ctypes.c_double * len(om))(*om)
         _native.check(_native.lib().wb_cosx_get_k_multi(
             self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
-            _native.ptr(qd.contiguous()), len(om), arr, float(tile_tol),
+            _native.ptr(qd), len(om), arr, float(tile_tol),
             int(tile_pts), flags, _native.ptr(out), _native.ptr(ws), nbytes,
             self._stream(), _native.ctypes.byref(st) if st is not None else None),
             'wb_cosx_get_k_multi')
@@ -188,12 +234,13 @@ class CosxEngine:
         off), for the plain SGX K (dm the symmetric density, no projector);
         FP64 throughout (wb_cosx_k_grad)."""
         torch = _torch()
-        npts = int(coords_rel.shape[0])
+        coords_rel, weights, npts = self._grid_args(coords_rel, weights)
         natm = int(self.mol.natm)
         nbytes = int(_native.lib().wb_cosx_k_grad_workspace_bytes(self._h, npts, natm))
         ws = self.workspace(nbytes)
         out = torch.empty((natm, 3), dtype=torch.float64, device=self.device)
-        d = torch.as_tensor(dm, dtype=torch.float64, device=self.device).contiguous()
+        d = self._dm_arg(torch.as_tensor(dm, dtype=torch.float64, device=self.device),
+                         'dm')
         _native.check(_native.lib().wb_cosx_k_grad(
             self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
             _native.ptr(d), float(omega), float(tile_tol), natm, _native.ptr(out),
@@ -224,19 +271,19 @@ class CosxEngine:
         om = [float(w) for w in omegas]
         if not om:
             raise ValueError('omegas is empty')
-        npts = int(coords_rel.shape[0])
+        coords_rel, weights, npts = self._grid_args(coords_rel, weights)
+        qd = self._dm_arg(qd)
         nbytes = int(_native.lib().wb_cosx_fp64_workspace_bytes(self._h, npts))
         ws = self.workspace(nbytes)
         if out is None:
             out = torch.empty((len(om), self.nao, self.nao), dtype=torch.float64,
                               device=self.device)
-        if tuple(out.shape) != (len(om), self.nao, self.nao) or not out.is_contiguous():
-            raise ValueError('out must be a contiguous (%d, nao, nao) tensor' % len(om))
+        device_out(out, 'out', torch.float64, self.device, (len(om), self.nao, self.nao))
         st = _native.WbCosxStats() if stats else None
         arr = (_native.ctypes.c_double * len(om))(*om)
         _native.check(_native.lib().wb_cosx_get_k_fp64(
             self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
-            _native.ptr(qd.contiguous()), len(om), arr, float(tile_tol),
+            _native.ptr(qd), len(om), arr, float(tile_tol),
             _native.ptr(out), _native.ptr(ws), nbytes, self._stream(),
             _native.ctypes.byref(st) if st is not None else None),
             'wb_cosx_get_k_fp64')
@@ -248,20 +295,20 @@ class CosxEngine:
           stats=True):
         """G (nao, ld) FP32 from F (nao, ld) FP32 AO-major, one tile."""
         torch = _torch()
-        npts = int(coords_rel.shape[0])
+        coords_rel, weights, npts = self._grid_args(coords_rel, weights)
         ld = round32(npts)
-        if f.shape != (self.nao, ld) or f.dtype != torch.float32:
-            raise ValueError('f must be (nao, %d) float32' % ld)
+        f = device_arg(f, 'f', torch.float32, self.device, (self.nao, ld))
         # the G-only call needs no X / F / G buffers in the workspace
         nbytes = self.workspace_bytes(npts)
         ws = self.workspace(nbytes)
         if out is None:
             out = torch.empty((self.nao, ld), dtype=torch.float32,
                               device=self.device)
+        device_out(out, 'out', torch.float32, self.device, (self.nao, ld))
         st = _native.WbCosxStats() if stats else None
         _native.check(_native.lib().wb_cosx_g(
             self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
-            _native.ptr(f.contiguous()), float(omega), float(tile_tol),
+            _native.ptr(f), float(omega), float(tile_tol),
             _native.ptr(out), _native.ptr(ws), nbytes, self._stream(),
             _native.ctypes.byref(st) if st is not None else None), 'wb_cosx_g')
         if st is not None:
@@ -277,23 +324,20 @@ class CosxEngine:
         om = [float(w) for w in omegas]
         if not om:
             raise ValueError('omegas is empty')
-        npts = int(coords_rel.shape[0])
+        coords_rel, weights, npts = self._grid_args(coords_rel, weights)
         ld = round32(npts)
-        if f.shape != (self.nao, ld) or f.dtype != torch.float32:
-            raise ValueError('f must be (nao, %d) float32' % ld)
+        f = device_arg(f, 'f', torch.float32, self.device, (self.nao, ld))
         nbytes = self.workspace_bytes(npts)
         ws = self.workspace(nbytes)
         if out is None:
             out = torch.empty((len(om), self.nao, ld), dtype=torch.float32,
                               device=self.device)
-        if tuple(out.shape) != (len(om), self.nao, ld) or not out.is_contiguous():
-            raise ValueError('out must be a contiguous (%d, nao, %d) tensor'
-                             % (len(om), ld))
+        device_out(out, 'out', torch.float32, self.device, (len(om), self.nao, ld))
         st = _native.WbCosxStats() if stats else None
         arr = (_native.ctypes.c_double * len(om))(*om)
         _native.check(_native.lib().wb_cosx_g_multi(
             self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
-            _native.ptr(f.contiguous()), len(om), arr, float(tile_tol),
+            _native.ptr(f), len(om), arr, float(tile_tol),
             _native.ptr(out), _native.ptr(ws), nbytes, self._stream(),
             _native.ctypes.byref(st) if st is not None else None),
             'wb_cosx_g_multi')
@@ -304,12 +348,14 @@ class CosxEngine:
     def ozaki_f(self, X, qd):
         """F (nao, ld) FP32 = fl32(X QD) through the bf16 Ozaki split."""
         torch = _torch()
+        X = device_arg(X, 'X', torch.float64, self.device, (self.nao, None))
+        qd = self._dm_arg(qd)
         ld = int(X.shape[1])
         nbytes = int(_native.lib().wb_ozaki_workspace_bytes(self.nao, ld))
         ws = self.workspace(nbytes)
         out = torch.empty((self.nao, ld), dtype=torch.float32, device=self.device)
         _native.check(_native.lib().wb_cosx_ozaki_f(
-            self._h, _native.ptr(X), _native.ptr(qd.contiguous()), ld,
+            self._h, _native.ptr(X), _native.ptr(qd), ld,
             _native.ptr(out), _native.ptr(ws), nbytes, self._stream()),
             'wb_cosx_ozaki_f')
         return out
@@ -317,13 +363,19 @@ class CosxEngine:
     def ozaki_k(self, X, G, weights, out=None, accumulate=False):
         """K (nao, nao) FP64 = X^T (w o G) through the bf16 Ozaki split."""
         torch = _torch()
-        npts = int(weights.shape[0])
+        X = device_arg(X, 'X', torch.float64, self.device, (self.nao, None))
         ld = int(X.shape[1])
+        G = device_arg(G, 'G', torch.float32, self.device, (self.nao, ld))
+        weights = device_arg(weights, 'weights', torch.float64, self.device, (None,))
+        npts = int(weights.shape[0])
+        if npts > ld:
+            raise ValueError('%d weights for %d columns of X' % (npts, ld))
         nbytes = int(_native.lib().wb_ozaki_workspace_bytes(self.nao, ld))
         ws = self.workspace(nbytes)
         if out is None:
             out = torch.zeros((self.nao, self.nao), dtype=torch.float64,
                               device=self.device)
+        device_out(out, 'out', torch.float64, self.device, (self.nao, self.nao))
         _native.check(_native.lib().wb_cosx_ozaki_k(
             self._h, _native.ptr(X), _native.ptr(G), _native.ptr(weights), npts,
             1 if accumulate else 0, _native.ptr(out), _native.ptr(ws), nbytes,
@@ -333,10 +385,13 @@ class CosxEngine:
     def ao_eval(self, coords_rel, out=None):
         """X (nao, ld) FP64 AO-major."""
         torch = _torch()
+        coords_rel = device_arg(coords_rel, 'coords_rel', torch.float64, self.device,
+                                (None, 3))
         npts = int(coords_rel.shape[0])
         if out is None:
             out = torch.empty((self.nao, round32(npts)), dtype=torch.float64,
                               device=self.device)
+        device_out(out, 'out', torch.float64, self.device, (self.nao, round32(npts)))
         _native.check(_native.lib().wb_ao_eval(
             self._h, _native.ptr(coords_rel), npts, _native.ptr(out),
             self._stream()), 'wb_ao_eval')
@@ -345,10 +400,13 @@ class CosxEngine:
     def ao_eval_deriv1(self, coords_rel, out=None):
         """X and its gradients (4, nao, ld) FP64 AO-major."""
         torch = _torch()
+        coords_rel = device_arg(coords_rel, 'coords_rel', torch.float64, self.device,
+                                (None, 3))
         npts = int(coords_rel.shape[0])
         if out is None:
             out = torch.empty((4, self.nao, round32(npts)), dtype=torch.float64,
                               device=self.device)
+        device_out(out, 'out', torch.float64, self.device, (4, self.nao, round32(npts)))
         _native.check(_native.lib().wb_ao_eval_deriv1(
             self._h, _native.ptr(coords_rel), npts, _native.ptr(out),
             self._stream()), 'wb_ao_eval_deriv1')
@@ -358,10 +416,15 @@ class CosxEngine:
         """Semilocal XC density parameters (5, ld) FP64 (rho, grad, tau) from
         X (4, nao, ld) FP64 and T (1 or 4, nao, ld) FP32 = fl32(dm^T X_d)."""
         torch = _torch()
+        X = device_arg(X, 'X', torch.float64, self.device, (4, self.nao, None))
         ld = int(X.shape[2])
+        T = device_arg(T, 'T', torch.float32, self.device, (None, self.nao, ld))
+        if T.shape[0] < (4 if mgga else 1) or not 0 <= int(npts) <= ld:
+            raise ValueError('T needs %d planes and npts <= %d'
+                             % (4 if mgga else 1, ld))
         out = torch.empty((5, ld), dtype=torch.float64, device=self.device)
         _native.check(_native.lib().wb_xc_rho(
-            self._h, _native.ptr(X), _native.ptr(T.contiguous()), int(npts), ld,
+            self._h, _native.ptr(X), _native.ptr(T), int(npts), ld,
             1 if mgga else 0, _native.ptr(out), self._stream()), 'wb_xc_rho')
         return out
 
@@ -369,11 +432,15 @@ class CosxEngine:
         """Fock-side planes (1 or 4, nao, ld) FP32 from X and the
         density-parameter derivatives v (5, ld) FP64."""
         torch = _torch()
+        X = device_arg(X, 'X', torch.float64, self.device, (4, self.nao, None))
         ld = int(X.shape[2])
+        v = device_arg(v, 'v', torch.float64, self.device, (5, ld))
+        if not 0 <= int(npts) <= ld:
+            raise ValueError('npts must be in [0, %d]' % ld)
         out = torch.empty((4 if mgga else 1, self.nao, ld), dtype=torch.float32,
                           device=self.device)
         _native.check(_native.lib().wb_xc_aow(
-            self._h, _native.ptr(X), _native.ptr(v.contiguous()), int(npts), ld,
+            self._h, _native.ptr(X), _native.ptr(v), int(npts), ld,
             1 if mgga else 0, _native.ptr(out), self._stream()), 'wb_xc_aow')
         return out
 
@@ -381,6 +448,8 @@ class CosxEngine:
         """Dense (npts, nao, nao) FP32 contracted spherical integrals
         (validation only; refuses more than 2 GiB)."""
         torch = _torch()
+        coords_rel = device_arg(coords_rel, 'coords_rel', torch.float64, self.device,
+                                (None, 3))
         npts = int(coords_rel.shape[0])
         need = npts * self.nao * self.nao * 4
         if need > (2 << 30):
@@ -428,7 +497,11 @@ class KBuildGraph:
         """dm (nao, nao) FP64, host or device -> symmetrised K on the device
         (this graph's output buffer)."""
         torch = _torch()
-        self.qd.copy_(torch.as_tensor(dm, dtype=torch.float64), non_blocking=True)
+        dm = torch.as_tensor(dm, dtype=torch.float64)
+        if tuple(dm.shape) != tuple(self.qd.shape):
+            raise ValueError('dm has shape %s, expected %s'
+                             % (tuple(dm.shape), tuple(self.qd.shape)))
+        self.qd.copy_(dm, non_blocking=True)
         self.graph.replay()
         return self.out
 
@@ -463,7 +536,7 @@ class CosxBatch:
         self.omegas = tuple(float(w) for w in omegas)
         if len(self.omegas) not in (1, 2):
             raise ValueError('1 or 2 omegas')
-        self._grids = [(c.contiguous(), w.contiguous()) for c, w in grids]
+        self._grids = [e._grid_args(c, w)[:2] for e, (c, w) in zip(self.engines, grids)]
         n = len(self.engines)
         dev = self.engines[0].device
         P = _native.ctypes.c_void_p
@@ -502,10 +575,11 @@ class CosxBatch:
             out = [torch.empty((len(self.omegas), e.nao, e.nao), dtype=torch.float64,
                                device=self.device) for e in self.engines]
         P = _native.ctypes.c_void_p
-        qd_c = [q.contiguous() for q in qds]
-        for q, e in zip(qd_c, self.engines):
-            if tuple(q.shape) != (e.nao, e.nao):
-                raise ValueError('density of the wrong shape')
+        qd_c = [e._dm_arg(q) for q, e in zip(qds, self.engines)]
+        if len(out) != n:
+            raise ValueError('one output per molecule')
+        for k, e in zip(out, self.engines):
+            device_out(k, 'out', torch.float64, e.device, (len(self.omegas), e.nao, e.nao))
         st = _native.WbCosxStats() if stats else None
         _native.check(_native.lib().wb_cosx_batch_run(
             self._b, (P * n)(*[q.data_ptr() for q in qd_c]),

@@ -41,6 +41,7 @@ class Vv10Kernel:
     def kernel_sum(self, coords, q, W0, kappa):
         """coords (P, 3), q, W0, kappa (P,) on the device -> F, U, W FP64."""
         torch = _torch()
+        _check_points(coords, 'coords')
         dev = coords.device
         n = int(coords.shape[0])
         F = torch.zeros(n, dtype=torch.float64, device=dev)
@@ -50,8 +51,8 @@ class Vv10Kernel:
             self.last_pairs_kept = (0, 0)
             return F, U, W
         xyz = coords.to(torch.float32).contiguous()
-        q32, w32, k32 = (torch.as_tensor(a, device=dev).to(torch.float32).contiguous()
-                         for a in (q, W0, kappa))
+        q32, w32, k32 = (_per_point(a, n, dev, name) for a, name in
+                         ((q, 'q'), (W0, 'W0'), (kappa, 'kappa')))
         kept = _native.ctypes.c_int64()
         stream = _native.ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
         _native.check(_native.lib().wb_vv10_kernel_sum(
@@ -68,14 +69,20 @@ class Vv10Kernel:
         U, W (each molecule's sums over its own points only; bitwise equal
         to kernel_sum per molecule)."""
         torch = _torch()
+        if not coords or not len(coords) == len(q) == len(W0) == len(kappa):
+            raise ValueError('one coords, q, W0 and kappa array per molecule')
+        for c in coords:
+            _check_points(c, 'coords')
         sizes = [int(c.shape[0]) for c in coords]
         dev = coords[0].device
+        if any(c.device != dev for c in coords):
+            raise ValueError('coords of one batch must share a device')
         offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
         n = int(offsets[-1])
         xyz = torch.cat([c.to(torch.float32) for c in coords]).contiguous()
-        q32, w32, k32 = (torch.cat([torch.as_tensor(a, device=dev).to(torch.float32)
-                                    for a in arrs]).contiguous()
-                         for arrs in (q, W0, kappa))
+        q32, w32, k32 = (torch.cat([_per_point(a, m, dev, name)
+                                    for a, m in zip(arrs, sizes)]).contiguous()
+                         for arrs, name in ((q, 'q'), (W0, 'W0'), (kappa, 'kappa')))
         F = torch.zeros(n, dtype=torch.float64, device=dev)
         U = torch.zeros_like(F)
         W = torch.zeros_like(F)
@@ -89,6 +96,26 @@ class Vv10Kernel:
         self.last_pairs_kept = (int(kept.value), int(sum(m * m for m in sizes)))
         sl = [slice(int(offsets[i]), int(offsets[i + 1])) for i in range(len(sizes))]
         return [F[x] for x in sl], [U[x] for x in sl], [W[x] for x in sl]
+
+
+def _check_points(coords, name):
+    """coords must be an (n, 3) torch tensor on a CUDA device: the kernels
+    read its raw pointer."""
+    torch = _torch()
+    if not isinstance(coords, torch.Tensor) or not coords.is_cuda:
+        raise ValueError('%s must be a torch tensor on a CUDA device' % name)
+    if coords.dim() != 2 or coords.shape[1] != 3:
+        raise ValueError('%s has shape %s, expected (n, 3)'
+                         % (name, tuple(coords.shape)))
+
+
+def _per_point(a, n, dev, name):
+    """A per-point array (n,) as contiguous FP32 on dev."""
+    torch = _torch()
+    t = torch.as_tensor(a, device=dev).to(torch.float32).contiguous()
+    if t.dim() != 1 or t.shape[0] != n:
+        raise ValueError('%s has shape %s, expected (%d,)' % (name, tuple(t.shape), n))
+    return t
 
 
 def vv10_pointwise(rho0, grad, weights, nlc_pars):
