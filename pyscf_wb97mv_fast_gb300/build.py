@@ -5,7 +5,9 @@
 Translation units compile in parallel; the class kernels are regenerated
 first (csrc/gen_cosx.py).  Objects go to _build/ at the repository root, the
 library to pyscf_wb97mv_fast_gb300/_lib/.  Nothing is rebuilt when the
-sources are older than the library.
+sources are older than the library and the compile flags (WB_NVCC_EXTRA
+included) are those it was built with, recorded beside it in
+libwb97mv_gb300.so.flags.
 """
 import concurrent.futures
 import os
@@ -59,6 +61,20 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _flags():
+    """The flags that change the code: architecture and WB_NVCC_EXTRA
+    (e.g. WB_NVCC_EXTRA=-DWB_COSX_SPLIT=1)."""
+    return ARCH + os.environ.get('WB_NVCC_EXTRA', '').split()
+
+
+def _flags_changed(lib):
+    try:
+        with open(lib + '.flags') as fh:
+            return fh.read() != ' '.join(_flags())
+    except OSError:
+        return True
+
+
 def build(verbose=False, force=False, jobs=None):
     """Compile and link; returns the library path."""
     sys.path.insert(0, CSRC)
@@ -69,7 +85,7 @@ def build(verbose=False, force=False, jobs=None):
     gen_cosx.write()
     lib = library_path()
     deps = _deps()
-    if not force and not _stale(lib, deps):
+    if not force and not _stale(lib, deps) and not _flags_changed(lib):
         return lib
     home = cuda_home()
     nvcc = os.path.join(home, 'bin', 'nvcc')
@@ -104,6 +120,8 @@ def build(verbose=False, force=False, jobs=None):
     if res.returncode != 0:
         raise RuntimeError('link failed:\n%s\n%s' % (res.stdout, res.stderr))
     os.replace(tmp, lib)
+    with open(lib + '.flags', 'w') as fh:
+        fh.write(' '.join(_flags()))
     return lib
 
 
