@@ -11,6 +11,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -86,7 +87,17 @@ int device_boys(int dev, float4** out) {
     return WB_OK;
 }
 
+// the __constant__ tables (cart->sph, exp) per device, uploaded once per
+// process: a handle created on one thread must not rewrite constant memory
+// that another thread's kernels are reading
+std::mutex g_const_mu;
+std::set<int> g_const_dev;
+
 int upload_constants() {
+    int dev = 0;
+    WB_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_const_mu);
+    if (g_const_dev.count(dev)) return WB_OK;
     std::vector<double> c[4];
     for (int l = 0; l < 4; ++l) c[l] = wb::cart2sph(l);
     WB_CUDA(wb::upload_c2s_tables(c[0].data(), c[1].data(), c[2].data(),
@@ -100,6 +111,7 @@ int upload_constants() {
     for (int j = 0; j < 64; ++j)
         t64[j] = (double)std::exp2l(-(long double)j / 64.0L);   // rounded once
     WB_CUDA(wb::upload_exp_table(t64));
+    g_const_dev.insert(dev);
     return WB_OK;
 }
 

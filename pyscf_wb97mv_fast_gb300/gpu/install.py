@@ -12,7 +12,10 @@ dispatcher: the SGX objects of this mf (``mf.with_df`` and the long-range
 copies in ``mf.with_df._rsh_df``) go to ``GpuKBuilder`` (FP32 fused
 kernels, screened with k_tile_tol, FP64 GEMMs); every other SGX object keeps
 the original.  ``vv10=True`` (default) replaces ``mf._numint.nr_nlc_vxc`` by
-the GPU VV10 flow.
+the GPU VV10 flow.  ``overlap=True`` (default, as in the reference) wraps
+``mf.get_veff`` so that the semilocal XC and VV10 flows run on a worker
+thread, on their own CUDA stream, while this thread builds J and K with the
+K flow on another stream (reference :138-206).
 
 Deliberate contract change: no CPU fallback.  An error in a GPU flow of
 this mf propagates (Unsupported, NativeError, DeviceOutOfMemory) -- after
@@ -20,7 +23,11 @@ the out-of-memory retry, which halves the grid tile twice like the
 reference's _run_with_oom_retry (:99-109).  Importing this module does not
 import PySCF; ``install_gpu`` does.
 """
-import warnings
+import contextlib
+import threading
+import time
+
+import numpy as np
 
 from pyscf_wb97mv_fast_gb300.core.hooks import HookSet
 from pyscf_wb97mv_fast_gb300.gpu import sgx_k as sgx_k_mod
@@ -53,6 +60,132 @@ def _run_with_oom_retry(flow, builder):
     raise last
 
 
+def flow_streams():
+    """A factory of per-flow stream contexts: stream('k') / stream('xc')
+    makes the calling thread's device work run on a private stream of that
+    name (one per name and device, created on first use), after the work
+    already queued on the thread's current stream.  Each flow then waits
+    only for its own kernels when it reads a result back to the host, so
+    the K build and the XC / VV10 flows overlap on the device.  Without a
+    CUDA device it selects nothing: the flows themselves raise there."""
+    streams = {}
+    lock = threading.Lock()
+
+    def stream(name):
+        torch = sgx_k_mod._torch()
+        if not torch.cuda.is_available():
+            return contextlib.nullcontext()
+        dev = torch.cuda.current_device()
+        with lock:
+            s = streams.get((name, dev))
+            if s is None:
+                s = streams[(name, dev)] = torch.cuda.Stream(device=dev)
+        s.wait_stream(torch.cuda.current_stream(dev))
+        return torch.cuda.stream(s)
+    return stream
+
+
+_ABSENT = object()
+
+
+def _zero_xc(nao):
+    """Stands in for nr_rks / nr_nlc_vxc while the stock get_veff builds J
+    and K: no electrons, no energy, a zero potential."""
+    def zero(*args, **kwargs):
+        return 0, 0.0, np.zeros((nao, nao))
+    return zero
+
+
+def retag(like, arr, **override):
+    """arr with the tags of like (PySCF's tag_array attributes: ecoul,
+    exc, vj, vk), some of them replaced.  PySCF's lib.tag_array when PySCF
+    imports, else a view of arr as like's array type."""
+    tags = dict(getattr(like, '__dict__', {}))
+    tags.update(override)
+    try:
+        from pyscf import lib
+    except ImportError:
+        out = np.asarray(arr).view(type(like))
+        out.__dict__.update(tags)
+        return out
+    return lib.tag_array(arr, **tags)
+
+
+def _overlap_factory(mf, ni, timings, stream):
+    """mf.get_veff with the XC and VV10 flows on a worker thread.
+
+    The stock get_veff runs on this thread with ni.nr_rks and
+    ni.nr_nlc_vxc answering zero, so it builds J, K (through the K hook)
+    and the Coulomb and exchange energies only; the worker computes exc and
+    vxc of the same density meanwhile, and they are added afterwards (the
+    same sums in another order).  The C-ABI calls and PySCF's J/K release
+    the GIL, so both run at once.  Each call appends {'jk', 'xc', 'wait'}
+    wall seconds to timings: J/K on this thread, XC + VV10 on the worker,
+    and the wait for the worker after J/K.  A worker error is raised here.
+    Densities the flows do not take (hermi=2, several densities) go to the
+    stock get_veff unchanged."""
+    def factory(orig):
+        def get_veff(mol=None, dm=None, dm_last=None, vhf_last=None, hermi=1):
+            if mol is None:
+                mol = mf.mol
+            if dm is None:
+                dm = mf.make_rdm1()
+            if hermi == 2 or not (isinstance(dm, np.ndarray) and dm.ndim == 2):
+                return orig(mol, dm, dm_last, vhf_last, hermi)
+            # the grids as the stock get_veff would set them up
+            if mf.grids.coords is None:
+                mf.initialize_grids(mol, dm)
+            nlc = bool(mf.do_nlc())
+            if nlc and mf.nlcgrids.coords is None:
+                mf.nlcgrids.build(with_non0tab=True)
+            nlc_code = None
+            if nlc:
+                nlc_code = mf.xc if ni.libxc.is_nlc(mf.xc) else mf.nlc
+            xc_flow, nlc_flow = ni.nr_rks, ni.nr_nlc_vxc
+            res = {}
+
+            def worker():
+                t0 = time.perf_counter()
+                try:
+                    with stream('xc'):
+                        _, exc, vxc = xc_flow(mol, mf.grids, mf.xc, dm)
+                        if nlc:
+                            _, enlc, vnlc = nlc_flow(mol, mf.nlcgrids, nlc_code, dm)
+                            exc = exc + enlc
+                            vxc = vxc + vnlc
+                    res['xc'] = (exc, vxc)
+                except BaseException as err:           # noqa: BLE001
+                    res['error'] = err
+                res['t'] = time.perf_counter() - t0
+
+            th = threading.Thread(target=worker, name='wb-xc', daemon=True)
+            th.start()
+            # the instance's own entries, put back exactly afterwards (a
+            # method of the class shows through again)
+            own = {n: vars(ni).get(n, _ABSENT) for n in ('nr_rks', 'nr_nlc_vxc')}
+            zero = _zero_xc(dm.shape[0])
+            ni.nr_rks = ni.nr_nlc_vxc = zero
+            t0 = time.perf_counter()
+            try:
+                veff = orig(mol, dm, dm_last, vhf_last, hermi)
+            finally:
+                for n, v in own.items():
+                    if v is _ABSENT:
+                        delattr(ni, n)
+                    else:
+                        setattr(ni, n, v)
+                t1 = time.perf_counter()
+                th.join()
+            timings.append({'jk': t1 - t0, 'xc': res.get('t'),
+                            'wait': time.perf_counter() - t1})
+            if 'error' in res:
+                raise res['error']
+            exc, vxc = res['xc']
+            return retag(veff, np.asarray(veff) + vxc, exc=veff.exc + exc)
+        return get_veff
+    return factory
+
+
 def _sgx_jk_module():
     import pyscf.sgx.sgx_jk as mod
     return mod
@@ -79,7 +212,7 @@ def rsh_omegas(mf):
 def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
                 functional_factory=None, verify_ao=True,
                 gemm_dtype='float64', dtype='float32',
-                mem_fraction=DEFAULT_MEM_FRACTION, overlap=False,
+                mem_fraction=DEFAULT_MEM_FRACTION, overlap=True,
                 semilocal=True, k=True, k_tile_tol=1e-11,
                 openblas_threads=None, vv10=True, k_gemm='ozaki',
                 sgx_jk_module=None, k_omegas='auto', k_precision='fp32'):
@@ -95,13 +228,17 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
     omegas); 'auto' reads them from the range-separated functional of mf
     ((0, omega) when it has one), None builds one K per call.
     k_precision (an addition): 'fp32' (the mixed-precision K) or 'fp64'
-    (the plain FP64 GPU form, for an FP64 tail on the GPU).
+    (the plain FP64 GPU form, for an FP64 tail on the GPU).  overlap=True
+    wraps mf.get_veff (DFT objects only: mf.initialize_grids exists) to run
+    the XC and VV10 flows beside J/K, and fills hooks.timings.
     """
     if backend not in (None, 'cuda', 'cupy'):
         raise ValueError("backend must be None or 'cuda'")
     hooks = HookSet()
     hooks.k_stats = []
-    hooks.timings = []
+    hooks.timings = []        # overlap: one {'jk', 'xc', 'wait'} per get_veff
+    # overlap puts the K flow and the XC / VV10 flows on streams of their own
+    stream = flow_streams() if overlap else (lambda name: contextlib.nullcontext())
     if k:
         mod = sgx_jk_module if sgx_jk_module is not None else _sgx_jk_module()
         holder = {}
@@ -133,7 +270,8 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
                                                   direct_scf_tol=direct_scf_tol)
                     stats.update(bb.last_stats)
                     return kk
-                kk = _run_with_oom_retry(flow, b)
+                with stream('k'):
+                    kk = _run_with_oom_retry(flow, b)
                 hooks.k_stats.append(dict(stats))
                 return kk
             return get_k_only
@@ -168,10 +306,11 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
                                                verbose)
             return nr_nlc_vxc
         hooks.wrap(ni, 'nr_nlc_vxc', nlc_factory)
-    if overlap:
-        warnings.warn('overlap=True has no effect: the K, XC and VV10 '
-                      'flows run one after another on the device',
-                      RuntimeWarning)
+    if overlap and hasattr(mf, 'initialize_grids'):
+        ni = getattr(mf, '_numint', None)
+        if ni is None:
+            raise TypeError('mf has no _numint; not a DFT object?')
+        hooks.wrap(mf, 'get_veff', _overlap_factory(mf, ni, hooks.timings, stream))
     return hooks
 
 
