@@ -186,6 +186,19 @@ def _overlap_factory(mf, ni, timings, stream):
     return factory
 
 
+def check_scope(mol):
+    """Raise Unsupported now, at install time, for a molecule the GPU
+    flows do not take: a Cartesian basis, spinor shells, l above 3
+    (Molecule.from_pyscf).  Host-only; the reference raises the same
+    exception from its first K build (gpu/sgx_k.py:680-695)."""
+    from pyscf_wb97mv_fast_gb300 import _native
+    from pyscf_wb97mv_fast_gb300.cosx import as_molecule
+    try:
+        as_molecule(mol)
+    except (ValueError, TypeError) as err:
+        raise _native.Unsupported(_native.WB_ERR_UNSUPPORTED, str(err)) from err
+
+
 def _sgx_jk_module():
     import pyscf.sgx.sgx_jk as mod
     return mod
@@ -234,6 +247,8 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
     """
     if backend not in (None, 'cuda', 'cupy'):
         raise ValueError("backend must be None or 'cuda'")
+    if getattr(mf, 'mol', None) is not None and (k or semilocal or vv10):
+        check_scope(mf.mol)
     hooks = HookSet()
     hooks.k_stats = []
     hooks.timings = []        # overlap: one {'jk', 'xc', 'wait'} per get_veff

@@ -4,6 +4,7 @@ import subprocess
 import sys
 import types
 
+import numpy as np
 import pytest
 
 from pyscf_wb97mv_fast_gb300.core.hooks import HookSet, reset_diis, track_residual
@@ -202,3 +203,75 @@ def test_builder_pending_set_only_matches_same_inputs():
     b._pending = (key, dm.copy(), proj.copy(), {0.3: K})
     assert b._take_pending(key, dm, proj, 0.3) is K           # hit, consumed
     assert b._pending is None
+
+
+class FakeMole:
+    """PySCF Mole accessors over a Molecule (the ones Molecule.from_pyscf
+    reads), with switches for the inputs the GPU path refuses."""
+
+    def __init__(self, mol, cart=False, kappa=0, extra_l=None):
+        self._m = mol
+        self.cart = cart
+        self.basis = 'fake'
+        self._shells = list(mol.shells)
+        if extra_l is not None:
+            from pyscf_wb97mv_fast_gb300.basis import Shell
+            self._shells.append(Shell(0, extra_l, [1.0], [[1.0]]))
+        self._kappa = kappa
+        self._bas = np.asarray([[sh.atom, sh.l, sh.nprim, sh.nctr]
+                                for sh in self._shells], dtype=np.int32)
+        self.natm = mol.natm
+        self.nbas = len(self._shells)
+
+    def bas_kappa(self, i):
+        return self._kappa
+
+    def bas_angular(self, i):
+        return self._shells[i].l
+
+    def bas_exp(self, i):
+        return self._shells[i].exps
+
+    def _libcint_ctr_coeff(self, i):
+        return self._shells[i].coeffs
+
+    def atom_symbol(self, i):
+        return self._m.symbols[i]
+
+    def atom_coords(self):
+        return self._m.atom_coords()
+
+
+def test_from_pyscf_reads_a_mole_back():
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.systems import water_dimer
+    mol = Molecule.build(water_dimer(), 'synthetic-tzvp', gen_contract=True)
+    back = Molecule.from_pyscf(FakeMole(mol))
+    a, b = mol.packed(), back.packed()
+    assert back.nao == mol.nao and set(a) == set(b)
+    for key in a:
+        assert np.array_equal(a[key], b[key]), key
+
+
+@pytest.mark.parametrize('bad', ['cart', 'spinor', 'l4', 'not_a_mole'])
+def test_install_refuses_out_of_scope_molecules_up_front(bad):
+    from pyscf_wb97mv_fast_gb300 import _native
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.gpu.install import install_gpu
+    from pyscf_wb97mv_fast_gb300.systems import water_dimer
+    mol = Molecule.build(water_dimer(), 'synthetic-svp')
+    fake = {'cart': lambda: FakeMole(mol, cart=True),
+            'spinor': lambda: FakeMole(mol, kappa=-1),
+            'l4': lambda: FakeMole(mol, extra_l=4),
+            'not_a_mole': lambda: object()}[bad]()
+    mf, _ = _fake_mf()
+    mf.mol = fake
+    mod = types.ModuleType('fake_sgx_jk')
+    mod.get_k_only = lambda *a: None
+    orig = mod.get_k_only
+    with pytest.raises(_native.Unsupported):
+        install_gpu(mf, k=True, semilocal=False, vv10=False, sgx_jk_module=mod)
+    assert mod.get_k_only is orig                  # nothing was hooked
+    mf.mol = FakeMole(mol)                         # in scope: installs
+    install_gpu(mf, k=True, semilocal=False, vv10=False,
+                sgx_jk_module=mod).restore_all()
