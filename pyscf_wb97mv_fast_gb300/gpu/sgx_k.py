@@ -151,9 +151,15 @@ class GpuKBuilder:
         return st
 
     def get_k(self, sgx, dm, omega, hermi=1, direct_scf_tol=1e-13):
-        """K (nao, nao) FP64 host for one RKS density matrix on sgx's grid."""
+        """K (nao, nao) FP64 host for one RKS density matrix on sgx's grid.
+        With PYSCF_WB97MV_KPROFILE=1 each phase ends with a synchronisation
+        of the flow's stream and last_stats['phases'] holds its seconds
+        (checks, build, pjs, grid_state, proj_dm, kernel, post, to_host),
+        with the device phases of the kernel call in last_stats['phase_ms']
+        (reference gpu/sgx_k.py:667-679)."""
         t0 = time.perf_counter()
         torch = _torch()
+        lap = _Laps(torch) if profiling_enabled() else None
         if hermi != 1:
             raise Unsupported(_native.WB_ERR_UNSUPPORTED,
                               'GPU COSX K supports hermi=1 only')
@@ -164,7 +170,11 @@ class GpuKBuilder:
         if not np.allclose(dm, dm.T, rtol=0, atol=1e-12):
             raise Unsupported(_native.WB_ERR_UNSUPPORTED,
                               'GPU COSX K needs a symmetric density matrix')
+        if lap:
+            lap('checks')
         self._build()
+        if lap:
+            lap('build')
         if dm.shape[0] != self.nao:
             raise Unsupported(_native.WB_ERR_UNSUPPORTED,
                               'dm does not match the molecule')
@@ -178,7 +188,11 @@ class GpuKBuilder:
             pjs = sgx._pjs_data
         proj = np.asarray(pjs._overlap_correction_matrix, dtype=np.float64)
         sym = bool(pjs.sym_ovlp)
+        if lap:
+            lap('pjs')
         state = self._grid_state(grids)
+        if lap:
+            lap('grid_state')
         key = (state.fingerprint, sym, self.tile_tol, self.gemm, self.precision)
         omega = float(omega)
         hit = self._take_pending(key, dm, proj, omega)
@@ -192,6 +206,8 @@ class GpuKBuilder:
         dev = self.engine.device
         proj_d = torch.as_tensor(proj, device=dev)
         qd = proj_d @ torch.as_tensor(dm, dtype=torch.float64, device=dev)
+        if lap:
+            lap('proj_dm')
         tk0 = time.perf_counter()
         multi = self.omegas is not None and omega in self.omegas and len(self.omegas) > 1
         if self.precision == 'fp64':
@@ -202,16 +218,22 @@ class GpuKBuilder:
             Ks = self.engine.get_k_multi(state.coords, state.weights, qd,
                                          self.omegas, tile_tol=self.tile_tol,
                                          tile_pts=self._tile(state.ngrids),
-                                         gemm=self.gemm)
+                                         gemm=self.gemm, profile=bool(lap))
         else:
             Ks = self.engine.get_k(state.coords, state.weights, qd, omega,
                                    tile_tol=self.tile_tol,
                                    tile_pts=self._tile(state.ngrids),
-                                   gemm=self.gemm)[None]
+                                   gemm=self.gemm, profile=bool(lap))[None]
+        if lap:
+            lap('kernel')
         if sym:
             Ks = proj_d.T[None] @ Ks
         Ks = (Ks + Ks.transpose(1, 2)) * 0.5
+        if lap:
+            lap('post')
         Kh = Ks.cpu().numpy()
+        if lap:
+            lap('to_host')
         if multi:
             done = {w: Kh[j] for j, w in enumerate(self.omegas) if w != omega}
             self._pending = (key, dm.copy(), proj.copy(), done)
@@ -223,6 +245,8 @@ class GpuKBuilder:
         st['wall'] = time.perf_counter() - t0
         st['kernel'] = time.perf_counter() - tk0
         st['from_multi'] = False
+        if lap:
+            st['phases'] = lap.phases
         self.last_stats = st
         return Kh
 
@@ -291,3 +315,23 @@ class SyntheticSGX:
 
 def profiling_enabled():
     return os.environ.get('PYSCF_WB97MV_KPROFILE') == '1'
+
+
+class _Laps:
+    """lap(name): synchronise this thread's current CUDA stream and book the
+    seconds since the previous lap under name (phase timing of get_k)."""
+
+    def __init__(self, torch):
+        self._torch = torch
+        self.phases = {}
+        self._t = time.perf_counter()
+
+    def _sync(self):
+        if self._torch.cuda.is_available():
+            self._torch.cuda.current_stream().synchronize()
+
+    def __call__(self, name):
+        self._sync()
+        t = time.perf_counter()
+        self.phases[name] = self.phases.get(name, 0.0) + (t - self._t)
+        self._t = t
