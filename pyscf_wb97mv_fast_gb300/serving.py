@@ -50,11 +50,20 @@ class Rejected(ValueError):
     budget) or a server that is closed."""
 
 
+class Cancelled(Exception):
+    """A request cancelled before it started (Future.cancel)."""
+
+
+class Expired(TimeoutError):
+    """A request whose deadline passed before it started."""
+
+
 class Future:
     """Result handle of one request."""
 
-    def __init__(self, tag=None):
+    def __init__(self, tag=None, sched=None):
         self.tag = tag
+        self._sched = sched
         self._ev = threading.Event()
         self._value = None
         self._error = None
@@ -69,6 +78,12 @@ class Future:
 
     def done(self):
         return self._ev.is_set()
+
+    def cancel(self):
+        """Drop the request if it has not started: True, and result()
+        raises Cancelled.  False once it runs or is finished (a started
+        build is never interrupted on the device)."""
+        return self._sched is not None and self._sched._cancel(self)
 
     def result(self, timeout=None):
         if not self._ev.wait(timeout):
@@ -148,8 +163,12 @@ class Scheduler:
             self._cv.notify_all()
 
     # -- jobs ------------------------------------------------------------------
-    def submit(self, job, tag=None):
-        fut = Future(tag)
+    def submit(self, job, tag=None, deadline=None):
+        """Queue job; returns its Future.  deadline: seconds from now by
+        which the job must have started, else it is dropped and result()
+        raises Expired."""
+        fut = Future(tag, self)
+        t_end = None if deadline is None else fut.t_submit + float(deadline)
         with self._cv:
             if self._closed:
                 raise Rejected('scheduler is closed')
@@ -157,9 +176,37 @@ class Scheduler:
                 raise Rejected('request footprint %d bytes (+ %d resident) exceeds '
                                'the budget of %d bytes' % (job.footprint,
                                                            self.resident, self.budget))
-            self._queue.append((job, fut))
+            self._queue.append((job, fut, t_end))
             self._cv.notify_all()
         return fut
+
+    def _cancel(self, fut):
+        with self._cv:
+            for i, item in enumerate(self._queue):
+                if item[1] is fut:
+                    del self._queue[i]
+                    fut._finish(error=Cancelled('request cancelled before it started'))
+                    self._cv.notify_all()
+                    return True
+        return False
+
+    def _expire(self, now):
+        """Finish the queued jobs whose deadline has passed; returns the
+        seconds to the next deadline (None: no deadline queued)."""
+        keep, nxt = collections.deque(), None
+        for item in self._queue:
+            t_end = item[2]
+            if t_end is not None and now >= t_end:
+                item[1]._finish(error=Expired('request not started within its '
+                                              'deadline'))
+                continue
+            if t_end is not None:
+                nxt = t_end - now if nxt is None else min(nxt, t_end - now)
+            keep.append(item)
+        if len(keep) != len(self._queue):
+            self._queue = keep
+            self._cv.notify_all()
+        return nxt
 
     def _fits(self, job):
         if job.key in self._busy_keys:
@@ -172,7 +219,7 @@ class Scheduler:
         # first fit in arrival order; a key's jobs keep their order (an
         # earlier job of a busy or waiting key blocks its later ones)
         blocked = set()
-        for i, (job, fut) in enumerate(self._queue):
+        for i, (job, fut, _) in enumerate(self._queue):
             if job.key in blocked:
                 continue
             if self._fits(job):
@@ -186,12 +233,13 @@ class Scheduler:
             with self._cv:
                 item = None
                 while not self._closed or self._queue:
+                    wake = self._expire(time.perf_counter())
                     item = self._take()
                     if item is not None:
                         break
                     if self._closed and not self._queue:
                         break
-                    self._cv.wait()
+                    self._cv.wait(wake)
                 if item is None:
                     return
                 job, fut = item
@@ -341,11 +389,13 @@ class Session:
             self.footprint = 0
         self.closed = False
 
-    def submit(self, dm):
+    def submit(self, dm, deadline=None):
         """One exchange build with density dm (nao, nao) FP64 (host):
         returns a Future whose result is K (len(omegas), nao, nao) FP64 on
-        the host, symmetrised as the reference returns it."""
-        return self.server._submit(self, dm)
+        the host, symmetrised as the reference returns it.  deadline:
+        seconds within which the build must start (else Expired); the
+        Future's cancel() drops it while it waits."""
+        return self.server._submit(self, dm, deadline)
 
     def close(self):
         if not self.closed:
@@ -397,13 +447,14 @@ class ExchangeServer:
             s.engine.close()
         self._sched.release(s.resident)
 
-    def _submit(self, session, dm):
+    def _submit(self, session, dm, deadline=None):
         if session.closed:
             raise Rejected('session is closed')
         dm = np.ascontiguousarray(dm, dtype=np.float64)
         if dm.shape != (session.nao, session.nao):
             raise ValueError('dm must be (%d, %d)' % (session.nao, session.nao))
-        fut = self._sched.submit(_Job(session, dm, session.footprint))
+        fut = self._sched.submit(_Job(session, dm, session.footprint),
+                                 deadline=deadline)
         self.futures.append(fut)
         return fut
 

@@ -174,3 +174,44 @@ def test_session_headroom_prevents_starvation():
     with pytest.raises(Rejected):
         s.reserve(60, wait=True, headroom=50)       # can never fit
     s.close()
+
+
+def test_cancel_drops_a_waiting_request_only():
+    """A queued request can be cancelled; a running or finished one
+    cannot.  One slot: the first job runs while the others wait."""
+    from pyscf_wb97mv_fast_gb300.serving import Cancelled
+    rec = Recorder()
+    s = Scheduler(rec, slots=1, budget=None)
+    f1 = s.submit(Job('a', 1, key='a', dur=0.2))
+    time.sleep(0.05)
+    f2 = s.submit(Job('b', 1, key='b', dur=0.01))
+    f3 = s.submit(Job('c', 1, key='c', dur=0.01))
+    assert not f1.cancel()                        # running
+    assert f2.cancel() and not f2.cancel()        # waiting, then gone
+    with pytest.raises(Cancelled):
+        f2.result(1)
+    assert f3.result(5) == ('c', 0) and f1.result(5) == ('a', 0)
+    assert not f3.cancel()                        # finished
+    assert rec.order == ['a', 'c']
+    s.close()
+
+
+def test_deadline_expires_requests_that_cannot_start_in_time():
+    """Requests whose deadline passes while the budget is held are
+    dropped with Expired, and the idle slots wake for the deadline without
+    any other event; one that starts in time runs."""
+    from pyscf_wb97mv_fast_gb300.serving import Expired
+    rec = Recorder()
+    s = Scheduler(rec, slots=3, budget=100)
+    big = s.submit(Job('big', 90, key='big', dur=1.0))
+    time.sleep(0.05)
+    late = s.submit(Job('late', 50, key='late'), deadline=0.1)
+    ok = s.submit(Job('ok', 50, key='ok'), deadline=5.0)
+    t0 = time.perf_counter()
+    with pytest.raises(Expired):
+        late.result(5)
+    assert time.perf_counter() - t0 < 0.6         # at its deadline, not at big's end
+    assert ok.result(5)[0] == 'ok'
+    big.result(5)
+    assert 'late' not in rec.order and s.max_used <= 100
+    s.close()
