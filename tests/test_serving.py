@@ -215,3 +215,24 @@ def test_deadline_expires_requests_that_cannot_start_in_time():
     big.result(5)
     assert 'late' not in rec.order and s.max_used <= 100
     s.close()
+
+
+def test_allocation_failure_frees_its_slot_and_budget():
+    """A build whose device allocation fails (a fake DeviceOutOfMemory from
+    the run function) hands the error to its request and gives its slot
+    and bytes back: the next request, which needs the whole budget, runs."""
+    from pyscf_wb97mv_fast_gb300._native import DeviceOutOfMemory, WB_ERR_OUT_OF_MEMORY
+
+    def run(job, slot):
+        if job.name == 'oom':
+            raise DeviceOutOfMemory(WB_ERR_OUT_OF_MEMORY, 'cudaMallocAsync: out of memory')
+        return job.name
+
+    s = Scheduler(run, slots=1, budget=100)
+    f = s.submit(Job('oom', 100, key='a'))
+    g = s.submit(Job('next', 100, key='b'))
+    with pytest.raises(MemoryError, match='out of memory'):
+        f.result(5)
+    assert g.result(5) == 'next'
+    s.close()
+    assert s._used == 0 and s._running == 0 and s.max_used <= 100
