@@ -64,18 +64,20 @@ def flow_streams():
     """A factory of per-flow stream contexts: stream('k') / stream('xc')
     makes the calling thread's device work run on a private stream of that
     name (one per name and device, created on first use), after the work
-    already queued on the thread's current stream.  Each flow then waits
+    already queued on the thread's current stream.  device: the CUDA
+    device (default: the calling thread's current one; a worker thread
+    passes its caller's, since the current device is per thread).  Each flow then waits
     only for its own kernels when it reads a result back to the host, so
     the K build and the XC / VV10 flows overlap on the device.  Without a
     CUDA device it selects nothing: the flows themselves raise there."""
     streams = {}
     lock = threading.Lock()
 
-    def stream(name):
+    def stream(name, device=None):
         torch = sgx_k_mod._torch()
         if not torch.cuda.is_available():
             return contextlib.nullcontext()
-        dev = torch.cuda.current_device()
+        dev = torch.cuda.current_device() if device is None else int(device)
         with lock:
             s = streams.get((name, dev))
             if s is None:
@@ -86,6 +88,12 @@ def flow_streams():
 
 
 _ABSENT = object()
+
+
+def _current_device():
+    """This thread's CUDA device, None without CUDA."""
+    torch = sgx_k_mod._torch()
+    return torch.cuda.current_device() if torch.cuda.is_available() else None
 
 
 def _zero_xc(nao):
@@ -143,11 +151,12 @@ def _overlap_factory(mf, ni, timings, stream):
                 nlc_code = mf.xc if ni.libxc.is_nlc(mf.xc) else mf.nlc
             xc_flow, nlc_flow = ni.nr_rks, ni.nr_nlc_vxc
             res = {}
+            dev = _current_device()
 
             def worker():
                 t0 = time.perf_counter()
                 try:
-                    with stream('xc'):
+                    with stream('xc', dev):
                         _, exc, vxc = xc_flow(mol, mf.grids, mf.xc, dm)
                         if nlc:
                             _, enlc, vnlc = nlc_flow(mol, mf.nlcgrids, nlc_code, dm)
@@ -253,7 +262,8 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
     hooks.k_stats = []
     hooks.timings = []        # overlap: one {'jk', 'xc', 'wait'} per get_veff
     # overlap puts the K flow and the XC / VV10 flows on streams of their own
-    stream = flow_streams() if overlap else (lambda name: contextlib.nullcontext())
+    stream = (flow_streams() if overlap
+              else (lambda name, device=None: contextlib.nullcontext()))
     if k:
         mod = sgx_jk_module if sgx_jk_module is not None else _sgx_jk_module()
         holder = {}
