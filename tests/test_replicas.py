@@ -57,3 +57,22 @@ def test_single_rank_is_the_local_time():
     import bench
     assert bench.max_over_ranks(0.5, 1, None) == 0.5
     assert bench.replica_throughput(1.0e12, 0.5, 1) == 2.0e12
+
+
+def test_clock_summary_reads_nvidia_smi_samples():
+    """The clocks key of the bench line: median SM clock under load, the
+    maximum, and only throttle reasons that were Active (nvidia-smi csv,
+    noheader, nounits; unreadable lines are skipped)."""
+    import bench
+    c = bench.ClockSampler()
+    c.lines = ['2070, 2070, 650.1, Not Active, Not Active, Not Active, Not Active',
+               '1980, 2070, 1390.5, Not Active, Not Active, Not Active, Active',
+               '[N/A], 2070, 10.0, Not Active, Not Active, Not Active, Not Active',
+               'garbage',
+               '2055, 2070, 1200.0, Not Active, Not Active, Not Active, Not Active']
+    s = c.summary()
+    assert s == {'sm_mhz': 2055.0, 'sm_max_mhz': 2070.0,
+                 'reasons': ['sw_power_cap'], 'samples': 3}
+    c.lines = ['1200, 2070, 900.0, Active, Not Active, Active, Not Active']
+    assert c.summary()['reasons'] == ['hw_slowdown', 'sw_thermal_slowdown']
+    assert bench.ClockSampler().summary()['sm_mhz'] is None
