@@ -236,3 +236,33 @@ def test_allocation_failure_frees_its_slot_and_budget():
     assert g.result(5) == 'next'
     s.close()
     assert s._used == 0 and s._running == 0 and s.max_used <= 100
+
+
+def test_scheduler_invariants_on_random_mixes():
+    """Random job mixes (footprints, sessions, durations, slot counts,
+    budgets): the budget and the slot count are never exceeded, each
+    session's jobs run one at a time in submission order, and every job
+    finishes."""
+    hyp = pytest.importorskip('hypothesis')
+    st = pytest.importorskip('hypothesis.strategies')
+
+    @hyp.settings(max_examples=60, deadline=None)
+    @hyp.given(slots=st.integers(1, 4), budget=st.integers(10, 60),
+               jobs=st.lists(st.tuples(st.integers(1, 10), st.integers(0, 3),
+                                       st.sampled_from([0.0, 0.001, 0.003])),
+                             min_size=1, max_size=14))
+    def check(slots, budget, jobs):
+        rec = Recorder()
+        s = Scheduler(rec, slots=slots, budget=budget)
+        futs = [s.submit(Job('j%d' % i, fp, key=k, dur=d))
+                for i, (fp, k, d) in enumerate(jobs)]
+        for f in futs:
+            f.result(10)
+        s.close()
+        assert rec.max_running <= slots and rec.max_bytes <= budget
+        assert s.max_used <= budget and s._used == 0
+        for k in set(k for _, k, _ in jobs):
+            mine = ['j%d' % i for i, (_, kk, _) in enumerate(jobs) if kk == k]
+            assert [n for n in rec.order if n in mine] == mine
+
+    check()
