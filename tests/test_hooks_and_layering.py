@@ -275,3 +275,38 @@ def test_install_refuses_out_of_scope_molecules_up_front(bad):
     mf.mol = FakeMole(mol)                         # in scope: installs
     install_gpu(mf, k=True, semilocal=False, vv10=False,
                 sgx_jk_module=mod).restore_all()
+
+
+def test_restore_all_undoes_any_sequence_of_wraps():
+    """Random sequences of wraps (the same name several times included) on
+    a module function, an instance's own attribute and a class method seen
+    through an instance: restore_all leaves every object as it was,
+    including which attributes the instance owns."""
+    hyp = pytest.importorskip('hypothesis')
+    st = pytest.importorskip('hypothesis.strategies')
+
+    class K:
+        def meth(self):
+            return 'class'
+
+    @hyp.settings(max_examples=60, deadline=None)
+    @hyp.given(st.lists(st.sampled_from(['mod.f', 'obj.own', 'obj.meth']),
+                        max_size=8))
+    def check(seq):
+        mod = types.ModuleType('m')
+        mod.f = lambda: 'mod'
+        obj = K()
+        obj.own = lambda: 'own'
+        before = (mod.f, dict(vars(obj)))
+        hooks = HookSet()
+        for i, target in enumerate(seq):
+            owner, name = {'mod.f': (mod, 'f'), 'obj.own': (obj, 'own'),
+                           'obj.meth': (obj, 'meth')}[target]
+            hooks.wrap(owner, name, lambda orig, i=i: (lambda *a: (i, orig)))
+        hooks.restore_all()
+        assert mod.f is before[0] and vars(obj) == before[1]
+        assert obj.meth() == 'class' and obj.own() == 'own'
+        with pytest.raises(RuntimeError):
+            hooks.wrap(mod, 'f', lambda o: o)
+
+    check()
