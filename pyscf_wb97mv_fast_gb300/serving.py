@@ -272,15 +272,19 @@ class Scheduler:
 
 
 def latency_summary(futures):
-    """p50 / p99 / mean latency (s), requests per second over the span
-    from the first submit to the last completion."""
-    lat = np.array([f.latency for f in futures if f.latency is not None])
+    """p50 / p99 / mean latency (s) and requests per second, over the
+    requests that returned a result, from the first submit to the last
+    completion; 'failed' counts the finished ones that raised (errors,
+    cancelled, expired)."""
+    ok = [f for f in futures if f.done() and f._error is None]
+    failed = sum(1 for f in futures if f.done() and f._error is not None)
+    lat = np.array([f.latency for f in ok])
     if not len(lat):
-        return {'requests': 0}
+        return {'requests': 0, 'failed': failed}
     t0 = min(f.t_submit for f in futures)
-    t1 = max(f.t_done for f in futures if f.t_done is not None)
-    q = np.array([f.queued for f in futures if f.queued is not None])
-    return {'requests': int(len(lat)),
+    t1 = max(f.t_done for f in ok)
+    q = np.array([f.queued for f in ok if f.queued is not None])
+    return {'requests': int(len(lat)), 'failed': failed,
             'p50_s': float(np.percentile(lat, 50)),
             'p99_s': float(np.percentile(lat, 99)),
             'mean_s': float(lat.mean()),

@@ -193,6 +193,8 @@ def test_cancel_drops_a_waiting_request_only():
     assert f3.result(5) == ('c', 0) and f1.result(5) == ('a', 0)
     assert not f3.cancel()                        # finished
     assert rec.order == ['a', 'c']
+    summ = latency_summary([f1, f2, f3])          # the cancelled one failed
+    assert summ['requests'] == 2 and summ['failed'] == 1
     s.close()
 
 
