@@ -18,8 +18,6 @@ compact; the screening bound depends on the sub-block radius.
 When PySCF is present, its own SGX grids are used instead (the hook reads
 ``sgx.grids``); these grids stand in for them in the synthetic workloads.
 """
-import math
-
 import numpy as np
 
 # level -> (radial points for H/He, radial points for heavier atoms, n_theta)
