@@ -57,18 +57,20 @@ METRIC = 'COSX G TFLOP/s (algorithmic flop model of kept tasks)'
 UNIT = 'TFLOP/s'
 
 
-def workload(small=False, grid_level=None):
+def workload(small=False, grid_level=None, partition=None):
     from pyscf_wb97mv_fast_gb300.basis import Molecule
     from pyscf_wb97mv_fast_gb300.grids import build_grids
     from pyscf_wb97mv_fast_gb300.systems import water_cluster
     if small:
         mol = Molecule.build(water_cluster(8, box=7.0, seed=8), 'synthetic-svp')
-        g = build_grids(mol, level=1 if grid_level is None else grid_level)
+        g = build_grids(mol, level=1 if grid_level is None else grid_level,
+                        partition=partition)
         nocc = 40
     else:
         mol = Molecule.build(water_cluster(NWATER, box=BOX, seed=SEED),
                              'synthetic-svp')
-        g = build_grids(mol, level=GRID_LEVEL if grid_level is None else grid_level)
+        g = build_grids(mol, level=GRID_LEVEL if grid_level is None else grid_level,
+                        partition=partition)
         nocc = NOCC
     rng = np.random.default_rng(SEED)
     c, _ = np.linalg.qr(rng.normal(size=(mol.nao, nocc)))
@@ -205,8 +207,7 @@ def cpu_baseline(mol, g, dm, engine, budget_s=15.0):
     reference's 1e-14 pair cut (the oracle computes those, all of them: no
     task screening)."""
     import oracle
-    from pyscf_wb97mv_fast_gb300.cosx import model_flops_per_point
-    flops_per_pt, _ = model_flops_per_point(mol)
+    flops_per_pt, _ = oracle.model_flops_per_point(mol)
     cores = os.cpu_count() or 1
     rng = np.random.default_rng(1)
     X_idx = rng.choice(g.size, 64, replace=False)
@@ -675,11 +676,11 @@ def run_reference(args):
     if rank != 0:
         return
     import oracle
-    from pyscf_wb97mv_fast_gb300.cosx import model_flops_per_point
-    mol, g, dm = workload(args.small)
+    mol, g, dm = workload(args.small, partition=oracle.becke_partition)
     # model flops per point of the pairs kept by the reference's 1e-14 pair
-    # cut, as credited on the GPU (the CPU path does no task screening)
-    flops_per_pt, _ = model_flops_per_point(mol)
+    # cut (the CPU path does no task screening); the oracle and the
+    # pure-Python flop model count them, so this arm loads no product code
+    flops_per_pt, _ = oracle.model_flops_per_point(mol)
     cores = os.cpu_count() or 1
     rng = np.random.default_rng(2)
     npts = args.ref_points

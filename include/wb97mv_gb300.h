@@ -362,8 +362,11 @@ int wb_vv10_kernel_sum_batch(int nmol, const int64_t* offsets, const float* xyz,
  * every GPU that loads the library until the process exits; n above
  * WB_VV10_NOALLOC_MAX_POINTS is rejected with WB_ERR_INVALID_ARGUMENT.
  * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress, with that device current); make that first call
- * before any stream capture.  All calls on a device share the array and
+ * (cudaGetSymbolAddress, with that device current) and keeps it; make that
+ * first call before any stream capture.  The kept address is valid for the
+ * life of the device's primary context: after cudaDeviceReset (or any
+ * teardown of that context) do not call it again in the same process.
+ * All calls on a device share the array and
  * each call leaves its own contents there: calls whose work overlaps on
  * the GPU (different streams, or different host threads) race.  No
  * counterpart in the reference. */

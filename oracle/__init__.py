@@ -55,8 +55,11 @@ def _load():
         _lib.oracle_ao_eval.argtypes = basis + [P, I64, P]
         _lib.oracle_vv10_sum.argtypes = [P, P, P, P, I64, P, P, P]
         _lib.oracle_ao_eval_deriv1.argtypes = basis + [P, I64, P]
+        _lib.oracle_pair_keep.argtypes = basis + [D, P]
+        _lib.oracle_becke_partition.argtypes = [P, I64, P, P, I, P]
         for f in ('oracle_boys', 'oracle_int3c1e', 'oracle_cosx_g',
-                  'oracle_ao_eval', 'oracle_vv10_sum', 'oracle_ao_eval_deriv1'):
+                  'oracle_ao_eval', 'oracle_vv10_sum', 'oracle_ao_eval_deriv1',
+                  'oracle_pair_keep', 'oracle_becke_partition'):
             getattr(_lib, f).restype = I
     return _lib
 
@@ -104,6 +107,56 @@ def cosx_g(mol, coords, F, omega=0.0, pair_cutoff=1e-14):
     _load().oracle_cosx_g(*b.args, _p(c), len(c), float(omega),
                           float(pair_cutoff), _p(F), _p(G))
     return G
+
+
+def becke_partition(points, owner, atom_coords):
+    """Owner-atom Becke weights (FP64), the grid builder's partition
+    without the product library."""
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    own = np.ascontiguousarray(owner, dtype=np.int32)
+    at = np.ascontiguousarray(atom_coords, dtype=np.float64)
+    out = np.empty(len(pts))
+    if _load().oracle_becke_partition(_p(pts), len(pts), _p(own), _p(at),
+                                      len(at), _p(out)) != 0:
+        raise MemoryError('oracle_becke_partition')
+    return out
+
+
+def pair_keep(mol, pair_cutoff=1e-14):
+    """(nbas, nbas) bool, lower triangle: the shell pairs the reference's
+    magnitude cut keeps (gpu/shellpairs.py:287-294)."""
+    b = _Basis(mol)
+    n = len(mol.shells)
+    keep = np.zeros((n, n), dtype=np.uint8)
+    if _load().oracle_pair_keep(*b.args, float(pair_cutoff), _p(keep)) != 0:
+        raise MemoryError('oracle_pair_keep')
+    return keep.astype(bool)
+
+
+def model_flops_per_point(mol, pair_cutoff=1e-14):
+    """(model flops per grid point, kept pairs): the work the CPU baselines
+    are credited with, from the pure-Python flop model over the shell pairs
+    the oracle keeps.  A generally contracted shell counts once per
+    contraction column, as in the GPU kernels' work count."""
+    from pyscf_wb97mv_fast_gb300.flops_model import task_flops
+    keep = pair_keep(mol, pair_cutoff)
+    shells = mol.shells
+    total, npairs, cache = 0, 0, {}
+    for i, si in enumerate(shells):
+        for j in range(i + 1):
+            if not keep[i, j]:
+                continue
+            sj = shells[j]
+            for ci in range(si.nctr):
+                for cj in range(sj.nctr if j < i else ci + 1):
+                    diag = j == i and cj == ci
+                    key = (si.l, sj.l, si.nprim, sj.nprim, diag)
+                    v = cache.get(key)
+                    if v is None:
+                        v = cache[key] = task_flops(*key)
+                    total += v
+                    npairs += 1
+    return float(total), npairs
 
 
 def ao_eval(mol, coords):

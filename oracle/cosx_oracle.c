@@ -295,6 +295,20 @@ static unsigned char* pair_keep(const obasis* b, double cutoff) {
     return keep;
 }
 
+/* The pair cut alone, for the work credit of the CPU baselines: keep
+ * (nbas, nbas), 1 where pair (i >= j) is kept, lower triangle filled. */
+int oracle_pair_keep(OBASIS_ARGS, double cutoff, unsigned char* keep) {
+    obasis b;
+    make_basis(&b, OBASIS_PASS);
+    unsigned char* k = pair_keep(&b, cutoff);
+    if (!k) return 1;
+    for (size_t i = 0; i < (size_t)nbas * nbas; ++i) keep[i] = 0;
+    for (int i = 0; i < nbas; ++i)
+        for (int j = 0; j <= i; ++j) keep[(size_t)i * nbas + j] = k[(size_t)i * nbas + j];
+    free(k);
+    return 0;
+}
+
 /* F, G (ng, nao) point-major; G overwritten.  Only the shell pairs that
  * pair_keep keeps contribute. */
 int oracle_cosx_g(OBASIS_ARGS, const double* coords, int64_t ng, double omega,
@@ -451,4 +465,61 @@ int oracle_vv10_sum(const double* xyz, const double* q, const double* w0,
         W[i] = w;
     }
     return 0;
+}
+
+/* Becke fuzzy-cell weight of each point's owner atom (Becke 1988, three
+ * smoothing iterations, no atomic size adjustment): the grid partition of
+ * the synthetic workloads, for the CPU baselines that must not load the
+ * product library.  Same formula as the product's grid builder. */
+int oracle_becke_partition(const double* pts, int64_t n, const int* owner,
+                           const double* atoms, int natm, double* out) {
+    double* rinv = (double*)calloc((size_t)natm * natm, sizeof(double));
+    if (!rinv) return 1;
+    for (int a = 0; a < natm; ++a)
+        for (int b = 0; b < natm; ++b) {
+            if (a == b) continue;
+            double d2 = 0.0;
+            for (int x = 0; x < 3; ++x) {
+                const double d = atoms[a * 3 + x] - atoms[b * 3 + x];
+                d2 += d * d;
+            }
+            rinv[(size_t)a * natm + b] = 1.0 / sqrt(d2);
+        }
+    int fail = 0;
+#pragma omp parallel
+    {
+        double* dist = (double*)malloc(sizeof(double) * (size_t)natm);
+        double* P = (double*)malloc(sizeof(double) * (size_t)natm);
+        if (!dist || !P) {
+#pragma omp atomic write
+            fail = 1;
+        } else {
+#pragma omp for schedule(static)
+            for (int64_t i = 0; i < n; ++i) {
+                for (int a = 0; a < natm; ++a) {
+                    double d2 = 0.0;
+                    for (int x = 0; x < 3; ++x) {
+                        const double d = pts[i * 3 + x] - atoms[a * 3 + x];
+                        d2 += d * d;
+                    }
+                    dist[a] = sqrt(d2);
+                    P[a] = 1.0;
+                }
+                for (int a = 0; a < natm; ++a)
+                    for (int b = a + 1; b < natm; ++b) {
+                        double mu = (dist[a] - dist[b]) * rinv[(size_t)a * natm + b];
+                        for (int it = 0; it < 3; ++it) mu = 1.5 * mu - 0.5 * mu * mu * mu;
+                        P[a] *= 0.5 * (1.0 - mu);
+                        P[b] *= 0.5 * (1.0 + mu);
+                    }
+                double tot = 0.0;
+                for (int a = 0; a < natm; ++a) tot += P[a];
+                out[i] = tot > 0.0 ? P[owner[i]] / tot : 0.0;
+            }
+        }
+        free(dist);
+        free(P);
+    }
+    free(rinv);
+    return fail;
 }

@@ -296,8 +296,7 @@ __global__ void f64_to_f32_kernel(const double* __restrict__ in,
 cudaError_t launch_f64_to_f32(const double* in, float* out, int64_t n,
                               cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    int64_t blocks = (n + 255) / 256;
-    if (blocks > 152 * 64) blocks = 152 * 64;
+    const int64_t blocks = grid_stride_blocks(n, 256, 64);
     f64_to_f32_kernel<<<(unsigned)blocks, 256, 0, s>>>(in, out, n);
     return cudaGetLastError();
 }
@@ -318,8 +317,7 @@ cudaError_t launch_weight_g(const float* G, const double* w, int64_t npts,
                             int64_t ld, int nao, double* out, cudaStream_t s) {
     const int64_t total = ld * nao;
     if (total <= 0) return cudaSuccess;
-    int64_t blocks = (total + 255) / 256;
-    if (blocks > 152 * 64) blocks = 152 * 64;
+    const int64_t blocks = grid_stride_blocks(total, 256, 64);
     weight_g_kernel<<<(unsigned)blocks, 256, 0, s>>>(G, w, npts, ld, total, out);
     return cudaGetLastError();
 }

@@ -9,13 +9,11 @@ namespace wb {
 //   T < 36: Taylor expansion about the nearest node T_k = k/4,
 //     F_n(T) = sum_{j=0..6} F_{n+j}(T_k) (-h)^j / j!,  h = T - T_k exact,
 //     with F_n(T_k) carried as hi + lo and the lo part added to the tail
-//     before the single final addition.
-//   T >= 36: the asymptotic form F_n = (2n-1)!!/2^(n+1) sqrt(pi) T^-(n+1/2)
-//     in double-float arithmetic (FMA error terms), scaled by 2^100 so that
-//     no error term becomes subnormal; T > 1e30 gives 0.
-// The same algorithm as the reference (gpu/boys.py:14-44, :121-168); the
-// table layout and the Taylor evaluation order are this library's.
-// Row layout (5 float4):
+//     before the single final addition (the switch at 36 and the node
+//     spacing follow the reference, gpu/boys.py:14-44).
+//   T >= 36: the asymptotic form F_n = Gamma(n + 1/2) / (2 T^(n + 1/2)),
+//     evaluated on the mantissa of an exact split T = m 4^e (boys_asym).
+// Row layout of the Taylor table (5 float4):
 //   [h0 h1 h2 h3 | h4 h5 h6 l0 | h7 l1 h8 l2 | h9 l3 h10 l4 | h11 l5 h12 l6]
 // ---------------------------------------------------------------------------
 #define WB_BOYS_TSWITCH 36.0f
@@ -99,41 +97,74 @@ __device__ __forceinline__ void far_r000(const float r2, const float k0h,
     }
 }
 
+// Double-float helpers of the asymptotic branch: a value is hi + lo with
+// |lo| <= ulp(hi)/2.  df_prod is Dekker's product with an FMA for the exact
+// error of hi*hi and a renormalisation (about 44 significant bits).
+struct DFloat { float hi, lo; };
+
+__device__ __forceinline__ DFloat df_prod(const DFloat x, const DFloat y) {
+    const float top = x.hi * y.hi;
+    const float err = fmaf(x.hi, y.hi, -top) + fmaf(x.lo, y.hi, x.hi * y.lo);
+    const float hi = top + err;
+    return DFloat{hi, err - (hi - top)};
+}
+
+// T >= 36 (finite): F_n(T) = g_n T^-(n + 1/2), g_n = Gamma(n + 1/2)/2.  The
+// neglected term of the exact F_n is below exp(-T)/(2T) < 4e-18 there.
+//
+// T is split exactly as m 4^e with m in [1, 4) by moving 2e out of the
+// binary exponent.  Then F_n = [g_n r^(2n + 1)] 2^(-e (2n + 1)), r = m^-1/2
+// in (1/2, 1].  The bracket is at least g_n 2^-13 and at most g_n, so its
+// double-float evaluation never meets a subnormal error term whatever T is;
+// it is rounded once, and the power of two is applied exactly (a result
+// below the normal range rounds as any subnormal product would).
+//   r: rsqrt plus one Newton step, r = r0 + r0 (1 - m r0^2) / 2, the
+//      residual taken with the exact square of r0 (about 44 bits);
+//   r^(2n + 1): running double-float products by r^2;
+//   g_n: (2n - 1)!! sqrt(pi) / 2^(n + 1) as hi + lo (FP32 pairs of the
+//      exact values, rounded from 60-digit decimals).
+// Maximum error: one rounding (0.5 ulp) plus about 2^-40 relative.
+template<int L>
+__device__ __forceinline__ void boys_asym(const float T, float* F) {
+    const int bits = __float_as_int(T);
+    const int e = (((bits >> 23) & 0xff) - 127) >> 1;   // T >= 36: e >= 2
+    const float m = __int_as_float(bits - (e << 24));    // T / 4^e in [1, 4)
+    const float r0 = rsqrtf(m);
+    const float sq = r0 * r0;
+    const float resid = fmaf(-m, sq, 1.0f) - m * fmaf(r0, r0, -sq);
+    const DFloat r = DFloat{r0, 0.5f * r0 * resid};
+    const DFloat r2 = df_prod(r, r);
+    const float step = __int_as_float((127 - 2 * e) << 23);   // 2^-2e, exact
+    float scale = __int_as_float((127 - e) << 23);            // 2^-e
+    constexpr float gh[7] = {8.862269521e-01f, 4.431134760e-01f, 6.646701694e-01f,
+                             1.661675453e+00f, 5.815864086e+00f, 2.617138863e+01f,
+                             1.439426422e+02f};
+    constexpr float gl[7] = {-2.662319964e-08f, -1.331159982e-08f, 2.473608340e-08f,
+                             3.203788523e-08f, 1.121326036e-07f, 2.661781195e-07f,
+                             -3.304391839e-06f};
+    DFloat pw = r;                                  // r^(2n + 1)
+#pragma unroll
+    for (int n = 0; n <= L; ++n) {
+        const DFloat v = df_prod(DFloat{gh[n], gl[n]}, pw);
+        F[n] = (v.hi + v.lo) * scale;
+        if (n < L) {
+            pw = df_prod(pw, r2);
+            scale *= step;
+        }
+    }
+}
+
 template<int L>
 __device__ __forceinline__ void boys_fp32(float T, float* F,
                                           const float4* __restrict__ tab) {
     if (!(T > 0.0f)) T = 0.0f;
     if (T < WB_BOYS_TSWITCH) {
         boys_taylor<L>(T, F, tab);
-    } else if (T > 1e30f) {
+    } else if (T < INFINITY) {
+        boys_asym<L>(T, F);
+    } else {
 #pragma unroll
         for (int n = 0; n <= L; ++n) F[n] = 0.0f;
-    } else {
-        // s = 1/sqrt(T) as s_hi + s_lo: rsqrtf and one Newton correction
-        const float s0 = rsqrtf(T);
-        const float a = s0 * s0;
-        const float a_lo = fmaf(s0, s0, -a);
-        const float r = fmaf(-T, a, 1.0f) - T * a_lo;
-        const float s_hi = s0, s_lo = 0.5f * s0 * r;
-        const float u_hi = s_hi * s_hi;
-        const float u_lo = fmaf(s_hi, s_hi, -u_hi) + 2.0f * s_hi * s_lo;
-        // sqrt(pi)/2 = 0.886226925452758... as hi + lo, scaled by 2^100
-        const float c_hi = 0.886226952075958252f * 1.2676506002282294e30f;
-        const float c_lo = -2.662319964e-08f * 1.2676506002282294e30f;
-        float f_hi = c_hi * s_hi;
-        float f_lo = fmaf(c_hi, s_hi, -f_hi) + (c_hi * s_lo + c_lo * s_hi);
-        F[0] = (f_hi + f_lo) * 7.888609052210118e-31f;
-#pragma unroll
-        for (int n = 1; n <= L; ++n) {
-            const float cc = (float)n - 0.5f;
-            const float cu_hi = cc * u_hi;
-            const float cu_lo = fmaf(cc, u_hi, -cu_hi) + cc * u_lo;
-            const float p = f_hi * cu_hi;
-            const float e = fmaf(f_hi, cu_hi, -p) + (f_hi * cu_lo + f_lo * cu_hi);
-            f_hi = p + e;
-            f_lo = e - (f_hi - p);
-            F[n] = f_hi * 7.888609052210118e-31f;
-        }
     }
 }
 

@@ -34,7 +34,7 @@ __global__ void weight_g64_kernel(const double* __restrict__ G,
 cudaError_t launch_weight_g64(const double* G, const double* w, int64_t npts,
                               int64_t ld, int nao, double* out, cudaStream_t s) {
     const int64_t n = (int64_t)nao * ld;
-    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 32);
+    const int64_t blocks = grid_stride_blocks(n, 256, 32);
     weight_g64_kernel<<<(int)std::max<int64_t>(blocks, 1), 256, 0, s>>>(G, w, npts, ld,
                                                                       nao, out);
     return cudaGetLastError();

@@ -7,6 +7,29 @@
 
 namespace wb {
 
+// SMs of the current device (cached per device; 152 on a GB300).
+inline int sm_count() {
+    static int cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!cached[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            n <= 0)
+            return 152;
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
+// Blocks of a grid-stride loop over n items: enough for every item, capped
+// at ctas_per_sm resident blocks per SM of the current device.
+inline int64_t grid_stride_blocks(int64_t n, int threads, int ctas_per_sm) {
+    const int64_t want = (n + threads - 1) / threads;
+    const int64_t cap = (int64_t)sm_count() * ctas_per_sm;
+    return want < 1 ? 1 : (want < cap ? want : cap);
+}
+
 // per-class fused screen + G kernels (cosx_kernels_*.cu); far selects the
 // variant with the far-field R000 form (omega = 0, where T >= 36 is common);
 // stage_smem > 0 selects the variant that stages each task's primitive-pair

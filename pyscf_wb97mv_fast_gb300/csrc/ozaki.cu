@@ -30,6 +30,7 @@
 #include <cmath>
 #include <cstdint>
 
+#include "launch.hpp"
 #include "ozaki.hpp"
 
 namespace wb {
@@ -520,8 +521,7 @@ int ozaki_k_gemm_multi(cublasHandle_t hb, const double* X, const float* const* G
             CUDA_R_32F, nao, nc, nchunk, CUBLAS_COMPUTE_32F,
             CUBLAS_GEMM_DEFAULT));
     }
-    int64_t blocks = (nc + 255) / 256;
-    if (blocks > 152 * 32) blocks = 152 * 32;
+    const int64_t blocks = grid_stride_blocks(nc, 256, 32);
     k_combine_kernel<S><<<(unsigned)blocks, 256, 0, s>>>(C, nao, nb, nchunk, ex, ew,
                                                         accumulate, Kd);
     OZ_CUDA(cudaGetLastError());

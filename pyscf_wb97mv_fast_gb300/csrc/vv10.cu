@@ -6,10 +6,11 @@
 //   F_i = -1.5 sum_j T,  U_i = sum_j Tu,  W_i = sum_j Tw
 //
 // One thread per outer point, inner points staged through shared memory in
-// 256-point tiles.  Inside a tile the three sums are FP32 with Kahan
-// compensation, across tiles they accumulate in FP64 in a fixed order: no
-// atomics, bitwise reproducible.  One reciprocal per pair (rcp.approx plus
-// one Newton step): T = q / (g gp gt), Tu = T (g + gt) gp / (g gp gt).
+// 256-point tiles.  Inside a tile the sums run in FP32 over 16 pairs at a
+// time, and those partials join Kahan-compensated tile sums; across tiles
+// they accumulate in FP64 in a fixed order: no atomics, bitwise
+// reproducible.  One reciprocal per pair (rcp.approx plus one Newton step):
+// T = q / (g gp gt), Tu = T (g + gt) gp / (g gp gt).
 //
 // Distance pruning on the device: per 256-point tile the centroid, radius,
 // sum q, min w0 and min kappa (FP64); a (block, tile) pair is skipped when
@@ -25,11 +26,6 @@ namespace wb {
 
 constexpr int kVvTile = 256;
 
-// WB_VV10_FAST = 1: one reciprocal per pair and 16-pair partial sums (the
-// default); 0: three IEEE reciprocals and a Kahan step per pair
-#ifndef WB_VV10_FAST
-#define WB_VV10_FAST 1
-#endif
 // one Newton step on the approximate reciprocal (1 = on)
 #ifndef WB_VV10_NEWTON
 #define WB_VV10_NEWTON 1
@@ -103,6 +99,72 @@ __device__ __forceinline__ bool vv10_keep(const VvTileStats& a,
     return fmax(fmax(bf, bu), bw) >= tol;
 }
 
+// One outer point: its coordinates, w0 and kappa.
+struct VvOuter { float x, y, z, w0, k; };
+
+// FP64 running sums of one outer point and its count of pairs computed.
+struct VvSums {
+    double f = 0.0, u = 0.0, w = 0.0;
+    unsigned long long pairs = 0;
+};
+
+// Index i must be valid; callers clamp it for threads past the end.
+__device__ __forceinline__ VvOuter vv_load_outer(const float* __restrict__ xyz,
+                                                 const float* __restrict__ w0,
+                                                 const float* __restrict__ kap,
+                                                 const int64_t i) {
+    return VvOuter{xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], w0[i], kap[i]};
+}
+
+// F carries the -3/2 of the VV10 kernel; U and W are the plain sums.
+__device__ __forceinline__ void vv_store(const VvSums& acc, const int64_t i,
+                                         double* __restrict__ F,
+                                         double* __restrict__ U,
+                                         double* __restrict__ W) {
+    F[i] = acc.f * -1.5;
+    U[i] = acc.u;
+    W[i] = acc.w;
+}
+
+// Inner point j into shared slot t: (x, y, z, q) and (w0, kappa).
+__device__ __forceinline__ void vv_stage(float4* sp, float2* sk, const int t,
+                                         const float* __restrict__ xyz,
+                                         const float* __restrict__ q,
+                                         const float* __restrict__ w0,
+                                         const float* __restrict__ kap,
+                                         const int64_t j) {
+    const float* c = xyz + 3 * j;
+    sp[t] = make_float4(c[0], c[1], c[2], q[j]);
+    sk[t] = make_float2(w0[j], kap[j]);
+}
+
+// Compensated accumulation of x into (sum, comp) (Kahan, 1965).
+__device__ __forceinline__ void kahan_add(float& sum, float& comp, const float x) {
+    const float xc = x - comp;
+    const float t = sum + xc;
+    comp = (t - sum) - xc;
+    sum = t;
+}
+
+// Block-wide integer total of v, added once per block to *total (the
+// order of an integer sum does not matter).  Every thread of the block
+// must call it.
+template<int NT>
+__device__ __forceinline__ void vv_block_count(unsigned long long v,
+                                               unsigned long long* total) {
+    __shared__ unsigned long long warp_part[NT / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) warp_part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+#pragma unroll
+        for (int w = 0; w < NT / 32; ++w) t += warp_part[w];
+        atomicAdd(total, t);
+    }
+}
+
 // The pairs of one outer point with one staged inner tile (m points), the
 // one-reciprocal form: inv = 1/(g gp gt) from rcp.approx and one Newton
 // step, T = q inv and, with 1/g + 1/gt = (g + gt) gp inv, Tu = T (g + gt)
@@ -110,17 +172,16 @@ __device__ __forceinline__ bool vv10_keep(const VvTileStats& a,
 // tile sums once per 16 pairs; the tile sums join the FP64 totals.  Shared
 // by the single-molecule and the batched kernels (same arithmetic, same
 // order).
-__device__ __forceinline__ void vv10_tile_fast(
-    const float xi, const float yi, const float zi, const float w0i, const float ki,
-    const float4* sp, const float2* sk, const int m, double& f64, double& u64,
-    double& w64, unsigned long long& nkept) {
+__device__ __forceinline__ void vv10_tile_fast(const VvOuter& o, const float4* sp,
+                                               const float2* sk, const int m,
+                                               VvSums& acc) {
     float fs = 0.f, fc = 0.f, us = 0.f, uc = 0.f, ws = 0.f, wc = 0.f;
     auto pair = [&](const int t, float& pf, float& pu, float& pw) {
         const float4 pj = sp[t];
         const float2 kj = sk[t];
-        const float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+        const float dx = o.x - pj.x, dy = o.y - pj.y, dz = o.z - pj.z;
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float g = fmaf(r2, w0i, ki);
+        const float g = fmaf(r2, o.w0, o.k);
         const float gp = fmaf(r2, kj.x, kj.y);
         const float gt = g + gp;
         const float pr = g * gp * gt;
@@ -141,15 +202,20 @@ __device__ __forceinline__ void vv10_tile_fast(
         } else {
             for (int t = t0; t < m; ++t) pair(t, pf, pu, pw);
         }
-        float y, z;
-        y = pf - fc; z = fs + y; fc = (z - fs) - y; fs = z;
-        y = pu - uc; z = us + y; uc = (z - us) - y; us = z;
-        y = pw - wc; z = ws + y; wc = (z - ws) - y; ws = z;
+        kahan_add(fs, fc, pf);
+        kahan_add(us, uc, pu);
+        kahan_add(ws, wc, pw);
     }
-    f64 += (double)fs; u64 += (double)us; w64 += (double)ws;
-    nkept += (unsigned long long)m;
+    acc.f += (double)fs;
+    acc.u += (double)us;
+    acc.w += (double)ws;
+    acc.pairs += (unsigned long long)m;
 }
 
+// One block per 256-point outer tile.  Thread 0 decides whether the block
+// needs inner tile jt (the decision sits in a two-slot parity buffer so
+// the next decision cannot overwrite one still being read); the block
+// stages the tile and every live thread runs its pairs.
 __global__ void __launch_bounds__(kVvTile)
 vv10_sum_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
                 const float* __restrict__ w0, const float* __restrict__ kap,
@@ -158,72 +224,27 @@ vv10_sum_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
                 double* __restrict__ W, unsigned long long* __restrict__ kept) {
     __shared__ float4 sp[kVvTile];      // x, y, z, q
     __shared__ float2 sk[kVvTile];      // w0, kappa
-    __shared__ int s_keep[2];           // parity double buffer
+    __shared__ int s_keep[2];
     const int64_t i = (int64_t)blockIdx.x * kVvTile + threadIdx.x;
-    const bool active = i < n;
-    float xi = 0.f, yi = 0.f, zi = 0.f, w0i = 0.f, ki = 1.f;
-    if (active) {
-        xi = xyz[3 * i]; yi = xyz[3 * i + 1]; zi = xyz[3 * i + 2];
-        w0i = w0[i]; ki = kap[i];
-    }
-    const int64_t nt = (n + kVvTile - 1) / kVvTile;
-    double f64 = 0.0, u64 = 0.0, w64 = 0.0;
-    unsigned long long nkept = 0;
-    for (int64_t jt = 0; jt < nt; ++jt) {
+    const bool live = i < n;
+    const VvOuter o = vv_load_outer(xyz, w0, kap, live ? i : n - 1);
+    const int64_t ntiles = (n + kVvTile - 1) / kVvTile;
+    VvSums acc;
+    for (int64_t jt = 0; jt < ntiles; ++jt) {
         if (threadIdx.x == 0)
             s_keep[jt & 1] = vv10_keep(st[blockIdx.x], st[jt], tol);
         const int64_t j = jt * kVvTile + threadIdx.x;
         __syncthreads();
         if (!s_keep[jt & 1]) continue;  // uniform across the block
-        if (j < n) {
-            sp[threadIdx.x] = make_float4(xyz[3 * j], xyz[3 * j + 1],
-                                          xyz[3 * j + 2], q[j]);
-            sk[threadIdx.x] = make_float2(w0[j], kap[j]);
-        }
+        if (j < n) vv_stage(sp, sk, threadIdx.x, xyz, q, w0, kap, j);
         __syncthreads();
-        const int m = (int)min((int64_t)kVvTile, n - jt * kVvTile);
-#if WB_VV10_FAST
-        if (active)
-            vv10_tile_fast(xi, yi, zi, w0i, ki, sp, sk, m, f64, u64, w64, nkept);
-#else
-        if (active) {
-            float fs = 0.f, fc = 0.f, us = 0.f, uc = 0.f, ws = 0.f, wc = 0.f;
-            for (int t = 0; t < m; ++t) {
-                const float4 pj = sp[t];
-                const float2 kj = sk[t];
-                const float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                const float g = fmaf(r2, w0i, ki);
-                const float gp = fmaf(r2, kj.x, kj.y);
-                const float gt = g + gp;
-                const float T = pj.w * __frcp_rn(g * gp * gt);
-                const float Tu = T * (__frcp_rn(g) + __frcp_rn(gt));
-                const float Tw = Tu * r2;
-                float y, s;
-                y = T - fc;  s = fs + y; fc = (s - fs) - y; fs = s;
-                y = Tu - uc; s = us + y; uc = (s - us) - y; us = s;
-                y = Tw - wc; s = ws + y; wc = (s - ws) - y; ws = s;
-            }
-            f64 += (double)fs; u64 += (double)us; w64 += (double)ws;
-            nkept += (unsigned long long)m;
-        }
-#endif
+        if (live)
+            vv10_tile_fast(o, sp, sk, (int)min((int64_t)kVvTile, n - jt * kVvTile),
+                           acc);
         __syncthreads();
     }
-    if (active) { F[i] = -1.5 * f64; U[i] = u64; W[i] = w64; }
-    if (kept) {
-        // block total of kept pairs (deterministic integer sum)
-        __shared__ unsigned long long red[kVvTile / 32];
-        unsigned long long v = nkept;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long t = 0;
-            for (int w = 0; w < kVvTile / 32; ++w) t += red[w];
-            atomicAdd(kept, t);
-        }
-    }
+    if (live) vv_store(acc, i, F, U, W);
+    if (kept) vv_block_count<kVvTile>(acc.pairs, kept);
 }
 
 // Packed form (-DWB_VV10_PACKED=1; the default is the kernel above): two
@@ -303,18 +324,10 @@ vv10_sum_packed_kernel(const float* __restrict__ xyz, const float* __restrict__ 
     const int64_t i0 = (int64_t)blockIdx.x * kVvOuter + threadIdx.x;
     const int64_t i1 = i0 + kVvTile;
     const bool a0 = i0 < n, a1 = i1 < n;
-    float x0 = 0.f, y0 = 0.f, z0 = 0.f, w00 = 0.f, k0 = 1.f;
-    float x1 = 0.f, y1 = 0.f, z1 = 0.f, w01 = 0.f, k1 = 1.f;
-    if (a0) {
-        x0 = xyz[3 * i0]; y0 = xyz[3 * i0 + 1]; z0 = xyz[3 * i0 + 2];
-        w00 = w0[i0]; k0 = kap[i0];
-    }
-    if (a1) {
-        x1 = xyz[3 * i1]; y1 = xyz[3 * i1 + 1]; z1 = xyz[3 * i1 + 2];
-        w01 = w0[i1]; k1 = kap[i1];
-    }
-    const f2r xi = pk(x0, x1), yi = pk(y0, y1), zi = pk(z0, z1);
-    const f2r w0i = pk(w00, w01), ki = pk(k0, k1);
+    const VvOuter o0 = vv_load_outer(xyz, w0, kap, a0 ? i0 : n - 1);
+    const VvOuter o1 = vv_load_outer(xyz, w0, kap, a1 ? i1 : n - 1);
+    const f2r xi = pk(o0.x, o1.x), yi = pk(o0.y, o1.y), zi = pk(o0.z, o1.z);
+    const f2r w0i = pk(o0.w0, o1.w0), ki = pk(o0.k, o1.k);
     const f2r one = pk(1.0f, 1.0f);
     const int64_t nt = (n + kVvTile - 1) / kVvTile;
     const int64_t ob = 2 * (int64_t)blockIdx.x;           // outer stats tiles
@@ -339,6 +352,12 @@ vv10_sum_packed_kernel(const float* __restrict__ xyz, const float* __restrict__ 
         __syncthreads();
         const int m = (int)min((int64_t)kVvTile, n - jt * kVvTile);
         f2r fs = 0, fc = 0, us = 0, uc = 0, ws = 0, wc = 0;
+        auto kahan_add2 = [](f2r& sum, f2r& comp, const f2r x) {
+            const f2r xc = sub2(x, comp);
+            const f2r t = add2(sum, xc);
+            comp = sub2(sub2(t, sum), xc);
+            sum = t;
+        };
         auto pair = [&](const int t, f2r& pf, f2r& pu, f2r& pw) {
             const float4 a = sxy[t], b = szq[t], c = swk[t];
             const f2r xj = pk(a.x, a.y), yj = pk(a.z, a.w);
@@ -366,10 +385,9 @@ vv10_sum_packed_kernel(const float* __restrict__ xyz, const float* __restrict__ 
             } else {
                 for (int t = t0; t < m; ++t) pair(t, pf, pu, pw);
             }
-            f2r y, z;
-            y = sub2(pf, fc); z = add2(fs, y); fc = sub2(sub2(z, fs), y); fs = z;
-            y = sub2(pu, uc); z = add2(us, y); uc = sub2(sub2(z, us), y); us = z;
-            y = sub2(pw, wc); z = add2(ws, y); wc = sub2(sub2(z, ws), y); ws = z;
+            kahan_add2(fs, fc, pf);
+            kahan_add2(us, uc, pu);
+            kahan_add2(ws, wc, pw);
         }
         float lo, hi;
         upk(fs, lo, hi); f64[0] += (double)lo; f64[1] += (double)hi;
@@ -378,20 +396,12 @@ vv10_sum_packed_kernel(const float* __restrict__ xyz, const float* __restrict__ 
         nkept += (unsigned long long)m * ((a0 ? 1 : 0) + (a1 ? 1 : 0));
         __syncthreads();
     }
-    if (a0) { F[i0] = -1.5 * f64[0]; U[i0] = u64[0]; W[i0] = w64[0]; }
-    if (a1) { F[i1] = -1.5 * f64[1]; U[i1] = u64[1]; W[i1] = w64[1]; }
-    if (kept) {
-        __shared__ unsigned long long red[kVvTile / 32];
-        unsigned long long v = nkept;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long t = 0;
-            for (int w = 0; w < kVvTile / 32; ++w) t += red[w];
-            atomicAdd(kept, t);
-        }
-    }
+    VvSums s0, s1;
+    s0.f = f64[0]; s0.u = u64[0]; s0.w = w64[0];
+    s1.f = f64[1]; s1.u = u64[1]; s1.w = w64[1];
+    if (a0) vv_store(s0, i0, F, U, W);
+    if (a1) vv_store(s1, i1, F, U, W);
+    if (kept) vv_block_count<kVvTile>(nkept, kept);
 }
 
 }  // namespace
@@ -458,14 +468,9 @@ vv10_sum_seg_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
     const int64_t t = blockIdx.x;
     const int mol = sg.tmol[t];
     const int64_t i = sg.tstart[t] + threadIdx.x;
-    const bool active = (int)threadIdx.x < sg.tlen[t];
-    float xi = 0.f, yi = 0.f, zi = 0.f, w0i = 0.f, ki = 1.f;
-    if (active) {
-        xi = xyz[3 * i]; yi = xyz[3 * i + 1]; zi = xyz[3 * i + 2];
-        w0i = w0[i]; ki = kap[i];
-    }
-    double f64 = 0.0, u64 = 0.0, w64 = 0.0;
-    unsigned long long nkept = 0;
+    const bool live = (int)threadIdx.x < sg.tlen[t];
+    const VvOuter o = vv_load_outer(xyz, w0, kap, live ? i : sg.tstart[t]);
+    VvSums acc;
     const int jt0 = sg.mtile[mol], jt1 = sg.mtile[mol + 1];
     for (int jt = jt0; jt < jt1; ++jt) {
         if (threadIdx.x == 0)
@@ -474,29 +479,13 @@ vv10_sum_seg_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
         const int64_t j = sg.tstart[jt] + threadIdx.x;
         __syncthreads();
         if (!s_keep[jt & 1]) continue;  // uniform across the block
-        if ((int)threadIdx.x < m) {
-            sp[threadIdx.x] = make_float4(xyz[3 * j], xyz[3 * j + 1],
-                                          xyz[3 * j + 2], q[j]);
-            sk[threadIdx.x] = make_float2(w0[j], kap[j]);
-        }
+        if ((int)threadIdx.x < m) vv_stage(sp, sk, threadIdx.x, xyz, q, w0, kap, j);
         __syncthreads();
-        if (active)
-            vv10_tile_fast(xi, yi, zi, w0i, ki, sp, sk, m, f64, u64, w64, nkept);
+        if (live) vv10_tile_fast(o, sp, sk, m, acc);
         __syncthreads();
     }
-    if (active) { F[i] = -1.5 * f64; U[i] = u64; W[i] = w64; }
-    if (kept) {
-        __shared__ unsigned long long red[kVvTile / 32];
-        unsigned long long v = nkept;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned long long tot = 0;
-            for (int w = 0; w < kVvTile / 32; ++w) tot += red[w];
-            atomicAdd(kept, tot);
-        }
-    }
+    if (live) vv_store(acc, i, F, U, W);
+    if (kept) vv_block_count<kVvTile>(acc.pairs, kept);
 }
 
 cudaError_t launch_vv10_seg(const float* xyz, const float* q, const float* w0,
@@ -625,7 +614,10 @@ extern "C" int wb_vv10_kernel_sum_noalloc(const float* xyz, const float* q,
     void* scratch = nullptr;
     {
         // first call on this device: the device address of the array (the
-        // host-side name is only a stand-in), taken with the device current
+        // host-side name is only a stand-in), taken with the device current.
+        // It stays valid while the primary context lives; a cudaDeviceReset
+        // would leave it stale (the header tells callers not to call again
+        // after one)
         std::lock_guard<std::mutex> lk(g_noalloc_mu);
         if (!g_noalloc_ptr[dev]) {
             void* p = nullptr;

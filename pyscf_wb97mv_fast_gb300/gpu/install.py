@@ -231,17 +231,26 @@ def rsh_omegas(mf):
     return (omega,) if abs(float(alpha)) > 0.0 else None
 
 
-def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
+def install_gpu(mf, backend=None, blksize=8192, vv10_tile_tol=0.0,
                 functional_factory=None, verify_ao=True,
-                gemm_dtype='float64', dtype='float32',
+                gemm_dtype='float32', dtype='float32',
                 mem_fraction=DEFAULT_MEM_FRACTION, overlap=True,
-                semilocal=True, k=True, k_tile_tol=1e-11,
-                openblas_threads=None, vv10=True, k_gemm='ozaki',
+                semilocal=True, k=False, k_tile_tol=1e-11,
+                openblas_threads=1, vv10=True, k_gemm='ozaki',
                 sgx_jk_module=None, k_omegas='auto', k_precision='fp32'):
-    """Hook the GPU COSX K (and VV10) into mf; returns a HookSet.
+    """Hook the GPU flows into mf; returns a HookSet.
 
-    The keyword names follow the reference; backend must be None or
-    'cuda' (there is one backend).  semilocal=True replaces
+    The keywords and their defaults are the reference's
+    (gpu/install.py:209-213): the XC and VV10 hooks always, the COSX K hook
+    only with k=True.  backend must be None or 'cuda' (there is one
+    backend).  blksize is the grid block of the semilocal XC flow (points
+    per native call; None takes the whole grid); the K builder sizes its
+    own grid tiles, as the reference's does.  gemm_dtype and dtype are
+    accepted for the reference's 'float32' / 'float64' values: this flow's
+    GEMMs take FP64 inputs whichever is asked (the X·D products are
+    FP64-accurate and rounded once to FP32).  openblas_threads=1 holds a
+    pthreads OpenBLAS to one thread until restore_all (None: leave it).
+    semilocal=True replaces
     ``mf._numint.nr_rks`` by the GPU semilocal flow (gpu/xc.py), with
     functional_factory(xc_code, ni) -> XcFunctional (default: PySCF's
     libxc on the host).  sgx_jk_module lets tests pass a stand-in for
@@ -256,9 +265,17 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
     """
     if backend not in (None, 'cuda', 'cupy'):
         raise ValueError("backend must be None or 'cuda'")
+    for name, val in (('gemm_dtype', gemm_dtype), ('dtype', dtype)):
+        if val not in ('float32', 'float64'):
+            raise ValueError("%s must be 'float32' or 'float64'" % name)
     if getattr(mf, 'mol', None) is not None and (k or semilocal or vv10):
         check_scope(mf.mol)
     hooks = HookSet()
+    if openblas_threads is not None:
+        from pyscf_wb97mv_fast_gb300.core import blas_threads
+        undo = blas_threads.limit_openblas_threads(openblas_threads)
+        if undo is not None:
+            hooks.on_restore(undo)      # registered first: undone last
     hooks.k_stats = []
     hooks.timings = []        # overlap: one {'jk', 'xc', 'wait'} per get_veff
     # overlap puts the K flow and the XC / VV10 flows on streams of their own
@@ -280,7 +297,7 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
                     oms = (rsh_omegas(mf) if isinstance(k_omegas, str)
                            and k_omegas == 'auto' else k_omegas)
                     b = sgx_k_mod.GpuKBuilder(mf.mol, tile_tol=k_tile_tol,
-                                              blksize=blksize, gemm=k_gemm,
+                                              gemm=k_gemm,
                                               precision=k_precision,
                                               omegas=oms)
                     b._build()
@@ -307,7 +324,9 @@ def install_gpu(mf, backend=None, blksize=None, vv10_tile_tol=0.0,
         if ni is None:
             raise TypeError('mf has no _numint; not a DFT object?')
         from pyscf_wb97mv_fast_gb300.gpu import xc as xc_mod
-        xctx = xc_mod.XcContext(mf.mol, functional_factory=functional_factory)
+        xctx = xc_mod.XcContext(mf.mol, functional_factory=functional_factory,
+                                **({} if blksize is None
+                                   else {'tile_pts': int(blksize)}))
 
         def rks_factory(orig):
             def nr_rks(mol, grids, xc_code, dms, relativity=0, hermi=1,

@@ -96,11 +96,12 @@ def becke_weights_reference(points, atom_coords, owner):
     return P[np.arange(n), owner] / tot
 
 
-def _becke_weights(points, atom_coords, owner):
-    from pyscf_wb97mv_fast_gb300.cosx import becke_partition
+def _becke_weights(points, atom_coords, owner, partition=None):
     if atom_coords.shape[0] == 1:
         return np.ones(points.shape[0])
-    return becke_partition(points, owner, atom_coords)
+    if partition is None:
+        from pyscf_wb97mv_fast_gb300.cosx import becke_partition as partition
+    return partition(points, owner, atom_coords)
 
 
 def morton_order(coords, bits=10):
@@ -115,8 +116,10 @@ def morton_order(coords, bits=10):
     return np.argsort(code, kind='stable')
 
 
-def build_grids(mol, level=2, prune=1e-15, order='morton'):
-    """Becke grids for a Molecule (or anything with symbols/atom_coords)."""
+def build_grids(mol, level=2, prune=1e-15, order='morton', partition=None):
+    """Becke grids for a Molecule (or anything with symbols/atom_coords).
+    partition(points, owner, atom_coords) -> weights replaces the native
+    Becke routine (the CPU baselines pass the oracle's)."""
     nrad_h, nrad_heavy, n_theta = GRID_LEVELS[level]
     ang_xyz, ang_w = angular_grid(n_theta)
     coords = mol.atom_coords()
@@ -131,7 +134,8 @@ def build_grids(mol, level=2, prune=1e-15, order='morton'):
         wts.append((wr[:, None] * ang_w[None, :]).ravel())
         own.append(np.full(len(pts[-1]), ia))
     pts = np.concatenate(pts)
-    wts = np.concatenate(wts) * _becke_weights(pts, coords, np.concatenate(own))
+    wts = np.concatenate(wts) * _becke_weights(pts, coords, np.concatenate(own),
+                                               partition)
     keep = wts > prune
     pts, wts = pts[keep], wts[keep]
     if order == 'morton' and len(pts):

@@ -1,6 +1,7 @@
 """Generates the golden fixtures of tests/golden/ by running the reference's
-own Python (Cedrus810/pyscf-wb97mv-fast, read from /root/reference) on this
-project's synthetic molecules.
+own Python (Cedrus810/pyscf-wb97mv-fast: a checkout of it, named by the
+first argument or by WB_REFERENCE_ROOT) on this project's synthetic
+molecules.
 
 PySCF is not installed, so the few PySCF names the reference modules import
 are stubbed: ``pyscf.gto.mole.cart2sph`` is served by this project's
@@ -11,8 +12,9 @@ contracted integrals (gpu/shellpairs.py int3c1e_reference, pair_bound), the
 FP64 AO evaluation (gpu/ao_eval.py) and the VV10 kernel sum
 (gpu/vv10.py Vv10Kernel, NumPy path) -- is the reference's code, unmodified.
 
-Run from the repository root:  python tests/golden/make_golden.py
-The output files are committed; tests never read /root/reference.
+Run from the repository root:
+    python tests/golden/make_golden.py <reference checkout>
+The output files are committed; tests never read the reference.
 """
 import os
 import sys
@@ -20,7 +22,16 @@ import types
 
 import numpy as np
 
-REF = '/root/reference'
+
+def _reference_root():
+    root = (sys.argv[1] if len(sys.argv) > 1
+            else os.environ.get('WB_REFERENCE_ROOT', ''))
+    if not root or not os.path.isdir(os.path.join(root, 'pyscf_wb97mv_fast')):
+        raise SystemExit('usage: make_golden.py <reference checkout> '
+                         '(or set WB_REFERENCE_ROOT)')
+    return root
+
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
@@ -29,7 +40,7 @@ from pyscf_wb97mv_fast_gb300.basis import Molecule, cart2sph  # noqa: E402
 from pyscf_wb97mv_fast_gb300.systems import water_dimer  # noqa: E402
 
 
-def install_stubs():
+def install_stubs(ref_root):
     pyscf = types.ModuleType('pyscf')
     gto = types.ModuleType('pyscf.gto')
     mole = types.ModuleType('pyscf.gto.mole')
@@ -60,7 +71,7 @@ def install_stubs():
     xc.Unsupported = Unsupported
     xc._prepare_dm = _prepare_dm
     sys.modules['pyscf_wb97mv_fast.gpu.xc'] = xc
-    sys.path.insert(0, REF)
+    sys.path.insert(0, ref_root)
 
 
 class RefMol:
@@ -85,7 +96,7 @@ def points(mol, rng, n):
 
 
 def main():
-    install_stubs()
+    install_stubs(_reference_root())
     from pyscf_wb97mv_fast.gpu import boys as rboys
     from pyscf_wb97mv_fast.gpu import shellpairs as rsp
     from pyscf_wb97mv_fast.gpu import ao_eval as rao

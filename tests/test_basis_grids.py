@@ -109,3 +109,17 @@ def test_drug_like_molecule():
     tz = Molecule.build(atoms, 'synthetic-tzvp')
     assert tz.nao > 1.9 * svp.nao
     assert max(sh.l for sh in tz.shells) == 3
+
+
+def test_oracle_partition_gives_the_native_grid():
+    """The reference arm of the bench builds its grid with the oracle's
+    Becke partition (no product library); the grid is the native one."""
+    import oracle
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    from pyscf_wb97mv_fast_gb300.systems import water_cluster
+    mol = Molecule.build(water_cluster(4, box=6.0, seed=3), 'synthetic-svp')
+    a = build_grids(mol, level=0)
+    b = build_grids(mol, level=0, partition=oracle.becke_partition)
+    np.testing.assert_array_equal(a.coords, b.coords)
+    np.testing.assert_allclose(a.weights, b.weights, rtol=1e-14, atol=0)

@@ -26,3 +26,19 @@ def test_pair_table_size_and_symmetry():
     nb = mol.nbas
     assert t.shape == (nb * (nb + 1) // 2,)
     assert np.all(t > 0)
+
+
+def test_oracle_work_credit_matches_the_native_count():
+    """The CPU baselines credit the work from the oracle's pair cut and the
+    pure-Python model (so the reference arm loads no product library); it
+    equals the native library's count of the same pairs."""
+    import oracle
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.cosx import model_flops_per_point
+    from pyscf_wb97mv_fast_gb300.systems import water_cluster, water_dimer
+    mols = [Molecule.build(water_dimer(), 'synthetic-svp'),
+            Molecule.build(water_dimer(), 'synthetic-tzvp'),
+            Molecule.build(water_dimer(), 'synthetic-svp', gen_contract=True),
+            Molecule.build(water_cluster(8, box=7.0, seed=8), 'synthetic-svp')]
+    for m in mols:
+        assert oracle.model_flops_per_point(m) == model_flops_per_point(m)

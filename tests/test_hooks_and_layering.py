@@ -310,3 +310,87 @@ def test_restore_all_undoes_any_sequence_of_wraps():
             hooks.wrap(mod, 'f', lambda o: o)
 
     check()
+
+
+def test_install_gpu_defaults_are_the_references():
+    """The keyword defaults of install_gpu equal the reference's signature
+    (pyscf_wb97mv_fast/gpu/install.py:209-213); the additions come after
+    them and are opt-in."""
+    import inspect
+    from pyscf_wb97mv_fast_gb300.gpu.install import install_gpu
+    ref = dict(backend=None, blksize=8192, vv10_tile_tol=0.0,
+               functional_factory=None, verify_ao=True, gemm_dtype='float32',
+               dtype='float32', mem_fraction=0.6, overlap=True, semilocal=True,
+               k=False, k_tile_tol=1e-11, openblas_threads=1)
+    params = list(inspect.signature(install_gpu).parameters.values())
+    assert [p.name for p in params[:len(ref) + 1]] == ['mf'] + list(ref)
+    for p in params[1:len(ref) + 1]:
+        assert p.default == ref[p.name], p.name
+    extra = {p.name: p.default for p in params[len(ref) + 1:]}
+    assert extra == dict(vv10=True, k_gemm='ozaki', sgx_jk_module=None,
+                         k_omegas='auto', k_precision='fp32')
+
+
+def test_install_default_places_no_k_hook():
+    """install_gpu(mf) with the reference's default k=False leaves the
+    module function get_k_only alone."""
+    from pyscf_wb97mv_fast_gb300.gpu.install import install_gpu
+    mod = types.SimpleNamespace(get_k_only=lambda *a, **k: 'cpu')
+    orig = mod.get_k_only
+    mf = types.SimpleNamespace(mol=None, with_df=object())
+    hooks = install_gpu(mf, semilocal=False, vv10=False, overlap=False,
+                        sgx_jk_module=mod, openblas_threads=None)
+    assert mod.get_k_only is orig
+    hooks.restore_all()
+
+
+def test_install_rejects_unknown_gemm_dtype():
+    from pyscf_wb97mv_fast_gb300.gpu.install import install_gpu
+    mf = types.SimpleNamespace(mol=None)
+    with pytest.raises(ValueError):
+        install_gpu(mf, semilocal=False, vv10=False, gemm_dtype='bfloat16')
+
+
+class _FakeBlas:
+    def __init__(self, parallel, threads):
+        self.par, self.threads, self.calls = parallel, threads, []
+
+    def lib(self):
+        from pyscf_wb97mv_fast_gb300.core.blas_threads import BlasLib
+        return BlasLib('fake', lambda: self.par, lambda: self.threads,
+                       self._set)
+
+    def _set(self, n):
+        self.calls.append(n)
+        self.threads = n
+
+
+def test_openblas_limit_touches_pthreads_builds_and_restores():
+    from pyscf_wb97mv_fast_gb300.core.blas_threads import limit_openblas_threads
+    pth, omp, seq = _FakeBlas(1, 8), _FakeBlas(2, 8), _FakeBlas(0, 1)
+    undo = limit_openblas_threads(1, libs=[pth.lib(), omp.lib(), seq.lib()],
+                                  environ={})
+    assert pth.threads == 1 and omp.calls == [] and seq.calls == []
+    undo()
+    assert pth.threads == 8
+
+
+def test_openblas_limit_respects_user_environment():
+    from pyscf_wb97mv_fast_gb300.core.blas_threads import limit_openblas_threads
+    pth = _FakeBlas(1, 8)
+    assert limit_openblas_threads(1, libs=[pth.lib()],
+                                  environ={'OPENBLAS_NUM_THREADS': '4'}) is None
+    assert pth.calls == []
+    assert limit_openblas_threads(1, libs=[_FakeBlas(0, 1).lib()], environ={}) is None
+
+
+def test_openblas_limit_reads_this_process_maps():
+    """The real scan runs (numpy's OpenBLAS, when it is a pthreads build,
+    is found and limited, then restored)."""
+    from pyscf_wb97mv_fast_gb300.core import blas_threads
+    libs = blas_threads.mapped_blas_libraries()
+    before = [int(lib.get_threads()) for lib in libs]
+    undo = blas_threads.limit_openblas_threads(1, libs=libs, environ={})
+    if undo is not None:
+        undo()
+    assert [int(lib.get_threads()) for lib in libs] == before
