@@ -662,6 +662,104 @@ def serving_timing(torch, rates=(4.0, 16.0), slots=4, seed=5):
     return out
 
 
+def parity_vs_oracle(mol, g, dm, eng, torch, npts, seed=11):
+    """The checker: max|dK|/max|K| and 1/4 tr(D dK) of the mixed-precision
+    multi-omega K against the FP64 oracle on a seeded subset of the grid
+    (same molecule, density, screen and kernels as the timed step).
+    Untimed; the oracle runs on the host."""
+    import oracle
+    idx = np.sort(np.random.default_rng(seed).choice(g.size, npts, replace=False))
+    coords, w = g.coords[idx], g.weights[idx]
+    K = eng.get_k_multi(eng.relative(coords), torch.as_tensor(w, device=eng.device),
+                        torch.as_tensor(dm, device=eng.device), OMEGAS,
+                        tile_tol=TILE_TOL)
+    K = (0.5 * (K + K.transpose(1, 2))).cpu().numpy()
+    out = {'points': int(npts), 'of': int(g.size), 'seed': seed,
+           'gates': 'max|dK| < 1e-6 max|K|; |dE| < 3e-7 (omega 0), 1e-7 (0.3) Ha'}
+    for j, omega in enumerate(OMEGAS):
+        ref = oracle.cosx_k(mol, coords, w, dm, omega)
+        dk = K[j] - ref
+        rel = float(np.abs(dk).max() / np.abs(ref).max())
+        de = 0.25 * float(np.sum(dm * dk))
+        out['omega=%g' % omega] = {
+            'max_dK_over_max_K': rel, 'dE_quarter_tr_D_dK': de,
+            'pass': bool(rel < 1e-6 and abs(de) < (3e-7 if omega == 0.0 else 1e-7))}
+    return out
+
+
+def alkane_timing(torch, peak, steps=3, n_carbon=20, level=2):
+    """All-trans C20H42 in the def2-TZVP structure (f shells, every (3, x)
+    class): one multi-omega K build per step on its level-2 grid, the G
+    phase alone, per-class work, and parity on 1,000 points."""
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine, round32
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    from pyscf_wb97mv_fast_gb300.systems import alkane
+    mol = Molecule.build(alkane(n_carbon), 'synthetic-tzvp')
+    g = build_grids(mol, level=level)
+    rng = np.random.default_rng(20)
+    c, _ = np.linalg.qr(rng.normal(size=(mol.nao, mol.nelectron // 2)))
+    dm = 2.0 * c @ c.T
+    eng = CosxEngine(mol)
+    cd = eng.relative(g.coords)
+    wd = torch.as_tensor(g.weights, device=eng.device)
+    qd = torch.as_tensor(dm, device=eng.device)
+    K = torch.empty((len(OMEGAS), mol.nao, mol.nao), dtype=torch.float64,
+                    device=eng.device)
+
+    def step():
+        eng.get_k_multi(cd, wd, qd, OMEGAS, tile_tol=TILE_TOL, out=K, stats=False)
+    step()
+    eng.get_k_multi(cd, wd, qd, OMEGAS, tile_tol=TILE_TOL, out=K, stats=True,
+                    profile=True)
+    st = dict(eng.last_stats)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    t_step = e0.elapsed_time(e1) / 1e3 / steps
+    X = eng.ao_eval(cd)
+    F = eng.ozaki_f(X, qd)
+    del X
+    Gt = torch.empty((len(OMEGAS), mol.nao, round32(g.size)), dtype=torch.float32,
+                     device=eng.device)
+    eng.g_multi(cd, wd, F, OMEGAS, TILE_TOL, out=Gt, stats=True)
+    gst = dict(eng.last_stats)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        eng.g_multi(cd, wd, F, OMEGAS, TILE_TOL, out=Gt, stats=False)
+    e1.record()
+    torch.cuda.synchronize()
+    t_g = e0.elapsed_time(e1) / 1e3 / steps
+    del F, Gt
+    g_tf = gst['model_flops'] / t_g / 1e12
+    names = ['(%d,%d)' % (la, lb) for la in range(4) for lb in range(la + 1)]
+    out = {
+        'molecule': 'all-trans C%dH%d (C-C 1.53, C-H 1.09 A)' % (n_carbon, 2 * n_carbon + 2),
+        'basis': 'synthetic def2-TZVP structure (f shells)', 'nao': mol.nao,
+        'grid_points': int(g.size), 'grid_level': level, 'omegas': list(OMEGAS),
+        'k_tile_tol': TILE_TOL,
+        'ms_per_step': t_step * 1e3,
+        'cosx_g_tflops_step': st['model_flops'] / t_step / 1e12,
+        'g_phase_ms': t_g * 1e3, 'g_phase_tflops': g_tf,
+        'g_roofline_frac_fp32': g_tf / peak if peak else None,
+        'phases_ms': st.get('phase_ms'),
+        'tasks_kept': st['pairs_kept'], 'tasks_total': st['pairs_total'],
+        'classes': {names[c]: {'tasks_kept': gst['kept_class'][c],
+                               'model_gflop': round(gst['flops_class'][c] / 1e9, 3),
+                               'share': round(gst['flops_class'][c] /
+                                              max(gst['model_flops'], 1), 4)}
+                    for c in range(10) if gst['kept_class'][c]},
+        'parity': parity_vs_oracle(mol, g, dm, eng, torch, 1000),
+    }
+    eng.close()
+    return out
+
+
 def run_sample(oracle, mol, g, dm, idx):
     coords = g.coords[idx]
     X = oracle.ao_eval(mol, coords)
@@ -755,6 +853,10 @@ def main():
                     help='keep the compiled-in per-class kernel variants')
     ap.add_argument('--no-batched', action='store_true',
                     help='skip the batched (many molecules per launch) leg')
+    ap.add_argument('--no-alkane', action='store_true',
+                    help='skip the C20H42 / def2-TZVP (f shells) leg')
+    ap.add_argument('--no-parity', action='store_true',
+                    help='skip the oracle check of K on a grid subset')
     ap.add_argument('--batched-molecules', type=int, default=64,
                     help='water clusters in the batched leg (profiling: fewer)')
     args = ap.parse_args()
@@ -921,6 +1023,9 @@ def main():
     batched = None if (args.no_batched or world > 1) else batched_timing(
         torch, nmol=args.batched_molecules)
     k_grad = None if (args.no_grad or world > 1) else grad_timing(torch)
+    alk = None if (args.no_alkane or world > 1) else alkane_timing(torch, peak)
+    torch.cuda.empty_cache()
+    parity = None if args.no_parity else parity_vs_oracle(mol, g, dm, eng, torch, 3000)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -948,6 +1053,8 @@ def main():
             'batched': batched,
             'autotune': tuned,
             'k_grad': k_grad,
+            'alkane_c20_tzvp': alk,
+            'parity_vs_fp64_oracle': parity,
             'clocks': clocks.summary(),
             'gpu_launches': launches_step * args.steps,
             'tasks_kept': kept, 'tasks_total': total,

@@ -247,6 +247,19 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
               float* g_out, void* workspace, size_t workspace_bytes,
               void* stream, wb_cosx_stats* stats);
 
+/* The fused screen of the G kernels alone, as a mask: keep (nblk, npairs)
+ * uint8 on the device, row-major, 1 where the class kernels keep task
+ * (point block, pair) at tile_tol.  Blocks hold 32 << level points (level
+ * 0, 1, 2; nblk = ceil(round32(npts) / (32 << level))); pair k is row k of
+ * wb_cosx_export_pairs.  Same block statistics, pair bound data and screen
+ * function as wb_cosx_g; same workspace.  A test aid: replaces the device
+ * keep mask (_keep_mask_device, gpu/sgx_k.py:866-903) that the
+ * reference's superset test reads (tests/gpu/test_sgx_k.py:166-206). */
+int wb_cosx_screen_mask(wb_cosx* h, const double* coords, const double* weights,
+                        int64_t npts, const float* f, double tile_tol, int level,
+                        unsigned char* keep, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
 /* wb_cosx_g for nomega omegas and one F: the block statistics are formed
  * once, and omegas are taken in pairs by the two-omega class kernels (one
  * screen, F loads and distances per pair of omegas), as in

@@ -291,3 +291,102 @@ def cosx_k(mol, coords, weights, dm, omega=0.0, proj=None, sym=False,
     if return_parts:
         return K, X, F, G
     return K
+
+
+# -- the reference's FP64 screening bound (test aid) --------------------------
+
+_BOUND_ETA = 0.25
+
+
+def _c2s_tau(l):
+    """max over spherical columns of sum over Cartesians |c2s| (the
+    reference's per-shell tau, gpu/shellpairs.py:220)."""
+    from pyscf_wb97mv_fast_gb300.basis import cart2sph
+    return float(np.abs(cart2sph(l)).sum(axis=0).max())
+
+
+def _bound_c_grid(la, lb, p, rpa, rpb):
+    """C_ab = sup_{s >= 0} (s + |PA|)^la (s + |PB|)^lb exp(-eta p s^2) as the
+    reference finds it (gpu/shellpairs.py:123-168): the maximum over 4097
+    equally spaced s in [0, s_max], s_max where the envelope has fallen
+    below 1e-30 of its scale, times 1.01; la = lb = 0 gives 1."""
+    if la == 0 and lb == 0:
+        return np.ones_like(p)
+    L = float(la + lb)
+    rmax = np.maximum(rpa, rpb)
+    s = np.sqrt(np.maximum(0.0, (L * np.log(rmax + 1.0) + 69.0) / (_BOUND_ETA * p)))
+    for _ in range(8):
+        s = np.sqrt(np.maximum(0.0, (L * np.log(np.maximum(s, 1e-300) + rmax) + 69.0)
+                               / (_BOUND_ETA * p)))
+    x = np.linspace(0.0, 1.0, 4097)[:, None] * (1.05 * s)[None, :]
+    f = (x + rpa) ** la * (x + rpb) ** lb * np.exp(-_BOUND_ETA * p * x * x)
+    return f.max(axis=0) * 1.01
+
+
+def screen_pairs_fp64(mol, pair_cutoff=1e-14):
+    """Per kept shell pair (ish >= jsh): (ish, jsh, P (m, 3), p' (m,),
+    pref (m,), tau) over its primitive pairs, the data of the reference's
+    locked bound (gpu/shellpairs.py:286-370): pref = cmax_a cmax_b K_AB C_ab
+    2 pi / p', p' = 0.75 p, tau = tau_l(ish) tau_l(jsh)."""
+    keep = pair_keep(mol, pair_cutoff)
+    shells = mol.shells
+    xyz = mol.atom_coords()
+    out = []
+    for i, si in enumerate(shells):
+        A = xyz[si.atom]
+        ca = np.abs(np.asarray(si.coeffs).reshape(si.nprim, si.nctr)).max(axis=1)
+        for j in range(i + 1):
+            if not keep[i, j]:
+                continue
+            sj = shells[j]
+            B = xyz[sj.atom]
+            cb = np.abs(np.asarray(sj.coeffs).reshape(sj.nprim, sj.nctr)).max(axis=1)
+            al = np.repeat(np.asarray(si.exps, dtype=np.float64), sj.nprim)
+            be = np.tile(np.asarray(sj.exps, dtype=np.float64), si.nprim)
+            cab = np.repeat(ca, sj.nprim) * np.tile(cb, si.nprim)
+            p = al + be
+            P = (al[:, None] * A + be[:, None] * B) / p[:, None]
+            K = np.exp(-al * be / p * float(((A - B) ** 2).sum()))
+            C = _bound_c_grid(si.l, sj.l, p, np.linalg.norm(P - A, axis=1),
+                              np.linalg.norm(P - B, axis=1))
+            pp = (1.0 - _BOUND_ETA) * p
+            out.append((i, j, P, pp, cab * K * C * (2.0 * np.pi / pp),
+                        _c2s_tau(si.l) * _c2s_tau(sj.l)))
+    return out
+
+
+def screen_keep_fp64(mol, coords, weights, F, tol, block_pts=32,
+                     pair_cutoff=1e-14):
+    """The reference's host screen (GpuKBuilder._kept_host,
+    gpu/sgx_k.py:926-958) in FP64: keep (nblk, npairs) bool for blocks of
+    block_pts consecutive points, where tau sum_prim pref F0(p' d^2) times
+    max_g w_g max(sum_{t in A} |F_gt|, sum_{t in B} |F_gt|) >= tol, with d
+    the distance of P from the block centroid less the block radius
+    (gpu/shellpairs.py:545-555).  Returns (keep, [(ish, jsh), ...])."""
+    from scipy.special import erf
+    coords = np.asarray(coords, dtype=np.float64)
+    w = np.asarray(weights, dtype=np.float64)
+    F = np.asarray(F, dtype=np.float64)
+    ng = len(coords)
+    nblk = -(-ng // block_pts)
+    ao_loc = mol.packed()['ao_loc']
+    fw = np.abs(F) * w[:, None]
+    seg = np.add.reduceat(fw, ao_loc[:-1], axis=1)           # (ng, nbas)
+    msh = np.zeros((nblk, seg.shape[1]))
+    cen = np.zeros((nblk, 3))
+    rad = np.zeros(nblk)
+    for b in range(nblk):
+        sl = slice(b * block_pts, min(ng, (b + 1) * block_pts))
+        msh[b] = seg[sl].max(axis=0)
+        cen[b] = coords[sl].mean(axis=0)
+        rad[b] = np.linalg.norm(coords[sl] - cen[b], axis=1).max()
+    pairs = screen_pairs_fp64(mol, pair_cutoff)
+    keep = np.zeros((nblk, len(pairs)), dtype=bool)
+    for k, (i, j, P, pp, pref, tau) in enumerate(pairs):
+        d = np.linalg.norm(P[None, :, :] - cen[:, None, :], axis=2) - rad[:, None]
+        T = pp[None, :] * np.maximum(d, 0.0) ** 2
+        Ts = np.maximum(T, 1e-300)
+        f0 = np.where(T > 1e-14, 0.5 * np.sqrt(np.pi / Ts) * erf(np.sqrt(Ts)), 1.0)
+        bound = tau * (f0 * pref[None, :]).sum(axis=1)
+        keep[:, k] = bound * np.maximum(msh[:, i], msh[:, j]) >= tol
+    return keep, [(i, j) for (i, j, *_rest) in pairs]

@@ -38,7 +38,7 @@ LMAX = 3                       # highest supported shell angular momentum (f)
 ANGSTROM = 1.0 / 0.52917721092  # bohr per angstrom (CODATA 2010, PySCF's value)
 
 _SYMBOL_Z = {'H': 1, 'He': 2, 'Li': 3, 'Be': 4, 'B': 5, 'C': 6, 'N': 7,
-             'O': 8, 'F': 9, 'Ne': 10, 'S': 16, 'Cl': 17}
+             'O': 8, 'F': 9, 'Ne': 10, 'S': 16, 'Cl': 17, 'Br': 35}
 
 
 def cart_components(l):
@@ -175,6 +175,11 @@ _SYNTH = {
         'Cl': [(0, 5, 48000.0, 5.5), (0, 3, 50.0, 3.0), (0, 1, 0.55, 1.0),
                (0, 1, 0.21, 1.0), (1, 5, 360.0, 3.5), (1, 1, 0.42, 1.0),
                (1, 1, 0.14, 1.0), (2, 1, 0.65, 1.0)],
+        # [5s4p2d]
+        'Br': [(0, 6, 400000.0, 6.0), (0, 4, 400.0, 3.5), (0, 2, 10.0, 3.0),
+               (0, 1, 0.40, 1.0), (0, 1, 0.14, 1.0),
+               (1, 5, 2000.0, 4.5), (1, 3, 40.0, 3.0), (1, 1, 0.40, 1.0),
+               (1, 1, 0.13, 1.0), (2, 4, 100.0, 3.5), (2, 1, 0.50, 1.0)],
     },
     'synthetic-tzvp': {
         'H': [(0, 3, 34.0, 5.0), (0, 1, 0.32, 1.0), (0, 1, 0.10, 1.0),
@@ -205,6 +210,13 @@ _SYNTH = {
                (1, 5, 700.0, 4.0), (1, 2, 4.80, 3.0), (1, 1, 0.55, 1.0),
                (1, 1, 0.18, 1.0), (2, 1, 1.90, 1.0), (2, 1, 0.52, 1.0),
                (3, 1, 0.70, 1.0)],
+        # [6s5p4d1f]
+        'Br': [(0, 8, 1200000.0, 5.5), (0, 3, 600.0, 3.5), (0, 2, 20.0, 3.0),
+               (0, 1, 1.50, 1.0), (0, 1, 0.45, 1.0), (0, 1, 0.15, 1.0),
+               (1, 6, 4000.0, 4.5), (1, 3, 60.0, 3.0), (1, 1, 2.50, 1.0),
+               (1, 1, 0.45, 1.0), (1, 1, 0.15, 1.0),
+               (2, 4, 150.0, 3.5), (2, 1, 3.00, 1.0), (2, 1, 0.90, 1.0),
+               (2, 1, 0.30, 1.0), (3, 1, 0.50, 1.0)],
     },
 }
 

@@ -315,6 +315,27 @@ class CosxEngine:
             self.last_stats = st.as_dict()
         return out
 
+    def screen_mask(self, coords_rel, weights, f, tile_tol, level=0):
+        """(nblk, npairs) uint8 device mask of the tasks the fused G
+        kernels keep at tile_tol, for blocks of 32 << level points; pair k
+        is row k of pair_table() (wb_cosx_screen_mask)."""
+        torch = _torch()
+        if level not in (0, 1, 2):
+            raise ValueError('level must be 0, 1 or 2')
+        coords_rel, weights, npts = self._grid_args(coords_rel, weights)
+        ld = round32(npts)
+        f = device_arg(f, 'f', torch.float32, self.device, (self.nao, ld))
+        nbytes = self.workspace_bytes(npts)
+        ws = self.workspace(nbytes)
+        nblk = -(-ld // (32 << level))
+        keep = torch.zeros((nblk, max(self.npairs, 1)), dtype=torch.uint8,
+                           device=self.device)
+        _native.check(_native.lib().wb_cosx_screen_mask(
+            self._h, _native.ptr(coords_rel), _native.ptr(weights), npts,
+            _native.ptr(f), float(tile_tol), int(level), _native.ptr(keep),
+            _native.ptr(ws), nbytes, self._stream()), 'wb_cosx_screen_mask')
+        return keep[:, :self.npairs]
+
     def g_multi(self, coords_rel, weights, f, omegas, tile_tol=0.0, out=None,
                 stats=True):
         """G for several omegas from one F: (len(omegas), nao, ld) FP32,

@@ -6,6 +6,7 @@
 
 #include "boys.cuh"
 #include "launch.hpp"
+#include "screen.cuh"
 
 namespace wb {
 
@@ -1011,6 +1012,40 @@ cudaError_t launch_fma_probe(int64_t iters, int blocks, int threads,
         fma2_probe_kernel<<<blocks, threads, 0, s>>>(iters, out);
     else
         fma_probe_kernel<<<blocks, threads, 0, s>>>(iters, out);
+    return cudaGetLastError();
+}
+
+// -- screen mask (test aid) ---------------------------------------------------
+// keep[blk * npairs + k] = 1 where the fused G kernels keep task (blk, k)
+// at block level lv (blocks of 32 << lv points): the same screen_pair call,
+// on the same block statistics and pair data, as the class kernels make.
+__global__ void screen_mask_kernel(const CosxArgs A, const int lv, const int npairs,
+                                   unsigned char* __restrict__ keep) {
+    const int64_t total = (int64_t)A.nblk[lv] * npairs;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int blk = (int)(idx / npairs);
+        const int k = (int)(idx - (int64_t)blk * npairs);
+        int c = 0;
+        while (c < kClasses - 1 && !(k >= A.cls_pb[c] && k < A.cls_pe[c])) ++c;
+        bool kp = true;
+        if (A.tol > 0.0f) {
+            const int2 sh = A.pshell[k];
+            const float* ms = A.blk_msh[lv] + (int64_t)blk * A.nvshell;
+            kp = screen_pair(A.tol, A.bnd + A.pp_begin[c], A.bpref + A.pp_begin[c],
+                             A.blk_cr[lv][blk], A.khdr[k], A.ptau[k],
+                             fmaxf(ms[sh.x], ms[sh.y]));
+        }
+        keep[idx] = kp ? 1 : 0;
+    }
+}
+
+cudaError_t launch_screen_mask(const CosxArgs& a, int lv, int npairs,
+                               unsigned char* keep, cudaStream_t s) {
+    const int64_t total = (int64_t)a.nblk[lv] * npairs;
+    if (total <= 0) return cudaSuccess;
+    screen_mask_kernel<<<(unsigned)grid_stride_blocks(total, 256, 16), 256, 0, s>>>(
+        a, lv, npairs, keep);
     return cudaGetLastError();
 }
 

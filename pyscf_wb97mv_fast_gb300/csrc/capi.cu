@@ -1927,6 +1927,29 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
                       stats, launches);
 }
 
+int wb_cosx_screen_mask(wb_cosx* h, const double* coords, const double* weights,
+                        int64_t npts, const float* f, double tile_tol, int level,
+                        unsigned char* keep, void* workspace,
+                        size_t workspace_bytes, void* stream) {
+    if (!h || !f || !keep || npts <= 0 || !coords || !weights || level < 0 ||
+        level > 2)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_screen_mask: bad arguments");
+    if (!(tile_tol >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_screen_mask: tile_tol must be >= 0");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t ldt = round32(npts);
+    const WsLayout L = ws_layout(h, ldt, false);
+    if (!workspace || workspace_bytes < L.total)
+        return fail(WB_ERR_WORKSPACE, "wb_cosx_screen_mask: workspace needs " +
+                                          std::to_string(L.total) + " bytes");
+    int launches = 0;
+    int st = tile_prep(h, coords, weights, npts, ldt, f, workspace, L, s, &launches);
+    if (st != WB_OK) return st;
+    const wb::CosxArgs a = make_args(h, workspace, L, ldt, npts, f, tile_tol);
+    WB_CUDA(wb::launch_screen_mask(a, level, h->hp.npairs, keep, s));
+    return WB_OK;
+}
+
 int wb_cosx_g_multi(wb_cosx* h, const double* coords, const double* weights,
                     int64_t npts, const float* f, int nomega,
                     const double* omegas, double tile_tol, float* g_out,

@@ -25,6 +25,7 @@
 #include "launch.hpp"
 #include "cosx_device.cuh"
 #include "generated/cosx_layout.h"
+#include "screen.cuh"
 
 namespace wb {
 
@@ -47,31 +48,6 @@ constexpr int min_blocks(int cls, int nw = 1) {
     long long v = nw == 2 ? WB_COSX_MIN_BLOCKS2 : WB_COSX_MIN_BLOCKS;
     for (int i = cls; i < kClasses - 1; ++i) v >>= 4;
     return (int)(v & 15) > 0 ? (int)(v & 15) : 1;
-}
-
-// tp = (tau, tau * sum pref), f = max(msh_A, msh_B) of the block; bnd and
-// bpref start at the class's first primitive pair (hdr.z is class-local)
-__device__ __forceinline__ bool screen_pair(const float tol,
-                                            const float4* __restrict__ bnd,
-                                            const float* __restrict__ bpref,
-                                            const float4 cr, const int4 hdr,
-                                            const float2 tp, const float f) {
-    // F_0 <= 1: tau * sum(pref) * f bounds the full estimate from above
-    if (tp.y * f * 1.0001f < tol) return false;
-    const int pp0 = hdr.z, npp = hdr.w & 0xffff;
-    float b = 0.0f;
-    for (int m = pp0; m < pp0 + npp; ++m) {
-        const float4 bp = bnd[m];
-        const float dx = bp.x - cr.x, dy = bp.y - cr.y, dz = bp.z - cr.z;
-        const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
-        float d = dist - cr.w - 1e-5f * (dist + cr.w) - 1e-6f;
-        d = fmaxf(d, 0.0f);
-        const float T = bp.w * d * d;
-        const float f0 = (T > 1e-12f)
-            ? 0.88622692545f * erff(sqrtf(T)) * rsqrtf(T) : 1.0f;
-        b += bpref[m] * f0;
-    }
-    return tp.x * b * f >= tol;
 }
 
 __device__ __forceinline__ int4 shfl_int4(const int4 v, int src) {

@@ -137,6 +137,9 @@ cudaError_t launch_weight_g(const float* G, const double* w, int64_t npts,
 cudaError_t launch_dense_impl(const CosxArgs& a, int npairs, const int* pclass,
                               const int* pl, const int* estride, int nao,
                               float* out, cudaStream_t s);
+// the fused screen alone: keep (a.nblk[lv], npairs) uint8 (test aid)
+cudaError_t launch_screen_mask(const CosxArgs& a, int lv, int npairs,
+                               unsigned char* keep, cudaStream_t s);
 cudaError_t launch_boys(const float* t, int64_t n, int nmax,
                         const float4* tab, float* out, cudaStream_t s);
 // VV10 double sum; ws must hold vv10_workspace_bytes(n) bytes

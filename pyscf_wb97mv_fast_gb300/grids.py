@@ -31,7 +31,7 @@ GRID_LEVELS = {
 
 # Becke radial length scale per element (bohr)
 _RADIAL_SCALE = {'H': 0.9, 'He': 0.9, 'C': 1.3, 'N': 1.2, 'O': 1.1,
-                 'F': 1.0, 'S': 1.8, 'Cl': 1.7}
+                 'F': 1.0, 'S': 1.8, 'Cl': 1.7, 'Br': 1.9}
 
 
 class Grids:

@@ -11,6 +11,10 @@
   small-molecule drugs (C, N, O, S, F, Cl, H): a benzene ring carrying the
   halogens and a side chain of C, N, O and S, filled with hydrogens.
 
+* ``read_xyz(path_or_text)``: atoms of an XYZ file (count line, comment
+  line, then ``symbol x y z`` in Angstrom), for validation molecules such
+  as the reference's drug geometries (benchmarks/systems/drugs/*.xyz).
+
 All coordinates are returned in Angstrom as [(symbol, (x, y, z))].
 """
 import math
@@ -87,6 +91,31 @@ def alkane(n, cc=1.53, ch=1.09):
         vv = np.array([v[0], -v[1], 0.0])
         vv /= np.linalg.norm(vv)
         atoms.append(('H', tuple(cs[end] + ch * vv)))
+    return atoms
+
+
+def read_xyz(src):
+    """[(symbol, (x, y, z))] in Angstrom from an XYZ file path or its text.
+    The first line gives the atom count, the second is a comment; element
+    symbols are normalised to 'Xx' capitalisation."""
+    if '\n' not in src:
+        with open(src) as fh:
+            src = fh.read()
+    lines = src.strip('\n').splitlines()
+    try:
+        n = int(lines[0].split()[0])
+    except (IndexError, ValueError):
+        raise ValueError('XYZ: the first line must give the atom count')
+    body = lines[2:2 + n]
+    if len(body) != n:
+        raise ValueError('XYZ: %d atoms announced, %d lines found' % (n, len(body)))
+    atoms = []
+    for ln in body:
+        f = ln.split()
+        if len(f) < 4:
+            raise ValueError('XYZ: bad atom line %r' % ln)
+        sym = f[0][0].upper() + f[0][1:].lower()
+        atoms.append((sym, (float(f[1]), float(f[2]), float(f[3]))))
     return atoms
 
 

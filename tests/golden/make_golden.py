@@ -13,7 +13,7 @@ FP64 AO evaluation (gpu/ao_eval.py) and the VV10 kernel sum
 (gpu/vv10.py Vv10Kernel, NumPy path) -- is the reference's code, unmodified.
 
 Run from the repository root:
-    python tests/golden/make_golden.py <reference checkout>
+    python tests/golden/make_golden.py <reference checkout> [--only-drugs]
 The output files are committed; tests never read the reference.
 """
 import os
@@ -24,8 +24,8 @@ import numpy as np
 
 
 def _reference_root():
-    root = (sys.argv[1] if len(sys.argv) > 1
-            else os.environ.get('WB_REFERENCE_ROOT', ''))
+    args = [a for a in sys.argv[1:] if not a.startswith('--')]
+    root = args[0] if args else os.environ.get('WB_REFERENCE_ROOT', '')
     if not root or not os.path.isdir(os.path.join(root, 'pyscf_wb97mv_fast')):
         raise SystemExit('usage: make_golden.py <reference checkout> '
                          '(or set WB_REFERENCE_ROOT)')
@@ -95,8 +95,30 @@ def points(mol, rng, n):
     return np.vstack([mol.atom_coords(), far, pts])
 
 
+def write_drugs(ref_root):
+    """The reference's six validation geometries (benchmarks/systems/drugs/
+    *.xyz, README.md:118-128) as symbols and Angstrom coordinates, read with
+    this project's XYZ reader."""
+    from pyscf_wb97mv_fast_gb300.systems import read_xyz
+    ddir = os.path.join(ref_root, 'benchmarks', 'systems', 'drugs')
+    out = {}
+    for name in sorted(os.listdir(ddir)):
+        if not name.endswith('.xyz'):
+            continue
+        atoms = read_xyz(os.path.join(ddir, name))
+        tag = name[:-4]
+        out[tag + '_symbols'] = np.array([a[0] for a in atoms])
+        out[tag + '_coords'] = np.array([a[1] for a in atoms], dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, 'drugs.npz'), **out)
+
+
 def main():
-    install_stubs(_reference_root())
+    root = _reference_root()
+    if '--only-drugs' in sys.argv:
+        write_drugs(root)
+        return
+    write_drugs(root)
+    install_stubs(root)
     from pyscf_wb97mv_fast.gpu import boys as rboys
     from pyscf_wb97mv_fast.gpu import shellpairs as rsp
     from pyscf_wb97mv_fast.gpu import ao_eval as rao

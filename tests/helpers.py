@@ -91,3 +91,18 @@ class ToyNumInt:
 
     def _xc_type(self, xc_code):
         return self.xctype
+
+
+DRUGS = ('bromazepam', 'caffeine', 'chlorpromazine', 'fluoxetine', 'ibuprofen',
+         'sulfamethoxazole')
+
+
+def drug(name, basis='synthetic-tzvp'):
+    """One of the reference's six validation molecules
+    (benchmarks/systems/drugs/*.xyz), from tests/golden/drugs.npz."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                             'golden', 'drugs.npz'))
+    atoms = [(s, tuple(float(x) for x in c))
+             for s, c in zip(d[name + '_symbols'].tolist(), d[name + '_coords'])]
+    return Molecule.build(atoms, basis)

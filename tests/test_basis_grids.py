@@ -123,3 +123,19 @@ def test_oracle_partition_gives_the_native_grid():
     b = build_grids(mol, level=0, partition=oracle.becke_partition)
     np.testing.assert_array_equal(a.coords, b.coords)
     np.testing.assert_allclose(a.weights, b.weights, rtol=1e-14, atol=0)
+
+
+def test_read_xyz_and_drug_fixture():
+    from pyscf_wb97mv_fast_gb300.systems import read_xyz
+    atoms = read_xyz('3\ncomment\nO 0 0 0\nh 0.9572 0 0\nH -0.24 0.927 0\n')
+    assert [a[0] for a in atoms] == ['O', 'H', 'H']
+    assert atoms[1][1] == (0.9572, 0.0, 0.0)
+    with pytest.raises(ValueError):
+        read_xyz('4\nc\nO 0 0 0\n')
+    from helpers import DRUGS, drug
+    sizes = {n: drug(n).nao for n in DRUGS}
+    assert all(400 < v < 900 for v in sizes.values()), sizes
+    # Br carries d shells in both structures and an f shell in TZVP
+    m = drug('bromazepam')
+    assert 'Br' in m.symbols
+    assert max(sh.l for sh in m.shells if m.symbols[sh.atom] == 'Br') == 3
