@@ -247,6 +247,36 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
               float* g_out, void* workspace, size_t workspace_bytes,
               void* stream, wb_cosx_stats* stats);
 
+/* One-electron integrals of the handle's basis in FP64 on the device:
+ * s_out (overlap), t_out (kinetic energy) and v_out (attraction of natm
+ * point charges z[a] at xyz[3a..3a+2], bohr, absolute frame), each
+ * (nao, nao) row-major and symmetric.  Same contracted spherical AOs as
+ * wb_ao_eval.  xyz and z are host arrays.  The reference's SCF takes these
+ * from PySCF on the host (mol.intor('int1e_ovlp' / 'int1e_kin' /
+ * 'int1e_nuc') inside scf.hf, below staging/schedule.py:455-485); no
+ * reference GPU counterpart. */
+int wb_scf_int1e(wb_cosx* h, int natm, const double* xyz, const double* z,
+                 double* s_out, double* t_out, double* v_out, void* stream);
+
+/* Bytes of device workspace wb_hartree needs for npts points. */
+size_t wb_hartree_workspace_bytes(const wb_cosx* h, int64_t npts);
+
+/* Hartree potential of a density at grid points:
+ *   v_out[g] = sum_{mu nu} D_{mu nu} (mu nu | 1/|r - r_g|)
+ * coords (npts, 3) FP64 device (the handle frame, like wb_cosx_get_k), dm
+ * (nao, nao) FP64 device, symmetric.  Per iteration a Hermite density of
+ * every primitive pair is formed from dm; one warp per 32-point block then
+ * sums the pairs that pass the COSX kernels' locked bound times
+ * (2 - delta_AB) sum |D_AB| >= tol (0 keeps every pair).  fp64 = 1: FP64
+ * throughout; 0: FP32 Boys, recurrence and sums over 32-pair chunks, FP64
+ * across chunks.  Bitwise reproducible.  *tasks_kept (if not null, a
+ * synchronisation) receives the kept (block, pair) count.  With
+ * J = X^T (w o v) X it is the SCF's Coulomb matrix on the SGX grid (the
+ * reference's SCF gets J from PySCF's SGX get_jk, core/sgx_patch.py:33-53). */
+int wb_hartree(wb_cosx* h, const double* coords, int64_t npts, const double* dm,
+               double tol, int fp64, double* v_out, void* workspace,
+               size_t workspace_bytes, void* stream, int64_t* tasks_kept);
+
 /* The fused screen of the G kernels alone, as a mask: keep (nblk, npairs)
  * uint8 on the device, row-major, 1 where the class kernels keep task
  * (point block, pair) at tile_tol.  Blocks hold 32 << level points (level

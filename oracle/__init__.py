@@ -57,9 +57,12 @@ def _load():
         _lib.oracle_ao_eval_deriv1.argtypes = basis + [P, I64, P]
         _lib.oracle_pair_keep.argtypes = basis + [D, P]
         _lib.oracle_becke_partition.argtypes = [P, I64, P, P, I, P]
+        _lib.oracle_int1e_st.argtypes = basis + [P, P]
+        _lib.oracle_hartree.argtypes = basis + [P, I64, P, P]
         for f in ('oracle_boys', 'oracle_int3c1e', 'oracle_cosx_g',
                   'oracle_ao_eval', 'oracle_vv10_sum', 'oracle_ao_eval_deriv1',
-                  'oracle_pair_keep', 'oracle_becke_partition'):
+                  'oracle_pair_keep', 'oracle_becke_partition', 'oracle_int1e_st',
+                  'oracle_hartree'):
             getattr(_lib, f).restype = I
     return _lib
 
@@ -120,6 +123,30 @@ def becke_partition(points, owner, atom_coords):
                                       len(at), _p(out)) != 0:
         raise MemoryError('oracle_becke_partition')
     return out
+
+
+def int1e(mol):
+    """(S, T, V) FP64 (nao, nao): overlap, kinetic energy and the nuclear
+    attraction of the molecule's own nuclei (V from the dense 3-centre
+    integrals at the nuclei)."""
+    b = _Basis(mol)
+    S = np.zeros((b.nao, b.nao))
+    T = np.zeros((b.nao, b.nao))
+    _load().oracle_int1e_st(*b.args, _p(S), _p(T))
+    xyz = np.ascontiguousarray(mol.atom_coords(), dtype=np.float64)
+    A = int3c1e(mol, xyz)
+    V = -np.einsum('c,cmn->mn', np.asarray(mol.atom_charges(), dtype=np.float64), A)
+    return S, T, V
+
+
+def hartree(mol, coords, dm):
+    """v_H(g) = sum D_{mu nu} (mu nu | 1/|r - g|), FP64, every pair."""
+    b = _Basis(mol)
+    c = np.ascontiguousarray(coords, dtype=np.float64)
+    D = np.ascontiguousarray(dm, dtype=np.float64)
+    v = np.zeros(len(c))
+    _load().oracle_hartree(*b.args, _p(c), len(c), _p(D), _p(v))
+    return v
 
 
 def pair_keep(mol, pair_cutoff=1e-14):

@@ -523,3 +523,139 @@ int oracle_becke_partition(const double* pts, int64_t n, const int* owner,
     free(rinv);
     return fail;
 }
+
+/* ---- one-electron integrals and the Hartree potential (SCF oracle) ------ */
+
+/* 1-D Hermite coefficients E[i][j][t] for i <= la, j <= lbx (lbx <= 5) */
+#define EJX 6
+#define ETX 10
+static void hermite_ext(int la, int lbx, double p, double xpa, double xpb,
+                        double E[LMAX + 1][EJX][ETX]) {
+    memset(E, 0, sizeof(double) * (LMAX + 1) * EJX * ETX);
+    const double inv2p = 0.5 / p;
+    E[0][0][0] = 1.0;
+    for (int i = 1; i <= la; ++i)
+        for (int t = 0; t <= i; ++t) {
+            double v = 0.0;
+            if (t > 0) v += E[i - 1][0][t - 1] * inv2p;
+            if (t <= i - 1) v += xpa * E[i - 1][0][t];
+            if (t + 1 <= i - 1) v += (t + 1) * E[i - 1][0][t + 1];
+            E[i][0][t] = v;
+        }
+    for (int j = 1; j <= lbx; ++j)
+        for (int i = 0; i <= la; ++i)
+            for (int t = 0; t <= i + j; ++t) {
+                double v = 0.0;
+                if (t > 0) v += E[i][j - 1][t - 1] * inv2p;
+                if (t <= i + j - 1) v += xpb * E[i][j - 1][t];
+                if (t + 1 <= i + j - 1) v += (t + 1) * E[i][j - 1][t + 1];
+                E[i][j][t] = v;
+            }
+}
+
+/* Overlap S and kinetic T (nao, nao) in FP64 (Helgaker, Jorgensen, Olsen
+ * ch. 9: S = K (pi/p)^(3/2) prod E^{ij}_0; the kinetic operator per axis
+ * -2 b^2 S_(i,j+2) + b (2j+1) S_ij - j(j-1)/2 S_(i,j-2)). */
+int oracle_int1e_st(OBASIS_ARGS, double* S, double* T) {
+    obasis b;
+    make_basis(&b, OBASIS_PASS);
+    int* ao = ao_offsets(&b);
+    const int nao = ao[nbas];
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int ish = 0; ish < nbas; ++ish)
+        for (int jsh = 0; jsh < nbas; ++jsh) {
+            const int la = b.shell_l[ish], lb = b.shell_l[jsh];
+            const int npi = b.shell_nprim[ish], npj = b.shell_nprim[jsh];
+            const int nci = b.shell_nctr[ish], ncj = b.shell_nctr[jsh];
+            const int nca = ncart(la), ncb = ncart(lb), nsa = nsph(la), nsb = nsph(lb);
+            const double* A = b.atom_coords + 3 * b.shell_atom[ish];
+            const double* B = b.atom_coords + 3 * b.shell_atom[jsh];
+            double d2 = 0.0;
+            for (int x = 0; x < 3; ++x) d2 += (A[x] - B[x]) * (A[x] - B[x]);
+            for (int ci = 0; ci < nci; ++ci)
+                for (int cj = 0; cj < ncj; ++cj) {
+                    double cs[100], ct[100];
+                    for (int q = 0; q < 100; ++q) cs[q] = ct[q] = 0.0;
+                    for (int a = 0; a < npi; ++a)
+                        for (int c = 0; c < npj; ++c) {
+                            const double al = b.exps[b.shell_exp_off[ish] + a];
+                            const double be = b.exps[b.shell_exp_off[jsh] + c];
+                            const double p = al + be;
+                            const double cc = b.coeffs[b.shell_coef_off[ish] + a * nci + ci] *
+                                              b.coeffs[b.shell_coef_off[jsh] + c * ncj + cj] *
+                                              exp(-al * be / p * d2);
+                            double E[3][LMAX + 1][EJX][ETX];
+                            for (int x = 0; x < 3; ++x) {
+                                const double P = (al * A[x] + be * B[x]) / p;
+                                hermite_ext(la, lb + 2, p, P - A[x], P - B[x], E[x]);
+                            }
+                            const double n3 = cc * pow(M_PI / p, 1.5);
+                            for (int qa = 0; qa < nca; ++qa) {
+                                int ia[3];
+                                cart_comp(la, qa, &ia[0], &ia[1], &ia[2]);
+                                for (int qb = 0; qb < ncb; ++qb) {
+                                    int ib[3];
+                                    cart_comp(lb, qb, &ib[0], &ib[1], &ib[2]);
+                                    double s1[3], t1[3];
+                                    for (int x = 0; x < 3; ++x) {
+                                        const int i = ia[x], j = ib[x];
+                                        s1[x] = E[x][i][j][0];
+                                        t1[x] = -2.0 * be * be * E[x][i][j + 2][0] +
+                                                be * (2 * j + 1) * E[x][i][j][0] -
+                                                (j >= 2 ? 0.5 * j * (j - 1) * E[x][i][j - 2][0] : 0.0);
+                                    }
+                                    cs[qa * ncb + qb] += n3 * s1[0] * s1[1] * s1[2];
+                                    ct[qa * ncb + qb] += n3 * (t1[0] * s1[1] * s1[2] +
+                                                               s1[0] * t1[1] * s1[2] +
+                                                               s1[0] * s1[1] * t1[2]);
+                                }
+                            }
+                        }
+                    for (int m1 = 0; m1 < nsa; ++m1)
+                        for (int m2 = 0; m2 < nsb; ++m2) {
+                            double vs = 0.0, vt = 0.0;
+                            for (int qa = 0; qa < nca; ++qa)
+                                for (int qb = 0; qb < ncb; ++qb) {
+                                    const double w = b.c2s[la][qa * nsa + m1] *
+                                                     b.c2s[lb][qb * nsb + m2];
+                                    vs += w * cs[qa * ncb + qb];
+                                    vt += w * ct[qa * ncb + qb];
+                                }
+                            const int64_t e = (int64_t)(ao[ish] + ci * nsa + m1) * nao +
+                                              ao[jsh] + cj * nsb + m2;
+                            S[e] = vs;
+                            T[e] = vt;
+                        }
+                }
+        }
+    free(ao);
+    return 0;
+}
+
+/* Hartree potential v[g] = sum_{mu nu} D_{mu nu} (mu nu | 1/|r - g|) at ng
+ * points (absolute frame), every shell pair (no screening), FP64. */
+int oracle_hartree(OBASIS_ARGS, const double* coords, int64_t ng, const double* D,
+                   double* v) {
+    obasis b;
+    make_basis(&b, OBASIS_PASS);
+    int* ao = ao_offsets(&b);
+    const int nao = ao[nbas];
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int64_t g = 0; g < ng; ++g) {
+        double acc = 0.0;
+        double A[16 * 16];
+        for (int ish = 0; ish < nbas; ++ish)
+            for (int jsh = 0; jsh <= ish; ++jsh) {
+                int ni, nj;
+                pair_block(&b, ish, jsh, coords + 3 * g, 0.0, A, &ni, &nj);
+                const double w = ish == jsh ? 1.0 : 2.0;
+                for (int m = 0; m < ni; ++m)
+                    for (int n = 0; n < nj; ++n)
+                        acc += w * D[(int64_t)(ao[ish] + m) * nao + ao[jsh] + n] *
+                               A[m * 16 + n];
+            }
+        v[g] = acc;
+    }
+    free(ao);
+    return 0;
+}

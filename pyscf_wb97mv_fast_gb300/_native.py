@@ -38,7 +38,8 @@ NCLASS = 10
 EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_cosx_export_pairs', 'wb_cosx_workspace_bytes',
             'wb_cosx_get_k', 'wb_cosx_get_k_multi', 'wb_cosx_g',
-            'wb_cosx_g_multi', 'wb_cosx_screen_mask', 'wb_ao_eval',
+            'wb_cosx_g_multi', 'wb_cosx_screen_mask', 'wb_scf_int1e',
+            'wb_hartree_workspace_bytes', 'wb_hartree', 'wb_ao_eval',
             'wb_ao_eval_deriv1', 'wb_xc_rho', 'wb_xc_aow',
             'wb_int3c1e_dense',
             'wb_boys_fp32', 'wb_boys_f64_host', 'wb_model_flops_per_point',
@@ -141,6 +142,10 @@ def _declare(lib):
                                    ctypes.POINTER(WbCosxStats)]),
         'wb_cosx_screen_mask': (_INT, [_P, _P, _P, _I64, _P, _D, _INT, _P, _P,
                                        ctypes.c_size_t, _P]),
+        'wb_scf_int1e': (_INT, [_P, _INT, _P, _P, _P, _P, _P, _P]),
+        'wb_hartree_workspace_bytes': (ctypes.c_size_t, [_P, _I64]),
+        'wb_hartree': (_INT, [_P, _P, _I64, _P, _D, _INT, _P, _P, ctypes.c_size_t,
+                              _P, ctypes.POINTER(ctypes.c_int64)]),
         'wb_ao_eval': (_INT, [_P, _P, _I64, _P, _P]),
         'wb_ao_eval_deriv1': (_INT, [_P, _P, _I64, _P, _P]),
         'wb_xc_rho': (_INT, [_P, _P, _P, _I64, _I64, _INT, _P, _P]),

@@ -343,6 +343,20 @@ class Molecule:
     def nelectron(self):
         return int(sum(_SYMBOL_Z[s] for s in self.symbols))
 
+    def atom_charges(self):
+        """Nuclear charges (all-electron) of the atoms."""
+        return np.array([_SYMBOL_Z[s] for s in self.symbols], dtype=np.int64)
+
+    def energy_nuc(self):
+        """Nuclear repulsion energy (hartree) of the point charges."""
+        z = self.atom_charges().astype(np.float64)
+        r = self._coords
+        e = 0.0
+        for i in range(len(z)):
+            d = np.linalg.norm(r[:i] - r[i], axis=1)
+            e += float(np.sum(z[i] * z[:i] / d))
+        return e
+
     def ao_loc_nr(self):
         return self._ao_loc.copy()
 

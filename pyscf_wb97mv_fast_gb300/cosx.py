@@ -315,6 +315,50 @@ class CosxEngine:
             self.last_stats = st.as_dict()
         return out
 
+    def int1e(self, nuc_xyz=None, nuc_z=None):
+        """(S, T, V) FP64 (nao, nao) on the device: overlap, kinetic energy
+        and nuclear attraction (wb_scf_int1e).  The nuclei default to the
+        molecule's own (absolute frame, bohr; all-electron charges)."""
+        torch = _torch()
+        xyz = np.ascontiguousarray(self.mol.atom_coords() if nuc_xyz is None
+                                   else nuc_xyz, dtype=np.float64).reshape(-1, 3)
+        z = np.ascontiguousarray(self.mol.atom_charges() if nuc_z is None else nuc_z,
+                                 dtype=np.float64).ravel()
+        if len(z) != len(xyz):
+            raise ValueError('one charge per nucleus')
+        out = [torch.empty((self.nao, self.nao), dtype=torch.float64, device=self.device)
+               for _ in range(3)]
+        _native.check(_native.lib().wb_scf_int1e(
+            self._h, len(z), xyz.ctypes.data_as(_native.ctypes.c_void_p),
+            z.ctypes.data_as(_native.ctypes.c_void_p), *[_native.ptr(o) for o in out],
+            self._stream()), 'wb_scf_int1e')
+        return tuple(out)
+
+    def hartree(self, coords_rel, dm, tol=0.0, fp64=True, out=None, stats=False):
+        """Hartree potential (npts,) FP64 on the device at coords_rel (the
+        kernel frame) of the symmetric density dm (wb_hartree); tol screens
+        (block, pair) tasks by the locked bound times the pair's |D|."""
+        torch = _torch()
+        coords_rel = device_arg(coords_rel, 'coords_rel', torch.float64, self.device)
+        if coords_rel.dim() != 2 or coords_rel.shape[1] != 3:
+            raise ValueError('coords_rel must be (npts, 3)')
+        npts = int(coords_rel.shape[0])
+        D = self._dm_arg(dm, 'dm')
+        nbytes = int(_native.lib().wb_hartree_workspace_bytes(self._h, npts))
+        ws = self.workspace(nbytes)
+        if out is None:
+            out = torch.empty(npts, dtype=torch.float64, device=self.device)
+        device_out(out, 'out', torch.float64, self.device, (npts,))
+        kept = _native.ctypes.c_int64(-1)
+        _native.check(_native.lib().wb_hartree(
+            self._h, _native.ptr(coords_rel), npts, _native.ptr(D), float(tol),
+            1 if fp64 else 0, _native.ptr(out), _native.ptr(ws), nbytes,
+            self._stream(), _native.ctypes.byref(kept) if stats else None),
+            'wb_hartree')
+        if stats:
+            self.last_hartree_kept = int(kept.value)
+        return out
+
     def screen_mask(self, coords_rel, weights, f, tile_tol, level=0):
         """(nblk, npairs) uint8 device mask of the tasks the fused G
         kernels keep at tile_tol, for blocks of 32 << level points; pair k

@@ -19,6 +19,7 @@
 #include "cosx_fp64.hpp"
 #include "cosx_grad64.hpp"
 #include "generated/cosx_layout.h"
+#include "scf.hpp"
 #include "launch.hpp"
 #include "ozaki.hpp"
 #include "wb97mv_gb300.h"
@@ -111,6 +112,13 @@ int upload_constants() {
     for (int j = 0; j < 64; ++j)
         t64[j] = (double)std::exp2l(-(long double)j / 64.0L);   // rounded once
     WB_CUDA(wb::upload_exp_table(t64));
+    {
+        double all[110];
+        int o = 0;
+        for (int l = 0; l < 4; ++l)
+            for (size_t i = 0; i < c[l].size(); ++i) all[o++] = c[l][i];
+        WB_CUDA(wb::scf::upload_int1e_c2s(all));
+    }
     g_const_dev.insert(dev);
     return WB_OK;
 }
@@ -198,6 +206,16 @@ struct wb_cosx {
     double* f64_alpha = nullptr;     // bra exponent per primitive pair
     double* f64_vsxyz = nullptr;     // virtual shell centres (3 each)
     int* vs_atom = nullptr;          // virtual shell atoms
+    double origin[3] = {0.0, 0.0, 0.0};   // frame of the device coordinates
+    // SCF helpers (wb_scf_int1e, wb_hartree), set up on first use: per pair
+    // L = la + lb; per primitive pair the offset of its Hermite density and
+    // p in FP32; nuclei (x, y, z, Z) in the handle frame
+    int* pair_L = nullptr;
+    long long* dh_off = nullptr;
+    float* p32 = nullptr;
+    int64_t ndh = 0;
+    double* nuc = nullptr;
+    int nuc_cap = 0;
 };
 
 namespace {
@@ -672,6 +690,80 @@ int ensure_fp64(wb_cosx* h) {
     return WB_OK;
 }
 
+// per-pair L, per-primitive-pair Hermite-density offsets and FP32 p of
+// the Hartree potential (first wb_hartree call on the handle)
+int ensure_hartree(wb_cosx* h) {
+    if (h->pair_L) return WB_OK;
+    const wb::HostPairs& hp = h->hp;
+    std::vector<int> L((size_t)std::max(hp.npairs, 1), 0);
+    std::vector<long long> off((size_t)std::max(hp.npp, 1), 0);
+    std::vector<float> p32((size_t)std::max(hp.npp, 1), 0.0f);
+    long long tot = 0;
+    for (int k = 0; k < hp.npairs; ++k) {
+        const int l = hp.vsh[hp.pshell[2 * k]].l + hp.vsh[hp.pshell[2 * k + 1]].l;
+        L[k] = l;
+        const int pp0 = hp.hdr[4 * k + 2], npp = hp.hdr[4 * k + 3] & 0xffff;
+        for (int m = pp0; m < pp0 + npp; ++m) {
+            off[m] = tot;
+            tot += (l + 1) * (l + 2) * (l + 3) / 6;
+        }
+    }
+    for (int m = 0; m < hp.npp; ++m) p32[m] = (float)hp.p[m];
+    int* dL = nullptr;
+    long long* dO = nullptr;
+    float* dP = nullptr;
+    cudaError_t e = cudaMalloc(&dL, sizeof(int) * L.size());
+    if (e == cudaSuccess) e = cudaMalloc(&dO, sizeof(long long) * off.size());
+    if (e == cudaSuccess) e = cudaMalloc(&dP, sizeof(float) * p32.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpy(dL, L.data(), sizeof(int) * L.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(dO, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(dP, p32.data(), sizeof(float) * p32.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        for (void* q : {(void*)dL, (void*)dO, (void*)dP})
+            if (q) cudaFree(q);
+        return cuda_fail(e, "Hartree pair tables");
+    }
+    h->pair_L = dL;
+    h->dh_off = dO;
+    h->p32 = dP;
+    h->ndh = std::max<long long>(tot, 1);
+    return WB_OK;
+}
+
+struct HartreeLayout {
+    size_t counters = 0, cr = 0, dabs = 0, dh64 = 0, dh32 = 0, total = 0;
+};
+
+HartreeLayout hartree_layout(const wb_cosx* h, int64_t npts, int64_t ndh) {
+    HartreeLayout L;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align256(off + bytes);
+        return o;
+    };
+    const int64_t nblk = (npts + 31) / 32;
+    L.counters = take(256);
+    L.cr = take(sizeof(float4) * (size_t)std::max<int64_t>(nblk, 1));
+    L.dabs = take(sizeof(float) * (size_t)std::max(h->hp.npairs, 1));
+    L.dh64 = take(sizeof(double) * (size_t)ndh);
+    L.dh32 = take(sizeof(float) * (size_t)ndh);
+    L.total = off;
+    return L;
+}
+
+int64_t hartree_ndh(const wb::HostPairs& hp) {
+    int64_t tot = 0;
+    for (int k = 0; k < hp.npairs; ++k) {
+        const int l = hp.vsh[hp.pshell[2 * k]].l + hp.vsh[hp.pshell[2 * k + 1]].l;
+        tot += (int64_t)(hp.hdr[4 * k + 3] & 0xffff) * (l + 1) * (l + 2) * (l + 3) / 6;
+    }
+    return std::max<int64_t>(tot, 1);
+}
+
 struct WsLayout64 {
     WsLayout base;                  // counters, work, block statistics
     size_t X = 0, F64 = 0, F32 = 0, G64 = 0, WG = 0, total = 0;
@@ -819,6 +911,7 @@ int wb_cosx_create(const wb_basis* basis, const double origin[3],
         wb_cosx_destroy(h);
         return code;
     };
+    for (int x = 0; x < 3; ++x) h->origin[x] = origin[x];
     if (cudaGetDevice(&h->device) != cudaSuccess) return cleanup(cuda_fail(cudaGetLastError(), "cudaGetDevice"));
     cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device);
     if ((st = upload_constants()) != WB_OK) return cleanup(st);
@@ -1021,6 +1114,8 @@ int wb_cosx_destroy(wb_cosx* h) {
     if (h->f64_alpha) cudaFree(h->f64_alpha);
     if (h->f64_vsxyz) cudaFree(h->f64_vsxyz);
     if (h->vs_atom) cudaFree(h->vs_atom);
+    for (void* q : {(void*)h->pair_L, (void*)h->dh_off, (void*)h->p32, (void*)h->nuc})
+        if (q) cudaFree(q);
     delete h;
     return WB_OK;
 }
@@ -1925,6 +2020,123 @@ int wb_cosx_g(wb_cosx* h, const double* coords, const double* weights,
     if (st != WB_OK) return st;
     return read_stats(h, workspace, L, (ldt / 32) * (int64_t)h->hp.npairs, s,
                       stats, launches);
+}
+
+int wb_scf_int1e(wb_cosx* h, int natm, const double* xyz, const double* z,
+                 double* s_out, double* t_out, double* v_out, void* stream) {
+    if (!h || natm < 0 || (natm && (!xyz || !z)) || !s_out || !t_out || !v_out)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_scf_int1e: bad arguments");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int st = ensure_fp64(h);
+    if (st != WB_OK) return st;
+    if (natm > h->nuc_cap) {
+        WB_CUDA(cudaStreamSynchronize(s));
+        if (h->nuc) cudaFree(h->nuc);
+        h->nuc = nullptr;
+        h->nuc_cap = 0;
+        WB_CUDA(cudaMalloc(&h->nuc, sizeof(double) * 4 * (size_t)natm));
+        h->nuc_cap = natm;
+    }
+    if (natm) {
+        std::vector<double> nz(4 * (size_t)natm);
+        for (int a = 0; a < natm; ++a) {
+            for (int x = 0; x < 3; ++x) nz[3 * a + x] = xyz[3 * a + x] - h->origin[x];
+            nz[3 * (size_t)natm + a] = z[a];
+        }
+        WB_CUDA(cudaMemcpyAsync(h->nuc, nz.data(), sizeof(double) * nz.size(),
+                                cudaMemcpyHostToDevice, s));
+        WB_CUDA(cudaStreamSynchronize(s));     // nz is a host temporary
+    }
+    wb::scf::Int1eArgs a;
+    a.nbas = h->nbas;
+    a.nao = h->hp.nao;
+    a.sh_l = h->sh_l; a.sh_np = h->sh_np; a.sh_nc = h->sh_nc;
+    a.sh_eoff = h->sh_eoff; a.sh_coff = h->sh_coff; a.sh_ao0 = h->sh_ao0;
+    a.sh_ctr = h->sh_ctr; a.exps = h->exps; a.coeffs = h->coeffs;
+    a.natm = natm;
+    a.nuc_xyz = h->nuc;
+    a.nuc_z = h->nuc + 3 * (size_t)natm;
+    a.boys = h->f64_boys;
+    a.S = s_out; a.T = t_out; a.V = v_out;
+    WB_CUDA(wb::scf::launch_int1e(a, s));
+    return WB_OK;
+}
+
+size_t wb_hartree_workspace_bytes(const wb_cosx* h, int64_t npts) {
+    if (!h || npts < 0) return 0;
+    return hartree_layout(h, npts, hartree_ndh(h->hp)).total;
+}
+
+int wb_hartree(wb_cosx* h, const double* coords, int64_t npts, const double* dm,
+               double tol, int fp64, double* v_out, void* workspace,
+               size_t workspace_bytes, void* stream, int64_t* tasks_kept) {
+    if (!h || npts <= 0 || !coords || !dm || !v_out || !(tol >= 0.0))
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_hartree: bad arguments");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int st = ensure_fp64(h);
+    if (st != WB_OK) return st;
+    if ((st = ensure_hartree(h)) != WB_OK) return st;
+    const HartreeLayout L = hartree_layout(h, npts, h->ndh);
+    if (!workspace || workspace_bytes < L.total)
+        return fail(WB_ERR_WORKSPACE, "wb_hartree: workspace needs " +
+                                          std::to_string(L.total) + " bytes");
+    WB_CUDA(cudaMemsetAsync(at<void>(workspace, L.counters), 0, 256, s));
+    wb::scf::DhArgs d;
+    std::memset(&d, 0, sizeof(d));
+    d.npairs = h->hp.npairs;
+    d.nao = h->hp.nao;
+    d.D = dm;
+    d.hdr = h->hdr;
+    d.pclass = h->pclass;
+    d.pcls_l = h->pclass;
+    d.E = h->f64_E;
+    for (int c = 0; c < wb::NCLASS; ++c) {
+        d.e_base[c] = h->f64_ebase[c];
+        d.pp_begin[c] = h->hp.cls[c].pp_begin;
+    }
+    d.pref = h->pref;
+    d.dh_off = h->dh_off;
+    d.dh64 = at<double>(workspace, L.dh64);
+    d.dh32 = at<float>(workspace, L.dh32);
+    d.pair_dabs = at<float>(workspace, L.dabs);
+    WB_CUDA(wb::scf::launch_dh(d, s));
+    const int nblk = (int)((npts + 31) / 32);
+    WB_CUDA(wb::scf::launch_block_geom(coords, npts, nblk, at<float4>(workspace, L.cr), s));
+    wb::scf::HartreeArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.coords = coords;
+    a.npts = npts;
+    a.blk_cr = at<float4>(workspace, L.cr);
+    a.nblk = nblk;
+    a.npairs = h->hp.npairs;
+    a.hdr = h->hdr;
+    a.pair_L = h->pair_L;
+    a.ptau = h->ptau;
+    a.bnd = h->bnd;
+    a.bpref = h->bpref;
+    a.pair_dabs = d.pair_dabs;
+    a.P = h->f64_P;
+    a.p = h->p;
+    a.geo = h->geo;
+    a.p32 = h->p32;
+    a.dh_off = h->dh_off;
+    a.dh64 = d.dh64;
+    a.dh32 = d.dh32;
+    a.boys32 = h->boys;
+    a.boys64 = h->f64_boys;
+    a.tol = tol > 0.0 ? (float)(tol / 1.001) : 0.0f;
+    if (tol > 0.0 && a.tol <= 0.0f) a.tol = 1e-38f;
+    a.v = v_out;
+    a.work = at<int>(workspace, L.counters);
+    a.kept = at<unsigned long long>(workspace, L.counters + 64);
+    WB_CUDA(wb::scf::launch_hartree(a, fp64 != 0, s));
+    if (tasks_kept) {
+        unsigned long long kept = 0;
+        WB_CUDA(cudaMemcpyAsync(&kept, a.kept, sizeof(kept), cudaMemcpyDeviceToHost, s));
+        WB_CUDA(cudaStreamSynchronize(s));
+        *tasks_kept = (int64_t)kept;
+    }
+    return WB_OK;
 }
 
 int wb_cosx_screen_mask(wb_cosx* h, const double* coords, const double* weights,

@@ -870,6 +870,76 @@ def layout_source():
         '}  // namespace wb', ''])
 
 
+def _hartree_ridx(L, t, u, v):
+    """Packed index of R_tuv (t + u + v <= L): v-major, then u, then t."""
+    k = 0
+    for vv in range(v):
+        for uu in range(L - vv + 1):
+            k += L - vv - uu + 1
+    for uu in range(u):
+        k += L - v - uu + 1
+    return k + t
+
+
+def hartree_source():
+    """Straight-line Hermite Coulomb sums of the Hartree-potential kernel
+    (csrc/scf_kernels.cu): for L = 0..6,
+
+        hermite_dot_L(r0, x, y, z, dh) = sum_{t+u+v<=L} dh[idx(t,u,v)] R_tuv
+
+    with R^(n)_000 = r0[n] and the McMurchie-Davidson recurrence
+    R^(n)_{t+1,u,v} = t R^(n+1)_{t-1,u,v} + x R^(n+1)_{t,u,v} (u, v the same
+    with y, z), written level by level as named values (no in-place
+    array), so the compiler sees plain register code."""
+    out = ['// Generated by csrc/gen_cosx.py (hartree_source); do not edit.',
+           '#pragma once', '', 'namespace wb {', 'namespace scf {', '']
+    for L in range(7):
+        out.append('template<typename Real>')
+        out.append('__device__ __forceinline__ Real hermite_dot_%d(const Real* r0, '
+                   'const Real x, const Real y, const Real z, const Real* dh) {' % L)
+        names = {}
+
+        def nm(n, t, u, v):
+            return 'r%d_%d_%d_%d' % (n, t, u, v)
+        for n in range(L, -1, -1):
+            m = L - n
+            for v in range(m + 1):
+                for u in range(m + 1 - v):
+                    for t in range(m + 1 - u - v):
+                        if t == u == v == 0:
+                            expr = 'r0[%d]' % n
+                        elif t > 0:
+                            a = nm(n + 1, t - 1, u, v)
+                            expr = 'x * %s' % a
+                            if t >= 2:
+                                expr = 'Real(%d) * %s + %s' % (t - 1, nm(n + 1, t - 2, u, v), expr)
+                        elif u > 0:
+                            a = nm(n + 1, 0, u - 1, v)
+                            expr = 'y * %s' % a
+                            if u >= 2:
+                                expr = 'Real(%d) * %s + %s' % (u - 1, nm(n + 1, 0, u - 2, v), expr)
+                        else:
+                            a = nm(n + 1, 0, 0, v - 1)
+                            expr = 'z * %s' % a
+                            if v >= 2:
+                                expr = 'Real(%d) * %s + %s' % (v - 1, nm(n + 1, 0, 0, v - 2), expr)
+                        out.append('    const Real %s = %s;' % (nm(n, t, u, v), expr))
+        terms = []
+        for v in range(L + 1):
+            for u in range(L + 1 - v):
+                for t in range(L + 1 - u - v):
+                    terms.append((_hartree_ridx(L, t, u, v), nm(0, t, u, v)))
+        terms.sort()
+        out.append('    Real s = Real(0);')
+        for q, name in terms:
+            out.append('    s += dh[%d] * %s;' % (q, name))
+        out.append('    return s;')
+        out.append('}')
+        out.append('')
+    out += ['}  // namespace scf', '}  // namespace wb', '']
+    return '\n'.join(out)
+
+
 def _write_if_changed(path, src):
     os.makedirs(os.path.dirname(path), exist_ok=True)
     old = None
@@ -887,6 +957,8 @@ def write(path=None):
     _write_if_changed(path, source())
     _write_if_changed(os.path.join(os.path.dirname(path), 'cosx_layout.h'),
                       layout_source())
+    _write_if_changed(os.path.join(os.path.dirname(path), 'hartree_r.cuh'),
+                      hartree_source())
     return path
 
 

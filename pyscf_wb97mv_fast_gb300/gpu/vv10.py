@@ -167,6 +167,41 @@ def _prepare_dm(dm, hermi):
     return dm
 
 
+def vv10_energy_fock(eng, g, D, nlc_pars, kernel=None):
+    """E_nl and V_nl of one density on a device grid, all on the device:
+    g holds coordinates (engine frame), weights and the deriv-1 AO values
+    X (4, nao, ld) (scf.DeviceGrid); D (nao, nao) FP64 device.  The same
+    steps as gpu_nr_nlc_vxc for one parameter set (b, C) with factor 1:
+    GGA density, threshold rho >= 1e-8, pointwise terms, the pair sum, the
+    GGA potential and vmat = X^T (w v) X + transpose.  Returns (E_nl
+    device scalar, V_nl (nao, nao))."""
+    torch = _torch()
+    kernel = kernel or Vv10Kernel(0.0)
+    n = g.n
+    ao = g.X[:, :, :n]
+    w = g.weights
+    T = D @ ao[0]
+    rho0 = (T * ao[0]).sum(dim=0)
+    grad = 2.0 * torch.einsum('mp,dmp->dp', T, ao[1:4])
+    ind = rho0 >= THRESH
+    q, W0, kappa, dW0dR, dW0dG, dKdR, Beta = vv10_pointwise(
+        rho0[ind], grad[:, ind], w[ind], nlc_pars)
+    F, U, W = kernel.kernel_sum(g.coords[ind].to(torch.float32), q, W0, kappa)
+    exc = torch.zeros(n, dtype=torch.float64, device=D.device)
+    v0 = torch.zeros_like(exc)
+    v1 = torch.zeros_like(exc)
+    exc[ind] = Beta + 0.5 * F
+    v0[ind] = Beta + F + 1.5 * (U * dKdR + W * dW0dR)
+    v1[ind] = 1.5 * W * dW0dG
+    e_nl = (rho0 * w * exc).sum()
+    wv = torch.empty((4, n), dtype=torch.float64, device=D.device)
+    wv[0] = 0.5 * v0 * w
+    wv[1:4] = 2.0 * v1[None, :] * grad * w[None, :]
+    aow = torch.einsum('dmp,dp->mp', ao, wv)
+    vmat = ao[0] @ aow.T
+    return e_nl, vmat + vmat.T
+
+
 def gpu_nr_nlc_vxc(ctx, ni, mol, grids, xc_code, dm, relativity=0, hermi=1,
                    max_memory=2000, verbose=None):
     """GPU replacement of NumInt.nr_nlc_vxc (RKS ground state)."""

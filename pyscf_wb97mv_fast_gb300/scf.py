@@ -1,0 +1,426 @@
+"""Device-resident RKS SCF of the wB97M-V / COSX(pjs) hot path.
+
+The reference runs its SCF through PySCF's loop on the host (scf.hf.kernel)
+with the GPU K, XC and VV10 hooked in, staged by StagedSCF
+(staging/schedule.py:99-485, run_staged :455-485): coarse grids and FP32 GPU
+work early, fine grids and an FP64 tail late.  PySCF is not available on
+these machines, so this module is the SCF loop itself, built from this
+library's pieces and kept on the device from the first Fock build to the
+converged energy:
+
+    H = T + V                       wb_scf_int1e (FP64, once)
+    K(0), K(omega)                  COSX multi-omega build: FP32 class
+                                    kernels (mixed) or the plain FP64 form
+    J = X^T (w o v_H) X             v_H from wb_hartree on the SGX grid
+                                    (analytic potential, quadrature of
+                                    mu nu v_H), FP32 or FP64
+    E_xc, V_xc                      the functional on the XC grid
+    E_nl, V_nl                      VV10 on the NLC grid (FP32 pair sum,
+                                    FP64 elsewhere, as in the reference)
+    F = H + J - K_x / 2 + V_xc + V_nl,  K_x = a K(0) + b K(omega)
+    C from F C = S C e              FP64 eigensolver on the device
+    CDIIS on the commutator X^T (F D S - S D F) X
+
+and the energy
+    E = tr(D H) + tr(D J)/2 - tr(D K_x)/4 + E_xc + E_nl + E_nuc.
+
+Staging follows the reference's StagePlan (this package's
+staging.schedule.StagePlan): S0 on coarse grids without VV10, S1 and S2 on
+the final grids, then the FP64 tail (FP64 K, J and density GEMMs) from
+which convergence is declared.  ``precision='fp64'`` runs the plain FP64
+form on the final grids from the start: the comparison point of the
+mixed-precision form and, checked against the oracle's SCF, the FP64
+reference energy of molecules too large for the host oracle.
+
+The semilocal functional is a stated stand-in: wB97M-V's pointwise
+meta-GGA lives in libxc (third party, not on these machines).
+``RshLdaVv10`` keeps wB97M-V's exact-exchange split (0.15 of the
+full-range K plus 0.85 of the long-range K at omega = 0.3: short-range
+0.15, long-range 1.0) and its VV10 parameters (b = 6.0, C = 0.01), with a
+short-range LDA exchange (0.85) and VWN5 correlation for the semilocal
+part.
+"""
+import math
+import time
+
+import numpy as np
+
+from pyscf_wb97mv_fast_gb300.cosx import CosxEngine, as_molecule, round32
+from pyscf_wb97mv_fast_gb300.staging.schedule import StagePlan
+
+
+def _torch():
+    import torch
+    return torch
+
+
+# -- the functional --------------------------------------------------------------
+
+# large-a expansion of the short-range LDA exchange attenuation,
+# F(a) = sum_k c_k a^(-2k), k = 1..8 (series of the closed form below)
+_SR_SERIES = (1.0 / 36.0, -1.0 / 960.0, 1.0 / 26880.0, -1.0 / 829440.0,
+              1.0 / 28385280.0, -1.0 / 1073479680.0, 1.0 / 44590694400.0,
+              -1.0 / 2021444812800.0)
+_VWN5 = dict(A=0.0310907, x0=-0.10498, b=3.72744, c=12.9352)
+
+
+class RshLdaVv10:
+    """Range-separated hybrid with wB97M-V's exact-exchange split and VV10.
+
+    E_xc = -1/4 tr[D (alpha K(0) + beta K(omega))] + cx_sr E_x^{SR-LDA}(omega)
+           + E_c^{VWN5} + E_nl^{VV10}(b, C)
+
+    * the short-range LDA exchange per volume is e_x^LDA F(a),
+      e_x^LDA = -3/4 (3/pi)^(1/3) rho^(4/3), a = omega / (2 k_F),
+      k_F = (3 pi^2 rho)^(1/3),
+      F(a) = 1 - 8/3 a [sqrt(pi) erf(1/(2a)) + (2a - 4a^3) exp(-1/(4a^2))
+                        - 3a + 4a^3]
+      (the erfc-attenuated uniform-gas exchange; its large-a series, eight
+      terms, for a >= 1.5, where the closed form cancels: both are within
+      5e-13 relative there);
+    * VWN5: Vosko, Wilk, Nusair, Can. J. Phys. 58, 1200 (1980), the
+      paramagnetic fit (A, x0, b, c) = (0.0310907, -0.10498, 3.72744,
+      12.9352), hartree.
+    """
+
+    name = 'rsh-lda-vv10'
+
+    def __init__(self, omega=0.3, alpha=0.15, beta=0.85, cx_sr=0.85,
+                 nlc=(6.0, 0.01)):
+        self.omega = float(omega)
+        self.alpha = float(alpha)
+        self.beta = float(beta)
+        self.cx_sr = float(cx_sr)
+        self.nlc = tuple(nlc) if nlc else None
+
+    @property
+    def omegas(self):
+        return (0.0, self.omega)
+
+    def eval(self, rho):
+        """(e, v) per grid point for the density rho (torch FP64): e the
+        semilocal energy per volume, v = de/drho."""
+        torch = _torch()
+        r = torch.clamp(rho, min=1e-300)
+        live = rho > 1e-14
+        ex_lda = -0.75 * (3.0 / math.pi) ** (1.0 / 3.0) * r ** (4.0 / 3.0)
+        kf = (3.0 * math.pi ** 2 * r) ** (1.0 / 3.0)
+        a = self.omega / (2.0 * kf)
+        F, dF = _sr_attenuation(a)
+        ex = ex_lda * F
+        vx = (ex_lda / r) * (4.0 / 3.0 * F - a / 3.0 * dF)
+        ec, vc = _vwn5(r)
+        e = self.cx_sr * ex + r * ec
+        v = self.cx_sr * vx + vc
+        zero = torch.zeros_like(rho)
+        return torch.where(live, e, zero), torch.where(live, v, zero)
+
+
+def _sr_attenuation(a):
+    torch = _torch()
+    big = a >= 1.5
+    a_s = torch.where(big, torch.ones_like(a), a)       # closed form branch
+    b = 1.0 / (4.0 * a_s * a_s)
+    eb = torch.exp(-b)
+    g = (math.sqrt(math.pi) * torch.special.erf(1.0 / (2.0 * a_s))
+         + (2.0 * a_s - 4.0 * a_s ** 3) * eb - 3.0 * a_s + 4.0 * a_s ** 3)
+    dg = 12.0 * a_s * a_s * (1.0 - eb) - 3.0
+    F_c = 1.0 - 8.0 / 3.0 * a_s * g
+    dF_c = -8.0 / 3.0 * (g + a_s * dg)
+    a_l = torch.where(big, a, 2.0 * torch.ones_like(a))   # series branch
+    y = 1.0 / (a_l * a_l)
+    F_s = torch.zeros_like(a)
+    dF_s = torch.zeros_like(a)
+    yk = torch.ones_like(a)
+    for k, c in enumerate(_SR_SERIES, start=1):
+        yk = yk * y
+        F_s = F_s + c * yk
+        dF_s = dF_s - 2.0 * k * c * yk / a_l
+    return torch.where(big, F_s, F_c), torch.where(big, dF_s, dF_c)
+
+
+def _vwn5(rho):
+    """epsilon_c (per electron) and v_c of the paramagnetic VWN5 fit."""
+    torch = _torch()
+    A, x0, b, c = (_VWN5[k] for k in ('A', 'x0', 'b', 'c'))
+    Q = math.sqrt(4.0 * c - b * b)
+    X0 = x0 * x0 + b * x0 + c
+    rs = (3.0 / (4.0 * math.pi * rho)) ** (1.0 / 3.0)
+    x = torch.sqrt(rs)
+    X = x * x + b * x + c
+    at = torch.atan(Q / (2.0 * x + b))
+    den = (2.0 * x + b) ** 2 + Q * Q
+    ec = A * (torch.log(x * x / X) + 2.0 * b / Q * at
+              - b * x0 / X0 * (torch.log((x - x0) ** 2 / X) + 2.0 * (b + 2.0 * x0) / Q * at))
+    dec = A * (2.0 / x - (2.0 * x + b) / X - 4.0 * b / den
+               - b * x0 / X0 * (2.0 / (x - x0) - (2.0 * x + b) / X
+                                - 4.0 * (b + 2.0 * x0) / den))
+    return ec, ec - x / 6.0 * dec
+
+
+# -- grids -----------------------------------------------------------------------
+
+class DeviceGrid:
+    """One integration grid on the device: coordinates in the engine frame,
+    weights, and the AO values (deriv 0, or 0 and 1), evaluated once."""
+
+    def __init__(self, eng, grids, deriv=0):
+        torch = _torch()
+        self.level = getattr(grids, 'level', None)
+        self.n = int(grids.weights.size)
+        self.coords = eng.relative(np.asarray(grids.coords, dtype=np.float64))
+        self.weights = torch.as_tensor(np.asarray(grids.weights, dtype=np.float64),
+                                       device=eng.device)
+        self.deriv = deriv
+        if deriv == 0:
+            self.X = eng.ao_eval(self.coords)             # (nao, ld)
+        else:
+            self.X = eng.ao_eval_deriv1(self.coords)      # (4, nao, ld)
+        self.ld = int(self.X.shape[-1])
+        w = torch.zeros(self.ld, dtype=torch.float64, device=eng.device)
+        w[:self.n] = self.weights
+        self.wpad = w
+
+
+# -- the SCF -----------------------------------------------------------------------
+
+DEFAULT_FINAL = dict(xc=2, sgx=1, nlc=1)
+DEFAULT_COARSE = dict(xc=1, sgx=0)
+
+
+class DeviceRKS:
+    """RKS SCF on one GPU for a Molecule (see the module docstring).
+
+    ``levels`` are the final grid levels (xc, sgx, nlc; nlc None turns VV10
+    off) and ``coarse`` those of stage S0 (xc, sgx; no VV10), as in the
+    reference's staging table (schedule.py:91-96).  ``k_tile_tol`` is the
+    COSX screen, ``j_tol`` the Hartree-potential screen.
+    """
+
+    def __init__(self, mol, functional=None, levels=None, coarse=None,
+                 k_tile_tol=1e-11, j_tol=1e-14, device=None, verbose=False):
+        torch = _torch()
+        self.mol = as_molecule(mol)
+        self.functional = functional or RshLdaVv10()
+        self.levels = dict(DEFAULT_FINAL, **(levels or {}))
+        self.coarse = dict(DEFAULT_COARSE, **(coarse or {}))
+        self.k_tile_tol = float(k_tile_tol)
+        self.j_tol = float(j_tol)
+        self.verbose = verbose
+        t0 = time.perf_counter()
+        self.eng = CosxEngine(self.mol, device=device)
+        self.device = self.eng.device
+        S, T, V = self.eng.int1e()
+        self.S = S
+        self.H = T + V
+        self.e_nuc = float(self.mol.energy_nuc())
+        # canonical orthogonalisation X = U s^(-1/2) (s > 1e-9 kept)
+        s, U = torch.linalg.eigh(S)
+        keep = s > 1e-9
+        self.Xo = U[:, keep] / torch.sqrt(s[keep])[None, :]
+        self.nocc = self.mol.nelectron // 2
+        self._grid_cache = {}
+        self.t_setup = time.perf_counter() - t0
+
+    # -- pieces --------------------------------------------------------------
+    def grid(self, kind, level):
+        """DeviceGrid of kind 'xc' / 'sgx' (deriv 0) or 'nlc' (deriv 1)."""
+        key = (kind, level)
+        g = self._grid_cache.get(key)
+        if g is None:
+            from pyscf_wb97mv_fast_gb300.grids import build_grids
+            g = DeviceGrid(self.eng, build_grids(self.mol, level=level),
+                           deriv=1 if kind == 'nlc' else 0)
+            self._grid_cache[key] = g
+        return g
+
+    def _vmat(self, g, v, fp64):
+        """X^T diag(w v) X over grid g (deriv-0 AO values), symmetric."""
+        torch = _torch()
+        X = g.X if g.deriv == 0 else g.X[0]
+        if fp64:
+            wv = torch.zeros(g.ld, dtype=torch.float64, device=self.device)
+            wv[:g.n] = g.weights * v[:g.n]
+            M = (X * wv[None, :]) @ X.T
+        else:
+            G = torch.zeros_like(X, dtype=torch.float32)
+            G[:, :g.n] = (X[:, :g.n] * v[None, :g.n]).to(torch.float32)
+            M = self.eng.ozaki_k(X, G, g.weights)
+        return 0.5 * (M + M.T)
+
+    def _density(self, g, D, fp64):
+        torch = _torch()
+        X = g.X if g.deriv == 0 else g.X[0]
+        if fp64:
+            T = D @ X
+        else:
+            T = self.eng.ozaki_f(X, D).to(torch.float64)
+        return (T * X).sum(dim=0)[:g.n]
+
+    def k_matrices(self, D, g, fp64):
+        om = self.functional.omegas
+        if fp64:
+            Kb = self.eng.get_k_fp64(g.coords, g.weights, D, om,
+                                     tile_tol=self.k_tile_tol, stats=False)
+        else:
+            Kb = self.eng.get_k_multi(g.coords, g.weights, D, om,
+                                      tile_tol=self.k_tile_tol, stats=False)
+        return 0.5 * (Kb + Kb.transpose(1, 2))
+
+    def vv10(self, D, g):
+        """(E_nl, V_nl) on the NLC grid g (device scalars / matrix)."""
+        from pyscf_wb97mv_fast_gb300.gpu.vv10 import vv10_energy_fock
+        return vv10_energy_fock(self.eng, g, D, self.functional.nlc)
+
+    def fock(self, D, grids, fp64):
+        """(E, F, parts) for density D with grids = dict(xc=, sgx=, nlc=)
+        DeviceGrids (nlc may be None)."""
+        torch = _torch()
+        f = self.functional
+        K = self.k_matrices(D, grids['sgx'], fp64)
+        Kx = f.alpha * K[0] + f.beta * K[1]
+        vh = self.eng.hartree(grids['sgx'].coords, D, tol=self.j_tol, fp64=fp64)
+        J = self._vmat(grids['sgx'], vh, fp64)
+        gx = grids['xc']
+        rho = self._density(gx, D, fp64)
+        e, v = f.eval(rho)
+        exc = (gx.weights * e).sum()
+        Vxc = self._vmat(gx, v, fp64)
+        if grids.get('nlc') is not None and f.nlc:
+            enl, Vnl = self.vv10(D, grids['nlc'])
+        else:
+            enl, Vnl = torch.zeros((), dtype=torch.float64, device=self.device), 0.0
+        F = self.H + J - 0.5 * Kx + Vxc + Vnl
+        e1 = (D * self.H).sum()
+        ej = 0.5 * (D * J).sum()
+        ek = -0.25 * (D * Kx).sum()
+        E = e1 + ej + ek + exc + enl + self.e_nuc
+        return E, F, dict(e1=e1, ej=ej, ek=ek, exc=exc, enl=enl)
+
+    def _diag(self, F):
+        torch = _torch()
+        Fo = self.Xo.T @ F @ self.Xo
+        e, Co = torch.linalg.eigh(Fo)
+        C = self.Xo @ Co
+        Cocc = C[:, :self.nocc]
+        return 2.0 * Cocc @ Cocc.T, e
+
+    def _commutator(self, F, D):
+        FDS = F @ D @ self.S
+        return self.Xo.T @ (FDS - FDS.T) @ self.Xo
+
+    def core_guess(self):
+        return self._diag(self.H)[0]
+
+    # -- the loop --------------------------------------------------------------
+    def kernel(self, precision='mixed', dm0=None, conv_tol=1e-9, conv_tol_grad=1e-5,
+               max_cycle=80, diis_space=8, plan=None, reference_energy=None):
+        """Run the SCF; returns a dict with e_tot, converged, cycles, wall
+        (seconds, device-synchronised), per-cycle history and, for the
+        staged form, the energy at the end of each stage.  precision:
+        'mixed' (staged, FP32 GPU work, FP64 tail) or 'fp64' (the plain FP64
+        form on the final grids)."""
+        torch = _torch()
+        if precision not in ('mixed', 'fp64'):
+            raise ValueError("precision must be 'mixed' or 'fp64'")
+        torch.cuda.synchronize(self.device)
+        t0 = time.perf_counter()
+        staged = precision == 'mixed'
+        if staged:
+            plan = plan or StagePlan(fp64_final=True, tau_fp64=1e-6, tau_fp64_g=1e-4)
+        D = self.core_guess() if dm0 is None else torch.as_tensor(
+            dm0, dtype=torch.float64, device=self.device)
+        stage, fp64 = (0, False) if staged else (2, True)
+        diis = _Cdiis(diis_space)
+        hist, stage_end = [], []
+        e_last, converged = None, False
+        for cycle in range(max_cycle):
+            grids = self._stage_grids(stage)
+            E, F, parts = self.fock(D, grids, fp64)
+            comm = self._commutator(F, D)
+            gnorm = float(torch.linalg.norm(comm))
+            Ef = float(E)
+            dE = math.inf if e_last is None else abs(Ef - e_last)
+            hist.append(dict(cycle=cycle, stage=stage, fp64=fp64, e=Ef, dE=dE,
+                             gnorm=gnorm, t=time.perf_counter() - t0))
+            if self.verbose:
+                print('cycle %2d S%d %s E=%.12f dE=%.2e |g|=%.2e'
+                      % (cycle, stage, 'fp64' if fp64 else 'fp32', Ef, dE, gnorm))
+            may_stop = (not staged) or plan.may_converge
+            if may_stop and dE < conv_tol and gnorm < conv_tol_grad:
+                converged = True
+                break
+            decision = plan.after_cycle(dE, gnorm) if staged else None
+            if decision is not None:
+                stage_end.append(dict(stage=stage, fp64=fp64, e=Ef, cycles=cycle + 1))
+                if decision[0] == 'stage':
+                    stage = decision[1]
+                else:
+                    fp64 = True
+                diis = _Cdiis(diis_space)      # the functional changed
+                e_last = None
+                D = self._diag(F)[0]
+                continue
+            e_last = Ef
+            Fd = diis.update(F, comm)
+            D = self._diag(Fd)[0]
+        torch.cuda.synchronize(self.device)
+        wall = time.perf_counter() - t0
+        out = dict(e_tot=hist[-1]['e'], converged=converged, cycles=len(hist),
+                   wall=wall, setup_s=self.t_setup, history=hist,
+                   precision=precision, stages=stage_end,
+                   parts={k: float(v) for k, v in parts.items()}, dm=D)
+        if reference_energy is not None:
+            out['error_vs_reference'] = out['e_tot'] - float(reference_energy)
+            for h in hist:
+                h['err'] = h['e'] - float(reference_energy)
+            for s in stage_end:
+                s['err'] = s['e'] - float(reference_energy)
+        return out
+
+    def _stage_grids(self, stage):
+        if stage == 0:
+            return dict(xc=self.grid('xc', self.coarse['xc']),
+                        sgx=self.grid('sgx', self.coarse['sgx']), nlc=None)
+        nlc = self.levels['nlc']
+        return dict(xc=self.grid('xc', self.levels['xc']),
+                    sgx=self.grid('sgx', self.levels['sgx']),
+                    nlc=None if nlc is None else self.grid('nlc', nlc))
+
+
+class _Cdiis:
+    """Pulay's commutator DIIS on the device (P. Pulay, J. Comput. Chem. 3,
+    556 (1982)): extrapolated F = sum c_i F_i with sum c_i = 1 minimising
+    |sum c_i e_i|, e_i the orthonormal-basis commutators."""
+
+    def __init__(self, space=8):
+        self.space = int(space)
+        self.F, self.e = [], []
+
+    def update(self, F, e):
+        torch = _torch()
+        self.F.append(F)
+        self.e.append(e)
+        if len(self.F) > self.space:
+            self.F.pop(0)
+            self.e.pop(0)
+        n = len(self.F)
+        if n < 2:
+            return F
+        E = torch.stack([x.reshape(-1) for x in self.e])
+        B = torch.zeros((n + 1, n + 1), dtype=torch.float64, device=F.device)
+        B[:n, :n] = E @ E.T
+        B[:n, n] = -1.0
+        B[n, :n] = -1.0
+        rhs = torch.zeros(n + 1, dtype=torch.float64, device=F.device)
+        rhs[n] = -1.0
+        scale = B[:n, :n].diagonal().max()
+        if scale > 0:
+            B[:n, :n] /= scale
+        # the (n+1)-square system is solved on the host (least squares: the
+        # error vectors can be nearly dependent)
+        c = np.linalg.lstsq(B.cpu().numpy(), rhs.cpu().numpy(), rcond=None)[0][:n]
+        out = torch.zeros_like(F)
+        for ci, Fi in zip(c, self.F):
+            out += float(ci) * Fi
+        return out

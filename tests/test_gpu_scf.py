@@ -1,0 +1,84 @@
+"""The device SCF against the oracle's host SCF (oracle/scf.py): the same
+functional, grids and algorithm, FP64 and unscreened on the host.
+
+* the plain FP64 device form reaches the oracle's energy to 1e-9 Ha (its
+  screens, k_tile_tol 1e-11 and the Hartree screen, are the difference);
+* the mixed-precision staged form (FP32 stages on coarse then final
+  grids, FP64 tail) reaches it to 1e-8 Ha, the benchmark spec's gate;
+* the per-cycle pieces match the oracle's Fock build on a fixed density.
+
+The oracle energies come from tests/golden/scf_energies.json (written by
+tests/golden/make_scf_golden.py, which runs oracle/scf.py); the small case
+also runs the oracle live.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import dimer
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _golden():
+    with open(os.path.join(HERE, 'golden', 'scf_energies.json')) as fh:
+        return json.load(fh)
+
+
+def _dimer_case():
+    from pyscf_wb97mv_fast_gb300.scf import DeviceRKS
+    mol = dimer('synthetic-svp')
+    return mol, DeviceRKS(mol, levels=dict(xc=1, sgx=0, nlc=0),
+                          coarse=dict(xc=0, sgx=0))
+
+
+def test_fock_build_matches_oracle_on_a_fixed_density():
+    import torch
+    from oracle.scf import HostScf
+    from pyscf_wb97mv_fast_gb300.grids import build_grids
+    mol, rks = _dimer_case()
+    grids = {k: build_grids(mol, level=lv) for k, lv in (('xc', 1), ('sgx', 0), ('nlc', 0))}
+    host = HostScf(mol, grids)
+    D = host.diag(host.H)
+    E_ref, F_ref = host.fock(D)
+    dg = rks._stage_grids(2)
+    E, F, _ = rks.fock(torch.as_tensor(D, device=rks.device), dg, fp64=True)
+    assert abs(float(E) - E_ref) < 1e-9
+    assert np.abs(F.cpu().numpy() - F_ref).max() < 1e-9
+    E32, F32, _ = rks.fock(torch.as_tensor(D, device=rks.device), dg, fp64=False)
+    assert abs(float(E32) - E_ref) < 1e-5
+    assert np.abs(F32.cpu().numpy() - F_ref).max() < 1e-5
+
+
+def test_fp64_and_mixed_scf_reach_the_oracle_energy_water_dimer():
+    mol, rks = _dimer_case()
+    e_ref = _golden()['water_dimer_svp_xc1_sgx0_nlc0']['e_tot']
+    r64 = rks.kernel(precision='fp64', reference_energy=e_ref)
+    assert r64['converged']
+    assert abs(r64['error_vs_reference']) < 1e-9, r64['error_vs_reference']
+    rmx = rks.kernel(precision='mixed', reference_energy=e_ref)
+    assert rmx['converged']
+    assert abs(rmx['error_vs_reference']) < 1e-8, rmx['error_vs_reference']
+    # the staged run went through S0, S1, S2 and the FP64 tail
+    assert [s['stage'] for s in rmx['stages']][:2] == [0, 1]
+    assert rmx['history'][-1]['fp64']
+
+
+def test_mixed_scf_water8_config1_reaches_the_oracle_energy():
+    """Config 1's molecule and grids: 8 seeded waters, synthetic def2-SVP
+    (192 AOs), XC level 2, SGX level 1, VV10 level 1."""
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.scf import DeviceRKS
+    from pyscf_wb97mv_fast_gb300.systems import water_cluster
+    g = _golden().get('water8_svp_xc2_sgx1_nlc1')
+    if g is None:
+        pytest.skip('no oracle energy fixture for water8')
+    mol = Molecule.build(water_cluster(8, box=7.0, seed=8), 'synthetic-svp')
+    rks = DeviceRKS(mol, levels=dict(xc=2, sgx=1, nlc=1))
+    r = rks.kernel(precision='mixed', reference_energy=g['e_tot'])
+    assert r['converged']
+    assert abs(r['error_vs_reference']) < 1e-8, r['error_vs_reference']
