@@ -760,6 +760,114 @@ def alkane_timing(torch, peak, steps=3, n_carbon=20, level=2):
     return out
 
 
+def reference_gpu_timing(g, eng, F, Gt, t_g, torch, vv10_points=209707):
+    """The reference's own CUDA kernels on this GPU (oracle/ref_gpu: the
+    extracted sgx_screen_mask, sgx_k_cls<LA,LB> and vv10_kernel_sum, built
+    for sm_103a, launched with the reference's shapes) next to this
+    library's, on the same grid, F and density; the G phases are
+    cross-checked element by element."""
+    from oracle.ref_gpu import runner
+    why = runner.available()
+    if why:
+        return {'unavailable': why}
+    ref = runner.RefGpu(device=eng.device.index or 0)
+    n = g.size
+    Fpm = F[:, :n].T.contiguous()                     # (npts, nao) point-major
+    out = {'what': 'reference kernels extracted unmodified from gpu/sgx_k.py and '
+                   'gpu/vv10.py, compiled with nvcc -arch=sm_103a; per 155,648-point '
+                   'tile: sub-block stats + sgx_screen_mask (screen_ms), per-class CSR '
+                   '(host round trips, csr_host_ms, not counted), sgx_k_cls launches '
+                   '(class_kernels_ms)',
+           'ours_g_phase_ms': t_g * 1e3}
+    total = 0.0
+    for j, omega in enumerate(OMEGAS):
+        ref.g_phase(g.coords, g.weights, Fpm, omega, TILE_TOL)       # warm-up
+        G, st = ref.g_phase(g.coords, g.weights, Fpm, omega, TILE_TOL)
+        mine = Gt[j][:, :n].T
+        scale = float(mine.abs().max())
+        st['max_dG_vs_ours_over_max_G'] = float((G - mine).abs().max()) / scale
+        st['ms'] = st['screen_ms'] + st['class_kernels_ms']
+        total += st['ms']
+        out['omega=%g' % omega] = st
+        del G
+    out['ref_g_phase_ms'] = total
+    out['speedup_g_phase'] = total / (t_g * 1e3)
+    # VV10 double sum: both kernels on the same seeded inputs (every pair)
+    rng = np.random.default_rng(31)
+    xyz = torch.as_tensor(rng.uniform(-9.0, 9.0, (vv10_points, 3)), dtype=torch.float32,
+                          device=eng.device)
+    q, w0, kap = (torch.as_tensor(rng.uniform(lo, hi, vv10_points), dtype=torch.float32,
+                                  device=eng.device)
+                  for lo, hi in ((1e-6, 1e-2), (0.3, 3.0), (0.4, 2.0)))
+    from pyscf_wb97mv_fast_gb300.gpu.vv10 import Vv10Kernel
+    mine_k = Vv10Kernel(0.0)
+
+    def tmin(fn, reps=3):
+        fn()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return min(ts)
+    t_ref = tmin(lambda: ref.vv10(xyz, q, w0, kap))
+    t_mine = tmin(lambda: mine_k.kernel_sum(xyz, q, w0, kap))
+    Fr, Ur, Wr = ref.vv10(xyz, q, w0, kap)
+    Fm, Um, Wm = mine_k.kernel_sum(xyz, q, w0, kap)
+    out['vv10'] = {'points': vv10_points, 'inputs': 'seeded uniform (every pair kept)',
+                   'ref_ms': t_ref, 'ours_ms': t_mine, 'speedup': t_ref / t_mine,
+                   'max_rel_diff_F': float(((-1.5 * Fr - Fm).abs() / Fm.abs()).max()),
+                   'max_rel_diff_U': float(((Ur - Um).abs() / Um.abs()).max())}
+    return out
+
+
+def scf_timing(torch):
+    """Config 1 (8 seeded waters, synthetic def2-SVP, XC level 2, SGX
+    level 1, VV10 level 1): the device SCF in its mixed-precision staged
+    form and its plain FP64 form, each from the core guess to convergence;
+    energies against the oracle's host SCF (tests/golden/scf_energies.json,
+    oracle/scf.py); wall time to reach 1e-8 Ha of it."""
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.scf import DeviceRKS
+    from pyscf_wb97mv_fast_gb300.systems import water_cluster
+    path = os.path.join(ROOT, 'tests', 'golden', 'scf_energies.json')
+    with open(path) as fh:
+        golden = json.load(fh)
+    ref = golden.get('water8_svp_xc2_sgx1_nlc1', {}).get('e_tot')
+    mol = Molecule.build(water_cluster(8, box=7.0, seed=8), 'synthetic-svp')
+    rks = DeviceRKS(mol, levels=dict(xc=2, sgx=1, nlc=1))
+    # warm-up: grids, AO values and first launches (not timed)
+    rks.kernel(precision='mixed', max_cycle=2)
+    rks.kernel(precision='fp64', max_cycle=2)
+    out = {'molecule': '8 seeded waters in a 7 A cube (seed 8), synthetic def2-SVP',
+           'nao': mol.nao, 'levels': rks.levels, 'coarse': rks.coarse,
+           'functional': rks.functional.name, 'oracle_energy': ref,
+           'oracle': 'oracle/scf.py (host FP64, unscreened) via '
+                     'tests/golden/scf_energies.json'}
+    for form in ('mixed', 'fp64'):
+        r = rks.kernel(precision=form, reference_energy=ref)
+        t_hit = None
+        if ref is not None:
+            for h in r['history']:
+                if abs(h['e'] - ref) < 1e-8 and (form == 'fp64' or h['fp64']):
+                    t_hit = h['t']
+                    break
+        out[form] = {'e_tot': r['e_tot'], 'error_vs_oracle': r.get('error_vs_reference'),
+                     'converged': r['converged'], 'cycles': r['cycles'],
+                     'wall_s': r['wall'], 'wall_to_1e-8_s': t_hit,
+                     'cycles_fp64': sum(1 for h in r['history'] if h['fp64']),
+                     'stages': [{k: v for k, v in s.items()} for s in r['stages']]}
+    m, f = out['mixed'], out['fp64']
+    out['fp64_over_mixed_wall'] = f['wall_s'] / m['wall_s']
+    if m['wall_to_1e-8_s'] and f['wall_to_1e-8_s']:
+        out['fp64_over_mixed_to_1e-8'] = f['wall_to_1e-8_s'] / m['wall_to_1e-8_s']
+    rks.eng.close()
+    return out
+
+
 def run_sample(oracle, mol, g, dm, idx):
     coords = g.coords[idx]
     X = oracle.ao_eval(mol, coords)
@@ -855,6 +963,10 @@ def main():
                     help='skip the batched (many molecules per launch) leg')
     ap.add_argument('--no-alkane', action='store_true',
                     help='skip the C20H42 / def2-TZVP (f shells) leg')
+    ap.add_argument('--no-scf', action='store_true',
+                    help='skip the device SCF leg (config 1, mixed vs FP64)')
+    ap.add_argument('--no-reference-gpu', action='store_true',
+                    help="skip the reference's own kernels on this GPU")
     ap.add_argument('--no-parity', action='store_true',
                     help='skip the oracle check of K on a grid subset')
     ap.add_argument('--batched-molecules', type=int, default=64,
@@ -991,6 +1103,8 @@ def main():
         eng.g_multi(coords_d, w_d, F, OMEGAS, TILE_TOL, out=Gt, stats=False)
     t_g = timed(g_step, max(2, args.steps), 1)
     del X
+    refgpu = None if args.no_reference_gpu else reference_gpu_timing(g, eng, F, Gt, t_g,
+                                                                     torch)
     peak = fp32_peak(torch)
     achieved = g_flops / t_g / 1e12
     prof = traffic_from_profile()
@@ -1025,6 +1139,8 @@ def main():
     k_grad = None if (args.no_grad or world > 1) else grad_timing(torch)
     alk = None if (args.no_alkane or world > 1) else alkane_timing(torch, peak)
     torch.cuda.empty_cache()
+    scf = None if (args.no_scf or world > 1) else scf_timing(torch)
+    torch.cuda.empty_cache()
     parity = None if args.no_parity else parity_vs_oracle(mol, g, dm, eng, torch, 3000)
 
     cpu = None
@@ -1054,6 +1170,8 @@ def main():
             'autotune': tuned,
             'k_grad': k_grad,
             'alkane_c20_tzvp': alk,
+            'scf': scf,
+            'reference_gpu': refgpu,
             'parity_vs_fp64_oracle': parity,
             'clocks': clocks.summary(),
             'gpu_launches': launches_step * args.steps,

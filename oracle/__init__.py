@@ -41,6 +41,34 @@ def build(force=False):
     return LIB
 
 
+REF_DIR = os.path.join(HERE, '_ref')
+REF_GPU_LIB = os.path.join(REF_DIR, 'libref_gpu.so')
+
+
+def build_ref_gpu(force=False):
+    """Compile the reference's extracted CUDA kernels with this directory's
+    launchers (ref_gpu/harness.cu) into oracle/_ref/libref_gpu.so, when
+    oracle/_ref/ref_kernels.cuh exists; returns the library path or None.
+    Test infrastructure: the GPU-side baseline arm of bench.py."""
+    src = os.path.join(REF_DIR, 'ref_kernels.cuh')
+    harness = os.path.join(HERE, 'ref_gpu', 'harness.cu')
+    if not os.path.exists(src):
+        return None
+    if (not force and os.path.exists(REF_GPU_LIB)
+            and os.path.getmtime(REF_GPU_LIB) >= max(os.path.getmtime(src),
+                                                     os.path.getmtime(harness))):
+        return REF_GPU_LIB
+    nvcc = os.path.join(os.environ.get('CUDA_HOME', '/usr/local/cuda'), 'bin', 'nvcc')
+    cmd = [nvcc, '-gencode', 'arch=compute_103a,code=sm_103a', '-std=c++14', '-O3',
+           '-Xcompiler', '-fPIC', '-shared', '-I', REF_DIR, harness,
+           '-o', REF_GPU_LIB + '.tmp']
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError('reference kernel build failed:\n' + res.stderr[-3000:])
+    os.replace(REF_GPU_LIB + '.tmp', REF_GPU_LIB)
+    return REF_GPU_LIB
+
+
 def _load():
     global _lib
     if _lib is None:

@@ -47,11 +47,14 @@ def test_fock_build_matches_oracle_on_a_fixed_density():
     E_ref, F_ref = host.fock(D)
     dg = rks._stage_grids(2)
     E, F, _ = rks.fock(torch.as_tensor(D, device=rks.device), dg, fp64=True)
+    # the screens (k_tile_tol 1e-11, Hartree 1e-14) move single Fock
+    # elements by up to ~1e-10 of max|F|; the energy by less
+    scale = np.abs(F_ref).max()
     assert abs(float(E) - E_ref) < 1e-9
-    assert np.abs(F.cpu().numpy() - F_ref).max() < 1e-9
+    assert np.abs(F.cpu().numpy() - F_ref).max() < 1e-9 * scale
     E32, F32, _ = rks.fock(torch.as_tensor(D, device=rks.device), dg, fp64=False)
     assert abs(float(E32) - E_ref) < 1e-5
-    assert np.abs(F32.cpu().numpy() - F_ref).max() < 1e-5
+    assert np.abs(F32.cpu().numpy() - F_ref).max() < 1e-6 * scale
 
 
 def test_fp64_and_mixed_scf_reach_the_oracle_energy_water_dimer():
