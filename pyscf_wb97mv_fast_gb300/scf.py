@@ -220,6 +220,8 @@ class DeviceRKS:
         self.Xo = U[:, keep] / torch.sqrt(s[keep])[None, :]
         self.nocc = self.mol.nelectron // 2
         self._grid_cache = {}
+        self.profile = None           # dict of part -> seconds when profiling
+        self._t_last = 0.0
         self.t_setup = time.perf_counter() - t0
 
     # -- pieces --------------------------------------------------------------
@@ -272,30 +274,54 @@ class DeviceRKS:
         from pyscf_wb97mv_fast_gb300.gpu.vv10 import vv10_energy_fock
         return vv10_energy_fock(self.eng, g, D, self.functional.nlc)
 
-    def fock(self, D, grids, fp64):
-        """(E, F, parts) for density D with grids = dict(xc=, sgx=, nlc=)
-        DeviceGrids (nlc may be None)."""
+    def _tick(self, name):
+        """Per-part wall time (device-synchronised) when profiling."""
+        if self.profile is None:
+            return
+        torch = _torch()
+        torch.cuda.synchronize(self.device)
+        now = time.perf_counter()
+        if name is not None:
+            self.profile[name] = self.profile.get(name, 0.0) + now - self._t_last
+        self._t_last = now
+
+    def fock(self, D, grids, fp64, base=None):
+        """(E, F, parts, base') for density D with grids = dict(xc=, sgx=,
+        nlc=) DeviceGrids (nlc may be None).  ``base`` = (D0, Kx0) of an
+        earlier build on the same grids and precision makes the exchange
+        build incremental: K_x = K_x0 + K_x(D - D0), the COSX screen then
+        running on F = X (D - D0), whose small entries drop most tasks (the
+        incremental Fock build of a direct SCF).  base' is (D, K_x)."""
         torch = _torch()
         f = self.functional
-        K = self.k_matrices(D, grids['sgx'], fp64)
-        Kx = f.alpha * K[0] + f.beta * K[1]
+        self._tick(None)
+        if base is None:
+            K = self.k_matrices(D, grids['sgx'], fp64)
+            Kx = f.alpha * K[0] + f.beta * K[1]
+        else:
+            dK = self.k_matrices(D - base[0], grids['sgx'], fp64)
+            Kx = base[1] + (f.alpha * dK[0] + f.beta * dK[1])
+        self._tick('k')
         vh = self.eng.hartree(grids['sgx'].coords, D, tol=self.j_tol, fp64=fp64)
         J = self._vmat(grids['sgx'], vh, fp64)
+        self._tick('j')
         gx = grids['xc']
         rho = self._density(gx, D, fp64)
         e, v = f.eval(rho)
         exc = (gx.weights * e).sum()
         Vxc = self._vmat(gx, v, fp64)
+        self._tick('xc')
         if grids.get('nlc') is not None and f.nlc:
             enl, Vnl = self.vv10(D, grids['nlc'])
         else:
             enl, Vnl = torch.zeros((), dtype=torch.float64, device=self.device), 0.0
+        self._tick('vv10')
         F = self.H + J - 0.5 * Kx + Vxc + Vnl
         e1 = (D * self.H).sum()
         ej = 0.5 * (D * J).sum()
         ek = -0.25 * (D * Kx).sum()
         E = e1 + ej + ek + exc + enl + self.e_nuc
-        return E, F, dict(e1=e1, ej=ej, ek=ek, exc=exc, enl=enl)
+        return E, F, dict(e1=e1, ej=ej, ek=ek, exc=exc, enl=enl), (D, Kx)
 
     def _diag(self, F):
         torch = _torch()
@@ -314,12 +340,19 @@ class DeviceRKS:
 
     # -- the loop --------------------------------------------------------------
     def kernel(self, precision='mixed', dm0=None, conv_tol=1e-9, conv_tol_grad=1e-5,
-               max_cycle=80, diis_space=8, plan=None, reference_energy=None):
+               max_cycle=80, diis_space=8, plan=None, reference_energy=None,
+               incremental=True, rebuild_every=8, profile=False):
         """Run the SCF; returns a dict with e_tot, converged, cycles, wall
         (seconds, device-synchronised), per-cycle history and, for the
         staged form, the energy at the end of each stage.  precision:
         'mixed' (staged, FP32 GPU work, FP64 tail) or 'fp64' (the plain FP64
-        form on the final grids)."""
+        form on the final grids).  incremental: FP64 exchange builds after
+        the first of a stage are incremental (K_x(D) = K_x(D0) + K_x(D -
+        D0)), with a full rebuild every rebuild_every cycles and at every
+        stage or precision switch, as PySCF's direct SCF does (the
+        reference forces that rebuild on its switches,
+        staging/schedule.py:335-346); FP32 builds are always full.
+        profile: per-part seconds in out['profile'] (synchronises)."""
         torch = _torch()
         if precision not in ('mixed', 'fp64'):
             raise ValueError("precision must be 'mixed' or 'fp64'")
@@ -334,9 +367,15 @@ class DeviceRKS:
         diis = _Cdiis(diis_space)
         hist, stage_end = [], []
         e_last, converged = None, False
+        base, since_full = None, 0
+        self.profile = {} if profile else None
         for cycle in range(max_cycle):
             grids = self._stage_grids(stage)
-            E, F, parts = self.fock(D, grids, fp64)
+            use = (base if incremental and fp64 and since_full < rebuild_every
+                   else None)
+            E, F, parts, built = self.fock(D, grids, fp64, base=use)
+            since_full = 1 if use is None else since_full + 1
+            base = built
             comm = self._commutator(F, D)
             gnorm = float(torch.linalg.norm(comm))
             Ef = float(E)
@@ -359,6 +398,7 @@ class DeviceRKS:
                     fp64 = True
                 diis = _Cdiis(diis_space)      # the functional changed
                 e_last = None
+                base = None                    # full rebuild after a switch
                 D = self._diag(F)[0]
                 continue
             e_last = Ef
@@ -369,7 +409,11 @@ class DeviceRKS:
         out = dict(e_tot=hist[-1]['e'], converged=converged, cycles=len(hist),
                    wall=wall, setup_s=self.t_setup, history=hist,
                    precision=precision, stages=stage_end,
-                   parts={k: float(v) for k, v in parts.items()}, dm=D)
+                   parts={k: float(v) for k, v in parts.items()}, dm=D,
+                   incremental=bool(incremental))
+        if self.profile is not None:
+            out['profile'] = dict(self.profile)
+            self.profile = None
         if reference_energy is not None:
             out['error_vs_reference'] = out['e_tot'] - float(reference_energy)
             for h in hist:

@@ -46,13 +46,13 @@ def test_fock_build_matches_oracle_on_a_fixed_density():
     D = host.diag(host.H)
     E_ref, F_ref = host.fock(D)
     dg = rks._stage_grids(2)
-    E, F, _ = rks.fock(torch.as_tensor(D, device=rks.device), dg, fp64=True)
+    E, F, _, _ = rks.fock(torch.as_tensor(D, device=rks.device), dg, fp64=True)
     # the screens (k_tile_tol 1e-11, Hartree 1e-14) move single Fock
     # elements by up to ~1e-10 of max|F|; the energy by less
     scale = np.abs(F_ref).max()
     assert abs(float(E) - E_ref) < 1e-9
     assert np.abs(F.cpu().numpy() - F_ref).max() < 1e-9 * scale
-    E32, F32, _ = rks.fock(torch.as_tensor(D, device=rks.device), dg, fp64=False)
+    E32, F32, _, _ = rks.fock(torch.as_tensor(D, device=rks.device), dg, fp64=False)
     assert abs(float(E32) - E_ref) < 1e-5
     assert np.abs(F32.cpu().numpy() - F_ref).max() < 1e-6 * scale
 
@@ -69,6 +69,18 @@ def test_fp64_and_mixed_scf_reach_the_oracle_energy_water_dimer():
     # the staged run went through S0, S1, S2 and the FP64 tail
     assert [s['stage'] for s in rmx['stages']][:2] == [0, 1]
     assert rmx['history'][-1]['fp64']
+
+
+def test_incremental_exchange_builds_reach_the_same_energy():
+    """The FP64 SCF with incremental exchange builds (K_x(D) = K_x(D0) +
+    K_x(D - D0), full rebuild every 8 cycles) converges to the energy of
+    full builds, to 1e-10 Ha."""
+    mol, rks = _dimer_case()
+    full = rks.kernel(precision='fp64', incremental=False)
+    inc = rks.kernel(precision='fp64', incremental=True, profile=True)
+    assert full['converged'] and inc['converged']
+    assert abs(full['e_tot'] - inc['e_tot']) < 1e-10
+    assert set(inc['profile']) >= {'k', 'j', 'xc'}
 
 
 def test_mixed_scf_water8_config1_reaches_the_oracle_energy():
