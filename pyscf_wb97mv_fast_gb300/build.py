@@ -63,7 +63,7 @@ def _stale(target, deps):
 
 def _flags():
     """The flags that change the code: architecture and WB_NVCC_EXTRA
-    (e.g. WB_NVCC_EXTRA=-DWB_COSX_SPLIT=1)."""
+    (e.g. WB_NVCC_EXTRA=-DWB_COSX_SPLIT=0)."""
     return ARCH + os.environ.get('WB_NVCC_EXTRA', '').split()
 
 

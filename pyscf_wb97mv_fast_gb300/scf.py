@@ -285,31 +285,47 @@ class DeviceRKS:
             self.profile[name] = self.profile.get(name, 0.0) + now - self._t_last
         self._t_last = now
 
-    def fock(self, D, grids, fp64, base=None):
+    def fock(self, D, grids, fp64, base=None, inc32=False):
         """(E, F, parts, base') for density D with grids = dict(xc=, sgx=,
-        nlc=) DeviceGrids (nlc may be None).  ``base`` = (D0, Kx0) of an
-        earlier build on the same grids and precision makes the exchange
-        build incremental: K_x = K_x0 + K_x(D - D0), the COSX screen then
-        running on F = X (D - D0), whose small entries drop most tasks (the
-        incremental Fock build of a direct SCF).  base' is (D, K_x)."""
+        nlc=) DeviceGrids (nlc may be None).
+
+        ``base`` (a dict of an earlier full build on the same grids and
+        precision: D0, K_x0, J0, rho0) makes the build incremental from
+        that fixed base, as a direct SCF's incremental Fock build:
+        K_x = K_x0 + K_x(D - D0), its COSX screen running on F = X (D - D0),
+        whose small entries drop most tasks.  With ``inc32`` (the staged
+        form's FP64 tail) the increments of K_x, J and rho are built with
+        the FP32 kernels: their rounding is ~1e-7 of the increment, itself
+        small, so the operator stays FP64-accurate on the FP64 base.
+        Without it (the plain FP64 form) only K_x is incremental, in FP64.
+        base' is the base to keep (a new one after a full build)."""
         torch = _torch()
         f = self.functional
+        gs, gx = grids['sgx'], grids['xc']
         self._tick(None)
-        if base is None:
-            K = self.k_matrices(D, grids['sgx'], fp64)
+        full = base is None
+        dD = None if full else D - base['D']
+        if full:
+            K = self.k_matrices(D, gs, fp64)
             Kx = f.alpha * K[0] + f.beta * K[1]
         else:
-            dK = self.k_matrices(D - base[0], grids['sgx'], fp64)
-            Kx = base[1] + (f.alpha * dK[0] + f.beta * dK[1])
+            dK = self.k_matrices(dD, gs, fp64 and not inc32)
+            Kx = base['Kx'] + (f.alpha * dK[0] + f.beta * dK[1])
         self._tick('k')
-        vh = self.eng.hartree(grids['sgx'].coords, D, tol=self.j_tol, fp64=fp64)
-        J = self._vmat(grids['sgx'], vh, fp64)
+        if full or not inc32:
+            vh = self.eng.hartree(gs.coords, D, tol=self.j_tol, fp64=fp64)
+            J = self._vmat(gs, vh, fp64)
+        else:
+            vh = self.eng.hartree(gs.coords, dD, tol=self.j_tol, fp64=False)
+            J = base['J'] + self._vmat(gs, vh, False)
         self._tick('j')
-        gx = grids['xc']
-        rho = self._density(gx, D, fp64)
+        if full or not inc32:
+            rho = self._density(gx, D, fp64)
+        else:
+            rho = base['rho'] + self._density(gx, dD, False)
         e, v = f.eval(rho)
         exc = (gx.weights * e).sum()
-        Vxc = self._vmat(gx, v, fp64)
+        Vxc = self._vmat(gx, v, fp64 and not inc32)
         self._tick('xc')
         if grids.get('nlc') is not None and f.nlc:
             enl, Vnl = self.vv10(D, grids['nlc'])
@@ -321,7 +337,8 @@ class DeviceRKS:
         ej = 0.5 * (D * J).sum()
         ek = -0.25 * (D * Kx).sum()
         E = e1 + ej + ek + exc + enl + self.e_nuc
-        return E, F, dict(e1=e1, ej=ej, ek=ek, exc=exc, enl=enl), (D, Kx)
+        new_base = dict(D=D, Kx=Kx, J=J, rho=rho) if full else base
+        return E, F, dict(e1=e1, ej=ej, ek=ek, exc=exc, enl=enl), new_base
 
     def _diag(self, F):
         torch = _torch()
@@ -346,12 +363,13 @@ class DeviceRKS:
         (seconds, device-synchronised), per-cycle history and, for the
         staged form, the energy at the end of each stage.  precision:
         'mixed' (staged, FP32 GPU work, FP64 tail) or 'fp64' (the plain FP64
-        form on the final grids).  incremental: FP64 exchange builds after
-        the first of a stage are incremental (K_x(D) = K_x(D0) + K_x(D -
-        D0)), with a full rebuild every rebuild_every cycles and at every
-        stage or precision switch, as PySCF's direct SCF does (the
-        reference forces that rebuild on its switches,
-        staging/schedule.py:335-346); FP32 builds are always full.
+        form on the final grids).  incremental: after a full FP64 build the
+        next FP64 cycles build from it as a fixed base (``fock``): the
+        staged form's tail adds FP32 increments of K, J and rho, the plain
+        FP64 form FP64 increments of K; a full rebuild every rebuild_every
+        cycles and at every stage or precision switch, as PySCF's direct
+        SCF does (the reference forces that rebuild on its switches,
+        staging/schedule.py:335-346).  FP32 stages always build in full.
         profile: per-part seconds in out['profile'] (synchronises)."""
         torch = _torch()
         if precision not in ('mixed', 'fp64'):
@@ -373,9 +391,9 @@ class DeviceRKS:
             grids = self._stage_grids(stage)
             use = (base if incremental and fp64 and since_full < rebuild_every
                    else None)
-            E, F, parts, built = self.fock(D, grids, fp64, base=use)
+            E, F, parts, base = self.fock(D, grids, fp64, base=use,
+                                          inc32=staged)
             since_full = 1 if use is None else since_full + 1
-            base = built
             comm = self._commutator(F, D)
             gnorm = float(torch.linalg.norm(comm))
             Ef = float(E)
