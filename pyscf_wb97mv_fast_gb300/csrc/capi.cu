@@ -1619,6 +1619,9 @@ int wb_cosx_batch_create(int nmol, wb_cosx* const* handles,
         for (int c = 0; c < wb::NCLASS; ++c) {
             bb.rec[c] = at<float4>(b->ws[m], L.recb) + h->hp.rec_off[c];
             bb.Gcls[c] = a.Gcls2[c];
+#if WB_COSX_SPLIT
+            bb.GclsH[c] = a.Gcls2H[c];
+#endif
         }
         args[m] = a;
         args[nmol + m] = bb;
@@ -1630,7 +1633,7 @@ int wb_cosx_batch_create(int nmol, wb_cosx* const* handles,
             int n = 0;
             if (h->hp.cls[c].pair_end > h->hp.cls[c].pair_begin) {
                 const int pc = b->dual[c] ? h->pts2[c] : h->pts[c];
-                n = args[m].nblk[pc == 4 ? 2 : pc - 1];
+                n = (WB_COSX_SPLIT ? 2 : 1) * args[m].nblk[pc == 4 ? 2 : pc - 1];
             }
             if ((int64_t)o[m] + n > INT32_MAX)
                 return batch_fail(b, fail(WB_ERR_UNSUPPORTED,
@@ -1822,8 +1825,15 @@ int wb_cosx_batch_run(wb_cosx_batch* b, const double* const* qd,
         float* Gs[2] = {at<float>(ws, L.G32), at<float>(ws, L.G32b)};
         const size_t gcl[2] = {L.gcls, L.gcls2};
         double* Ks[2] = {k_out[m] + kk * b->kidx[0], k_out[m] + kk * b->kidx[1]};
+#if WB_COSX_SPLIT
+        const size_t gclH[2] = {L.gclsH, L.gcls2H};
+        for (int w = 0; w < b->nom; ++w)
+            WB_CUDA(wb::launch_gsum2(at<float>(ws, gcl[w]), at<float>(ws, gclH[w]),
+                                     h->gsrc, nao, ld, Gs[w], s));
+#else
         for (int w = 0; w < b->nom; ++w)
             WB_CUDA(wb::launch_gsum(at<float>(ws, gcl[w]), h->gsrc, nao, ld, Gs[w], s));
+#endif
         launches += b->nom;
         if (b->gemm == WB_K_GEMM_OZAKI_BF16) {
             const float* Gc[2] = {Gs[0], Gs[1]};

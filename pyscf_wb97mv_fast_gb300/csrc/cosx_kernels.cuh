@@ -653,12 +653,18 @@ cosx_class_kernel_batch(const CosxArgs* __restrict__ args,
         }
         const CosxArgs& Am = sA[warp];
 #if WB_COSX_SPLIT
-        // the batched form does not split: one item per block, buffer set 0
-        cosx_class_block<LA, LB, FAR, STAGE, NW>(Am, Am.cls_pb[CLS], Am.cls_pe[CLS],
-                                                 item - item_off[m], stab, wstage,
-                                                 rmax, sbuf, kept, flops,
-                                                 ints WB_STAGER_ARG, 0,
-                                                 item - item_off[m]);
+        // two items per block, as in the single-molecule kernel: half h of
+        // block it >> 1 writes buffer set h (summed after set 0)
+        {
+            const int it = item - item_off[m];
+            const int h = it & 1;
+            const int split = Am.cls_split[CLS];
+            cosx_class_block<LA, LB, FAR, STAGE, NW>(Am, h ? split : Am.cls_pb[CLS],
+                                                     h ? Am.cls_pe[CLS] : split,
+                                                     it >> 1, stab, wstage, rmax, sbuf,
+                                                     kept, flops, ints WB_STAGER_ARG,
+                                                     h, it);
+        }
 #else
         cosx_class_block<LA, LB, FAR, STAGE, NW>(Am, Am.cls_pb[CLS], Am.cls_pe[CLS],
                                                  item - item_off[m], stab, wstage,
