@@ -269,10 +269,11 @@ class DeviceRKS:
                                       tile_tol=self.k_tile_tol, stats=False)
         return 0.5 * (Kb + Kb.transpose(1, 2))
 
-    def vv10(self, D, g):
-        """(E_nl, V_nl) on the NLC grid g (device scalars / matrix)."""
+    def vv10(self, D, g, fp64=True):
+        """(E_nl, V_nl) on the NLC grid g (device scalars / matrix); the
+        FP32 stages take its two GEMMs through the bf16 split."""
         from pyscf_wb97mv_fast_gb300.gpu.vv10 import vv10_energy_fock
-        return vv10_energy_fock(self.eng, g, D, self.functional.nlc)
+        return vv10_energy_fock(self.eng, g, D, self.functional.nlc, fp32=not fp64)
 
     def _tick(self, name):
         """Per-part wall time (device-synchronised) when profiling."""
@@ -328,7 +329,7 @@ class DeviceRKS:
         Vxc = self._vmat(gx, v, fp64 and not inc32)
         self._tick('xc')
         if grids.get('nlc') is not None and f.nlc:
-            enl, Vnl = self.vv10(D, grids['nlc'])
+            enl, Vnl = self.vv10(D, grids['nlc'], fp64)
         else:
             enl, Vnl = torch.zeros((), dtype=torch.float64, device=self.device), 0.0
         self._tick('vv10')
