@@ -877,6 +877,71 @@ def scf_timing(torch):
     return out
 
 
+def _scf_record(r, ref):
+    """The per-form fields of an SCF leg: energy, error against ref, walls
+    (whole run, and to the first FP64 cycle within 1e-8 Ha of ref)."""
+    t_hit = None
+    if ref is not None:
+        for h in r['history']:
+            if abs(h['e'] - ref) < 1e-8 and h['fp64']:
+                t_hit = h['t']
+                break
+    return {'e_tot': r['e_tot'], 'error_vs_reference': r.get('error_vs_reference'),
+            'converged': r['converged'], 'cycles': r['cycles'], 'wall_s': r['wall'],
+            'wall_to_1e-8_s': t_hit,
+            'cycles_fp64': sum(1 for h in r['history'] if h['fp64']),
+            'stages': [dict(s) for s in r['stages']]}
+
+
+def scf_c20_timing(torch, n_carbon=20):
+    """Config 3: the staged mixed-precision SCF of all-trans C20H42 in the
+    synthetic def2-TZVP structure (f shells) on the reference's per-stage
+    grid table (XC 1/3/3, SGX 1/1/2, NLC off/1/3), against the plain FP64
+    form on the final grids.  The host oracle SCF needs about 45 min for
+    192 AOs, so the FP64 form's converged energy -- the form pinned to the
+    oracle's SCF to 2e-10 Ha on config 1 and on an f-shell molecule in the
+    GPU tests -- is the FP64 reference energy here.  Each form runs once
+    from the core guess (per-part profile on); grids and AO values are
+    built by an untimed warm-up."""
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.scf import DeviceRKS, REFERENCE_STAGE_LEVELS
+    from pyscf_wb97mv_fast_gb300.systems import alkane
+    mol = Molecule.build(alkane(n_carbon), 'synthetic-tzvp')
+    rks = DeviceRKS(mol, stage_levels=REFERENCE_STAGE_LEVELS)
+    t0 = time.perf_counter()
+    for st in (0, 1, 2):
+        grids = rks._stage_grids(st)
+    setup = time.perf_counter() - t0
+    rks.kernel(precision='mixed', max_cycle=1)
+    rks.kernel(precision='fp64', max_cycle=1)
+    r64 = rks.kernel(precision='fp64', profile=True)
+    ref = r64['e_tot']
+    rmx = rks.kernel(precision='mixed', profile=True, reference_energy=ref)
+    r64['error_vs_reference'] = 0.0
+    for h in r64['history']:
+        h['err'] = h['e'] - ref
+    out = {'molecule': 'all-trans C%dH%d (C-C 1.53, C-H 1.09 A)' % (n_carbon, 2 * n_carbon + 2),
+           'basis': 'synthetic def2-TZVP structure (f shells)', 'nao': mol.nao,
+           'stage_levels': {k: list(v) for k, v in REFERENCE_STAGE_LEVELS.items()},
+           'grid_points': {'%s_level%d' % (k, lv): int(rks.grid(k, lv).n)
+                           for k, v in REFERENCE_STAGE_LEVELS.items() for lv in set(v)
+                           if lv is not None},
+           'grid_setup_s': setup, 'functional': rks.functional.name,
+           'reference_energy': ref,
+           'reference': 'the plain FP64 device form on the final grids (pinned to the '
+                        'host oracle SCF on config 1 and on ethane/TZVP)'}
+    out['mixed'] = _scf_record(rmx, ref)
+    out['mixed']['profile_s'] = {k: round(v, 3) for k, v in rmx['profile'].items()}
+    out['fp64'] = _scf_record(r64, ref)
+    out['fp64']['profile_s'] = {k: round(v, 3) for k, v in r64['profile'].items()}
+    out['fp64_over_mixed_wall'] = r64['wall'] / rmx['wall']
+    m, f = out['mixed'], out['fp64']
+    if m['wall_to_1e-8_s'] and f['wall_to_1e-8_s']:
+        out['fp64_over_mixed_to_1e-8'] = f['wall_to_1e-8_s'] / m['wall_to_1e-8_s']
+    rks.eng.close()
+    return out
+
+
 def run_sample(oracle, mol, g, dm, idx):
     coords = g.coords[idx]
     X = oracle.ao_eval(mol, coords)
@@ -974,6 +1039,9 @@ def main():
                     help='skip the C20H42 / def2-TZVP (f shells) leg')
     ap.add_argument('--no-scf', action='store_true',
                     help='skip the device SCF leg (config 1, mixed vs FP64)')
+    ap.add_argument('--scf-c20', action='store_true',
+                    help='add the C20H42 / def2-TZVP staged SCF leg (config 3; '
+                         'minutes: its plain FP64 run is the reference energy)')
     ap.add_argument('--no-reference-gpu', action='store_true',
                     help="skip the reference's own kernels on this GPU")
     ap.add_argument('--no-parity', action='store_true',
@@ -1149,6 +1217,7 @@ def main():
     alk = None if (args.no_alkane or world > 1) else alkane_timing(torch, peak)
     torch.cuda.empty_cache()
     scf = None if (args.no_scf or world > 1) else scf_timing(torch)
+    scf_c20 = scf_c20_timing(torch) if (args.scf_c20 and world == 1) else None
     torch.cuda.empty_cache()
     parity = None if args.no_parity else parity_vs_oracle(mol, g, dm, eng, torch, 3000)
 
@@ -1180,6 +1249,7 @@ def main():
             'k_grad': k_grad,
             'alkane_c20_tzvp': alk,
             'scf': scf,
+            'scf_c20h42_tzvp': scf_c20,
             'reference_gpu': refgpu,
             'parity_vs_fp64_oracle': parity,
             'clocks': clocks.summary(),

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "f32x2.cuh"
+
 namespace wb {
 
 // ---------------------------------------------------------------------------
@@ -68,33 +70,44 @@ __device__ __forceinline__ void boys_taylor(float T, float* F,
 // in double-float (rsqrt and one Newton correction), the powers and the
 // odd double factorials in double-float, one rounding per R000_n -- the
 // same accuracy as c_n times the asymptotic F_n in double-float.
-template<int L>
-__device__ __forceinline__ void far_r000(const float r2, const float k0h,
-                                         const float k0l, float* R) {
-    const float s0 = rsqrtf(r2);
-    const float a = s0 * s0;
-    const float a_lo = fmaf(s0, s0, -a);
-    const float rr = fmaf(-r2, a, 1.0f) - r2 * a_lo;
-    const float sh = s0, sl = 0.5f * s0 * rr;
-    R[0] = fmaf(k0h, sh, fmaf(k0h, sl, k0l * sh));
+// V = float (one point) or float2 (a lane's two points, packed); the two
+// forms give bitwise the same values.
+template<int L, typename V>
+__device__ __forceinline__ void far_r000_v(const V r2, const float k0h_s,
+                                           const float k0l_s, V* R) {
+    const V k0h = v_const<V>(k0h_s), k0l = v_const<V>(k0l_s);
+    const V s0 = v_rsqrt(r2);
+    const V a = v_mul(s0, s0);
+    const V a_lo = v_fma(s0, s0, v_neg(a));
+    // 1 - r2 s0^2 with the square exact
+    const V rr = v_fma(v_neg(r2), a_lo, v_fma(v_neg(r2), a, v_const<V>(1.0f)));
+    const V sh = s0, sl = v_mul(v_mul(v_const<V>(0.5f), s0), rr);
+    R[0] = v_fma(k0h, sh, v_fma(k0h, sl, v_mul(k0l, sh)));
     if (L >= 1) {
-        const float uh = sh * sh;
-        const float ul = fmaf(sh, sh, -uh) + 2.0f * sh * sl;
-        float th = k0h * sh;
-        float tl = fmaf(k0h, sh, -th) + fmaf(k0h, sl, k0l * sh);
+        const V uh = v_mul(sh, sh);
+        const V ul = v_fma(v_mul(v_const<V>(2.0f), sh), sl, v_fma(sh, sh, v_neg(uh)));
+        V th = v_mul(k0h, sh);
+        V tl = v_add(v_fma(k0h, sh, v_neg(th)), v_fma(k0h, sl, v_mul(k0l, sh)));
 #pragma unroll
         for (int n = 1; n <= L; ++n) {
             // t *= u, then R000_n = t (-(2n-1)!!)
-            const float p = th * uh;
-            const float e = fmaf(th, uh, -p) + fmaf(th, ul, tl * uh);
-            th = p + e;
-            tl = e - (th - p);
-            float df = 1.0f;
-            for (int j = 1; j <= n; ++j) df *= -(float)(2 * j - 1);
-            const float q = th * df;
-            R[n] = q + (fmaf(th, df, -q) + tl * df);
+            const V p = v_mul(th, uh);
+            const V e = v_add(v_fma(th, uh, v_neg(p)), v_fma(th, ul, v_mul(tl, uh)));
+            th = v_add(p, e);
+            tl = v_sub(e, v_sub(th, p));
+            float dfs = 1.0f;
+            for (int j = 1; j <= n; ++j) dfs *= -(float)(2 * j - 1);
+            const V df = v_const<V>(dfs);
+            const V q = v_mul(th, df);
+            R[n] = v_add(q, v_fma(tl, df, v_fma(th, df, v_neg(q))));
         }
     }
+}
+
+template<int L>
+__device__ __forceinline__ void far_r000(const float r2, const float k0h,
+                                         const float k0l, float* R) {
+    far_r000_v<L, float>(r2, k0h, k0l, R);
 }
 
 // Double-float helpers of the asymptotic branch: a value is hi + lo with

@@ -60,6 +60,15 @@ __device__ __forceinline__ void gb_add(float* p, const float y) {
     atomicAdd(p, y);
 }
 
+// Packed FP32 (f32x2.cuh) in the PTS = 2 two-omega task bodies: the
+// distances, far-field R000, recurrences, Hermite sums and accumulations
+// of the lane's two points in float2 halves (the near-field Boys sums stay
+// per point: each point reads its own table row).  -DWB_COSX_F32X2=0
+// compiles the scalar form.
+#ifndef WB_COSX_F32X2
+#define WB_COSX_F32X2 1
+#endif
+
 }  // namespace wb
 
 namespace wb {

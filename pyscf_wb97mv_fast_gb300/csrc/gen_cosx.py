@@ -87,8 +87,19 @@ def rname(t, u, v):
     return 'r_%d_%d_%d' % (t, u, v)
 
 
-def gen_recurrence(L, lines, ind):
-    """In-place R recurrence over levels n = L .. 0 (only t+u+v <= L-n)."""
+def gen_recurrence(L, lines, ind, packed=False):
+    """In-place R recurrence over levels n = L .. 0 (only t+u+v <= L-n).
+    packed: the same operations on float2 (two grid points per lane)."""
+    def mul(d, a):
+        return ('mul2(%s, %s)' if packed else '%s * %s') % (d, a)
+
+    def step(d, a, c, b):
+        if not packed:
+            return 'fmaf(%s, %s, %s * %s)' % (d, a, flit(c), b)
+        # c * b with c = 1 is b exactly (the scalar form's compiler folds it)
+        cb = b if c == 1 else 'mul2(bc2(%s), %s)' % (flit(c), b)
+        return 'fma2(%s, %s, %s)' % (d, a, cb)
+
     for n in range(L, -1, -1):
         m = L - n
         if m >= 1:
@@ -97,28 +108,25 @@ def gen_recurrence(L, lines, ind):
                 for v in range(m - u):
                     for t in range(m - u - v, 0, -1):
                         if t == 1:
-                            expr = 'dx * %s' % rname(0, u, v)
+                            expr = mul('dx', rname(0, u, v))
                         else:
-                            expr = 'fmaf(dx, %s, %s * %s)' % (
-                                rname(t - 1, u, v), flit(t - 1),
-                                rname(t - 2, u, v))
+                            expr = step('dx', rname(t - 1, u, v), t - 1,
+                                        rname(t - 2, u, v))
                         lines.append('%s%s = %s;' % (ind, rname(t, u, v), expr))
             # t = 0, u >= 1
             for v in range(m):
                 for u in range(m - v, 0, -1):
                     if u == 1:
-                        expr = 'dy * %s' % rname(0, 0, v)
+                        expr = mul('dy', rname(0, 0, v))
                     else:
-                        expr = 'fmaf(dy, %s, %s * %s)' % (
-                            rname(0, u - 1, v), flit(u - 1), rname(0, u - 2, v))
+                        expr = step('dy', rname(0, u - 1, v), u - 1, rname(0, u - 2, v))
                     lines.append('%s%s = %s;' % (ind, rname(0, u, v), expr))
             # t = u = 0, v >= 1
             for v in range(m, 0, -1):
                 if v == 1:
-                    expr = 'dz * %s' % rname(0, 0, 0)
+                    expr = mul('dz', rname(0, 0, 0))
                 else:
-                    expr = 'fmaf(dz, %s, %s * %s)' % (
-                        rname(0, 0, v - 1), flit(v - 1), rname(0, 0, v - 2))
+                    expr = step('dz', rname(0, 0, v - 1), v - 1, rname(0, 0, v - 2))
                 lines.append('%s%s = %s;' % (ind, rname(0, 0, v), expr))
         lines.append('%s%s = R000_%d;' % (ind, rname(0, 0, 0), n))
 
@@ -127,11 +135,20 @@ def ename(ax, i, j, t):
     return 'e%s_%d_%d_%d' % ('xyz'[ax], i, j, t)
 
 
-def gen_hermite(la, lb, ca_c, cb_c, ind, lines, tag):
+def gen_hermite(la, lb, ca_c, cb_c, ind, lines, tag, packed=False):
     """s = sum_t Ex sum_u Ey sum_v Ez R_tuv for one (ca, cb); returns the
-    variable holding it."""
+    variable holding it.  packed: float2 operations, the E values read
+    from their broadcast pairs B<name>."""
     (i, j, k) = ca_c
     (ip, jp, kp) = cb_c
+    ty = 'float2' if packed else 'float'
+
+    def mul(e, r):
+        return ('mul2(B%s, %s)' if packed else '%s * %s') % (e, r)
+
+    def fma(e, r, acc):
+        return ('fma2(B%s, %s, %s)' if packed else 'fmaf(%s, %s, %s)') % (e, r, acc)
+
     s_terms = []
     for t in range(i + ip + 1):
         u_terms = []
@@ -143,8 +160,8 @@ def gen_hermite(la, lb, ca_c, cb_c, ind, lines, tag):
                 acc = None
                 for v in range(k + kp + 1):
                     e = ename(2, k, kp, v)
-                    acc = ('%s * %s' % (e, rname(t, u, v)) if acc is None
-                           else 'fmaf(%s, %s, %s)' % (e, rname(t, u, v), acc))
+                    acc = (mul(e, rname(t, u, v)) if acc is None
+                           else fma(e, rname(t, u, v), acc))
                 zexpr = acc
             if j == 0 and jp == 0:
                 u_terms.append(zexpr)
@@ -157,9 +174,8 @@ def gen_hermite(la, lb, ca_c, cb_c, ind, lines, tag):
             acc = None
             for (e, z) in u_terms:
                 zv = 'z%s_%d_%d' % (tag, t, len(lines))
-                lines.append('%sconst float %s = %s;' % (ind, zv, z))
-                acc = ('%s * %s' % (e, zv) if acc is None
-                       else 'fmaf(%s, %s, %s)' % (e, zv, acc))
+                lines.append('%sconst %s %s = %s;' % (ind, ty, zv, z))
+                acc = mul(e, zv) if acc is None else fma(e, zv, acc)
             yexpr = acc
         if i == 0 and ip == 0:
             s_terms.append(yexpr)
@@ -171,12 +187,11 @@ def gen_hermite(la, lb, ca_c, cb_c, ind, lines, tag):
         acc = None
         for (e, y) in s_terms:
             yv = 'y%s_%d' % (tag, len(lines))
-            lines.append('%sconst float %s = %s;' % (ind, yv, y))
-            acc = ('%s * %s' % (e, yv) if acc is None
-                   else 'fmaf(%s, %s, %s)' % (e, yv, acc))
+            lines.append('%sconst %s %s = %s;' % (ind, ty, yv, y))
+            acc = mul(e, yv) if acc is None else fma(e, yv, acc)
         sexpr = acc
     sv = 's%s' % tag
-    lines.append('%sconst float %s = %s;' % (ind, sv, sexpr))
+    lines.append('%sconst %s %s = %s;' % (ind, ty, sv, sexpr))
     return sv
 
 
@@ -583,19 +598,25 @@ def rec_stride2(la, lb):
     return 2 + 2 * n_om(la, lb) + e_stride(la, lb) // 4
 
 
-def gen_r000(la, lb, J, lines, of_prefix, near_first, slot):
+def gen_r000(la, lb, J, lines, of_prefix, near_first, slot, packed=False):
     """R0[slot][p][n] for every point from the distances r2v, with the
     omega record fields named <of_prefix><q>: warp-uniform all-far /
     all-near branches (the likelier one tested first), per point for mixed
-    warps."""
+    warps.  packed (PTS = 2): R0p[slot][n] float2 pairs, the all-far branch
+    on both points at once (far_r000_v<L, float2>)."""
     L = la + lb
     nom = n_om(la, lb)
     comp = 'xyzw'
     o = lambda q: '%s%d' % (of_prefix, q)
     of = o(nom - 1)
 
-    def near(ind):
-        lines.append(ind + 'const float T = fmaf(%s.x, r2v[p], %s.y * r2v[p]);' % (o(0), o(0)))
+    def dst(p, n):
+        return ('R0p[%d][%d].%s' % (slot, n, 'xy'[int(p)]) if packed
+                else 'R0[%d][p][%d]' % (slot, n))
+
+    def near(ind, p='p'):
+        lines.append(ind + 'const float T = fmaf(%s.x, r2v[%s], %s.y * r2v[%s]);'
+                     % (o(0), p, o(0), p))
         lines.append(ind + 'float Fb[%d];' % (L + 1))
         lines.append(ind + 'boys_taylor<%d>(T, Fb, stab);' % L)
         for n in range(L + 1):
@@ -603,11 +624,40 @@ def gen_r000(la, lb, J, lines, of_prefix, near_first, slot):
             fl = fh + 1
             ch = '%s.%s' % (o(fh // 4), comp[fh % 4])
             cl = '%s.%s' % (o(fl // 4), comp[fl % 4])
-            lines.append(ind + 'R0[%d][p][%d] = fmaf(%s, Fb[%d], %s * Fb[%d]);'
-                         % (slot, n, ch, n, cl, n))
+            lines.append(ind + '%s = fmaf(%s, Fb[%d], %s * Fb[%d]);'
+                         % (dst(p, n), ch, n, cl, n))
 
-    def far(ind):
-        lines.append(ind + 'far_r000<%d>(r2v[p], %s.x, %s.y, R0[%d][p]);' % (L, of, of, slot))
+    def far(ind, p='p'):
+        if not packed:
+            lines.append(ind + 'far_r000<%d>(r2v[p], %s.x, %s.y, R0[%d][p]);'
+                         % (L, of, of, slot))
+            return
+        lines.append(ind + 'float Rt[%d];' % (L + 1))
+        lines.append(ind + 'far_r000<%d>(r2v[%s], %s.x, %s.y, Rt);' % (L, p, of, of))
+        for n in range(L + 1):
+            lines.append(ind + '%s = Rt[%d];' % (dst(p, n), n))
+
+    def far_all(ind):
+        lines.append(ind + 'far_r000_v<%d, float2>(r2, %s.x, %s.y, R0p[%d]);'
+                     % (L, of, of, slot))
+
+    def per_point(ind, body):
+        if packed:
+            for p in range(2):
+                lines.append(ind + '{')
+                body(ind + '    ', str(p))
+                lines.append(ind + '}')
+        else:
+            lines.append(ind + '#pragma unroll')
+            lines.append(ind + 'for (int p = 0; p < PTS; ++p) {')
+            body(ind + '    ')
+            lines.append(ind + '}')
+
+    def branch(kind, ind):
+        if kind == 'far' and packed:
+            far_all(ind)
+        else:
+            per_point(ind, far if kind == 'far' else near)
 
     lines.append(J + '{')
     K = J + '    '
@@ -618,35 +668,34 @@ def gen_r000(la, lb, J, lines, of_prefix, near_first, slot):
     lines.append(K + '    allfar = allfar && f;')
     lines.append(K + '    allnear = allnear && !f;')
     lines.append(K + '}')
-    first, second = (('allnear', near), ('allfar', far)) if near_first else (('allfar', far), ('allnear', near))
+    first, second = (('allnear', 'near'), ('allfar', 'far')) if near_first else (('allfar', 'far'), ('allnear', 'near'))
     lines.append(K + 'if (__all_sync(0xffffffffu, %s)) {' % first[0])
-    lines.append(K + '    #pragma unroll')
-    lines.append(K + '    for (int p = 0; p < PTS; ++p) {')
-    first[1](K + '        ')
-    lines.append(K + '    }')
+    branch(first[1], K + '    ')
     lines.append(K + '} else if (__all_sync(0xffffffffu, %s)) {' % second[0])
-    lines.append(K + '    #pragma unroll')
-    lines.append(K + '    for (int p = 0; p < PTS; ++p) {')
-    second[1](K + '        ')
-    lines.append(K + '    }')
+    branch(second[1], K + '    ')
     lines.append(K + '} else {')
-    lines.append(K + '    #pragma unroll')
-    lines.append(K + '    for (int p = 0; p < PTS; ++p) {')
-    lines.append(K + '        if (r2v[p] >= %s.z) {' % of)
-    far(K + '            ')
-    lines.append(K + '        } else {')
-    near(K + '            ')
-    lines.append(K + '        }')
-    lines.append(K + '    }')
+
+    def mixed(ind, p='p'):
+        lines.append(ind + 'if (r2v[%s] >= %s.z) {' % (p, of))
+        far(ind + '    ', p)
+        lines.append(ind + '} else {')
+        near(ind + '    ', p)
+        lines.append(ind + '}')
+    per_point(K + '    ', mixed)
     lines.append(K + '}')
     lines.append(J + '}')
 
 
-def gen_prim_body_dual(la, lb, diag, J, lines):
+def gen_prim_body_dual(la, lb, diag, J, lines, packed=False):
     """Dual-omega work of one primitive pair whose record is at q (shared
     memory): the distances once, then for each omega slot the R000 sources
     (slot 0: all-far tested first, slot 1: all-near first), the R
-    recurrence, the Hermite sums and the Y (and X) accumulation."""
+    recurrence, the Hermite sums and the Y (and X) accumulation.
+
+    packed (PTS = 2): the distances, recurrence, Hermite sums and
+    accumulations run on float2 pairs of the lane's two points, the same
+    operations in the same order as the scalar body; the R000 sources
+    (Boys function, far form, the warp votes) stay per point."""
     L = la + lb
     ca = cart_components(la)
     cb = cart_components(lb)
@@ -674,14 +723,27 @@ def gen_prim_body_dual(la, lb, diag, J, lines):
                 nm = flat[4 * k + c]
                 if nm is not None:
                     lines.append(J + 'const float %s = ev%d.%s;' % (nm, k, comp[c]))
-    lines.append(J + 'float dxv[PTS], dyv[PTS], dzv[PTS], r2v[PTS], R0[2][PTS][%d];' % (L + 1))
-    lines.append(J + '#pragma unroll')
-    lines.append(J + 'for (int p = 0; p < PTS; ++p) {')
-    lines.append(J + '    dxv[p] = (ph.x - gxh[p]) + (pl.x - gxl[p]);')
-    lines.append(J + '    dyv[p] = (ph.y - gyh[p]) + (pl.y - gyl[p]);')
-    lines.append(J + '    dzv[p] = (ph.z - gzh[p]) + (pl.z - gzl[p]);')
-    lines.append(J + '    r2v[p] = fmaf(dxv[p], dxv[p], fmaf(dyv[p], dyv[p], dzv[p] * dzv[p]));')
-    lines.append(J + '}')
+                    if packed:
+                        lines.append(J + 'const float2 B%s = bc2(%s);' % (nm, nm))
+    if packed:
+        # a - b as a + (-b) (exact), the grid's negated pairs made once per task
+        lines.append(J + 'float r2v[PTS];')
+        lines.append(J + 'float2 R0p[2][%d];' % (L + 1))
+        for ax in 'xyz':
+            lines.append(J + 'const float2 d%s = add2(add2(bc2(ph.%s), NG%sH), '
+                         'add2(bc2(pl.%s), NG%sL));' % (ax, ax, ax.upper(), ax, ax.upper()))
+        lines.append(J + 'const float2 r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));')
+        lines.append(J + 'r2v[0] = r2.x;')
+        lines.append(J + 'r2v[1] = r2.y;')
+    else:
+        lines.append(J + 'float dxv[PTS], dyv[PTS], dzv[PTS], r2v[PTS], R0[2][PTS][%d];' % (L + 1))
+        lines.append(J + '#pragma unroll')
+        lines.append(J + 'for (int p = 0; p < PTS; ++p) {')
+        lines.append(J + '    dxv[p] = (ph.x - gxh[p]) + (pl.x - gxl[p]);')
+        lines.append(J + '    dyv[p] = (ph.y - gyh[p]) + (pl.y - gyl[p]);')
+        lines.append(J + '    dzv[p] = (ph.z - gzh[p]) + (pl.z - gzl[p]);')
+        lines.append(J + '    r2v[p] = fmaf(dxv[p], dxv[p], fmaf(dyv[p], dyv[p], dzv[p] * dzv[p]));')
+        lines.append(J + '}')
     # the common case of a full-range + long-range pair: slot a far and slot
     # b near for the whole warp -- one vote, both slots in one basic block
     ofa, ofb = 'oa%d' % (nom - 1), 'ob%d' % (nom - 1)
@@ -691,26 +753,54 @@ def gen_prim_body_dual(la, lb, diag, J, lines):
     lines.append(J + '    farnear = farnear && r2v[p] >= %s.z && r2v[p] < %s.z;' % (ofa, ofb))
     lines.append(J + 'if (__all_sync(0xffffffffu, farnear)) {')
     K = J + '    '
-    lines.append(K + '#pragma unroll')
-    lines.append(K + 'for (int p = 0; p < PTS; ++p) {')
-    lines.append(K + '    far_r000<%d>(r2v[p], %s.x, %s.y, R0[0][p]);' % (L, ofa, ofa))
-    lines.append(K + '    const float T = fmaf(ob0.x, r2v[p], ob0.y * r2v[p]);')
-    lines.append(K + '    float Fb[%d];' % (L + 1))
-    lines.append(K + '    boys_taylor<%d>(T, Fb, stab);' % L)
-    for n in range(L + 1):
-        fh = 2 + 2 * n
-        fl = fh + 1
-        ch = 'ob%d.%s' % (fh // 4, comp[fh % 4])
-        cl = 'ob%d.%s' % (fl // 4, comp[fl % 4])
-        lines.append(K + '    R0[1][p][%d] = fmaf(%s, Fb[%d], %s * Fb[%d]);'
-                     % (n, ch, n, cl, n))
-    lines.append(K + '}')
+
+    def near_b(ind, p, dst):
+        lines.append(ind + 'const float T = fmaf(ob0.x, r2v[%s], ob0.y * r2v[%s]);' % (p, p))
+        lines.append(ind + 'float Fb[%d];' % (L + 1))
+        lines.append(ind + 'boys_taylor<%d>(T, Fb, stab);' % L)
+        for n in range(L + 1):
+            fh = 2 + 2 * n
+            fl = fh + 1
+            ch = 'ob%d.%s' % (fh // 4, comp[fh % 4])
+            cl = 'ob%d.%s' % (fl // 4, comp[fl % 4])
+            lines.append(ind + '%s = fmaf(%s, Fb[%d], %s * Fb[%d]);'
+                         % (dst(n), ch, n, cl, n))
+
+    if packed:
+        lines.append(K + 'far_r000_v<%d, float2>(r2, %s.x, %s.y, R0p[0]);' % (L, ofa, ofa))
+        for p in range(2):
+            lines.append(K + '{')
+            near_b(K + '    ', str(p), lambda n, p=p: 'R0p[1][%d].%s' % (n, 'xy'[p]))
+            lines.append(K + '}')
+    else:
+        lines.append(K + '#pragma unroll')
+        lines.append(K + 'for (int p = 0; p < PTS; ++p) {')
+        lines.append(K + '    far_r000<%d>(r2v[p], %s.x, %s.y, R0[0][p]);' % (L, ofa, ofa))
+        near_b(K + '    ', 'p', lambda n: 'R0[1][p][%d]' % n)
+        lines.append(K + '}')
     lines.append(J + '} else {')
-    gen_r000(la, lb, K, lines, 'oa', False, 0)
-    gen_r000(la, lb, K, lines, 'ob', True, 1)
+    gen_r000(la, lb, K, lines, 'oa', False, 0, packed)
+    gen_r000(la, lb, K, lines, 'ob', True, 1, packed)
     lines.append(J + '}')
     lines.append(J + '#pragma unroll')
     lines.append(J + 'for (int w = 0; w < 2; ++w) {')
+    if packed:
+        K = J + '    '
+        for n in range(L + 1):
+            lines.append(K + 'const float2 R000_%d = R0p[w][%d];' % (n, n))
+        lines.append(K + 'float2 ' + ', '.join(rname(*x) for x in tuv) + ';')
+        gen_recurrence(L, lines, K, packed=True)
+        for ia, cac in enumerate(ca):
+            for ib, cbc in enumerate(cb):
+                tag = '%d_%d' % (ia, ib)
+                sv = gen_hermite(la, lb, cac, cbc, K, lines, tag, packed=True)
+                lines.append(K + 'Yp[w][%d] = fma2(f0p[%d], %s, Yp[w][%d]);'
+                             % (ib, ia, sv, ib))
+                if not diag:
+                    lines.append(K + 'Xp[w][%d] = fma2(%s, h0p[%d], Xp[w][%d]);'
+                                 % (ia, sv, ib, ia))
+        lines.append(J + '}')
+        return
     lines.append(J + '#pragma unroll')
     lines.append(J + 'for (int p = 0; p < PTS; ++p) {')
     K = J + '    '
@@ -818,6 +908,102 @@ def gen_class_dual(la, lb, diag):
     return '\n'.join(lines)
 
 
+def gen_class_dual_packed(la, lb, diag):
+    """The PTS = 2 form of gen_class_dual: accumulators, F values and the
+    lane's two grid points held as float2 pairs, the primitive-pair work
+    on the packed FP32 instructions (bitwise the scalar form's results)."""
+    nb = 2 * lb + 1
+    nca = (la + 1) * (la + 2) // 2
+    ncb = (lb + 1) * (lb + 2) // 2
+    lines = []
+    I = '    '
+    J = I * 2
+    lines.append('template<> struct CosxTask2<%d, %d, %s, 2> {'
+                 % (la, lb, 'true' if diag else 'false'))
+    lines.append('static __device__ __forceinline__ void run(')
+    lines.append('    float* const* Gp, const int ld, const int gb0,')
+    lines.append('    const float4* __restrict__ rp, const int npp, const bool* ok,')
+    lines.append('    const float* gxh, const float* gyh, const float* gzh,')
+    lines.append('    const float* gxl, const float* gyl, const float* gzl,')
+    lines.append('    const float4* __restrict__ stab, const float* f0,')
+    lines.append('    const float* fb, float* Xa)')
+    lines.append('{')
+    lines.append(I + 'constexpr int PTS = 2;')
+    for ax in 'xyz':
+        for hl in 'hl':
+            lines.append(I + 'const float2 NG%s%s = make_float2(-g%s%s[0], -g%s%s[1]);'
+                         % (ax.upper(), hl.upper(), ax, hl, ax, hl))
+    lines.append(I + 'float2 f0p[%d], Yp[2][%d];' % (nca, ncb))
+    for c in range(nca):
+        lines.append(I + 'f0p[%d] = make_float2(f0[%d], f0[%d]);' % (c, c, nca + c))
+    for c in range(ncb):
+        lines.append(I + 'Yp[0][%d] = make_float2(0.0f, 0.0f);' % c)
+        lines.append(I + 'Yp[1][%d] = make_float2(0.0f, 0.0f);' % c)
+    if not diag:
+        lines.append(I + 'float2 h0p[%d], Xp[2][%d];' % (ncb, nca))
+        lines.append('#if !WB_COSX_GB_RED')
+        lines.append(I + 'float gbo[2][PTS][%d];' % nb)
+        lines.append(I + '#pragma unroll')
+        lines.append(I + 'for (int w = 0; w < 2; ++w)')
+        lines.append(I + '#pragma unroll')
+        lines.append(I + 'for (int p = 0; p < PTS; ++p) {')
+        for nu in range(nb):
+            lines.append(J + 'gbo[w][p][%d] = Gp[w * PTS + p][(long long)(gb0 + %d) * ld];'
+                         % (nu, nu))
+        lines.append(I + '}')
+        lines.append('#endif')
+        lines.append(I + '#pragma unroll')
+        lines.append(I + 'for (int w = 0; w < 2; ++w) {')
+        for c in range(nca):
+            lines.append(J + 'Xp[w][%d] = make_float2(Xa[(w * PTS) * %d + %d], '
+                         'Xa[(w * PTS + 1) * %d + %d]);' % (c, nca, c, nca, c))
+        lines.append(I + '}')
+        for p in range(2):
+            for nu in range(nb):
+                lines.append(I + 'const float fb%d_%d = fb[%d];' % (p, nu, p * nb + nu))
+            gen_transform_in(lb, 'fb%d_' % p, 'h%d_' % p, I, lines)
+        for c in range(ncb):
+            lines.append(I + 'h0p[%d] = make_float2(h0_%d, h1_%d);' % (c, c, c))
+    lines.append(I + '#pragma unroll 1')
+    lines.append(I + 'for (int m = 0; m < npp; ++m) {')
+    lines.append(J + 'const float4* __restrict__ q = rp + m * %d;' % rec_stride2(la, lb))
+    lines.append(J + '{')
+    gen_prim_body_dual(la, lb, diag, J + I, lines, packed=True)
+    lines.append(J + '}')
+    lines.append(I + '}')
+    lines.append(I + '#pragma unroll')
+    lines.append(I + 'for (int w = 0; w < 2; ++w) {')
+    for p in range(2):
+        h = 'xy'[p]
+        lines.append(I + '{')
+        if diag:
+            for c in range(ncb):
+                lines.append(J + 'Xa[(w * PTS + %d) * %d + %d] += Yp[w][%d].%s;'
+                             % (p, nca, c, c, h))
+        else:
+            for c in range(ncb):
+                lines.append(J + 'const float Y%d = Yp[w][%d].%s;' % (c, c, h))
+            gen_transform_out(lb, 'Y', 'gy', J, lines)
+            lines.append(J + 'if (ok[%d]) {' % p)
+            for nu in range(nb):
+                lines.append('#if WB_COSX_GB_RED')
+                lines.append(J + '    gb_add(Gp[w * PTS + %d] + (long long)(gb0 + %d) * ld, gy%d);'
+                             % (p, nu, nu))
+                lines.append('#else')
+                lines.append(J + '    Gp[w * PTS + %d][(long long)(gb0 + %d) * ld] = gbo[w][%d][%d] + gy%d;'
+                             % (p, nu, p, nu, nu))
+                lines.append('#endif')
+            lines.append(J + '}')
+            for c in range(nca):
+                lines.append(J + 'Xa[(w * PTS + %d) * %d + %d] = Xp[w][%d].%s;'
+                             % (p, nca, c, c, h))
+        lines.append(I + '}')
+    lines.append(I + '}')
+    lines.append('}')
+    lines.append('};')
+    return '\n'.join(lines)
+
+
 def source():
     out = ['// Generated by csrc/gen_cosx.py -- do not edit by hand.',
            '// One straight-line task body per shell-pair class (la >= lb),',
@@ -845,6 +1031,14 @@ def source():
         out.append('')
         if la == lb:
             out.append(gen_class_dual(la, lb, True))
+            out.append('')
+        if la + lb <= 3:
+            out.append('#if WB_COSX_F32X2')
+            out.append(gen_class_dual_packed(la, lb, False))
+            if la == lb:
+                out.append('')
+                out.append(gen_class_dual_packed(la, lb, True))
+            out.append('#endif')
             out.append('')
     # E strides table for the host
     out.append('#define WB_E_STRIDES {%s}' % ', '.join(

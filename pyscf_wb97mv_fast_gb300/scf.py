@@ -186,22 +186,38 @@ class DeviceGrid:
 
 DEFAULT_FINAL = dict(xc=2, sgx=1, nlc=1)
 DEFAULT_COARSE = dict(xc=1, sgx=0)
+# the reference's per-stage grid table (staging/schedule.py:91-96): S0, S1,
+# S2 levels of the XC, SGX and NLC grids, None = VV10 off
+REFERENCE_STAGE_LEVELS = dict(xc=(1, 3, 3), sgx=(1, 1, 2), nlc=(None, 1, 3))
 
 
 class DeviceRKS:
     """RKS SCF on one GPU for a Molecule (see the module docstring).
 
     ``levels`` are the final grid levels (xc, sgx, nlc; nlc None turns VV10
-    off) and ``coarse`` those of stage S0 (xc, sgx; no VV10), as in the
-    reference's staging table (schedule.py:91-96).  ``k_tile_tol`` is the
-    COSX screen, ``j_tol`` the Hartree-potential screen.
+    off) and ``coarse`` those of stage S0 (xc, sgx; no VV10); S1 and S2 use
+    the final grids.  ``stage_levels`` (kind -> (S0, S1, S2) levels, e.g.
+    REFERENCE_STAGE_LEVELS, the reference's table in schedule.py:91-96)
+    sets every stage's grids instead; the final grids are S2's.
+    ``k_tile_tol`` is the COSX screen, ``j_tol`` the Hartree-potential
+    screen.
     """
 
     def __init__(self, mol, functional=None, levels=None, coarse=None,
-                 k_tile_tol=1e-11, j_tol=1e-14, device=None, verbose=False):
+                 k_tile_tol=1e-11, j_tol=1e-14, device=None, verbose=False,
+                 stage_levels=None):
         torch = _torch()
         self.mol = as_molecule(mol)
         self.functional = functional or RshLdaVv10()
+        self.stage_levels = None
+        if stage_levels is not None:
+            if levels is not None or coarse is not None:
+                raise ValueError('give stage_levels or levels/coarse, not both')
+            self.stage_levels = {k: tuple(stage_levels[k]) for k in ('xc', 'sgx', 'nlc')}
+            if any(len(v) != 3 for v in self.stage_levels.values()):
+                raise ValueError('stage_levels: three levels (S0, S1, S2) per grid')
+            levels = {k: v[2] for k, v in self.stage_levels.items()}
+            coarse = {k: self.stage_levels[k][0] for k in ('xc', 'sgx')}
         self.levels = dict(DEFAULT_FINAL, **(levels or {}))
         self.coarse = dict(DEFAULT_COARSE, **(coarse or {}))
         self.k_tile_tol = float(k_tile_tol)
@@ -442,6 +458,10 @@ class DeviceRKS:
         return out
 
     def _stage_grids(self, stage):
+        if self.stage_levels is not None:
+            lv = {k: v[stage] for k, v in self.stage_levels.items()}
+            return dict(xc=self.grid('xc', lv['xc']), sgx=self.grid('sgx', lv['sgx']),
+                        nlc=None if lv['nlc'] is None else self.grid('nlc', lv['nlc']))
         if stage == 0:
             return dict(xc=self.grid('xc', self.coarse['xc']),
                         sgx=self.grid('sgx', self.coarse['sgx']), nlc=None)

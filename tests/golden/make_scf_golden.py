@@ -5,7 +5,8 @@ the bench's SCF leg.
 
 Run from the repository root (each case is merged into the file):
     python tests/golden/make_scf_golden.py [case ...]
-Cases: water_dimer_svp_xc1_sgx0_nlc0, water8_svp_xc2_sgx1_nlc1.
+Cases: water_dimer_svp_xc1_sgx0_nlc0, water8_svp_xc2_sgx1_nlc1,
+ethane_tzvp_xc1_sgx0_nlc0 (f shells).
 """
 import json
 import os
@@ -18,12 +19,13 @@ sys.path.insert(0, ROOT)
 
 from pyscf_wb97mv_fast_gb300.basis import Molecule  # noqa: E402
 from pyscf_wb97mv_fast_gb300.grids import build_grids  # noqa: E402
-from pyscf_wb97mv_fast_gb300.systems import water_cluster, water_dimer  # noqa: E402
+from pyscf_wb97mv_fast_gb300.systems import alkane, water_cluster, water_dimer  # noqa: E402
 
 CASES = {
     'water_dimer_svp_xc1_sgx0_nlc0': (lambda: water_dimer(), 'synthetic-svp', 1, 0, 0),
     'water8_svp_xc2_sgx1_nlc1': (lambda: water_cluster(8, box=7.0, seed=8),
                                  'synthetic-svp', 2, 1, 1),
+    'ethane_tzvp_xc1_sgx0_nlc0': (lambda: alkane(2), 'synthetic-tzvp', 1, 0, 0),
 }
 
 

@@ -8,8 +8,8 @@ functional, grids and algorithm, FP64 and unscreened on the host.
 * the per-cycle pieces match the oracle's Fock build on a fixed density.
 
 The oracle energies come from tests/golden/scf_energies.json (written by
-tests/golden/make_scf_golden.py, which runs oracle/scf.py); the small case
-also runs the oracle live.
+tests/golden/make_scf_golden.py, which runs oracle/scf.py): the water dimer
+and config 1's eight waters in SVP, and ethane in TZVP (f shells).
 """
 import json
 import os
@@ -103,3 +103,40 @@ def test_mixed_scf_water8_config1_reaches_the_oracle_energy():
     r = rks.kernel(precision='mixed', reference_energy=g['e_tot'])
     assert r['converged']
     assert abs(r['error_vs_reference']) < 1e-8, r['error_vs_reference']
+
+
+def test_fp64_and_mixed_scf_with_f_shells_reach_the_oracle_energy():
+    """Ethane in the synthetic def2-TZVP structure (98 AOs, f shells on C):
+    every (l_A, l_B) class up to (3, 3) in K, the one-electron integrals
+    and the Hartree potential up to L = 6."""
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.scf import DeviceRKS
+    from pyscf_wb97mv_fast_gb300.systems import alkane
+    e_ref = _golden()['ethane_tzvp_xc1_sgx0_nlc0']['e_tot']
+    mol = Molecule.build(alkane(2), 'synthetic-tzvp')
+    rks = DeviceRKS(mol, levels=dict(xc=1, sgx=0, nlc=0), coarse=dict(xc=0, sgx=0))
+    r64 = rks.kernel(precision='fp64', reference_energy=e_ref)
+    assert r64['converged']
+    assert abs(r64['error_vs_reference']) < 1e-9, r64['error_vs_reference']
+    rmx = rks.kernel(precision='mixed', reference_energy=e_ref)
+    assert rmx['converged']
+    assert abs(rmx['error_vs_reference']) < 1e-8, rmx['error_vs_reference']
+
+
+def test_reference_stage_table_switches_grids():
+    """stage_levels (the reference's per-stage XC / SGX / NLC table): S0
+    without VV10 on its own grids, S2 on the final ones; the mixed form
+    still reaches the plain FP64 form's energy on the final grids."""
+    from pyscf_wb97mv_fast_gb300.scf import DeviceRKS
+    mol = dimer('synthetic-svp')
+    table = dict(xc=(0, 1, 1), sgx=(0, 0, 1), nlc=(None, 0, 1))
+    rks = DeviceRKS(mol, stage_levels=table)
+    assert rks.levels == dict(xc=1, sgx=1, nlc=1)
+    g0, g1, g2 = (rks._stage_grids(s) for s in (0, 1, 2))
+    assert g0['nlc'] is None and g1['nlc'] is not None
+    assert g1['sgx'] is g0['sgx'] and g2['sgx'] is not g1['sgx']
+    r64 = rks.kernel(precision='fp64')
+    rmx = rks.kernel(precision='mixed', reference_energy=r64['e_tot'])
+    assert r64['converged'] and rmx['converged']
+    assert [s['stage'] for s in rmx['stages']][:2] == [0, 1]
+    assert abs(rmx['error_vs_reference']) < 1e-8, rmx['error_vs_reference']
