@@ -312,13 +312,38 @@ def vv10_timing(mol, dm, eng, torch, peak, calls=2):
     m = int(xyz.shape[0])
     pairs = float(m) * m
     tflops = 27.0 * pairs / t / 1e12
-    return {'points': m, 'grid': 'level 1 (%d points, rho >= %g kept)' % (n, THRESH),
-            'ms_per_call': t * 1e3, 'pairs_per_s': pairs / t,
-            'achieved_tflops': tflops, 'peak_tflops': peak,
-            'frac': tflops / peak if peak else None,
-            'work': '27 operations per pair (24 flops + 3 reciprocals), '
-                    'every pair kept (tile_tol 0)',
-            'parameters': 'b = 6.0, C = 0.01 (the wB97M-V VV10 set)'}
+    out = {'points': m, 'grid': 'level 1 (%d points, rho >= %g kept)' % (n, THRESH),
+           'ms_per_call': t * 1e3, 'pairs_per_s': pairs / t,
+           'achieved_tflops': tflops, 'peak_tflops': peak,
+           'frac': tflops / peak if peak else None,
+           'work': '27 operations per pair (24 flops + 3 reciprocals), '
+                   'every pair kept (tile_tol 0)',
+           'parameters': 'b = 6.0, C = 0.01 (the wB97M-V VV10 set)'}
+    # the distance-pruned sum (the reference's tile-pair bounds,
+    # gpu/vv10.py:21-31): time, kept pairs and the change of the VV10
+    # energy's pair term, E_F = 1/2 sum_i q_i F_i (F = -1.5 x the raw sum)
+    F0 = kern.kernel_sum(xyz, q, W0, kappa)[0]
+    e_full = 0.5 * float((q.to(torch.float64) * F0).sum())
+    pruned = {}
+    for tol in (1e-12, 1e-10, 1e-8):
+        kp = Vv10Kernel(tol)
+        kp.kernel_sum(xyz, q, W0, kappa)
+        tp = []
+        for _ in range(calls):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            Fp = kp.kernel_sum(xyz, q, W0, kappa)[0]
+            e1.record()
+            e1.synchronize()
+            tp.append(e0.elapsed_time(e1) * 1e-3)
+        kept, total = kp.last_pairs_kept
+        e_p = 0.5 * float((q.to(torch.float64) * Fp).sum())
+        pruned['%g' % tol] = {'ms_per_call': min(tp) * 1e3,
+                              'pairs_kept_fraction': kept / total if total else None,
+                              'dE_pair_term_Ha': e_p - e_full}
+    out['distance_pruned'] = pruned
+    return out
 
 
 def fp64_form_timing(eng, coords_d, w_d, qd_d, K_mixed, t_mixed, dm, torch,
@@ -1004,7 +1029,7 @@ def config_dict(mol, g, args):
                             else 'multi-omega (shared AO values and F)',
             'l2': 'inputs larger than L2 (X alone is %.1f GB)'
                   % (8.0 * mol.nao * g.size / 1e9),
-            'gemm': args.gemm, 'parallelism': 'replicas'}
+            'gemm': args.gemm, 'f_engine': args.f_engine, 'parallelism': 'replicas'}
 
 
 def main():
@@ -1014,6 +1039,9 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--gemm', default='ozaki', choices=['ozaki', 'native', 'emulated'])
+    ap.add_argument('--f-engine', default='tc', choices=['tc', 'library'],
+                    help="the Ozaki F product: this library's tcgen05 kernel or "
+                         "cuBLAS level GEMMs (bitwise the same F)")
     ap.add_argument('--small', action='store_true',
                     help='8 waters / grid level 1 (profiling captures)')
     ap.add_argument('--grid-level', type=int, default=None,
@@ -1063,7 +1091,8 @@ def main():
 
     from pyscf_wb97mv_fast_gb300 import build as _build
     _build.build()
-    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine, round32
+    from pyscf_wb97mv_fast_gb300.cosx import CosxEngine, round32, set_f_engine
+    set_f_engine(args.f_engine)
 
     mol, g, dm = workload(args.small, args.grid_level)
     eng = CosxEngine(mol, device=local)

@@ -307,7 +307,7 @@ int wb_cosx_g_multi(wb_cosx* h, const double* coords, const double* weights,
 /* The two FP64-accurate GEMMs of the K build on the bf16 tensor cores
  * (Ozaki split, WB_K_GEMM_OZAKI_BF16), callable alone:
  *   wb_cosx_ozaki_f: f_out (nao, ld) FP32 = fl32(X QD), x (nao, ld) FP64
- *     AO-major, qd (nao, nao) row-major; needs 5 nao < 4096.
+ *     AO-major, qd (nao, nao) row-major; needs 7 nao < 16384.
  *     Replaces F = (X @ proj_dm).astype(float32) (gpu/sgx_k.py:722).
  *   wb_cosx_ozaki_k: k_out (nao, nao) row-major (+)= X^T (w o G) over npts
  *     points, g (nao, ld) FP32.  Replaces K += X.T @ (w64 * G)
@@ -321,6 +321,18 @@ int wb_cosx_ozaki_k(wb_cosx* h, const double* x, const float* g,
                     const double* weights, int64_t npts, int accumulate,
                     double* k_out, void* workspace, size_t workspace_bytes,
                     void* stream);
+
+/* Engine of the F product (process-wide, every F of the K builds and of
+ * wb_cosx_ozaki_f): WB_OZAKI_ENGINE_TC (the default) is this library's
+ * tensor-core kernel (TMA tile loads, tcgen05 MMAs into TMEM, the exact
+ * level combination fused into its epilogue); WB_OZAKI_ENGINE_LIBRARY runs
+ * one cuBLAS bf16 GEMM per level.  Both give bitwise the same F.  Replaces
+ * no reference call (the reference's F GEMM is one CuPy FP64 matmul,
+ * gpu/sgx_k.py:722); returns WB_OK or WB_ERR_INVALID_ARGUMENT. */
+#define WB_OZAKI_ENGINE_LIBRARY 0
+#define WB_OZAKI_ENGINE_TC 1
+int wb_ozaki_set_f_engine(int engine);
+int wb_ozaki_get_f_engine(void);
 
 /* AO values X (nao, ldp) FP64 AO-major at npts points (FP64 arithmetic).
  * Replaces AoEvaluator.eval(deriv=0) with dtype FP64 (gpu/ao_eval.py:186-329). */

@@ -46,6 +46,7 @@ EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_vv10_kernel_sum',
             'wb_becke_partition', 'wb_fp32_fma_probe', 'wb_fp32x2_fma_probe',
             'wb_ozaki_workspace_bytes', 'wb_cosx_ozaki_f', 'wb_cosx_ozaki_k',
+            'wb_ozaki_set_f_engine', 'wb_ozaki_get_f_engine',
             'wb_vv10_kernel_sum_noalloc', 'wb_vv10_kernel_sum_batch',
             'wb_cosx_fp64_workspace_bytes', 'wb_cosx_get_k_fp64',
             'wb_cosx_set_class_variant', 'wb_cosx_get_class_variant',
@@ -165,6 +166,8 @@ def _declare(lib):
         'wb_fp32x2_fma_probe': (_INT, [_I64, _P, _I64, _P, ctypes.POINTER(_D)]),
         'wb_ozaki_workspace_bytes': (ctypes.c_size_t, [_INT, _I64]),
         'wb_cosx_ozaki_f': (_INT, [_P, _P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
+        'wb_ozaki_set_f_engine': (_INT, [_INT]),
+        'wb_ozaki_get_f_engine': (_INT, []),
         'wb_cosx_ozaki_k': (_INT, [_P, _P, _P, _P, _I64, _INT, _P, _P,
                                    ctypes.c_size_t, _P]),
         'wb_cosx_fp64_workspace_bytes': (ctypes.c_size_t, [_P, _I64]),

@@ -27,7 +27,7 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 SOURCES = ['cosx_kernels_spd.cu', 'cosx_kernels_f.cu', 'cosx_batch_spd.cu',
            'cosx_batch_f.cu', 'cosx_fp64.cu', 'cosx_fp64_f.cu', 'cosx_grad64.cu',
            'aux_kernels.cu', 'scf_kernels.cu',
-           'vv10.cu', 'ozaki.cu', 'capi.cu', 'host_pairs.cpp']
+           'vv10.cu', 'ozaki.cu', 'ozaki_tc.cu', 'capi.cu', 'host_pairs.cpp']
 
 
 def cuda_home():

@@ -55,6 +55,27 @@ def device_out(t, name, dtype, device, shape):
     return t
 
 
+F_ENGINES = {'library': 0, 'tc': 1}
+
+
+def set_f_engine(name):
+    """Engine of the F product of the Ozaki split (process-wide): 'tc' (the
+    default, this library's tcgen05 tensor-core kernel with the level
+    combination fused) or 'library' (cuBLAS bf16 level GEMMs); both give
+    bitwise the same F.  Returns the previous engine's name."""
+    if name not in F_ENGINES:
+        raise ValueError('F engine must be one of %s' % sorted(F_ENGINES))
+    prev = get_f_engine()
+    _native.check(_native.lib().wb_ozaki_set_f_engine(F_ENGINES[name]),
+                  'wb_ozaki_set_f_engine')
+    return prev
+
+
+def get_f_engine():
+    code = int(_native.lib().wb_ozaki_get_f_engine())
+    return {v: k for k, v in F_ENGINES.items()}[code]
+
+
 def as_molecule(mol):
     """A Molecule from a Molecule or a PySCF Mole."""
     if isinstance(mol, Molecule):

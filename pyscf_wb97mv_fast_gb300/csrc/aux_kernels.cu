@@ -579,21 +579,16 @@ __device__ __forceinline__ void ao_shell(const AoArgs& A, int sh, int64_t g,
                                          double dx, double dy, double dz,
                                          double r2, const double* etab) {
     constexpr int NC = (L + 1) * (L + 2) / 2, NS = 2 * L + 1;
-    double mono[NC];
-    {
-        int c = 0;
-#pragma unroll
-        for (int lx = L; lx >= 0; --lx)
-#pragma unroll
-            for (int ly = L - lx; ly >= 0; --ly) {
-                mono[c++] = ipow(dx, lx) * ipow(dy, ly) * ipow(dz, L - lx - ly);
-            }
-    }
     const double* c2s = c2s_ptr<L>();
     const int np = A.sh_np[sh], nc = A.sh_nc[sh];
     const double* ex = A.exps + A.sh_eoff[sh];
     const double* co = A.coeffs + A.sh_coff[sh];
     const int ao0 = A.sh_ao0[sh];
+    // the spherical angular factors, formed on the first contraction with a
+    // nonzero radial part: at most points of a cluster every primitive of a
+    // shell is below exp(-70), and the FP64 angular work is skipped there
+    double ang[NS];
+    bool have_ang = false;
     for (int ci = 0; ci < nc; ++ci) {
         double rad = 0.0;
         for (int k = 0; k < np; ++k) {
@@ -602,13 +597,31 @@ __device__ __forceinline__ void ao_shell(const AoArgs& A, int sh, int64_t g,
             const double a = ex[k] * r2;
             if (a < 70.0) rad += co[k * nc + ci] * exp_neg(a, etab);
         }
+        if (rad == 0.0) {
 #pragma unroll
-        for (int m = 0; m < NS; ++m) {
-            double v = 0.0;
-#pragma unroll
-            for (int c = 0; c < NC; ++c) v += c2s[c * NS + m] * mono[c];
-            A.X[(int64_t)(ao0 + ci * NS + m) * A.ld + g] = rad * v;
+            for (int m = 0; m < NS; ++m) A.X[(int64_t)(ao0 + ci * NS + m) * A.ld + g] = 0.0;
+            continue;
         }
+        if (!have_ang) {
+            double mono[NC];
+            int c = 0;
+#pragma unroll
+            for (int lx = L; lx >= 0; --lx)
+#pragma unroll
+                for (int ly = L - lx; ly >= 0; --ly)
+                    mono[c++] = ipow(dx, lx) * ipow(dy, ly) * ipow(dz, L - lx - ly);
+#pragma unroll
+            for (int m = 0; m < NS; ++m) {
+                double v = 0.0;
+#pragma unroll
+                for (int q = 0; q < NC; ++q) v += c2s[q * NS + m] * mono[q];
+                ang[m] = v;
+            }
+            have_ang = true;
+        }
+#pragma unroll
+        for (int m = 0; m < NS; ++m)
+            A.X[(int64_t)(ao0 + ci * NS + m) * A.ld + g] = rad * ang[m];
     }
 }
 
@@ -666,6 +679,17 @@ __device__ __forceinline__ void ao_shell_d1(const AoArgs& A, int sh, int64_t g,
             const double e = co[k * nc + ci] * exp_neg(a, etab);
             rad0 += e;
             rad1 += -2.0 * ex[k] * e;
+        }
+        if (rad0 == 0.0 && rad1 == 0.0) {     // every primitive skipped
+#pragma unroll
+            for (int m = 0; m < NS; ++m) {
+                const int64_t o = (int64_t)(ao0 + ci * NS + m) * A.ld + g;
+                A.X[o] = 0.0;
+                A.X[plane + o] = 0.0;
+                A.X[2 * plane + o] = 0.0;
+                A.X[3 * plane + o] = 0.0;
+            }
+            continue;
         }
         double cv[NC], cgx[NC], cgy[NC], cgz[NC];
         {

@@ -1256,11 +1256,12 @@ int wb_cosx_get_k_multi(wb_cosx* h, const double* coords,
         launches += 1;
         if ((st = phase_to(1)) != WB_OK) return st;
         if (oz_f) {
-            const int r = wb::ozaki_f_gemm(h->cublas, X, qd, nao, ldt, F32,
-                                           at<void>(workspace, L.oz), s);
+            const int r = wb::ozaki_f_gemm(
+                h->cublas, X, qd, nao, ldt, F32, at<void>(workspace, L.oz), s,
+                at<unsigned long long>(workspace, L.counters) + 3 * wb::NCLASS);
             if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
                                "ozaki F GEMM failed, code " + std::to_string(r));
-            launches += 4 + wb::kOzSlices;
+            launches += wb::ozaki_f_launches();
         } else {
             // F(g, mu) = sum_l X(g, l) QD(l, mu); QD row-major = col-major QD^T
             WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)ldt,
@@ -1752,11 +1753,12 @@ int wb_cosx_batch_run(wb_cosx_batch* b, const double* const* qd,
         const double* X = at<double>(ws, L.X);
         float* F32 = at<float>(ws, L.F32);
         if (b->gemm == WB_K_GEMM_OZAKI_BF16 && wb::ozaki_f_supported(nao)) {
-            const int r = wb::ozaki_f_gemm(h->cublas, X, qd[m], nao, ld, F32,
-                                           b->scratch, s);
+            const int r = wb::ozaki_f_gemm(
+                h->cublas, X, qd[m], nao, ld, F32, b->scratch, s,
+                at<unsigned long long>(ws, L.counters) + 3 * wb::NCLASS);
             if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
                                "ozaki F GEMM failed, code " + std::to_string(r));
-            launches += 4 + wb::kOzSlices;
+            launches += wb::ozaki_f_launches();
         } else {
             double* F64 = static_cast<double*>(b->scratch);
             WB_CUBLAS(cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_T, (int)ld, nao, nao,
@@ -2249,6 +2251,19 @@ int wb_cosx_ozaki_f(wb_cosx* h, const double* x, const double* qd,
     if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
                        "ozaki F GEMM failed, code " + std::to_string(r));
     return WB_OK;
+}
+
+int wb_ozaki_set_f_engine(int engine) {
+    if (engine != WB_OZAKI_ENGINE_LIBRARY && engine != WB_OZAKI_ENGINE_TC)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_ozaki_set_f_engine: unknown engine");
+    wb::ozaki_set_f_engine(engine == WB_OZAKI_ENGINE_TC ? wb::kOzEngineTc
+                                                        : wb::kOzEngineLibrary);
+    return WB_OK;
+}
+
+int wb_ozaki_get_f_engine(void) {
+    return wb::ozaki_get_f_engine() == wb::kOzEngineTc ? WB_OZAKI_ENGINE_TC
+                                                       : WB_OZAKI_ENGINE_LIBRARY;
 }
 
 int wb_cosx_ozaki_k(wb_cosx* h, const double* x, const float* g,

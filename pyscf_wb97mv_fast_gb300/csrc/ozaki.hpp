@@ -22,9 +22,27 @@ size_t ozaki_k_bytes(int nao, int64_t ld, int nrhs = 1);
 
 // F (nao, ld) FP32 AO-major = fl32(X QD); X (nao, ld) FP64 AO-major, QD
 // (nao, nao) row-major FP64.  Returns 0, a cudaError_t, or 1000 + cuBLAS
-// status.
+// status.  status (optional, device): bit 0 is set when a wait of the
+// tensor-core kernel gave up (the affected F entries are NaN).
 int ozaki_f_gemm(cublasHandle_t hb, const double* X, const double* QD,
-                 int nao, int64_t ld, float* F, void* ws, cudaStream_t s);
+                 int nao, int64_t ld, float* F, void* ws, cudaStream_t s,
+                 unsigned long long* status = nullptr);
+
+// the two engines of the F product (bitwise the same F): this library's
+// tcgen05 kernel (the default) and cuBLAS level GEMMs
+constexpr int kOzEngineLibrary = 0;
+constexpr int kOzEngineTc = 1;
+void ozaki_set_f_engine(int engine);
+int ozaki_get_f_engine();
+// this library's kernel launches of one F product under the current engine
+inline int ozaki_f_launches() { return ozaki_get_f_engine() == kOzEngineTc ? 4 : 4 + kOzSlices; }
+int ozaki_f_gemm_cublas(cublasHandle_t hb, const double* X, const double* QD,
+                        int nao, int64_t ld, float* F, void* ws, cudaStream_t s);
+int ozaki_f_gemm_tc(const double* X, const double* QD, int nao, int64_t ld, float* F,
+                    void* ws, cudaStream_t s, unsigned long long* status);
+size_t ozaki_f_tc_bytes(int nao, int64_t ld);
+// exponent of max_l |X(l, g)| per point g (shared by both engines)
+void f_rowmax(const double* X, int nao, int64_t ld, int* erow, cudaStream_t s);
 
 // K (nao, nao) row-major (+)= X^T (w o G) over the npts valid points.
 // x_sliced: ws already holds the slices of this X (an earlier call on the
