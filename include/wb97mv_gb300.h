@@ -322,6 +322,21 @@ int wb_cosx_ozaki_k(wb_cosx* h, const double* x, const float* g,
                     double* k_out, void* workspace, size_t workspace_bytes,
                     void* stream);
 
+/* The same two products with FP64 operands on the output / G side, for
+ * the SCF's FP64 tail (the reference's FP64 numint GEMMs, gpu/xc.py:130-201
+ * and gpu/vv10.py:288-297, run there in FP64):
+ *   wb_cosx_ozaki_f64: f_out (nao, ld) FP64 = X QD, the combined 42-bit
+ *     level sums rounded once to FP64;
+ *   wb_cosx_ozaki_k64: k_out (+)= X^T (w o G) with g (nao, ld) FP64.
+ * Same workspace and limits as wb_cosx_ozaki_f / wb_cosx_ozaki_k. */
+int wb_cosx_ozaki_f64(wb_cosx* h, const double* x, const double* qd,
+                      int64_t ld, double* f_out, void* workspace,
+                      size_t workspace_bytes, void* stream);
+int wb_cosx_ozaki_k64(wb_cosx* h, const double* x, const double* g,
+                      const double* weights, int64_t npts, int accumulate,
+                      double* k_out, void* workspace, size_t workspace_bytes,
+                      void* stream);
+
 /* Engine of the F product (process-wide, every F of the K builds and of
  * wb_cosx_ozaki_f): WB_OZAKI_ENGINE_TC (the default) is this library's
  * tensor-core kernel (TMA tile loads, tcgen05 MMAs into TMEM, the exact

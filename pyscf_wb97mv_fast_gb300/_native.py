@@ -47,6 +47,7 @@ EXPORTED = ('wb_cosx_create', 'wb_cosx_destroy', 'wb_cosx_get_info',
             'wb_becke_partition', 'wb_fp32_fma_probe', 'wb_fp32x2_fma_probe',
             'wb_ozaki_workspace_bytes', 'wb_cosx_ozaki_f', 'wb_cosx_ozaki_k',
             'wb_ozaki_set_f_engine', 'wb_ozaki_get_f_engine',
+            'wb_cosx_ozaki_f64', 'wb_cosx_ozaki_k64',
             'wb_vv10_kernel_sum_noalloc', 'wb_vv10_kernel_sum_batch',
             'wb_cosx_fp64_workspace_bytes', 'wb_cosx_get_k_fp64',
             'wb_cosx_set_class_variant', 'wb_cosx_get_class_variant',
@@ -167,9 +168,12 @@ def _declare(lib):
         'wb_ozaki_workspace_bytes': (ctypes.c_size_t, [_INT, _I64]),
         'wb_cosx_ozaki_f': (_INT, [_P, _P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
         'wb_ozaki_set_f_engine': (_INT, [_INT]),
+        'wb_cosx_ozaki_f64': (_INT, [_P, _P, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
         'wb_ozaki_get_f_engine': (_INT, []),
         'wb_cosx_ozaki_k': (_INT, [_P, _P, _P, _P, _I64, _INT, _P, _P,
                                    ctypes.c_size_t, _P]),
+        'wb_cosx_ozaki_k64': (_INT, [_P, _P, _P, _P, _I64, _INT, _P, _P,
+                                     ctypes.c_size_t, _P]),
         'wb_cosx_fp64_workspace_bytes': (ctypes.c_size_t, [_P, _I64]),
         'wb_cosx_set_class_variant': (_INT, [_P, _INT, _INT, _INT]),
         'wb_cosx_k_grad_workspace_bytes': (ctypes.c_size_t, [_P, _I64, _INT]),

@@ -431,27 +431,33 @@ class CosxEngine:
             self.last_stats = st.as_dict()
         return out
 
-    def ozaki_f(self, X, qd):
-        """F (nao, ld) FP32 = fl32(X QD) through the bf16 Ozaki split."""
+    def ozaki_f(self, X, qd, fp64=False):
+        """F (nao, ld) = X^T-side product QD^T X through the bf16 Ozaki split:
+        FP32 (fl32 of the product) or, with fp64, FP64 (the 42-bit level
+        sums rounded once)."""
         torch = _torch()
         X = device_arg(X, 'X', torch.float64, self.device, (self.nao, None))
         qd = self._dm_arg(qd)
         ld = int(X.shape[1])
         nbytes = int(_native.lib().wb_ozaki_workspace_bytes(self.nao, ld))
         ws = self.workspace(nbytes)
-        out = torch.empty((self.nao, ld), dtype=torch.float32, device=self.device)
-        _native.check(_native.lib().wb_cosx_ozaki_f(
+        dt = torch.float64 if fp64 else torch.float32
+        out = torch.empty((self.nao, ld), dtype=dt, device=self.device)
+        fn = 'wb_cosx_ozaki_f64' if fp64 else 'wb_cosx_ozaki_f'
+        _native.check(getattr(_native.lib(), fn)(
             self._h, _native.ptr(X), _native.ptr(qd), ld,
-            _native.ptr(out), _native.ptr(ws), nbytes, self._stream()),
-            'wb_cosx_ozaki_f')
+            _native.ptr(out), _native.ptr(ws), nbytes, self._stream()), fn)
         return out
 
     def ozaki_k(self, X, G, weights, out=None, accumulate=False):
-        """K (nao, nao) FP64 = X^T (w o G) through the bf16 Ozaki split."""
+        """K (nao, nao) FP64 = X^T (w o G) through the bf16 Ozaki split; G
+        FP32, or FP64 (w o G then formed from the FP64 values)."""
         torch = _torch()
         X = device_arg(X, 'X', torch.float64, self.device, (self.nao, None))
         ld = int(X.shape[1])
-        G = device_arg(G, 'G', torch.float32, self.device, (self.nao, ld))
+        g64 = getattr(G, 'dtype', None) == torch.float64
+        G = device_arg(G, 'G', torch.float64 if g64 else torch.float32, self.device,
+                       (self.nao, ld))
         weights = device_arg(weights, 'weights', torch.float64, self.device, (None,))
         npts = int(weights.shape[0])
         if npts > ld:
@@ -462,10 +468,11 @@ class CosxEngine:
             out = torch.zeros((self.nao, self.nao), dtype=torch.float64,
                               device=self.device)
         device_out(out, 'out', torch.float64, self.device, (self.nao, self.nao))
-        _native.check(_native.lib().wb_cosx_ozaki_k(
+        fn = 'wb_cosx_ozaki_k64' if g64 else 'wb_cosx_ozaki_k'
+        _native.check(getattr(_native.lib(), fn)(
             self._h, _native.ptr(X), _native.ptr(G), _native.ptr(weights), npts,
             1 if accumulate else 0, _native.ptr(out), _native.ptr(ws), nbytes,
-            self._stream()), 'wb_cosx_ozaki_k')
+            self._stream()), fn)
         return out
 
     def ao_eval(self, coords_rel, out=None):

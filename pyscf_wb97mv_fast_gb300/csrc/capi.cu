@@ -2253,6 +2253,46 @@ int wb_cosx_ozaki_f(wb_cosx* h, const double* x, const double* qd,
     return WB_OK;
 }
 
+int wb_cosx_ozaki_f64(wb_cosx* h, const double* x, const double* qd,
+                      int64_t ld, double* f_out, void* workspace,
+                      size_t workspace_bytes, void* stream) {
+    if (!h || !x || !qd || !f_out || ld <= 0 || ld % 32)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_ozaki_f64: bad arguments");
+    const int nao = h->hp.nao;
+    if (!wb::ozaki_f_supported(nao))
+        return fail(WB_ERR_UNSUPPORTED, "wb_cosx_ozaki_f64: nao too large for one "
+                                        "exact FP32 level sum");
+    if (!workspace || workspace_bytes < wb::ozaki_f_bytes(nao, ld))
+        return fail(WB_ERR_WORKSPACE, "wb_cosx_ozaki_f64: workspace too small");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    WB_CUBLAS(cublasSetStream(h->cublas, s));
+    WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+    const int r = wb::ozaki_f_gemm64(h->cublas, x, qd, nao, ld, f_out, workspace, s);
+    if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
+                       "ozaki F64 GEMM failed, code " + std::to_string(r));
+    return WB_OK;
+}
+
+int wb_cosx_ozaki_k64(wb_cosx* h, const double* x, const double* g,
+                      const double* weights, int64_t npts, int accumulate,
+                      double* k_out, void* workspace, size_t workspace_bytes,
+                      void* stream) {
+    if (!h || !x || !g || !weights || !k_out || npts <= 0)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_ozaki_k64: bad arguments");
+    const int nao = h->hp.nao;
+    const int64_t ld = round32(npts);
+    if (!workspace || workspace_bytes < wb::ozaki_k_bytes(nao, ld))
+        return fail(WB_ERR_WORKSPACE, "wb_cosx_ozaki_k64: workspace too small");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    WB_CUBLAS(cublasSetStream(h->cublas, s));
+    WB_CUBLAS(cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+    const int r = wb::ozaki_k_gemm64(h->cublas, x, g, weights, nao, ld, npts,
+                                     accumulate, k_out, workspace, s);
+    if (r) return fail(r >= 1000 ? WB_ERR_CUBLAS : WB_ERR_CUDA,
+                       "ozaki K64 GEMM failed, code " + std::to_string(r));
+    return WB_OK;
+}
+
 int wb_ozaki_set_f_engine(int engine) {
     if (engine != WB_OZAKI_ENGINE_LIBRARY && engine != WB_OZAKI_ENGINE_TC)
         return fail(WB_ERR_INVALID_ARGUMENT, "wb_ozaki_set_f_engine: unknown engine");

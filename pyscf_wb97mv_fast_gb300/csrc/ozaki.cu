@@ -128,11 +128,11 @@ __global__ void f_slice_qd_kernel(const double* __restrict__ QD, int nao,
 
 // x y = 2^(e+f-2W+2) sum_l C_l 2^(B (2S-2-l))
 //     = 2^(e+f-2W+2+B(S-1)) * [sum_l C_l 2^(B (S-1-l))]
-template<int S>
+template<int S, typename T>
 __global__ void f_combine_kernel(const float* __restrict__ C, int nao,
                                  int64_t ld, const int* __restrict__ erow,
                                  const int* __restrict__ ecol,
-                                 float* __restrict__ F) {
+                                 T* __restrict__ F) {
     const int mu = blockIdx.y;
     const int64_t g = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
     if (g >= ld) return;                    // ld is a multiple of 4
@@ -149,12 +149,16 @@ __global__ void f_combine_kernel(const float* __restrict__ C, int nao,
     for (int l = 0; l < S; ++l) {
         v[0][l] = c[l].x; v[1][l] = c[l].y; v[2][l] = c[l].z; v[3][l] = c[l].w;
     }
-    float4 out;
-    out.x = scaled_ll_to_float(combine_levels<S>(v[0]), er.x + base);
-    out.y = scaled_ll_to_float(combine_levels<S>(v[1]), er.y + base);
-    out.z = scaled_ll_to_float(combine_levels<S>(v[2]), er.z + base);
-    out.w = scaled_ll_to_float(combine_levels<S>(v[3]), er.w + base);
-    *reinterpret_cast<float4*>(F + i) = out;
+    const T o0 = scaled_ll_to<T>(combine_levels<S>(v[0]), er.x + base);
+    const T o1 = scaled_ll_to<T>(combine_levels<S>(v[1]), er.y + base);
+    const T o2 = scaled_ll_to<T>(combine_levels<S>(v[2]), er.z + base);
+    const T o3 = scaled_ll_to<T>(combine_levels<S>(v[3]), er.w + base);
+    if constexpr (sizeof(T) == 4) {
+        *reinterpret_cast<float4*>(F + i) = make_float4(o0, o1, o2, o3);
+    } else {
+        *reinterpret_cast<double2*>(F + i) = make_double2(o0, o1);
+        *reinterpret_cast<double2*>(F + i + 2) = make_double2(o2, o3);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -169,9 +173,9 @@ __global__ void f_combine_kernel(const float* __restrict__ C, int nao,
 // ex (an earlier omega of the same tile); only w o G is sliced.  B holds nb
 // columns per chunk (several right-hand sides side by side); this launch
 // fills columns boff .. boff + nao - 1.
-template<int S, int KC, bool DOX>
+template<int S, int KC, bool DOX, typename GT>
 __global__ void __launch_bounds__(KC / 8)
-k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
+k_slice_kernel(const double* __restrict__ X, const GT* __restrict__ G,
                const double* __restrict__ w, int nao, int64_t ld,
                int64_t npts, int* __restrict__ ex, int* __restrict__ ew,
                __nv_bfloat16* __restrict__ A, __nv_bfloat16* __restrict__ B,
@@ -186,9 +190,21 @@ k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
     if (g0 + 8 <= npts) {
         const double2* xp = reinterpret_cast<const double2*>(X + (int64_t)col * ld + g0);
         const double2* wp = reinterpret_cast<const double2*>(w + g0);
-        const float4* gp = reinterpret_cast<const float4*>(G + (int64_t)col * ld + g0);
-        const float4 ga = __ldg(gp), gb = __ldg(gp + 1);
-        const float gv[8] = {ga.x, ga.y, ga.z, ga.w, gb.x, gb.y, gb.z, gb.w};
+        double gv[8];
+        if constexpr (sizeof(GT) == 4) {
+            const float4* gp = reinterpret_cast<const float4*>(G + (int64_t)col * ld + g0);
+            const float4 ga = __ldg(gp), gb = __ldg(gp + 1);
+            gv[0] = ga.x; gv[1] = ga.y; gv[2] = ga.z; gv[3] = ga.w;
+            gv[4] = gb.x; gv[5] = gb.y; gv[6] = gb.z; gv[7] = gb.w;
+        } else {
+            const double2* gp = reinterpret_cast<const double2*>(G + (int64_t)col * ld + g0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const double2 t = __ldg(gp + u);
+                gv[2 * u] = t.x;
+                gv[2 * u + 1] = t.y;
+            }
+        }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const double2 b = __ldg(wp + u);
@@ -198,8 +214,8 @@ k_slice_kernel(const double* __restrict__ X, const float* __restrict__ G,
             } else {
                 xv[2 * u] = 0.0; xv[2 * u + 1] = 0.0;
             }
-            wv[2 * u] = b.x * (double)gv[2 * u];
-            wv[2 * u + 1] = b.y * (double)gv[2 * u + 1];
+            wv[2 * u] = b.x * gv[2 * u];
+            wv[2 * u + 1] = b.y * gv[2 * u + 1];
         }
     } else {
 #pragma unroll
@@ -349,8 +365,17 @@ int ozaki_f_gemm(cublasHandle_t hb, const double* X, const double* QD,
     return ozaki_f_gemm_cublas(hb, X, QD, nao, ld, F, ws, s);
 }
 
-int ozaki_f_gemm_cublas(cublasHandle_t hb, const double* X, const double* QD,
-                        int nao, int64_t ld, float* F, void* ws, cudaStream_t s) {
+int ozaki_f_gemm64(cublasHandle_t hb, const double* X, const double* QD,
+                   int nao, int64_t ld, double* F, void* ws, cudaStream_t s,
+                   unsigned long long* status) {
+    if (g_f_engine.load() == kOzEngineTc)
+        return ozaki_f_gemm_tc64(X, QD, nao, ld, F, ws, s, status);
+    return ozaki_f_gemm_cublas64(hb, X, QD, nao, ld, F, ws, s);
+}
+
+template<typename T>
+static int f_gemm_cublas_t(cublasHandle_t hb, const double* X, const double* QD,
+                           int nao, int64_t ld, T* F, void* ws, cudaStream_t s) {
     constexpr int S = kOzSlices;
     char* p = static_cast<char*>(ws);
     int* erow = reinterpret_cast<int*>(p); p += al(sizeof(int) * ld);
@@ -381,16 +406,27 @@ int ozaki_f_gemm_cublas(cublasHandle_t hb, const double* X, const double* QD,
     }
     {
         dim3 grid((unsigned)((ld / 4 + 255) / 256), (unsigned)nao);
-        f_combine_kernel<S><<<grid, 256, 0, s>>>(C, nao, ld, erow, ecol, F);
+        f_combine_kernel<S, T><<<grid, 256, 0, s>>>(C, nao, ld, erow, ecol, F);
         OZ_CUDA(cudaGetLastError());
     }
     return 0;
 }
 
-int ozaki_k_gemm_multi(cublasHandle_t hb, const double* X, const float* const* G,
-                       int nrhs, const double* w, int nao, int64_t ld,
-                       int64_t npts, int accumulate, double* const* K, void* ws,
-                       cudaStream_t s, bool x_sliced) {
+int ozaki_f_gemm_cublas(cublasHandle_t hb, const double* X, const double* QD,
+                        int nao, int64_t ld, float* F, void* ws, cudaStream_t s) {
+    return f_gemm_cublas_t<float>(hb, X, QD, nao, ld, F, ws, s);
+}
+
+int ozaki_f_gemm_cublas64(cublasHandle_t hb, const double* X, const double* QD,
+                          int nao, int64_t ld, double* F, void* ws, cudaStream_t s) {
+    return f_gemm_cublas_t<double>(hb, X, QD, nao, ld, F, ws, s);
+}
+
+template<typename GT>
+static int k_gemm_multi_t(cublasHandle_t hb, const double* X, const GT* const* G,
+                          int nrhs, const double* w, int nao, int64_t ld,
+                          int64_t npts, int accumulate, double* const* K, void* ws,
+                          cudaStream_t s, bool x_sliced) {
     constexpr int S = kOzSlices, KC = kOzKc;
     if (nrhs < 1 || nrhs > 8) return (int)cudaErrorInvalidValue;
     const int nchunk = (int)((ld + KC - 1) / KC);
@@ -411,10 +447,10 @@ int ozaki_k_gemm_multi(cublasHandle_t hb, const double* X, const float* const* G
     dim3 grid(nchunk, nao);
     for (int r = 0; r < nrhs; ++r) {
         if (x_sliced || r > 0)
-            k_slice_kernel<S, KC, false><<<grid, KC / 8, 0, s>>>(
+            k_slice_kernel<S, KC, false, GT><<<grid, KC / 8, 0, s>>>(
                 X, G[r], w, nao, ld, npts, ex, ew, A, B, nb, r * nao);
         else
-            k_slice_kernel<S, KC, true><<<grid, KC / 8, 0, s>>>(
+            k_slice_kernel<S, KC, true, GT><<<grid, KC / 8, 0, s>>>(
                 X, G[r], w, nao, ld, npts, ex, ew, A, B, nb, r * nao);
         OZ_CUDA(cudaGetLastError());
     }
@@ -435,6 +471,21 @@ int ozaki_k_gemm_multi(cublasHandle_t hb, const double* X, const float* const* G
                                                         accumulate, Kd);
     OZ_CUDA(cudaGetLastError());
     return 0;
+}
+
+int ozaki_k_gemm_multi(cublasHandle_t hb, const double* X, const float* const* G,
+                       int nrhs, const double* w, int nao, int64_t ld,
+                       int64_t npts, int accumulate, double* const* K, void* ws,
+                       cudaStream_t s, bool x_sliced) {
+    return k_gemm_multi_t<float>(hb, X, G, nrhs, w, nao, ld, npts, accumulate, K, ws, s,
+                                 x_sliced);
+}
+
+int ozaki_k_gemm64(cublasHandle_t hb, const double* X, const double* G,
+                   const double* w, int nao, int64_t ld, int64_t npts,
+                   int accumulate, double* K, void* ws, cudaStream_t s) {
+    return k_gemm_multi_t<double>(hb, X, &G, 1, w, nao, ld, npts, accumulate, &K, ws, s,
+                                  false);
 }
 
 int ozaki_k_gemm(cublasHandle_t hb, const double* X, const float* G,

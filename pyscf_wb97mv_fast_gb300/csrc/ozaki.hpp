@@ -28,6 +28,17 @@ int ozaki_f_gemm(cublasHandle_t hb, const double* X, const double* QD,
                  int nao, int64_t ld, float* F, void* ws, cudaStream_t s,
                  unsigned long long* status = nullptr);
 
+// the same product with FP64 output: the combined level sums (42 bits
+// relative to the per-point / per-column maxima) rounded once to FP64
+int ozaki_f_gemm64(cublasHandle_t hb, const double* X, const double* QD,
+                   int nao, int64_t ld, double* F, void* ws, cudaStream_t s,
+                   unsigned long long* status = nullptr);
+
+// K (+)= X^T (w o G) with G FP64 (w o G formed in FP64 before the split)
+int ozaki_k_gemm64(cublasHandle_t hb, const double* X, const double* G,
+                   const double* w, int nao, int64_t ld, int64_t npts,
+                   int accumulate, double* K, void* ws, cudaStream_t s);
+
 // the two engines of the F product (bitwise the same F): this library's
 // tcgen05 kernel (the default) and cuBLAS level GEMMs
 constexpr int kOzEngineLibrary = 0;
@@ -40,6 +51,10 @@ int ozaki_f_gemm_cublas(cublasHandle_t hb, const double* X, const double* QD,
                         int nao, int64_t ld, float* F, void* ws, cudaStream_t s);
 int ozaki_f_gemm_tc(const double* X, const double* QD, int nao, int64_t ld, float* F,
                     void* ws, cudaStream_t s, unsigned long long* status);
+int ozaki_f_gemm_cublas64(cublasHandle_t hb, const double* X, const double* QD,
+                          int nao, int64_t ld, double* F, void* ws, cudaStream_t s);
+int ozaki_f_gemm_tc64(const double* X, const double* QD, int nao, int64_t ld, double* F,
+                      void* ws, cudaStream_t s, unsigned long long* status);
 size_t ozaki_f_tc_bytes(int nao, int64_t ld);
 // exponent of max_l |X(l, g)| per point g (shared by both engines)
 void f_rowmax(const double* X, int nao, int64_t ld, int* erow, cudaStream_t s);

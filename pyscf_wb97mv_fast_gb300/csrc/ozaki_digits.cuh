@@ -116,6 +116,21 @@ __device__ __forceinline__ float scaled_ll_to_float(long long v, int sc) {
     return __uint_as_float(bits);
 }
 
+// v 2^sc as FP64: one rounding of v to 53 bits, then an exact scaling (sc
+// stays inside pow2's range for the clamped exponents of the split)
+__device__ __forceinline__ double scaled_ll_to_double(long long v, int sc) {
+    return (double)v * pow2(sc);
+}
+
+// the combined value in the output type of an F product (FP32 or FP64)
+template<typename T> __device__ __forceinline__ T scaled_ll_to(long long v, int sc);
+template<> __device__ __forceinline__ float scaled_ll_to<float>(long long v, int sc) {
+    return scaled_ll_to_float(v, sc);
+}
+template<> __device__ __forceinline__ double scaled_ll_to<double>(long long v, int sc) {
+    return scaled_ll_to_double(v, sc);
+}
+
 // value of the combined levels: sum_l C_l 2^(B (S-1-l)) as an exact int64
 // (every level is an integer below 2^24 in magnitude: 32-bit conversion)
 template<int S>

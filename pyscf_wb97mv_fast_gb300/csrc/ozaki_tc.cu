@@ -128,19 +128,21 @@ f_slice_qd_km_kernel(const double* __restrict__ QD, int nao, int* __restrict__ e
 
 // -- the GEMM + combine ----------------------------------------------------------
 
+template<typename T>
 struct FTcArgs {
     const int* erow;
     const int* ecol;
-    float* F;
+    T* F;
     int nao;
     int64_t ld;
     int nkb;                      // 64-wide blocks of the AO index
     unsigned long long* status;   // bit 0: a wait gave up
 };
 
+template<typename T>
 __global__ void __launch_bounds__(128, 1)
 ozaki_f_tc_kernel(const __grid_constant__ CUtensorMap mapA,
-                  const __grid_constant__ CUtensorMap mapB, const FTcArgs P) {
+                  const __grid_constant__ CUtensorMap mapB, const FTcArgs<T> P) {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = tc::smem_u32(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
@@ -269,7 +271,7 @@ ozaki_f_tc_kernel(const __grid_constant__ CUtensorMap mapA,
                 if (mu < P.nao) {
                     const int sc = er + P.ecol[mu] - 2 * kW + 2 + kB * (S - 1);
                     P.F[(int64_t)mu * P.ld + g] =
-                        bad ? __int_as_float(0x7fc00000) : scaled_ll_to_float(acc[q], sc);
+                        bad ? (T)__int_as_float(0x7fc00000) : scaled_ll_to<T>(acc[q], sc);
                 }
             }
         }
@@ -333,8 +335,9 @@ size_t ozaki_f_tc_bytes(int nao, int64_t ld) {
            al(sizeof(unsigned long long));
 }
 
-int ozaki_f_gemm_tc(const double* X, const double* QD, int nao, int64_t ld, float* F,
-                    void* ws, cudaStream_t s, unsigned long long* status) {
+template<typename T>
+static int f_gemm_tc_t(const double* X, const double* QD, int nao, int64_t ld, T* F,
+                       void* ws, cudaStream_t s, unsigned long long* status) {
     if (!ozaki_f_supported(nao) || ld % 2 != 0 || ld > (int64_t)kBM * 65535)
         return (int)cudaErrorInvalidValue;
     const size_t kp = (size_t)pad8(nao);
@@ -350,24 +353,30 @@ int ozaki_f_gemm_tc(const double* X, const double* QD, int nao, int64_t ld, floa
     CUtensorMap mapA, mapB;
     if (!make_map(&mapA, A, nao, ld, kBM) || !make_map(&mapB, B, nao, nao, kBN))
         return (int)cudaErrorNotSupported;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(ozaki_f_tc_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             kSmemBytes);
-        if (e != cudaSuccess) return (int)e;
-        attr_set = true;
-    }
+    cudaError_t e = cudaFuncSetAttribute(ozaki_f_tc_kernel<T>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kSmemBytes);
+    if (e != cudaSuccess) return (int)e;
     f_rowmax(X, nao, ld, erow, s);
     {
         dim3 grid((unsigned)((ld + 63) / 64), (unsigned)((kp + 63) / 64));
         f_slice_x_km_kernel<<<grid, 256, 0, s>>>(X, nao, ld, erow, A);
     }
     f_slice_qd_km_kernel<<<nao, 256, 0, s>>>(QD, nao, ecol, B);
-    FTcArgs a{erow, ecol, F, nao, ld, (nao + kBK - 1) / kBK, status};
+    FTcArgs<T> a{erow, ecol, F, nao, ld, (nao + kBK - 1) / kBK, status};
     dim3 grid((unsigned)((nao + kBN - 1) / kBN), (unsigned)((ld + kBM - 1) / kBM));
-    ozaki_f_tc_kernel<<<grid, 128, kSmemBytes, s>>>(mapA, mapB, a);
+    ozaki_f_tc_kernel<T><<<grid, 128, kSmemBytes, s>>>(mapA, mapB, a);
     return (int)cudaGetLastError();
+}
+
+int ozaki_f_gemm_tc(const double* X, const double* QD, int nao, int64_t ld, float* F,
+                    void* ws, cudaStream_t s, unsigned long long* status) {
+    return f_gemm_tc_t<float>(X, QD, nao, ld, F, ws, s, status);
+}
+
+int ozaki_f_gemm_tc64(const double* X, const double* QD, int nao, int64_t ld, double* F,
+                      void* ws, cudaStream_t s, unsigned long long* status) {
+    return f_gemm_tc_t<double>(X, QD, nao, ld, F, ws, s, status);
 }
 
 }  // namespace wb

@@ -167,23 +167,35 @@ def _prepare_dm(dm, hermi):
     return dm
 
 
-def vv10_energy_fock(eng, g, D, nlc_pars, kernel=None, fp32=False):
+def vv10_energy_fock(eng, g, D, nlc_pars, kernel=None, fp32=False, gemm='fp64'):
     """E_nl and V_nl of one density on a device grid, all on the device:
     g holds coordinates (engine frame), weights and the deriv-1 AO values
     X (4, nao, ld) (scf.DeviceGrid); D (nao, nao) FP64 device.  The same
     steps as gpu_nr_nlc_vxc for one parameter set (b, C) with factor 1:
     GGA density, threshold rho >= 1e-8, pointwise terms, the pair sum, the
     GGA potential and vmat = X^T (w v) X + transpose.  Returns (E_nl
-    device scalar, V_nl (nao, nao)).  fp32: the two GEMMs through the
-    bf16 Ozaki split (D X rounded once to FP32, the Fock side from an
-    FP32-rounded G), as the FP32 stages of the SCF take them."""
+    device scalar, V_nl (nao, nao)).  The two GEMMs (D X and the Fock
+    side) run as gemm:
+      'fp64'    plain FP64 GEMMs;
+      'split64' the bf16 Ozaki split with FP64 operands and results (42
+                bits of the per-row / per-column maxima), the SCF's FP64
+                tail;
+      'fp32'    the split with D X rounded once to FP32 and the Fock side
+                from an FP32-rounded G, the SCF's FP32 stages (fp32=True
+                is the same)."""
     torch = _torch()
+    if fp32:
+        gemm = 'fp32'
+    if gemm not in ('fp64', 'split64', 'fp32'):
+        raise ValueError("gemm must be 'fp64', 'split64' or 'fp32'")
     kernel = kernel or Vv10Kernel(0.0)
     n = g.n
     ao = g.X[:, :, :n]
     w = g.weights
-    if fp32:
+    if gemm == 'fp32':
         T = eng.ozaki_f(g.X[0], D)[:, :n].to(torch.float64)
+    elif gemm == 'split64':
+        T = eng.ozaki_f(g.X[0], D, fp64=True)[:, :n]
     else:
         T = D @ ao[0]
     rho0 = (T * ao[0]).sum(dim=0)
@@ -199,13 +211,15 @@ def vv10_energy_fock(eng, g, D, nlc_pars, kernel=None, fp32=False):
     v0[ind] = Beta + F + 1.5 * (U * dKdR + W * dW0dR)
     v1[ind] = 1.5 * W * dW0dG
     e_nl = (rho0 * w * exc).sum()
-    if fp32:
-        # G = 1/2 v0 X0 + sum_d 2 v1 grad_d X_d, then X0^T (w o fl32(G))
+    if gemm != 'fp64':
+        # G = 1/2 v0 X0 + sum_d 2 v1 grad_d X_d, then X0^T (w o G), G FP64
+        # or rounded once to FP32
         vv = torch.empty((4, n), dtype=torch.float64, device=D.device)
         vv[0] = 0.5 * v0
         vv[1:4] = 2.0 * v1[None, :] * grad
-        G = torch.zeros_like(g.X[0], dtype=torch.float32)
-        G[:, :n] = torch.einsum('dmp,dp->mp', ao, vv).to(torch.float32)
+        dt = torch.float32 if gemm == 'fp32' else torch.float64
+        G = torch.zeros_like(g.X[0], dtype=dt)
+        G[:, :n] = torch.einsum('dmp,dp->mp', ao, vv).to(dt)
         vmat = eng.ozaki_k(g.X[0], G, w)
         return e_nl, vmat + vmat.T
     wv = torch.empty((4, n), dtype=torch.float64, device=D.device)

@@ -191,6 +191,16 @@ DEFAULT_COARSE = dict(xc=1, sgx=0)
 REFERENCE_STAGE_LEVELS = dict(xc=(1, 3, 3), sgx=(1, 1, 2), nlc=(None, 1, 3))
 
 
+def _gemm_mode(gemm):
+    if gemm is True:
+        return 'fp64'
+    if gemm is False:
+        return 'fp32'
+    if gemm not in ('fp64', 'split64', 'fp32'):
+        raise ValueError("gemm must be 'fp64', 'split64' or 'fp32'")
+    return gemm
+
+
 class DeviceRKS:
     """RKS SCF on one GPU for a Molecule (see the module docstring).
 
@@ -252,25 +262,33 @@ class DeviceRKS:
             self._grid_cache[key] = g
         return g
 
-    def _vmat(self, g, v, fp64):
-        """X^T diag(w v) X over grid g (deriv-0 AO values), symmetric."""
+    def _vmat(self, g, v, gemm):
+        """X^T diag(w v) X over grid g (deriv-0 AO values), symmetric.
+        gemm: 'fp64' (plain FP64 GEMM), 'split64' (the bf16 Ozaki split
+        with the FP64 G = X v) or 'fp32' (the split with G rounded to
+        FP32); True / False stand for 'fp64' / 'fp32'."""
         torch = _torch()
+        gemm = _gemm_mode(gemm)
         X = g.X if g.deriv == 0 else g.X[0]
-        if fp64:
+        if gemm == 'fp64':
             wv = torch.zeros(g.ld, dtype=torch.float64, device=self.device)
             wv[:g.n] = g.weights * v[:g.n]
             M = (X * wv[None, :]) @ X.T
         else:
-            G = torch.zeros_like(X, dtype=torch.float32)
-            G[:, :g.n] = (X[:, :g.n] * v[None, :g.n]).to(torch.float32)
+            dt = torch.float32 if gemm == 'fp32' else torch.float64
+            G = torch.zeros_like(X, dtype=dt)
+            G[:, :g.n] = (X[:, :g.n] * v[None, :g.n]).to(dt)
             M = self.eng.ozaki_k(X, G, g.weights)
         return 0.5 * (M + M.T)
 
-    def _density(self, g, D, fp64):
+    def _density(self, g, D, gemm):
         torch = _torch()
+        gemm = _gemm_mode(gemm)
         X = g.X if g.deriv == 0 else g.X[0]
-        if fp64:
+        if gemm == 'fp64':
             T = D @ X
+        elif gemm == 'split64':
+            T = self.eng.ozaki_f(X, D, fp64=True)
         else:
             T = self.eng.ozaki_f(X, D).to(torch.float64)
         return (T * X).sum(dim=0)[:g.n]
@@ -285,11 +303,13 @@ class DeviceRKS:
                                       tile_tol=self.k_tile_tol, stats=False)
         return 0.5 * (Kb + Kb.transpose(1, 2))
 
-    def vv10(self, D, g, fp64=True):
-        """(E_nl, V_nl) on the NLC grid g (device scalars / matrix); the
-        FP32 stages take its two GEMMs through the bf16 split."""
+    def vv10(self, D, g, gemm=True):
+        """(E_nl, V_nl) on the NLC grid g (device scalars / matrix); gemm as
+        for _vmat: the FP32 stages take its two GEMMs through the bf16
+        split, the staged form's FP64 tail through the FP64 split."""
         from pyscf_wb97mv_fast_gb300.gpu.vv10 import vv10_energy_fock
-        return vv10_energy_fock(self.eng, g, D, self.functional.nlc, fp32=not fp64)
+        return vv10_energy_fock(self.eng, g, D, self.functional.nlc,
+                                gemm=_gemm_mode(gemm))
 
     def _tick(self, name):
         """Per-part wall time (device-synchronised) when profiling."""
@@ -313,12 +333,16 @@ class DeviceRKS:
         whose small entries drop most tasks.  With ``inc32`` (the staged
         form's FP64 tail) the increments of K_x, J and rho are built with
         the FP32 kernels: their rounding is ~1e-7 of the increment, itself
-        small, so the operator stays FP64-accurate on the FP64 base.
-        Without it (the plain FP64 form) only K_x is incremental, in FP64.
+        small, so the operator stays FP64-accurate on the FP64 base; the
+        tail's quadrature GEMMs (J, rho, V_xc, VV10) run through the FP64
+        form of the bf16 split (42 bits of the row / column maxima, FP64
+        operands and results).  Without it (the plain FP64 form) only K_x
+        is incremental, in FP64, and every GEMM is a plain FP64 GEMM.
         base' is the base to keep (a new one after a full build)."""
         torch = _torch()
         f = self.functional
         gs, gx = grids['sgx'], grids['xc']
+        gemm = 'fp32' if not fp64 else ('split64' if inc32 else 'fp64')
         self._tick(None)
         full = base is None
         dD = None if full else D - base['D']
@@ -331,21 +355,21 @@ class DeviceRKS:
         self._tick('k')
         if full or not inc32:
             vh = self.eng.hartree(gs.coords, D, tol=self.j_tol, fp64=fp64)
-            J = self._vmat(gs, vh, fp64)
+            J = self._vmat(gs, vh, gemm)
         else:
             vh = self.eng.hartree(gs.coords, dD, tol=self.j_tol, fp64=False)
-            J = base['J'] + self._vmat(gs, vh, False)
+            J = base['J'] + self._vmat(gs, vh, 'fp32')
         self._tick('j')
         if full or not inc32:
-            rho = self._density(gx, D, fp64)
+            rho = self._density(gx, D, gemm)
         else:
-            rho = base['rho'] + self._density(gx, dD, False)
+            rho = base['rho'] + self._density(gx, dD, 'fp32')
         e, v = f.eval(rho)
         exc = (gx.weights * e).sum()
-        Vxc = self._vmat(gx, v, fp64 and not inc32)
+        Vxc = self._vmat(gx, v, gemm)
         self._tick('xc')
         if grids.get('nlc') is not None and f.nlc:
-            enl, Vnl = self.vv10(D, grids['nlc'], fp64)
+            enl, Vnl = self.vv10(D, grids['nlc'], gemm)
         else:
             enl, Vnl = torch.zeros((), dtype=torch.float64, device=self.device), 0.0
         self._tick('vv10')

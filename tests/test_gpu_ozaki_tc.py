@@ -45,9 +45,9 @@ def test_tc_engine_is_bitwise_the_library_engine(name):
     assert not torch.isnan(F_tc).any()
     assert torch.equal(F_tc, F_lib), name
     # and F is fl32 of the FP64 product to FP32 rounding
-    ref = (dm.T @ X).to(torch.float32)
+    ref = dm.T @ X
     scale = ref.abs().amax(dim=0, keepdim=True).clamp_min(1e-300)
-    assert float(((F_tc - ref).abs() / scale).max()) < 1e-6
+    assert float(((F_tc.to(torch.float64) - ref).abs() / scale).max()) < 1e-6
 
 
 def test_tc_engine_in_the_k_build_matches_library_engine():
@@ -71,3 +71,35 @@ def test_tc_engine_in_the_k_build_matches_library_engine():
         cosx.set_f_engine(prev)
     assert torch.equal(out['tc'], out['library'])
     assert cosx.get_f_engine() == prev
+
+
+@pytest.mark.parametrize('engine', ['tc', 'library'])
+def test_fp64_output_split_is_42_bit_accurate(engine):
+    """wb_cosx_ozaki_f64 / _k64 (the SCF FP64 tail's quadrature GEMMs):
+    within 2^-40 of the per-point / per-column maxima of an FP64 product,
+    and the two F engines agree bitwise."""
+    import torch
+    from pyscf_wb97mv_fast_gb300 import cosx
+    mol = dimer('synthetic-tzvp')
+    eng, X, dm = _case(mol, 4000, 5)
+    prev = cosx.set_f_engine(engine)
+    try:
+        F64 = eng.ozaki_f(X, dm, fp64=True)
+        cosx.set_f_engine('library' if engine == 'tc' else 'tc')
+        F64b = eng.ozaki_f(X, dm, fp64=True)
+    finally:
+        cosx.set_f_engine(prev)
+    assert F64.dtype == torch.float64
+    assert torch.equal(F64, F64b)
+    ref = dm.T @ X
+    bound = (X.abs().amax(dim=0, keepdim=True) *
+             dm.abs().amax(dim=0)[:, None]) * mol.nao * 2.0 ** -40
+    assert bool(((F64 - ref).abs() <= bound + 1e-300).all())
+    # K side with an FP64 G: X^T (w o G)
+    n = X.shape[1]
+    w = torch.rand(n, dtype=torch.float64, device='cuda') + 0.5
+    G = torch.randn_like(X)
+    K = eng.ozaki_k(X, G, w)
+    Kref = X @ (w[None, :] * G).T
+    scale = float(X.abs().max()) * float((w[None, :] * G).abs().max()) * n
+    assert float((K - Kref).abs().max()) < scale * 2.0 ** -40
