@@ -549,17 +549,33 @@ def batched_timing(torch, nmol=64, seed=4, iters=3):
     del shared
     torch.cuda.empty_cache()
     free, _ = torch.cuda.mem_get_info(engines[0].device)
-    budget = 0.6 * free
-    waves, cur, used = [], [], scratch
-    for i, b in enumerate(wsb_batch):
-        if cur and used + b > budget:
-            waves.append(cur)
-            cur, used = [], scratch
-        cur.append(i)
-        used += b
-    waves.append(cur)
-    batches = [CosxBatch([engines[i] for i in wv], [grids[i] for i in wv], OMEGAS,
-                         tile_tol=TILE_TOL) for wv in waves]
+
+    def plan(budget):
+        waves, cur, used = [], [], scratch
+        for i, b in enumerate(wsb_batch):
+            if cur and used + b > budget:
+                waves.append(cur)
+                cur, used = [], scratch
+            cur.append(i)
+            used += b
+        waves.append(cur)
+        return waves
+
+    # as few waves as the free HBM allows: 85 % of it first, fewer bytes per
+    # wave if the workspaces do not fit after all
+    for frac in (0.85, 0.6, 0.4):
+        waves = plan(frac * free)
+        try:
+            batches = [CosxBatch([engines[i] for i in wv], [grids[i] for i in wv],
+                                 OMEGAS, tile_tol=TILE_TOL) for wv in waves]
+            break
+        except torch.OutOfMemoryError:
+            batches = None
+            for e in engines:
+                e._ws = None
+            torch.cuda.empty_cache()
+    if batches is None:
+        raise RuntimeError('batched leg: the workspaces do not fit')
     bouts = [[outs[i] for i in wv] for wv in waves]
 
     def batched():
@@ -911,11 +927,14 @@ def _scf_record(r, ref):
             if abs(h['e'] - ref) < 1e-8 and h['fp64']:
                 t_hit = h['t']
                 break
+    tail = [h for h in r['history'] if h['fp64']][-30:]
     return {'e_tot': r['e_tot'], 'error_vs_reference': r.get('error_vs_reference'),
             'converged': r['converged'], 'cycles': r['cycles'], 'wall_s': r['wall'],
             'wall_to_1e-8_s': t_hit,
             'cycles_fp64': sum(1 for h in r['history'] if h['fp64']),
-            'stages': [dict(s) for s in r['stages']]}
+            'stages': [dict(s) for s in r['stages']],
+            'fp64_cycles': [{'cycle': h['cycle'], 'err': h.get('err'), 'dE': h['dE'],
+                             'gnorm': h['gnorm'], 't': round(h['t'], 3)} for h in tail]}
 
 
 def scf_c20_timing(torch, n_carbon=20):
@@ -1039,7 +1058,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--gemm', default='ozaki', choices=['ozaki', 'native', 'emulated'])
-    ap.add_argument('--f-engine', default='tc', choices=['tc', 'library'],
+    ap.add_argument('--f-engine', default='library', choices=['library', 'tc'],
                     help="the Ozaki F product: this library's tcgen05 kernel or "
                          "cuBLAS level GEMMs (bitwise the same F)")
     ap.add_argument('--small', action='store_true',

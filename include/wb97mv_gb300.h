@@ -338,10 +338,12 @@ int wb_cosx_ozaki_k64(wb_cosx* h, const double* x, const double* g,
                       void* stream);
 
 /* Engine of the F product (process-wide, every F of the K builds and of
- * wb_cosx_ozaki_f): WB_OZAKI_ENGINE_TC (the default) is this library's
+ * wb_cosx_ozaki_f / _f64): WB_OZAKI_ENGINE_LIBRARY (the default) runs one
+ * cuBLAS bf16 GEMM per level; WB_OZAKI_ENGINE_TC is this library's
  * tensor-core kernel (TMA tile loads, tcgen05 MMAs into TMEM, the exact
- * level combination fused into its epilogue); WB_OZAKI_ENGINE_LIBRARY runs
- * one cuBLAS bf16 GEMM per level.  Both give bitwise the same F.  Replaces
+ * level combination fused into its epilogue), slower on the bench step
+ * (its seven level accumulators allow 64-wide tiles only).  Both give
+ * bitwise the same F.  Replaces
  * no reference call (the reference's F GEMM is one CuPy FP64 matmul,
  * gpu/sgx_k.py:722); returns WB_OK or WB_ERR_INVALID_ARGUMENT. */
 #define WB_OZAKI_ENGINE_LIBRARY 0

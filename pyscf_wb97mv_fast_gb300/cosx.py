@@ -59,9 +59,9 @@ F_ENGINES = {'library': 0, 'tc': 1}
 
 
 def set_f_engine(name):
-    """Engine of the F product of the Ozaki split (process-wide): 'tc' (the
-    default, this library's tcgen05 tensor-core kernel with the level
-    combination fused) or 'library' (cuBLAS bf16 level GEMMs); both give
+    """Engine of the F product of the Ozaki split (process-wide): 'library'
+    (the default, cuBLAS bf16 level GEMMs) or 'tc' (this library's tcgen05
+    tensor-core kernel with the level combination fused); both give
     bitwise the same F.  Returns the previous engine's name."""
     if name not in F_ENGINES:
         raise ValueError('F engine must be one of %s' % sorted(F_ENGINES))

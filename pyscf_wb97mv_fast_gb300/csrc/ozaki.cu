@@ -21,12 +21,14 @@
 // per-row / per-column maxima; the truncated products (i + j >= S) are
 // below 2^-W of them.
 //
-// The F product runs by default on this library's own tensor-core kernel
-// (ozaki_tc.cu: TMA, tcgen05 MMAs into TMEM, the level combination fused
-// into its epilogue); ozaki_set_f_engine(kOzEngineLibrary) selects the
-// library-GEMM form below (cuBLAS bf16 GEMMs with FP32 accumulation, one
-// per level, and this file's slicing and combination kernels) -- bitwise
-// the same result.  The K product's level GEMMs are cuBLAS GEMMs.
+// The level GEMMs are library GEMMs by default (cuBLAS bf16 GEMMs with FP32
+// accumulation, one per level) around this file's slicing and combination
+// kernels.  ozaki_set_f_engine(kOzEngineTc) runs the F product on this
+// library's own tensor-core kernel instead (ozaki_tc.cu: TMA, tcgen05 MMAs
+// into TMEM, the level combination fused into its epilogue) -- bitwise the
+// same result; its seven exact level accumulators leave room for 64-wide
+// N tiles only, and it measured 2.4x slower than the library form on the
+// bench step (18.4 vs 7.65 ms).  The K product's level GEMMs are cuBLAS.
 #include <cublas_v2.h>
 #include <cuda_bf16.h>
 
@@ -351,7 +353,7 @@ void f_rowmax(const double* X, int nao, int64_t ld, int* erow, cudaStream_t s) {
 }
 
 namespace {
-std::atomic<int> g_f_engine{kOzEngineTc};
+std::atomic<int> g_f_engine{kOzEngineLibrary};
 }
 
 void ozaki_set_f_engine(int engine) { g_f_engine.store(engine); }

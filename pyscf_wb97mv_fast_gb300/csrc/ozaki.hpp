@@ -39,8 +39,8 @@ int ozaki_k_gemm64(cublasHandle_t hb, const double* X, const double* G,
                    const double* w, int nao, int64_t ld, int64_t npts,
                    int accumulate, double* K, void* ws, cudaStream_t s);
 
-// the two engines of the F product (bitwise the same F): this library's
-// tcgen05 kernel (the default) and cuBLAS level GEMMs
+// the two engines of the F product (bitwise the same F): cuBLAS level
+// GEMMs (the default) and this library's tcgen05 kernel
 constexpr int kOzEngineLibrary = 0;
 constexpr int kOzEngineTc = 1;
 void ozaki_set_f_engine(int engine);
