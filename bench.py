@@ -986,6 +986,64 @@ def scf_c20_timing(torch, n_carbon=20):
     return out
 
 
+def scf_batched_timing(torch, nmol=64, seed=4):
+    """Config 4: nmol seeded water clusters of n in {4..32} waters
+    (uniform), synthetic def2-SVP, XC level 1 / SGX level 0 / VV10 level 0
+    (S0 on XC 0 / SGX 0), every molecule a full SCF.  The plain FP64 form of
+    each molecule (its own SCF, one after another) gives its FP64 reference
+    energy; the mixed staged form runs one molecule at a time and batched
+    (BatchedRKS: the FP32 exchange builds of all molecules in one batched
+    build per SGX level, their VV10 double sums in one launch).  Grids and
+    AO values are built by an untimed warm-up."""
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.scf import BatchedRKS
+    from pyscf_wb97mv_fast_gb300.systems import water_cluster
+    rng = np.random.default_rng(seed)
+    sizes = [int(x) for x in rng.integers(4, 33, size=nmol)]
+    mols = [Molecule.build(water_cluster(n, box=max(5.0, 3.2 * n ** (1.0 / 3.0)),
+                                         seed=300 + i), 'synthetic-svp')
+            for i, n in enumerate(sizes)]
+    levels, coarse = dict(xc=1, sgx=0, nlc=0), dict(xc=0, sgx=0)
+    b = BatchedRKS(mols, levels=levels, coarse=coarse)
+    b.kernel(precision='mixed', max_cycle=1)          # warm-up: grids, batches
+    for r in b.rks:
+        r.kernel(precision='fp64', max_cycle=1)
+
+    def seq(precision, refs=None):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = [r.kernel(precision=precision, reference_energy=None if refs is None
+                        else refs[i]) for i, r in enumerate(b.rks)]
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    r64, t64 = seq('fp64')
+    refs = [r['e_tot'] for r in r64]
+    rseq, tseq = seq('mixed', refs)
+    rb = b.kernel(precision='mixed', reference_energies=refs)
+    tb = rb[0]['batch_wall']
+    errs = [r['error_vs_reference'] for r in rb]
+    out = {'molecules': nmol, 'waters_per_cluster': sizes,
+           'levels': levels, 'coarse': coarse,
+           'nao_total': int(sum(r.mol.nao for r in b.rks)),
+           'reference': 'each molecule\'s plain FP64 device SCF on the final grids',
+           'fp64_sequential_wall_s': t64,
+           'mixed_sequential_wall_s': tseq,
+           'mixed_batched_wall_s': tb,
+           'fp64_over_mixed_batched': t64 / tb,
+           'batched_over_sequential_speedup': tseq / tb,
+           'all_converged': all(r['converged'] for r in rb) and all(r['converged'] for r in r64),
+           'max_abs_error_vs_fp64_Ha': max(abs(e) for e in errs),
+           'all_within_1e-8': all(abs(e) < 1e-8 for e in errs),
+           'batched_equals_sequential': all(a['e_tot'] == c['e_tot']
+                                            for a, c in zip(rb, rseq)),
+           'cycles_mixed': [r['cycles'] for r in rb],
+           'cycles_fp64': [r['cycles'] for r in r64],
+           'batched_exchange_builds': rb[0]['batched_exchange_builds']}
+    b.close()
+    return out
+
+
 def run_sample(oracle, mol, g, dm, idx):
     coords = g.coords[idx]
     X = oracle.ao_eval(mol, coords)
@@ -1086,6 +1144,9 @@ def main():
                     help='skip the C20H42 / def2-TZVP (f shells) leg')
     ap.add_argument('--no-scf', action='store_true',
                     help='skip the device SCF leg (config 1, mixed vs FP64)')
+    ap.add_argument('--scf-batched', type=int, default=0, metavar='N',
+                    help='add the batched-SCF leg over N water clusters (config 4; '
+                         'minutes for N = 64)')
     ap.add_argument('--scf-c20', action='store_true',
                     help='add the C20H42 / def2-TZVP staged SCF leg (config 3; '
                          'minutes: its plain FP64 run is the reference energy)')
@@ -1266,6 +1327,8 @@ def main():
     torch.cuda.empty_cache()
     scf = None if (args.no_scf or world > 1) else scf_timing(torch)
     scf_c20 = scf_c20_timing(torch) if (args.scf_c20 and world == 1) else None
+    scf_batched = (scf_batched_timing(torch, args.scf_batched)
+                   if (args.scf_batched > 0 and world == 1) else None)
     torch.cuda.empty_cache()
     parity = None if args.no_parity else parity_vs_oracle(mol, g, dm, eng, torch, 3000)
 
@@ -1298,6 +1361,7 @@ def main():
             'alkane_c20_tzvp': alk,
             'scf': scf,
             'scf_c20h42_tzvp': scf_c20,
+            'scf_batched': scf_batched,
             'reference_gpu': refgpu,
             'parity_vs_fp64_oracle': parity,
             'clocks': clocks.summary(),

@@ -217,7 +217,10 @@ int wb_cosx_get_k_fp64(wb_cosx* h, const double* coords, const double* weights,
  * wb_cosx_batch_run takes one density per molecule (qd[m], (nao_m,
  * nao_m) row-major) and writes nomega unsymmetrised K matrices per
  * molecule to k_out[m], as wb_cosx_get_k_multi does (omega j at k_out[m]
- * + j nao_m^2).  A run makes no allocation and, with stats == NULL, no
+ * + j nao_m^2).  qd[m] == NULL leaves molecule m out of this run (its
+ * F is zero, so its screen keeps no task; k_out[m] may be NULL and is not
+ * written): the molecules of one plan can stand at different SCF stages.
+ * At least one molecule must be built.  A run makes no allocation and, with stats == NULL, no
  * host synchronisation, so it can be captured in a CUDA graph.  Each
  * molecule's K equals its wb_cosx_get_k_multi result when the handles
  * agree on the kernel variant of every class (the same elements and

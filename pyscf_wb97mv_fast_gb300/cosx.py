@@ -659,29 +659,36 @@ class CosxBatch:
 
     def run(self, qds, out=None, stats=False):
         """qds: one (nao, nao) FP64 device tensor per molecule -> a list of
-        (len(omegas), nao, nao) unsymmetrised K (out: the same, to reuse)."""
+        (len(omegas), nao, nao) unsymmetrised K (out: the same, to reuse).
+        A None density leaves its molecule out of the run (its entry of the
+        result is None)."""
         torch = _torch()
         n = len(self.engines)
         if len(qds) != n:
             raise ValueError('one density per molecule')
+        if all(q is None for q in qds):
+            raise ValueError('at least one density')
         if out is None:
-            out = [torch.empty((len(self.omegas), e.nao, e.nao), dtype=torch.float64,
-                               device=self.device) for e in self.engines]
+            out = [None if q is None else
+                   torch.empty((len(self.omegas), e.nao, e.nao), dtype=torch.float64,
+                               device=self.device) for q, e in zip(qds, self.engines)]
         P = _native.ctypes.c_void_p
-        qd_c = [e._dm_arg(q) for q, e in zip(qds, self.engines)]
+        qd_c = [None if q is None else e._dm_arg(q) for q, e in zip(qds, self.engines)]
         if len(out) != n:
             raise ValueError('one output per molecule')
-        for k, e in zip(out, self.engines):
-            device_out(k, 'out', torch.float64, e.device, (len(self.omegas), e.nao, e.nao))
+        for q, k, e in zip(qd_c, out, self.engines):
+            if q is not None:
+                device_out(k, 'out', torch.float64, e.device,
+                           (len(self.omegas), e.nao, e.nao))
         st = _native.WbCosxStats() if stats else None
         _native.check(_native.lib().wb_cosx_batch_run(
-            self._b, (P * n)(*[q.data_ptr() for q in qd_c]),
-            (P * n)(*[k.data_ptr() for k in out]), CosxEngine._stream(),
-            _native.ctypes.byref(st) if st is not None else None),
+            self._b, (P * n)(*[None if q is None else q.data_ptr() for q in qd_c]),
+            (P * n)(*[None if q is None else k.data_ptr() for q, k in zip(qd_c, out)]),
+            CosxEngine._stream(), _native.ctypes.byref(st) if st is not None else None),
             'wb_cosx_batch_run')
         if st is not None:
             self.last_stats = st.as_dict()
-        return out
+        return [None if q is None else k for q, k in zip(qd_c, out)]
 
     def close(self):
         if getattr(self, '_b', None):

@@ -1731,9 +1731,14 @@ int wb_cosx_batch_run(wb_cosx_batch* b, const double* const* qd,
                       double* const* k_out, void* stream, wb_cosx_stats* stats) {
     if (!b || !qd || !k_out)
         return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_batch_run: bad arguments");
-    for (int m = 0; m < b->nmol; ++m)
-        if (!qd[m] || !k_out[m])
-            return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_batch_run: null matrix");
+    int active = 0;
+    for (int m = 0; m < b->nmol; ++m) {
+        if (qd[m] && !k_out[m])
+            return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_batch_run: null output");
+        active += qd[m] ? 1 : 0;
+    }
+    if (!active)
+        return fail(WB_ERR_INVALID_ARGUMENT, "wb_cosx_batch_run: no molecule to build");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int nmol = b->nmol;
     int launches = 0;
@@ -1752,7 +1757,10 @@ int wb_cosx_batch_run(wb_cosx_batch* b, const double* const* qd,
                                     sizeof(unsigned long long) * kCounterWords, s));
         const double* X = at<double>(ws, L.X);
         float* F32 = at<float>(ws, L.F32);
-        if (b->gemm == WB_K_GEMM_OZAKI_BF16 && wb::ozaki_f_supported(nao)) {
+        if (!qd[m]) {
+            // an inactive molecule: F = 0, so its screen keeps no task
+            WB_CUDA(cudaMemsetAsync(F32, 0, sizeof(float) * (size_t)nao * ld, s));
+        } else if (b->gemm == WB_K_GEMM_OZAKI_BF16 && wb::ozaki_f_supported(nao)) {
             const int r = wb::ozaki_f_gemm(
                 h->cublas, X, qd[m], nao, ld, F32, b->scratch, s,
                 at<unsigned long long>(ws, L.counters) + 3 * wb::NCLASS);
@@ -1817,6 +1825,7 @@ int wb_cosx_batch_run(wb_cosx_batch* b, const double* const* qd,
     }
     // per molecule: G of each slot, then K
     for (int m = 0; m < nmol; ++m) {
+        if (!qd[m]) continue;
         wb_cosx* h = b->h[m];
         const WsLayout& L = b->L[m];
         void* ws = b->ws[m];

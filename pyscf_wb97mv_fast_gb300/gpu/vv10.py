@@ -167,6 +167,69 @@ def _prepare_dm(dm, hermi):
     return dm
 
 
+def vv10_prepare(eng, g, D, nlc_pars, gemm='fp64'):
+    """The steps of vv10_energy_fock before the double sum (the GGA density
+    on the NLC grid g, the threshold and the pointwise terms): a state for
+    vv10_finish; st['xyz'], st['q'], st['W0'], st['kappa'] are the double
+    sum's inputs (Vv10Kernel.kernel_sum or, for several molecules,
+    kernel_sum_batch).  gemm as in vv10_energy_fock."""
+    torch = _torch()
+    if gemm not in ('fp64', 'split64', 'fp32'):
+        raise ValueError("gemm must be 'fp64', 'split64' or 'fp32'")
+    n = g.n
+    ao = g.X[:, :, :n]
+    w = g.weights
+    if gemm == 'fp32':
+        T = eng.ozaki_f(g.X[0], D)[:, :n].to(torch.float64)
+    elif gemm == 'split64':
+        T = eng.ozaki_f(g.X[0], D, fp64=True)[:, :n]
+    else:
+        T = D @ ao[0]
+    rho0 = (T * ao[0]).sum(dim=0)
+    grad = 2.0 * torch.einsum('mp,dmp->dp', T, ao[1:4])
+    ind = rho0 >= THRESH
+    q, W0, kappa, dW0dR, dW0dG, dKdR, Beta = vv10_pointwise(
+        rho0[ind], grad[:, ind], w[ind], nlc_pars)
+    return dict(eng=eng, g=g, gemm=gemm, n=n, rho0=rho0, grad=grad, ind=ind,
+                xyz=g.coords[ind].to(torch.float32), q=q, W0=W0, kappa=kappa,
+                dW0dR=dW0dR, dW0dG=dW0dG, dKdR=dKdR, Beta=Beta)
+
+
+def vv10_finish(st, F, U, W):
+    """E_nl and V_nl from a vv10_prepare state and the double sums F, U, W
+    of its points."""
+    torch = _torch()
+    g, n, ind, w = st['g'], st['n'], st['ind'], st['g'].weights
+    ao = g.X[:, :, :n]
+    Beta = st['Beta']
+    dev = st['rho0'].device
+    exc = torch.zeros(n, dtype=torch.float64, device=dev)
+    v0 = torch.zeros_like(exc)
+    v1 = torch.zeros_like(exc)
+    exc[ind] = Beta + 0.5 * F
+    v0[ind] = Beta + F + 1.5 * (U * st['dKdR'] + W * st['dW0dR'])
+    v1[ind] = 1.5 * W * st['dW0dG']
+    e_nl = (st['rho0'] * w * exc).sum()
+    grad = st['grad']
+    if st['gemm'] != 'fp64':
+        # G = 1/2 v0 X0 + sum_d 2 v1 grad_d X_d, then X0^T (w o G), G FP64
+        # or rounded once to FP32
+        vv = torch.empty((4, n), dtype=torch.float64, device=dev)
+        vv[0] = 0.5 * v0
+        vv[1:4] = 2.0 * v1[None, :] * grad
+        dt = torch.float32 if st['gemm'] == 'fp32' else torch.float64
+        G = torch.zeros_like(g.X[0], dtype=dt)
+        G[:, :n] = torch.einsum('dmp,dp->mp', ao, vv).to(dt)
+        vmat = st['eng'].ozaki_k(g.X[0], G, w)
+        return e_nl, vmat + vmat.T
+    wv = torch.empty((4, n), dtype=torch.float64, device=dev)
+    wv[0] = 0.5 * v0 * w
+    wv[1:4] = 2.0 * v1[None, :] * grad * w[None, :]
+    aow = torch.einsum('dmp,dp->mp', ao, wv)
+    vmat = ao[0] @ aow.T
+    return e_nl, vmat + vmat.T
+
+
 def vv10_energy_fock(eng, g, D, nlc_pars, kernel=None, fp32=False, gemm='fp64'):
     """E_nl and V_nl of one density on a device grid, all on the device:
     g holds coordinates (engine frame), weights and the deriv-1 AO values
@@ -183,51 +246,10 @@ def vv10_energy_fock(eng, g, D, nlc_pars, kernel=None, fp32=False, gemm='fp64'):
       'fp32'    the split with D X rounded once to FP32 and the Fock side
                 from an FP32-rounded G, the SCF's FP32 stages (fp32=True
                 is the same)."""
-    torch = _torch()
-    if fp32:
-        gemm = 'fp32'
-    if gemm not in ('fp64', 'split64', 'fp32'):
-        raise ValueError("gemm must be 'fp64', 'split64' or 'fp32'")
+    st = vv10_prepare(eng, g, D, nlc_pars, 'fp32' if fp32 else gemm)
     kernel = kernel or Vv10Kernel(0.0)
-    n = g.n
-    ao = g.X[:, :, :n]
-    w = g.weights
-    if gemm == 'fp32':
-        T = eng.ozaki_f(g.X[0], D)[:, :n].to(torch.float64)
-    elif gemm == 'split64':
-        T = eng.ozaki_f(g.X[0], D, fp64=True)[:, :n]
-    else:
-        T = D @ ao[0]
-    rho0 = (T * ao[0]).sum(dim=0)
-    grad = 2.0 * torch.einsum('mp,dmp->dp', T, ao[1:4])
-    ind = rho0 >= THRESH
-    q, W0, kappa, dW0dR, dW0dG, dKdR, Beta = vv10_pointwise(
-        rho0[ind], grad[:, ind], w[ind], nlc_pars)
-    F, U, W = kernel.kernel_sum(g.coords[ind].to(torch.float32), q, W0, kappa)
-    exc = torch.zeros(n, dtype=torch.float64, device=D.device)
-    v0 = torch.zeros_like(exc)
-    v1 = torch.zeros_like(exc)
-    exc[ind] = Beta + 0.5 * F
-    v0[ind] = Beta + F + 1.5 * (U * dKdR + W * dW0dR)
-    v1[ind] = 1.5 * W * dW0dG
-    e_nl = (rho0 * w * exc).sum()
-    if gemm != 'fp64':
-        # G = 1/2 v0 X0 + sum_d 2 v1 grad_d X_d, then X0^T (w o G), G FP64
-        # or rounded once to FP32
-        vv = torch.empty((4, n), dtype=torch.float64, device=D.device)
-        vv[0] = 0.5 * v0
-        vv[1:4] = 2.0 * v1[None, :] * grad
-        dt = torch.float32 if gemm == 'fp32' else torch.float64
-        G = torch.zeros_like(g.X[0], dtype=dt)
-        G[:, :n] = torch.einsum('dmp,dp->mp', ao, vv).to(dt)
-        vmat = eng.ozaki_k(g.X[0], G, w)
-        return e_nl, vmat + vmat.T
-    wv = torch.empty((4, n), dtype=torch.float64, device=D.device)
-    wv[0] = 0.5 * v0 * w
-    wv[1:4] = 2.0 * v1[None, :] * grad * w[None, :]
-    aow = torch.einsum('dmp,dp->mp', ao, wv)
-    vmat = ao[0] @ aow.T
-    return e_nl, vmat + vmat.T
+    F, U, W = kernel.kernel_sum(st['xyz'], st['q'], st['W0'], st['kappa'])
+    return vv10_finish(st, F, U, W)
 
 
 def gpu_nr_nlc_vxc(ctx, ni, mol, grids, xc_code, dm, relativity=0, hermi=1,

@@ -259,6 +259,7 @@ class DeviceRKS:
             from pyscf_wb97mv_fast_gb300.grids import build_grids
             g = DeviceGrid(self.eng, build_grids(self.mol, level=level),
                            deriv=1 if kind == 'nlc' else 0)
+            g.level = level
             self._grid_cache[key] = g
         return g
 
@@ -322,7 +323,11 @@ class DeviceRKS:
             self.profile[name] = self.profile.get(name, 0.0) + now - self._t_last
         self._t_last = now
 
-    def fock(self, D, grids, fp64, base=None, inc32=False):
+    def gemm_mode(self, fp64, inc32):
+        """The quadrature-GEMM form of a Fock build (see fock)."""
+        return 'fp32' if not fp64 else ('split64' if inc32 else 'fp64')
+
+    def fock(self, D, grids, fp64, base=None, inc32=False, k=None, vv10=None):
         """(E, F, parts, base') for density D with grids = dict(xc=, sgx=,
         nlc=) DeviceGrids (nlc may be None).
 
@@ -338,19 +343,24 @@ class DeviceRKS:
         form of the bf16 split (42 bits of the row / column maxima, FP64
         operands and results).  Without it (the plain FP64 form) only K_x
         is incremental, in FP64, and every GEMM is a plain FP64 GEMM.
-        base' is the base to keep (a new one after a full build)."""
+        base' is the base to keep (a new one after a full build).
+
+        k (the symmetrised exchange matrices of D, or of D - base['D'] for
+        an incremental build, built the way this build would) and vv10
+        ((E_nl, V_nl) of D on the NLC grid) come from a batch of molecules
+        (BatchedRKS) instead of being built here."""
         torch = _torch()
         f = self.functional
         gs, gx = grids['sgx'], grids['xc']
-        gemm = 'fp32' if not fp64 else ('split64' if inc32 else 'fp64')
+        gemm = self.gemm_mode(fp64, inc32)
         self._tick(None)
         full = base is None
         dD = None if full else D - base['D']
         if full:
-            K = self.k_matrices(D, gs, fp64)
+            K = self.k_matrices(D, gs, fp64) if k is None else k
             Kx = f.alpha * K[0] + f.beta * K[1]
         else:
-            dK = self.k_matrices(dD, gs, fp64 and not inc32)
+            dK = self.k_matrices(dD, gs, fp64 and not inc32) if k is None else k
             Kx = base['Kx'] + (f.alpha * dK[0] + f.beta * dK[1])
         self._tick('k')
         if full or not inc32:
@@ -368,7 +378,9 @@ class DeviceRKS:
         exc = (gx.weights * e).sum()
         Vxc = self._vmat(gx, v, gemm)
         self._tick('xc')
-        if grids.get('nlc') is not None and f.nlc:
+        if vv10 is not None:
+            enl, Vnl = vv10
+        elif grids.get('nlc') is not None and f.nlc:
             enl, Vnl = self.vv10(D, grids['nlc'], gemm)
         else:
             enl, Vnl = torch.zeros((), dtype=torch.float64, device=self.device), 0.0
@@ -413,72 +425,20 @@ class DeviceRKS:
         staging/schedule.py:335-346).  FP32 stages always build in full.
         profile: per-part seconds in out['profile'] (synchronises)."""
         torch = _torch()
-        if precision not in ('mixed', 'fp64'):
-            raise ValueError("precision must be 'mixed' or 'fp64'")
         torch.cuda.synchronize(self.device)
-        t0 = time.perf_counter()
-        staged = precision == 'mixed'
-        if staged:
-            plan = plan or StagePlan(fp64_final=True, tau_fp64=1e-6, tau_fp64_g=1e-4)
-        D = self.core_guess() if dm0 is None else torch.as_tensor(
-            dm0, dtype=torch.float64, device=self.device)
-        stage, fp64 = (0, False) if staged else (2, True)
-        diis = _Cdiis(diis_space)
-        hist, stage_end = [], []
-        e_last, converged = None, False
-        base, since_full = None, 0
+        run = ScfRun(self, precision, dm0, conv_tol, conv_tol_grad, max_cycle,
+                     diis_space, plan, reference_energy, incremental, rebuild_every)
         self.profile = {} if profile else None
-        for cycle in range(max_cycle):
-            grids = self._stage_grids(stage)
-            use = (base if incremental and fp64 and since_full < rebuild_every
-                   else None)
-            E, F, parts, base = self.fock(D, grids, fp64, base=use,
-                                          inc32=staged)
-            since_full = 1 if use is None else since_full + 1
-            comm = self._commutator(F, D)
-            gnorm = float(torch.linalg.norm(comm))
-            Ef = float(E)
-            dE = math.inf if e_last is None else abs(Ef - e_last)
-            hist.append(dict(cycle=cycle, stage=stage, fp64=fp64, e=Ef, dE=dE,
-                             gnorm=gnorm, t=time.perf_counter() - t0))
-            if self.verbose:
-                print('cycle %2d S%d %s E=%.12f dE=%.2e |g|=%.2e'
-                      % (cycle, stage, 'fp64' if fp64 else 'fp32', Ef, dE, gnorm))
-            may_stop = (not staged) or plan.may_converge
-            if may_stop and dE < conv_tol and gnorm < conv_tol_grad:
-                converged = True
-                break
-            decision = plan.after_cycle(dE, gnorm) if staged else None
-            if decision is not None:
-                stage_end.append(dict(stage=stage, fp64=fp64, e=Ef, cycles=cycle + 1))
-                if decision[0] == 'stage':
-                    stage = decision[1]
-                else:
-                    fp64 = True
-                diis = _Cdiis(diis_space)      # the functional changed
-                e_last = None
-                base = None                    # full rebuild after a switch
-                D = self._diag(F)[0]
-                continue
-            e_last = Ef
-            Fd = diis.update(F, comm)
-            D = self._diag(Fd)[0]
+        while not run.done:
+            req = run.request()
+            E, F, parts, base = self.fock(run.D, req['grids'], req['fp64'],
+                                          base=req['base'], inc32=run.staged)
+            run.advance(E, F, parts, base)
         torch.cuda.synchronize(self.device)
-        wall = time.perf_counter() - t0
-        out = dict(e_tot=hist[-1]['e'], converged=converged, cycles=len(hist),
-                   wall=wall, setup_s=self.t_setup, history=hist,
-                   precision=precision, stages=stage_end,
-                   parts={k: float(v) for k, v in parts.items()}, dm=D,
-                   incremental=bool(incremental))
+        out = run.result()
         if self.profile is not None:
             out['profile'] = dict(self.profile)
             self.profile = None
-        if reference_energy is not None:
-            out['error_vs_reference'] = out['e_tot'] - float(reference_energy)
-            for h in hist:
-                h['err'] = h['e'] - float(reference_energy)
-            for s in stage_end:
-                s['err'] = s['e'] - float(reference_energy)
         return out
 
     def _stage_grids(self, stage):
@@ -493,6 +453,121 @@ class DeviceRKS:
         return dict(xc=self.grid('xc', self.levels['xc']),
                     sgx=self.grid('sgx', self.levels['sgx']),
                     nlc=None if nlc is None else self.grid('nlc', nlc))
+
+
+class ScfRun:
+    """One SCF between its Fock builds: the loop of DeviceRKS.kernel cut
+    where the builds of several molecules can be shared (BatchedRKS steps
+    many runs at once).  request() names this cycle's build; advance()
+    takes its result (E, F) and does the rest of the cycle: the
+    commutator, the convergence test, the stage plan's switches, DIIS and
+    the diagonalisation.  The caller synchronises the device before
+    construction (the wall clock starts there)."""
+
+    def __init__(self, rks, precision='mixed', dm0=None, conv_tol=1e-9,
+                 conv_tol_grad=1e-5, max_cycle=80, diis_space=8, plan=None,
+                 reference_energy=None, incremental=True, rebuild_every=8):
+        torch = _torch()
+        if precision not in ('mixed', 'fp64'):
+            raise ValueError("precision must be 'mixed' or 'fp64'")
+        self.t0 = time.perf_counter()
+        self.rks = rks
+        self.precision = precision
+        self.staged = precision == 'mixed'
+        self.plan = None
+        if self.staged:
+            self.plan = plan or StagePlan(fp64_final=True, tau_fp64=1e-6,
+                                          tau_fp64_g=1e-4)
+        self.D = rks.core_guess() if dm0 is None else torch.as_tensor(
+            dm0, dtype=torch.float64, device=rks.device)
+        self.stage, self.fp64 = (0, False) if self.staged else (2, True)
+        self.diis_space = diis_space
+        self.diis = _Cdiis(diis_space)
+        self.hist, self.stage_end = [], []
+        self.e_last, self.converged, self.done = None, False, False
+        self.base, self.since_full, self._use = None, 0, None
+        self.conv_tol, self.conv_tol_grad = conv_tol, conv_tol_grad
+        self.max_cycle = int(max_cycle)
+        self.incremental, self.rebuild_every = bool(incremental), int(rebuild_every)
+        self.reference_energy = reference_energy
+        self.cycle = 0
+        self.parts = {}
+        self.done = self.max_cycle <= 0
+
+    def request(self):
+        """This cycle's build: grids, fp64, the incremental base (or None),
+        and the exchange build it needs -- k_mode 'fp32' (the FP32 class
+        kernels) or 'fp64' (the plain FP64 form) of k_dm, the density for a
+        full build or its change from the base for an incremental one."""
+        grids = self.rks._stage_grids(self.stage)
+        use = (self.base if self.incremental and self.fp64
+               and self.since_full < self.rebuild_every else None)
+        self._use = use
+        if use is None:
+            k_mode, k_dm = ('fp64' if self.fp64 else 'fp32'), self.D
+        else:
+            k_mode = 'fp64' if (self.fp64 and not self.staged) else 'fp32'
+            k_dm = self.D - use['D']
+        return dict(grids=grids, fp64=self.fp64, base=use, k_mode=k_mode, k_dm=k_dm,
+                    gemm=self.rks.gemm_mode(self.fp64, self.staged))
+
+    def advance(self, E, F, parts, base):
+        torch = _torch()
+        rks = self.rks
+        self.base = base
+        self.since_full = 1 if self._use is None else self.since_full + 1
+        self.parts = parts
+        comm = rks._commutator(F, self.D)
+        gnorm = float(torch.linalg.norm(comm))
+        Ef = float(E)
+        dE = math.inf if self.e_last is None else abs(Ef - self.e_last)
+        cycle = self.cycle
+        self.cycle += 1
+        self.hist.append(dict(cycle=cycle, stage=self.stage, fp64=self.fp64, e=Ef,
+                              dE=dE, gnorm=gnorm, t=time.perf_counter() - self.t0))
+        if rks.verbose:
+            print('cycle %2d S%d %s E=%.12f dE=%.2e |g|=%.2e'
+                  % (cycle, self.stage, 'fp64' if self.fp64 else 'fp32', Ef, dE, gnorm))
+        may_stop = (not self.staged) or self.plan.may_converge
+        if may_stop and dE < self.conv_tol and gnorm < self.conv_tol_grad:
+            self.converged = self.done = True
+            return
+        decision = self.plan.after_cycle(dE, gnorm) if self.staged else None
+        if decision is not None:
+            self.stage_end.append(dict(stage=self.stage, fp64=self.fp64, e=Ef,
+                                       cycles=cycle + 1))
+            if decision[0] == 'stage':
+                self.stage = decision[1]
+            else:
+                self.fp64 = True
+            self.diis = _Cdiis(self.diis_space)      # the functional changed
+            self.e_last = None
+            self.base = None                         # full rebuild after a switch
+            self.D = rks._diag(F)[0]
+        else:
+            self.e_last = Ef
+            Fd = self.diis.update(F, comm)
+            self.D = rks._diag(Fd)[0]
+        if self.cycle >= self.max_cycle:
+            self.done = True
+
+    def result(self):
+        """The run's result dict (wall from construction to now)."""
+        wall = time.perf_counter() - self.t0
+        hist = self.hist
+        out = dict(e_tot=hist[-1]['e'] if hist else None, converged=self.converged,
+                   cycles=len(hist), wall=wall, setup_s=self.rks.t_setup, history=hist,
+                   precision=self.precision, stages=self.stage_end,
+                   parts={k: float(v) for k, v in self.parts.items()}, dm=self.D,
+                   incremental=self.incremental)
+        ref = self.reference_energy
+        if ref is not None and hist:
+            out['error_vs_reference'] = out['e_tot'] - float(ref)
+            for h in hist:
+                h['err'] = h['e'] - float(ref)
+            for st in self.stage_end:
+                st['err'] = st['e'] - float(ref)
+        return out
 
 
 class _Cdiis:
@@ -531,3 +606,118 @@ class _Cdiis:
         for ci, Fi in zip(c, self.F):
             out += float(ci) * Fi
         return out
+
+
+class BatchedRKS:
+    """The SCFs of several molecules in lockstep on one GPU.  Every cycle
+    the exchange builds that run on the FP32 class kernels -- the FP32
+    stages' full builds and the FP64 tail's increments -- of all molecules
+    are one batched build (CosxBatch: one launch per class kernel over the
+    molecules, per SGX grid level), and the VV10 double sums of all
+    molecules one launch (Vv10Kernel.kernel_sum_batch); the plain-FP64
+    exchange builds (the tail's full bases), J, the semilocal XC, Fock
+    assembly, DIIS and the diagonalisation run per molecule.  Each molecule
+    follows its own stage plan and stops at its own convergence; a
+    molecule that is done, or whose build this cycle is not batched, is
+    left out of the batch run.  The batched builds are bitwise the
+    per-molecule ones, so each molecule's SCF is the one DeviceRKS runs
+    alone.  The arguments after mols are those of DeviceRKS, for every
+    molecule."""
+
+    def __init__(self, mols, functional=None, levels=None, coarse=None,
+                 k_tile_tol=1e-11, j_tol=1e-14, device=None, stage_levels=None):
+        if not mols:
+            raise ValueError('no molecule')
+        self.rks = [DeviceRKS(m, functional, levels, coarse, k_tile_tol, j_tol,
+                              device=device, stage_levels=stage_levels) for m in mols]
+        self.k_tile_tol = float(k_tile_tol)
+        self._kb = {}
+
+    def _k_batch(self, level):
+        """The batched exchange build on the SGX grids of one level (its own
+        engines: a batch owns its engines' workspaces while it lives)."""
+        from pyscf_wb97mv_fast_gb300.cosx import CosxBatch, CosxEngine
+        b = self._kb.get(level)
+        if b is None:
+            engines = [CosxEngine(r.mol, device=r.device) for r in self.rks]
+            grids = []
+            for r in self.rks:
+                g = r.grid('sgx', level)
+                grids.append((g.coords, g.weights))
+            b = CosxBatch(engines, grids, self.rks[0].functional.omegas,
+                          tile_tol=self.k_tile_tol)
+            self._kb[level] = b
+        return b
+
+    def kernel(self, precision='mixed', reference_energies=None, **kw):
+        """Run every molecule's SCF (precision and the keywords of
+        DeviceRKS.kernel, for every molecule); returns one result dict per
+        molecule, plus out-of-band 'wall' (the whole batch) in each."""
+        from pyscf_wb97mv_fast_gb300.gpu.vv10 import Vv10Kernel, vv10_finish, vv10_prepare
+        torch = _torch()
+        dev = self.rks[0].device
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        refs = reference_energies or [None] * len(self.rks)
+        runs = [ScfRun(r, precision, reference_energy=e, **kw)
+                for r, e in zip(self.rks, refs)]
+        vv = Vv10Kernel(0.0)
+        n = len(runs)
+        batched_builds = 0
+        while not all(r.done for r in runs):
+            act = [i for i in range(n) if not runs[i].done]
+            req = {i: runs[i].request() for i in act}
+            # exchange: the FP32-kernel builds batched per SGX level
+            K = {}
+            by_level = {}
+            for i in act:
+                if req[i]['k_mode'] == 'fp32':
+                    by_level.setdefault(req[i]['grids']['sgx'].level, []).append(i)
+                else:
+                    K[i] = self.rks[i].k_matrices(req[i]['k_dm'], req[i]['grids']['sgx'],
+                                                  True)
+            for level, idx in by_level.items():
+                qds = [req[i]['k_dm'] if i in idx else None for i in range(n)]
+                out = self._k_batch(level).run(qds)
+                batched_builds += 1
+                for i in idx:
+                    K[i] = 0.5 * (out[i] + out[i].transpose(1, 2))
+            # VV10: the double sums of every molecule with an NLC grid in one
+            # launch
+            st = {}
+            for i in act:
+                r = self.rks[i]
+                g = req[i]['grids'].get('nlc')
+                if g is not None and r.functional.nlc:
+                    st[i] = vv10_prepare(r.eng, g, runs[i].D, r.functional.nlc,
+                                         req[i]['gemm'])
+            V = {}
+            if st:
+                idx = sorted(st)
+                F, U, W = vv.kernel_sum_batch([st[i]['xyz'] for i in idx],
+                                              [st[i]['q'] for i in idx],
+                                              [st[i]['W0'] for i in idx],
+                                              [st[i]['kappa'] for i in idx])
+                for j, i in enumerate(idx):
+                    V[i] = vv10_finish(st[i], F[j], U[j], W[j])
+            for i in act:
+                r = self.rks[i]
+                E, Fk, parts, base = r.fock(runs[i].D, req[i]['grids'], req[i]['fp64'],
+                                            base=req[i]['base'], inc32=runs[i].staged,
+                                            k=K[i], vv10=V.get(i))
+                runs[i].advance(E, Fk, parts, base)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+        outs = [r.result() for r in runs]
+        for o in outs:
+            o['batch_wall'] = wall
+            o['batched_exchange_builds'] = batched_builds
+        return outs
+
+    def close(self):
+        for b in self._kb.values():
+            b.close()
+        self._kb = {}
+        for r in self.rks:
+            r.eng.close()
+
