@@ -1044,6 +1044,54 @@ def scf_batched_timing(torch, nmol=64, seed=4):
     return out
 
 
+def serving_scf_timing(torch, n_req=12, rates=(2.0, 8.0), slots=4, seed=7):
+    """Config-5 shape with whole SCF solves as requests (ScfServer): a
+    seeded mix of water clusters (4-12 waters, synthetic def2-SVP) and
+    n-alkanes (C6-C10, synthetic def2-TZVP), XC level 1 / SGX 0 / VV10 0.
+    The plain per-request form solves them one after another (one slot);
+    the served form takes Poisson arrivals into `slots` overlapping solves.
+    Reports solves/s and p50 / p99 time to the converged energy, and
+    whether every served energy is bitwise its plain solve's."""
+    from pyscf_wb97mv_fast_gb300.basis import Molecule
+    from pyscf_wb97mv_fast_gb300.serving import ScfServer, poisson_arrivals, replay
+    from pyscf_wb97mv_fast_gb300.systems import alkane, water_cluster
+    rng = np.random.default_rng(seed)
+    mols, names = [], []
+    for i in range(n_req):
+        if rng.random() < 0.5:
+            n = int(rng.integers(4, 13))
+            mols.append(Molecule.build(water_cluster(n, box=max(5.0, 3.2 * n ** (1 / 3)),
+                                                     seed=500 + i), 'synthetic-svp'))
+            names.append('water%d/svp' % n)
+        else:
+            c = int(rng.integers(6, 11))
+            mols.append(Molecule.build(alkane(c), 'synthetic-tzvp'))
+            names.append('C%dH%d/tzvp' % (c, 2 * c + 2))
+    levels, coarse = dict(xc=1, sgx=0, nlc=0), dict(xc=0, sgx=0)
+    warm = ScfServer(slots=1, levels=levels, coarse=coarse)
+    warm.submit(mols[0]).result()
+    warm.close()
+    plain = ScfServer(slots=1, levels=levels, coarse=coarse)
+    pf = [plain.submit(m) for m in mols]
+    pr = [f.result() for f in pf]
+    plain.close()
+    out = {'requests': names, 'levels': levels, 'coarse': coarse,
+           'plain': plain.summary(), 'served': {}}
+    for rate in rates:
+        srv = ScfServer(slots=slots, levels=levels, coarse=coarse)
+        arr = poisson_arrivals(n_req, rate, seed)
+        futs = replay([lambda m=m: srv.submit(m) for m in mols], arr)
+        res = [f.result() for f in futs]
+        srv.close()
+        sm = srv.summary()
+        sm['rate_per_s'] = rate
+        sm['bitwise_equal_to_plain'] = all(a['e_tot'] == b['e_tot']
+                                           for a, b in zip(pr, res))
+        sm['all_converged'] = all(r['converged'] for r in res)
+        out['served']['rate=%g' % rate] = sm
+    return out
+
+
 def run_sample(oracle, mol, g, dm, idx):
     coords = g.coords[idx]
     X = oracle.ao_eval(mol, coords)
@@ -1147,6 +1195,8 @@ def main():
     ap.add_argument('--scf-batched', type=int, default=0, metavar='N',
                     help='add the batched-SCF leg over N water clusters (config 4; '
                          'minutes for N = 64)')
+    ap.add_argument('--serving-scf', action='store_true',
+                    help='add the served-SCF leg (whole SCF solves as requests)')
     ap.add_argument('--scf-c20', action='store_true',
                     help='add the C20H42 / def2-TZVP staged SCF leg (config 3; '
                          'minutes: its plain FP64 run is the reference energy)')
@@ -1329,6 +1379,7 @@ def main():
     scf_c20 = scf_c20_timing(torch) if (args.scf_c20 and world == 1) else None
     scf_batched = (scf_batched_timing(torch, args.scf_batched)
                    if (args.scf_batched > 0 and world == 1) else None)
+    serving_scf = serving_scf_timing(torch) if (args.serving_scf and world == 1) else None
     torch.cuda.empty_cache()
     parity = None if args.no_parity else parity_vs_oracle(mol, g, dm, eng, torch, 3000)
 
@@ -1362,6 +1413,7 @@ def main():
             'scf': scf,
             'scf_c20h42_tzvp': scf_c20,
             'scf_batched': scf_batched,
+            'serving_scf': serving_scf,
             'reference_gpu': refgpu,
             'parity_vs_fp64_oracle': parity,
             'clocks': clocks.summary(),

@@ -317,7 +317,7 @@ class DeviceRKS:
         if self.profile is None:
             return
         torch = _torch()
-        torch.cuda.synchronize(self.device)
+        torch.cuda.current_stream(self.device).synchronize()
         now = time.perf_counter()
         if name is not None:
             self.profile[name] = self.profile.get(name, 0.0) + now - self._t_last
@@ -425,7 +425,9 @@ class DeviceRKS:
         staging/schedule.py:335-346).  FP32 stages always build in full.
         profile: per-part seconds in out['profile'] (synchronises)."""
         torch = _torch()
-        torch.cuda.synchronize(self.device)
+        # the current stream only: solves on other streams keep running
+        stream = torch.cuda.current_stream(self.device)
+        stream.synchronize()
         run = ScfRun(self, precision, dm0, conv_tol, conv_tol_grad, max_cycle,
                      diis_space, plan, reference_energy, incremental, rebuild_every)
         self.profile = {} if profile else None
@@ -434,7 +436,7 @@ class DeviceRKS:
             E, F, parts, base = self.fock(run.D, req['grids'], req['fp64'],
                                           base=req['base'], inc32=run.staged)
             run.advance(E, F, parts, base)
-        torch.cuda.synchronize(self.device)
+        stream.synchronize()
         out = run.result()
         if self.profile is not None:
             out['profile'] = dict(self.profile)
@@ -656,7 +658,8 @@ class BatchedRKS:
         from pyscf_wb97mv_fast_gb300.gpu.vv10 import Vv10Kernel, vv10_finish, vv10_prepare
         torch = _torch()
         dev = self.rks[0].device
-        torch.cuda.synchronize(dev)
+        stream = torch.cuda.current_stream(dev)
+        stream.synchronize()
         t0 = time.perf_counter()
         refs = reference_energies or [None] * len(self.rks)
         runs = [ScfRun(r, precision, reference_energy=e, **kw)
@@ -706,7 +709,7 @@ class BatchedRKS:
                                             base=req[i]['base'], inc32=runs[i].staged,
                                             k=K[i], vv10=V.get(i))
                 runs[i].advance(E, Fk, parts, base)
-        torch.cuda.synchronize(dev)
+        stream.synchronize()
         wall = time.perf_counter() - t0
         outs = [r.result() for r in runs]
         for o in outs:

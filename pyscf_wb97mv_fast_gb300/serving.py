@@ -1,4 +1,5 @@
-"""Continuous batching of COSX exchange builds on one GPU.
+"""Continuous batching of COSX exchange builds, and of whole SCF solves
+(ScfServer), on one GPU.
 
 The reference runs one SCF at a time.  Batch throughput is an explicit
 non-goal there (docs/design.en.md:44), and its K builder serves one
@@ -495,6 +496,121 @@ class ExchangeServer:
             # the workspace goes back to the allocator's cache for other builds
             eng._ws = None
         return out.numpy()
+
+    def close(self):
+        self._sched.close(wait=True)
+
+    def summary(self):
+        out = latency_summary(self.futures)
+        out['slots'] = self._sched.slots
+        out['budget_bytes'] = self._sched.budget
+        out['max_concurrent'] = self._sched.max_running
+        out['max_bytes_admitted'] = self._sched.max_used
+        return out
+
+
+class _ScfJob:
+    """One SCF solve request (Scheduler job)."""
+
+    def __init__(self, mol, footprint, reference_energy, precision, tag):
+        self.mol = mol
+        self.footprint = int(footprint)
+        self.reference_energy = reference_energy
+        self.precision = precision
+        self.key = ('scf', tag)
+
+
+# grid points per atom of this package's grids by level (Becke-partitioned
+# atom grids; measured on water clusters and alkanes, rounded up)
+_POINTS_PER_ATOM = {0: 1500, 1: 3100, 2: 5200, 3: 12000, 4: 24000}
+
+
+class ScfServer:
+    """Continuous batching of whole SCF solves on one GPU.
+
+    A request is one molecule; its solve (DeviceRKS.kernel, the staged
+    mixed form by default) keeps the density, the DIIS history, the grids
+    and their AO values on the device from its first Fock build to the
+    converged energy.  Requests that arrive while others run are admitted
+    as soon as a slot and their device-memory footprint are free (the
+    Scheduler: first fit in arrival order, one host thread and CUDA stream
+    per slot), so the solves of different molecules overlap on the device.
+    Every kernel of a solve has a fixed summation order and the solves
+    synchronise their own streams only, so a molecule's energy is bitwise
+    the same alone and in the mix.
+
+    levels / coarse / stage_levels: the grids of every solve (as for
+    DeviceRKS).  budget: device bytes for running solves (default 60 % of
+    the free device memory at start-up)."""
+
+    def __init__(self, device=0, slots=4, budget=None, levels=None, coarse=None,
+                 stage_levels=None, k_tile_tol=1e-11):
+        import torch
+        self.device = torch.device('cuda', device if isinstance(device, int)
+                                   else torch.device(device).index or 0)
+        if budget is None:
+            free, _ = torch.cuda.mem_get_info(self.device)
+            budget = int(0.6 * free)
+        self.levels, self.coarse, self.stage_levels = levels, coarse, stage_levels
+        self.k_tile_tol = float(k_tile_tol)
+        self._streams = [torch.cuda.Stream(device=self.device) for _ in range(slots)]
+        self._sched = Scheduler(self._run, slots=slots, budget=budget)
+        self._n = 0
+        self.futures = []
+
+    @property
+    def scheduler(self):
+        return self._sched
+
+    def footprint(self, mol):
+        """Device bytes of one solve (an upper estimate): the AO values of
+        its XC and SGX grids and the deriv-1 values of its NLC grid (FP64),
+        the exchange build's workspace (about 40 bytes per AO and SGX
+        point) and the pair data."""
+        from pyscf_wb97mv_fast_gb300.scf import DEFAULT_COARSE, DEFAULT_FINAL
+        if self.stage_levels is not None:
+            lv = {k: max(x for x in v if x is not None) if any(x is not None for x in v)
+                  else None for k, v in self.stage_levels.items()}
+        else:
+            lv = dict(DEFAULT_FINAL, **(self.levels or {}))
+        natm = int(mol.natm)
+        pts = {k: (0 if v is None else _POINTS_PER_ATOM.get(int(v), 24000) * natm)
+               for k, v in lv.items()}
+        nao = int(mol.nao)
+        xc_c = dict(DEFAULT_COARSE, **(self.coarse or {}))['xc']
+        ao = 8 * nao * (pts['xc'] + pts['sgx'] + 4 * pts['nlc'] +
+                        _POINTS_PER_ATOM.get(int(xc_c), 0) * natm)
+        return ao + 40 * nao * pts['sgx'] + 64 * nao * nao + (64 << 20)
+
+    def submit(self, mol, reference_energy=None, precision='mixed', deadline=None):
+        """Queue the solve of mol (a Molecule); returns its Future, whose
+        result() is the solve's summary (e_tot, converged, cycles, wall,
+        error_vs_reference)."""
+        from pyscf_wb97mv_fast_gb300.cosx import as_molecule
+        mol = as_molecule(mol)
+        self._n += 1
+        fut = self._sched.submit(_ScfJob(mol, self.footprint(mol), reference_energy,
+                                         precision, self._n), deadline=deadline)
+        self.futures.append(fut)
+        return fut
+
+    def _run(self, job, slot):
+        import torch
+        from pyscf_wb97mv_fast_gb300.scf import DeviceRKS
+        stream = self._streams[slot]
+        with torch.cuda.device(self.device), torch.cuda.stream(stream):
+            rks = DeviceRKS(job.mol, levels=self.levels, coarse=self.coarse,
+                            stage_levels=self.stage_levels, k_tile_tol=self.k_tile_tol,
+                            device=self.device.index)
+            try:
+                r = rks.kernel(precision=job.precision,
+                               reference_energy=job.reference_energy)
+            finally:
+                rks.eng.close()
+        out = {k: r.get(k) for k in ('e_tot', 'converged', 'cycles', 'wall',
+                                     'error_vs_reference', 'precision')}
+        out['nao'] = int(job.mol.nao)
+        return out
 
     def close(self):
         self._sched.close(wait=True)

@@ -63,3 +63,23 @@ def test_batched_scf_reaches_the_oracle_energy_of_each_molecule():
     for r in res:
         assert r['converged']
         assert abs(r['error_vs_reference']) < 1e-8, r['error_vs_reference']
+
+
+def test_scf_server_solves_alone_and_in_the_mix_equal():
+    """ScfServer: whole SCF solves as requests, three slots overlapping on
+    the device; each molecule's energy is bitwise its solve alone."""
+    from pyscf_wb97mv_fast_gb300.scf import DeviceRKS
+    from pyscf_wb97mv_fast_gb300.serving import ScfServer
+    mols = _mols()
+    alone = [DeviceRKS(m, levels=LEVELS, coarse=COARSE).kernel()['e_tot'] for m in mols]
+    srv = ScfServer(slots=3, levels=LEVELS, coarse=COARSE)
+    try:
+        futs = [srv.submit(m) for m in mols]
+        res = [f.result(timeout=600) for f in futs]
+    finally:
+        srv.close()
+    for a, r in zip(alone, res):
+        assert r['converged']
+        assert r['e_tot'] == a
+    s = srv.summary()
+    assert s['requests'] == 3 and s['max_concurrent'] >= 2
