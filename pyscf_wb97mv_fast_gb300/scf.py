@@ -411,7 +411,7 @@ class DeviceRKS:
     # -- the loop --------------------------------------------------------------
     def kernel(self, precision='mixed', dm0=None, conv_tol=1e-9, conv_tol_grad=1e-5,
                max_cycle=80, diis_space=8, plan=None, reference_energy=None,
-               incremental=True, rebuild_every=8, profile=False):
+               incremental=True, rebuild_every=None, profile=False):
         """Run the SCF; returns a dict with e_tot, converged, cycles, wall
         (seconds, device-synchronised), per-cycle history and, for the
         staged form, the energy at the end of each stage.  precision:
@@ -419,10 +419,15 @@ class DeviceRKS:
         form on the final grids).  incremental: after a full FP64 build the
         next FP64 cycles build from it as a fixed base (``fock``): the
         staged form's tail adds FP32 increments of K, J and rho, the plain
-        FP64 form FP64 increments of K; a full rebuild every rebuild_every
-        cycles and at every stage or precision switch, as PySCF's direct
-        SCF does (the reference forces that rebuild on its switches,
-        staging/schedule.py:335-346).  FP32 stages always build in full.
+        FP64 form FP64 increments of K; a full rebuild at every stage or
+        precision switch (the reference forces that rebuild on its
+        switches, staging/schedule.py:335-346) and every rebuild_every
+        cycles -- by default 8 for the plain FP64 form, as PySCF's direct
+        SCF does, and never for the staged form's tail, whose increments
+        are built afresh each cycle from its one FP64 base (a rebuild there
+        only re-draws the screening error, about 1e-8 Ha on C20H42, and
+        costs a full FP64 exchange build).  FP32 stages always build in
+        full.
         profile: per-part seconds in out['profile'] (synchronises)."""
         torch = _torch()
         # the current stream only: solves on other streams keep running
@@ -468,10 +473,12 @@ class ScfRun:
 
     def __init__(self, rks, precision='mixed', dm0=None, conv_tol=1e-9,
                  conv_tol_grad=1e-5, max_cycle=80, diis_space=8, plan=None,
-                 reference_energy=None, incremental=True, rebuild_every=8):
+                 reference_energy=None, incremental=True, rebuild_every=None):
         torch = _torch()
         if precision not in ('mixed', 'fp64'):
             raise ValueError("precision must be 'mixed' or 'fp64'")
+        if rebuild_every is None:
+            rebuild_every = 8 if precision == 'fp64' else 1 << 30
         self.t0 = time.perf_counter()
         self.rks = rks
         self.precision = precision
