@@ -986,62 +986,74 @@ def scf_c20_timing(torch, n_carbon=20):
     return out
 
 
-def scf_batched_timing(torch, nmol=64, seed=4):
+def scf_batched_timing(torch, nmol=64, seed=4, wave=16):
     """Config 4: nmol seeded water clusters of n in {4..32} waters
     (uniform), synthetic def2-SVP, XC level 1 / SGX level 0 / VV10 level 0
     (S0 on XC 0 / SGX 0), every molecule a full SCF.  The plain FP64 form of
     each molecule (its own SCF, one after another) gives its FP64 reference
     energy; the mixed staged form runs one molecule at a time and batched
     (BatchedRKS: the FP32 exchange builds of all molecules in one batched
-    build per SGX level, their VV10 double sums in one launch).  Grids and
-    AO values are built by an untimed warm-up."""
+    build per SGX level, their VV10 double sums in one launch).  A batch
+    keeps every molecule's grids and AO values resident (about 3.5 GB for
+    a 20-water cluster), so the molecules run in waves of `wave`; walls
+    are summed over the waves.  Grids and AO values are built by an
+    untimed warm-up."""
     from pyscf_wb97mv_fast_gb300.basis import Molecule
     from pyscf_wb97mv_fast_gb300.scf import BatchedRKS
     from pyscf_wb97mv_fast_gb300.systems import water_cluster
     rng = np.random.default_rng(seed)
     sizes = [int(x) for x in rng.integers(4, 33, size=nmol)]
-    mols = [Molecule.build(water_cluster(n, box=max(5.0, 3.2 * n ** (1.0 / 3.0)),
-                                         seed=300 + i), 'synthetic-svp')
-            for i, n in enumerate(sizes)]
     levels, coarse = dict(xc=1, sgx=0, nlc=0), dict(xc=0, sgx=0)
-    b = BatchedRKS(mols, levels=levels, coarse=coarse)
-    b.kernel(precision='mixed', max_cycle=1)          # warm-up: grids, batches
-    for r in b.rks:
-        r.kernel(precision='fp64', max_cycle=1)
+    t64 = tseq = tb = 0.0
+    errs, conv, equal, cyc_m, cyc_f, nb, nao_tot = [], True, True, [], [], 0, 0
 
-    def seq(precision, refs=None):
+    def timed(fn):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        out = [r.kernel(precision=precision, reference_energy=None if refs is None
-                        else refs[i]) for i, r in enumerate(b.rks)]
+        out = fn()
         torch.cuda.synchronize()
         return out, time.perf_counter() - t0
 
-    r64, t64 = seq('fp64')
-    refs = [r['e_tot'] for r in r64]
-    rseq, tseq = seq('mixed', refs)
-    rb = b.kernel(precision='mixed', reference_energies=refs)
-    tb = rb[0]['batch_wall']
-    errs = [r['error_vs_reference'] for r in rb]
-    out = {'molecules': nmol, 'waters_per_cluster': sizes,
-           'levels': levels, 'coarse': coarse,
-           'nao_total': int(sum(r.mol.nao for r in b.rks)),
-           'reference': 'each molecule\'s plain FP64 device SCF on the final grids',
-           'fp64_sequential_wall_s': t64,
-           'mixed_sequential_wall_s': tseq,
-           'mixed_batched_wall_s': tb,
-           'fp64_over_mixed_batched': t64 / tb,
-           'batched_over_sequential_speedup': tseq / tb,
-           'all_converged': all(r['converged'] for r in rb) and all(r['converged'] for r in r64),
-           'max_abs_error_vs_fp64_Ha': max(abs(e) for e in errs),
-           'all_within_1e-8': all(abs(e) < 1e-8 for e in errs),
-           'batched_equals_sequential': all(a['e_tot'] == c['e_tot']
-                                            for a, c in zip(rb, rseq)),
-           'cycles_mixed': [r['cycles'] for r in rb],
-           'cycles_fp64': [r['cycles'] for r in r64],
-           'batched_exchange_builds': rb[0]['batched_exchange_builds']}
-    b.close()
-    return out
+    for w0 in range(0, nmol, wave):
+        mols = [Molecule.build(water_cluster(n, box=max(5.0, 3.2 * n ** (1.0 / 3.0)),
+                                             seed=300 + i), 'synthetic-svp')
+                for i, n in list(enumerate(sizes))[w0:w0 + wave]]
+        b = BatchedRKS(mols, levels=levels, coarse=coarse)
+        b.kernel(precision='mixed', max_cycle=1)       # warm-up: grids, batches
+        for r in b.rks:
+            r.kernel(precision='fp64', max_cycle=1)
+        r64, t = timed(lambda: [r.kernel(precision='fp64') for r in b.rks])
+        t64 += t
+        refs = [r['e_tot'] for r in r64]
+        rseq, t = timed(lambda: [r.kernel(precision='mixed', reference_energy=e)
+                                 for r, e in zip(b.rks, refs)])
+        tseq += t
+        rb = b.kernel(precision='mixed', reference_energies=refs)
+        tb += rb[0]['batch_wall']
+        errs += [r['error_vs_reference'] for r in rb]
+        conv = conv and all(r['converged'] for r in rb + r64)
+        equal = equal and all(a['e_tot'] == c['e_tot'] for a, c in zip(rb, rseq))
+        cyc_m += [r['cycles'] for r in rb]
+        cyc_f += [r['cycles'] for r in r64]
+        nb += rb[0]['batched_exchange_builds']
+        nao_tot += int(sum(r.mol.nao for r in b.rks))
+        b.close()
+        del b, r64, rseq, rb
+        torch.cuda.empty_cache()
+    return {'molecules': nmol, 'waters_per_cluster': sizes, 'wave': wave,
+            'levels': levels, 'coarse': coarse, 'nao_total': nao_tot,
+            'reference': "each molecule's plain FP64 device SCF on the final grids",
+            'fp64_sequential_wall_s': t64,
+            'mixed_sequential_wall_s': tseq,
+            'mixed_batched_wall_s': tb,
+            'fp64_over_mixed_batched': t64 / tb,
+            'batched_over_sequential_speedup': tseq / tb,
+            'all_converged': conv,
+            'max_abs_error_vs_fp64_Ha': max(abs(e) for e in errs),
+            'all_within_1e-8': all(abs(e) < 1e-8 for e in errs),
+            'batched_equals_sequential': equal,
+            'cycles_mixed': cyc_m, 'cycles_fp64': cyc_f,
+            'batched_exchange_builds': nb}
 
 
 def serving_scf_timing(torch, n_req=12, rates=(2.0, 8.0), slots=4, seed=7):
