@@ -176,7 +176,7 @@ __global__ void f_combine_kernel(const float* __restrict__ C, int nao,
 // columns per chunk (several right-hand sides side by side); this launch
 // fills columns boff .. boff + nao - 1.
 template<int S, int KC, bool DOX, typename GT>
-__global__ void __launch_bounds__(KC / 8)
+__global__ void __launch_bounds__(KC / 8, 4)
 k_slice_kernel(const double* __restrict__ X, const GT* __restrict__ G,
                const double* __restrict__ w, int nao, int64_t ld,
                int64_t npts, int* __restrict__ ex, int* __restrict__ ew,
@@ -263,26 +263,24 @@ k_slice_kernel(const double* __restrict__ X, const GT* __restrict__ G,
     }
     const int64_t colbase = (int64_t)c * S * KC * nao + (int64_t)col * S * KC;
     const int64_t colbase_b = (int64_t)c * S * KC * nb + (int64_t)(boff + col) * S * KC;
-    float d1[8][S], d2[8][S];
+    // one operand's digits at a time: the X slices, then the w o G ones
+    // (half the live registers of both at once)
+    auto store = [&](const double* v, const int e, __nv_bfloat16* dst, const bool desc) {
+        float d[8][S];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-        if (DOX) digits<S>(xv[u], e1, d1[u]);
-        digits<S>(wv[u], e2, d2[u]);
-    }
+        for (int u = 0; u < 8; ++u) digits<S>(v[u], e, d[u]);
 #pragma unroll
-    for (int i = 0; i < S; ++i) {
-        __nv_bfloat162 pa[4], pb[4];
+        for (int i = 0; i < S; ++i) {
+            __nv_bfloat162 p[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (DOX) pa[u] = __floats2bfloat162_rn(d1[2 * u][i], d1[2 * u + 1][i]);
-            pb[u] = __floats2bfloat162_rn(d2[2 * u][i], d2[2 * u + 1][i]);
+            for (int u = 0; u < 4; ++u)
+                p[u] = __floats2bfloat162_rn(d[2 * u][i], d[2 * u + 1][i]);
+            *reinterpret_cast<uint4*>(dst + (int64_t)(desc ? S - 1 - i : i) * KC + k0) =
+                *reinterpret_cast<const uint4*>(p);
         }
-        if (DOX)
-            *reinterpret_cast<uint4*>(A + colbase + (int64_t)i * KC + k0) =
-                *reinterpret_cast<const uint4*>(pa);
-        *reinterpret_cast<uint4*>(B + colbase_b + (int64_t)(S - 1 - i) * KC + k0) =
-            *reinterpret_cast<const uint4*>(pb);
-    }
+    };
+    if (DOX) store(xv, e1, A + colbase, false);
+    store(wv, e2, B + colbase_b, true);
 }
 
 // K_r[mu, nu] (+)= sum_c 2^(ex+ew-2W+2+B(S-1)) [sum_l C[l][c] 2^(B (S-1-l))]
@@ -301,7 +299,24 @@ __global__ void k_combine_kernel(const float* __restrict__ C, int nao, int nb,
          i += (int64_t)gridDim.x * blockDim.x) {
         const int mu = (int)(i % nao), col = (int)(i / nao);   // C col-major
         double acc = 0.0;
-        for (int c = 0; c < nchunk; ++c) {
+        // four chunks' loads in flight at once; the sum stays in chunk order
+        constexpr int U = 4;
+        int c = 0;
+        for (; c + U <= nchunk; c += U) {
+            float v[U][S];
+            int sc[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+#pragma unroll
+                for (int l = 0; l < S; ++l)
+                    v[u][l] = __ldg(C + ((int64_t)l * nchunk + c + u) * nc + i);
+                sc[u] = ex[(int64_t)(c + u) * nao + mu] + ew[(int64_t)(c + u) * nb + col] -
+                        2 * kW + 2 + kB * (S - 1);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) acc += (double)combine_levels<S>(v[u]) * pow2(sc[u]);
+        }
+        for (; c < nchunk; ++c) {
             float v[S];
 #pragma unroll
             for (int l = 0; l < S; ++l) v[l] = C[((int64_t)l * nchunk + c) * nc + i];
