@@ -690,6 +690,14 @@ int ensure_fp64(wb_cosx* h) {
     return WB_OK;
 }
 
+// Hermite-density entries of one primitive pair of total angular momentum
+// l, padded to a multiple of 4: every pair's block starts 16-byte aligned
+// (FP32) and 32-byte aligned (FP64), so the kernel reads it with vector
+// loads (the padding entries are read and never used)
+inline int64_t hartree_nr_padded(int l) {
+    return ((int64_t)(l + 1) * (l + 2) * (l + 3) / 6 + 3) & ~(int64_t)3;
+}
+
 // per-pair L, per-primitive-pair Hermite-density offsets and FP32 p of
 // the Hartree potential (first wb_hartree call on the handle)
 int ensure_hartree(wb_cosx* h) {
@@ -705,7 +713,7 @@ int ensure_hartree(wb_cosx* h) {
         const int pp0 = hp.hdr[4 * k + 2], npp = hp.hdr[4 * k + 3] & 0xffff;
         for (int m = pp0; m < pp0 + npp; ++m) {
             off[m] = tot;
-            tot += (l + 1) * (l + 2) * (l + 3) / 6;
+            tot += hartree_nr_padded(l);
         }
     }
     for (int m = 0; m < hp.npp; ++m) p32[m] = (float)hp.p[m];
@@ -759,7 +767,7 @@ int64_t hartree_ndh(const wb::HostPairs& hp) {
     int64_t tot = 0;
     for (int k = 0; k < hp.npairs; ++k) {
         const int l = hp.vsh[hp.pshell[2 * k]].l + hp.vsh[hp.pshell[2 * k + 1]].l;
-        tot += (int64_t)(hp.hdr[4 * k + 3] & 0xffff) * (l + 1) * (l + 2) * (l + 3) / 6;
+        tot += (int64_t)(hp.hdr[4 * k + 3] & 0xffff) * hartree_nr_padded(l);
     }
     return std::max<int64_t>(tot, 1);
 }

@@ -1086,7 +1086,20 @@ def hartree_source():
     with y, z), written level by level as named values (no in-place
     array), so the compiler sees plain register code."""
     out = ['// Generated by csrc/gen_cosx.py (hartree_source); do not edit.',
-           '#pragma once', '', 'namespace wb {', 'namespace scf {', '']
+           '#pragma once', '', 'namespace wb {', 'namespace scf {', '',
+           '// four consecutive Hermite-density entries (a 16-byte aligned',
+           '// block: float4, or two double2)',
+           'template<typename Real> struct Hq4 { Real x, y, z, w; };',
+           '__device__ __forceinline__ Hq4<float> ld_hq4(const float* p) {',
+           '    const float4 v = __ldg(reinterpret_cast<const float4*>(p));',
+           '    return {v.x, v.y, v.z, v.w};',
+           '}',
+           '__device__ __forceinline__ Hq4<double> ld_hq4(const double* p) {',
+           '    const double2 a = __ldg(reinterpret_cast<const double2*>(p));',
+           '    const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);',
+           '    return {a.x, a.y, b.x, b.y};',
+           '}',
+           '']
     for L in range(7):
         out.append('template<typename Real>')
         out.append('__device__ __forceinline__ Real hermite_dot_%d(const Real* r0, '
@@ -1124,9 +1137,13 @@ def hartree_source():
                 for t in range(L + 1 - u - v):
                     terms.append((_hartree_ridx(L, t, u, v), nm(0, t, u, v)))
         terms.sort()
+        # dh is read four entries at a time (its block is padded to a
+        # multiple of 4); the sum keeps the entry order
+        for g in range((len(terms) + 3) // 4):
+            out.append('    const Hq4<Real> d%d = ld_hq4(dh + %d);' % (g, 4 * g))
         out.append('    Real s = Real(0);')
         for q, name in terms:
-            out.append('    s += dh[%d] * %s;' % (q, name))
+            out.append('    s += d%d.%s * %s;' % (q // 4, 'xyzw'[q % 4], name))
         out.append('    return s;')
         out.append('}')
         out.append('')
