@@ -986,7 +986,7 @@ def scf_c20_timing(torch, n_carbon=20):
     return out
 
 
-def scf_batched_timing(torch, nmol=64, seed=4, wave=16):
+def scf_batched_timing(torch, nmol=64, seed=4, wave=16, max_waters=32):
     """Config 4: nmol seeded water clusters of n in {4..32} waters
     (uniform), synthetic def2-SVP, XC level 1 / SGX level 0 / VV10 level 0
     (S0 on XC 0 / SGX 0), every molecule a full SCF.  The plain FP64 form of
@@ -1002,7 +1002,7 @@ def scf_batched_timing(torch, nmol=64, seed=4, wave=16):
     from pyscf_wb97mv_fast_gb300.scf import BatchedRKS
     from pyscf_wb97mv_fast_gb300.systems import water_cluster
     rng = np.random.default_rng(seed)
-    sizes = [int(x) for x in rng.integers(4, 33, size=nmol)]
+    sizes = [int(x) for x in rng.integers(4, max_waters + 1, size=nmol)]
     levels, coarse = dict(xc=1, sgx=0, nlc=0), dict(xc=0, sgx=0)
     t64 = tseq = tb = 0.0
     errs, conv, equal, cyc_m, cyc_f, nb, nao_tot = [], True, True, [], [], 0, 0
@@ -1024,12 +1024,16 @@ def scf_batched_timing(torch, nmol=64, seed=4, wave=16):
             r.kernel(precision='fp64', max_cycle=1)
         r64, t = timed(lambda: [r.kernel(precision='fp64') for r in b.rks])
         t64 += t
+        print('scf_batched: wave %d: FP64 SCFs %.1f s' % (w0 // wave, t), file=sys.stderr,
+              flush=True)
         refs = [r['e_tot'] for r in r64]
         rseq, t = timed(lambda: [r.kernel(precision='mixed', reference_energy=e)
                                  for r, e in zip(b.rks, refs)])
         tseq += t
         rb = b.kernel(precision='mixed', reference_energies=refs)
         tb += rb[0]['batch_wall']
+        print('scf_batched: wave %d: mixed one by one %.1f s, batched %.1f s'
+              % (w0 // wave, t, rb[0]['batch_wall']), file=sys.stderr, flush=True)
         errs += [r['error_vs_reference'] for r in rb]
         conv = conv and all(r['converged'] for r in rb + r64)
         equal = equal and all(a['e_tot'] == c['e_tot'] for a, c in zip(rb, rseq))
@@ -1041,6 +1045,7 @@ def scf_batched_timing(torch, nmol=64, seed=4, wave=16):
         del b, r64, rseq, rb
         torch.cuda.empty_cache()
     return {'molecules': nmol, 'waters_per_cluster': sizes, 'wave': wave,
+            'max_waters': max_waters,
             'levels': levels, 'coarse': coarse, 'nao_total': nao_tot,
             'reference': "each molecule's plain FP64 device SCF on the final grids",
             'fp64_sequential_wall_s': t64,
@@ -1205,8 +1210,11 @@ def main():
     ap.add_argument('--no-scf', action='store_true',
                     help='skip the device SCF leg (config 1, mixed vs FP64)')
     ap.add_argument('--scf-batched', type=int, default=0, metavar='N',
-                    help='add the batched-SCF leg over N water clusters (config 4; '
-                         'minutes for N = 64)')
+                    help='add the batched-SCF leg over N water clusters in waves '
+                         'of 16 (config 4; each molecule also runs its plain FP64 '
+                         'SCF: about 20 s a molecule)')
+    ap.add_argument('--scf-batched-max-waters', type=int, default=32,
+                    help='largest cluster of the batched-SCF leg')
     ap.add_argument('--serving-scf', action='store_true',
                     help='add the served-SCF leg (whole SCF solves as requests)')
     ap.add_argument('--scf-c20', action='store_true',
@@ -1389,7 +1397,8 @@ def main():
     torch.cuda.empty_cache()
     scf = None if (args.no_scf or world > 1) else scf_timing(torch)
     scf_c20 = scf_c20_timing(torch) if (args.scf_c20 and world == 1) else None
-    scf_batched = (scf_batched_timing(torch, args.scf_batched)
+    scf_batched = (scf_batched_timing(torch, args.scf_batched,
+                                      max_waters=args.scf_batched_max_waters)
                    if (args.scf_batched > 0 and world == 1) else None)
     serving_scf = serving_scf_timing(torch) if (args.serving_scf and world == 1) else None
     torch.cuda.empty_cache()
