@@ -262,27 +262,41 @@ class Scheduler:
                 self._cv.notify_all()
             fut._finish(value, error)
 
-    def close(self, wait=True):
-        """No more submissions; the queued jobs still run."""
+    def close(self, wait=True, timeout=None):
+        """No more submissions; the queued jobs still run.  With a timeout
+        (seconds), the jobs still queued when it runs out -- e.g. one whose
+        footprint no longer fits beside the resident sessions -- finish
+        with Rejected, and close returns once the running ones end."""
         with self._cv:
             self._closed = True
             self._cv.notify_all()
-        if wait:
+        if not wait:
+            return
+        t_end = None if timeout is None else time.perf_counter() + float(timeout)
+        for t in self._workers:
+            t.join(None if t_end is None else max(0.0, t_end - time.perf_counter()))
+        if any(t.is_alive() for t in self._workers):
+            with self._cv:
+                while self._queue:
+                    _, fut, _ = self._queue.popleft()
+                    fut._finish(error=Rejected('scheduler closed before the request '
+                                               'could be admitted'))
+                self._cv.notify_all()
             for t in self._workers:
                 t.join()
 
 
 def latency_summary(futures):
     """p50 / p99 / mean latency (s) and requests per second, over the
-    requests that returned a result, from the first submit to the last
-    completion; 'failed' counts the finished ones that raised (errors,
-    cancelled, expired)."""
+    requests that returned a result, from the first submit of one of them
+    to the last completion; 'failed' counts the finished ones that raised
+    (errors, cancelled, expired)."""
     ok = [f for f in futures if f.done() and f._error is None]
     failed = sum(1 for f in futures if f.done() and f._error is not None)
     lat = np.array([f.latency for f in ok])
     if not len(lat):
         return {'requests': 0, 'failed': failed}
-    t0 = min(f.t_submit for f in futures)
+    t0 = min(f.t_submit for f in ok)
     t1 = max(f.t_done for f in ok)
     q = np.array([f.queued for f in ok if f.queued is not None])
     return {'requests': int(len(lat)), 'failed': failed,

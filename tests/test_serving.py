@@ -268,3 +268,45 @@ def test_scheduler_invariants_on_random_mixes():
             assert [n for n in rec.order if n in mine] == mine
 
     check()
+
+
+def test_close_with_timeout_rejects_a_job_that_can_never_fit():
+    """A queued job that fit when it was submitted, but no longer does
+    beside sessions reserved later, cannot block close() for ever: with a
+    timeout it finishes with Rejected."""
+    gate = threading.Event()
+
+    def run(job, slot):
+        if job.name == 'b':
+            gate.wait(5.0)
+        return job.name
+
+    s = Scheduler(run, slots=2, budget=100)
+    s.reserve(40)                                   # session A
+    fb = s.submit(Job('b', 50, 'b'))                # runs: 90 of 100
+    time.sleep(0.05)
+    fa = s.submit(Job('a', 50, 'a'))                # fits at submit, waits for b
+    s.reserve(20)                                   # session C: 60 resident
+    gate.set()                                      # b ends; a needs 110 > 100
+    t0 = time.perf_counter()
+    s.close(timeout=0.3)
+    assert time.perf_counter() - t0 < 3.0
+    assert fb.result(timeout=1.0) == 'b'
+    with pytest.raises(Rejected):
+        fa.result(timeout=1.0)
+
+
+def test_latency_span_starts_at_the_first_successful_request():
+    class F:
+        def __init__(self, t_submit, t_done, error=None):
+            self.t_submit, self.t_done, self._error = t_submit, t_done, error
+            self.t_start = t_submit
+            self.latency = t_done - t_submit
+            self.queued = 0.0
+
+        def done(self):
+            return True
+    futs = [F(0.0, 0.5, error=RuntimeError('cancelled')), F(10.0, 11.0), F(10.5, 12.0)]
+    out = latency_summary(futs)
+    assert out['requests'] == 2 and out['failed'] == 1
+    assert out['span_s'] == pytest.approx(2.0)
