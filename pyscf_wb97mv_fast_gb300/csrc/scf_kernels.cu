@@ -501,88 +501,6 @@ __device__ __forceinline__ typename HartreeTraits<F64>::Real hartree_pp(const Ha
     else return hermite_dot_6<Real>(r0, px, py, pz, dh);
 }
 
-// The same for the lane's two points (two 32-point sub-blocks of a
-// warp's 64-point block): the pair's data are read once; each point's sum
-// takes the pair only where its own sub-block kept it (use[q], uniform
-// over the warp), so every point's value is the one-point kernel's.
-template<bool F64, int L>
-__device__ __forceinline__ void hartree_pp2(const HartreeArgs& A, const int m,
-                                            const double* gx, const double* gy,
-                                            const double* gz, const float3* gh,
-                                            const float3* gl, const void* stab,
-                                            const bool* use,
-                                            typename HartreeTraits<F64>::Real* acc) {
-    typedef typename HartreeTraits<F64>::Real Real;
-    double Pd[3] = {0.0, 0.0, 0.0};
-    float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
-    Real p;
-    if constexpr (F64) {
-        Pd[0] = A.P[3 * m]; Pd[1] = A.P[3 * m + 1]; Pd[2] = A.P[3 * m + 2];
-        p = A.p[m];
-    } else {
-        hi = A.geo[2 * m];
-        lo = A.geo[2 * m + 1];
-        p = A.p32[m];
-    }
-    const int64_t off = A.dh_off[m];
-    const Real* dh;
-    if constexpr (F64) dh = A.dh64 + off; else dh = A.dh32 + off;
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        if (!use[q]) continue;
-        Real px, py, pz;
-        if constexpr (F64) {
-            px = Pd[0] - gx[q]; py = Pd[1] - gy[q]; pz = Pd[2] - gz[q];
-        } else {
-            px = (hi.x - gh[q].x) + (lo.x - gl[q].x);
-            py = (hi.y - gh[q].y) + (lo.y - gl[q].y);
-            pz = (hi.z - gh[q].z) + (lo.z - gl[q].z);
-        }
-        const Real T = p * (px * px + py * py + pz * pz);
-        Real F[L + 1], r0[L + 1];
-        if constexpr (F64)
-            boys64<L>(T, static_cast<const double*>(stab), F);
-        else
-            boys_fp32<L>(T, F, static_cast<const float4*>(stab));
-        Real m2p = Real(1);
-#pragma unroll
-        for (int n = 0; n <= L; ++n) {
-            r0[n] = m2p * F[n];
-            m2p *= Real(-2) * p;
-        }
-        Real v;
-        if constexpr (L == 0) v = hermite_dot_0<Real>(r0, px, py, pz, dh);
-        else if constexpr (L == 1) v = hermite_dot_1<Real>(r0, px, py, pz, dh);
-        else if constexpr (L == 2) v = hermite_dot_2<Real>(r0, px, py, pz, dh);
-        else if constexpr (L == 3) v = hermite_dot_3<Real>(r0, px, py, pz, dh);
-        else if constexpr (L == 4) v = hermite_dot_4<Real>(r0, px, py, pz, dh);
-        else if constexpr (L == 5) v = hermite_dot_5<Real>(r0, px, py, pz, dh);
-        else v = hermite_dot_6<Real>(r0, px, py, pz, dh);
-        acc[q] += v;
-    }
-}
-
-template<bool F64>
-__device__ __forceinline__ void hartree_pair2(
-    const HartreeArgs& A, const int L, const int pp0, const int npp, const double* gx,
-    const double* gy, const double* gz, const float3* gh, const float3* gl,
-    const void* stab, const bool* use, typename HartreeTraits<F64>::Real* acc) {
-    typename HartreeTraits<F64>::Real s[2] = {0, 0};
-    for (int m = pp0; m < pp0 + npp; ++m) {
-        switch (L) {
-        case 0: hartree_pp2<F64, 0>(A, m, gx, gy, gz, gh, gl, stab, use, s); break;
-        case 1: hartree_pp2<F64, 1>(A, m, gx, gy, gz, gh, gl, stab, use, s); break;
-        case 2: hartree_pp2<F64, 2>(A, m, gx, gy, gz, gh, gl, stab, use, s); break;
-        case 3: hartree_pp2<F64, 3>(A, m, gx, gy, gz, gh, gl, stab, use, s); break;
-        case 4: hartree_pp2<F64, 4>(A, m, gx, gy, gz, gh, gl, stab, use, s); break;
-        case 5: hartree_pp2<F64, 5>(A, m, gx, gy, gz, gh, gl, stab, use, s); break;
-        default: hartree_pp2<F64, 6>(A, m, gx, gy, gz, gh, gl, stab, use, s); break;
-        }
-    }
-    acc[0] += s[0];
-    acc[1] += s[1];
-}
-
 template<bool F64>
 __device__ __forceinline__ typename HartreeTraits<F64>::Real hartree_pair(
     const HartreeArgs& A, const int L, const int pp0, const int npp, const double gx,
@@ -667,97 +585,6 @@ __global__ void __launch_bounds__(128) hartree_kernel(const HartreeArgs A) {
     if (lane == 0 && A.kept) atomicAdd(A.kept, kept);
 }
 
-// Two points per lane: one warp per 64-point block (two 32-point
-// sub-blocks), the pair data and loop overhead shared by the two points.
-// Each lane screens its pair against both sub-blocks; the warp walks the
-// pairs either sub-block kept, and each point adds only the pairs its own
-// sub-block kept, in the same order as the one-point kernel: the values
-// are bitwise that kernel's.
-template<bool F64>
-__global__ void __launch_bounds__(128) hartree_kernel2(const HartreeArgs A) {
-    typedef typename HartreeTraits<F64>::Real Real;
-    extern __shared__ float4 smem[];
-    {
-        const int n = HartreeTraits<F64>::kTabBytes / 16;
-        const float4* src = F64 ? reinterpret_cast<const float4*>(A.boys64) : A.boys32;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) smem[i] = src[i];
-    }
-    __syncthreads();
-    const void* stab = smem;
-    const int lane = threadIdx.x & 31;
-    const int nwork = (A.nblk + 1) / 2;
-    unsigned long long kept = 0;
-    for (;;) {
-        int blk = 0;
-        if (lane == 0) blk = atomicAdd(A.work, 1);
-        blk = __shfl_sync(0xffffffffu, blk, 0);
-        if (blk >= nwork) break;
-        bool ok[2], sub[2];
-        int64_t g0[2];
-        double gx[2], gy[2], gz[2];
-        float3 gh[2], gl[2];
-        float4 cr[2];
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const int sb = 2 * blk + q;
-            sub[q] = sb < A.nblk;
-            g0[q] = (int64_t)sb * 32 + lane;
-            ok[q] = g0[q] < A.npts;
-            const int64_t g = ok[q] ? g0[q] : A.npts - 1;
-            gx[q] = A.coords[3 * g]; gy[q] = A.coords[3 * g + 1]; gz[q] = A.coords[3 * g + 2];
-            gh[q] = make_float3(0.f, 0.f, 0.f);
-            gl[q] = gh[q];
-            if (!F64) {
-                gh[q] = make_float3((float)gx[q], (float)gy[q], (float)gz[q]);
-                gl[q] = make_float3((float)(gx[q] - (double)gh[q].x),
-                                    (float)(gy[q] - (double)gh[q].y),
-                                    (float)(gz[q] - (double)gh[q].z));
-            }
-            cr[q] = sub[q] ? A.blk_cr[sb] : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        double v[2] = {0.0, 0.0};
-        for (int c0 = 0; c0 < A.npairs; c0 += 32) {
-            const int k = c0 + lane;
-            const bool in = k < A.npairs;
-            bool keep[2] = {in && sub[0], in && sub[1]};
-            int4 h = make_int4(0, 0, 0, 0);
-            if (in) {
-                h = A.hdr[k];
-                if (A.tol > 0.0f) {
-                    const float2 tau = A.ptau[k];
-                    const float dabs = A.pair_dabs[k];
-#pragma unroll
-                    for (int q = 0; q < 2; ++q)
-                        if (keep[q])
-                            keep[q] = screen_pair(A.tol, A.bnd, A.bpref, cr[q], h, tau,
-                                                  dabs);
-                }
-            }
-            const unsigned m0 = __ballot_sync(0xffffffffu, keep[0]);
-            const unsigned m1 = __ballot_sync(0xffffffffu, keep[1]);
-            kept += __popc(m0) + __popc(m1);
-            Real chunk[2] = {0, 0};
-            unsigned mask = m0 | m1;
-            while (mask) {
-                const int src = __ffs(mask) - 1;
-                mask &= mask - 1;
-                const int kk = c0 + src;
-                const int pp0 = __shfl_sync(0xffffffffu, h.z, src);
-                const int npp = __shfl_sync(0xffffffffu, h.w, src) & 0xffff;
-                const int L = A.pair_L[kk];
-                const bool use[2] = {((m0 >> src) & 1u) != 0, ((m1 >> src) & 1u) != 0};
-                hartree_pair2<F64>(A, L, pp0, npp, gx, gy, gz, gh, gl, stab, use, chunk);
-            }
-            v[0] += (double)chunk[0];
-            v[1] += (double)chunk[1];
-        }
-#pragma unroll
-        for (int q = 0; q < 2; ++q)
-            if (ok[q]) A.v[g0[q]] = v[q];
-    }
-    if (lane == 0 && A.kept) atomicAdd(A.kept, kept);
-}
-
 cudaError_t launch_block_geom(const double* xyz, int64_t npts, int nblk, float4* cr,
                               cudaStream_t s) {
     if (nblk <= 0) return cudaSuccess;
@@ -766,25 +593,23 @@ cudaError_t launch_block_geom(const double* xyz, int64_t npts, int nblk, float4*
     return cudaGetLastError();
 }
 
-// -DWB_HARTREE_NP=1: the one-point-per-lane kernel (bitwise the same v)
-#ifndef WB_HARTREE_NP
-#define WB_HARTREE_NP 2
-#endif
-
+// One point per lane.  A two-point form (the pair's data read once for
+// both points, each point keeping its own sub-block's screen: bitwise the
+// same values) measured slower in the device SCF (J 0.250 against
+// 0.234 s on 8 waters): its extra registers cost more occupancy than the
+// shared loads saved.
 cudaError_t launch_hartree(const HartreeArgs& a, bool fp64, cudaStream_t s) {
     if (a.nblk <= 0) return cudaSuccess;
-    const int items = WB_HARTREE_NP == 2 ? (a.nblk + 1) / 2 : a.nblk;
-    const int grid = std::max(1, std::min(items / 4 + 1, sm_count() * 8));
+    const int grid = std::max(1, std::min(a.nblk / 4 + 1, sm_count() * 8));
     if (fp64) {
         const size_t smem = HartreeTraits<true>::kTabBytes;
-        auto* k = WB_HARTREE_NP == 2 ? hartree_kernel2<true> : hartree_kernel<true>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(hartree_kernel<true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
-        k<<<grid, 128, smem, s>>>(a);
+        hartree_kernel<true><<<grid, 128, smem, s>>>(a);
     } else {
-        auto* k = WB_HARTREE_NP == 2 ? hartree_kernel2<false> : hartree_kernel<false>;
-        k<<<grid, 128, HartreeTraits<false>::kTabBytes, s>>>(a);
+        hartree_kernel<false><<<grid, 128, HartreeTraits<false>::kTabBytes, s>>>(a);
     }
     return cudaGetLastError();
 }
