@@ -885,8 +885,7 @@ def scf_timing(torch):
         golden = json.load(fh)
     ref = golden.get('water8_svp_xc2_sgx1_nlc1', {}).get('e_tot')
     mol = Molecule.build(water_cluster(8, box=7.0, seed=8), 'synthetic-svp')
-    rks = DeviceRKS(mol, levels=dict(xc=2, sgx=1, nlc=1),
-                    purify=os.environ.get('WB_SCF_PURIFY', '1') != '0')
+    rks = DeviceRKS(mol, levels=dict(xc=2, sgx=1, nlc=1))
     # warm-up: grids, AO values and first launches (not timed)
     rks.kernel(precision='mixed', max_cycle=2)
     rks.kernel(precision='fp64', max_cycle=2)

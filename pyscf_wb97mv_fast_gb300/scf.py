@@ -191,54 +191,6 @@ DEFAULT_COARSE = dict(xc=1, sgx=0)
 REFERENCE_STAGE_LEVELS = dict(xc=(1, 3, 3), sgx=(1, 1, 2), nlc=(None, 1, 3))
 
 
-# the largest orthonormal basis whose density comes from purification
-# (above it the eigensolver is cheaper than the purification's GEMMs)
-PURIFY_MAX_NAO = 384
-
-
-def _purify(Fo, nocc, tol=1e-12, max_iter=96):
-    """The projector onto the nocc lowest eigenvectors of the symmetric Fo
-    by canonical purification (A. H. R. Palser and D. E. Manolopoulos,
-    Phys. Rev. B 58, 12704 (1998)): from the trace-correct linear map of
-    Fo within its Gershgorin bounds, P <- ((1-2c)P + (1+c)P^2 - P^3)/(1-c)
-    for c <= 1/2, else ((1+c)P^2 - P^3)/c, with c = tr(P^2-P^3)/tr(P-P^2),
-    until max|P^2 - P| < tol, then one McWeeny step.  Returns None if it
-    does not converge (no gap at the Fermi level, or too many steps)."""
-    torch = _torch()
-    n = Fo.shape[0]
-    if not 0 < nocc < n:
-        return None
-    eye = torch.eye(n, dtype=Fo.dtype, device=Fo.device)
-    d = Fo.diagonal()
-    r = Fo.abs().sum(dim=1) - d.abs()
-    emin, emax = float((d - r).min()), float((d + r).max())
-    mu = float(d.sum()) / n
-    if not emin < mu < emax:
-        return None
-    lam = min(nocc / (emax - mu), (n - nocc) / (mu - emin))
-    P = (lam / n) * (mu * eye - Fo) + (nocc / n) * eye
-    for it in range(max_iter):
-        P2 = P @ P
-        if it % 2 == 1:
-            err = float((P2 - P).abs().max())
-            if not math.isfinite(err):
-                return None
-            if err < tol:
-                P3 = P2 @ P
-                P = 3.0 * P2 - 2.0 * P3                 # McWeeny polish
-                return 0.5 * (P + P.T)
-        P3 = P2 @ P
-        t1 = torch.trace(P - P2)
-        t2 = torch.trace(P2 - P3)
-        c = torch.where(t1.abs() > 0, t2 / t1, torch.zeros_like(t1)).clamp(1e-12, 1 - 1e-12)
-        # each branch maps [0, 1] monotonically onto itself (fixed points
-        # 0 and 1) and keeps the trace
-        low = ((1.0 - 2.0 * c) * P + (1.0 + c) * P2 - P3) / (1.0 - c)
-        high = ((1.0 + c) * P2 - P3) / c
-        P = torch.where(c <= 0.5, low, high)
-    return None
-
-
 def _gemm_mode(gemm):
     if gemm is True:
         return 'fp64'
@@ -263,7 +215,7 @@ class DeviceRKS:
 
     def __init__(self, mol, functional=None, levels=None, coarse=None,
                  k_tile_tol=1e-11, j_tol=1e-14, device=None, verbose=False,
-                 stage_levels=None, purify=True):
+                 stage_levels=None):
         torch = _torch()
         self.mol = as_molecule(mol)
         self.functional = functional or RshLdaVv10()
@@ -281,7 +233,6 @@ class DeviceRKS:
         self.k_tile_tol = float(k_tile_tol)
         self.j_tol = float(j_tol)
         self.verbose = verbose
-        self.purify = bool(purify)
         t0 = time.perf_counter()
         self.eng = CosxEngine(self.mol, device=device)
         self.device = self.eng.device
@@ -443,18 +394,8 @@ class DeviceRKS:
         return E, F, dict(e1=e1, ej=ej, ek=ek, exc=exc, enl=enl), new_base
 
     def _diag(self, F):
-        """(D, orbital energies or None) of the Fock matrix F, FP64 on the
-        device: D = 2 Xo P Xo^T with P the projector onto the nocc lowest
-        eigenvectors of Fo = Xo^T F Xo.  Up to PURIFY_MAX_NAO orthonormal
-        functions P comes from canonical purification (_purify: FP64 GEMMs
-        only; the eigensolver's many small kernels cost more there), above
-        that, or if purification does not converge, from torch.linalg.eigh."""
         torch = _torch()
         Fo = self.Xo.T @ F @ self.Xo
-        if self.purify and Fo.shape[0] <= PURIFY_MAX_NAO:
-            P = _purify(Fo, self.nocc)
-            if P is not None:
-                return 2.0 * (self.Xo @ P @ self.Xo.T), None
         e, Co = torch.linalg.eigh(Fo)
         C = self.Xo @ Co
         Cocc = C[:, :self.nocc]

@@ -93,26 +93,3 @@ def test_reference_energy_and_bad_precision():
     with pytest.raises(ValueError):
         ScfRun(rks, 'bf16')
     assert ScfRun(rks, 'mixed', max_cycle=0).done
-
-
-def test_purification_gives_the_eigensolver_projector():
-    """_purify (canonical purification, FP64 GEMMs): the projector onto the
-    nocc lowest eigenvectors to 1e-13, with its trace; None (the caller then
-    diagonalises) when the Fermi level is degenerate."""
-    from pyscf_wb97mv_fast_gb300.scf import _purify
-    gen = torch.Generator().manual_seed(3)
-    for n, nocc, gap in ((96, 20, 0.4), (150, 61, 0.02)):
-        Q, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, generator=gen))
-        ev = torch.cat([-20.0 * torch.rand(nocc, dtype=torch.float64, generator=gen) - gap / 2,
-                        8.0 * torch.rand(n - nocc, dtype=torch.float64, generator=gen) + gap / 2])
-        F = Q @ torch.diag(ev) @ Q.T
-        P = _purify(F, nocc)
-        _, C = torch.linalg.eigh(F)
-        ref = C[:, :nocc] @ C[:, :nocc].T
-        assert P is not None
-        assert float((P - ref).abs().max()) < 1e-13
-        assert abs(float(torch.trace(P)) - nocc) < 1e-10
-    ev = torch.cat([-torch.ones(4, dtype=torch.float64), torch.zeros(2, dtype=torch.float64),
-                    torch.ones(14, dtype=torch.float64)])
-    Q, _ = torch.linalg.qr(torch.randn(20, 20, dtype=torch.float64, generator=gen))
-    assert _purify(Q @ torch.diag(ev) @ Q.T, 5) is None
