@@ -42,7 +42,7 @@ constexpr int kBoysFloat4 = 145 * 5;
 // the same for the dual-omega kernels (two sets of integrals and
 // accumulators per lane): -DWB_COSX_MIN_BLOCKS2=0x<10 hex digits>LL
 #ifndef WB_COSX_MIN_BLOCKS2
-#define WB_COSX_MIN_BLOCKS2 0x4433321111LL
+#define WB_COSX_MIN_BLOCKS2 0x5433321111LL
 #endif
 constexpr int min_blocks(int cls, int nw = 1) {
     long long v = nw == 2 ? WB_COSX_MIN_BLOCKS2 : WB_COSX_MIN_BLOCKS;
