@@ -872,7 +872,7 @@ def reference_gpu_timing(g, eng, F, Gt, t_g, torch, vv10_points=209707):
 
 
 def scf_timing(torch):
-    """Config 1 (8 seeded waters, synthetic def2-SVP, XC level 2, SGX
+    """Eight seeded waters (synthetic def2-SVP, XC level 2, SGX
     level 1, VV10 level 1): the device SCF in its mixed-precision staged
     form and its plain FP64 form, each from the core guess to convergence;
     energies against the oracle's host SCF (tests/golden/scf_energies.json,
@@ -938,12 +938,12 @@ def _scf_record(r, ref):
 
 
 def scf_c20_timing(torch, n_carbon=20):
-    """Config 3: the staged mixed-precision SCF of all-trans C20H42 in the
+    """The staged mixed-precision SCF of all-trans C20H42 in the
     synthetic def2-TZVP structure (f shells) on the reference's per-stage
     grid table (XC 1/3/3, SGX 1/1/2, NLC off/1/3), against the plain FP64
     form on the final grids.  The host oracle SCF needs about 45 min for
     192 AOs, so the FP64 form's converged energy -- the form pinned to the
-    oracle's SCF to 2e-10 Ha on config 1 and on an f-shell molecule in the
+    oracle's SCF to 2e-10 Ha on eight waters in SVP and on an f-shell molecule in the
     GPU tests -- is the FP64 reference energy here.  Each form runs once
     from the core guess (per-part profile on); grids and AO values are
     built by an untimed warm-up."""
@@ -973,7 +973,7 @@ def scf_c20_timing(torch, n_carbon=20):
            'grid_setup_s': setup, 'functional': rks.functional.name,
            'reference_energy': ref,
            'reference': 'the plain FP64 device form on the final grids (pinned to the '
-                        'host oracle SCF on config 1 and on ethane/TZVP)'}
+                        'host oracle SCF on eight waters/SVP and on ethane/TZVP)'}
     out['mixed'] = _scf_record(rmx, ref)
     out['mixed']['profile_s'] = {k: round(v, 3) for k, v in rmx['profile'].items()}
     out['fp64'] = _scf_record(r64, ref)
@@ -987,7 +987,7 @@ def scf_c20_timing(torch, n_carbon=20):
 
 
 def scf_batched_timing(torch, nmol=64, seed=4, wave=16, max_waters=32):
-    """Config 4: nmol seeded water clusters of n in {4..32} waters
+    """nmol seeded water clusters of n in {4..32} waters
     (uniform), synthetic def2-SVP, XC level 1 / SGX level 0 / VV10 level 0
     (S0 on XC 0 / SGX 0), every molecule a full SCF.  The plain FP64 form of
     each molecule (its own SCF, one after another) gives its FP64 reference
@@ -1208,17 +1208,17 @@ def main():
     ap.add_argument('--no-alkane', action='store_true',
                     help='skip the C20H42 / def2-TZVP (f shells) leg')
     ap.add_argument('--no-scf', action='store_true',
-                    help='skip the device SCF leg (config 1, mixed vs FP64)')
+                    help='skip the device SCF leg (8 waters / SVP, mixed vs FP64)')
     ap.add_argument('--scf-batched', type=int, default=0, metavar='N',
                     help='add the batched-SCF leg over N water clusters in waves '
-                         'of 16 (config 4; each molecule also runs its plain FP64 '
+                         'of 16 (each molecule also runs its plain FP64 '
                          'SCF: about 20 s a molecule)')
     ap.add_argument('--scf-batched-max-waters', type=int, default=32,
                     help='largest cluster of the batched-SCF leg')
     ap.add_argument('--serving-scf', action='store_true',
                     help='add the served-SCF leg (whole SCF solves as requests)')
     ap.add_argument('--scf-c20', action='store_true',
-                    help='add the C20H42 / def2-TZVP staged SCF leg (config 3; '
+                    help='add the C20H42 / def2-TZVP staged SCF leg ('
                          'minutes: its plain FP64 run is the reference energy)')
     ap.add_argument('--no-reference-gpu', action='store_true',
                     help="skip the reference's own kernels on this GPU")

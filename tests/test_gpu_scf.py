@@ -4,12 +4,12 @@ functional, grids and algorithm, FP64 and unscreened on the host.
 * the plain FP64 device form reaches the oracle's energy to 1e-9 Ha (its
   screens, k_tile_tol 1e-11 and the Hartree screen, are the difference);
 * the mixed-precision staged form (FP32 stages on coarse then final
-  grids, FP64 tail) reaches it to 1e-8 Ha, the north star's gate;
+  grids, FP64 tail) reaches it to 1e-8 Ha, the energy tolerance of the staged path;
 * the per-cycle pieces match the oracle's Fock build on a fixed density.
 
 The oracle energies come from tests/golden/scf_energies.json (written by
 tests/golden/make_scf_golden.py, which runs oracle/scf.py): the water dimer
-and config 1's eight waters in SVP, and ethane in TZVP (f shells).
+and eight seeded waters in SVP, and ethane in TZVP (f shells).
 """
 import json
 import os
@@ -89,8 +89,8 @@ def test_incremental_builds_reach_the_same_energy():
         assert r['converged'] and abs(r['e_tot'] - e_ref) < 2e-9, r['e_tot'] - e_ref
 
 
-def test_mixed_scf_water8_config1_reaches_the_oracle_energy():
-    """Config 1's molecule and grids: 8 seeded waters, synthetic def2-SVP
+def test_mixed_scf_water8_svp_reaches_the_oracle_energy():
+    """The molecule and grids: 8 seeded waters, synthetic def2-SVP
     (192 AOs), XC level 2, SGX level 1, VV10 level 1."""
     from pyscf_wb97mv_fast_gb300.basis import Molecule
     from pyscf_wb97mv_fast_gb300.scf import DeviceRKS
