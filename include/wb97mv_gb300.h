@@ -436,11 +436,10 @@ int wb_vv10_kernel_sum_batch(int nmol, const int64_t* offsets, const float* xyz,
  * kept-pair counter) is a file-scope device array of fixed size, held by
  * every GPU that loads the library until the process exits; n above
  * WB_VV10_NOALLOC_MAX_POINTS is rejected with WB_ERR_INVALID_ARGUMENT.
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress, with that device current) and keeps it; make that
- * first call before any stream capture.  The kept address is valid for the
- * life of the device's primary context: after cudaDeviceReset (or any
- * teardown of that context) do not call it again in the same process.
+ * Each call looks up the array's device address in the current context
+ * (cudaGetSymbolAddress, no allocation), so a context torn down and made
+ * again is served; make the first call on a device before any stream
+ * capture (it may load the library's module into the context).
  * All calls on a device share the array and
  * each call leaves its own contents there: calls whose work overlaps on
  * the GPU (different streams, or different host threads) race.  No

@@ -549,7 +549,6 @@ cudaError_t launch_vv10(const float* xyz, const float* q, const float* w0,
 // entry point serves at most WB_VV10_NOALLOC_MAX_POINTS points, and every
 // GPU that loads the library holds it until the process exits.
 // ---------------------------------------------------------------------------
-#include <mutex>
 #include <string>
 
 #include "wb97mv_gb300.h"
@@ -568,10 +567,6 @@ constexpr size_t kNoallocBytes =
 
 // [0, 256): kept-pair counter; [256, ...): one VvTileStats per tile
 static __device__ __align__(256) unsigned char g_vv10_scratch[kNoallocBytes];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kMaxDevices] = {};
 
 int noalloc_fail(int code, const char* msg, cudaError_t e = cudaSuccess) {
     std::string m(msg);
@@ -604,32 +599,14 @@ extern "C" int wb_vv10_kernel_sum_noalloc(const float* xyz, const float* q,
         if (pairs_kept) *pairs_kept = 0;
         return WB_OK;
     }
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess)
-        return noalloc_fail(WB_ERR_CUDA, "wb_vv10_kernel_sum_noalloc: cudaGetDevice", e);
-    if (dev < 0 || dev >= kMaxDevices)
-        return noalloc_fail(WB_ERR_INVALID_ARGUMENT,
-                            "wb_vv10_kernel_sum_noalloc: device index too large");
+    // the array's device address in the current context, looked up on every
+    // call (a host-side table query, no allocation), so that a context torn
+    // down and made again never leaves a stale address behind
     void* scratch = nullptr;
-    {
-        // first call on this device: the device address of the array (the
-        // host-side name is only a stand-in), taken with the device current.
-        // It stays valid while the primary context lives; a cudaDeviceReset
-        // would leave it stale (the header tells callers not to call again
-        // after one)
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_vv10_scratch);
-            if (e != cudaSuccess || !p)
-                return noalloc_fail(WB_ERR_CUDA,
-                                    "wb_vv10_kernel_sum_noalloc: "
-                                    "cudaGetSymbolAddress", e);
-            g_noalloc_ptr[dev] = p;
-        }
-        scratch = g_noalloc_ptr[dev];
-    }
+    cudaError_t e = cudaGetSymbolAddress(&scratch, g_vv10_scratch);
+    if (e != cudaSuccess || !scratch)
+        return noalloc_fail(WB_ERR_CUDA,
+                            "wb_vv10_kernel_sum_noalloc: cudaGetSymbolAddress", e);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     // launch_vv10 zeroes the counter and overwrites every tile record it
     // reads; nothing else in the array must start at zero
