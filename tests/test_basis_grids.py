@@ -20,6 +20,52 @@ def test_cart2sph_orthonormal_on_the_sphere():
         assert np.allclose(G, np.eye(2 * l + 1), atol=1e-12)
 
 
+def _real_harmonic_table(l, x, y, z):
+    """The real spherical harmonics r^l Y_lm in Cartesian form, unit-
+    normalised on the sphere, written out from the standard table (not from
+    the solid-harmonic expansion that ``cart2sph`` evaluates), in the
+    column order of PySCF's ``gto.mole.cart2sph(l)`` that the reference
+    applies (``gpu/ao_eval.py:73``, ``gpu/shellpairs.py:219``): (x, y, z)
+    for l = 1, m = -l .. l for l >= 2."""
+    pi = math.pi
+    if l == 0:
+        return [np.full_like(x, 0.5 / math.sqrt(pi))]
+    if l == 1:
+        c = math.sqrt(3.0 / (4.0 * pi))
+        return [c * x, c * y, c * z]
+    if l == 2:
+        a = 0.5 * math.sqrt(15.0 / pi)
+        return [a * x * y, a * y * z,
+                0.25 * math.sqrt(5.0 / pi) * (2 * z * z - x * x - y * y),
+                a * x * z, 0.25 * math.sqrt(15.0 / pi) * (x * x - y * y)]
+    if l == 3:
+        c3 = 0.25 * math.sqrt(35.0 / (2.0 * pi))
+        c1 = 0.25 * math.sqrt(21.0 / (2.0 * pi))
+        return [c3 * y * (3 * x * x - y * y),
+                0.5 * math.sqrt(105.0 / pi) * x * y * z,
+                c1 * y * (4 * z * z - x * x - y * y),
+                0.25 * math.sqrt(7.0 / pi) * z * (2 * z * z - 3 * x * x - 3 * y * y),
+                c1 * x * (4 * z * z - x * x - y * y),
+                0.25 * math.sqrt(105.0 / pi) * z * (x * x - y * y),
+                c3 * x * (x * x - 3 * y * y)]
+    raise ValueError(l)
+
+
+@pytest.mark.parametrize('l', [0, 1, 2, 3])
+def test_cart2sph_matches_the_real_harmonic_table(l):
+    """Order, signs and normalisation of every spherical component against
+    an independent statement of the convention: a column permutation, a sign
+    flip or a wrong m normalisation would pass the orthonormality test above
+    but fails here."""
+    rng = np.random.default_rng(l)
+    x, y, z = rng.uniform(-1.5, 1.5, size=(3, 64))
+    P = np.stack([x ** i * y ** j * z ** k for (i, j, k) in cart_components(l)],
+                 axis=1)
+    got = P @ cart2sph(l)
+    want = np.stack(_real_harmonic_table(l, x, y, z), axis=1)
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-13)
+
+
 @pytest.mark.parametrize('basis', ['synthetic-svp', 'synthetic-tzvp'])
 def test_contracted_functions_are_normalised(basis):
     atoms = water_cluster(1, 1.0, seed=0) + [('F', (3.0, 0, 0)), ('S', (6.0, 0, 0)),
