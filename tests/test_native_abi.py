@@ -32,6 +32,59 @@ def test_library_exports_every_header_function():
     assert set(names) <= set(_native.EXPORTED) | {'wb_cosx'}
 
 
+def header_prototypes():
+    """{name: (return type, [parameter declarations])} of every function
+    the headers declare (comments stripped)."""
+    out = {}
+    for fn in os.listdir(os.path.join(ROOT, 'include')):
+        if not fn.endswith('.h'):
+            continue
+        with open(os.path.join(ROOT, 'include', fn)) as fh:
+            text = fh.read()
+        text = re.sub(r'/\*.*?\*/', ' ', text, flags=re.S)
+        text = re.sub(r'//[^\n]*', ' ', text)
+        for ret, name, params in re.findall(
+                r'([A-Za-z_][\w \t\*]*?)\b(wb_\w+)\s*\(([^()]*)\)\s*;', text):
+            plist = [p.strip() for p in params.split(',')]
+            if plist == ['void'] or plist == ['']:
+                plist = []
+            out[name] = (' '.join(ret.split()), plist)
+    return out
+
+
+def _param_kind(decl):
+    if '*' in decl or '[' in decl:
+        return 'ptr'
+    words = [w for w in decl.replace('const', ' ').split()]
+    return words[0] if len(words) >= 2 else words[-1]
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every argtypes / restype that the Python side declares has the
+    header's arity and, parameter by parameter, its kind (a pointer or the
+    same scalar type): a mismatch would hand a kernel a wrong pointer or
+    size without any error on the host."""
+    lib = _native.lib()
+    scalars = {'int': ctypes.c_int, 'int64_t': ctypes.c_int64,
+               'double': ctypes.c_double, 'size_t': ctypes.c_size_t}
+    rets = {'int': ctypes.c_int, 'int64_t': ctypes.c_int64,
+            'size_t': ctypes.c_size_t, 'const char*': ctypes.c_char_p}
+    protos = header_prototypes()
+    assert set(protos) == set(header_functions())
+    for name, (ret, params) in protos.items():
+        fn = getattr(lib, name)
+        assert fn.restype is rets[ret.replace(' *', '*')], (name, ret)
+        assert fn.argtypes is not None, name
+        assert len(fn.argtypes) == len(params), (name, params)
+        for decl, at in zip(params, fn.argtypes):
+            kind = _param_kind(decl)
+            if kind == 'ptr':
+                assert (at in (ctypes.c_void_p, ctypes.c_char_p)
+                        or issubclass(at, ctypes._Pointer)), (name, decl, at)
+            else:
+                assert at is scalars[kind], (name, decl, at)
+
+
 def test_status_strings_and_version():
     lib = _native.lib()
     assert lib.wb_version() >= 1
