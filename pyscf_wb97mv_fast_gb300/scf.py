@@ -725,9 +725,20 @@ class BatchedRKS:
         return outs
 
     def close(self):
+        """Frees the batched builds, the engines they own (one per molecule
+        and grid level, destroyed after their batch) and every molecule's
+        own engine."""
         for b in self._kb.values():
             b.close()
+            for e in b.engines:
+                e.close()
         self._kb = {}
         for r in self.rks:
             r.eng.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 

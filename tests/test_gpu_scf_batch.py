@@ -55,11 +55,10 @@ def test_batched_scf_reaches_the_oracle_energy_of_each_molecule():
     mols = [dimer('synthetic-svp'), Molecule.build(alkane(2), 'synthetic-tzvp')]
     refs = [gold['water_dimer_svp_xc1_sgx0_nlc0']['e_tot'],
             gold['ethane_tzvp_xc1_sgx0_nlc0']['e_tot']]
-    b = BatchedRKS(mols, levels=LEVELS, coarse=COARSE)
-    try:
+    with BatchedRKS(mols, levels=LEVELS, coarse=COARSE) as b:
         res = b.kernel(precision='mixed', reference_energies=refs)
-    finally:
-        b.close()
+        engines = [e for kb in b._kb.values() for e in kb.engines]
+    assert engines and all(e._h is None for e in engines)
     for r in res:
         assert r['converged']
         assert abs(r['error_vs_reference']) < 1e-8, r['error_vs_reference']
