@@ -285,6 +285,12 @@ class Scheduler:
             for t in self._workers:
                 t.join()
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
 
 def latency_summary(futures):
     """p50 / p99 / mean latency (s) and requests per second, over the
@@ -514,6 +520,12 @@ class ExchangeServer:
     def close(self):
         self._sched.close(wait=True)
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
     def summary(self):
         out = latency_summary(self.futures)
         out['slots'] = self._sched.slots
@@ -628,6 +640,12 @@ class ScfServer:
 
     def close(self):
         self._sched.close(wait=True)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
     def summary(self):
         out = latency_summary(self.futures)

@@ -296,6 +296,21 @@ def test_close_with_timeout_rejects_a_job_that_can_never_fit():
         fa.result(timeout=1.0)
 
 
+def test_scheduler_as_context_manager_runs_queued_jobs_then_stops():
+    """Leaving a with-block closes the scheduler: the jobs queued in it
+    still run to the end, its workers stop, and it takes no new request."""
+    def run(job, slot):
+        time.sleep(0.01)
+        return job.name
+
+    with Scheduler(run, slots=2, budget=100) as s:
+        futs = [s.submit(Job(str(i), 30, str(i))) for i in range(6)]
+    assert [f.result(timeout=0) for f in futs] == [str(i) for i in range(6)]
+    assert not any(t.is_alive() for t in s._workers)
+    with pytest.raises(Rejected):
+        s.submit(Job('late', 10, 'late'))
+
+
 def test_latency_span_starts_at_the_first_successful_request():
     class F:
         def __init__(self, t_submit, t_done, error=None):
