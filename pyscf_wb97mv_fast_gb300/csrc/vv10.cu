@@ -212,11 +212,29 @@ __device__ __forceinline__ void vv10_tile_fast(const VvOuter& o, const float4* s
     acc.pairs += (unsigned long long)m;
 }
 
-// One block per 256-point outer tile.  Thread 0 decides whether the block
-// needs inner tile jt (the decision sits in a two-slot parity buffer so
-// the next decision cannot overwrite one still being read); the block
-// stages the tile and every live thread runs its pairs.
-__global__ void __launch_bounds__(kVvTile)
+// Warp 0 of a block: the keep decisions of the 32 inner tiles
+// [u0, u0 + 32) against outer tile `self` (tiles at or past u_end are
+// dropped), one per lane, as one ballot word in keep_word.  A decision is
+// an FP64 bound with a square root and two divisions; evaluating 32 at
+// once keeps that latency off the block's per-tile path (one thread
+// evaluating each tile in turn while the block waited cost 12 % of the
+// sum at tile_tol 1e-12).
+__device__ __forceinline__ void vv_keep_word(const VvTileStats* __restrict__ st,
+                                             const int64_t self, const int64_t u0,
+                                             const int64_t u_end, const double tol,
+                                             unsigned* keep_word) {
+    const int64_t u = u0 + threadIdx.x;
+    const bool kp = u < u_end && vv10_keep(st[self], st[u], tol);
+    const unsigned bits = __ballot_sync(0xffffffffu, kp);
+    if (threadIdx.x == 0) *keep_word = bits;
+}
+
+// One block per 256-point outer tile.  Warp 0 decides, 32 inner tiles at
+// a time, which of them the block needs (the decision words sit in a
+// two-slot parity buffer, so the next word cannot overwrite one still
+// being read); the block stages each kept tile and every live thread runs
+// its pairs.
+__global__ void __launch_bounds__(kVvTile, 5)
 vv10_sum_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
                 const float* __restrict__ w0, const float* __restrict__ kap,
                 int64_t n, double tol, const VvTileStats* __restrict__ st,
@@ -224,18 +242,19 @@ vv10_sum_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
                 double* __restrict__ W, unsigned long long* __restrict__ kept) {
     __shared__ float4 sp[kVvTile];      // x, y, z, q
     __shared__ float2 sk[kVvTile];      // w0, kappa
-    __shared__ int s_keep[2];
+    __shared__ unsigned s_keep[2];
     const int64_t i = (int64_t)blockIdx.x * kVvTile + threadIdx.x;
     const bool live = i < n;
     const VvOuter o = vv_load_outer(xyz, w0, kap, live ? i : n - 1);
     const int64_t ntiles = (n + kVvTile - 1) / kVvTile;
     VvSums acc;
     for (int64_t jt = 0; jt < ntiles; ++jt) {
-        if (threadIdx.x == 0)
-            s_keep[jt & 1] = vv10_keep(st[blockIdx.x], st[jt], tol);
+        const int sl = (int)((jt >> 5) & 1);
+        if ((jt & 31) == 0 && threadIdx.x < 32)
+            vv_keep_word(st, blockIdx.x, jt, ntiles, tol, &s_keep[sl]);
         const int64_t j = jt * kVvTile + threadIdx.x;
         __syncthreads();
-        if (!s_keep[jt & 1]) continue;  // uniform across the block
+        if (!((s_keep[sl] >> (jt & 31)) & 1u)) continue;  // uniform across the block
         if (j < n) vv_stage(sp, sk, threadIdx.x, xyz, q, w0, kap, j);
         __syncthreads();
         if (live)
@@ -464,7 +483,7 @@ vv10_sum_seg_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
                     double* __restrict__ W, unsigned long long* __restrict__ kept) {
     __shared__ float4 sp[kVvTile];      // x, y, z, q
     __shared__ float2 sk[kVvTile];      // w0, kappa
-    __shared__ int s_keep[2];
+    __shared__ unsigned s_keep[2];
     const int64_t t = blockIdx.x;
     const int mol = sg.tmol[t];
     const int64_t i = sg.tstart[t] + threadIdx.x;
@@ -473,12 +492,14 @@ vv10_sum_seg_kernel(const float* __restrict__ xyz, const float* __restrict__ q,
     VvSums acc;
     const int jt0 = sg.mtile[mol], jt1 = sg.mtile[mol + 1];
     for (int jt = jt0; jt < jt1; ++jt) {
-        if (threadIdx.x == 0)
-            s_keep[jt & 1] = vv10_keep(st[t], st[jt], tol);
+        const int k = jt - jt0;          // the tile's index within its molecule
+        const int sl = (k >> 5) & 1;
+        if ((k & 31) == 0 && threadIdx.x < 32)
+            vv_keep_word(st, t, jt, jt1, tol, &s_keep[sl]);
         const int m = sg.tlen[jt];
         const int64_t j = sg.tstart[jt] + threadIdx.x;
         __syncthreads();
-        if (!s_keep[jt & 1]) continue;  // uniform across the block
+        if (!((s_keep[sl] >> (k & 31)) & 1u)) continue;  // uniform across the block
         if ((int)threadIdx.x < m) vv_stage(sp, sk, threadIdx.x, xyz, q, w0, kap, j);
         __syncthreads();
         if (live) vv10_tile_fast(o, sp, sk, m, acc);
